@@ -1,0 +1,204 @@
+"""Generate the golden fixtures in this folder by running the reference itself.
+
+Run from the repository root in a container where the reference checkout is
+available (read-only is fine):
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+
+Every fixture comes from the reference's own code path.  Its adaptive
+``zvode`` integrator is swapped for a fixed-step RK4 harness that drives the
+reference's own ``eom`` callables (the integrator the GPU path implements);
+tight-tolerance ``zvode`` runs are stored beside them for the integrator gap.
+The outputs are small ``.npz`` files committed next to this script; nothing
+at test time reads the reference.
+"""
+import os
+import sys
+import warnings
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+
+def rk4_harness(step):
+    """Drop-in for qspectra.simulate.utils.integrate with a fixed-step RK4."""
+    def integrate(f, y0, t, t0=None, method_name='zvode', f_params=None,
+                  save_func=None, **kwargs):
+        y0 = np.asarray(y0)
+        if y0.ndim > 1:
+            return np.array([integrate(f, yi, t, t0, method_name, f_params,
+                                       save_func) for yi in y0])
+        t = np.asarray(t, float)
+        if t0 is None:
+            t0 = t[0]
+        save = (lambda x: x) if save_func is None else save_func
+        y = np.array(y0, dtype=complex)
+        out = []
+        cur = t0
+        h = step
+        for ti in t:
+            n = int(round((ti - cur) / h))
+            for _ in range(n):
+                k1 = f(cur, y)
+                k2 = f(cur + h / 2, y + h / 2 * k1)
+                k3 = f(cur + h / 2, y + h / 2 * k2)
+                k4 = f(cur + h, y + h * k3)
+                y = y + h / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+                cur = cur + h
+            out.append(save(y))
+        return np.array(out)
+    return integrate
+
+
+def main(ref_root):
+    sys.path.insert(0, ref_root)
+    sys.path.insert(0, ROOT)
+    warnings.simplefilter('ignore')
+    import qspectra as qs
+    import qspectra.simulate.response as qresp
+    import qspectra.simulate.eom as qeom
+    import qspectra.simulate.utils as qutils
+    from qspectra.dynamics import heom as qheom
+    from qspectra_gb300 import workloads as wl
+
+    out = {}
+
+    # ---- Debye correlation functions (bath.py:17-31, 84-102) -------------
+    xs = np.concatenate([np.linspace(-900, 900, 37), [0.0, 1e-9, -3.5, 777.7]])
+    for tag, (TK, lam, gam) in {'77K': (77, 35, 106), '300K': (300, 40, 100),
+                                '10K': (10, 35, 106)}.items():
+        b = qs.DebyeBath(qs.CM_K * TK, lam, gam)
+        out['corr_x'] = xs
+        out['corr_complex_' + tag] = np.array([b.corr_func_complex(x) for x in xs])
+        out['corr_real_' + tag] = np.array([b.corr_func_real(x) for x in xs])
+
+    # ---- Redfield Liouvillians on a dimer, every option ------------------
+    dimer = np.array([[12881., 120], [120, 12719]])
+    dip2 = [[1, 0, 0], [2 * np.cos(.3), 2 * np.sin(.3), 0]]
+    bath77 = qs.DebyeBath(qs.CM_K * 77, 35, 106)
+    ham = qs.ElectronicHamiltonian(dimer, bath=bath77, dipoles=dip2)
+    for sec in (False, True):
+        for dic in (False, True):
+            for basis in ('site', 'eigen'):
+                m = qs.RedfieldModel(ham, hilbert_subspace='gef',
+                                     unit_convert=qs.CM_FS, secular=sec,
+                                     discard_imag_corr=dic,
+                                     evolve_basis=basis)
+                key = 'dimer_L_sec{}_dic{}_{}'.format(int(sec), int(dic), basis)
+                out[key] = m.evolution_super_operator
+    out['dimer_H'] = dimer
+    out['dimer_dipoles'] = np.array(dip2)
+
+    # ---- 7-site workload: Liouvillian blocks, trajectories, spectra -------
+    H7 = wl.fmo7_hamiltonian()
+    extra = wl.energy_spread_for_dt(H7, 1.0, qs.CM_FS)
+    ham7 = qs.ElectronicHamiltonian(
+        H7, bath=bath77, dipoles=[[1, 0, 0]] * 7,
+        disorder=wl.fwhm_for_sd(80.0), random_seed=1, energy_spread_extra=extra)
+    m7 = qs.RedfieldModel(ham7, hilbert_subspace='ge', unit_convert=qs.CM_FS,
+                          secular=False)
+    assert m7.time_step == 1.0, m7.time_step
+    idx_ee = m7.liouville_subspace_index('ee')
+    idx_eg = m7.liouville_subspace_index('eg')
+    Lfull = m7.evolution_super_operator
+    out['fmo7_H'] = H7
+    out['fmo7_extra'] = extra
+    out['fmo7_rw'] = m7.rw_freq
+    out['fmo7_L_ee'] = Lfull[np.ix_(idx_ee, idx_ee)]
+    out['fmo7_L_eg'] = Lfull[np.ix_(idx_eg, idx_eg)]
+    out['fmo7_E'], out['fmo7_U'] = m7.hamiltonian.eig('ge')
+
+    rk4 = rk4_harness(1.0)
+    qeom.integrate = rk4
+    qresp.integrate = rk4
+    psi = np.zeros(7)
+    psi[0] = 1.0
+    t, rhos = qs.simulate_dynamics(m7, psi, duration=1000.0)
+    out['fmo7_dyn_t'] = t
+    out['fmo7_dyn_pops'] = np.einsum('tii->ti', rhos).real
+    out['fmo7_dyn_rho_every10'] = rhos[::10]
+    t, sig = qs.linear_response(m7, 'gg->eg->gg', 2048.0)
+    out['fmo7_abs_t'] = t
+    out['fmo7_abs_signal'] = sig
+    f, X = qs.absorption_spectra(m7, 2048.0)
+    out['fmo7_abs_f'] = f
+    out['fmo7_abs_X'] = X
+
+    # small ensemble: disorder draws and the averaged spectrum
+    draws = np.array([np.diag(h.H_1exc) for h in ham7.sample_ensemble(8)])
+    out['fmo7_sample_diag'] = draws
+    f, X = qs.absorption_spectra(m7, 2048.0, ensemble_size=8)
+    out['fmo7_ens8_abs_X'] = X
+    t, rhos = qs.simulate_dynamics(m7, psi, duration=1000.0, ensemble_size=8)
+    out['fmo7_ens8_pops'] = np.einsum('tii->ti', rhos).real
+
+    # tight zvode for the integrator gap (reference as shipped)
+    qeom.integrate = qutils.integrate
+    qresp.integrate = qutils.integrate
+    t, rhos = qs.simulate_dynamics(m7, psi, duration=1000.0, rtol=1e-12,
+                                   atol=1e-14, nsteps=100000)
+    out['fmo7_dyn_pops_zvode'] = np.einsum('tii->ti', rhos).real
+    f, X = qs.absorption_spectra(m7, 2048.0, rtol=1e-12, atol=1e-14,
+                                 nsteps=100000)
+    out['fmo7_abs_X_zvode'] = X
+
+    # ---- third-order response on a 3-site chain, 'gef' --------------------
+    qeom.integrate = rk4_harness(2.0)
+    qresp.integrate = rk4_harness(2.0)
+    H3 = wl.chain_hamiltonian(n_sites=3, seed=7)
+    bath300 = qs.DebyeBath(qs.CM_K * 300, 40, 100)
+    extra3 = wl.energy_spread_for_dt(H3, 2.0, qs.CM_FS)
+    ham3 = qs.ElectronicHamiltonian(H3, bath=bath300, dipoles=[[1, 0, 0]] * 3,
+                                    energy_spread_extra=extra3)
+    m3 = qs.RedfieldModel(ham3, hilbert_subspace='gef', unit_convert=qs.CM_FS,
+                          secular=False)
+    assert m3.time_step == 2.0
+    out['chain3_H'] = H3
+    out['chain3_extra'] = extra3
+    for geo in ('-++', '+-+'):
+        (t1, t2, t3), S = qs.third_order_response(
+            m3, coherence_time_max=40.0, population_times=[0.0, 20.0, 50.0],
+            geometry=geo)
+        out['chain3_3rd_' + geo] = S
+    out['chain3_t1'] = t1
+
+    # ---- HEOM generators (heom.py:298-443) --------------------------------
+    H2 = np.array([[12400., -100], [-100, 12480]])
+    hamh = qs.ElectronicHamiltonian(H2, bath=qs.DebyeBath(qs.CM_K * 300, 35, 106),
+                                    dipoles=[[1, 0, 0]] * 2)
+    for tag, kw in {'K1lc3': dict(K=1, level_cutoff=3, low_temp_corr=True),
+                    'K0lc4': dict(K=0, level_cutoff=4, low_temp_corr=True),
+                    'K0lc3_nolt': dict(K=0, level_cutoff=3, low_temp_corr=False),
+                    'K1lc3_mod': dict(K=1, level_cutoff=3, low_temp_corr=True,
+                                      modified_HEOM=True)}.items():
+        hm = qs.HEOMModel(hamh, hilbert_subspace='e', unit_convert=qs.CM_FS, **kw)
+        L = hm.HEOM_tensor('ee').tocoo()
+        out['heom2_{}_row'.format(tag)] = L.row
+        out['heom2_{}_col'.format(tag)] = L.col
+        out['heom2_{}_val'.format(tag)] = L.data
+        out['heom2_{}_n'.format(tag)] = np.array(L.shape)
+        out['heom2_{}_order'.format(tag)] = np.array(
+            [a.reshape(-1) for a in hm.ado_indices])
+    out['heom2_H'] = H2
+    H3r = wl.ring_hamiltonian(n_sites=3, seed=5)
+    hm = qs.HEOMModel(qs.ElectronicHamiltonian(
+        H3r, bath=qs.DebyeBath(qs.CM_K * 300, 35, 106)),
+        hilbert_subspace='e', unit_convert=qs.CM_FS, K=0, level_cutoff=3)
+    L = hm.HEOM_tensor('ee').tocsr()
+    out['heom3_H'] = H3r
+    rho0 = np.zeros(9, complex)
+    rho0[0] = 1
+    y0 = np.zeros(L.shape[0], complex)
+    y0[:9] = rho0
+    eom = hm.equation_of_motion('ee')
+    traj = rk4_harness(0.5)(eom, y0, np.arange(0, 100.0, 0.5))
+    out['heom3_traj_node0'] = traj[:, :9]
+
+    np.savez_compressed(os.path.join(HERE, 'reference_golden.npz'), **out)
+    print('wrote', len(out), 'arrays')
+
+
+if __name__ == '__main__':
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')

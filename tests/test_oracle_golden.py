@@ -1,0 +1,136 @@
+"""Pin the CPU oracle against fixtures produced by running the reference itself."""
+import numpy as np
+import pytest
+
+import oracle as orc
+from conftest import rel_err
+from qspectra_gb300 import workloads as wl
+
+CM_FS = orc.CM_FS
+
+
+def fmo7_model(golden, sample=None):
+    bath = orc.DebyeBathSpec(orc.CM_K * 77, 35, 106)
+    ham = orc.ElectronicHamiltonianSpec(
+        golden['fmo7_H'], dipoles=[[1, 0, 0]] * 7, disorder=wl.fwhm_for_sd(80.0),
+        random_seed=1, energy_spread_extra=float(golden['fmo7_extra']), bath=bath)
+    m = orc.RedfieldSpec(ham, bath, 'ge', CM_FS, secular=False)
+    return m if sample is None else m.sample(sample)
+
+
+def test_constants_match_reference_values():
+    assert orc.CM_FS == np.pi * 2 * 2.99792458e-5
+    assert orc.CM_K == 0.69503476
+
+
+@pytest.mark.parametrize('tag,TK,lam,gam', [('77K', 77, 35, 106),
+                                            ('300K', 300, 40, 100),
+                                            ('10K', 10, 35, 106)])
+def test_debye_corr(golden, tag, TK, lam, gam):
+    b = orc.DebyeBathSpec(orc.CM_K * TK, lam, gam)
+    xs = golden['corr_x']
+    c = np.array([b.corr_complex(x) for x in xs])
+    r = np.array([b.corr_real(x) for x in xs])
+    assert rel_err(c, golden['corr_complex_' + tag]) < 1e-14
+    assert rel_err(r, golden['corr_real_' + tag]) < 1e-14
+
+
+@pytest.mark.parametrize('sec', [0, 1])
+@pytest.mark.parametrize('dic', [0, 1])
+@pytest.mark.parametrize('basis', ['site', 'eigen'])
+def test_redfield_dimer_all_options(golden, sec, dic, basis):
+    bath = orc.DebyeBathSpec(orc.CM_K * 77, 35, 106)
+    ham = orc.ElectronicHamiltonianSpec(golden['dimer_H'],
+                                        dipoles=golden['dimer_dipoles'])
+    m = orc.RedfieldSpec(ham, bath, 'gef', CM_FS, secular=bool(sec),
+                         discard_imag_corr=bool(dic), evolve_basis=basis)
+    L = m.evolution_super_operator()
+    ref = golden['dimer_L_sec{}_dic{}_{}'.format(sec, dic, basis)]
+    if basis == 'eigen':
+        # eigenvector signs are arbitrary; compare sign-invariant magnitudes
+        assert rel_err(np.abs(L), np.abs(ref)) < 1e-12
+    else:
+        assert rel_err(L, ref) < 1e-12
+
+
+def test_fmo7_blocks_and_time_step(golden):
+    m = fmo7_model(golden)
+    assert m.time_step == 1.0
+    assert m.ham.rw_freq == pytest.approx(float(golden['fmo7_rw']), rel=1e-15)
+    assert rel_err(m.eom_matrix('ee'), golden['fmo7_L_ee']) < 1e-12
+    assert rel_err(m.eom_matrix('eg'), golden['fmo7_L_eg']) < 1e-12
+
+
+def test_fmo7_rk4_dynamics_and_absorption(golden):
+    m = fmo7_model(golden)
+    psi = np.zeros(7)
+    psi[0] = 1
+    t, rhos = orc.simulate_dynamics(m, psi, 1000.0)
+    pops = np.einsum('tii->ti', rhos).real
+    assert rel_err(pops, golden['fmo7_dyn_pops']) < 1e-12
+    assert rel_err(rhos[::10], golden['fmo7_dyn_rho_every10']) < 1e-12
+    t, sig = orc.linear_response(m, 2048.0)
+    assert rel_err(sig, golden['fmo7_abs_signal']) < 1e-12
+    f, X = orc.absorption_spectra(m, 2048.0)
+    assert rel_err(f, golden['fmo7_abs_f']) < 1e-14
+    assert rel_err(X, golden['fmo7_abs_X']) < 1e-12
+    # integrator gap to the reference's own tight zvode run (RK4 at 1 fs)
+    assert rel_err(pops, golden['fmo7_dyn_pops_zvode']) < 1e-5
+    assert rel_err(X, golden['fmo7_abs_X_zvode']) < 1e-5
+
+
+def test_fmo7_disorder_and_small_ensemble(golden):
+    m = fmo7_model(golden)
+    draws = np.array([np.diag(m.sample(n).ham.H1) for n in range(8)])
+    np.testing.assert_array_equal(draws, golden['fmo7_sample_diag'])
+    _, X = orc.ensemble_average(m, 8, orc.absorption_spectra, 2048.0)
+    assert rel_err(X, golden['fmo7_ens8_abs_X']) < 1e-12
+    psi = np.zeros(7)
+    psi[0] = 1
+    _, rhos = orc.ensemble_average(m, 8, orc.simulate_dynamics, psi, 1000.0)
+    pops = np.einsum('tii->ti', rhos).real
+    assert rel_err(pops, golden['fmo7_ens8_pops']) < 1e-12
+
+
+@pytest.mark.parametrize('geo', ['-++', '+-+'])
+def test_third_order_chain3(golden, geo):
+    bath = orc.DebyeBathSpec(orc.CM_K * 300, 40, 100)
+    ham = orc.ElectronicHamiltonianSpec(
+        golden['chain3_H'], dipoles=[[1, 0, 0]] * 3,
+        energy_spread_extra=float(golden['chain3_extra']), bath=bath)
+    m = orc.RedfieldSpec(ham, bath, 'gef', CM_FS, secular=False)
+    assert m.time_step == 2.0
+    _, S = orc.third_order_response(m, 40.0, [0.0, 20.0, 50.0], geometry=geo)
+    assert rel_err(S, golden['chain3_3rd_' + geo]) < 1e-11
+
+
+@pytest.mark.parametrize('tag,kw', [
+    ('K1lc3', dict(K=1, level_cutoff=3, low_temp_corr=True)),
+    ('K0lc4', dict(K=0, level_cutoff=4, low_temp_corr=True)),
+    ('K0lc3_nolt', dict(K=0, level_cutoff=3, low_temp_corr=False)),
+    ('K1lc3_mod', dict(K=1, level_cutoff=3, low_temp_corr=True,
+                       modified_HEOM=True))])
+def test_heom_generator(golden, tag, kw):
+    import scipy.sparse as sps
+    bath = orc.DebyeBathSpec(orc.CM_K * 300, 35, 106)
+    ham = orc.ElectronicHamiltonianSpec(golden['heom2_H'])
+    hm = orc.HEOMSpec(ham, bath, 'e', 1.0, **kw)
+    order = np.array([a.reshape(-1) for a in hm.ados])
+    np.testing.assert_array_equal(order, golden['heom2_{}_order'.format(tag)])
+    L = hm.heom_tensor('ee').toarray()
+    n = tuple(golden['heom2_{}_n'.format(tag)])
+    ref = sps.coo_matrix((golden['heom2_{}_val'.format(tag)],
+                          (golden['heom2_{}_row'.format(tag)],
+                           golden['heom2_{}_col'.format(tag)])), shape=n).toarray()
+    assert rel_err(L, ref) < 1e-13
+
+
+def test_heom_trajectory(golden):
+    bath = orc.DebyeBathSpec(orc.CM_K * 300, 35, 106)
+    ham = orc.ElectronicHamiltonianSpec(golden['heom3_H'])
+    hm = orc.HEOMSpec(ham, bath, 'e', CM_FS, K=0, level_cutoff=3)
+    L = hm.eom_matrix('ee')
+    y0 = np.zeros(L.shape[0], complex)
+    y0[0] = 1
+    traj = orc.rk4_integrate_sparse(L, y0, 199, 0.5)
+    assert rel_err(traj[:, :9], golden['heom3_traj_node0']) < 1e-12
