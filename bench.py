@@ -1,0 +1,313 @@
+#!/usr/bin/env python3
+"""Disorder-averaged spectra per second on one GB300.
+
+Workload (the batched-disorder configuration): 7-site Frenkel exciton
+Hamiltonian (E_i ~ U(12000, 12600), J_ij ~ N(0, 50^2), seed 1234), Debye bath
+λ = 35 cm^-1, γ = 106 cm^-1, T = 77 K, non-secular Redfield in the 'ge'
+Hilbert space, Gaussian static disorder SD 80 cm^-1, 16384 samples.  One
+step = the whole ensemble: per-sample Redfield generators, the 'eg'
+absorption signal over 2048 points and the 'ee' populations over 1000 points
+at dt = 1 fs (RK4), ensemble means and the DFT to the absorption spectrum.
+The unit is one disorder-averaged spectrum (all 16384 samples).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ('disorder-averaged spectra/sec at ≤1e-4 rel err vs FP64; '
+          'adjoint/forward time')
+UNIT = 'spectra/s'
+N_SAMPLES = 16384
+ABS_TIME, DYN_TIME = 2048.0, 1000.0
+CLOCK_QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+               'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+               'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+CONFIG = {'workload': 'fmo7 Redfield ensemble: 7 sites, 16384 disorder samples '
+                      '(SD 80 cm^-1), absorption 2048 x 1 fs + ee populations '
+                      '1000 x 1 fs',
+          'n_samples': N_SAMPLES, 'n_sites': 7, 'dt_fs': 1.0,
+          'absorption_points': 2048, 'population_points': 1000,
+          'hilbert_subspace': 'ge', 'secular': False,
+          'l2': 'no flush needed: each step rebuilds ~1.3 GB of generators and '
+                'propagators (> 129 MB L2)'}
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=10)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    p.add_argument('--samples', type=int, default=N_SAMPLES)
+    p.add_argument('--cpu-samples-per-core', type=int, default=24)
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--fp64-steps', type=int, default=2)
+    return p.parse_args()
+
+
+def fmo7_inputs():
+    from qspectra_gb300 import workloads as wl
+    from qspectra_gb300.constants import CM_FS
+    H = wl.fmo7_hamiltonian()
+    extra = wl.energy_spread_for_dt(H, 1.0, CM_FS)
+    return H, extra, wl.fwhm_for_sd(80.0)
+
+
+# ----------------------------------------------------------------- clocks
+def clocks_start(index=0):
+    try:
+        return subprocess.Popen(['nvidia-smi', '--query-gpu=' + CLOCK_QUERY,
+                                 '--format=csv,noheader,nounits', '-lms', '200',
+                                 '-i', str(index)],
+                                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                text=True)
+    except OSError:
+        return None
+
+
+def clocks_stop(proc):
+    if proc is None:
+        return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+    proc.terminate()
+    try:
+        out, _ = proc.communicate(timeout=10)
+    except subprocess.TimeoutExpired:
+        proc.kill()
+        out, _ = proc.communicate()
+    sm, smax, reasons, power = [], [], set(), []
+    names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+    for line in out.strip().splitlines():
+        f = [x.strip() for x in line.split(',')]
+        if len(f) < 9:
+            continue
+        try:
+            sm.append(float(f[1]))
+            smax.append(float(f[2]))
+            power.append(float(f[3]))
+        except ValueError:
+            continue
+        for name, val in zip(names, f[5:9]):
+            if val.lower().startswith('active'):
+                reasons.add(name)
+    if not sm:
+        return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['no samples']}
+    return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(smax),
+            'power_w_max': max(power) if power else None, 'samples': len(sm),
+            'reasons': sorted(reasons)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_baseline(H, extra, fwhm, per_core, n_full=N_SAMPLES, steps=1, warmup=0):
+    """Oracle port of the reference path over a spawn pool of all host cores."""
+    import multiprocessing as mp
+    from oracle import baseline as ob
+    cores = os.cpu_count() or 1
+    n = per_core * cores
+    ctx = mp.get_context('spawn')
+    # one BLAS thread per worker process (spawned children read these at import)
+    for var in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+        os.environ[var] = '1'
+    vals = []
+    with ctx.Pool(cores) as pool:
+        ob.time_fmo7_samples(H, extra, fwhm, cores, workers=cores, pool=pool)  # warm
+        for k in range(warmup + steps):
+            wall, _, _ = ob.time_fmo7_samples(H, extra, fwhm, n, workers=cores, pool=pool,
+                                              start=k * n)
+            if k >= warmup:
+                vals.append(1.0 / (wall / n * n_full))
+    return {'value': float(np.mean(vals)), 'unit': UNIT, 'cores': cores, 'kind': 'port',
+            'sample': '{} disorder samples per measurement ({} per core) of the same '
+                      'workload, one sample at a time per process like the reference '
+                      'ensemble loop; spectra/s extrapolated linearly to {} samples'.format(
+                          n, per_core, n_full)}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return 0
+    H, extra, fwhm = fmo7_inputs()
+    base = cpu_baseline(H, extra, fwhm, args.cpu_samples_per_core, args.samples,
+                        steps=args.steps, warmup=args.warmup)
+    val = base['value']
+    line = {'metric': METRIC, 'value': val, 'unit': UNIT, 'impl': 'reference',
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': 1000.0 / val, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'c128',
+            'data': 'synthetic (seeded)', 'config': dict(CONFIG),
+            'cpu_baseline': base,
+            'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# -------------------------------------------------------------- GPU arm
+def fma_peak_tflops(torch, native):
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4000
+    out = torch.empty(blocks * threads, dtype=torch.float32, device='cuda')
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        native.probe_fma(native.QSX_FP32, blocks, threads, iters, out)
+        e1.record()
+        torch.cuda.synchronize()
+        flops = 2.0 * blocks * threads * iters * 16 * 8
+        best = max(best, flops / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def ncu_traffic(path=os.path.join(ROOT, 'profiles', 'rk4_rows_f32_fmo7.md')):
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r'traffic_bytes_per_full_launch:\s*([0-9.eE+]+)', txt)
+    return float(m.group(1)) if m else None
+
+
+def our_arm(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group('nccl')
+    import qspectra_gb300 as qg
+    from qspectra_gb300 import _native
+    from qspectra_gb300.simulate.ensemble import RedfieldEnsembleWorkload
+
+    H, extra, fwhm = fmo7_inputs()
+    S = args.samples
+    ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 77, 35, 106),
+                                   dipoles=[[1, 0, 0]] * 7, disorder=fwhm, random_seed=1,
+                                   energy_spread_extra=extra)
+    model = qg.RedfieldModel(ham, hilbert_subspace='ge', unit_convert=qg.CM_FS,
+                             secular=False)
+    psi = np.zeros(7)
+    psi[0] = 1.0
+    work = RedfieldEnsembleWorkload(model, ABS_TIME, DYN_TIME, psi)
+    off_host = torch.as_tensor(model.hamiltonian.disorder_offsets(S, start=rank * S)).pin_memory()
+    off = off_host.cuda()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        work.run(off, 'fp32')
+    barrier()
+    clk = clocks_start(local) if rank == 0 else None
+    events = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        X32, P32, status = work.run(off, 'fp32', events)
+    e1.record()
+    barrier()
+    clocks = clocks_stop(clk) if rank == 0 else None
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    if int(status.item()) & _native.QSX_ERR_NONFINITE:
+        raise _native.IntegratorError('non-finite state in the timed run')
+    value = world * 1000.0 / ms
+    dyn_ms = statistics.mean(a.elapsed_time(b) for a, b in events['dyn'])
+
+    # end to end through the library call with host buffers
+    for _ in range(2):
+        work.run_host(off_host, 'fp32')
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        Xh, Ph = work.run_host(off_host, 'fp32')
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # plain FP64 form, side by side, and the FP32 error against it
+    work.run(off, 'fp64')
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(args.fp64_steps):
+        X64, P64, _ = work.run(off, 'fp64')
+    f1.record()
+    torch.cuda.synchronize()
+    fp64_ms = f0.elapsed_time(f1) / args.fp64_steps
+    err_spec = float((X32 - X64).abs().max() / X64.abs().max())
+    err_pop = float((P32 - P64).abs().max() / P64.abs().max())
+
+    if rank != 0:
+        return 0
+    peak = fma_peak_tflops(torch, _native)
+    flops_dyn = float(S) * (DYN_TIME - 1) * 49 * 49 * 8  # complex GEMV per step
+    achieved = flops_dyn / (dyn_ms * 1e-3) / 1e12
+    traffic = ncu_traffic()
+    base = None
+    if world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(H, extra, fwhm, args.cpu_samples_per_core, S)
+    nf = Xh.size
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'c64 split-word (FP32 bulk, FP64 Redfield build)',
+        'data': 'synthetic (seeded Hamiltonians and disorder draws)',
+        'config': dict(CONFIG, parallelism='replicas (weak: each GPU runs its own '
+                                           '16384-sample ensemble)' if world > 1 else 'single GPU'),
+        'fp32_vs_fp64_rel_err': {'spectrum': err_spec, 'populations': err_pop},
+        'fp64_ms_per_step': fp64_ms, 'speedup_fp32_vs_fp64': fp64_ms / ms,
+        'e2e': {'value': world * 1000.0 / e2e_ms, 'unit': UNIT,
+                'h2d_bytes_per_step': int(off_host.numel() * 8),
+                'd2h_bytes_per_step': int((nf + Ph.size + 1) * 8)},
+        'roofline': {'kernel': 'rk4_rows_f32<49,5> (ee populations)',
+                     'bound': 'fp32_fma', 'achieved': achieved, 'peak': peak,
+                     'unit': 'TFLOP/s', 'frac': achieved / peak,
+                     'peak_source': 'measured live by qsx_probe_fma (FP32 FMA); '
+                                    'MEASURED_PEAKS.json has no CUDA-core figure',
+                     'flops_per_launch': flops_dyn, 'launch_ms': dyn_ms,
+                     'traffic': traffic},
+        'gpu_launches': 11 * args.steps,
+        'clocks': clocks,
+    }
+    if base is not None:
+        line['cpu_baseline'] = base
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == 'reference':
+        return reference_arm(args)
+    return our_arm(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -1,0 +1,187 @@
+/*
+ * qsx — C ABI of the GB300 (sm_103a) Liouville-space propagation library.
+ *
+ * Every entry point takes caller-owned DEVICE pointers (plain pointers and
+ * sizes), an explicit cudaStream_t passed as void*, and returns an int status
+ * (QSX_OK = 0).  Nothing is allocated by the library: buffers and scratch
+ * ("workspace") come from the caller; qsx_*_workspace_bytes says how much.
+ * complex128 arrays are interleaved {re, im} doubles (the layout of
+ * torch.complex128 / numpy.complex128), complex64 interleaved floats.
+ * No C++ exception crosses this boundary; qsx_last_error_string() describes
+ * the last failure on the calling host thread.
+ *
+ * Each declaration names the reference (whaley-group-berkeley/qspectra)
+ * function it replaces, by file:line within that project.
+ */
+#ifndef QSX_H_
+#define QSX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  QSX_OK = 0,
+  QSX_ERR_INVALID_ARG = 1, /* bad shape, size, subspace index or pointer */
+  QSX_ERR_CUDA = 2,        /* a CUDA runtime call or launch failed */
+  QSX_ERR_UNSUPPORTED = 3, /* valid request this build does not implement */
+  QSX_ERR_NONFINITE = 4    /* a NaN/Inf was detected in a state */
+};
+
+enum { QSX_FP64 = 0, QSX_FP32 = 1 };
+
+/* Message for the last non-zero status on this host thread. */
+const char* qsx_last_error_string(void);
+
+/* Library ABI version (major * 100 + minor). */
+int qsx_version(void);
+
+/*
+ * One-sided Debye bath correlation function C(x) at n points, complex128 out.
+ * Replaces DebyeBath.corr_func_complex (qspectra/bath.py:84-102) with its
+ * truncated Matsubara sum of `matsubara_cutoff` terms evaluated in closed
+ * form, and Bath.corr_func_real (qspectra/bath.py:17-31) when real_only != 0.
+ */
+int qsx_debye_corr(const double* x, int64_t n, double temperature,
+                   double reorg_energy, double cutoff_freq,
+                   int matsubara_cutoff, int real_only, double* out,
+                   void* stream);
+
+/*
+ * Batched real-symmetric eigensolver (cyclic Jacobi, FP64), n <= 32.
+ * H, U: [batch][n][n] row-major; E: [batch][n].  Eigenvalues are sorted
+ * ascending inside each diagonal block [block_starts[k], block_starts[k+1])
+ * (block_starts is a HOST array of nblocks + 1 ints), which reproduces the
+ * g/e/f manifold ordering of Hamiltonian.eig (qspectra/hamiltonian.py:310-328,
+ * scipy.linalg.eigh of the non-rotating H).  U holds eigenvectors as columns.
+ */
+int qsx_eigh_batched(const double* H, int n, int64_t batch, int nblocks,
+                     const int* block_starts, double* E, double* U,
+                     void* stream);
+
+/*
+ * Redfield operators per disorder sample, FP64.  Replaces redfield_tensor
+ * (qspectra/dynamics/redfield.py:9-74) by its exact operator factorisation:
+ *   Kt_i = U^T diag(occ_i) U,  Mt_i[c][d] = Kt_i[c][d] * C(E_d - E_c),
+ *   GS   = sum_i Kt_i Mt_i      (the eigenbasis Gamma_abbc contraction),
+ * with C the Debye correlation function (qsx_debye_corr).  Outputs are
+ * scaled by unit_convert.  site_basis != 0 returns G = U GS U^T and
+ * M_i = U Mt_i U^T (K_i = diag(occ_i) then needs no output; pass K = NULL);
+ * site_basis == 0 returns GS, Mt_i and Kt_i (K must be non-NULL).
+ *   E [batch][n], U [batch][n][n], occ [n_sites][n] (shared),
+ *   G complex128 [batch][n][n], M complex128 [batch][n_sites][n][n],
+ *   K real [batch][n_sites][n][n].  n <= 32, n_sites <= 32.
+ */
+int qsx_redfield_operators_batched(const double* E, const double* U, int n,
+                                   int64_t batch, const double* occ,
+                                   int n_sites, double temperature,
+                                   double reorg_energy, double cutoff_freq,
+                                   int matsubara_cutoff, int discard_imag_corr,
+                                   double unit_convert, int site_basis,
+                                   double* G, double* M, double* K,
+                                   void* stream);
+
+/*
+ * Dense Liouvillian block L[idx, idx] (transposed when transpose != 0, the
+ * Heisenberg picture).  Replaces RedfieldModel.evolution_super_operator
+ * (qspectra/dynamics/redfield.py:95-104, 146-152) sliced by
+ * LiouvilleSpaceModel.equation_of_motion (liouville_space.py:316-330):
+ *   L[(a,b),(c,d)] = -i uc (H_ac d_bd - d_ac H_db) - s_abcd R_abcd,
+ *   R_abcd = d_bd G_ac + d_ac conj(G_bd)
+ *          - sum_i (K_i,ac conj(M_i,bd) + M_i,ac K_i,bd),
+ * with (a,b) <-> column-stacked index a + n*b, s = secular mask
+ * (redfield.py:77-83) when secular != 0 (eigenbasis inputs only) else 1.
+ *   H real [n][n] per sample (stride H_stride elements, 0 = shared),
+ *   G, M from qsx_redfield_operators_batched, K real [n_sites][n][n] with
+ *   stride K_stride (0 = shared); K == NULL means the site-basis number
+ *   operators K_i = diag(occ_i) given by occ [n_sites][n] (device),
+ *   idx int32 [m] (device), L complex128 [batch][m][m].
+ */
+int qsx_redfield_liouvillian_batched(const double* H, int64_t H_stride,
+                                     const double* G, const double* M,
+                                     const double* K, int64_t K_stride,
+                                     const double* occ,
+                                     int n, int n_sites, int64_t batch,
+                                     double unit_convert, const int* idx,
+                                     int m, int secular, int transpose,
+                                     double* L, void* stream);
+
+/*
+ * RK4 propagator D = P - I with P = sum_{k<=4} (hL)^k / k!, i.e. exactly one
+ * classical RK4 step of dy/dt = L y (the step inside the integrate loop,
+ * qspectra/simulate/utils.py:44-49, with zvode replaced by RK4).
+ * L complex128 [batch][m][m]; D complex64 (QSX_FP32) or complex128
+ * (QSX_FP64) [batch][m][m].  m <= 64.
+ */
+int qsx_rk4_propagator_batched(const double* L, int m, int64_t batch,
+                               double h, int precision, void* D, void* stream);
+
+/*
+ * Batched fixed-step RK4 time loop for linear equations of motion.
+ * Replaces integrate / _integrate (qspectra/simulate/utils.py:16-109) for
+ * eom(t, y) = L y, and the serial ensemble loop of optional_ensemble_average
+ * (qspectra/simulate/decorators.py:40-64) when out_mean is set.
+ */
+typedef struct {
+  int32_t precision;      /* QSX_FP64 or QSX_FP32 (split-word FP32 state) */
+  int32_t form;           /* 0: matrix = D = P - I, 1: matrix = L (stages) */
+  int32_t m;              /* state dimension */
+  int32_t nsteps;         /* RK4 steps */
+  int64_t batch;          /* independent samples */
+  const void* matrix;     /* complex64/complex128 [batch][m][m] */
+  int64_t matrix_stride;  /* elements between samples, 0 = shared */
+  double h;               /* step, used by form 1 */
+  const double* y0;       /* complex128 [batch][m] */
+  int64_t y0_stride;      /* elements between samples, 0 = shared */
+  int32_t save_every;     /* output every save_every steps, from step 0 */
+  int32_t nproj;          /* rows of proj (dense projections), 0 = none */
+  const double* proj;     /* complex128 [nproj][m] per sample */
+  int64_t proj_stride;    /* elements between samples, 0 = shared */
+  int32_t nselect;        /* selected state components, 0 = none */
+  int32_t pad0;
+  const int32_t* select;  /* int32 [nselect] (device) */
+  double* out_state;      /* complex128 [batch][nsave][m] or NULL */
+  double* out_proj;       /* complex128 [batch][nsave][nout] or NULL */
+  double* out_mean;       /* complex128 [nsave][nout] or NULL */
+  double mean_scale;      /* out_mean = mean_scale * sum over samples */
+  void* workspace;        /* scratch for out_mean partial sums */
+  size_t workspace_bytes;
+  int32_t* status;        /* device int: set to QSX_ERR_NONFINITE on NaN/Inf */
+} qsx_rk4_args;
+/* nsave = nsteps / save_every + 1; nout = nproj if nproj > 0 else nselect. */
+
+/* sizeof(qsx_rk4_args) as compiled into the library, for FFI bindings to
+ * check their struct declaration against. */
+size_t qsx_rk4_args_bytes(void);
+
+int qsx_rk4_workspace_bytes(const qsx_rk4_args* args, size_t* bytes);
+int qsx_rk4_batched(const qsx_rk4_args* args, void* stream);
+
+/*
+ * Direct discrete Fourier transform of uniformly sampled signals,
+ *   X[b][k] = dt * sum_n x[b][n] exp(i * sign * (freqs[k] - rw_freq) * uc * t_n),
+ * t_n = t0 + n dt.  With freqs on the FFT grid this equals fourier_transform
+ * (qspectra/simulate/utils.py:154-219: zero padding to a symmetric time
+ * grid, fftshift/fft/ifftshift, sign flip, + rw_freq); any other grid
+ * (e.g. 1024 frequencies in a window) is evaluated directly.
+ * x complex128 [batch][nt], freqs float64 [nf] (device), X complex128 [batch][nf].
+ */
+int qsx_dft_batched(const double* x, int nt, int64_t batch, double t0,
+                    double dt, const double* freqs, int nf, double rw_freq,
+                    double unit_convert, int sign, double* X, void* stream);
+
+/*
+ * Peak-throughput probes (no reference counterpart): each thread runs
+ * `iters` iterations of 8 independent FMA chains (FP32 or FP64) and writes
+ * one value to out[thread].  Used to measure the CUDA-core FMA roofline.
+ */
+int qsx_probe_fma(int precision, int64_t blocks, int threads, int iters,
+                  void* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QSX_H_ */

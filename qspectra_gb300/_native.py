@@ -1,0 +1,327 @@
+"""ctypes binding of the qsx C ABI (include/qsx.h) plus thin torch wrappers.
+
+Every wrapper takes CUDA tensors, checks dtype/shape/contiguity, launches on
+torch's current stream and returns CUDA tensors.  There is no CPU fallback:
+if the library is not built or no GPU is present the call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, '_lib', 'libqsx.so')
+
+QSX_FP64 = 0
+QSX_FP32 = 1
+QSX_ERR_NONFINITE = 4
+
+_c_int = ctypes.c_int
+_c_i64 = ctypes.c_int64
+_c_dbl = ctypes.c_double
+_c_vp = ctypes.c_void_p
+
+
+class QsxError(RuntimeError):
+    """A non-zero status returned by the qsx library."""
+
+
+class IntegratorError(QsxError):
+    """Non-finite state during integration (cf. simulate/utils.py:12-13)."""
+
+
+class Rk4Args(ctypes.Structure):
+    _fields_ = [
+        ('precision', ctypes.c_int32), ('form', ctypes.c_int32),
+        ('m', ctypes.c_int32), ('nsteps', ctypes.c_int32),
+        ('batch', ctypes.c_int64),
+        ('matrix', _c_vp), ('matrix_stride', ctypes.c_int64),
+        ('h', ctypes.c_double),
+        ('y0', _c_vp), ('y0_stride', ctypes.c_int64),
+        ('save_every', ctypes.c_int32), ('nproj', ctypes.c_int32),
+        ('proj', _c_vp), ('proj_stride', ctypes.c_int64),
+        ('nselect', ctypes.c_int32), ('pad0', ctypes.c_int32),
+        ('select', _c_vp),
+        ('out_state', _c_vp), ('out_proj', _c_vp), ('out_mean', _c_vp),
+        ('mean_scale', ctypes.c_double),
+        ('workspace', _c_vp), ('workspace_bytes', ctypes.c_size_t),
+        ('status', _c_vp),
+    ]
+
+
+_PROTOS = {
+    'qsx_last_error_string': (ctypes.c_char_p, []),
+    'qsx_version': (_c_int, []),
+    'qsx_debye_corr': (_c_int, [_c_vp, _c_i64, _c_dbl, _c_dbl, _c_dbl, _c_int,
+                                _c_int, _c_vp, _c_vp]),
+    'qsx_eigh_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int,
+                                  ctypes.POINTER(ctypes.c_int), _c_vp, _c_vp,
+                                  _c_vp]),
+    'qsx_redfield_operators_batched': (_c_int, [
+        _c_vp, _c_vp, _c_int, _c_i64, _c_vp, _c_int, _c_dbl, _c_dbl, _c_dbl,
+        _c_int, _c_int, _c_dbl, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
+    'qsx_redfield_liouvillian_batched': (_c_int, [
+        _c_vp, _c_i64, _c_vp, _c_vp, _c_vp, _c_i64, _c_vp, _c_int, _c_int,
+        _c_i64, _c_dbl, _c_vp, _c_int, _c_int, _c_int, _c_vp, _c_vp]),
+    'qsx_rk4_propagator_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl,
+                                            _c_int, _c_vp, _c_vp]),
+    'qsx_rk4_args_bytes': (ctypes.c_size_t, []),
+    'qsx_rk4_workspace_bytes': (_c_int, [ctypes.POINTER(Rk4Args),
+                                         ctypes.POINTER(ctypes.c_size_t)]),
+    'qsx_rk4_batched': (_c_int, [ctypes.POINTER(Rk4Args), _c_vp]),
+    'qsx_dft_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
+                                 _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
+    'qsx_probe_fma': (_c_int, [_c_int, _c_i64, _c_int, _c_int, _c_vp, _c_vp]),
+}
+
+_LIB = None
+
+
+def exported_symbols():
+    """Names the header declares (for the ABI test)."""
+    return sorted(_PROTOS)
+
+
+def load(path=LIB_PATH):
+    """Load libqsx.so and attach prototypes (no GPU needed)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(path):
+            raise QsxError(
+                'qsx CUDA library not found at {}; build it with '
+                '`python -m qspectra_gb300.build`'.format(path))
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+def _check(status, what):
+    if status != 0:
+        msg = load().qsx_last_error_string().decode(errors='replace')
+        raise QsxError('{} failed (status {}): {}'.format(what, status, msg))
+
+
+def _stream():
+    return _c_vp(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t):
+    return None if t is None else _c_vp(t.data_ptr())
+
+
+def _need(t, dtype, name, ndim=None):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise ValueError('{} must be a CUDA tensor'.format(name))
+    if t.dtype != dtype:
+        raise ValueError('{} must be {} (got {})'.format(name, dtype, t.dtype))
+    if not t.is_contiguous():
+        raise ValueError('{} must be contiguous'.format(name))
+    if ndim is not None and t.dim() != ndim:
+        raise ValueError('{} must have {} dims'.format(name, ndim))
+    return t
+
+
+def require_gpu():
+    if not torch.cuda.is_available():
+        raise QsxError('qspectra_gb300 needs a CUDA GPU; none is visible')
+    load()
+
+
+# --------------------------------------------------------------- wrappers
+def debye_corr(x, temperature, reorg_energy, cutoff_freq, matsubara_cutoff=1000,
+               real_only=False):
+    require_gpu()
+    x = _need(x.contiguous(), torch.float64, 'x')
+    out = torch.empty(x.shape, dtype=torch.complex128, device=x.device)
+    _check(load().qsx_debye_corr(_p(x), x.numel(), temperature, reorg_energy,
+                                 cutoff_freq, matsubara_cutoff, int(real_only),
+                                 _p(out), _stream()), 'qsx_debye_corr')
+    return out
+
+
+def eigh(H, block_starts):
+    """Batched Jacobi eigensolver; H (B, n, n) float64 CUDA."""
+    require_gpu()
+    _need(H, torch.float64, 'H', 3)
+    B, n, _ = H.shape
+    E = torch.empty((B, n), dtype=torch.float64, device=H.device)
+    U = torch.empty((B, n, n), dtype=torch.float64, device=H.device)
+    blk = (ctypes.c_int * len(block_starts))(*[int(v) for v in block_starts])
+    _check(load().qsx_eigh_batched(_p(H), n, B, len(block_starts) - 1, blk,
+                                   _p(E), _p(U), _stream()), 'qsx_eigh_batched')
+    return E, U
+
+
+def redfield_operators(E, U, occ, bath, unit_convert, discard_imag_corr=False,
+                       site_basis=True, matsubara_cutoff=1000):
+    require_gpu()
+    _need(E, torch.float64, 'E', 2)
+    _need(U, torch.float64, 'U', 3)
+    _need(occ, torch.float64, 'occ', 2)
+    B, n = E.shape
+    N = occ.shape[0]
+    dev = E.device
+    G = torch.empty((B, n, n), dtype=torch.complex128, device=dev)
+    M = torch.empty((B, N, n, n), dtype=torch.complex128, device=dev)
+    K = None if site_basis else torch.empty((B, N, n, n), dtype=torch.float64,
+                                            device=dev)
+    _check(load().qsx_redfield_operators_batched(
+        _p(E), _p(U), n, B, _p(occ), N, bath.temperature, bath.reorg_energy,
+        bath.cutoff_freq, matsubara_cutoff, int(discard_imag_corr), unit_convert,
+        int(site_basis), _p(G), _p(M), _p(K), _stream()),
+        'qsx_redfield_operators_batched')
+    return G, M, K
+
+
+def redfield_liouvillian(H, G, M, idx, unit_convert, K=None, occ=None,
+                         secular=False, transpose=False):
+    """Dense L[idx, idx] per sample (complex128)."""
+    require_gpu()
+    _need(G, torch.complex128, 'G', 3)
+    _need(M, torch.complex128, 'M', 4)
+    B, n, _ = G.shape
+    N = M.shape[1]
+    H = _need(H, torch.float64, 'H')
+    h_stride = 0 if H.dim() == 2 else n * n
+    if K is not None:
+        _need(K, torch.float64, 'K')
+        k_stride = 0 if K.dim() == 3 else N * n * n
+    else:
+        _need(occ, torch.float64, 'occ', 2)
+        k_stride = 0
+    idx = _need(idx, torch.int32, 'idx', 1)
+    m = idx.numel()
+    L = torch.empty((B, m, m), dtype=torch.complex128, device=G.device)
+    _check(load().qsx_redfield_liouvillian_batched(
+        _p(H), h_stride, _p(G), _p(M), _p(K), k_stride, _p(occ), n, N, B,
+        unit_convert, _p(idx), m, int(secular), int(transpose), _p(L),
+        _stream()), 'qsx_redfield_liouvillian_batched')
+    return L
+
+
+def rk4_propagator(L, h, precision=QSX_FP64):
+    require_gpu()
+    _need(L, torch.complex128, 'L', 3)
+    B, m, _ = L.shape
+    dt = torch.complex64 if precision == QSX_FP32 else torch.complex128
+    D = torch.empty((B, m, m), dtype=dt, device=L.device)
+    _check(load().qsx_rk4_propagator_batched(_p(L), m, B, h, precision, _p(D),
+                                             _stream()),
+           'qsx_rk4_propagator_batched')
+    return D
+
+
+def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
+        state=False, proj=None, select=None, per_sample=True, mean=False,
+        check_finite=True, workspace=None):
+    """Batched RK4 time loop (see qsx_rk4_args in include/qsx.h).
+
+    matrix: (B, m, m) complex64 (FP32) / complex128 (FP64), or (m, m) shared.
+    y0: (B, m) or (m,) complex128.  proj: (P, m) or (B, P, m) complex128.
+    select: sequence of state indices.  Returns a dict with 'state'
+    (B, nsave, m), 'proj' (B, nsave, P) and/or 'mean' (nsave, P).
+    """
+    require_gpu()
+    if precision is None:
+        precision = QSX_FP32 if matrix.dtype == torch.complex64 else QSX_FP64
+    want = torch.complex64 if precision == QSX_FP32 else torch.complex128
+    _need(matrix, want, 'matrix')
+    m = matrix.shape[-1]
+    dev = matrix.device
+    y0 = _need(y0.to(torch.complex128).contiguous(), torch.complex128, 'y0')
+    B = matrix.shape[0] if matrix.dim() == 3 else (y0.shape[0] if y0.dim() == 2 else 1)
+    if matrix.dim() == 3 and matrix.shape[0] != B:
+        raise ValueError('matrix batch does not match')
+    if y0.dim() == 2 and y0.shape[0] != B:
+        raise ValueError('y0 batch does not match')
+    if nsteps % save_every:
+        raise ValueError('nsteps must be a multiple of save_every')
+    nsave = nsteps // save_every + 1
+    a = Rk4Args()
+    a.precision = precision
+    a.form = form
+    a.m = m
+    a.nsteps = nsteps
+    a.batch = B
+    a.matrix = matrix.data_ptr()
+    a.matrix_stride = m * m if matrix.dim() == 3 else 0
+    a.h = h
+    a.y0 = y0.data_ptr()
+    a.y0_stride = m if y0.dim() == 2 else 0
+    a.save_every = save_every
+    keep = []
+    nout = 0
+    if proj is not None:
+        proj = _need(proj.to(torch.complex128).contiguous(), torch.complex128, 'proj')
+        a.nproj = proj.shape[-2]
+        a.proj = proj.data_ptr()
+        a.proj_stride = a.nproj * m if proj.dim() == 3 else 0
+        nout = a.nproj
+        keep.append(proj)
+    if select is not None:
+        sel_np = np.asarray(select, dtype=np.int64).reshape(-1)
+        if sel_np.size == 0 or sel_np.min() < 0 or sel_np.max() >= m:
+            raise ValueError('select indices must lie in [0, {})'.format(m))
+        sel = torch.as_tensor(sel_np, dtype=torch.int32).to(dev).contiguous()
+        a.nselect = sel.numel()
+        a.select = sel.data_ptr()
+        nout = a.nselect
+        keep.append(sel)
+    out = {}
+    if state:
+        out['state'] = torch.empty((B, nsave, m), dtype=torch.complex128, device=dev)
+        a.out_state = out['state'].data_ptr()
+    if nout and per_sample:
+        out['proj'] = torch.empty((B, nsave, nout), dtype=torch.complex128, device=dev)
+        a.out_proj = out['proj'].data_ptr()
+    if nout and mean:
+        out['mean'] = torch.empty((nsave, nout), dtype=torch.complex128, device=dev)
+        a.out_mean = out['mean'].data_ptr()
+        a.mean_scale = 1.0 / B
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    a.status = status.data_ptr()
+    lib = load()
+    if mean and nout:
+        nbytes = ctypes.c_size_t(0)
+        _check(lib.qsx_rk4_workspace_bytes(ctypes.byref(a), ctypes.byref(nbytes)),
+               'qsx_rk4_workspace_bytes')
+        if workspace is None or workspace.numel() < nbytes.value:
+            workspace = torch.empty(max(nbytes.value, 1), dtype=torch.uint8, device=dev)
+        a.workspace = workspace.data_ptr()
+        a.workspace_bytes = workspace.numel()
+    _check(lib.qsx_rk4_batched(ctypes.byref(a), _stream()), 'qsx_rk4_batched')
+    if check_finite:
+        st = int(status.item())
+        if st & QSX_ERR_NONFINITE:
+            raise IntegratorError('non-finite state during RK4 integration')
+        if st & 1:
+            raise QsxError('qsx_rk4_batched: index table out of range')
+    out['status'] = status
+    return out
+
+
+def dft(x, t0, dt, freqs, rw_freq=0.0, unit_convert=1.0, sign=1):
+    """X[b, k] = dt Σ_n x[b, n] exp(i sign (f_k - rw) uc (t0 + n dt))."""
+    require_gpu()
+    x = _need(x.to(torch.complex128).contiguous(), torch.complex128, 'x')
+    squeeze = x.dim() == 1
+    if squeeze:
+        x = x[None]
+    freqs = _need(torch.as_tensor(freqs, dtype=torch.float64, device=x.device).contiguous(),
+                  torch.float64, 'freqs', 1)
+    B, nt = x.shape
+    X = torch.empty((B, freqs.numel()), dtype=torch.complex128, device=x.device)
+    _check(load().qsx_dft_batched(_p(x), nt, B, t0, dt, _p(freqs), freqs.numel(),
+                                  rw_freq, unit_convert, sign, _p(X), _stream()),
+           'qsx_dft_batched')
+    return X[0] if squeeze else X
+
+
+def probe_fma(precision, blocks, threads, iters, out):
+    _check(load().qsx_probe_fma(precision, blocks, threads, iters, _p(out),
+                                _stream()), 'qsx_probe_fma')

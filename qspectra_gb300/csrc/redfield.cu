@@ -1,0 +1,457 @@
+// Redfield Liouvillian construction on the GPU (FP64): bath correlation
+// function, batched Jacobi eigensolver, operator-form Redfield tensor, dense
+// Liouvillian blocks and the RK4 one-step propagator.
+#include <cmath>
+
+#include "qsx_bath.cuh"
+#include "qsx_common.cuh"
+
+namespace qsx {
+
+// ------------------------------------------------------------------ C(x)
+__global__ void debye_corr_kernel(const double* x, int64_t n, DebyeParams p,
+                                  double2* out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = debye_corr(p, x[i]);
+}
+
+// ------------------------------------------------------------ eigensolver
+// One warp per matrix, matrix and eigenvectors in shared memory.  Cyclic
+// Jacobi sweeps (Golub & Van Loan, Alg. 8.4.3): for each pair (p, q) every
+// lane updates one row/column.  Block-diagonal inputs stay exactly block
+// diagonal because rotations of an exactly zero pair are skipped.
+constexpr int EIGH_NMAX = 32;
+constexpr int EIGH_WARPS = 4;
+
+struct BlockTable {
+  int v[EIGH_NMAX + 1];
+};
+
+__global__ void __launch_bounds__(32 * EIGH_WARPS)
+    eigh_jacobi_kernel(const double* __restrict__ H, int n, int64_t batch,
+                       int nblocks, BlockTable blocks, double* E, double* U) {
+  __shared__ double sA[EIGH_WARPS][EIGH_NMAX][EIGH_NMAX + 1];
+  __shared__ double sV[EIGH_WARPS][EIGH_NMAX][EIGH_NMAX + 1];
+  __shared__ int sBlk[EIGH_NMAX + 1];
+  const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int64_t b = (int64_t)blockIdx.x * EIGH_WARPS + w;
+  if (threadIdx.x <= nblocks && threadIdx.x <= EIGH_NMAX) sBlk[threadIdx.x] = blocks.v[threadIdx.x];
+  __syncthreads();
+  if (b >= batch) return;
+  double(*A)[EIGH_NMAX + 1] = sA[w];
+  double(*V)[EIGH_NMAX + 1] = sV[w];
+  const double* h = H + b * n * n;
+  for (int r = 0; r < n; ++r) {
+    if (lane < n) {
+      A[r][lane] = h[r * n + lane];
+      V[r][lane] = (r == lane) ? 1.0 : 0.0;
+    }
+  }
+  __syncwarp();
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    if (lane < n) {
+      for (int c = 0; c < n; ++c) {
+        double v = A[lane][c];
+        if (c == lane) dia += v * v; else off += v * v;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dia += __shfl_xor_sync(0xffffffffu, dia, o);
+    }
+    if (!(off > 1e-30 * dia) || off == 0.0) break;
+    for (int p = 0; p < n - 1; ++p) {
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[p][q];
+        if (apq == 0.0) continue;
+        const double app = A[p][p], aqq = A[q][q];
+        const double tau = (aqq - app) / (2.0 * apq);
+        const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + hypot(1.0, tau));
+        const double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
+        __syncwarp();
+        if (lane < n) {  // A <- A J and V <- V J on row `lane`
+          double akp = A[lane][p], akq = A[lane][q];
+          A[lane][p] = c * akp - s * akq;
+          A[lane][q] = s * akp + c * akq;
+          double vkp = V[lane][p], vkq = V[lane][q];
+          V[lane][p] = c * vkp - s * vkq;
+          V[lane][q] = s * vkp + c * vkq;
+        }
+        __syncwarp();
+        if (lane < n) {  // A <- J^T A on column `lane`
+          double apk = A[p][lane], aqk = A[q][lane];
+          A[p][lane] = c * apk - s * aqk;
+          A[q][lane] = s * apk + c * aqk;
+        }
+        __syncwarp();
+        if (lane == 0) {
+          A[p][q] = 0.0;
+          A[q][p] = 0.0;
+        }
+        __syncwarp();
+      }
+    }
+  }
+  // sort ascending inside each block (stable on ties)
+  if (lane < n) {
+    int blk = 0;
+    while (blk < nblocks - 1 && lane >= sBlk[blk + 1]) ++blk;
+    const int lo = sBlk[blk], hi = sBlk[blk + 1];
+    const double ev = A[lane][lane];
+    int rank = lo;
+    for (int j = lo; j < hi; ++j) {
+      double ej = A[j][j];
+      if (ej < ev || (ej == ev && j < lane)) ++rank;
+    }
+    E[b * n + rank] = ev;
+    for (int r = 0; r < n; ++r) U[b * n * n + r * n + rank] = V[r][lane];
+  }
+}
+
+// ------------------------------------------------- Redfield operator form
+// One CTA per sample.  Shared layout (n <= 32): U, Kt real; Cw, Mt, GS, T1
+// complex.  See qsx_redfield_operators_batched in qsx.h for the algebra.
+__device__ __forceinline__ void smem_matmul_rc(const double* A, const double2* B,
+                                               double2* C, int n, bool accumulate) {
+  // C = A (real) * B (complex)
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int r = e / n, c = e % n;
+    double2 acc = accumulate ? C[e] : cmk(0.0, 0.0);
+    for (int k = 0; k < n; ++k) {
+      double a = A[r * n + k];
+      double2 bb = B[k * n + c];
+      acc.x = fma(a, bb.x, acc.x);
+      acc.y = fma(a, bb.y, acc.y);
+    }
+    C[e] = acc;
+  }
+}
+
+__device__ __forceinline__ void smem_matmul_crT(const double2* A, const double* B,
+                                                double2* C, int n) {
+  // C = A (complex) * B^T (real)
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    int r = e / n, c = e % n;
+    double2 acc = cmk(0.0, 0.0);
+    for (int k = 0; k < n; ++k) {
+      double bb = B[c * n + k];
+      double2 a = A[r * n + k];
+      acc.x = fma(a.x, bb, acc.x);
+      acc.y = fma(a.y, bb, acc.y);
+    }
+    C[e] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    redfield_operators_kernel(const double* __restrict__ E, const double* __restrict__ U,
+                              int n, int64_t batch, const double* __restrict__ occ,
+                              int n_sites, DebyeParams bath, double uc, int site_basis,
+                              double2* G, double2* M, double* K) {
+  extern __shared__ double2 smem2[];
+  const int nn = n * n;
+  double2* sC = smem2;               // nn   (16-byte arrays first)
+  double2* sMt = sC + nn;            // nn
+  double2* sGS = sMt + nn;           // nn
+  double2* sT1 = sGS + nn;           // nn
+  double* sU = (double*)(sT1 + nn);  // nn
+  double* sUt = sU + nn;             // nn, U^T
+  double* sKt = sUt + nn;            // nn
+  double* sE = sKt + nn;             // n (<= 32)
+  const int64_t b = blockIdx.x;
+  const double* u = U + b * nn;
+  for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+    int r = e / n, c = e % n;
+    double v = u[e];
+    sU[e] = v;
+    sUt[c * n + r] = v;
+    sGS[e] = cmk(0.0, 0.0);
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    sE[i] = E[b * n + i];
+    double w = 0.0;  // total bath coupling weight of site-basis state i
+    for (int k = 0; k < n_sites; ++k) w += occ[k * n + i];
+    sE[32 + i] = w;
+  }
+  __syncthreads();
+  // correlation function only where some Kt_i[c][d] can be non-zero
+  for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+    int c = e / n, d = e % n;
+    double need = 0.0;
+    for (int s = 0; s < n; ++s) need += fabs(sU[s * n + c] * sU[s * n + d]) * sE[32 + s];
+    sC[e] = need > 0.0 ? debye_corr(bath, sE[d] - sE[c]) : cmk(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int i = 0; i < n_sites; ++i) {
+    const double* oc = occ + i * n;
+    for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+      int c = e / n, d = e % n;
+      double acc = 0.0;
+      for (int s = 0; s < n; ++s) {
+        double o = oc[s];
+        if (o != 0.0) acc = fma(sU[s * n + c] * o, sU[s * n + d], acc);
+      }
+      sKt[e] = acc;
+      double2 cw = sC[e];
+      sMt[e] = cmk(acc * cw.x, acc * cw.y);
+    }
+    __syncthreads();
+    smem_matmul_rc(sKt, sMt, sGS, n, true);  // GS += Kt_i Mt_i
+    __syncthreads();
+    double2* Mi = M + (b * n_sites + i) * nn;
+    if (site_basis) {
+      smem_matmul_rc(sU, sMt, sT1, n, false);  // T1 = U Mt_i
+      __syncthreads();
+      smem_matmul_crT(sT1, sU, sMt, n);        // Mt_i <- T1 U^T
+      __syncthreads();
+      for (int e = threadIdx.x; e < nn; e += blockDim.x) Mi[e] = cscale(sMt[e], uc);
+    } else {
+      double* Ki = K + (b * n_sites + i) * nn;
+      for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+        Mi[e] = cscale(sMt[e], uc);
+        Ki[e] = sKt[e];
+      }
+    }
+    __syncthreads();
+  }
+  double2* g = G + b * nn;
+  if (site_basis) {
+    smem_matmul_rc(sU, sGS, sT1, n, false);
+    __syncthreads();
+    smem_matmul_crT(sT1, sU, sMt, n);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += blockDim.x) g[e] = cscale(sMt[e], uc);
+  } else {
+    for (int e = threadIdx.x; e < nn; e += blockDim.x) g[e] = cscale(sGS[e], uc);
+  }
+}
+
+// ----------------------------------------------- dense Liouvillian block
+__global__ void liouvillian_kernel(const double* __restrict__ H, int64_t H_stride,
+                                   const double2* __restrict__ G,
+                                   const double2* __restrict__ M,
+                                   const double* __restrict__ K, int64_t K_stride,
+                                   const double* __restrict__ occ, int n, int n_sites,
+                                   double uc, const int* __restrict__ idx, int m,
+                                   int secular, int transpose, double2* L) {
+  const int64_t b = blockIdx.y;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)m * m) return;
+  int r = (int)(e / m), cc = (int)(e % m);
+  if (transpose) { int t = r; r = cc; cc = t; }
+  const int ir = idx[r], ic = idx[cc];
+  const int nn = n * n;
+  if (ir < 0 || ir >= nn || ic < 0 || ic >= nn) {  // bad index table: no access
+    L[b * (int64_t)m * m + e] = cmk(nan(""), nan(""));
+    return;
+  }
+  const int a = ir % n, bb = ir / n, c = ic % n, d = ic / n;
+  const double* h = H + b * H_stride;
+  const double2* g = G + b * nn;
+  const double2* mm = M + b * (int64_t)n_sites * nn;
+  // coherent part: -i uc (H_ac d_bd - d_ac H_db)
+  double hre = 0.0;
+  if (bb == d) hre += h[a * n + c];
+  if (a == c) hre -= h[d * n + bb];
+  double2 val = cmk(0.0, -uc * hre);
+  double2 R = cmk(0.0, 0.0);
+  if (bb == d) R = cadd(R, g[a * n + c]);
+  if (a == c) R = cadd(R, cconj(g[bb * n + d]));
+  if (K == nullptr) {
+    // site basis, K_i = diag(occ_i)
+    if (a == c) {
+      for (int i = 0; i < n_sites; ++i) {
+        double o = occ[i * n + a];
+        if (o != 0.0) R = csub(R, cscale(cconj(mm[i * nn + bb * n + d]), o));
+      }
+    }
+    if (bb == d) {
+      for (int i = 0; i < n_sites; ++i) {
+        double o = occ[i * n + bb];
+        if (o != 0.0) R = csub(R, cscale(mm[i * nn + a * n + c], o));
+      }
+    }
+  } else {
+    const double* k = K + b * K_stride;
+    for (int i = 0; i < n_sites; ++i) {
+      double kac = k[i * nn + a * n + c], kbd = k[i * nn + bb * n + d];
+      if (kac != 0.0) R = csub(R, cscale(cconj(mm[i * nn + bb * n + d]), kac));
+      if (kbd != 0.0) R = csub(R, cscale(mm[i * nn + a * n + c], kbd));
+    }
+  }
+  if (secular && !((a == bb && c == d) || (a == c && bb == d))) R = cmk(0.0, 0.0);
+  L[b * (int64_t)m * m + e] = csub(val, R);
+}
+
+// ------------------------------------------------ RK4 one-step propagator
+// D = h L (I + hL/2 (I + hL/3 (I + hL/4))), Horner form of P - I.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    propagator_kernel(const double2* __restrict__ L, int m, double h,
+                      typename cplx<T>::type* D) {
+  using C = typename cplx<T>::type;
+  extern __shared__ unsigned char smraw[];
+  C* sL = (C*)smraw;
+  C* sX = sL + m * m;
+  C* sY = sX + m * m;
+  const int64_t b = blockIdx.x;
+  const int mm = m * m;
+  const double2* l = L + b * mm;
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) {
+    double2 v = l[e];
+    sL[e] = cmk((T)v.x, (T)v.y);
+    int r = e / m, c = e % m;
+    T s = (T)(h / 4.0);
+    sX[e] = cmk((T)(r == c ? 1 : 0) + s * (T)v.x, s * (T)v.y);
+  }
+  __syncthreads();
+  const T coef[3] = {(T)(h / 3.0), (T)(h / 2.0), (T)h};
+  for (int stage = 0; stage < 3; ++stage) {
+    for (int e = threadIdx.x; e < mm; e += blockDim.x) {
+      int r = e / m, c = e % m;
+      C acc = cmk((T)0, (T)0);
+      for (int k = 0; k < m; ++k) cfma(acc, sL[r * m + k], sX[k * m + c]);
+      sY[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < mm; e += blockDim.x) {
+      int r = e / m, c = e % m;
+      C y = sY[e];
+      if (stage < 2)
+        sX[e] = cmk((T)(r == c ? 1 : 0) + coef[stage] * y.x, coef[stage] * y.y);
+      else
+        D[b * mm + e] = cmk(coef[2] * y.x, coef[2] * y.y);
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace qsx
+
+using namespace qsx;
+
+extern "C" {
+
+int qsx_debye_corr(const double* x, int64_t n, double temperature,
+                   double reorg_energy, double cutoff_freq, int matsubara_cutoff,
+                   int real_only, double* out, void* stream) {
+  QSX_CHECK_ARG(n >= 0 && (n == 0 || (x && out)), "qsx_debye_corr: bad arguments");
+  QSX_CHECK_ARG(temperature > 0 && cutoff_freq > 0 && matsubara_cutoff >= 1,
+                "qsx_debye_corr: temperature, cutoff and matsubara_cutoff must be positive");
+  if (n == 0) return QSX_OK;
+  DebyeParams p = make_debye(temperature, reorg_energy, cutoff_freq,
+                             matsubara_cutoff, real_only);
+  debye_corr_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      x, n, p, (double2*)out);
+  QSX_LAUNCH_CHECK("qsx_debye_corr");
+  return QSX_OK;
+}
+
+int qsx_eigh_batched(const double* H, int n, int64_t batch, int nblocks,
+                     const int* block_starts, double* E, double* U, void* stream) {
+  QSX_CHECK_ARG(n >= 1 && n <= EIGH_NMAX, "qsx_eigh_batched: need 1 <= n <= %d (got %d)",
+                EIGH_NMAX, n);
+  QSX_CHECK_ARG(batch >= 0 && nblocks >= 1 && nblocks <= n && block_starts,
+                "qsx_eigh_batched: bad batch/blocks");
+  QSX_CHECK_ARG(block_starts[0] == 0 && block_starts[nblocks] == n,
+                "qsx_eigh_batched: blocks must cover [0, n)");
+  for (int k = 0; k < nblocks; ++k)
+    QSX_CHECK_ARG(block_starts[k] < block_starts[k + 1],
+                  "qsx_eigh_batched: blocks must be non-empty and increasing");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(H && E && U, "qsx_eigh_batched: null pointer");
+  BlockTable tb;
+  for (int k = 0; k <= EIGH_NMAX; ++k) tb.v[k] = k <= nblocks ? block_starts[k] : n;
+  unsigned grid = (unsigned)((batch + EIGH_WARPS - 1) / EIGH_WARPS);
+  eigh_jacobi_kernel<<<grid, 32 * EIGH_WARPS, 0, (cudaStream_t)stream>>>(
+      H, n, batch, nblocks, tb, E, U);
+  QSX_LAUNCH_CHECK("qsx_eigh_batched");
+  return QSX_OK;
+}
+
+int qsx_redfield_operators_batched(const double* E, const double* U, int n,
+                                   int64_t batch, const double* occ, int n_sites,
+                                   double temperature, double reorg_energy,
+                                   double cutoff_freq, int matsubara_cutoff,
+                                   int discard_imag_corr, double unit_convert,
+                                   int site_basis, double* G, double* M, double* K,
+                                   void* stream) {
+  QSX_CHECK_ARG(n >= 1 && n <= 32 && n_sites >= 1 && n_sites <= 32,
+                "qsx_redfield_operators_batched: need 1 <= n, n_sites <= 32 (got %d, %d)",
+                n, n_sites);
+  QSX_CHECK_ARG(temperature > 0 && cutoff_freq > 0 && matsubara_cutoff >= 1,
+                "qsx_redfield_operators_batched: bad bath parameters");
+  QSX_CHECK_ARG(batch >= 0, "qsx_redfield_operators_batched: negative batch");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(E && U && occ && G && M && (site_basis || K),
+                "qsx_redfield_operators_batched: null pointer");
+  QSX_CHECK_ARG(batch <= 0x7fffffff, "qsx_redfield_operators_batched: batch too large");
+  DebyeParams p = make_debye(temperature, reorg_energy, cutoff_freq, matsubara_cutoff,
+                             discard_imag_corr);
+  const size_t nn = (size_t)n * n;
+  const size_t smem = (3 * nn + 64) * sizeof(double) + 4 * nn * sizeof(double2);
+  cudaError_t e = cudaFuncSetAttribute(redfield_operators_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_operators_batched");
+  redfield_operators_kernel<<<(unsigned)batch, 256, smem, (cudaStream_t)stream>>>(
+      E, U, n, batch, occ, n_sites, p, unit_convert, site_basis, (double2*)G,
+      (double2*)M, K);
+  QSX_LAUNCH_CHECK("qsx_redfield_operators_batched");
+  return QSX_OK;
+}
+
+int qsx_redfield_liouvillian_batched(const double* H, int64_t H_stride, const double* G,
+                                     const double* M, const double* K, int64_t K_stride,
+                                     const double* occ, int n, int n_sites, int64_t batch,
+                                     double unit_convert, const int* idx, int m,
+                                     int secular, int transpose, double* L, void* stream) {
+  QSX_CHECK_ARG(n >= 1 && n_sites >= 1 && m >= 1 && (int64_t)m <= (int64_t)n * n,
+                "qsx_redfield_liouvillian_batched: bad sizes n=%d n_sites=%d m=%d", n,
+                n_sites, m);
+  QSX_CHECK_ARG(batch >= 0 && batch <= 65535,
+                "qsx_redfield_liouvillian_batched: batch must be in [0, 65535]");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(H && G && M && idx && L && (K || occ),
+                "qsx_redfield_liouvillian_batched: null pointer");
+  const int64_t mm = (int64_t)m * m;
+  dim3 grid((unsigned)((mm + 255) / 256), (unsigned)batch);
+  liouvillian_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(
+      H, H_stride, (const double2*)G, (const double2*)M, K, K_stride, occ, n, n_sites,
+      unit_convert, idx, m, secular, transpose, (double2*)L);
+  QSX_LAUNCH_CHECK("qsx_redfield_liouvillian_batched");
+  return QSX_OK;
+}
+
+int qsx_rk4_propagator_batched(const double* L, int m, int64_t batch, double h,
+                               int precision, void* D, void* stream) {
+  QSX_CHECK_ARG(m >= 1 && m <= 64, "qsx_rk4_propagator_batched: need 1 <= m <= 64 (got %d)",
+                m);
+  QSX_CHECK_ARG(batch >= 0 && batch <= 0x7fffffff, "qsx_rk4_propagator_batched: bad batch");
+  QSX_CHECK_ARG(precision == QSX_FP32 || precision == QSX_FP64,
+                "qsx_rk4_propagator_batched: bad precision");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(L && D, "qsx_rk4_propagator_batched: null pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t mm = (size_t)m * m;
+  if (precision == QSX_FP32) {
+    size_t smem = 3 * mm * sizeof(float2);
+    cudaError_t e = cudaFuncSetAttribute(propagator_kernel<float>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_propagator_batched");
+    propagator_kernel<float><<<(unsigned)batch, 256, smem, s>>>((const double2*)L, m, h,
+                                                                (float2*)D);
+  } else {
+    size_t smem = 3 * mm * sizeof(double2);
+    cudaError_t e = cudaFuncSetAttribute(propagator_kernel<double>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_propagator_batched");
+    propagator_kernel<double><<<(unsigned)batch, 256, smem, s>>>((const double2*)L, m, h,
+                                                                 (double2*)D);
+  }
+  QSX_LAUNCH_CHECK("qsx_rk4_propagator_batched");
+  return QSX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,596 @@
+// Batched fixed-step RK4 time loop for dy/dt = L y (one independent L per
+// disorder sample), replacing integrate() of qspectra/simulate/utils.py:16-109
+// and the serial ensemble loop of qspectra/simulate/decorators.py:40-64.
+//
+// Three kernels, chosen by qsx_rk4_batched:
+//   rk4_small_f32<M>  M <= 8, one thread per sample, propagator D = P - I in
+//                     registers, split-word FP32 state (absorption 'eg').
+//   rk4_rows_f32<M,G> M in {9,16,25,36,49,64}: one thread per row of D held
+//                     in registers, G samples per CTA, persistent grid,
+//                     state broadcast through shared memory (population 'ee').
+//   rk4_generic<T>    any M <= 4096, FP64 or FP32, propagator or RK4 stage
+//                     form, one CTA per sample, matrix in shared memory when
+//                     it fits (the plain FP64 form and odd sizes).
+// Ensemble means are reduced deterministically: every kernel writes partial
+// sums per "slot" (warp, CTA or sample) into caller workspace and
+// rk4_reduce_kernel sums the slots in a fixed order in FP64.
+#include <algorithm>
+
+#include "qsx_common.cuh"
+
+namespace qsx {
+
+struct Rk4P {
+  int m, nsteps, save_every, nsave, nproj, nselect, nout, form;
+  int64_t batch;
+  const void* matrix;
+  int64_t matrix_stride;
+  double h;
+  const double2* y0;
+  int64_t y0_stride;
+  const double2* proj;
+  int64_t proj_stride;
+  const int* select;
+  double2* out_state;
+  double2* out_proj;
+  double2* partial;  // [nslots][nsave][nout] or null
+  int* status;
+};
+
+__device__ __forceinline__ float2 f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
+
+// ---------------------------------------------------------------- small M
+template <int M>
+__global__ void __launch_bounds__(128) rk4_small_f32(Rk4P p) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = s < p.batch;
+  const int lane = threadIdx.x & 31;
+  const int64_t slot = s >> 5;
+  float2 D[M][M];
+  float yh[M][2], yl[M][2];
+  const float2* dm = (const float2*)p.matrix + (valid ? s * p.matrix_stride : 0);
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+#pragma unroll
+    for (int j = 0; j < M; ++j) D[i][j] = valid ? dm[i * M + j] : make_float2(0.f, 0.f);
+  }
+  const double2* y0 = p.y0 + (valid ? s * p.y0_stride : 0);
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    double2 v = valid ? y0[i] : make_double2(0.0, 0.0);
+    yh[i][0] = (float)v.x;
+    yh[i][1] = (float)v.y;
+    yl[i][0] = (float)(v.x - (double)yh[i][0]);
+    yl[i][1] = (float)(v.y - (double)yh[i][1]);
+  }
+  const double2* W = p.proj + (p.nproj ? (valid ? s * p.proj_stride : 0) : 0);
+  auto save = [&](int k) {
+    if (p.out_state && valid) {
+      double2* o = p.out_state + (s * p.nsave + k) * M;
+#pragma unroll
+      for (int i = 0; i < M; ++i)
+        o[i] = make_double2((double)yh[i][0] + (double)yl[i][0],
+                            (double)yh[i][1] + (double)yl[i][1]);
+    }
+    for (int q = 0; q < p.nout; ++q) {
+      float2 v = make_float2(0.f, 0.f);
+      if (p.nproj) {
+#pragma unroll
+        for (int j = 0; j < M; ++j) cfma(v, f2(W[q * M + j]), make_float2(yh[j][0], yh[j][1]));
+      } else {
+        const int sel = p.select[q];
+#pragma unroll
+        for (int j = 0; j < M; ++j)
+          if (j == sel) v = make_float2(yh[j][0], yh[j][1]);
+      }
+      if (!valid) v = make_float2(0.f, 0.f);
+      if (p.out_proj && valid)
+        p.out_proj[(s * p.nsave + k) * p.nout + q] = make_double2(v.x, v.y);
+      if (p.partial) {
+        double sx = v.x, sy = v.y;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          sx += __shfl_xor_sync(0xffffffffu, sx, o);
+          sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        }
+        if (lane == 0) p.partial[(slot * p.nsave + k) * p.nout + q] = make_double2(sx, sy);
+      }
+    }
+  };
+  save(0);
+  for (int step = 1; step <= p.nsteps; ++step) {
+    float z[M][2];
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < M; ++j) cfma(acc, D[i][j], make_float2(yh[j][0], yh[j][1]));
+      z[i][0] = acc.x;
+      z[i][1] = acc.y;
+    }
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      dd_add(yh[i][0], yl[i][0], z[i][0]);
+      dd_add(yh[i][1], yl[i][1], z[i][1]);
+    }
+    if (step % p.save_every == 0) save(step / p.save_every);
+  }
+  if (valid && p.status) {
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < M; ++i) ok = ok && isfinite(yh[i][0]) && isfinite(yh[i][1]);
+    if (!ok) atomicOr(p.status, QSX_ERR_NONFINITE);
+  }
+}
+
+// ------------------------------------------------------------- rows (ee)
+__host__ __device__ constexpr int rows_stride(int M) {
+  // float2 elements per sample slot: even (16-byte pairs) and == 2 mod 16 so
+  // the samples sharing a warp read from different bank quads.
+  int mp = (M % 2) ? M + 1 : M;
+  while (mp % 16 != 2) mp += 2;
+  return mp;
+}
+
+template <int M, int G, int MINB>
+__global__ void __launch_bounds__(256, MINB) rk4_rows_f32(Rk4P p, int64_t ngroups) {
+  constexpr int ST = rows_stride(M);
+  constexpr int MP = (M % 2) ? M + 1 : M;
+  __shared__ __align__(16) float2 ybuf[2][G][ST];
+  __shared__ double2 stash[2][G][M];
+  const int tid = threadIdx.x;
+  const int g = tid / M, r = tid % M;
+  const bool active = tid < G * M;
+  // zero the padding column once (pairs read up to MP - 1)
+  if (tid < G) {
+    for (int j = M; j < ST; ++j) {
+      ybuf[0][tid][j] = make_float2(0.f, 0.f);
+      ybuf[1][tid][j] = make_float2(0.f, 0.f);
+    }
+  }
+  int savecount = 0;
+  for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const bool first = grp == blockIdx.x;
+    const int64_t s = grp * G + g;
+    const bool valid = active && s < p.batch;
+    float2 drow[M];
+    const float2* dm = (const float2*)p.matrix + (valid ? s * p.matrix_stride + (int64_t)r * M : 0);
+#pragma unroll
+    for (int j = 0; j < M; ++j) drow[j] = valid ? dm[j] : make_float2(0.f, 0.f);
+    float yhx = 0.f, yhy = 0.f, ylx = 0.f, yly = 0.f;
+    if (valid) {
+      double2 v = p.y0[s * p.y0_stride + r];
+      yhx = (float)v.x;
+      yhy = (float)v.y;
+      ylx = (float)(v.x - (double)yhx);
+      yly = (float)(v.y - (double)yhy);
+    }
+    if (active) ybuf[0][g][r] = make_float2(yhx, yhy);
+    __syncthreads();
+    auto save = [&](int k, int par) {
+      if (!active) return;
+      if (p.out_state && valid)
+        p.out_state[(s * p.nsave + k) * M + r] =
+            make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
+      for (int q = 0; q < p.nout; ++q) {
+        if (p.select[q] == r) {
+          double2 v = valid ? make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly)
+                            : make_double2(0.0, 0.0);
+          if (p.out_proj && valid) p.out_proj[(s * p.nsave + k) * p.nout + q] = v;
+          if (p.partial) stash[par][g][q] = v;
+        }
+      }
+    };
+    auto reduce = [&](int k, int par) {
+      if (!p.partial) return;
+      for (int q = tid; q < p.nout; q += blockDim.x) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int gg = 0; gg < G; ++gg) acc = cadd(acc, stash[par][gg][q]);
+        double2* dst = p.partial + ((int64_t)blockIdx.x * p.nsave + k) * p.nout + q;
+        *dst = first ? acc : cadd(*dst, acc);
+      }
+    };
+    save(0, savecount & 1);
+    __syncthreads();
+    reduce(0, savecount & 1);
+    ++savecount;
+    for (int step = 1; step <= p.nsteps; ++step) {
+      const float2* cur = ybuf[(step - 1) & 1][active ? g : 0];
+      float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < MP; j += 2) {
+        const float4 v = *reinterpret_cast<const float4*>(&cur[j]);
+        cfma(a0, drow[j], make_float2(v.x, v.y));
+        if (j + 1 < M) cfma(a1, drow[j + 1], make_float2(v.z, v.w));
+      }
+      dd_add(yhx, ylx, a0.x + a1.x);
+      dd_add(yhy, yly, a0.y + a1.y);
+      if (active) ybuf[step & 1][g][r] = make_float2(yhx, yhy);
+      const bool sv = (step % p.save_every) == 0;
+      if (sv) save(step / p.save_every, savecount & 1);
+      __syncthreads();
+      if (sv) {
+        reduce(step / p.save_every, savecount & 1);
+        ++savecount;
+      }
+    }
+    if (valid && p.status && !(isfinite(yhx) && isfinite(yhy))) atomicOr(p.status, QSX_ERR_NONFINITE);
+    __syncthreads();
+  }
+}
+
+// -------------------------------------------------------------- generic
+constexpr int GEN_MAXR = 4;  // rows per thread (M <= 4 * 1024)
+
+template <typename T>
+__global__ void __launch_bounds__(1024) rk4_generic(Rk4P p, int mat_in_smem) {
+  using C = typename cplx<T>::type;
+  constexpr bool SPLIT = sizeof(T) == 4;
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int M = p.m;
+  double2* red = (double2*)sm;      // [32] block reduction (16-byte aligned first)
+  C* ybuf = (C*)(red + 32);         // [2][M] current state (hi) / stage input
+  C* smat = ybuf + 2 * M;           // [M][M] when it fits
+  const int64_t s = blockIdx.x;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const C* gm = (const C*)p.matrix + s * p.matrix_stride;
+  const C* mat = mat_in_smem ? smat : gm;
+  if (mat_in_smem)
+    for (int64_t e = tid; e < (int64_t)M * M; e += nt) smat[e] = gm[e];
+  // per-row state in registers: y (hi, lo for FP32) and the stage accumulator
+  C yh[GEN_MAXR], yl[GEN_MAXR], kac[GEN_MAXR];
+#pragma unroll
+  for (int k = 0; k < GEN_MAXR; ++k) {
+    int r = tid + k * nt;
+    double2 v = r < M ? p.y0[s * p.y0_stride + r] : make_double2(0.0, 0.0);
+    yh[k] = cmk((T)v.x, (T)v.y);
+    yl[k] = SPLIT ? cmk((T)(v.x - (double)yh[k].x), (T)(v.y - (double)yh[k].y)) : cmk((T)0, (T)0);
+    kac[k] = cmk((T)0, (T)0);
+    if (r < M) ybuf[r] = yh[k];
+  }
+  __syncthreads();
+  const double2* W = p.proj + (p.nproj ? s * p.proj_stride : 0);
+  auto save = [&](int k, const C* ycur) {
+    if (p.out_state) {
+#pragma unroll
+      for (int q = 0; q < GEN_MAXR; ++q) {
+        int r = tid + q * nt;
+        if (r < M)
+          p.out_state[(s * p.nsave + k) * M + r] =
+              make_double2((double)yh[q].x + (double)yl[q].x, (double)yh[q].y + (double)yl[q].y);
+      }
+    }
+    if (p.nselect) {
+      for (int q = tid; q < p.nselect; q += nt) {
+        const int si = p.select[q];
+        if (si < 0 || si >= M) {  // bad index table: record it, touch nothing
+          if (p.status) atomicOr(p.status, QSX_ERR_INVALID_ARG);
+          continue;
+        }
+        C v = ycur[si];
+        double2 dv = make_double2((double)v.x, (double)v.y);
+        if (p.out_proj) p.out_proj[(s * p.nsave + k) * p.nout + q] = dv;
+        if (p.partial) p.partial[(s * p.nsave + k) * p.nout + q] = dv;
+      }
+    }
+    for (int q = 0; q < p.nproj; ++q) {
+      double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int k2 = 0; k2 < GEN_MAXR; ++k2) {
+        int r = tid + k2 * nt;
+        if (r < M) {
+          double2 yv = make_double2((double)yh[k2].x + (double)yl[k2].x,
+                                    (double)yh[k2].y + (double)yl[k2].y);
+          cfma(acc, W[(int64_t)q * M + r], yv);
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      }
+      if ((tid & 31) == 0) red[tid >> 5] = acc;
+      __syncthreads();
+      if (tid == 0) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int w = 0; w < (nt + 31) / 32; ++w) t = cadd(t, red[w]);
+        if (p.out_proj) p.out_proj[(s * p.nsave + k) * p.nout + q] = t;
+        if (p.partial) p.partial[(s * p.nsave + k) * p.nout + q] = t;
+      }
+      __syncthreads();
+    }
+  };
+  // y_out = mat * x for this thread's rows
+  auto matvec = [&](const C* x, C* out) {
+#pragma unroll
+    for (int q = 0; q < GEN_MAXR; ++q) {
+      int r = tid + q * nt;
+      C acc = cmk((T)0, (T)0);
+      if (r < M) {
+        const C* row = mat + (int64_t)r * M;
+        for (int j = 0; j < M; ++j) cfma(acc, row[j], x[j]);
+      }
+      out[q] = acc;
+    }
+  };
+  auto add_state = [&](int q, C z) {
+    if (SPLIT) {
+      float hx = yh[q].x, lx = yl[q].x, hy = yh[q].y, ly = yl[q].y;
+      dd_add(hx, lx, (float)z.x);
+      dd_add(hy, ly, (float)z.y);
+      yh[q] = cmk((T)hx, (T)hy);
+      yl[q] = cmk((T)lx, (T)ly);
+    } else {
+      yh[q] = cmk(yh[q].x + z.x, yh[q].y + z.y);
+    }
+  };
+  save(0, ybuf);
+  __syncthreads();
+  const T h = (T)p.h;
+  // Invariant at the start of a step: ybuf[cur] holds the state (hi part).
+  int cur = 0;
+  for (int step = 1; step <= p.nsteps; ++step) {
+    C* b0 = ybuf + cur * M;
+    C* b1 = ybuf + (1 - cur) * M;
+    C z[GEN_MAXR];
+    if (p.form == 0) {
+      // propagator form: y <- y + D y
+      matvec(b0, z);
+#pragma unroll
+      for (int q = 0; q < GEN_MAXR; ++q) {
+        int r = tid + q * nt;
+        if (r < M) {
+          add_state(q, z[q]);
+          b1[r] = yh[q];
+        }
+      }
+      __syncthreads();
+      cur = 1 - cur;
+    } else {
+      // classical RK4 stages: inputs alternate b0 -> b1 -> b0 -> b1, new y -> b0
+      const T half = h / (T)2;
+#pragma unroll 1
+      for (int st = 0; st < 4; ++st) {
+        const C* in = (st & 1) ? b1 : b0;
+        C* outb = (st & 1) ? b0 : b1;
+        matvec(in, z);
+#pragma unroll
+        for (int q = 0; q < GEN_MAXR; ++q) {
+          int r = tid + q * nt;
+          if (r >= M) continue;
+          if (st == 0) {
+            kac[q] = z[q];
+            outb[r] = cmk(yh[q].x + half * z[q].x, yh[q].y + half * z[q].y);
+          } else if (st == 1) {
+            kac[q] = cmk(kac[q].x + (T)2 * z[q].x, kac[q].y + (T)2 * z[q].y);
+            outb[r] = cmk(yh[q].x + half * z[q].x, yh[q].y + half * z[q].y);
+          } else if (st == 2) {
+            kac[q] = cmk(kac[q].x + (T)2 * z[q].x, kac[q].y + (T)2 * z[q].y);
+            outb[r] = cmk(yh[q].x + h * z[q].x, yh[q].y + h * z[q].y);
+          } else {
+            C inc = cmk((kac[q].x + z[q].x) * (h / (T)6), (kac[q].y + z[q].y) * (h / (T)6));
+            add_state(q, inc);
+            outb[r] = yh[q];
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (step % p.save_every == 0) save(step / p.save_every, ybuf + cur * M);
+    __syncthreads();
+  }
+  if (p.status) {
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < GEN_MAXR; ++q)
+      if (tid + q * nt < M) ok = ok && isfinite((double)yh[q].x) && isfinite((double)yh[q].y);
+    if (!ok) atomicOr(p.status, QSX_ERR_NONFINITE);
+  }
+}
+
+// ----------------------------------------------------------------- reduce
+__global__ void rk4_reduce_kernel(const double2* __restrict__ partial, int64_t nslots,
+                                  int64_t per, double scale, double2* out) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= per) return;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int64_t sl = 0; sl < nslots; ++sl) acc = cadd(acc, partial[sl * per + e]);
+  out[e] = cscale(acc, scale);
+}
+
+// ------------------------------------------------------------------ plan
+enum Kind { K_SMALL = 0, K_ROWS = 1, K_GENERIC = 2 };
+
+struct Plan {
+  Kind kind;
+  int64_t nslots;
+  int64_t grid;
+  int threads;
+  size_t smem;
+  int mat_in_smem;
+  int64_t ngroups;
+};
+
+template <int M, int G, int MINB>
+static cudaError_t rows_occupancy(int* blocks) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, rk4_rows_f32<M, G, MINB>, 256, 0);
+}
+
+#define QSX_ROWS_TABLE(X) X(9, 28, 2) X(16, 16, 2) X(25, 10, 2) X(36, 7, 2) X(49, 5, 2) X(64, 4, 1)
+
+static bool rows_supported(int m, int* G) {
+#define X(MM, GG, BB) if (m == MM) { *G = GG; return true; }
+  QSX_ROWS_TABLE(X)
+#undef X
+  return false;
+}
+
+static int validate(const qsx_rk4_args* a) {
+  QSX_CHECK_ARG(a != nullptr, "qsx_rk4: null args");
+  QSX_CHECK_ARG(a->precision == QSX_FP32 || a->precision == QSX_FP64, "qsx_rk4: bad precision");
+  QSX_CHECK_ARG(a->form == 0 || a->form == 1, "qsx_rk4: form must be 0 (propagator) or 1 (stages)");
+  QSX_CHECK_ARG(a->m >= 1 && a->m <= GEN_MAXR * 1024, "qsx_rk4: need 1 <= m <= %d (got %d)",
+                GEN_MAXR * 1024, a->m);
+  QSX_CHECK_ARG(a->nsteps >= 0 && a->save_every >= 1 && a->nsteps % a->save_every == 0,
+                "qsx_rk4: nsteps must be a non-negative multiple of save_every");
+  QSX_CHECK_ARG(a->batch >= 0 && a->batch <= 0x7fffffffLL, "qsx_rk4: bad batch");
+  QSX_CHECK_ARG(!(a->nproj > 0 && a->nselect > 0), "qsx_rk4: use proj or select, not both");
+  QSX_CHECK_ARG(a->nproj >= 0 && a->nproj <= 64 && a->nselect >= 0 && a->nselect <= a->m,
+                "qsx_rk4: bad nproj/nselect");
+  QSX_CHECK_ARG(a->nproj == 0 || a->proj, "qsx_rk4: proj is null");
+  QSX_CHECK_ARG(a->nselect == 0 || a->select, "qsx_rk4: select is null");
+  QSX_CHECK_ARG((a->out_proj == nullptr && a->out_mean == nullptr) || a->nproj + a->nselect > 0,
+                "qsx_rk4: projections requested without proj/select");
+  QSX_CHECK_ARG(a->batch == 0 || (a->matrix && a->y0), "qsx_rk4: null matrix or y0");
+  return QSX_OK;
+}
+
+static int make_plan(const qsx_rk4_args* a, Plan* pl) {
+  int G = 0;
+  const int m = a->m;
+  const int64_t nsave = a->nsteps / a->save_every + 1;
+  (void)nsave;
+  if (a->precision == QSX_FP32 && a->form == 0 && m <= 8) {
+    pl->kind = K_SMALL;
+    pl->threads = 128;
+    pl->grid = (a->batch + 127) / 128;
+    pl->nslots = pl->grid * 4;
+    pl->smem = 0;
+    return QSX_OK;
+  }
+  if (a->precision == QSX_FP32 && a->form == 0 && rows_supported(m, &G)) {
+    // nselect-only outputs (the per-row kernel has no dense projection)
+    if (a->nproj == 0) {
+      int dev = 0, sms = 0, occ = 0;
+      cudaError_t e = cudaGetDevice(&dev);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+#define X(MM, GG, BB) \
+  if (e == cudaSuccess && m == MM) e = rows_occupancy<MM, GG, BB>(&occ);
+      QSX_ROWS_TABLE(X)
+#undef X
+      if (e != cudaSuccess) return cuda_status(e, "qsx_rk4 plan");
+      pl->kind = K_ROWS;
+      pl->threads = 256;
+      pl->ngroups = (a->batch + G - 1) / G;
+      pl->grid = std::max<int64_t>(1, std::min<int64_t>(pl->ngroups, (int64_t)sms * std::max(occ, 1)));
+      pl->nslots = pl->grid;
+      pl->smem = 0;
+      return QSX_OK;
+    }
+  }
+  pl->kind = K_GENERIC;
+  int nt = ((std::min(m, 1024) + 31) / 32) * 32;
+  QSX_CHECK_ARG((m + nt - 1) / nt <= GEN_MAXR, "qsx_rk4: m too large");
+  pl->threads = nt;
+  pl->grid = a->batch;
+  pl->nslots = a->batch;
+  size_t cs = a->precision == QSX_FP32 ? sizeof(float2) : sizeof(double2);
+  size_t base = 2 * (size_t)m * cs + 32 * sizeof(double2);
+  size_t mat = (size_t)m * m * cs;
+  pl->mat_in_smem = (base + mat) <= 160 * 1024;
+  pl->smem = base + (pl->mat_in_smem ? mat : 0);
+  return QSX_OK;
+}
+
+}  // namespace qsx
+
+using namespace qsx;
+
+extern "C" {
+
+size_t qsx_rk4_args_bytes(void) { return sizeof(qsx_rk4_args); }
+
+int qsx_rk4_workspace_bytes(const qsx_rk4_args* a, size_t* bytes) {
+  int st = validate(a);
+  if (st) return st;
+  QSX_CHECK_ARG(bytes != nullptr, "qsx_rk4_workspace_bytes: null output");
+  *bytes = 0;
+  if (a->out_mean == nullptr || a->batch == 0) return QSX_OK;
+  Plan pl;
+  st = make_plan(a, &pl);
+  if (st) return st;
+  const int64_t nsave = a->nsteps / a->save_every + 1;
+  const int64_t nout = a->nproj > 0 ? a->nproj : a->nselect;
+  *bytes = (size_t)pl.nslots * nsave * nout * sizeof(double2);
+  return QSX_OK;
+}
+
+int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
+  int st = validate(a);
+  if (st) return st;
+  if (a->batch == 0) return QSX_OK;
+  Plan pl;
+  st = make_plan(a, &pl);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  Rk4P p;
+  p.m = a->m;
+  p.nsteps = a->nsteps;
+  p.save_every = a->save_every;
+  p.nsave = a->nsteps / a->save_every + 1;
+  p.nproj = a->nproj;
+  p.nselect = a->nselect;
+  p.nout = a->nproj > 0 ? a->nproj : a->nselect;
+  p.form = a->form;
+  p.batch = a->batch;
+  p.matrix = a->matrix;
+  p.matrix_stride = a->matrix_stride;
+  p.h = a->h;
+  p.y0 = (const double2*)a->y0;
+  p.y0_stride = a->y0_stride;
+  p.proj = (const double2*)a->proj;
+  p.proj_stride = a->proj_stride;
+  p.select = a->select;
+  p.out_state = (double2*)a->out_state;
+  p.out_proj = (double2*)a->out_proj;
+  p.partial = nullptr;
+  p.status = a->status;
+  const int64_t per = (int64_t)p.nsave * p.nout;
+  if (a->out_mean) {
+    size_t need = (size_t)pl.nslots * per * sizeof(double2);
+    QSX_CHECK_ARG(a->workspace && a->workspace_bytes >= need,
+                  "qsx_rk4_batched: workspace of %zu bytes needed (got %zu)", need,
+                  a->workspace_bytes);
+    p.partial = (double2*)a->workspace;
+  }
+  switch (pl.kind) {
+    case K_SMALL: {
+      switch (a->m) {
+#define S(MM) case MM: rk4_small_f32<MM><<<(unsigned)pl.grid, pl.threads, 0, s>>>(p); break;
+        S(1) S(2) S(3) S(4) S(5) S(6) S(7) S(8)
+#undef S
+      }
+      break;
+    }
+    case K_ROWS: {
+#define X(MM, GG, BB) \
+  if (a->m == MM) rk4_rows_f32<MM, GG, BB><<<(unsigned)pl.grid, 256, 0, s>>>(p, pl.ngroups);
+      QSX_ROWS_TABLE(X)
+#undef X
+      break;
+    }
+    case K_GENERIC: {
+      cudaError_t e;
+      if (a->precision == QSX_FP32) {
+        e = cudaFuncSetAttribute(rk4_generic<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)pl.smem);
+        if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_batched");
+        rk4_generic<float><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(p, pl.mat_in_smem);
+      } else {
+        e = cudaFuncSetAttribute(rk4_generic<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)pl.smem);
+        if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_batched");
+        rk4_generic<double><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(p, pl.mat_in_smem);
+      }
+      break;
+    }
+  }
+  QSX_LAUNCH_CHECK("qsx_rk4_batched");
+  if (a->out_mean) {
+    rk4_reduce_kernel<<<(unsigned)((per + 255) / 256), 256, 0, s>>>(
+        p.partial, pl.nslots, per, a->mean_scale, (double2*)a->out_mean);
+    QSX_LAUNCH_CHECK("qsx_rk4_batched reduce");
+  }
+  return QSX_OK;
+}
+
+}  // extern "C"

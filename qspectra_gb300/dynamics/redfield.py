@@ -1,0 +1,122 @@
+"""Redfield theory on the GPU (qspectra/dynamics/redfield.py).
+
+``RedfieldModel`` keeps the reference constructor and API.  Its generator is
+built per disorder sample on the GPU in FP64: Jacobi eigensolve of the
+rotating-frame Hamiltonian (qsx_eigh_batched), Debye correlation function and
+operator-form Redfield tensor (qsx_redfield_operators_batched), then the
+requested dense Liouville block (qsx_redfield_liouvillian_batched).
+``RedfieldBuild`` does the same for a whole batch of samples at once and is
+what the ensemble drivers use.
+"""
+import numpy as np
+import torch
+
+from .. import _native
+from ..operator_tools import n_excitations
+from .liouville_space import LiouvilleSpaceModel
+
+EIGH_JACOBI_MAX = 32
+
+
+def manifold_bounds(n_sites, hilbert_subspace):
+    """[0, end_g, end_e, ...] block boundaries of the manifolds present."""
+    sizes = dict(zip('gef', n_excitations(n_sites)))
+    out = [0]
+    for letter in 'gef':
+        if letter in hilbert_subspace and sizes[letter] > 0:
+            out.append(out[-1] + int(sizes[letter]))
+    return out
+
+
+class RedfieldBuild:
+    """Batched FP64 Redfield generator for S disorder samples.
+
+    ``H`` is (S, n, n) float64 on the GPU: rotating-frame Hamiltonians on the
+    model's Hilbert subspace.  Eigen-decomposition and the operator form are
+    computed once; ``block`` then assembles any Liouville block.
+    """
+
+    def __init__(self, H, n_sites, hilbert_subspace, occ, bath, unit_convert,
+                 secular=False, discard_imag_corr=False, evolve_basis='site'):
+        self.H = H
+        self.n = H.shape[-1]
+        self.n_sites = n_sites
+        self.unit_convert = unit_convert
+        self.secular = secular
+        self.evolve_basis = evolve_basis
+        self.occ = torch.as_tensor(occ, dtype=torch.float64, device=H.device).contiguous()
+        bounds = manifold_bounds(n_sites, hilbert_subspace)
+        if self.n <= EIGH_JACOBI_MAX:
+            self.E, self.U = _native.eigh(H, bounds)
+        else:
+            raise _native.QsxError(
+                'Hilbert space of {} states exceeds the {}-state Redfield '
+                'build; use the operator-form third-order path'.format(
+                    self.n, EIGH_JACOBI_MAX))
+        self.site_ops = evolve_basis == 'site' and not secular
+        self.G, self.M, self.K = _native.redfield_operators(
+            self.E, self.U, self.occ, bath, unit_convert, discard_imag_corr,
+            site_basis=self.site_ops, matsubara_cutoff=bath.matsubara_cutoff)
+
+    def block(self, idx, transpose=False):
+        """(S, m, m) complex128 generator on the column-stacked indices ``idx``."""
+        idx_np = np.asarray(idx, dtype=np.int64)
+        idx_t = torch.as_tensor(idx_np, dtype=torch.int32, device=self.H.device)
+        uc = self.unit_convert
+        if self.site_ops:
+            return _native.redfield_liouvillian(self.H, self.G, self.M, idx_t, uc,
+                                                occ=self.occ, transpose=transpose)
+        Hd = torch.diag_embed(self.E).contiguous()
+        L = _native.redfield_liouvillian(Hd, self.G, self.M, idx_t, uc, K=self.K,
+                                         secular=self.secular)
+        if self.evolve_basis == 'site':
+            # (U ⊗ U) restricted to idx: U is block-diagonal over manifolds and
+            # idx is a union of Liouville blocks, so the restriction is exact.
+            n = self.n
+            a, b = idx_np % n, idx_np // n
+            ai = torch.as_tensor(a, device=self.H.device)
+            bi = torch.as_tensor(b, device=self.H.device)
+            U = self.U.to(torch.complex128)
+            W = U[:, ai][:, :, ai] * U[:, bi][:, :, bi]
+            L = W @ L @ W.transpose(-1, -2)
+        if transpose:
+            L = L.transpose(-1, -2)
+        return L.contiguous()
+
+
+class RedfieldModel(LiouvilleSpaceModel):
+    """Redfield dynamics, each site coupled to an identical independent bath
+    (redfield.py:107-152)."""
+
+    def __init__(self, hamiltonian, rw_freq=None, hilbert_subspace='gef',
+                 unit_convert=1, secular=True, discard_imag_corr=False,
+                 evolve_basis='site', sparse_matrix=False):
+        super().__init__(hamiltonian, rw_freq, hilbert_subspace, unit_convert,
+                         evolve_basis, sparse_matrix)
+        self.secular = secular
+        self.discard_imag_corr = discard_imag_corr
+
+    def __repr__(self):
+        return ('RedfieldModel(hilbert_subspace={!r}, unit_convert={!r}, '
+                'secular={!r}, discard_imag_corr={!r}, evolve_basis={!r})').format(
+            self.hilbert_subspace, self.unit_convert, self.secular,
+            self.discard_imag_corr, self.evolve_basis)
+
+    def build_batch(self, H):
+        """RedfieldBuild for a (S, n, n) batch of rotating-frame Hamiltonians."""
+        ham = self.hamiltonian
+        return RedfieldBuild(H, ham.n_sites, self.hilbert_subspace,
+                             ham.occupation_table(self.hilbert_subspace), ham.bath,
+                             self.unit_convert, self.secular, self.discard_imag_corr,
+                             self.evolve_basis)
+
+    def _build(self):
+        if 'build' not in self._cache:
+            _native.require_gpu()
+            H = torch.as_tensor(self.hamiltonian.H(self.hilbert_subspace),
+                                dtype=torch.float64).cuda()[None].contiguous()
+            self._cache['build'] = self.build_batch(H)
+        return self._cache['build']
+
+    def _block(self, idx, transpose):
+        return self._build().block(idx, transpose)[0]

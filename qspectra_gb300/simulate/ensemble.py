@@ -1,0 +1,223 @@
+"""Batched disorder ensembles on one GPU.
+
+The reference averages over static disorder with a serial Python loop, one
+full model rebuild and zvode solve per sample (decorators.py:40-64,
+hamiltonian.py:233-274).  Here every sample's rotating-frame Hamiltonian is
+built on the device, the Redfield generators for all samples are produced by
+one batched build, their RK4 propagators by one kernel, and the time loops of
+all samples run in one persistent kernel that also reduces the ensemble mean.
+"""
+import numpy as np
+import torch
+
+from .. import _native
+from ..dynamics.redfield import RedfieldModel
+from ..operator_tools import hilbert_subspace_index
+
+
+class SampleBatch:
+    """Disorder samples n = start .. start + size - 1 of a model's Hamiltonian.
+
+    ``offsets`` holds the diagonal site-energy shifts (the same RandomState
+    draws as ``sample(n)``); ``H(subspace)`` returns the (S, n, n) float64
+    rotating-frame Hamiltonians on the GPU.
+    """
+
+    def __init__(self, model, size, start=0, offsets=None):
+        self.model = model
+        self.size = int(size)
+        self.start = int(start)
+        ham = model.hamiltonian
+        if offsets is None:
+            offsets = ham.disorder_offsets(size, start)
+        self.offsets = torch.as_tensor(np.asarray(offsets, float),
+                                       dtype=torch.float64).cuda()
+
+    def H(self, subspace):
+        ham = self.model.hamiltonian
+        base = torch.as_tensor(ham.H(subspace), dtype=torch.float64).cuda()
+        n = base.shape[0]
+        H = base.expand(self.size, n, n).clone()
+        if 'e' in subspace:
+            sl = hilbert_subspace_index('e', subspace, ham.n_sites)
+            idx = torch.arange(sl.start, sl.stop, device=H.device)
+            H[:, idx, idx] += self.offsets
+        if 'f' in subspace:
+            sl = hilbert_subspace_index('f', subspace, ham.n_sites)
+            pairs = [(i, j) for i in range(ham.n_sites) for j in range(i + 1, ham.n_sites)]
+            ii = torch.as_tensor([p[0] for p in pairs], device=H.device)
+            jj = torch.as_tensor([p[1] for p in pairs], device=H.device)
+            idx = torch.arange(sl.start, sl.stop, device=H.device)
+            H[:, idx, idx] += self.offsets[:, ii] + self.offsets[:, jj]
+        return H.contiguous()
+
+
+def redfield_batch_build(model, batch):
+    if not isinstance(model, RedfieldModel):
+        raise NotImplementedError('batched ensembles need a RedfieldModel')
+    return model.build_batch(batch.H(model.hilbert_subspace))
+
+
+def ensemble_linear_signal(model, time_max, ensemble_size, polarization='xx',
+                           precision='fp32', path='gg->eg->gg', start=0,
+                           offsets=None, return_build=False):
+    """Disorder-averaged Heisenberg-picture linear response (response.py:15-43).
+
+    Returns (t, mean signal) with the signal on the GPU (complex128).
+    """
+    from .utils import PRECISIONS, step_plan
+    prec = PRECISIONS[precision]
+    subs = path.split('->')
+    dt = model.time_step
+    t = np.arange(0, time_max, dt)
+    batch = SampleBatch(model, ensemble_size, start, offsets)
+    build = redfield_batch_build(model, batch)
+    rho0 = model.thermal_state(subs[0])
+    total = None
+    for sim in subs[1].split(','):
+        V0 = model.dipole_operator('{}->{}'.format(subs[0], sim), polarization[0], '+')
+        V1 = model.dipole_operator('{}->{}'.format(sim, subs[2]), polarization[1], '-')
+        v_rho0 = V0.commutator(rho0)
+        LT = build.block(model.liouville_subspace_index(sim), transpose=True)
+        D = _native.rk4_propagator(LT, dt, prec)
+        y0 = torch.as_tensor(-V1.bra_vector, dtype=torch.complex128).cuda()
+        proj = torch.as_tensor(np.asarray(v_rho0)[None, :], dtype=torch.complex128).cuda()
+        steps = step_plan(t, 0.0, dt)
+        out = _native.rk4(D, y0, int(steps[-1]), 1,
+                          proj=proj, per_sample=False, mean=True, check_finite=False)
+        sig = out['mean'][:, 0]
+        total = sig if total is None else total + sig
+        if int(out['status'].item()) & _native.QSX_ERR_NONFINITE:
+            raise _native.IntegratorError('non-finite state in ensemble propagation')
+    if return_build:
+        return t, total, build
+    return t, total
+
+
+def ensemble_populations(model, initial_state, duration, ensemble_size,
+                         liouville_subspace='ee', precision='fp32', full_state=False,
+                         start=0, offsets=None):
+    """Disorder-averaged density matrices or populations (eom.py:11-26).
+
+    Returns (t, mean) with mean (T, M) complex128 on the GPU over the
+    selected components (all M when full_state, else the diagonal).
+    """
+    from .utils import PRECISIONS
+    prec = PRECISIONS[precision]
+    dt = model.time_step
+    t = np.arange(0, duration, dt)
+    batch = SampleBatch(model, ensemble_size, start, offsets)
+    build = redfield_batch_build(model, batch)
+    rho0 = np.asarray(initial_state)
+    if rho0.ndim == 1:
+        rho0 = np.outer(rho0.conj(), rho0)
+    y0 = model.density_matrix_to_state_vector(rho0, liouville_subspace)
+    idx = model.liouville_subspace_index(liouville_subspace)
+    L = build.block(idx, transpose=False)
+    D = _native.rk4_propagator(L, dt, prec)
+    M = len(idx)
+    if full_state:
+        select = list(range(M))
+    else:
+        nn = int(round(np.sqrt(M)))
+        select = [i * nn + i for i in range(nn)]
+    y0t = torch.as_tensor(y0, dtype=torch.complex128).cuda()
+    out = _native.rk4(D, y0t, len(t) - 1, 1,
+                      select=select, per_sample=False, mean=True, check_finite=False)
+    if int(out['status'].item()) & _native.QSX_ERR_NONFINITE:
+        raise _native.IntegratorError('non-finite state in ensemble propagation')
+    return t, out['mean']
+
+
+class RedfieldEnsembleWorkload:
+    """Disorder-averaged absorption spectrum plus population dynamics.
+
+    The batched form of ``absorption_spectra(model, absorption_time,
+    ensemble_size=S)`` together with ``simulate_dynamics(model,
+    initial_state, dynamics_time, ensemble_size=S)`` (response.py:103-154,
+    eom.py:29-74, decorators.py:40-64).  Everything that does not depend on
+    the disorder draws (dipole vectors, subspace indices, frequency grid) is
+    prepared once; ``run`` takes the (S, n_sites) site-energy offsets and
+    does the whole pipeline on the GPU:
+
+      H_s -> Jacobi eigensolve -> Redfield operators -> L_eg^T, L_ee
+          -> RK4 propagators -> batched RK4 + ensemble means -> DFT.
+    """
+
+    def __init__(self, model, absorption_time, dynamics_time, initial_state,
+                 polarization='xx', freqs=None):
+        if not isinstance(model, RedfieldModel) or model.hilbert_subspace != 'ge':
+            raise NotImplementedError("the workload runs a RedfieldModel on 'ge'")
+        from .utils import fft_frequencies
+        self.model = model
+        ham = model.hamiltonian
+        self.n_sites = ham.n_sites
+        self.dt = model.time_step
+        self.t_abs = np.arange(0, absorption_time, self.dt)
+        self.t_dyn = np.arange(0, dynamics_time, self.dt)
+        dev = torch.device('cuda', torch.cuda.current_device())
+        self.H_base = torch.as_tensor(ham.H('ge'), dtype=torch.float64, device=dev)
+        self.e_idx = torch.arange(1, 1 + self.n_sites, device=dev)
+        self.idx_eg = model.liouville_subspace_index('eg')
+        self.idx_ee = model.liouville_subspace_index('ee')
+        rho0 = model.thermal_state('gg')
+        V0 = model.dipole_operator('gg->eg', polarization[0], '+')
+        V1 = model.dipole_operator('eg->gg', polarization[1], '-')
+        self.proj = torch.as_tensor(np.asarray(V0.commutator(rho0))[None, :],
+                                    dtype=torch.complex128, device=dev)
+        self.y_abs = torch.as_tensor(-V1.bra_vector, dtype=torch.complex128, device=dev)
+        rho = np.asarray(initial_state)
+        if rho.ndim == 1:
+            rho = np.outer(rho.conj(), rho)
+        self.y_dyn = torch.as_tensor(model.density_matrix_to_state_vector(rho, 'ee'),
+                                     dtype=torch.complex128, device=dev)
+        self.select = [i * self.n_sites + i for i in range(self.n_sites)]
+        self.freqs_np = (fft_frequencies(self.t_abs, model.rw_freq, model.unit_convert)
+                         if freqs is None else np.asarray(freqs, float))
+        self.freqs = torch.as_tensor(self.freqs_np, device=dev)
+        from .utils import symmetric_grid
+        t_sym, _ = symmetric_grid(self.t_abs)
+        self.dft_t0 = self.t_abs[0] - t_sym[t_sym.size // 2]
+
+    def run(self, offsets, precision='fp32', events=None):
+        """(spectrum (F,) float64, populations (T, n_sites) float64) on the GPU.
+
+        ``offsets`` is a (S, n_sites) float64 CUDA tensor.  ``events`` (a dict)
+        collects CUDA events around the population propagation.
+        """
+        from .utils import PRECISIONS
+        prec = PRECISIONS[precision]
+        S = offsets.shape[0]
+        H = self.H_base.expand(S, -1, -1).clone()
+        H[:, self.e_idx, self.e_idx] += offsets
+        build = self.model.build_batch(H)
+        LT = build.block(self.idx_eg, transpose=True)
+        D_eg = _native.rk4_propagator(LT, self.dt, prec)
+        sig = _native.rk4(D_eg, self.y_abs, len(self.t_abs) - 1, 1, proj=self.proj,
+                          per_sample=False, mean=True, check_finite=False)
+        X = _native.dft(-sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
+                        self.model.rw_freq, self.model.unit_convert, 1)
+        L = build.block(self.idx_ee)
+        D_ee = _native.rk4_propagator(L, self.dt, prec)
+        if events is not None:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+        pop = _native.rk4(D_ee, self.y_dyn, len(self.t_dyn) - 1, 1, select=self.select,
+                          per_sample=False, mean=True, check_finite=False)
+        if events is not None:
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record()
+            events.setdefault('dyn', []).append((e0, e1))
+        status = sig['status'] | pop['status']
+        return X.real, pop['mean'].real, status
+
+    def run_host(self, offsets_host, precision='fp32'):
+        """End-to-end call with host buffers: pinned offsets in, numpy out."""
+        dev = self.H_base.device
+        off = offsets_host.to(dev, non_blocking=True)
+        X, pops, status = self.run(off, precision)
+        out = torch.cat([X, pops.reshape(-1), status.to(torch.float64)]).to('cpu')
+        n = X.numel()
+        if int(out[-1].item()) & _native.QSX_ERR_NONFINITE:
+            raise _native.IntegratorError('non-finite state in ensemble propagation')
+        return out[:n].numpy(), out[n:-1].numpy().reshape(pops.shape)

@@ -1,0 +1,211 @@
+"""Response-function spectra (qspectra/simulate/response.py).
+
+Same signatures as the reference plus ``precision`` ('fp64' default, 'fp32'
+for the batched split-word form).  ``ensemble_size`` runs the disorder
+average as one batched GPU pipeline instead of a serial loop.
+"""
+import numpy as np
+import torch
+
+from ..polarization import check_polarizations
+from .ensemble import ensemble_linear_signal
+from .utils import fourier_transform, integrate
+
+PUMP_PROBE_PATHWAYS = {'GSB': 'gg->eg->gg',
+                       'ESE': 'ee->eg->gg',
+                       'ESA': 'ee->fe->ee'}
+
+# Liouville pathways of Abramavicius et al., Chem. Rev. 109, 2350 (2009),
+# Figs. 4-6 (the same table as response.py:252-264).
+THIRD_ORDER_PATHWAYS = {
+    '-++': {'ESE': 'gg->ge->ee->eg->gg',
+            'GSB': 'gg->ge->gg->eg->gg',
+            'ESA': 'gg->ge->ee->fe->ee'},
+    '+-+': {'ESE': 'gg->eg->ee->eg->gg',
+            'GSB': 'gg->eg->gg->eg->gg',
+            'ESA': 'gg->eg->ee->fe->ee'},
+    '++-': {'ESA1': 'gg->eg->fg->fe->ee',
+            'ESA2': 'gg->eg->fg->eg->gg'},
+}
+
+
+def _parse_pathways(possible, include_signal):
+    sel = [v for k, v in possible.items() if include_signal is None or k in include_signal]
+    if not sel:
+        raise ValueError('at least one Liouville space pathway must be selected, '
+                         'i.e., include_signal must include at least one of %r'
+                         % list(possible.keys()))
+    return sel
+
+
+def _single_linear_response(model, liouv_space_path, time_max, initial_state,
+                            polarization, precision, **kw):
+    """response.py:15-43 for one model (Heisenberg picture when available)."""
+    subs = liouv_space_path.split('->')
+    if initial_state is None:
+        initial_state = model.thermal_state(subs[0])
+    t = np.arange(0, time_max, model.time_step)
+    signal = 0
+    for sim in subs[1].split(','):
+        V = [model.dipole_operator('{}->{}'.format(a, b), p, tr)
+             for a, b, p, tr in zip(subs[:-1], subs[1:], polarization, '+-')]
+        v_rho0 = V[0].commutator(np.asarray(initial_state))
+        try:
+            eom = model.equation_of_motion(sim, heisenberg_picture=True)
+        except NotImplementedError:
+            eom = model.equation_of_motion(sim)
+            signal = signal - integrate(eom, v_rho0, t, save_func=V[1].expectation_value,
+                                        precision=precision, **kw)
+        else:
+            v_gt = integrate(eom, -V[1].bra_vector, t, precision=precision, **kw)
+            signal = signal + np.tensordot(v_rho0, v_gt, (-1, -1))
+    return t, signal
+
+
+def _isotropic(fn, polarization, order=2):
+    pols = check_polarizations(polarization, order)
+    weight = np.dot(*pols)
+    total = 0
+    t = None
+    for p in ['xx', 'yy', 'zz']:
+        t, s = fn(p)
+        total = total + s
+    return t, total * weight / 3.0
+
+
+def linear_response(dynamical_model, liouv_space_path, time_max,
+                    initial_state=None, polarization='xx', ensemble_size=None,
+                    ensemble_random_orientations=False,
+                    exact_isotropic_average=False, precision='fp64',
+                    **integrate_kwargs):
+    """Linear response function under the RWA (response.py:46-100)."""
+    if ensemble_random_orientations:
+        raise NotImplementedError('random ensemble orientations are not on the '
+                                  'accelerated path')
+
+    def one(pol):
+        if ensemble_size is not None:
+            if initial_state is not None:
+                raise NotImplementedError('ensemble runs start from the thermal state')
+            t, sig = ensemble_linear_signal(dynamical_model, time_max, ensemble_size,
+                                            pol, precision, path=liouv_space_path)
+            return t, sig.cpu().numpy()
+        return _single_linear_response(dynamical_model, liouv_space_path, time_max,
+                                       initial_state, pol, precision,
+                                       **integrate_kwargs)
+
+    if exact_isotropic_average:
+        return _isotropic(one, polarization)
+    return one(polarization)
+
+
+def absorption_spectra(dynamical_model, time_max, correlation_decay_time=None,
+                       polarization='xx', ensemble_size=None,
+                       ensemble_random_orientations=False,
+                       exact_isotropic_average=False, precision='fp64',
+                       freqs=None, **integrate_kwargs):
+    """Absorption spectrum (response.py:103-154); ``freqs`` picks a custom grid."""
+    t, x = linear_response(dynamical_model, 'gg->eg->gg', time_max,
+                           polarization=polarization, ensemble_size=ensemble_size,
+                           ensemble_random_orientations=ensemble_random_orientations,
+                           exact_isotropic_average=exact_isotropic_average,
+                           precision=precision, **integrate_kwargs)
+    if correlation_decay_time is not None:
+        x = x * np.exp(-t / correlation_decay_time)
+    f, X = fourier_transform(t, -x, rw_freq=dynamical_model.rw_freq,
+                             unit_convert=dynamical_model.unit_convert, freqs=freqs)
+    return f, X.real
+
+
+def impulsive_probe(dynamical_model, state, time_max, polarization='xx',
+                    initial_liouv_subspace='gg,ge,eg,ee',
+                    include_signal='GSB,ESE,ESA', precision='fp64',
+                    **integrate_kwargs):
+    """Impulsive probe of a 2nd-order state (response.py:174-244)."""
+    init = np.asarray(state) - dynamical_model.thermal_state(initial_liouv_subspace)
+    total = 0
+    t = None
+    for path in _parse_pathways(PUMP_PROBE_PATHWAYS, include_signal):
+        first = path.split('->')[0]
+        portion = np.apply_along_axis(
+            lambda s: dynamical_model.map_between_subspaces(s, initial_liouv_subspace, first),
+            -1, init)
+        t, sig = _single_linear_response(dynamical_model, path, time_max, portion,
+                                         polarization, precision, **integrate_kwargs)
+        total = total + sig
+    return fourier_transform(t, total, rw_freq=dynamical_model.rw_freq,
+                             unit_convert=dynamical_model.unit_convert)
+
+
+def _single_third_order(model, coherence_time_max, population_time_max,
+                        population_times, geometry, polarization, include_signal,
+                        precision, **kw):
+    """Sum over Liouville pathways, Heisenberg picture for t3 (response.py:267-337)."""
+    dt = model.time_step
+    t1 = np.arange(0, coherence_time_max, dt)
+    t2 = (np.arange(0, population_time_max, dt) if population_times is None
+          else np.asarray(population_times, float))
+    t3 = np.arange(0, coherence_time_max, dt)
+    rho0 = model.thermal_state('gg')
+    total = 0
+    for path in _parse_pathways(THIRD_ORDER_PATHWAYS[geometry], include_signal):
+        subs = path.split('->')
+        V = [model.dipole_operator('{}->{}'.format(a, b), p, tr)
+             for a, b, p, tr in zip(subs[:-1], subs[1:], polarization, geometry + '-')]
+        eom = [model.equation_of_motion(s) for s in subs[1:-1]]
+        v_rho0 = V[0].commutator(rho0)
+        v_rho1 = integrate(eom[0], v_rho0, t1, save_func=V[1].commutator,
+                           precision=precision, step=dt, **kw)
+        v_rho2 = integrate(eom[1], v_rho1, t2, t0=0, save_func=V[2].commutator,
+                           precision=precision, step=dt, **kw)
+        try:
+            eom_h = model.equation_of_motion(subs[3], heisenberg_picture=True)
+        except NotImplementedError:
+            total = total + integrate(eom[2], v_rho2, t3, save_func=V[3].expectation_value,
+                                      precision=precision, step=dt, **kw)
+        else:
+            v_gt3 = integrate(eom_h, V[3].bra_vector, t3, precision=precision, step=dt, **kw)
+            total = total + np.einsum('ci,abi', v_gt3, v_rho2)
+    return (t1, t2, t3), total
+
+
+def third_order_response(dynamical_model, coherence_time_max,
+                         population_time_max=None, population_times=None,
+                         geometry='-++', polarization='xxxx', include_signal=None,
+                         ensemble_size=None, ensemble_random_orientations=False,
+                         exact_isotropic_average=False, precision='fp64',
+                         **integrate_kwargs):
+    """Third-order response function under the RWA (response.py:340-427)."""
+    if exact_isotropic_average or ensemble_random_orientations:
+        raise NotImplementedError('isotropic averaging is not on the accelerated path')
+    if ensemble_size is None:
+        return _single_third_order(dynamical_model, coherence_time_max,
+                                   population_time_max, population_times, geometry,
+                                   polarization, include_signal, precision,
+                                   **integrate_kwargs)
+    total = 0
+    ticks = None
+    for m in dynamical_model.sample_ensemble(ensemble_size):
+        ticks, s = _single_third_order(m, coherence_time_max, population_time_max,
+                                       population_times, geometry, polarization,
+                                       include_signal, precision, **integrate_kwargs)
+        total = total + s
+    return ticks, total / ensemble_size
+
+
+def two_dimensional_spectra(dynamical_model, coherence_time_max,
+                            population_time_max=None, population_times=None,
+                            geometry='-++', polarization='xxxx', include_signal=None,
+                            ensemble_size=None, ensemble_random_orientations=False,
+                            exact_isotropic_average=False, precision='fp64',
+                            **integrate_kwargs):
+    """2D spectrum: FT over t1 (sign -1) and t3 (response.py:430-455)."""
+    (t1, t2, t3), X = third_order_response(
+        dynamical_model, coherence_time_max, population_time_max, population_times,
+        geometry, polarization, include_signal, ensemble_size,
+        ensemble_random_orientations, exact_isotropic_average, precision,
+        **integrate_kwargs)
+    rw, uc = dynamical_model.rw_freq, dynamical_model.unit_convert
+    f1, X1 = fourier_transform(t1, X, 0, rw_freq=rw, sign=-1, unit_convert=uc)
+    f3, X3 = fourier_transform(t3, X1, 2, rw_freq=rw, unit_convert=uc)
+    return (f1, t2, f3), X3

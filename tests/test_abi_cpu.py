@@ -1,0 +1,57 @@
+"""The C-ABI library loads and exports every symbol include/qsx.h declares (no GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+from qspectra_gb300 import _native
+
+HEADER = os.path.join(ROOT, 'include', 'qsx.h')
+
+
+def header_functions():
+    text = open(HEADER).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    return sorted(set(re.findall(r'\b(qsx_[a-z0-9_]+)\s*\(', text)))
+
+
+@pytest.fixture(scope='module')
+def lib():
+    if not os.path.exists(_native.LIB_PATH):
+        from qspectra_gb300 import build
+        build.build()
+    return _native.load()
+
+
+def test_header_and_binding_agree():
+    assert header_functions() == _native.exported_symbols()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in header_functions():
+        assert hasattr(lib, name), name
+
+
+def test_version_and_error_string(lib):
+    assert lib.qsx_version() >= 100
+    assert isinstance(lib.qsx_last_error_string(), bytes)
+
+
+def test_argument_validation_without_gpu(lib):
+    blk = (ctypes.c_int * 2)(0, 40)
+    st = lib.qsx_eigh_batched(None, 40, 1, 1, blk, None, None, None)
+    assert st == 1  # QSX_ERR_INVALID_ARG, rejected before any CUDA call
+    assert b'n <= 32' in lib.qsx_last_error_string()
+    st = lib.qsx_rk4_propagator_batched(None, 65, 1, 1.0, 0, None, None)
+    assert st == 1
+    a = _native.Rk4Args()
+    a.precision, a.form, a.m, a.nsteps, a.save_every = 0, 0, 7, 5, 2
+    st = lib.qsx_rk4_batched(ctypes.byref(a), None)
+    assert st == 1 and b'multiple of save_every' in lib.qsx_last_error_string()
+
+
+def test_rk4_args_layout_matches_library(lib):
+    assert ctypes.sizeof(_native.Rk4Args) == lib.qsx_rk4_args_bytes()
+    assert _native.Rk4Args.batch.offset == 16

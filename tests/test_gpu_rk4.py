@@ -1,0 +1,93 @@
+"""Every RK4 kernel shape against the oracle's stage-form RK4 on random generators."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as orc
+from conftest import rel_err
+from qspectra_gb300 import _native
+
+pytestmark = pytest.mark.gpu
+
+
+def random_generators(B, M, seed, scale=0.05):
+    """Stable complex generators with |hL| ~ scale (like Redfield at dt = 1 fs)."""
+    rng = np.random.RandomState(seed)
+    A = (rng.randn(B, M, M) + 1j * rng.randn(B, M, M)) * scale / np.sqrt(M)
+    A -= 0.5 * scale * np.eye(M)[None]  # damping keeps the trajectories bounded
+    return A
+
+
+def oracle_run(L, y0, nsteps, h, every):
+    out = []
+    for b in range(L.shape[0]):
+        t = np.arange(0, nsteps + 1, every) * h
+        out.append(orc.rk4_integrate(L[b], y0[b], t, h=h))
+    return np.array(out)
+
+
+CASES = [(1, 5), (3, 37), (7, 129), (8, 33), (9, 61), (16, 17), (25, 11), (36, 9),
+         (49, 23), (64, 5), (10, 7), (70, 3)]
+
+
+@pytest.mark.parametrize('M,B', CASES)
+@pytest.mark.parametrize('prec', ['fp64', 'fp32'])
+def test_kernels_state_and_means(M, B, prec):
+    h, nsteps, every = 1.0, 40, 4
+    L = random_generators(B, M, seed=M * 100 + B)
+    rng = np.random.RandomState(M)
+    y0 = rng.randn(B, M) + 1j * rng.randn(B, M)
+    ref = oracle_run(L, y0, nsteps, h, every)
+    Lt = torch.as_tensor(L).cuda()
+    y0t = torch.as_tensor(y0).cuda()
+    precision = _native.QSX_FP32 if prec == 'fp32' else _native.QSX_FP64
+    tol = 1e-5 if prec == 'fp32' else 1e-12
+    if M <= 64:
+        mat = _native.rk4_propagator(Lt, h, precision)
+        form = 0
+    else:
+        mat = Lt.to(torch.complex64 if prec == 'fp32' else torch.complex128)
+        form = 1
+    out = _native.rk4(mat, y0t, nsteps, every, form=form, h=h, state=True)
+    assert rel_err(out['state'].cpu().numpy(), ref) < tol
+    sel = [0, M - 1, M // 2]
+    out = _native.rk4(mat, y0t, nsteps, every, form=form, h=h, select=sel, mean=True)
+    assert rel_err(out['proj'].cpu().numpy(), ref[:, :, sel]) < tol
+    assert rel_err(out['mean'].cpu().numpy(), ref[:, :, sel].mean(0)) < tol
+    W = rng.randn(2, M) + 1j * rng.randn(2, M)
+    if not (prec == 'fp32' and form == 0 and M in (9, 16, 25, 36, 49, 64)):
+        out = _native.rk4(mat, y0t, nsteps, every, form=form, h=h,
+                          proj=torch.as_tensor(W).cuda(), mean=True)
+        want = np.einsum('pm,btm->btp', W, ref)
+        assert rel_err(out['proj'].cpu().numpy(), want) < tol
+        assert rel_err(out['mean'].cpu().numpy(), want.mean(0)) < tol
+
+
+def test_stage_form_matches_propagator_form_fp64():
+    B, M, h = 3, 12, 0.5
+    L = random_generators(B, M, 5)
+    y0 = np.ones((B, M), complex)
+    Lt = torch.as_tensor(L).cuda()
+    a = _native.rk4(_native.rk4_propagator(Lt, h), torch.as_tensor(y0).cuda(), 30, 1,
+                    state=True)['state']
+    b = _native.rk4(Lt, torch.as_tensor(y0).cuda(), 30, 1, form=1, h=h, state=True)['state']
+    assert rel_err(a.cpu().numpy(), b.cpu().numpy()) < 1e-13
+
+
+def test_zero_steps_and_shared_inputs():
+    M = 7
+    L = torch.as_tensor(random_generators(1, M, 2)[0]).cuda()
+    y0 = torch.arange(M, dtype=torch.complex128, device='cuda')
+    D = _native.rk4_propagator(L[None], 1.0, _native.QSX_FP32)[0]
+    out = _native.rk4(D, y0.expand(5, M).contiguous(), 0, 1, state=True)
+    assert torch.allclose(out['state'][:, 0], y0.expand(5, M))
+
+
+def test_propagator_is_one_rk4_step():
+    L = random_generators(2, 9, 8)
+    Lt = torch.as_tensor(L).cuda()
+    D = _native.rk4_propagator(Lt, 0.7).cpu().numpy()
+    for b in range(2):
+        hL = 0.7 * L[b]
+        P = np.eye(9) + hL + hL @ hL / 2 + hL @ hL @ hL / 6 + hL @ hL @ hL @ hL / 24
+        assert rel_err(D[b], P - np.eye(9)) < 1e-14
