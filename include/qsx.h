@@ -110,6 +110,24 @@ int qsx_redfield_liouvillian_batched(const double* H, int64_t H_stride,
                                      double* L, void* stream);
 
 /*
+ * Liouvillian block and its RK4 propagator in one pass (site basis,
+ * non-secular): D = P - I (as qsx_rk4_propagator_batched) of the block
+ * L[idx, idx] (transposed when transpose != 0) that
+ * qsx_redfield_liouvillian_batched produces with K == NULL, built in shared
+ * memory and never written to HBM.  Replaces the same reference code as
+ * those two calls (redfield.py:95-104 and 146-152, liouville_space.py:316-330,
+ * simulate/utils.py:44-49).  m <= 64; returns QSX_ERR_UNSUPPORTED when the
+ * operators plus three m x m tiles exceed 227 KB of shared memory.
+ */
+int qsx_redfield_propagator_batched(const double* H, int64_t H_stride,
+                                    const double* G, const double* M,
+                                    const double* occ, int n, int n_sites,
+                                    int64_t batch, double unit_convert,
+                                    const int* idx, int m, int transpose,
+                                    double h, int precision, void* D,
+                                    void* stream);
+
+/*
  * RK4 propagator D = P - I with P = sum_{k<=4} (hL)^k / k!, i.e. exactly one
  * classical RK4 step of dy/dt = L y (the step inside the integrate loop,
  * qspectra/simulate/utils.py:44-49, with zvode replaced by RK4).

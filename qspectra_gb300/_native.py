@@ -64,6 +64,9 @@ _PROTOS = {
     'qsx_redfield_liouvillian_batched': (_c_int, [
         _c_vp, _c_i64, _c_vp, _c_vp, _c_vp, _c_i64, _c_vp, _c_int, _c_int,
         _c_i64, _c_dbl, _c_vp, _c_int, _c_int, _c_int, _c_vp, _c_vp]),
+    'qsx_redfield_propagator_batched': (_c_int, [
+        _c_vp, _c_i64, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_i64, _c_dbl, _c_vp,
+        _c_int, _c_int, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_rk4_propagator_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl,
                                             _c_int, _c_vp, _c_vp]),
     'qsx_rk4_args_bytes': (ctypes.c_size_t, []),
@@ -204,6 +207,30 @@ def redfield_liouvillian(H, G, M, idx, unit_convert, K=None, occ=None,
     return L
 
 
+def redfield_propagator(H, G, M, occ, idx, unit_convert, h, precision=QSX_FP64,
+                        transpose=False):
+    """Fused site-basis generator block + RK4 propagator; None if it does not fit."""
+    require_gpu()
+    _need(G, torch.complex128, 'G', 3)
+    _need(M, torch.complex128, 'M', 4)
+    _need(occ, torch.float64, 'occ', 2)
+    B, n, _ = G.shape
+    N = M.shape[1]
+    H = _need(H, torch.float64, 'H')
+    h_stride = 0 if H.dim() == 2 else n * n
+    idx = _need(idx, torch.int32, 'idx', 1)
+    m = idx.numel()
+    dt = torch.complex64 if precision == QSX_FP32 else torch.complex128
+    D = torch.empty((B, m, m), dtype=dt, device=G.device)
+    st = load().qsx_redfield_propagator_batched(
+        _p(H), h_stride, _p(G), _p(M), _p(occ), n, N, B, unit_convert, _p(idx), m,
+        int(transpose), h, precision, _p(D), _stream())
+    if st == 3:  # QSX_ERR_UNSUPPORTED: too large for shared memory
+        return None
+    _check(st, 'qsx_redfield_propagator_batched')
+    return D
+
+
 def rk4_propagator(L, h, precision=QSX_FP64):
     require_gpu()
     _need(L, torch.complex128, 'L', 3)
@@ -267,6 +294,8 @@ def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
         sel_np = np.asarray(select, dtype=np.int64).reshape(-1)
         if sel_np.size == 0 or sel_np.min() < 0 or sel_np.max() >= m:
             raise ValueError('select indices must lie in [0, {})'.format(m))
+        if len(np.unique(sel_np)) != sel_np.size:
+            raise ValueError('select indices must be distinct')
         sel = torch.as_tensor(sel_np, dtype=torch.int32).to(dev).contiguous()
         a.nselect = sel.numel()
         a.select = sel.data_ptr()

@@ -11,38 +11,41 @@
 
 namespace qsx {
 
-constexpr int DFT_TILE = 1024;
-
+// grid (ceil(nf / 32), batch), 256 threads: lane = frequency, the 8 warps
+// split the time samples, partial sums meet in shared memory (fixed order).
 __global__ void __launch_bounds__(256)
     dft_kernel(const double2* __restrict__ x, int nt, double t0, double dt,
                const double* __restrict__ freqs, int nf, double rw, double uc, int sign,
                double2* __restrict__ X) {
-  __shared__ double2 tile[DFT_TILE];
+  __shared__ double2 part[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t b = blockIdx.y;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const double w = k < nf ? (double)sign * (freqs[k] - rw) * uc : 0.0;
-  const double delta = w * dt;
+  const int k = blockIdx.x * 32 + lane;
+  const double wk = k < nf ? (double)sign * (freqs[k] - rw) * uc : 0.0;
   double sd, cd;
-  sincos(delta, &sd, &cd);
-  double2 acc = make_double2(0.0, 0.0);
+  sincos(wk * dt, &sd, &cd);
+  const int chunk = (nt + 7) / 8;
+  const int n0 = w * chunk, n1 = min(nt, n0 + chunk);
   const double2* xb = x + b * nt;
-  for (int base = 0; base < nt; base += DFT_TILE) {
-    const int len = min(DFT_TILE, nt - base);
-    __syncthreads();
-    for (int i = threadIdx.x; i < len; i += blockDim.x) tile[i] = xb[base + i];
-    __syncthreads();
-    double2 ph = make_double2(1.0, 0.0);
-    for (int i = 0; i < len; ++i) {
-      if ((i & 31) == 0) {
-        double s, c;
-        sincos(w * (t0 + (double)(base + i) * dt), &s, &c);
-        ph = make_double2(c, s);
-      }
-      cfma(acc, tile[i], ph);
-      ph = make_double2(ph.x * cd - ph.y * sd, ph.x * sd + ph.y * cd);
+  double2 acc = make_double2(0.0, 0.0);
+  double2 ph = make_double2(1.0, 0.0);
+  for (int n = n0; n < n1; ++n) {
+    if (((n - n0) & 31) == 0) {
+      double s, c;
+      sincos(wk * (t0 + (double)n * dt), &s, &c);
+      ph = make_double2(c, s);
     }
+    cfma(acc, __ldg(&xb[n]), ph);
+    ph = make_double2(ph.x * cd - ph.y * sd, ph.x * sd + ph.y * cd);
   }
-  if (k < nf) X[b * nf + k] = cscale(acc, dt);
+  part[w][lane] = acc;
+  __syncthreads();
+  if (w == 0 && k < nf) {
+    double2 t = part[0][lane];
+#pragma unroll
+    for (int i = 1; i < 8; ++i) t = cadd(t, part[i][lane]);
+    X[b * nf + k] = cscale(t, dt);
+  }
 }
 
 }  // namespace qsx
@@ -55,7 +58,7 @@ extern "C" int qsx_dft_batched(const double* x, int nt, int64_t batch, double t0
   QSX_CHECK_ARG(sign == 1 || sign == -1, "qsx_dft_batched: sign must be +1 or -1");
   if (batch == 0) return QSX_OK;
   QSX_CHECK_ARG(x && freqs && X, "qsx_dft_batched: null pointer");
-  dim3 grid((unsigned)((nf + 255) / 256), (unsigned)batch);
+  dim3 grid((unsigned)((nf + 31) / 32), (unsigned)batch);
   qsx::dft_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(
       (const double2*)x, nt, t0, dt, freqs, nf, rw_freq, unit_convert, sign, (double2*)X);
   QSX_LAUNCH_CHECK("qsx_dft_batched");

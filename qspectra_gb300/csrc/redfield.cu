@@ -1,6 +1,7 @@
 // Redfield Liouvillian construction on the GPU (FP64): bath correlation
 // function, batched Jacobi eigensolver, operator-form Redfield tensor, dense
 // Liouvillian blocks and the RK4 one-step propagator.
+#include <algorithm>
 #include <cmath>
 
 #include "qsx_bath.cuh"
@@ -26,6 +27,101 @@ constexpr int EIGH_WARPS = 4;
 struct BlockTable {
   int v[EIGH_NMAX + 1];
 };
+
+// Classical Jacobi rotation zeroing a_pq (Golub & Van Loan, Alg. 8.4.1):
+// returns c = cos, s = sin and t = tan of the angle.
+__device__ __forceinline__ void jacobi_rotation(double app, double aqq, double apq,
+                                                double& c, double& s, double& t) {
+  const double tau = (aqq - app) / (2.0 * apq);
+  t = fabs(tau) < 1e100
+          ? (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(fma(tau, tau, 1.0)))
+          : 0.5 / tau;
+  c = rsqrt(fma(t, t, 1.0));
+  s = t * c;
+}
+__device__ __forceinline__ void jacobi_rotation(double app, double aqq, double apq,
+                                                double& c, double& s) {
+  double t;
+  jacobi_rotation(app, aqq, apq, c, s, t);
+}
+
+// One thread per matrix for a diagonal block of size NB <= 8 starting at
+// row/column `off` of each n x n input: the upper triangle of the block and
+// its eigenvectors live in registers (fully unrolled sweeps, compile-time
+// indices).  Symmetric update: a_pp -= t a_pq, a_qq += t a_pq, and for
+// k != p, q the pair (a_kp, a_kq) rotates by (c, s).
+template <int NB>
+__global__ void __launch_bounds__(64)
+    eigh_block_kernel(const double* __restrict__ H, int n, int off, int64_t batch,
+                      double* E, double* U) {
+#define AS(i, j) A[(i) < (j) ? (i) : (j)][(i) < (j) ? (j) : (i)]
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  double A[NB][NB], V[NB][NB];
+  const double* h = H + b * n * n;
+#pragma unroll
+  for (int i = 0; i < NB; ++i)
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      if (j >= i) A[i][j] = h[(off + i) * n + off + j];
+      V[i][j] = i == j ? 1.0 : 0.0;
+    }
+  for (int sweep = 0; sweep < 30; ++sweep) {
+    double offd = 0.0, dia = 0.0;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      dia = fma(A[i][i], A[i][i], dia);
+#pragma unroll
+      for (int j = i + 1; j < NB; ++j) offd = fma(A[i][j], A[i][j], offd);
+    }
+    if (!(offd > 1e-32 * dia)) break;
+#pragma unroll
+    for (int p = 0; p < NB - 1; ++p) {
+#pragma unroll
+      for (int q = p + 1; q < NB; ++q) {
+        const double apq = A[p][q];
+        if (apq != 0.0) {
+          double c, s, t;
+          jacobi_rotation(A[p][p], A[q][q], apq, c, s, t);
+          A[p][p] = fma(-t, apq, A[p][p]);
+          A[q][q] = fma(t, apq, A[q][q]);
+          A[p][q] = 0.0;
+#pragma unroll
+          for (int k = 0; k < NB; ++k) {
+            if (k == p || k == q) continue;
+            const double g = AS(k, p), hh = AS(k, q);
+            AS(k, p) = c * g - s * hh;
+            AS(k, q) = s * g + c * hh;
+          }
+#pragma unroll
+          for (int k = 0; k < NB; ++k) {  // V <- V J
+            const double vkp = V[k][p], vkq = V[k][q];
+            V[k][p] = c * vkp - s * vkq;
+            V[k][q] = s * vkp + c * vkq;
+          }
+        }
+      }
+    }
+  }
+  // ascending order inside the block (stable on ties)
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    int rank = 0;
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+      rank += (A[j][j] < A[i][i] || (A[j][j] == A[i][i] && j < i)) ? 1 : 0;
+    E[b * n + off + rank] = A[i][i];
+#pragma unroll
+    for (int r = 0; r < NB; ++r) U[b * n * n + (off + r) * n + off + rank] = V[r][i];
+  }
+#undef AS
+}
+
+// zero the off-block entries of U (the block kernels write only their blocks)
+__global__ void zero_kernel(double* p, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0.0;
+}
 
 __global__ void __launch_bounds__(32 * EIGH_WARPS)
     eigh_jacobi_kernel(const double* __restrict__ H, int n, int64_t batch,
@@ -65,10 +161,11 @@ __global__ void __launch_bounds__(32 * EIGH_WARPS)
       for (int q = p + 1; q < n; ++q) {
         const double apq = A[p][q];
         if (apq == 0.0) continue;
-        const double app = A[p][p], aqq = A[q][q];
-        const double tau = (aqq - app) / (2.0 * apq);
-        const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + hypot(1.0, tau));
-        const double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
+        // one lane evaluates the rotation (FP64 divide/sqrt are scarce here)
+        double c = 1.0, s = 0.0;
+        if (lane == 0) jacobi_rotation(A[p][p], A[q][q], apq, c, s);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        s = __shfl_sync(0xffffffffu, s, 0);
         __syncwarp();
         if (lane < n) {  // A <- A J and V <- V J on row `lane`
           double akp = A[lane][p], akq = A[lane][q];
@@ -197,16 +294,21 @@ __global__ void __launch_bounds__(256)
       sMt[e] = cmk(acc * cw.x, acc * cw.y);
     }
     __syncthreads();
-    smem_matmul_rc(sKt, sMt, sGS, n, true);  // GS += Kt_i Mt_i
-    __syncthreads();
     double2* Mi = M + (b * n_sites + i) * nn;
     if (site_basis) {
       smem_matmul_rc(sU, sMt, sT1, n, false);  // T1 = U Mt_i
       __syncthreads();
-      smem_matmul_crT(sT1, sU, sMt, n);        // Mt_i <- T1 U^T
+      smem_matmul_crT(sT1, sU, sMt, n);        // Mt_i <- T1 U^T (site basis)
       __syncthreads();
-      for (int e = threadIdx.x; e < nn; e += blockDim.x) Mi[e] = cscale(sMt[e], uc);
+      // G_site = sum_i diag(occ_i) M_i: row s of G gathers row s of every M_i
+      for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+        Mi[e] = cscale(sMt[e], uc);
+        const double o = oc[e / n];
+        if (o != 0.0) sGS[e] = cadd(sGS[e], cscale(sMt[e], o));
+      }
     } else {
+      smem_matmul_rc(sKt, sMt, sGS, n, true);  // GS += Kt_i Mt_i (eigenbasis)
+      __syncthreads();
       double* Ki = K + (b * n_sites + i) * nn;
       for (int e = threadIdx.x; e < nn; e += blockDim.x) {
         Mi[e] = cscale(sMt[e], uc);
@@ -216,15 +318,7 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
   }
   double2* g = G + b * nn;
-  if (site_basis) {
-    smem_matmul_rc(sU, sGS, sT1, n, false);
-    __syncthreads();
-    smem_matmul_crT(sT1, sU, sMt, n);
-    __syncthreads();
-    for (int e = threadIdx.x; e < nn; e += blockDim.x) g[e] = cscale(sMt[e], uc);
-  } else {
-    for (int e = threadIdx.x; e < nn; e += blockDim.x) g[e] = cscale(sGS[e], uc);
-  }
+  for (int e = threadIdx.x; e < nn; e += blockDim.x) g[e] = cscale(sGS[e], uc);
 }
 
 // ----------------------------------------------- dense Liouvillian block
@@ -285,25 +379,19 @@ __global__ void liouvillian_kernel(const double* __restrict__ H, int64_t H_strid
 }
 
 // ------------------------------------------------ RK4 one-step propagator
-// D = h L (I + hL/2 (I + hL/3 (I + hL/4))), Horner form of P - I.
+// D = h L (I + hL/2 (I + hL/3 (I + hL/4))), Horner form of P - I.  sL holds
+// L on entry; sX, sY are m x m scratch tiles; D receives the result.
 template <typename T>
-__global__ void __launch_bounds__(256)
-    propagator_kernel(const double2* __restrict__ L, int m, double h,
-                      typename cplx<T>::type* D) {
+__device__ void horner_propagator(typename cplx<T>::type* sL, typename cplx<T>::type* sX,
+                                  typename cplx<T>::type* sY, int m, double h,
+                                  typename cplx<T>::type* D) {
   using C = typename cplx<T>::type;
-  extern __shared__ unsigned char smraw[];
-  C* sL = (C*)smraw;
-  C* sX = sL + m * m;
-  C* sY = sX + m * m;
-  const int64_t b = blockIdx.x;
   const int mm = m * m;
-  const double2* l = L + b * mm;
   for (int e = threadIdx.x; e < mm; e += blockDim.x) {
-    double2 v = l[e];
-    sL[e] = cmk((T)v.x, (T)v.y);
     int r = e / m, c = e % m;
     T s = (T)(h / 4.0);
-    sX[e] = cmk((T)(r == c ? 1 : 0) + s * (T)v.x, s * (T)v.y);
+    C v = sL[e];
+    sX[e] = cmk((T)(r == c ? 1 : 0) + s * v.x, s * v.y);
   }
   __syncthreads();
   const T coef[3] = {(T)(h / 3.0), (T)(h / 2.0), (T)h};
@@ -321,10 +409,106 @@ __global__ void __launch_bounds__(256)
       if (stage < 2)
         sX[e] = cmk((T)(r == c ? 1 : 0) + coef[stage] * y.x, coef[stage] * y.y);
       else
-        D[b * mm + e] = cmk(coef[2] * y.x, coef[2] * y.y);
+        D[e] = cmk(coef[2] * y.x, coef[2] * y.y);
     }
     __syncthreads();
   }
+}
+
+// One site-basis Redfield generator element (the K == NULL branch of
+// liouvillian_kernel): -i uc (H_ac d_bd - d_ac H_db) - R_abcd with
+// R_abcd = d_bd G_ac + d_ac conj(G_bd) - d_ac sum_i occ_ia conj(M_i,bd)
+//          - d_bd sum_i occ_ib M_i,ac.
+__device__ __forceinline__ double2 site_generator_element(const double* h, const double2* g,
+                                                          const double2* mm, const double* occ,
+                                                          int n, int n_sites, double uc,
+                                                          int a, int bb, int c, int d) {
+  const int nn = n * n;
+  double hre = 0.0;
+  if (bb == d) hre += h[a * n + c];
+  if (a == c) hre -= h[d * n + bb];
+  double2 R = cmk(0.0, 0.0);
+  if (bb == d) {
+    R = cadd(R, g[a * n + c]);
+    for (int i = 0; i < n_sites; ++i) {
+      double o = occ[i * n + bb];
+      if (o != 0.0) R = csub(R, cscale(mm[i * nn + a * n + c], o));
+    }
+  }
+  if (a == c) {
+    R = cadd(R, cconj(g[bb * n + d]));
+    for (int i = 0; i < n_sites; ++i) {
+      double o = occ[i * n + a];
+      if (o != 0.0) R = csub(R, cscale(cconj(mm[i * nn + bb * n + d]), o));
+    }
+  }
+  return csub(cmk(0.0, -uc * hre), R);
+}
+
+// Fused: site-basis generator block -> shared memory -> Horner propagator.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    redfield_propagator_kernel(const double* __restrict__ H, int64_t H_stride,
+                               const double2* __restrict__ G, const double2* __restrict__ Mo,
+                               const double* __restrict__ occ, int n, int n_sites, double uc,
+                               const int* __restrict__ idx, int m, int transpose, double h,
+                               typename cplx<T>::type* D) {
+  using C = typename cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nn = n * n;
+  double2* sG = (double2*)smraw;
+  double2* sM = sG + nn;
+  double* sH = (double*)(sM + (size_t)n_sites * nn);
+  double* sOcc = sH + nn;
+  int* sIdx = (int*)(sOcc + n_sites * n);
+  size_t off = (size_t)((unsigned char*)(sIdx + m) - smraw);
+  off = (off + 15) & ~(size_t)15;
+  C* sL = (C*)(smraw + off);
+  C* sX = sL + m * m;
+  C* sY = sX + m * m;
+  const int64_t b = blockIdx.x;
+  for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+    sG[e] = G[b * nn + e];
+    sH[e] = H[b * H_stride + e];
+  }
+  for (int e = threadIdx.x; e < n_sites * nn; e += blockDim.x) sM[e] = Mo[b * n_sites * nn + e];
+  for (int e = threadIdx.x; e < n_sites * n; e += blockDim.x) sOcc[e] = occ[e];
+  for (int e = threadIdx.x; e < m; e += blockDim.x) {
+    int v = idx[e];
+    sIdx[e] = (v >= 0 && v < nn) ? v : -1;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+    int r = e / m, cc = e % m;
+    if (transpose) { int t = r; r = cc; cc = t; }
+    const int ir = sIdx[r], ic = sIdx[cc];
+    double2 v = cmk(nan(""), nan(""));
+    if (ir >= 0 && ic >= 0)
+      v = site_generator_element(sH, sG, sM, sOcc, n, n_sites, uc, ir % n, ir / n, ic % n, ic / n);
+    sL[e] = cmk((T)v.x, (T)v.y);
+  }
+  __syncthreads();
+  horner_propagator<T>(sL, sX, sY, m, h, D + b * (int64_t)m * m);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    propagator_kernel(const double2* __restrict__ L, int m, double h,
+                      typename cplx<T>::type* D) {
+  using C = typename cplx<T>::type;
+  extern __shared__ unsigned char smraw[];
+  C* sL = (C*)smraw;
+  C* sX = sL + m * m;
+  C* sY = sX + m * m;
+  const int64_t b = blockIdx.x;
+  const int mm = m * m;
+  const double2* l = L + b * mm;
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) {
+    double2 v = l[e];
+    sL[e] = cmk((T)v.x, (T)v.y);
+  }
+  __syncthreads();
+  horner_propagator<T>(sL, sX, sY, m, h, D + b * mm);
 }
 
 }  // namespace qsx
@@ -361,11 +545,28 @@ int qsx_eigh_batched(const double* H, int n, int64_t batch, int nblocks,
                   "qsx_eigh_batched: blocks must be non-empty and increasing");
   if (batch == 0) return QSX_OK;
   QSX_CHECK_ARG(H && E && U, "qsx_eigh_batched: null pointer");
-  BlockTable tb;
-  for (int k = 0; k <= EIGH_NMAX; ++k) tb.v[k] = k <= nblocks ? block_starts[k] : n;
-  unsigned grid = (unsigned)((batch + EIGH_WARPS - 1) / EIGH_WARPS);
-  eigh_jacobi_kernel<<<grid, 32 * EIGH_WARPS, 0, (cudaStream_t)stream>>>(
-      H, n, batch, nblocks, tb, E, U);
+  cudaStream_t st = (cudaStream_t)stream;
+  int maxb = 0;
+  for (int k = 0; k < nblocks; ++k) maxb = std::max(maxb, block_starts[k + 1] - block_starts[k]);
+  if (maxb > 8) {
+    BlockTable tb;
+    for (int k = 0; k <= EIGH_NMAX; ++k) tb.v[k] = k <= nblocks ? block_starts[k] : n;
+    unsigned grid = (unsigned)((batch + EIGH_WARPS - 1) / EIGH_WARPS);
+    eigh_jacobi_kernel<<<grid, 32 * EIGH_WARPS, 0, st>>>(H, n, batch, nblocks, tb, E, U);
+    QSX_LAUNCH_CHECK("qsx_eigh_batched");
+    return QSX_OK;
+  }
+  const int64_t total = batch * n * n;
+  zero_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(U, total);
+  const unsigned grid = (unsigned)((batch + 63) / 64);
+  for (int k = 0; k < nblocks; ++k) {
+    const int off = block_starts[k], nb = block_starts[k + 1] - off;
+    switch (nb) {
+#define B(NB) case NB: eigh_block_kernel<NB><<<grid, 64, 0, st>>>(H, n, off, batch, E, U); break;
+      B(1) B(2) B(3) B(4) B(5) B(6) B(7) B(8)
+#undef B
+    }
+  }
   QSX_LAUNCH_CHECK("qsx_eigh_batched");
   return QSX_OK;
 }
@@ -421,6 +622,53 @@ int qsx_redfield_liouvillian_batched(const double* H, int64_t H_stride, const do
       H, H_stride, (const double2*)G, (const double2*)M, K, K_stride, occ, n, n_sites,
       unit_convert, idx, m, secular, transpose, (double2*)L);
   QSX_LAUNCH_CHECK("qsx_redfield_liouvillian_batched");
+  return QSX_OK;
+}
+
+int qsx_redfield_propagator_batched(const double* H, int64_t H_stride, const double* G,
+                                    const double* M, const double* occ, int n, int n_sites,
+                                    int64_t batch, double unit_convert, const int* idx, int m,
+                                    int transpose, double h, int precision, void* D,
+                                    void* stream) {
+  QSX_CHECK_ARG(n >= 1 && n_sites >= 1 && m >= 1 && m <= 64 && (int64_t)m <= (int64_t)n * n,
+                "qsx_redfield_propagator_batched: bad sizes n=%d n_sites=%d m=%d", n, n_sites,
+                m);
+  QSX_CHECK_ARG(batch >= 0 && batch <= 0x7fffffff,
+                "qsx_redfield_propagator_batched: bad batch");
+  QSX_CHECK_ARG(precision == QSX_FP32 || precision == QSX_FP64,
+                "qsx_redfield_propagator_batched: bad precision");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(H && G && M && occ && idx && D,
+                "qsx_redfield_propagator_batched: null pointer");
+  const size_t nn = (size_t)n * n;
+  size_t head = (nn + (size_t)n_sites * nn) * sizeof(double2) +
+                (nn + (size_t)n_sites * n) * sizeof(double) + (size_t)m * sizeof(int);
+  head = (head + 15) & ~(size_t)15;
+  const size_t cs = precision == QSX_FP32 ? sizeof(float2) : sizeof(double2);
+  const size_t smem = head + 3 * (size_t)m * m * cs;
+  if (smem > 227 * 1024) {
+    set_error("qsx_redfield_propagator_batched: %zu bytes of shared memory needed; use "
+              "qsx_redfield_liouvillian_batched + qsx_rk4_propagator_batched", smem);
+    return QSX_ERR_UNSUPPORTED;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e;
+  if (precision == QSX_FP32) {
+    e = cudaFuncSetAttribute(redfield_propagator_kernel<float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_batched");
+    redfield_propagator_kernel<float><<<(unsigned)batch, 256, smem, s>>>(
+        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, unit_convert, idx, m,
+        transpose, h, (float2*)D);
+  } else {
+    e = cudaFuncSetAttribute(redfield_propagator_kernel<double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_batched");
+    redfield_propagator_kernel<double><<<(unsigned)batch, 256, smem, s>>>(
+        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, unit_convert, idx, m,
+        transpose, h, (double2*)D);
+  }
+  QSX_LAUNCH_CHECK("qsx_redfield_propagator_batched");
   return QSX_OK;
 }
 

@@ -33,92 +33,140 @@ struct Rk4P {
   const int* select;
   double2* out_state;
   double2* out_proj;
-  double2* partial;  // [nslots][nsave][nout] or null
+  double2* partial;   // generic kernel: [nslots][nsave][nout] double2, or null
+  float2* partial32;  // FP32 kernels: [nslots][nsave][nout] float2, or null
   int* status;
 };
 
 __device__ __forceinline__ float2 f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
 
 // ---------------------------------------------------------------- small M
+// rk4_lanes_f32<M>: M <= 8.  LPS lanes per sample (a power of two dividing
+// 32), lane q holding rows [q*R, q*R + R) of D and of the state in registers.
+// Each step gathers the M state values with shuffles, updates its rows in
+// split-word FP32 and, at save steps, folds the projections of all samples
+// of the warp into one FP32 partial sum per warp (slot = warp).
 template <int M>
-__global__ void __launch_bounds__(128) rk4_small_f32(Rk4P p) {
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__host__ __device__ constexpr int lanes_per_sample() {
+  return M == 1 ? 1 : (M == 2 ? 2 : 4);
+}
+
+constexpr int LANES_MAXPROJ = 4;
+
+template <int M>
+__global__ void __launch_bounds__(128) rk4_lanes_f32(Rk4P p) {
+  constexpr int LPS = lanes_per_sample<M>();
+  constexpr int R = (M + LPS - 1) / LPS;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t s = gt / LPS;
+  const int q = (int)(gt % LPS);
   const bool valid = s < p.batch;
-  const int lane = threadIdx.x & 31;
-  const int64_t slot = s >> 5;
-  float2 D[M][M];
-  float yh[M][2], yl[M][2];
+  const unsigned lane = threadIdx.x & 31;
+  const int base = (int)(lane & ~(unsigned)(LPS - 1));
+  const int64_t slot = gt >> 5;
+  float2 D[R][M];
+  float yh[R][2], yl[R][2];
   const float2* dm = (const float2*)p.matrix + (valid ? s * p.matrix_stride : 0);
 #pragma unroll
-  for (int i = 0; i < M; ++i) {
+  for (int i = 0; i < R; ++i) {
+    const int row = q * R + i;
 #pragma unroll
-    for (int j = 0; j < M; ++j) D[i][j] = valid ? dm[i * M + j] : make_float2(0.f, 0.f);
-  }
-  const double2* y0 = p.y0 + (valid ? s * p.y0_stride : 0);
-#pragma unroll
-  for (int i = 0; i < M; ++i) {
-    double2 v = valid ? y0[i] : make_double2(0.0, 0.0);
+    for (int j = 0; j < M; ++j)
+      D[i][j] = (valid && row < M) ? dm[row * M + j] : make_float2(0.f, 0.f);
+    double2 v = (valid && row < M) ? p.y0[s * p.y0_stride + row] : make_double2(0.0, 0.0);
     yh[i][0] = (float)v.x;
     yh[i][1] = (float)v.y;
     yl[i][0] = (float)(v.x - (double)yh[i][0]);
     yl[i][1] = (float)(v.y - (double)yh[i][1]);
   }
-  const double2* W = p.proj + (p.nproj ? (valid ? s * p.proj_stride : 0) : 0);
+  // projection rows for this lane's state components, in FP32 registers
+  float2 W[LANES_MAXPROJ][R];
+#pragma unroll
+  for (int k = 0; k < LANES_MAXPROJ; ++k)
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int row = q * R + i;
+      W[k][i] = (k < p.nproj && valid && row < M)
+                    ? f2(p.proj[(p.proj_stride ? s * p.proj_stride : 0) + k * M + row])
+                    : make_float2(0.f, 0.f);
+    }
+  int selrow[LANES_MAXPROJ];
+#pragma unroll
+  for (int k = 0; k < LANES_MAXPROJ; ++k) selrow[k] = k < p.nselect ? p.select[k] : -1;
   auto save = [&](int k) {
     if (p.out_state && valid) {
-      double2* o = p.out_state + (s * p.nsave + k) * M;
 #pragma unroll
-      for (int i = 0; i < M; ++i)
-        o[i] = make_double2((double)yh[i][0] + (double)yl[i][0],
-                            (double)yh[i][1] + (double)yl[i][1]);
-    }
-    for (int q = 0; q < p.nout; ++q) {
-      float2 v = make_float2(0.f, 0.f);
-      if (p.nproj) {
-#pragma unroll
-        for (int j = 0; j < M; ++j) cfma(v, f2(W[q * M + j]), make_float2(yh[j][0], yh[j][1]));
-      } else {
-        const int sel = p.select[q];
-#pragma unroll
-        for (int j = 0; j < M; ++j)
-          if (j == sel) v = make_float2(yh[j][0], yh[j][1]);
+      for (int i = 0; i < R; ++i) {
+        const int row = q * R + i;
+        if (row < M)
+          p.out_state[(s * p.nsave + k) * M + row] =
+              make_double2((double)yh[i][0] + (double)yl[i][0], (double)yh[i][1] + (double)yl[i][1]);
       }
-      if (!valid) v = make_float2(0.f, 0.f);
-      if (p.out_proj && valid)
-        p.out_proj[(s * p.nsave + k) * p.nout + q] = make_double2(v.x, v.y);
-      if (p.partial) {
-        double sx = v.x, sy = v.y;
+    }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          sx += __shfl_xor_sync(0xffffffffu, sx, o);
-          sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    for (int o = 0; o < LANES_MAXPROJ; ++o) {
+      if (o >= p.nout) break;
+      float vx = 0.f, vy = 0.f;
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        if (p.nproj) {
+          vx = fmaf(W[o][i].x, yh[i][0], vx);
+          vx = fmaf(-W[o][i].y, yh[i][1], vx);
+          vy = fmaf(W[o][i].x, yh[i][1], vy);
+          vy = fmaf(W[o][i].y, yh[i][0], vy);
+        } else if (q * R + i == selrow[o]) {
+          vx = yh[i][0];
+          vy = yh[i][1];
         }
-        if (lane == 0) p.partial[(slot * p.nsave + k) * p.nout + q] = make_double2(sx, sy);
+      }
+      if (!valid) vx = vy = 0.f;
+      // per-sample value: sum over the sample's LPS lanes
+      float sx = vx, sy = vy;
+#pragma unroll
+      for (int d = 1; d < LPS; d <<= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, d);
+        sy += __shfl_xor_sync(0xffffffffu, sy, d);
+      }
+      if (p.out_proj && valid && q == 0)
+        p.out_proj[(s * p.nsave + k) * p.nout + o] = make_double2(sx, sy);
+      if (p.partial32) {
+#pragma unroll
+        for (int d = LPS; d < 32; d <<= 1) {
+          sx += __shfl_xor_sync(0xffffffffu, sx, d);
+          sy += __shfl_xor_sync(0xffffffffu, sy, d);
+        }
+        if (lane == 0) p.partial32[(slot * p.nsave + k) * p.nout + o] = make_float2(sx, sy);
       }
     }
   };
   save(0);
   for (int step = 1; step <= p.nsteps; ++step) {
-    float z[M][2];
+    float zx[R], zy[R];
 #pragma unroll
-    for (int i = 0; i < M; ++i) {
-      float2 acc = make_float2(0.f, 0.f);
+    for (int i = 0; i < R; ++i) zx[i] = zy[i] = 0.f;
 #pragma unroll
-      for (int j = 0; j < M; ++j) cfma(acc, D[i][j], make_float2(yh[j][0], yh[j][1]));
-      z[i][0] = acc.x;
-      z[i][1] = acc.y;
+    for (int j = 0; j < M; ++j) {
+      const float vx = __shfl_sync(0xffffffffu, yh[j % R][0], base + j / R);
+      const float vy = __shfl_sync(0xffffffffu, yh[j % R][1], base + j / R);
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        zx[i] = fmaf(D[i][j].x, vx, zx[i]);
+        zx[i] = fmaf(-D[i][j].y, vy, zx[i]);
+        zy[i] = fmaf(D[i][j].x, vy, zy[i]);
+        zy[i] = fmaf(D[i][j].y, vx, zy[i]);
+      }
     }
 #pragma unroll
-    for (int i = 0; i < M; ++i) {
-      dd_add(yh[i][0], yl[i][0], z[i][0]);
-      dd_add(yh[i][1], yl[i][1], z[i][1]);
+    for (int i = 0; i < R; ++i) {
+      dd_add(yh[i][0], yl[i][0], zx[i]);
+      dd_add(yh[i][1], yl[i][1], zy[i]);
     }
     if (step % p.save_every == 0) save(step / p.save_every);
   }
   if (valid && p.status) {
     bool ok = true;
 #pragma unroll
-    for (int i = 0; i < M; ++i) ok = ok && isfinite(yh[i][0]) && isfinite(yh[i][1]);
+    for (int i = 0; i < R; ++i) ok = ok && isfinite(yh[i][0]) && isfinite(yh[i][1]);
     if (!ok) atomicOr(p.status, QSX_ERR_NONFINITE);
   }
 }
@@ -137,7 +185,7 @@ __global__ void __launch_bounds__(256, MINB) rk4_rows_f32(Rk4P p, int64_t ngroup
   constexpr int ST = rows_stride(M);
   constexpr int MP = (M % 2) ? M + 1 : M;
   __shared__ __align__(16) float2 ybuf[2][G][ST];
-  __shared__ double2 stash[2][G][M];
+  __shared__ float2 stash[2][G][M];
   const int tid = threadIdx.x;
   const int g = tid / M, r = tid % M;
   const bool active = tid < G * M;
@@ -148,9 +196,14 @@ __global__ void __launch_bounds__(256, MINB) rk4_rows_f32(Rk4P p, int64_t ngroup
       ybuf[1][tid][j] = make_float2(0.f, 0.f);
     }
   }
+  // this thread's output slot: the first q with select[q] == r (host checks
+  // that the select entries are distinct and in range)
+  int myq = -1;
+  if (active)
+    for (int q = 0; q < p.nout; ++q)
+      if (p.select[q] == r) { myq = q; break; }
   int savecount = 0;
   for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-    const bool first = grp == blockIdx.x;
     const int64_t s = grp * G + g;
     const bool valid = active && s < p.batch;
     float2 drow[M];
@@ -167,27 +220,32 @@ __global__ void __launch_bounds__(256, MINB) rk4_rows_f32(Rk4P p, int64_t ngroup
     }
     if (active) ybuf[0][g][r] = make_float2(yhx, yhy);
     __syncthreads();
+    // per-sample outputs go straight to global memory; ensemble partial sums
+    // are staged per sample in shared memory and summed over the G samples
+    // by threads q < nout after the step barrier, then stored (no
+    // read-modify-write) into this group's slot of the workspace.
     auto save = [&](int k, int par) {
       if (!active) return;
       if (p.out_state && valid)
         p.out_state[(s * p.nsave + k) * M + r] =
             make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
-      for (int q = 0; q < p.nout; ++q) {
-        if (p.select[q] == r) {
-          double2 v = valid ? make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly)
-                            : make_double2(0.0, 0.0);
-          if (p.out_proj && valid) p.out_proj[(s * p.nsave + k) * p.nout + q] = v;
-          if (p.partial) stash[par][g][q] = v;
-        }
+      if (myq >= 0) {
+        if (p.out_proj && valid)
+          p.out_proj[(s * p.nsave + k) * p.nout + myq] =
+              make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
+        if (p.partial32) stash[par][g][myq] = valid ? make_float2(yhx, yhy) : make_float2(0.f, 0.f);
       }
     };
     auto reduce = [&](int k, int par) {
-      if (!p.partial) return;
+      if (!p.partial32) return;
       for (int q = tid; q < p.nout; q += blockDim.x) {
-        double2 acc = make_double2(0.0, 0.0);
-        for (int gg = 0; gg < G; ++gg) acc = cadd(acc, stash[par][gg][q]);
-        double2* dst = p.partial + ((int64_t)blockIdx.x * p.nsave + k) * p.nout + q;
-        *dst = first ? acc : cadd(*dst, acc);
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int gg = 0; gg < G; ++gg) {
+          acc.x += stash[par][gg][q].x;
+          acc.y += stash[par][gg][q].y;
+        }
+        p.partial32[(grp * p.nsave + k) * p.nout + q] = acc;
       }
     };
     save(0, savecount & 1);
@@ -206,6 +264,146 @@ __global__ void __launch_bounds__(256, MINB) rk4_rows_f32(Rk4P p, int64_t ngroup
       dd_add(yhx, ylx, a0.x + a1.x);
       dd_add(yhy, yly, a0.y + a1.y);
       if (active) ybuf[step & 1][g][r] = make_float2(yhx, yhy);
+      const bool sv = (step % p.save_every) == 0;
+      if (sv) save(step / p.save_every, savecount & 1);
+      __syncthreads();
+      if (sv) {
+        reduce(step / p.save_every, savecount & 1);
+        ++savecount;
+      }
+    }
+    if (valid && p.status && !(isfinite(yhx) && isfinite(yhy))) atomicOr(p.status, QSX_ERR_NONFINITE);
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------ tiles (ee, M = T^2)
+// rk4_tile_f32<T, G>: the state dimension is M = T*T.  Each sample uses T
+// row-groups of 8 lanes; lane ct < T of row-group rt holds the T x T tile
+// D[rt*T + i][ct*T + j] in registers and reads only the T state values of its
+// column tile.  The 8 lanes then sum their partial rows with a 3-level
+// shuffle reduce-scatter (4 + 2 + 1 complex exchanges), after which lane ct
+// owns row rt*T + ct: it updates that state component (split-word FP32) and
+// publishes it for the next step.  One barrier per step.
+template <int T>
+__host__ __device__ constexpr int tile_stride() {
+  // odd float2 stride: the T column tiles of two samples sharing a warp fall
+  // in distinct banks
+  return (T * T) % 2 ? T * T : T * T + 1;
+}
+
+template <int T, int G, int MINB>
+__global__ void __launch_bounds__(G * 8 * T, MINB) rk4_tile_f32(Rk4P p, int64_t ngroups) {
+  constexpr int M = T * T;
+  constexpr int ST = tile_stride<T>();
+  __shared__ __align__(16) float2 ybuf[2][G][ST];
+  __shared__ float2 stash[2][G][M];
+  const int tid = threadIdx.x;
+  const int g = tid / (8 * T);
+  const int w = tid % (8 * T);
+  const int rt = w / 8, ct = w % 8;
+  const bool tile = ct < T;        // holds a tile and owns row rt*T + ct
+  const int r = rt * T + ct;       // owned row (valid when tile)
+  const unsigned lane = tid & 31;
+  const unsigned gmask = 0xffu << (lane & 24u);  // this row-group's 8 lanes
+  int myq = -1;
+  if (tile)
+    for (int q = 0; q < p.nout; ++q)
+      if (p.select[q] == r) { myq = q; break; }
+  int savecount = 0;
+  for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const int64_t s = grp * G + g;
+    const bool svalid = s < p.batch;
+    const bool valid = tile && svalid;
+    float2 Dt[T][T];
+    const float2* dm = (const float2*)p.matrix + (svalid ? s * p.matrix_stride : 0);
+#pragma unroll
+    for (int i = 0; i < T; ++i)
+#pragma unroll
+      for (int j = 0; j < T; ++j)
+        Dt[i][j] = valid ? dm[(rt * T + i) * M + ct * T + j] : make_float2(0.f, 0.f);
+    float yhx = 0.f, yhy = 0.f, ylx = 0.f, yly = 0.f;
+    if (valid) {
+      double2 v = p.y0[s * p.y0_stride + r];
+      yhx = (float)v.x;
+      yhy = (float)v.y;
+      ylx = (float)(v.x - (double)yhx);
+      yly = (float)(v.y - (double)yhy);
+    }
+    if (tile) ybuf[0][g][r] = make_float2(yhx, yhy);
+    __syncthreads();
+    auto save = [&](int k, int par) {
+      if (!tile) return;
+      if (p.out_state && valid)
+        p.out_state[(s * p.nsave + k) * M + r] =
+            make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
+      if (myq >= 0) {
+        if (p.out_proj && valid)
+          p.out_proj[(s * p.nsave + k) * p.nout + myq] =
+              make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
+        if (p.partial32) stash[par][g][myq] = valid ? make_float2(yhx, yhy) : make_float2(0.f, 0.f);
+      }
+    };
+    auto reduce = [&](int k, int par) {
+      if (!p.partial32) return;
+      for (int q = tid; q < p.nout; q += blockDim.x) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int gg = 0; gg < G; ++gg) {
+          acc.x += stash[par][gg][q].x;
+          acc.y += stash[par][gg][q].y;
+        }
+        p.partial32[(grp * p.nsave + k) * p.nout + q] = acc;
+      }
+    };
+    save(0, savecount & 1);
+    __syncthreads();
+    reduce(0, savecount & 1);
+    ++savecount;
+    const bool b2 = (ct >> 2) & 1, b1 = (ct >> 1) & 1, b0 = ct & 1;
+    for (int step = 1; step <= p.nsteps; ++step) {
+      const float2* cur = ybuf[(step - 1) & 1][g] + (tile ? ct * T : 0);
+      float zx[8], zy[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) { zx[i] = 0.f; zy[i] = 0.f; }
+      if (tile) {
+#pragma unroll
+        for (int j = 0; j < T; ++j) {
+          const float2 v = cur[j];
+#pragma unroll
+          for (int i = 0; i < T; ++i) {
+            zx[i] = fmaf(Dt[i][j].x, v.x, zx[i]);
+            zx[i] = fmaf(-Dt[i][j].y, v.y, zx[i]);
+            zy[i] = fmaf(Dt[i][j].x, v.y, zy[i]);
+            zy[i] = fmaf(Dt[i][j].y, v.x, zy[i]);
+          }
+        }
+      }
+      // reduce-scatter over the 8 lanes: keep half, send half, three times
+      float kx[4], ky[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float sx = b2 ? zx[k] : zx[4 + k], sy = b2 ? zy[k] : zy[4 + k];
+        const float rx = __shfl_xor_sync(gmask, sx, 4), ry = __shfl_xor_sync(gmask, sy, 4);
+        kx[k] = (b2 ? zx[4 + k] : zx[k]) + rx;
+        ky[k] = (b2 ? zy[4 + k] : zy[k]) + ry;
+      }
+      float mx[2], my[2];
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const float sx = b1 ? kx[k] : kx[2 + k], sy = b1 ? ky[k] : ky[2 + k];
+        const float rx = __shfl_xor_sync(gmask, sx, 2), ry = __shfl_xor_sync(gmask, sy, 2);
+        mx[k] = (b1 ? kx[2 + k] : kx[k]) + rx;
+        my[k] = (b1 ? ky[2 + k] : ky[k]) + ry;
+      }
+      const float sx = b0 ? mx[0] : mx[1], sy = b0 ? my[0] : my[1];
+      const float rx = __shfl_xor_sync(gmask, sx, 1), ry = __shfl_xor_sync(gmask, sy, 1);
+      const float zfx = (b0 ? mx[1] : mx[0]) + rx, zfy = (b0 ? my[1] : my[0]) + ry;
+      if (tile) {
+        dd_add(yhx, ylx, zfx);
+        dd_add(yhy, yly, zfy);
+        ybuf[step & 1][g][r] = make_float2(yhx, yhy);
+      }
       const bool sv = (step % p.save_every) == 0;
       if (sv) save(step / p.save_every, savecount & 1);
       __syncthreads();
@@ -388,17 +586,36 @@ __global__ void __launch_bounds__(1024) rk4_generic(Rk4P p, int mat_in_smem) {
 }
 
 // ----------------------------------------------------------------- reduce
-__global__ void rk4_reduce_kernel(const double2* __restrict__ partial, int64_t nslots,
-                                  int64_t per, double scale, double2* out) {
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= per) return;
+// out[e] = scale * sum over slots of partial[slot][e]: 32 outputs per CTA
+// (one per lane, coalesced), slots strided over the 8 warps, the 8 partial
+// sums combined in a fixed order (deterministic).
+template <typename P>
+__global__ void __launch_bounds__(256)
+    rk4_reduce_kernel(const P* __restrict__ partial, int64_t nslots, int64_t per, double scale,
+                      double2* out) {
+  __shared__ double2 red[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t e = (int64_t)blockIdx.x * 32 + lane;
   double2 acc = make_double2(0.0, 0.0);
-  for (int64_t sl = 0; sl < nslots; ++sl) acc = cadd(acc, partial[sl * per + e]);
-  out[e] = cscale(acc, scale);
+  if (e < per) {
+    for (int64_t sl = w; sl < nslots; sl += 8) {
+      P v = partial[sl * per + e];
+      acc.x += (double)v.x;
+      acc.y += (double)v.y;
+    }
+  }
+  red[w][lane] = acc;
+  __syncthreads();
+  if (w == 0 && e < per) {
+    double2 t = red[0][lane];
+#pragma unroll
+    for (int i = 1; i < 8; ++i) t = cadd(t, red[i][lane]);
+    out[e] = cscale(t, scale);
+  }
 }
 
 // ------------------------------------------------------------------ plan
-enum Kind { K_SMALL = 0, K_ROWS = 1, K_GENERIC = 2 };
+enum Kind { K_SMALL = 0, K_ROWS = 1, K_GENERIC = 2, K_TILE = 3 };
 
 struct Plan {
   Kind kind;
@@ -416,6 +633,21 @@ static cudaError_t rows_occupancy(int* blocks) {
 }
 
 #define QSX_ROWS_TABLE(X) X(9, 28, 2) X(16, 16, 2) X(25, 10, 2) X(36, 7, 2) X(49, 5, 2) X(64, 4, 1)
+// tile kernel: (T, G samples per CTA, min CTAs per SM); M = T * T
+#define QSX_TILE_TABLE(X) X(3, 10, 2) X(4, 8, 2) X(5, 6, 2) X(6, 5, 2) X(7, 4, 2) X(8, 4, 1)
+
+template <int T, int G, int MINB>
+static cudaError_t tile_occupancy(int* blocks) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, rk4_tile_f32<T, G, MINB>,
+                                                       G * 8 * T, 0);
+}
+
+static bool tile_supported(int m, int* T, int* G) {
+#define X(TT, GG, BB) if (m == TT * TT) { *T = TT; *G = GG; return true; }
+  QSX_TILE_TABLE(X)
+#undef X
+  return false;
+}
 
 static bool rows_supported(int m, int* G) {
 #define X(MM, GG, BB) if (m == MM) { *G = GG; return true; }
@@ -423,6 +655,8 @@ static bool rows_supported(int m, int* G) {
 #undef X
   return false;
 }
+
+static size_t partial_bytes(Kind k) { return k == K_GENERIC ? sizeof(double2) : sizeof(float2); }
 
 static int validate(const qsx_rk4_args* a) {
   QSX_CHECK_ARG(a != nullptr, "qsx_rk4: null args");
@@ -449,11 +683,32 @@ static int make_plan(const qsx_rk4_args* a, Plan* pl) {
   const int m = a->m;
   const int64_t nsave = a->nsteps / a->save_every + 1;
   (void)nsave;
-  if (a->precision == QSX_FP32 && a->form == 0 && m <= 8) {
+  if (a->precision == QSX_FP32 && a->form == 0 && m <= 8 && a->nproj <= LANES_MAXPROJ &&
+      a->nselect <= LANES_MAXPROJ) {
+    const int lps = m == 1 ? 1 : (m == 2 ? 2 : 4);
+    const int64_t threads = a->batch * lps;
     pl->kind = K_SMALL;
     pl->threads = 128;
-    pl->grid = (a->batch + 127) / 128;
+    pl->grid = (threads + 127) / 128;
     pl->nslots = pl->grid * 4;
+    pl->smem = 0;
+    return QSX_OK;
+  }
+  int T = 0;
+  if (a->precision == QSX_FP32 && a->form == 0 && a->nproj == 0 && tile_supported(m, &T, &G)) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+#define X(TT, GG, BB) \
+  if (e == cudaSuccess && T == TT) e = tile_occupancy<TT, GG, BB>(&occ);
+    QSX_TILE_TABLE(X)
+#undef X
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4 plan");
+    pl->kind = K_TILE;
+    pl->threads = G * 8 * T;
+    pl->ngroups = (a->batch + G - 1) / G;
+    pl->grid = std::max<int64_t>(1, std::min<int64_t>(pl->ngroups, (int64_t)sms * std::max(occ, 1)));
+    pl->nslots = pl->ngroups;
     pl->smem = 0;
     return QSX_OK;
   }
@@ -472,7 +727,7 @@ static int make_plan(const qsx_rk4_args* a, Plan* pl) {
       pl->threads = 256;
       pl->ngroups = (a->batch + G - 1) / G;
       pl->grid = std::max<int64_t>(1, std::min<int64_t>(pl->ngroups, (int64_t)sms * std::max(occ, 1)));
-      pl->nslots = pl->grid;
+      pl->nslots = pl->ngroups;
       pl->smem = 0;
       return QSX_OK;
     }
@@ -510,7 +765,7 @@ int qsx_rk4_workspace_bytes(const qsx_rk4_args* a, size_t* bytes) {
   if (st) return st;
   const int64_t nsave = a->nsteps / a->save_every + 1;
   const int64_t nout = a->nproj > 0 ? a->nproj : a->nselect;
-  *bytes = (size_t)pl.nslots * nsave * nout * sizeof(double2);
+  *bytes = (size_t)pl.nslots * nsave * nout * partial_bytes(pl.kind);
   return QSX_OK;
 }
 
@@ -543,19 +798,23 @@ int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
   p.out_state = (double2*)a->out_state;
   p.out_proj = (double2*)a->out_proj;
   p.partial = nullptr;
+  p.partial32 = nullptr;
   p.status = a->status;
   const int64_t per = (int64_t)p.nsave * p.nout;
   if (a->out_mean) {
-    size_t need = (size_t)pl.nslots * per * sizeof(double2);
+    size_t need = (size_t)pl.nslots * per * partial_bytes(pl.kind);
     QSX_CHECK_ARG(a->workspace && a->workspace_bytes >= need,
                   "qsx_rk4_batched: workspace of %zu bytes needed (got %zu)", need,
                   a->workspace_bytes);
-    p.partial = (double2*)a->workspace;
+    if (pl.kind == K_GENERIC)
+      p.partial = (double2*)a->workspace;
+    else
+      p.partial32 = (float2*)a->workspace;
   }
   switch (pl.kind) {
     case K_SMALL: {
       switch (a->m) {
-#define S(MM) case MM: rk4_small_f32<MM><<<(unsigned)pl.grid, pl.threads, 0, s>>>(p); break;
+#define S(MM) case MM: rk4_lanes_f32<MM><<<(unsigned)pl.grid, pl.threads, 0, s>>>(p); break;
         S(1) S(2) S(3) S(4) S(5) S(6) S(7) S(8)
 #undef S
       }
@@ -565,6 +824,14 @@ int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
 #define X(MM, GG, BB) \
   if (a->m == MM) rk4_rows_f32<MM, GG, BB><<<(unsigned)pl.grid, 256, 0, s>>>(p, pl.ngroups);
       QSX_ROWS_TABLE(X)
+#undef X
+      break;
+    }
+    case K_TILE: {
+#define X(TT, GG, BB)                                                               \
+  if (a->m == TT * TT)                                                              \
+    rk4_tile_f32<TT, GG, BB><<<(unsigned)pl.grid, GG * 8 * TT, 0, s>>>(p, pl.ngroups);
+      QSX_TILE_TABLE(X)
 #undef X
       break;
     }
@@ -586,8 +853,13 @@ int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
   }
   QSX_LAUNCH_CHECK("qsx_rk4_batched");
   if (a->out_mean) {
-    rk4_reduce_kernel<<<(unsigned)((per + 255) / 256), 256, 0, s>>>(
-        p.partial, pl.nslots, per, a->mean_scale, (double2*)a->out_mean);
+    const unsigned rg = (unsigned)((per + 31) / 32);
+    if (pl.kind == K_GENERIC)
+      rk4_reduce_kernel<double2><<<rg, 256, 0, s>>>(p.partial, pl.nslots, per, a->mean_scale,
+                                                    (double2*)a->out_mean);
+    else
+      rk4_reduce_kernel<float2><<<rg, 256, 0, s>>>(p.partial32, pl.nslots, per,
+                                                   a->mean_scale, (double2*)a->out_mean);
     QSX_LAUNCH_CHECK("qsx_rk4_batched reduce");
   }
   return QSX_OK;

@@ -92,9 +92,10 @@ class LinearMap:
     operators expose; numpy inputs give numpy outputs.
     """
 
-    def __init__(self, matrix):
+    def __init__(self, matrix, scalar=False):
         self.matrix = torch.as_tensor(np.asarray(matrix, dtype=complex),
                                       device=_device())
+        self.scalar = scalar  # one output row returned as a scalar (expectation)
 
     @property
     def shape(self):
@@ -103,6 +104,8 @@ class LinearMap:
     def __call__(self, state):
         x, is_tensor = _as_device(state)
         y = x @ self.matrix.T
+        if self.scalar:
+            y = y[..., 0]
         return y if is_tensor else y.cpu().numpy()
 
     dot = __call__
@@ -151,9 +154,9 @@ class LiouvilleSpaceOperator(SystemOperator):
         op = np.asanyarray(self.operator, dtype=complex)
         return matrix_to_bra_vec(op)[self.from_indices]
 
-    def _map(self, key, build):
+    def _map(self, key, build, scalar=False):
         if key not in self._maps:
-            self._maps[key] = LinearMap(build())
+            self._maps[key] = LinearMap(build(), scalar)
         return self._maps[key]
 
     def _left(self):
@@ -178,7 +181,7 @@ class LiouvilleSpaceOperator(SystemOperator):
 
     @property
     def expectation_value(self):
-        return self._map('expect', lambda: self.expectation_row[None, :])
+        return self._map('expect', lambda: self.expectation_row[None, :], scalar=True)
 
 
 class LiouvilleSpaceModel(DynamicalModel):

@@ -58,6 +58,21 @@ class RedfieldBuild:
             self.E, self.U, self.occ, bath, unit_convert, discard_imag_corr,
             site_basis=self.site_ops, matsubara_cutoff=bath.matsubara_cutoff)
 
+    def propagator(self, idx, h, precision=_native.QSX_FP64, transpose=False):
+        """(S, m, m) RK4 propagator D = P - I of the block ``idx`` (m <= 64).
+
+        Site-basis non-secular generators go through the fused kernel (the
+        block is built in shared memory and never stored); other cases build
+        the block first.
+        """
+        if self.site_ops and len(idx) <= 64:
+            idx_t = torch.as_tensor(np.asarray(idx), dtype=torch.int32, device=self.H.device)
+            D = _native.redfield_propagator(self.H, self.G, self.M, self.occ, idx_t,
+                                            self.unit_convert, h, precision, transpose)
+            if D is not None:
+                return D
+        return _native.rk4_propagator(self.block(idx, transpose), h, precision)
+
     def block(self, idx, transpose=False):
         """(S, m, m) complex128 generator on the column-stacked indices ``idx``."""
         idx_np = np.asarray(idx, dtype=np.int64)

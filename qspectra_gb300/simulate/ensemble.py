@@ -78,8 +78,7 @@ def ensemble_linear_signal(model, time_max, ensemble_size, polarization='xx',
         V0 = model.dipole_operator('{}->{}'.format(subs[0], sim), polarization[0], '+')
         V1 = model.dipole_operator('{}->{}'.format(sim, subs[2]), polarization[1], '-')
         v_rho0 = V0.commutator(rho0)
-        LT = build.block(model.liouville_subspace_index(sim), transpose=True)
-        D = _native.rk4_propagator(LT, dt, prec)
+        D = build.propagator(model.liouville_subspace_index(sim), dt, prec, transpose=True)
         y0 = torch.as_tensor(-V1.bra_vector, dtype=torch.complex128).cuda()
         proj = torch.as_tensor(np.asarray(v_rho0)[None, :], dtype=torch.complex128).cuda()
         steps = step_plan(t, 0.0, dt)
@@ -113,8 +112,7 @@ def ensemble_populations(model, initial_state, duration, ensemble_size,
         rho0 = np.outer(rho0.conj(), rho0)
     y0 = model.density_matrix_to_state_vector(rho0, liouville_subspace)
     idx = model.liouville_subspace_index(liouville_subspace)
-    L = build.block(idx, transpose=False)
-    D = _native.rk4_propagator(L, dt, prec)
+    D = build.propagator(idx, dt, prec)
     M = len(idx)
     if full_state:
         select = list(range(M))
@@ -191,14 +189,12 @@ class RedfieldEnsembleWorkload:
         H = self.H_base.expand(S, -1, -1).clone()
         H[:, self.e_idx, self.e_idx] += offsets
         build = self.model.build_batch(H)
-        LT = build.block(self.idx_eg, transpose=True)
-        D_eg = _native.rk4_propagator(LT, self.dt, prec)
+        D_eg = build.propagator(self.idx_eg, self.dt, prec, transpose=True)
         sig = _native.rk4(D_eg, self.y_abs, len(self.t_abs) - 1, 1, proj=self.proj,
                           per_sample=False, mean=True, check_finite=False)
         X = _native.dft(-sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
                         self.model.rw_freq, self.model.unit_convert, 1)
-        L = build.block(self.idx_ee)
-        D_ee = _native.rk4_propagator(L, self.dt, prec)
+        D_ee = build.propagator(self.idx_ee, self.dt, prec)
         if events is not None:
             e0 = torch.cuda.Event(enable_timing=True)
             e0.record()

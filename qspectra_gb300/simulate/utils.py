@@ -126,7 +126,7 @@ def integrate(f, y0, t, t0=None, method_name='rk4', f_params=None,
     if save_func is not None:
         if isinstance(save_func, LinearMap):
             state = state @ save_func.matrix.T
-            if save_func.matrix.shape[0] == 1:
+            if save_func.scalar:
                 state = state[..., 0]
         else:
             raise TypeError('save_func must be a linear operator map')

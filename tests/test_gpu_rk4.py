@@ -50,7 +50,7 @@ def test_kernels_state_and_means(M, B, prec):
         form = 1
     out = _native.rk4(mat, y0t, nsteps, every, form=form, h=h, state=True)
     assert rel_err(out['state'].cpu().numpy(), ref) < tol
-    sel = [0, M - 1, M // 2]
+    sel = sorted(set([0, M - 1, M // 2]))
     out = _native.rk4(mat, y0t, nsteps, every, form=form, h=h, select=sel, mean=True)
     assert rel_err(out['proj'].cpu().numpy(), ref[:, :, sel]) < tol
     assert rel_err(out['mean'].cpu().numpy(), ref[:, :, sel].mean(0)) < tol
@@ -77,7 +77,7 @@ def test_stage_form_matches_propagator_form_fp64():
 def test_zero_steps_and_shared_inputs():
     M = 7
     L = torch.as_tensor(random_generators(1, M, 2)[0]).cuda()
-    y0 = torch.arange(M, dtype=torch.complex128, device='cuda')
+    y0 = torch.arange(M, dtype=torch.float64, device='cuda').to(torch.complex128)
     D = _native.rk4_propagator(L[None], 1.0, _native.QSX_FP32)[0]
     out = _native.rk4(D, y0.expand(5, M).contiguous(), 0, 1, state=True)
     assert torch.allclose(out['state'][:, 0], y0.expand(5, M))
@@ -91,3 +91,20 @@ def test_propagator_is_one_rk4_step():
         hL = 0.7 * L[b]
         P = np.eye(9) + hL + hL @ hL / 2 + hL @ hL @ hL / 6 + hL @ hL @ hL @ hL / 24
         assert rel_err(D[b], P - np.eye(9)) < 1e-14
+
+
+def test_fused_redfield_propagator_matches_two_step_path(golden):
+    """qsx_redfield_propagator_batched == liouvillian block + rk4 propagator."""
+    import qspectra_gb300 as qg
+    from qspectra_gb300 import workloads as wl
+    ham = qg.ElectronicHamiltonian(golden['fmo7_H'], bath=qg.DebyeBath(qg.CM_K * 77, 35, 106),
+                                   dipoles=[[1, 0, 0]] * 7, disorder=wl.fwhm_for_sd(80.0))
+    m = qg.RedfieldModel(ham, hilbert_subspace='ge', unit_convert=qg.CM_FS, secular=False)
+    from qspectra_gb300.simulate.ensemble import SampleBatch
+    build = m.build_batch(SampleBatch(m, 37).H('ge'))
+    for sub, tr in [('ee', False), ('eg', True), ('gg,eg,ge,ee', False)]:
+        idx = m.liouville_subspace_index(sub)
+        for prec, tol in [(_native.QSX_FP64, 1e-13), (_native.QSX_FP32, 1e-5)]:
+            fused = build.propagator(idx, 1.0, prec, transpose=tr).cpu().numpy()
+            ref = _native.rk4_propagator(build.block(idx, tr), 1.0, prec).cpu().numpy()
+            assert rel_err(fused, ref) < tol
