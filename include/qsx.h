@@ -128,6 +128,19 @@ int qsx_redfield_propagator_batched(const double* H, int64_t H_stride,
                                     void* stream);
 
 /*
+ * K-step blocked propagator for the time loop: from D = P - I (complex64 or
+ * complex128 [batch][m][m], as qsx_rk4_propagator_batched returns) build
+ * [batch][m + nselect (K - 1)][m]: rows < m hold P^K - I, row
+ * m + (k - 1) nselect + q holds row select[q] of P^k - I (1 <= k < K).
+ * The same RK4 iterates as the step-by-step loop (simulate/utils.py:44-49),
+ * regrouped so qsx_rk4_batched with block_k = K does one matrix-vector pass
+ * per K steps.  m <= 64, K <= 64; select int32 [nselect] (device).
+ */
+int qsx_rk4_block_matrix_batched(const void* D, int m, int64_t batch,
+                                 int precision, int K, const int* select,
+                                 int nselect, void* out, void* stream);
+
+/*
  * RK4 propagator D = P - I with P = sum_{k<=4} (hL)^k / k!, i.e. exactly one
  * classical RK4 step of dy/dt = L y (the step inside the integrate loop,
  * qspectra/simulate/utils.py:44-49, with zvode replaced by RK4).
@@ -159,7 +172,7 @@ typedef struct {
   const double* proj;     /* complex128 [nproj][m] per sample */
   int64_t proj_stride;    /* elements between samples, 0 = shared */
   int32_t nselect;        /* selected state components, 0 = none */
-  int32_t pad0;
+  int32_t block_k;        /* > 1: K-step blocked matrix (see below), else 0 */
   const int32_t* select;  /* int32 [nselect] (device) */
   double* out_state;      /* complex128 [batch][nsave][m] or NULL */
   double* out_proj;       /* complex128 [batch][nsave][nout] or NULL */
@@ -169,7 +182,14 @@ typedef struct {
   size_t workspace_bytes;
   int32_t* status;        /* device int: set to QSX_ERR_NONFINITE on NaN/Inf */
 } qsx_rk4_args;
-/* nsave = nsteps / save_every + 1; nout = nproj if nproj > 0 else nselect. */
+/* nsave = nsteps / save_every + 1; nout = nproj if nproj > 0 else nselect.
+ *
+ * K-step blocking (block_k = K > 1): `matrix` holds, per sample, the
+ * (m + nselect (K - 1)) x m output of qsx_rk4_block_matrix_batched and one
+ * matrix-vector pass advances K RK4 steps while still producing the selected
+ * components at every step (same iterates y_{n+1} = P y_n, regrouped).
+ * Needs QSX_FP32, form 0, nselect outputs only, save_every 1, no out_state,
+ * nsteps % K == 0 and m in {9, 16, 25, 36, 49, 64}. */
 
 /* sizeof(qsx_rk4_args) as compiled into the library, for FFI bindings to
  * check their struct declaration against. */

@@ -41,7 +41,7 @@ class Rk4Args(ctypes.Structure):
         ('y0', _c_vp), ('y0_stride', ctypes.c_int64),
         ('save_every', ctypes.c_int32), ('nproj', ctypes.c_int32),
         ('proj', _c_vp), ('proj_stride', ctypes.c_int64),
-        ('nselect', ctypes.c_int32), ('pad0', ctypes.c_int32),
+        ('nselect', ctypes.c_int32), ('block_k', ctypes.c_int32),
         ('select', _c_vp),
         ('out_state', _c_vp), ('out_proj', _c_vp), ('out_mean', _c_vp),
         ('mean_scale', ctypes.c_double),
@@ -67,6 +67,8 @@ _PROTOS = {
     'qsx_redfield_propagator_batched': (_c_int, [
         _c_vp, _c_i64, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_i64, _c_dbl, _c_vp,
         _c_int, _c_int, _c_dbl, _c_int, _c_vp, _c_vp]),
+    'qsx_rk4_block_matrix_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int,
+                                              _c_vp, _c_int, _c_vp, _c_vp]),
     'qsx_rk4_propagator_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl,
                                             _c_int, _c_vp, _c_vp]),
     'qsx_rk4_args_bytes': (ctypes.c_size_t, []),
@@ -243,9 +245,26 @@ def rk4_propagator(L, h, precision=QSX_FP64):
     return D
 
 
+def rk4_block_matrix(D, K, select):
+    """(B, m + len(select) (K-1), m) K-step blocked matrix from D = P - I."""
+    require_gpu()
+    prec = QSX_FP32 if D.dtype == torch.complex64 else QSX_FP64
+    _need(D, D.dtype, 'D', 3)
+    B, m, _ = D.shape
+    sel_np = np.asarray(select, dtype=np.int64).reshape(-1)
+    if sel_np.size == 0 or sel_np.min() < 0 or sel_np.max() >= m:
+        raise ValueError('select indices must lie in [0, {})'.format(m))
+    sel = torch.as_tensor(sel_np, dtype=torch.int32, device=D.device)
+    out = torch.empty((B, m + sel.numel() * (K - 1), m), dtype=D.dtype, device=D.device)
+    _check(load().qsx_rk4_block_matrix_batched(_p(D), m, B, prec, K, _p(sel), sel.numel(),
+                                               _p(out), _stream()),
+           'qsx_rk4_block_matrix_batched')
+    return out
+
+
 def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
         state=False, proj=None, select=None, per_sample=True, mean=False,
-        check_finite=True, workspace=None):
+        check_finite=True, workspace=None, block_k=0):
     """Batched RK4 time loop (see qsx_rk4_args in include/qsx.h).
 
     matrix: (B, m, m) complex64 (FP32) / complex128 (FP64), or (m, m) shared.
@@ -259,6 +278,7 @@ def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
     want = torch.complex64 if precision == QSX_FP32 else torch.complex128
     _need(matrix, want, 'matrix')
     m = matrix.shape[-1]
+    rows = matrix.shape[-2]
     dev = matrix.device
     y0 = _need(y0.to(torch.complex128).contiguous(), torch.complex128, 'y0')
     B = matrix.shape[0] if matrix.dim() == 3 else (y0.shape[0] if y0.dim() == 2 else 1)
@@ -276,7 +296,8 @@ def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
     a.nsteps = nsteps
     a.batch = B
     a.matrix = matrix.data_ptr()
-    a.matrix_stride = m * m if matrix.dim() == 3 else 0
+    a.matrix_stride = rows * m if matrix.dim() == 3 else 0
+    a.block_k = block_k
     a.h = h
     a.y0 = y0.data_ptr()
     a.y0_stride = m if y0.dim() == 2 else 0

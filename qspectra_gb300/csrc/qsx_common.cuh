@@ -83,6 +83,9 @@ __device__ __forceinline__ void dd_add(float& hi, float& lo, float z) {
   lo = e - (hi - s);
 }
 
+__host__ __device__ __forceinline__ float2 cadd2(float2 a, float2 b) { return cmk(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ double2 cadd2(double2 a, double2 b) { return cmk(a.x + b.x, a.y + b.y); }
+
 __device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 
 }  // namespace qsx

@@ -379,73 +379,69 @@ __global__ void liouvillian_kernel(const double* __restrict__ H, int64_t H_strid
 }
 
 // ------------------------------------------------ RK4 one-step propagator
-// D = h L (I + hL/2 (I + hL/3 (I + hL/4))), Horner form of P - I.  sL holds
-// L on entry; sX, sY are m x m scratch tiles; D receives the result.
+// C = A * B for m x m complex tiles in shared memory.  Each thread owns a 4 x 4
+// block of C (8 shared loads per 16 complex MACs); `store(e, acc)` writes the
+// result element e = row * m + col.
+template <typename C, typename Store>
+__device__ __forceinline__ void smem_cgemm(const C* __restrict__ A, const C* __restrict__ B,
+                                           int m, Store store) {
+  using T = decltype(A[0].x);
+  const int nb = (m + 3) / 4;
+  for (int blk = threadIdx.x; blk < nb * nb; blk += blockDim.x) {
+    const int r0 = (blk / nb) * 4, c0 = (blk % nb) * 4;
+    C acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = cmk((T)0, (T)0);
+    for (int k = 0; k < m; ++k) {
+      C a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = (r0 + i < m) ? A[(r0 + i) * m + k] : cmk((T)0, (T)0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = (c0 + j < m) ? B[k * m + c0 + j] : cmk((T)0, (T)0);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], b[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (r0 + i < m && c0 + j < m) store((r0 + i) * m + c0 + j, acc[i][j]);
+  }
+}
+
+// D = P - I for one RK4 step, P = sum_{k<=4} A^k / k!, A = h L, evaluated
+// Paterson-Stockmeyer style with two products:
+//   A2 = A A,   D = A + A2 / 2 + A2 (A / 6 + A2 / 24).
+// On entry sA holds L; sA, sB, sC are m x m shared tiles.
 template <typename T>
-__device__ void horner_propagator(typename cplx<T>::type* sL, typename cplx<T>::type* sX,
-                                  typename cplx<T>::type* sY, int m, double h,
-                                  typename cplx<T>::type* D) {
+__device__ void rk4_polynomial(typename cplx<T>::type* sA, typename cplx<T>::type* sB,
+                               typename cplx<T>::type* sC, int m, double h,
+                               typename cplx<T>::type* D) {
   using C = typename cplx<T>::type;
   const int mm = m * m;
-  for (int e = threadIdx.x; e < mm; e += blockDim.x) {
-    int r = e / m, c = e % m;
-    T s = (T)(h / 4.0);
-    C v = sL[e];
-    sX[e] = cmk((T)(r == c ? 1 : 0) + s * v.x, s * v.y);
-  }
+  const T ht = (T)h;
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) sA[e] = cmk(ht * sA[e].x, ht * sA[e].y);
   __syncthreads();
-  const T coef[3] = {(T)(h / 3.0), (T)(h / 2.0), (T)h};
-  for (int stage = 0; stage < 3; ++stage) {
-    for (int e = threadIdx.x; e < mm; e += blockDim.x) {
-      int r = e / m, c = e % m;
-      C acc = cmk((T)0, (T)0);
-      for (int k = 0; k < m; ++k) cfma(acc, sL[r * m + k], sX[k * m + c]);
-      sY[e] = acc;
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < mm; e += blockDim.x) {
-      int r = e / m, c = e % m;
-      C y = sY[e];
-      if (stage < 2)
-        sX[e] = cmk((T)(r == c ? 1 : 0) + coef[stage] * y.x, coef[stage] * y.y);
-      else
-        D[e] = cmk(coef[2] * y.x, coef[2] * y.y);
-    }
-    __syncthreads();
-  }
+  smem_cgemm(sA, sA, m, [&](int e, C v) { sB[e] = v; });  // A2
+  __syncthreads();
+  const T c6 = (T)(1.0 / 6.0), c24 = (T)(1.0 / 24.0), c2 = (T)0.5;
+  for (int e = threadIdx.x; e < mm; e += blockDim.x)
+    sC[e] = cmk(c6 * sA[e].x + c24 * sB[e].x, c6 * sA[e].y + c24 * sB[e].y);
+  __syncthreads();
+  smem_cgemm(sB, sC, m, [&](int e, C z) {
+    D[e] = cmk(sA[e].x + c2 * sB[e].x + z.x, sA[e].y + c2 * sB[e].y + z.y);
+  });
 }
 
-// One site-basis Redfield generator element (the K == NULL branch of
-// liouvillian_kernel): -i uc (H_ac d_bd - d_ac H_db) - R_abcd with
-// R_abcd = d_bd G_ac + d_ac conj(G_bd) - d_ac sum_i occ_ia conj(M_i,bd)
-//          - d_bd sum_i occ_ib M_i,ac.
-__device__ __forceinline__ double2 site_generator_element(const double* h, const double2* g,
-                                                          const double2* mm, const double* occ,
-                                                          int n, int n_sites, double uc,
-                                                          int a, int bb, int c, int d) {
-  const int nn = n * n;
-  double hre = 0.0;
-  if (bb == d) hre += h[a * n + c];
-  if (a == c) hre -= h[d * n + bb];
-  double2 R = cmk(0.0, 0.0);
-  if (bb == d) {
-    R = cadd(R, g[a * n + c]);
-    for (int i = 0; i < n_sites; ++i) {
-      double o = occ[i * n + bb];
-      if (o != 0.0) R = csub(R, cscale(mm[i * nn + a * n + c], o));
-    }
-  }
-  if (a == c) {
-    R = cadd(R, cconj(g[bb * n + d]));
-    for (int i = 0; i < n_sites; ++i) {
-      double o = occ[i * n + a];
-      if (o != 0.0) R = csub(R, cscale(cconj(mm[i * nn + bb * n + d]), o));
-    }
-  }
-  return csub(cmk(0.0, -uc * hre), R);
-}
-
-// Fused: site-basis generator block -> shared memory -> Horner propagator.
+// Fused: site-basis generator block -> shared memory -> RK4 polynomial.
+// The block is assembled from the per-state operators
+//   B[s] = G - sum_i occ_is M_i,
+//   L[(a,b),(c,d)] = d_bd (-B[b]_ac - i uc H_ac) + d_ac (-conj(B[a]_bd) + i uc H_db),
+// which is the K == NULL branch of liouvillian_kernel regrouped.
 template <typename T>
 __global__ void __launch_bounds__(256)
     redfield_propagator_kernel(const double* __restrict__ H, int64_t H_stride,
@@ -456,39 +452,52 @@ __global__ void __launch_bounds__(256)
   using C = typename cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int nn = n * n;
-  double2* sG = (double2*)smraw;
-  double2* sM = sG + nn;
-  double* sH = (double*)(sM + (size_t)n_sites * nn);
-  double* sOcc = sH + nn;
-  int* sIdx = (int*)(sOcc + n_sites * n);
-  size_t off = (size_t)((unsigned char*)(sIdx + m) - smraw);
-  off = (off + 15) & ~(size_t)15;
-  C* sL = (C*)(smraw + off);
+  C* sB = (C*)smraw;                  // n * n * n
+  C* sHs = sB + (size_t)n * nn;       // n * n, i * uc * H stored as (0, uc H)
+  C* sL = sHs + nn;                   // m * m
   C* sX = sL + m * m;
   C* sY = sX + m * m;
+  int* sIdx = (int*)(sY + m * m);     // m
   const int64_t b = blockIdx.x;
-  for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-    sG[e] = G[b * nn + e];
-    sH[e] = H[b * H_stride + e];
+  const double2* g = G + b * nn;
+  const double2* mo = Mo + b * (int64_t)n_sites * nn;
+  for (int e = threadIdx.x; e < n * nn; e += blockDim.x) {
+    const int st = e / nn, xy = e % nn;
+    double2 v = g[xy];
+    for (int i = 0; i < n_sites; ++i) {
+      const double o = occ[i * n + st];
+      if (o != 0.0) v = csub(v, cscale(mo[i * nn + xy], o));
+    }
+    sB[e] = cmk((T)v.x, (T)v.y);
   }
-  for (int e = threadIdx.x; e < n_sites * nn; e += blockDim.x) sM[e] = Mo[b * n_sites * nn + e];
-  for (int e = threadIdx.x; e < n_sites * n; e += blockDim.x) sOcc[e] = occ[e];
+  for (int e = threadIdx.x; e < nn; e += blockDim.x) sHs[e] = cmk((T)0, (T)(uc * H[b * H_stride + e]));
   for (int e = threadIdx.x; e < m; e += blockDim.x) {
-    int v = idx[e];
+    const int v = idx[e];
     sIdx[e] = (v >= 0 && v < nn) ? v : -1;
   }
   __syncthreads();
   for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
     int r = e / m, cc = e % m;
-    if (transpose) { int t = r; r = cc; cc = t; }
+    if (transpose) { const int t = r; r = cc; cc = t; }
     const int ir = sIdx[r], ic = sIdx[cc];
-    double2 v = cmk(nan(""), nan(""));
-    if (ir >= 0 && ic >= 0)
-      v = site_generator_element(sH, sG, sM, sOcc, n, n_sites, uc, ir % n, ir / n, ic % n, ic / n);
-    sL[e] = cmk((T)v.x, (T)v.y);
+    C v = cmk((T)0, (T)0);
+    if (ir < 0 || ic < 0) {
+      v = cmk((T)nan(""), (T)nan(""));
+    } else {
+      const int a = ir % n, bb = ir / n, c = ic % n, d = ic / n;
+      if (bb == d) {  // -B[b]_ac - i uc H_ac
+        const C x = sB[bb * nn + a * n + c], hh = sHs[a * n + c];
+        v = cmk(v.x - x.x - hh.x, v.y - x.y - hh.y);
+      }
+      if (a == c) {  // -conj(B[a]_bd) + i uc H_db
+        const C x = sB[a * nn + bb * n + d], hh = sHs[d * n + bb];
+        v = cmk(v.x - x.x + hh.x, v.y + x.y + hh.y);
+      }
+    }
+    sL[e] = v;
   }
   __syncthreads();
-  horner_propagator<T>(sL, sX, sY, m, h, D + b * (int64_t)m * m);
+  rk4_polynomial<T>(sL, sX, sY, m, h, D + b * (int64_t)m * m);
 }
 
 template <typename T>
@@ -496,7 +505,7 @@ __global__ void __launch_bounds__(256)
     propagator_kernel(const double2* __restrict__ L, int m, double h,
                       typename cplx<T>::type* D) {
   using C = typename cplx<T>::type;
-  extern __shared__ unsigned char smraw[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   C* sL = (C*)smraw;
   C* sX = sL + m * m;
   C* sY = sX + m * m;
@@ -508,7 +517,86 @@ __global__ void __launch_bounds__(256)
     sL[e] = cmk((T)v.x, (T)v.y);
   }
   __syncthreads();
-  horner_propagator<T>(sL, sX, sY, m, h, D + b * mm);
+  rk4_polynomial<T>(sL, sX, sY, m, h, D + b * mm);
+}
+
+// ------------------------------------------- K-step blocked propagators
+// From D = P - I (one RK4 step) build, per sample, the (m + nsel (K-1)) x m
+// matrix whose first m rows are D_K = P^K - I and whose row m + (k-1) nsel + q
+// is row select[q] of D_k = P^k - I (k = 1 .. K-1).  D_K comes from binary
+// powering with (I + X)(I + Y) = I + X + Y + X Y; the selected rows follow
+// R_{k+1} = R_k + R_1 + R_k D.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    block_matrix_kernel(const typename cplx<T>::type* __restrict__ D, int m, int K,
+                        const int* __restrict__ sel, int nsel,
+                        typename cplx<T>::type* __restrict__ out) {
+  using C = typename cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int mm = m * m;
+  C* sD = (C*)smraw;  // D
+  C* sBase = sD + mm;
+  C* sRes = sBase + mm;
+  C* sTmp = sRes + mm;
+  C* sR = sTmp + mm;              // current selected rows R_k  [nsel][m]
+  C* sR2 = sR + nsel * m;          // next selected rows
+  const int64_t b = blockIdx.x;
+  const int rows = m + nsel * (K - 1);
+  const C* d = D + b * mm;
+  C* o = out + b * (int64_t)rows * m;
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) {
+    sD[e] = d[e];
+    sBase[e] = d[e];
+  }
+  for (int e = threadIdx.x; e < nsel * m; e += blockDim.x) {
+    const int q = e / m, c = e % m;
+    int r = sel[q];
+    r = (r >= 0 && r < m) ? r : 0;
+    sR[e] = d[r * m + c];
+    if (K > 1) o[(int64_t)(m + q) * m + c] = d[r * m + c];
+  }
+  __syncthreads();
+  // selected rows of D_2 .. D_{K-1}
+  for (int k = 2; k < K; ++k) {
+    for (int e = threadIdx.x; e < nsel * m; e += blockDim.x) {
+      const int q = e / m, c = e % m;
+      int r = sel[q];
+      r = (r >= 0 && r < m) ? r : 0;
+      C acc = cadd2(sR[e], sD[r * m + c]);
+      for (int j = 0; j < m; ++j) cfma(acc, sR[q * m + j], sD[j * m + c]);
+      sR2[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nsel * m; e += blockDim.x) {
+      sR[e] = sR2[e];
+      o[(int64_t)(m + (k - 1) * nsel + e / m) * m + e % m] = sR2[e];
+    }
+    __syncthreads();
+  }
+  // D_K by binary powering
+  bool have = false;
+  for (int kk = K; kk > 0; kk >>= 1) {
+    if (kk & 1) {
+      if (!have) {
+        for (int e = threadIdx.x; e < mm; e += blockDim.x) sRes[e] = sBase[e];
+        have = true;
+      } else {
+        smem_cgemm(sRes, sBase, m, [&](int e, C v) { sTmp[e] = v; });
+        __syncthreads();
+        for (int e = threadIdx.x; e < mm; e += blockDim.x)
+          sRes[e] = cadd2(cadd2(sRes[e], sBase[e]), sTmp[e]);
+      }
+      __syncthreads();
+    }
+    if (kk > 1) {
+      smem_cgemm(sBase, sBase, m, [&](int e, C v) { sTmp[e] = v; });
+      __syncthreads();
+      for (int e = threadIdx.x; e < mm; e += blockDim.x)
+        sBase[e] = cadd2(cadd2(sBase[e], sBase[e]), sTmp[e]);
+      __syncthreads();
+    }
+  }
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) o[e] = sRes[e];
 }
 
 }  // namespace qsx
@@ -596,7 +684,9 @@ int qsx_redfield_operators_batched(const double* E, const double* U, int n,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_operators_batched");
-  redfield_operators_kernel<<<(unsigned)batch, 256, smem, (cudaStream_t)stream>>>(
+  // one thread per matrix element (n^2 <= 1024), rounded to whole warps
+  const int threads = std::min(256, (int)((nn + 31) / 32) * 32);
+  redfield_operators_kernel<<<(unsigned)batch, threads, smem, (cudaStream_t)stream>>>(
       E, U, n, batch, occ, n_sites, p, unit_convert, site_basis, (double2*)G,
       (double2*)M, K);
   QSX_LAUNCH_CHECK("qsx_redfield_operators_batched");
@@ -641,11 +731,8 @@ int qsx_redfield_propagator_batched(const double* H, int64_t H_stride, const dou
   QSX_CHECK_ARG(H && G && M && occ && idx && D,
                 "qsx_redfield_propagator_batched: null pointer");
   const size_t nn = (size_t)n * n;
-  size_t head = (nn + (size_t)n_sites * nn) * sizeof(double2) +
-                (nn + (size_t)n_sites * n) * sizeof(double) + (size_t)m * sizeof(int);
-  head = (head + 15) & ~(size_t)15;
   const size_t cs = precision == QSX_FP32 ? sizeof(float2) : sizeof(double2);
-  const size_t smem = head + 3 * (size_t)m * m * cs;
+  const size_t smem = ((size_t)n * nn + nn + 3 * (size_t)m * m) * cs + (size_t)m * sizeof(int);
   if (smem > 227 * 1024) {
     set_error("qsx_redfield_propagator_batched: %zu bytes of shared memory needed; use "
               "qsx_redfield_liouvillian_batched + qsx_rk4_propagator_batched", smem);
@@ -669,6 +756,41 @@ int qsx_redfield_propagator_batched(const double* H, int64_t H_stride, const dou
         transpose, h, (double2*)D);
   }
   QSX_LAUNCH_CHECK("qsx_redfield_propagator_batched");
+  return QSX_OK;
+}
+
+int qsx_rk4_block_matrix_batched(const void* D, int m, int64_t batch, int precision, int K,
+                                 const int* select, int nselect, void* out, void* stream) {
+  QSX_CHECK_ARG(m >= 1 && m <= 64 && K >= 1 && K <= 64 && nselect >= 0 && nselect <= m,
+                "qsx_rk4_block_matrix_batched: need m <= 64, 1 <= K <= 64, nselect <= m");
+  QSX_CHECK_ARG(batch >= 0 && batch <= 0x7fffffff, "qsx_rk4_block_matrix_batched: bad batch");
+  QSX_CHECK_ARG(precision == QSX_FP32 || precision == QSX_FP64,
+                "qsx_rk4_block_matrix_batched: bad precision");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(D && out && (nselect == 0 || select),
+                "qsx_rk4_block_matrix_batched: null pointer");
+  const size_t cs = precision == QSX_FP32 ? sizeof(float2) : sizeof(double2);
+  const size_t smem = (4 * (size_t)m * m + 2 * (size_t)nselect * m) * cs;
+  if (smem > 227 * 1024) {
+    set_error("qsx_rk4_block_matrix_batched: %zu bytes of shared memory needed", smem);
+    return QSX_ERR_UNSUPPORTED;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e;
+  if (precision == QSX_FP32) {
+    e = cudaFuncSetAttribute(block_matrix_kernel<float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_block_matrix_batched");
+    block_matrix_kernel<float><<<(unsigned)batch, 256, smem, s>>>((const float2*)D, m, K, select,
+                                                                 nselect, (float2*)out);
+  } else {
+    e = cudaFuncSetAttribute(block_matrix_kernel<double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_block_matrix_batched");
+    block_matrix_kernel<double><<<(unsigned)batch, 256, smem, s>>>(
+        (const double2*)D, m, K, select, nselect, (double2*)out);
+  }
+  QSX_LAUNCH_CHECK("qsx_rk4_block_matrix_batched");
   return QSX_OK;
 }
 

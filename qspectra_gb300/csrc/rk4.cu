@@ -277,142 +277,112 @@ __global__ void __launch_bounds__(256, MINB) rk4_rows_f32(Rk4P p, int64_t ngroup
   }
 }
 
-// ------------------------------------------------------ tiles (ee, M = T^2)
-// rk4_tile_f32<T, G>: the state dimension is M = T*T.  Each sample uses T
-// row-groups of 8 lanes; lane ct < T of row-group rt holds the T x T tile
-// D[rt*T + i][ct*T + j] in registers and reads only the T state values of its
-// column tile.  The 8 lanes then sum their partial rows with a 3-level
-// shuffle reduce-scatter (4 + 2 + 1 complex exchanges), after which lane ct
-// owns row rt*T + ct: it updates that state component (split-word FP32) and
-// publishes it for the next step.  One barrier per step.
-template <int T>
-__host__ __device__ constexpr int tile_stride() {
-  // odd float2 stride: the T column tiles of two samples sharing a warp fall
-  // in distinct banks
-  return (T * T) % 2 ? T * T : T * T + 1;
-}
-
-template <int T, int G, int MINB>
-__global__ void __launch_bounds__(G * 8 * T, MINB) rk4_tile_f32(Rk4P p, int64_t ngroups) {
-  constexpr int M = T * T;
-  constexpr int ST = tile_stride<T>();
-  __shared__ __align__(16) float2 ybuf[2][G][ST];
-  __shared__ float2 stash[2][G][M];
+// ---------------------------------------------------- K-step blocked rows
+// rk4_block_f32<M>: the matrix of each sample has RT = M + nsel (K-1) rows
+// (qsx_rk4_block_matrix_batched): rows < M hold D_K = P^K - I, row
+// M + (k-1) nsel + q holds row select[q] of D_k.  One pass of the same
+// row-per-thread matrix-vector product as rk4_rows_f32 then advances the
+// state by K RK4 steps (main rows, split-word FP32) and yields the selected
+// components at the K - 1 intermediate steps (extra rows: y[sel] + z).
+// Outputs every step; ensemble partial sums per group as in rk4_rows_f32.
+template <int M>
+__global__ void __launch_bounds__(256, 2) rk4_block_f32(Rk4P p, int64_t ngroups, int G, int K) {
+  constexpr int ST = rows_stride(M);
+  constexpr int MP = (M % 2) ? M + 1 : M;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2* ybuf = (float2*)smraw;             // [2][G][ST]
+  float2* stash = ybuf + 2 * G * ST;         // [2][K][G][nsel]
+  const int nsel = p.nselect;
+  const int RT = M + nsel * (K - 1);
   const int tid = threadIdx.x;
-  const int g = tid / (8 * T);
-  const int w = tid % (8 * T);
-  const int rt = w / 8, ct = w % 8;
-  const bool tile = ct < T;        // holds a tile and owns row rt*T + ct
-  const int r = rt * T + ct;       // owned row (valid when tile)
-  const unsigned lane = tid & 31;
-  const unsigned gmask = 0xffu << (lane & 24u);  // this row-group's 8 lanes
-  int myq = -1;
-  if (tile)
-    for (int q = 0; q < p.nout; ++q)
+  const int g = tid / RT, r = tid % RT;
+  const bool active = tid < G * RT;
+  const bool main_row = active && r < M;
+  const int kx = main_row ? K : (r - M) / nsel + 1;  // step offset this row yields
+  const int qx = main_row ? -1 : (r - M) % nsel;
+  int myq = -1;  // main rows: the select slot this row fills at offset K
+  if (main_row)
+    for (int q = 0; q < nsel; ++q)
       if (p.select[q] == r) { myq = q; break; }
-  int savecount = 0;
+  const int selr = (active && !main_row) ? p.select[qx] : 0;
+  for (int e = tid; e < 2 * G * ST; e += blockDim.x) ybuf[e] = make_float2(0.f, 0.f);
+  __syncthreads();
+  auto stash_at = [&](int par, int k, int gg, int q) -> float2& {
+    return stash[((par * K + k) * G + gg) * nsel + q];
+  };
+  int parity = 0;
   for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
     const int64_t s = grp * G + g;
-    const bool svalid = s < p.batch;
-    const bool valid = tile && svalid;
-    float2 Dt[T][T];
-    const float2* dm = (const float2*)p.matrix + (svalid ? s * p.matrix_stride : 0);
+    const bool valid = active && s < p.batch;
+    float2 drow[M];
+    const float2* dm = (const float2*)p.matrix + (valid ? s * p.matrix_stride + (int64_t)r * M : 0);
 #pragma unroll
-    for (int i = 0; i < T; ++i)
-#pragma unroll
-      for (int j = 0; j < T; ++j)
-        Dt[i][j] = valid ? dm[(rt * T + i) * M + ct * T + j] : make_float2(0.f, 0.f);
+    for (int j = 0; j < M; ++j) drow[j] = valid ? dm[j] : make_float2(0.f, 0.f);
     float yhx = 0.f, yhy = 0.f, ylx = 0.f, yly = 0.f;
-    if (valid) {
+    if (valid && main_row) {
       double2 v = p.y0[s * p.y0_stride + r];
       yhx = (float)v.x;
       yhy = (float)v.y;
       ylx = (float)(v.x - (double)yhx);
       yly = (float)(v.y - (double)yhy);
     }
-    if (tile) ybuf[0][g][r] = make_float2(yhx, yhy);
-    __syncthreads();
-    auto save = [&](int k, int par) {
-      if (!tile) return;
-      if (p.out_state && valid)
-        p.out_state[(s * p.nsave + k) * M + r] =
+    if (main_row) ybuf[g * ST + r] = make_float2(yhx, yhy);
+    // step 0: selected components of y0
+    if (myq >= 0) {
+      stash_at(parity, 0, g, myq) = make_float2(yhx, yhy);
+      if (p.out_proj && valid)
+        p.out_proj[(s * p.nsave) * p.nout + myq] =
             make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
-      if (myq >= 0) {
-        if (p.out_proj && valid)
-          p.out_proj[(s * p.nsave + k) * p.nout + myq] =
-              make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
-        if (p.partial32) stash[par][g][myq] = valid ? make_float2(yhx, yhy) : make_float2(0.f, 0.f);
-      }
-    };
-    auto reduce = [&](int k, int par) {
-      if (!p.partial32) return;
-      for (int q = tid; q < p.nout; q += blockDim.x) {
-        float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int gg = 0; gg < G; ++gg) {
-          acc.x += stash[par][gg][q].x;
-          acc.y += stash[par][gg][q].y;
-        }
-        p.partial32[(grp * p.nsave + k) * p.nout + q] = acc;
-      }
-    };
-    save(0, savecount & 1);
-    __syncthreads();
-    reduce(0, savecount & 1);
-    ++savecount;
-    const bool b2 = (ct >> 2) & 1, b1 = (ct >> 1) & 1, b0 = ct & 1;
-    for (int step = 1; step <= p.nsteps; ++step) {
-      const float2* cur = ybuf[(step - 1) & 1][g] + (tile ? ct * T : 0);
-      float zx[8], zy[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) { zx[i] = 0.f; zy[i] = 0.f; }
-      if (tile) {
-#pragma unroll
-        for (int j = 0; j < T; ++j) {
-          const float2 v = cur[j];
-#pragma unroll
-          for (int i = 0; i < T; ++i) {
-            zx[i] = fmaf(Dt[i][j].x, v.x, zx[i]);
-            zx[i] = fmaf(-Dt[i][j].y, v.y, zx[i]);
-            zy[i] = fmaf(Dt[i][j].x, v.y, zy[i]);
-            zy[i] = fmaf(Dt[i][j].y, v.x, zy[i]);
-          }
-        }
-      }
-      // reduce-scatter over the 8 lanes: keep half, send half, three times
-      float kx[4], ky[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float sx = b2 ? zx[k] : zx[4 + k], sy = b2 ? zy[k] : zy[4 + k];
-        const float rx = __shfl_xor_sync(gmask, sx, 4), ry = __shfl_xor_sync(gmask, sy, 4);
-        kx[k] = (b2 ? zx[4 + k] : zx[k]) + rx;
-        ky[k] = (b2 ? zy[4 + k] : zy[k]) + ry;
-      }
-      float mx[2], my[2];
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const float sx = b1 ? kx[k] : kx[2 + k], sy = b1 ? ky[k] : ky[2 + k];
-        const float rx = __shfl_xor_sync(gmask, sx, 2), ry = __shfl_xor_sync(gmask, sy, 2);
-        mx[k] = (b1 ? kx[2 + k] : kx[k]) + rx;
-        my[k] = (b1 ? ky[2 + k] : ky[k]) + ry;
-      }
-      const float sx = b0 ? mx[0] : mx[1], sy = b0 ? my[0] : my[1];
-      const float rx = __shfl_xor_sync(gmask, sx, 1), ry = __shfl_xor_sync(gmask, sy, 1);
-      const float zfx = (b0 ? mx[1] : mx[0]) + rx, zfy = (b0 ? my[1] : my[0]) + ry;
-      if (tile) {
-        dd_add(yhx, ylx, zfx);
-        dd_add(yhy, yly, zfy);
-        ybuf[step & 1][g][r] = make_float2(yhx, yhy);
-      }
-      const bool sv = (step % p.save_every) == 0;
-      if (sv) save(step / p.save_every, savecount & 1);
-      __syncthreads();
-      if (sv) {
-        reduce(step / p.save_every, savecount & 1);
-        ++savecount;
-      }
     }
-    if (valid && p.status && !(isfinite(yhx) && isfinite(yhy))) atomicOr(p.status, QSX_ERR_NONFINITE);
+    __syncthreads();
+    if (p.partial32)
+      for (int q = tid; q < nsel; q += blockDim.x) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int gg = 0; gg < G; ++gg) acc = cadd2(acc, stash_at(parity, 0, gg, q));
+        p.partial32[(grp * p.nsave) * p.nout + q] = acc;
+      }
+    parity ^= 1;
+    const int nblk = p.nsteps / K;
+    for (int bs = 0; bs < nblk; ++bs) {
+      const float2* cur = ybuf + ((bs & 1) * G + (active ? g : 0)) * ST;
+      float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < MP; j += 2) {
+        const float4 v = *reinterpret_cast<const float4*>(&cur[j]);
+        cfma(a0, drow[j], make_float2(v.x, v.y));
+        if (j + 1 < M) cfma(a1, drow[j + 1], make_float2(v.z, v.w));
+      }
+      const int step0 = bs * K;
+      if (main_row) {
+        dd_add(yhx, ylx, a0.x + a1.x);
+        dd_add(yhy, yly, a0.y + a1.y);
+        ybuf[(((bs + 1) & 1) * G + g) * ST + r] = make_float2(yhx, yhy);
+        if (myq >= 0) {
+          stash_at(parity, K - 1, g, myq) = valid ? make_float2(yhx, yhy) : make_float2(0.f, 0.f);
+          if (p.out_proj && valid)
+            p.out_proj[(s * p.nsave + step0 + K) * p.nout + myq] =
+                make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
+        }
+      } else if (active) {
+        const float2 base = cur[selr];
+        const float2 v = valid ? make_float2(base.x + a0.x + a1.x, base.y + a0.y + a1.y)
+                               : make_float2(0.f, 0.f);
+        stash_at(parity, kx - 1, g, qx) = v;
+        if (p.out_proj && valid)
+          p.out_proj[(s * p.nsave + step0 + kx) * p.nout + qx] = make_double2(v.x, v.y);
+      }
+      __syncthreads();
+      if (p.partial32)
+        for (int e = tid; e < K * nsel; e += blockDim.x) {
+          const int k = e / nsel, q = e % nsel;
+          float2 acc = make_float2(0.f, 0.f);
+          for (int gg = 0; gg < G; ++gg) acc = cadd2(acc, stash_at(parity, k, gg, q));
+          p.partial32[(grp * p.nsave + step0 + k + 1) * p.nout + q] = acc;
+        }
+      parity ^= 1;
+    }
+    if (valid && main_row && p.status && !(isfinite(yhx) && isfinite(yhy)))
+      atomicOr(p.status, QSX_ERR_NONFINITE);
     __syncthreads();
   }
 }
@@ -615,10 +585,11 @@ __global__ void __launch_bounds__(256)
 }
 
 // ------------------------------------------------------------------ plan
-enum Kind { K_SMALL = 0, K_ROWS = 1, K_GENERIC = 2, K_TILE = 3 };
+enum Kind { K_SMALL = 0, K_ROWS = 1, K_GENERIC = 2, K_BLOCK = 3 };
 
 struct Plan {
   Kind kind;
+  int G;
   int64_t nslots;
   int64_t grid;
   int threads;
@@ -633,22 +604,6 @@ static cudaError_t rows_occupancy(int* blocks) {
 }
 
 #define QSX_ROWS_TABLE(X) X(9, 28, 2) X(16, 16, 2) X(25, 10, 2) X(36, 7, 2) X(49, 5, 2) X(64, 4, 1)
-// tile kernel: (T, G samples per CTA, min CTAs per SM); M = T * T
-#define QSX_TILE_TABLE(X) X(3, 10, 2) X(4, 8, 2) X(5, 6, 2) X(6, 5, 2) X(7, 4, 2) X(8, 4, 1)
-
-template <int T, int G, int MINB>
-static cudaError_t tile_occupancy(int* blocks) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, rk4_tile_f32<T, G, MINB>,
-                                                       G * 8 * T, 0);
-}
-
-static bool tile_supported(int m, int* T, int* G) {
-#define X(TT, GG, BB) if (m == TT * TT) { *T = TT; *G = GG; return true; }
-  QSX_TILE_TABLE(X)
-#undef X
-  return false;
-}
-
 static bool rows_supported(int m, int* G) {
 #define X(MM, GG, BB) if (m == MM) { *G = GG; return true; }
   QSX_ROWS_TABLE(X)
@@ -668,6 +623,7 @@ static int validate(const qsx_rk4_args* a) {
                 "qsx_rk4: nsteps must be a non-negative multiple of save_every");
   QSX_CHECK_ARG(a->batch >= 0 && a->batch <= 0x7fffffffLL, "qsx_rk4: bad batch");
   QSX_CHECK_ARG(!(a->nproj > 0 && a->nselect > 0), "qsx_rk4: use proj or select, not both");
+  QSX_CHECK_ARG(a->block_k >= 0 && a->block_k <= 64, "qsx_rk4: block_k must be in [0, 64]");
   QSX_CHECK_ARG(a->nproj >= 0 && a->nproj <= 64 && a->nselect >= 0 && a->nselect <= a->m,
                 "qsx_rk4: bad nproj/nselect");
   QSX_CHECK_ARG(a->nproj == 0 || a->proj, "qsx_rk4: proj is null");
@@ -681,6 +637,37 @@ static int validate(const qsx_rk4_args* a) {
 static int make_plan(const qsx_rk4_args* a, Plan* pl) {
   int G = 0;
   const int m = a->m;
+  if (a->block_k > 1) {
+    // K-step blocked rows kernel (matrix from qsx_rk4_block_matrix_batched)
+    const int K = a->block_k;
+    QSX_CHECK_ARG(a->precision == QSX_FP32 && a->form == 0 && a->nproj == 0 &&
+                      a->nselect >= 1 && a->save_every == 1 && a->out_state == nullptr &&
+                      a->nsteps % K == 0 && rows_supported(m, &G),
+                  "qsx_rk4: block_k needs FP32, form 0, select outputs only, save_every 1, "
+                  "nsteps %% block_k == 0 and m in {9,16,25,36,49,64}");
+    const int RT = m + a->nselect * (K - 1);
+    QSX_CHECK_ARG(RT <= 256, "qsx_rk4: block_k rows per sample exceed 256");
+    G = std::max(1, 256 / RT);
+    int dev = 0, sms = 0, occ = 0;
+    pl->smem = (2 * (size_t)G * 66 + 2 * (size_t)K * G * a->nselect) * sizeof(float2);
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = ((G * RT + 31) / 32) * 32;
+#define X(MM, GG, BB)                                                                    \
+  if (e == cudaSuccess && m == MM)                                                       \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rk4_block_f32<MM>, threads, \
+                                                      pl->smem);
+    QSX_ROWS_TABLE(X)
+#undef X
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4 plan");
+    pl->kind = K_BLOCK;
+    pl->G = G;
+    pl->threads = threads;
+    pl->ngroups = (a->batch + G - 1) / G;
+    pl->grid = std::max<int64_t>(1, std::min<int64_t>(pl->ngroups, (int64_t)sms * std::max(occ, 1)));
+    pl->nslots = pl->ngroups;
+    return QSX_OK;
+  }
   const int64_t nsave = a->nsteps / a->save_every + 1;
   (void)nsave;
   if (a->precision == QSX_FP32 && a->form == 0 && m <= 8 && a->nproj <= LANES_MAXPROJ &&
@@ -691,24 +678,6 @@ static int make_plan(const qsx_rk4_args* a, Plan* pl) {
     pl->threads = 128;
     pl->grid = (threads + 127) / 128;
     pl->nslots = pl->grid * 4;
-    pl->smem = 0;
-    return QSX_OK;
-  }
-  int T = 0;
-  if (a->precision == QSX_FP32 && a->form == 0 && a->nproj == 0 && tile_supported(m, &T, &G)) {
-    int dev = 0, sms = 0, occ = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-#define X(TT, GG, BB) \
-  if (e == cudaSuccess && T == TT) e = tile_occupancy<TT, GG, BB>(&occ);
-    QSX_TILE_TABLE(X)
-#undef X
-    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4 plan");
-    pl->kind = K_TILE;
-    pl->threads = G * 8 * T;
-    pl->ngroups = (a->batch + G - 1) / G;
-    pl->grid = std::max<int64_t>(1, std::min<int64_t>(pl->ngroups, (int64_t)sms * std::max(occ, 1)));
-    pl->nslots = pl->ngroups;
     pl->smem = 0;
     return QSX_OK;
   }
@@ -827,11 +796,12 @@ int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
 #undef X
       break;
     }
-    case K_TILE: {
-#define X(TT, GG, BB)                                                               \
-  if (a->m == TT * TT)                                                              \
-    rk4_tile_f32<TT, GG, BB><<<(unsigned)pl.grid, GG * 8 * TT, 0, s>>>(p, pl.ngroups);
-      QSX_TILE_TABLE(X)
+    case K_BLOCK: {
+#define X(MM, GG, BB)                                                                   \
+  if (a->m == MM)                                                                       \
+    rk4_block_f32<MM><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(p, pl.ngroups, pl.G, \
+                                                                    a->block_k);
+      QSX_ROWS_TABLE(X)
 #undef X
       break;
     }

@@ -52,6 +52,33 @@ class SampleBatch:
         return H.contiguous()
 
 
+ROWS_KERNEL_SIZES = (9, 16, 25, 36, 49, 64)
+
+
+def pick_block_k(nsteps, m, nselect, max_k=9):
+    """Largest K <= max_k dividing nsteps for the K-step blocked FP32 loop (1 = none)."""
+    if m not in ROWS_KERNEL_SIZES:
+        return 1
+    for K in range(max_k, 1, -1):
+        if nsteps % K == 0 and m + nselect * (K - 1) <= 256:
+            return K
+    return 1
+
+
+def propagate_selected_mean(D, y0, nsteps, select, precision):
+    """Ensemble mean of the selected components at every step (GPU).
+
+    FP32 runs use the K-step blocked loop when the step count allows it.
+    """
+    K = pick_block_k(nsteps, D.shape[-1], len(select)) if precision == _native.QSX_FP32 else 1
+    if K > 1:
+        blk = _native.rk4_block_matrix(D, K, select)
+        return _native.rk4(blk, y0, nsteps, 1, select=select, per_sample=False, mean=True,
+                           check_finite=False, block_k=K)
+    return _native.rk4(D, y0, nsteps, 1, select=select, per_sample=False, mean=True,
+                       check_finite=False)
+
+
 def redfield_batch_build(model, batch):
     if not isinstance(model, RedfieldModel):
         raise NotImplementedError('batched ensembles need a RedfieldModel')
@@ -120,8 +147,7 @@ def ensemble_populations(model, initial_state, duration, ensemble_size,
         nn = int(round(np.sqrt(M)))
         select = [i * nn + i for i in range(nn)]
     y0t = torch.as_tensor(y0, dtype=torch.complex128).cuda()
-    out = _native.rk4(D, y0t, len(t) - 1, 1,
-                      select=select, per_sample=False, mean=True, check_finite=False)
+    out = propagate_selected_mean(D, y0t, len(t) - 1, select, prec)
     if int(out['status'].item()) & _native.QSX_ERR_NONFINITE:
         raise _native.IntegratorError('non-finite state in ensemble propagation')
     return t, out['mean']
@@ -198,8 +224,8 @@ class RedfieldEnsembleWorkload:
         if events is not None:
             e0 = torch.cuda.Event(enable_timing=True)
             e0.record()
-        pop = _native.rk4(D_ee, self.y_dyn, len(self.t_dyn) - 1, 1, select=self.select,
-                          per_sample=False, mean=True, check_finite=False)
+        pop = propagate_selected_mean(D_ee, self.y_dyn, len(self.t_dyn) - 1, self.select,
+                                      prec)
         if events is not None:
             e1 = torch.cuda.Event(enable_timing=True)
             e1.record()

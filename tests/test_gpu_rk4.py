@@ -108,3 +108,35 @@ def test_fused_redfield_propagator_matches_two_step_path(golden):
             fused = build.propagator(idx, 1.0, prec, transpose=tr).cpu().numpy()
             ref = _native.rk4_propagator(build.block(idx, tr), 1.0, prec).cpu().numpy()
             assert rel_err(fused, ref) < tol
+
+
+@pytest.mark.parametrize('M,B,K,nsteps', [(9, 13, 3, 30), (49, 11, 9, 54), (25, 7, 4, 40),
+                                          (64, 5, 2, 10)])
+def test_block_k_matches_step_by_step(M, B, K, nsteps):
+    """K-step blocking gives the same RK4 iterates as the step-by-step loop."""
+    L = random_generators(B, M, seed=M + K)
+    rng = np.random.RandomState(K)
+    y0 = rng.randn(B, M) + 1j * rng.randn(B, M)
+    ref = oracle_run(L, y0, nsteps, 1.0, 1)
+    D = _native.rk4_propagator(torch.as_tensor(L).cuda(), 1.0, _native.QSX_FP32)
+    sel = [0, M // 3, M - 1, M // 2]
+    blk = _native.rk4_block_matrix(D, K, sel)
+    assert blk.shape == (B, M + len(sel) * (K - 1), M)
+    out = _native.rk4(blk, torch.as_tensor(y0).cuda(), nsteps, 1, select=sel, mean=True,
+                      block_k=K)
+    assert rel_err(out['proj'].cpu().numpy(), ref[:, :, sel]) < 1e-5
+    assert rel_err(out['mean'].cpu().numpy(), ref[:, :, sel].mean(0)) < 1e-5
+
+
+def test_block_matrix_powers_fp64():
+    L = random_generators(2, 16, 3)
+    D = _native.rk4_propagator(torch.as_tensor(L).cuda(), 0.5, _native.QSX_FP64)
+    sel = [1, 5]
+    blk = _native.rk4_block_matrix(D, 5, sel).cpu().numpy()
+    Dn = D.cpu().numpy()
+    for b in range(2):
+        P = np.eye(16) + Dn[b]
+        assert rel_err(blk[b, :16], np.linalg.matrix_power(P, 5) - np.eye(16)) < 1e-13
+        for k in range(1, 5):
+            Pk = np.linalg.matrix_power(P, k) - np.eye(16)
+            assert rel_err(blk[b, 16 + (k - 1) * 2:16 + k * 2], Pk[sel]) < 1e-13
