@@ -171,7 +171,7 @@ def fma_peak_tflops(torch, native):
     return best
 
 
-def ncu_traffic(path=os.path.join(ROOT, 'profiles', 'rk4_rows_f32_fmo7.md')):
+def ncu_traffic(path=os.path.join(ROOT, 'profiles', 'rk4_block_f32_fmo7.md')):
     try:
         txt = open(path).read()
     except OSError:
@@ -264,7 +264,8 @@ def our_arm(args):
     if rank != 0:
         return 0
     peak = fma_peak_tflops(torch, _native)
-    flops_dyn = float(S) * (DYN_TIME - 1) * 49 * 49 * 8  # complex GEMV per step
+    flops_dyn = events['dyn_flops']  # executed form (K-step blocked rows)
+    dense_equiv = float(S) * (DYN_TIME - 1) * 49 * 49 * 8  # one 49x49 GEMV per step
     achieved = flops_dyn / (dyn_ms * 1e-3) / 1e12
     traffic = ncu_traffic()
     base = None
@@ -284,14 +285,16 @@ def our_arm(args):
         'e2e': {'value': world * 1000.0 / e2e_ms, 'unit': UNIT,
                 'h2d_bytes_per_step': int(off_host.numel() * 8),
                 'd2h_bytes_per_step': int((nf + Ph.size + 1) * 8)},
-        'roofline': {'kernel': 'rk4_rows_f32<49,5> (ee populations)',
+        'roofline': {'kernel': 'rk4_block_f32<49> (ee populations, K={} step blocking)'.format(
+                         events['dyn_block_k']),
+                     'dense_step_equivalent_tflops': dense_equiv / (dyn_ms * 1e-3) / 1e12,
                      'bound': 'fp32_fma', 'achieved': achieved, 'peak': peak,
                      'unit': 'TFLOP/s', 'frac': achieved / peak,
                      'peak_source': 'measured live by qsx_probe_fma (FP32 FMA); '
                                     'MEASURED_PEAKS.json has no CUDA-core figure',
                      'flops_per_launch': flops_dyn, 'launch_ms': dyn_ms,
                      'traffic': traffic},
-        'gpu_launches': 11 * args.steps,
+        'gpu_launches': 12 * args.steps,
         'clocks': clocks,
     }
     if base is not None:

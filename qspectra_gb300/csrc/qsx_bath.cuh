@@ -12,8 +12,9 @@
 //   A = 1/(2(a−b)),  B = −1/(2(a+b)),  D = −b/((a−b)(a+b)),
 // and Σ_{k=1}^{K−1} 1/(k−z) = ψ(K−z) − ψ(1−z).  The two real sums
 // (z = ±a) depend only on (T, γ) and come in as constants fa, fb; the
-// x-dependent one uses the complex digamma below (recurrence up to Re z >= 16,
-// then the Stirling-type asymptotic series with Bernoulli numbers B2..B14).
+// x-dependent one adds its first 7 terms directly and takes the rest from
+// psi(K - iy) - psi(8 - iy), both from the Stirling-type asymptotic series
+// with Bernoulli numbers B2..B14 (|z| >= 8).
 #pragma once
 #include "qsx_common.cuh"
 
@@ -31,7 +32,8 @@ __device__ __forceinline__ double2 clog_(double2 z) {
   return cmk(log(hypot(z.x, z.y)), atan2(z.y, z.x));
 }
 
-// psi(z) for Re z >= 16 from ln z - 1/(2z) - sum_n B_2n / (2n z^2n).
+// psi(z) for |z| >= 8 from ln z - 1/(2z) - sum_{n=1..7} B_2n / (2n z^2n); the
+// first omitted term is below 2e-15 relative at |z| = 8.
 __device__ __forceinline__ double2 digamma_asymptotic(double2 z) {
   const double c1 = 1.0 / 12.0, c2 = -1.0 / 120.0, c3 = 1.0 / 252.0,
                c4 = -1.0 / 240.0, c5 = 1.0 / 132.0, c6 = -691.0 / 32760.0,
@@ -49,24 +51,24 @@ __device__ __forceinline__ double2 digamma_asymptotic(double2 z) {
   return csub(csub(clog_(z), cscale(zi, 0.5)), s);
 }
 
-__device__ __forceinline__ double2 digamma(double2 z) {
-  double2 acc = cmk(0.0, 0.0);
-  // psi(z) = psi(z + 1) - 1/z; at most 64 shifts (callers pass Re z >= -40).
-  for (int guard = 0; z.x < 16.0 && guard < 64; ++guard) {
-    acc = cadd(acc, crecip(z));
-    z.x += 1.0;
+// sum_{k=1}^{K-1} 1/(k - i y) = sum_{k<8} (k + i y)/(k^2 + y^2)
+//                              + psi(K - i y) - psi(8 - i y)   (K >= 9).
+__device__ __forceinline__ double2 harmonic_shifted(int K, double y) {
+  double2 head = cmk(0.0, 0.0);
+  const int kmax = K < 9 ? K : 8;
+  for (int k = 1; k < kmax; ++k) {
+    const double inv = 1.0 / fma((double)k, (double)k, y * y);
+    head.x = fma((double)k, inv, head.x);
+    head.y = fma(y, inv, head.y);
   }
-  return csub(digamma_asymptotic(z), acc);
+  if (K < 9) return head;
+  return cadd(head, csub(digamma_asymptotic(cmk((double)K, -y)),
+                         digamma_asymptotic(cmk(8.0, -y))));
 }
 
-__device__ __forceinline__ double2 debye_corr(const DebyeParams& p, double x) {
-  if (p.real_only) {
-    if (x == 0.0) return cmk(p.T * 2.0 * p.lam / p.gamma, 0.0);
-    // J(x) = 2λγx/(γ²+x²) is odd, so J_anti(x) = J(x) for both signs.
-    double J = 2.0 * p.lam * p.gamma * x / (p.gamma * p.gamma + x * x);
-    return cmk((1.0 / expm1(x / p.T) + 1.0) * J, 0.0);
-  }
-  if (x == 0.0) return cmk(p.lam * (2.0 * p.T / p.gamma), -p.lam);
+// Matsubara part S(x) = sum_{k=1}^{K-1} nu_k / ((nu_k^2 - g^2)(nu_k - i x)),
+// nu_k = 2 pi k T, in closed form; S(-x) = conj(S(x)).
+__device__ __forceinline__ double2 debye_matsubara(const DebyeParams& p, double x) {
   const double c = 2.0 * M_PI * p.T;
   const double a = p.gamma / c;
   const double2 b = cmk(0.0, x / c);
@@ -75,13 +77,46 @@ __device__ __forceinline__ double2 debye_corr(const DebyeParams& p, double x) {
   const double2 A = cscale(crecip(amb), 0.5);
   const double2 B = cscale(crecip(apb), -0.5);
   const double2 D = cscale(cdiv(b, cmul(amb, apb)), -1.0);
-  const double2 g = csub(digamma(cmk((double)p.matsubara - b.x, -b.y)),
-                         digamma(cmk(1.0 - b.x, -b.y)));
+  const double2 g = harmonic_shifted(p.matsubara, x / c);
   double2 S = cadd(cadd(cscale(A, p.fa), cscale(B, p.fb)), cmul(D, g));
-  S = cscale(S, 1.0 / (c * c));
+  return cscale(S, 1.0 / (c * c));
+}
+
+__device__ __forceinline__ double2 debye_real(const DebyeParams& p, double x) {
+  if (x == 0.0) return cmk(p.T * 2.0 * p.lam / p.gamma, 0.0);
+  // J(x) = 2λγx/(γ²+x²) is odd, so J_anti(x) = J(x) for both signs.
+  double J = 2.0 * p.lam * p.gamma * x / (p.gamma * p.gamma + x * x);
+  return cmk((1.0 / expm1(x / p.T) + 1.0) * J, 0.0);
+}
+
+// C(x) from its Matsubara part.
+__device__ __forceinline__ double2 debye_from_matsubara(const DebyeParams& p, double x,
+                                                        double2 S) {
   const double2 first = cdiv(cmk(p.cot_term, -1.0), cmk(p.gamma, -x));
-  const double2 tot = cadd(first, cscale(S, 4.0 * p.T));
-  return cscale(tot, p.lam * p.gamma);
+  return cscale(cadd(first, cscale(S, 4.0 * p.T)), p.lam * p.gamma);
+}
+
+__device__ __forceinline__ double2 debye_corr(const DebyeParams& p, double x) {
+  if (p.real_only) return debye_real(p, x);
+  if (x == 0.0) return cmk(p.lam * (2.0 * p.T / p.gamma), -p.lam);
+  return debye_from_matsubara(p, x, debye_matsubara(p, x));
+}
+
+// C(x) and C(-x) sharing one Matsubara evaluation.
+__device__ __forceinline__ void debye_corr_pair(const DebyeParams& p, double x, double2& cpos,
+                                                double2& cneg) {
+  if (p.real_only) {
+    cpos = debye_real(p, x);
+    cneg = debye_real(p, -x);
+    return;
+  }
+  if (x == 0.0) {
+    cpos = cneg = cmk(p.lam * (2.0 * p.T / p.gamma), -p.lam);
+    return;
+  }
+  const double2 S = debye_matsubara(p, x);
+  cpos = debye_from_matsubara(p, x, S);
+  cneg = debye_from_matsubara(p, -x, cconj(S));
 }
 
 // Host-side constants of the closed form (depend on T and gamma only).

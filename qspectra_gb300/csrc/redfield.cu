@@ -272,12 +272,23 @@ __global__ void __launch_bounds__(256)
     sE[32 + i] = w;
   }
   __syncthreads();
-  // correlation function only where some Kt_i[c][d] can be non-zero
+  // correlation function only where some Kt_i[c][d] can be non-zero; the
+  // pair (c, d), (d, c) shares one Matsubara evaluation (C(E_d - E_c) and
+  // C(E_c - E_d)), computed by the thread with c <= d.
   for (int e = threadIdx.x; e < nn; e += blockDim.x) {
     int c = e / n, d = e % n;
+    if (c > d) continue;
     double need = 0.0;
     for (int s = 0; s < n; ++s) need += fabs(sU[s * n + c] * sU[s * n + d]) * sE[32 + s];
-    sC[e] = need > 0.0 ? debye_corr(bath, sE[d] - sE[c]) : cmk(0.0, 0.0);
+    if (need > 0.0) {
+      double2 cp, cn;
+      debye_corr_pair(bath, sE[d] - sE[c], cp, cn);
+      sC[e] = cp;
+      sC[d * n + c] = cn;
+    } else {
+      sC[e] = cmk(0.0, 0.0);
+      sC[d * n + c] = cmk(0.0, 0.0);
+    }
   }
   __syncthreads();
   for (int i = 0; i < n_sites; ++i) {
@@ -385,10 +396,13 @@ __global__ void liouvillian_kernel(const double* __restrict__ H, int64_t H_strid
 template <typename C, typename Store>
 __device__ __forceinline__ void smem_cgemm(const C* __restrict__ A, const C* __restrict__ B,
                                            int m, Store store) {
+  // Thread (r', c') owns rows r' + i nb and columns c' + j nb (i, j < 4,
+  // nb = ceil(m / 4)): consecutive threads read consecutive B columns
+  // (conflict-free) and share A rows (broadcast).
   using T = decltype(A[0].x);
   const int nb = (m + 3) / 4;
   for (int blk = threadIdx.x; blk < nb * nb; blk += blockDim.x) {
-    const int r0 = (blk / nb) * 4, c0 = (blk % nb) * 4;
+    const int r0 = blk / nb, c0 = blk % nb;
     C acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -397,9 +411,11 @@ __device__ __forceinline__ void smem_cgemm(const C* __restrict__ A, const C* __r
     for (int k = 0; k < m; ++k) {
       C a[4], b[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = (r0 + i < m) ? A[(r0 + i) * m + k] : cmk((T)0, (T)0);
+      for (int i = 0; i < 4; ++i)
+        a[i] = (r0 + i * nb < m) ? A[(r0 + i * nb) * m + k] : cmk((T)0, (T)0);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = (c0 + j < m) ? B[k * m + c0 + j] : cmk((T)0, (T)0);
+      for (int j = 0; j < 4; ++j)
+        b[j] = (c0 + j * nb < m) ? B[k * m + c0 + j * nb] : cmk((T)0, (T)0);
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -409,7 +425,7 @@ __device__ __forceinline__ void smem_cgemm(const C* __restrict__ A, const C* __r
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int j = 0; j < 4; ++j)
-        if (r0 + i < m && c0 + j < m) store((r0 + i) * m + c0 + j, acc[i][j]);
+        if (r0 + i * nb < m && c0 + j * nb < m) store((r0 + i * nb) * m + c0 + j * nb, acc[i][j]);
   }
 }
 

@@ -335,11 +335,15 @@ __global__ void __launch_bounds__(256, 2) rk4_block_f32(Rk4P p, int64_t ngroups,
             make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
     }
     __syncthreads();
-    if (p.partial32)
+    // ensemble partial sums: FP64 fire-and-forget adds into this CTA's slice;
+    // a given (step, q) is always added by the same thread, in program order
+    if (p.partial)
       for (int q = tid; q < nsel; q += blockDim.x) {
         float2 acc = make_float2(0.f, 0.f);
         for (int gg = 0; gg < G; ++gg) acc = cadd2(acc, stash_at(parity, 0, gg, q));
-        p.partial32[(grp * p.nsave) * p.nout + q] = acc;
+        double2* dst = p.partial + ((int64_t)blockIdx.x * p.nsave) * p.nout + q;
+        atomicAdd(&dst->x, (double)acc.x);
+        atomicAdd(&dst->y, (double)acc.y);
       }
     parity ^= 1;
     const int nblk = p.nsteps / K;
@@ -372,12 +376,14 @@ __global__ void __launch_bounds__(256, 2) rk4_block_f32(Rk4P p, int64_t ngroups,
           p.out_proj[(s * p.nsave + step0 + kx) * p.nout + qx] = make_double2(v.x, v.y);
       }
       __syncthreads();
-      if (p.partial32)
+      if (p.partial)
         for (int e = tid; e < K * nsel; e += blockDim.x) {
           const int k = e / nsel, q = e % nsel;
           float2 acc = make_float2(0.f, 0.f);
           for (int gg = 0; gg < G; ++gg) acc = cadd2(acc, stash_at(parity, k, gg, q));
-          p.partial32[(grp * p.nsave + step0 + k + 1) * p.nout + q] = acc;
+          double2* dst = p.partial + ((int64_t)blockIdx.x * p.nsave + step0 + k + 1) * p.nout + q;
+          atomicAdd(&dst->x, (double)acc.x);
+          atomicAdd(&dst->y, (double)acc.y);
         }
       parity ^= 1;
     }
@@ -611,7 +617,9 @@ static bool rows_supported(int m, int* G) {
   return false;
 }
 
-static size_t partial_bytes(Kind k) { return k == K_GENERIC ? sizeof(double2) : sizeof(float2); }
+static size_t partial_bytes(Kind k) {
+  return (k == K_GENERIC || k == K_BLOCK) ? sizeof(double2) : sizeof(float2);
+}
 
 static int validate(const qsx_rk4_args* a) {
   QSX_CHECK_ARG(a != nullptr, "qsx_rk4: null args");
@@ -665,7 +673,7 @@ static int make_plan(const qsx_rk4_args* a, Plan* pl) {
     pl->threads = threads;
     pl->ngroups = (a->batch + G - 1) / G;
     pl->grid = std::max<int64_t>(1, std::min<int64_t>(pl->ngroups, (int64_t)sms * std::max(occ, 1)));
-    pl->nslots = pl->ngroups;
+    pl->nslots = pl->grid;  // one FP64 accumulator slice per CTA
     return QSX_OK;
   }
   const int64_t nsave = a->nsteps / a->save_every + 1;
@@ -775,10 +783,15 @@ int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
     QSX_CHECK_ARG(a->workspace && a->workspace_bytes >= need,
                   "qsx_rk4_batched: workspace of %zu bytes needed (got %zu)", need,
                   a->workspace_bytes);
-    if (pl.kind == K_GENERIC)
+    if (pl.kind == K_GENERIC) {
       p.partial = (double2*)a->workspace;
-    else
+    } else if (pl.kind == K_BLOCK) {
+      p.partial = (double2*)a->workspace;  // accumulated with atomic adds: start at zero
+      cudaError_t e = cudaMemsetAsync(a->workspace, 0, need, s);
+      if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_batched memset");
+    } else {
       p.partial32 = (float2*)a->workspace;
+    }
   }
   switch (pl.kind) {
     case K_SMALL: {
@@ -824,7 +837,7 @@ int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
   QSX_LAUNCH_CHECK("qsx_rk4_batched");
   if (a->out_mean) {
     const unsigned rg = (unsigned)((per + 31) / 32);
-    if (pl.kind == K_GENERIC)
+    if (pl.kind == K_GENERIC || pl.kind == K_BLOCK)
       rk4_reduce_kernel<double2><<<rg, 256, 0, s>>>(p.partial, pl.nslots, per, a->mean_scale,
                                                     (double2*)a->out_mean);
     else

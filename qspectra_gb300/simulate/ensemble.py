@@ -65,18 +65,30 @@ def pick_block_k(nsteps, m, nselect, max_k=9):
     return 1
 
 
-def propagate_selected_mean(D, y0, nsteps, select, precision):
+def propagate_selected_mean(D, y0, nsteps, select, precision, events=None):
     """Ensemble mean of the selected components at every step (GPU).
 
     FP32 runs use the K-step blocked loop when the step count allows it.
+    ``events`` (a dict) receives CUDA events around the time loop and the
+    matrix-vector work it executed ('flops').
     """
     K = pick_block_k(nsteps, D.shape[-1], len(select)) if precision == _native.QSX_FP32 else 1
-    if K > 1:
-        blk = _native.rk4_block_matrix(D, K, select)
-        return _native.rk4(blk, y0, nsteps, 1, select=select, per_sample=False, mean=True,
-                           check_finite=False, block_k=K)
-    return _native.rk4(D, y0, nsteps, 1, select=select, per_sample=False, mean=True,
-                       check_finite=False)
+    B, m = D.shape[0], D.shape[-1]
+    mat = _native.rk4_block_matrix(D, K, select) if K > 1 else D
+    rows = mat.shape[-2]
+    if events is not None:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+    out = _native.rk4(mat, y0, nsteps, 1, select=select, per_sample=False, mean=True,
+                      check_finite=False, block_k=K if K > 1 else 0)
+    if events is not None:
+        e1 = torch.cuda.Event(enable_timing=True)
+        e1.record()
+        events.setdefault('dyn', []).append((e0, e1))
+        # complex multiply-adds of the executed form, 8 real flops each
+        events['dyn_flops'] = 8.0 * B * (nsteps // K) * rows * m
+        events['dyn_block_k'] = K
+    return out
 
 
 def redfield_batch_build(model, batch):
@@ -221,15 +233,8 @@ class RedfieldEnsembleWorkload:
         X = _native.dft(-sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
                         self.model.rw_freq, self.model.unit_convert, 1)
         D_ee = build.propagator(self.idx_ee, self.dt, prec)
-        if events is not None:
-            e0 = torch.cuda.Event(enable_timing=True)
-            e0.record()
         pop = propagate_selected_mean(D_ee, self.y_dyn, len(self.t_dyn) - 1, self.select,
-                                      prec)
-        if events is not None:
-            e1 = torch.cuda.Event(enable_timing=True)
-            e1.record()
-            events.setdefault('dyn', []).append((e0, e1))
+                                      prec, events)
         status = sig['status'] | pop['status']
         return X.real, pop['mean'].real, status
 
