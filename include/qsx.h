@@ -199,6 +199,23 @@ int qsx_rk4_workspace_bytes(const qsx_rk4_args* args, size_t* bytes);
 int qsx_rk4_batched(const qsx_rk4_args* args, void* stream);
 
 /*
+ * Ensemble-mean K-step blocked RK4 loop that allocates nothing (no reference
+ * counterpart: an addition for callers that cannot call cudaMalloc, such as
+ * a plug-in inside a host application that owns all device memory, or an
+ * embedded runtime with a fixed memory budget).  Same arguments and results
+ * as qsx_rk4_batched with block_k > 1 and out_mean set, except that
+ * `workspace` is ignored: the partial sums live in a 16 MiB device array
+ * built into the library, which every GPU that loads the library keeps until
+ * the process exits.  Requests whose (nsteps + 1) * nselect * 16 bytes exceed
+ * 16 MiB are rejected with QSX_ERR_INVALID_ARG; larger batches run with fewer
+ * persistent CTAs so their partial sums fit.  The first call on each device
+ * looks up the array's address (cudaGetSymbolAddress) with that device
+ * current, so make it before any stream capture.  Every call shares the
+ * array and clears the part it uses: calls that overlap on the GPU race.
+ */
+int qsx_rk4_block_mean_noalloc(const qsx_rk4_args* args, void* stream);
+
+/*
  * Direct discrete Fourier transform of uniformly sampled signals,
  *   X[b][k] = dt * sum_n x[b][n] exp(i * sign * (freqs[k] - rw_freq) * uc * t_n),
  * t_n = t0 + n dt.  With freqs on the FFT grid this equals fourier_transform

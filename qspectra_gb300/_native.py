@@ -75,6 +75,7 @@ _PROTOS = {
     'qsx_rk4_workspace_bytes': (_c_int, [ctypes.POINTER(Rk4Args),
                                          ctypes.POINTER(ctypes.c_size_t)]),
     'qsx_rk4_batched': (_c_int, [ctypes.POINTER(Rk4Args), _c_vp]),
+    'qsx_rk4_block_mean_noalloc': (_c_int, [ctypes.POINTER(Rk4Args), _c_vp]),
     'qsx_dft_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
                                  _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_probe_fma': (_c_int, [_c_int, _c_i64, _c_int, _c_int, _c_vp, _c_vp]),

@@ -849,3 +849,107 @@ int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ no-allocation variant
+// Some callers cannot call cudaMalloc: a host application that owns all
+// device memory through its own pool and forbids allocations by plug-ins, an
+// embedded runtime with a fixed memory budget, or code running where an
+// allocation could fail late (e.g. inside the host's own out-of-memory
+// handling).  For them, qsx_rk4_block_mean_noalloc runs the K-step blocked
+// ensemble-mean loop with its partial sums in the file-scope device array
+// below instead of caller workspace.  The array is NOALLOC_SCRATCH_BYTES
+// (16 MiB); every GPU that loads this library keeps it until the process
+// exits.  Its device address is looked up once per device, by the first call
+// made with that device current, so make that first call before any stream
+// capture.  All calls share the array: two calls that overlap on the GPU
+// (different streams, or threads) race on it, and each call clears the part
+// it uses before running.
+namespace qsx {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)16 << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device (host code may
+// not take the address of a __device__ array directly).
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_block_mean_noalloc: cudaGetDevice");
+  QSX_CHECK_ARG(dev >= 0 && dev < NOALLOC_MAX_DEVICES,
+                "qsx_rk4_block_mean_noalloc: device index %d not supported", dev);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return cuda_status(e, "qsx_rk4_block_mean_noalloc: cudaGetSymbolAddress");
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return QSX_OK;
+}
+
+}  // namespace qsx
+
+extern "C" int qsx_rk4_block_mean_noalloc(const qsx_rk4_args* a, void* stream) {
+  int st = validate(a);
+  if (st) return st;
+  QSX_CHECK_ARG(a->block_k > 1 && a->out_mean != nullptr,
+                "qsx_rk4_block_mean_noalloc: needs block_k > 1 and out_mean");
+  if (a->batch == 0) return QSX_OK;
+  Plan pl;
+  st = make_plan(a, &pl);
+  if (st) return st;
+  const int64_t nsave = a->nsteps / a->save_every + 1;
+  const int64_t per = nsave * a->nselect;  // outputs per accumulator slice
+  const size_t slice = (size_t)per * sizeof(double2);
+  QSX_CHECK_ARG(slice <= NOALLOC_SCRATCH_BYTES,
+                "qsx_rk4_block_mean_noalloc: (nsteps + 1) * nselect = %lld outputs need %zu "
+                "bytes of scratch per slice; the built-in scratch holds %zu bytes",
+                (long long)per, slice, NOALLOC_SCRATCH_BYTES);
+  // fewer persistent CTAs when their slices would not all fit
+  const int64_t grid = std::max<int64_t>(
+      1, std::min<int64_t>(pl.grid, (int64_t)(NOALLOC_SCRATCH_BYTES / slice)));
+  void* scratch = nullptr;
+  st = noalloc_scratch(&scratch);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, (size_t)grid * slice, s);
+  if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_block_mean_noalloc: memset");
+  Rk4P p;
+  p.m = a->m;
+  p.nsteps = a->nsteps;
+  p.save_every = a->save_every;
+  p.nsave = (int)nsave;
+  p.nproj = 0;
+  p.nselect = a->nselect;
+  p.nout = a->nselect;
+  p.form = a->form;
+  p.batch = a->batch;
+  p.matrix = a->matrix;
+  p.matrix_stride = a->matrix_stride;
+  p.h = a->h;
+  p.y0 = (const double2*)a->y0;
+  p.y0_stride = a->y0_stride;
+  p.proj = nullptr;
+  p.proj_stride = 0;
+  p.select = a->select;
+  p.out_state = nullptr;
+  p.out_proj = (double2*)a->out_proj;
+  p.partial = (double2*)scratch;
+  p.partial32 = nullptr;
+  p.status = a->status;
+#define X(MM, GG, BB)                                                                    \
+  if (a->m == MM)                                                                        \
+    rk4_block_f32<MM><<<(unsigned)grid, pl.threads, pl.smem, s>>>(p, pl.ngroups, pl.G,   \
+                                                                  a->block_k);
+  QSX_ROWS_TABLE(X)
+#undef X
+  QSX_LAUNCH_CHECK("qsx_rk4_block_mean_noalloc");
+  rk4_reduce_kernel<double2><<<(unsigned)((per + 31) / 32), 256, 0, s>>>(
+      p.partial, grid, per, a->mean_scale, (double2*)a->out_mean);
+  QSX_LAUNCH_CHECK("qsx_rk4_block_mean_noalloc reduce");
+  return QSX_OK;
+}
