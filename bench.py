@@ -54,6 +54,7 @@ def parse_args():
     p.add_argument('--cpu-samples-per-core', type=int, default=24)
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--fp64-steps', type=int, default=2)
+    p.add_argument('--no-heom', action='store_true')
     return p.parse_args()
 
 
@@ -171,6 +172,48 @@ def fma_peak_tflops(torch, native):
     return best
 
 
+def heom_ring8(torch, qg, native, samples=64, nsteps=1999):
+    """HEOM workload: 8-site ring, K = 0, depth 4 (495 nodes x 64), 64 disorder
+    samples (SD 50 cm^-1), 1 ps at dt = 0.5 fs; FP32 split-word and FP64."""
+    from qspectra_gb300 import workloads as wl
+    H = wl.ring_hamiltonian()
+    ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 300, 35, 106),
+                                   disorder=wl.fwhm_for_sd(50.0), random_seed=7)
+    m = qg.HEOMModel(ham, hilbert_subspace='e', unit_convert=qg.CM_FS, K=0, level_cutoff=5,
+                     low_temp_corr=True)
+    tb = m.tables('ee')
+    offs = m.hamiltonian.disorder_offsets(samples)
+    base = m.hamiltonian.H('e')
+    Hb = torch.as_tensor(np.array([base + np.diag(o) for o in offs])).cuda()
+    y0 = torch.zeros(m.ado_count * 64, dtype=torch.complex128, device='cuda')
+    y0[0] = 1.0
+    out = {'workload': 'HEOM 8-site ring, K=0, depth 4 (495 nodes), 64 samples, '
+                       '1999 RK4 steps at 0.5 fs', 'nodes': m.ado_count}
+    res = {}
+    for name, prec, steps in (('fp32', native.QSX_FP32, nsteps), ('fp64', native.QSX_FP64, 200)):
+        native.heom_rk4(tb, Hb, Hb, y0, 10, 0.5, qg.CM_FS, batch=samples, save_every=10,
+                        precision=prec, per_sample=False, mean=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        r = native.heom_rk4(tb, Hb, Hb, y0, steps, 0.5, qg.CM_FS, batch=samples, save_every=1,
+                            precision=prec, per_sample=False, mean=True, check_finite=False)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        res[name] = r['mean']
+        out[name + '_ms'] = ms * (nsteps / steps)
+        out[name + '_steps_timed'] = steps
+    k = res['fp64'].shape[0]
+    a, b = res['fp32'][:k], res['fp64']
+    out['fp32_vs_fp64_rel_err_first_200_steps'] = float((a - b).abs().max() / b.abs().max())
+    # structured generator: 495 nodes x (2 x 8^3 commutator + coupling terms) per RHS
+    flops = 8.0 * samples * 4 * nsteps * m.ado_count * (2 * 8 ** 3 + 64 * tb.nterms)
+    out['fp32_tflops_executed_form'] = flops / (out['fp32_ms'] * 1e-3) / 1e12
+    out['fp64_ms_note'] = 'FP64 timed over 200 steps and scaled to 1999'
+    return out
+
+
 def ncu_traffic(path=os.path.join(ROOT, 'profiles', 'rk4_block_f32_fmo7.md')):
     try:
         txt = open(path).read()
@@ -261,6 +304,7 @@ def our_arm(args):
     err_spec = float((X32 - X64).abs().max() / X64.abs().max())
     err_pop = float((P32 - P64).abs().max() / P64.abs().max())
 
+    heom = heom_ring8(torch, qg, _native) if rank == 0 and not args.no_heom else None
     if rank != 0:
         return 0
     peak = fma_peak_tflops(torch, _native)
@@ -297,6 +341,8 @@ def our_arm(args):
         'gpu_launches': 12 * args.steps,
         'clocks': clocks,
     }
+    if heom is not None:
+        line['heom_ring8'] = heom
     if base is not None:
         line['cpu_baseline'] = base
     print(json.dumps(line), flush=True)

@@ -216,6 +216,59 @@ int qsx_rk4_batched(const qsx_rk4_args* args, void* stream);
 int qsx_rk4_block_mean_noalloc(const qsx_rk4_args* args, void* stream);
 
 /*
+ * Hierarchical equations of motion (HEOM).  Replaces HEOMModel.HEOM_tensor
+ * and equation_of_motion (qspectra/dynamics/heom.py:228-244, 298-443) by a
+ * structured generator on one Liouville block XY (nx x ny, column stacked)
+ * per hierarchy node n:
+ *   d rho_n/dt = uc { -i (Hx rho_n - rho_n Hy) - shift_n rho_n - W o rho_n
+ *                     + sum_t (alpha_t occx_j(a) + beta_t occy_j(b)) rho_{nbr_t} },
+ * j = site[n][t].  The host builds the node tables from the ADO enumeration
+ * (heom.py:92-174): shift_n = sum_jk n_jk nu_k, up terms (alpha, beta) =
+ * (-i m, i m), down terms (-i m c_k, i m conj(c_k)) (heom.py:410-442), W the
+ * low-temperature correction times its coefficient (heom.py:386-408), and the
+ * transposed tables for the Heisenberg picture (heom.py:236-237).
+ */
+typedef struct {
+  int32_t precision;   /* QSX_FP64, or QSX_FP32 (split-word FP32 state) */
+  int32_t nx, ny;      /* block dimensions, nx * ny <= 256 */
+  int32_t nnodes;      /* hierarchy nodes */
+  int32_t nterms;      /* coupling terms per node (padded with nbr = -1) */
+  int32_t n_sites;     /* bath sites (rows of occx / occy) */
+  int32_t nsteps;      /* RK4 steps */
+  int32_t save_every;  /* output every save_every steps */
+  int32_t save_nodes;  /* leading nodes saved per output (1 = physical rho) */
+  int32_t pad0;
+  int64_t batch;       /* disorder samples */
+  int64_t H_stride;    /* 0: Hx, Hy shared; else per sample [batch][n][n] */
+  const double* Hx;    /* real [nx][nx], rotating frame */
+  const double* Hy;    /* real [ny][ny] */
+  const double* occx;  /* [n_sites][nx] number-operator diagonals */
+  const double* occy;  /* [n_sites][ny] */
+  const double* W;     /* [nx * ny] low-temperature weights, or NULL */
+  const double* shift; /* [nnodes] */
+  const int32_t* nbr;  /* [nnodes][nterms] neighbour node, -1 = none */
+  const int32_t* site; /* [nnodes][nterms] */
+  const double* alpha; /* complex128 [nnodes][nterms] */
+  const double* beta;  /* complex128 [nnodes][nterms] */
+  double unit_convert;
+  double h;            /* RK4 step */
+  const double* y0;    /* complex128 [batch][nnodes][nx * ny] */
+  int64_t y0_stride;   /* 0 = one initial state for all samples */
+  double* out_state;   /* complex128 [batch][nsave][save_nodes * nx * ny] or NULL */
+  double* out_mean;    /* complex128 [nsave][save_nodes * nx * ny] or NULL */
+  void* workspace;
+  size_t workspace_bytes;
+  int32_t* status;     /* device int: QSX_ERR_NONFINITE on NaN/Inf */
+} qsx_heom_args;
+
+int qsx_heom_workspace_bytes(const qsx_heom_args* args, size_t* bytes);
+/* out = generator applied to x (FP64), both complex128 [batch][nnodes][nx*ny]. */
+int qsx_heom_rhs(const qsx_heom_args* args, const double* x, double* out, void* stream);
+/* Fixed-step RK4 loop (stage form), the integrate() loop for HEOM. */
+int qsx_heom_rk4(const qsx_heom_args* args, void* stream);
+size_t qsx_heom_args_bytes(void);
+
+/*
  * Direct discrete Fourier transform of uniformly sampled signals,
  *   X[b][k] = dt * sum_n x[b][n] exp(i * sign * (freqs[k] - rw_freq) * uc * t_n),
  * t_n = t0 + n dt.  With freqs on the FFT grid this equals fourier_transform

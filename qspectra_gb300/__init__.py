@@ -12,6 +12,7 @@ from .dynamics.base import DynamicalModel, SystemOperator
 from .dynamics.liouville_space import (EquationOfMotion, LiouvilleSpaceModel,
                                        LiouvilleSpaceOperator, ket_vec_to_matrix,
                                        matrix_to_bra_vec, matrix_to_ket_vec)
+from .dynamics.heom import HEOMModel
 from .dynamics.redfield import RedfieldModel
 from .hamiltonian import ElectronicHamiltonian, HamiltonianError
 from .operator_tools import (SubspaceError, all_states, basis_transform_operator,
@@ -30,7 +31,7 @@ __all__ = [
     'DebyeBath', 'CM_FS', 'CM_FS_LINEAR', 'CM_K', 'GAUSSIAN_SD_FWHM',
     'DynamicalModel', 'SystemOperator', 'EquationOfMotion',
     'LiouvilleSpaceModel', 'LiouvilleSpaceOperator', 'ket_vec_to_matrix',
-    'matrix_to_bra_vec', 'matrix_to_ket_vec', 'RedfieldModel',
+    'matrix_to_bra_vec', 'matrix_to_ket_vec', 'RedfieldModel', 'HEOMModel',
     'ElectronicHamiltonian', 'HamiltonianError', 'SubspaceError', 'all_states',
     'basis_transform_operator', 'basis_transform_vector', 'n_excitations',
     'unit_vec', 'check_polarizations', 'polarization_vector',

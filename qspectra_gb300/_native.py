@@ -50,6 +50,23 @@ class Rk4Args(ctypes.Structure):
     ]
 
 
+class HeomArgs(ctypes.Structure):
+    _fields_ = [
+        ('precision', ctypes.c_int32), ('nx', ctypes.c_int32), ('ny', ctypes.c_int32),
+        ('nnodes', ctypes.c_int32), ('nterms', ctypes.c_int32), ('n_sites', ctypes.c_int32),
+        ('nsteps', ctypes.c_int32), ('save_every', ctypes.c_int32),
+        ('save_nodes', ctypes.c_int32), ('pad0', ctypes.c_int32),
+        ('batch', ctypes.c_int64), ('H_stride', ctypes.c_int64),
+        ('Hx', _c_vp), ('Hy', _c_vp), ('occx', _c_vp), ('occy', _c_vp), ('W', _c_vp),
+        ('shift', _c_vp), ('nbr', _c_vp), ('site', _c_vp), ('alpha', _c_vp), ('beta', _c_vp),
+        ('unit_convert', ctypes.c_double), ('h', ctypes.c_double),
+        ('y0', _c_vp), ('y0_stride', ctypes.c_int64),
+        ('out_state', _c_vp), ('out_mean', _c_vp),
+        ('workspace', _c_vp), ('workspace_bytes', ctypes.c_size_t),
+        ('status', _c_vp),
+    ]
+
+
 _PROTOS = {
     'qsx_last_error_string': (ctypes.c_char_p, []),
     'qsx_version': (_c_int, []),
@@ -76,6 +93,11 @@ _PROTOS = {
                                          ctypes.POINTER(ctypes.c_size_t)]),
     'qsx_rk4_batched': (_c_int, [ctypes.POINTER(Rk4Args), _c_vp]),
     'qsx_rk4_block_mean_noalloc': (_c_int, [ctypes.POINTER(Rk4Args), _c_vp]),
+    'qsx_heom_args_bytes': (ctypes.c_size_t, []),
+    'qsx_heom_workspace_bytes': (_c_int, [ctypes.POINTER(HeomArgs),
+                                          ctypes.POINTER(ctypes.c_size_t)]),
+    'qsx_heom_rhs': (_c_int, [ctypes.POINTER(HeomArgs), _c_vp, _c_vp, _c_vp]),
+    'qsx_heom_rk4': (_c_int, [ctypes.POINTER(HeomArgs), _c_vp]),
     'qsx_dft_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
                                  _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_probe_fma': (_c_int, [_c_int, _c_i64, _c_int, _c_int, _c_vp, _c_vp]),
@@ -376,3 +398,75 @@ def dft(x, t0, dt, freqs, rw_freq=0.0, unit_convert=1.0, sign=1):
 def probe_fma(precision, blocks, threads, iters, out):
     _check(load().qsx_probe_fma(precision, blocks, threads, iters, _p(out),
                                 _stream()), 'qsx_probe_fma')
+
+
+def _heom_args(tables, Hx, Hy, unit_convert, batch, precision=QSX_FP64):
+    """Fill HeomArgs from HEOMTables (device copies kept alive by the caller)."""
+    d = tables.device()
+    _need(Hx, torch.float64, 'Hx')
+    _need(Hy, torch.float64, 'Hy')
+    a = HeomArgs()
+    a.precision = precision
+    a.nx, a.ny, a.nnodes = tables.nx, tables.ny, tables.nnodes
+    a.nterms, a.n_sites = tables.nterms, tables.n_sites
+    a.save_every, a.save_nodes = 1, 1
+    a.batch = batch
+    a.H_stride = 1 if Hx.dim() == 3 else 0
+    a.Hx, a.Hy = Hx.data_ptr(), Hy.data_ptr()
+    a.occx, a.occy = d['occx'].data_ptr(), d['occy'].data_ptr()
+    a.W = d['W'].data_ptr() if d['W'] is not None else None
+    a.shift, a.nbr, a.site = d['shift'].data_ptr(), d['nbr'].data_ptr(), d['site'].data_ptr()
+    a.alpha, a.beta = d['alpha'].data_ptr(), d['beta'].data_ptr()
+    a.unit_convert = unit_convert
+    return a
+
+
+def heom_rhs(tables, Hx, Hy, x, unit_convert):
+    """Generator applied to x (B, nnodes * nx * ny) complex128 on the GPU."""
+    require_gpu()
+    x = _need(x.to(torch.complex128).contiguous(), torch.complex128, 'x', 2)
+    B = x.shape[0]
+    if Hx.dim() == 3 and Hx.shape[0] != B:
+        raise ValueError('per-sample H does not match the batch')
+    a = _heom_args(tables, Hx, Hy, unit_convert, B)
+    out = torch.empty_like(x)
+    _check(load().qsx_heom_rhs(ctypes.byref(a), _p(x), _p(out), _stream()), 'qsx_heom_rhs')
+    return out
+
+
+def heom_rk4(tables, Hx, Hy, y0, nsteps, h, unit_convert, batch=None, save_every=1,
+             save_nodes=1, precision=QSX_FP64, per_sample=True, mean=False,
+             check_finite=True):
+    """RK4 loop over the HEOM generator for all samples (qsx_heom_rk4)."""
+    require_gpu()
+    y0 = _need(y0.to(torch.complex128).contiguous(), torch.complex128, 'y0')
+    if batch is None:
+        batch = Hx.shape[0] if Hx.dim() == 3 else (y0.shape[0] if y0.dim() == 2 else 1)
+    a = _heom_args(tables, Hx, Hy, unit_convert, batch, precision)
+    a.nsteps, a.save_every, a.save_nodes = nsteps, save_every, save_nodes
+    a.h = h
+    a.y0, a.y0_stride = y0.data_ptr(), (1 if y0.dim() == 2 else 0)
+    nsave = nsteps // save_every + 1
+    E = tables.nx * tables.ny
+    dev = y0.device
+    out = {}
+    if per_sample:
+        out['state'] = torch.empty((batch, nsave, save_nodes * E), dtype=torch.complex128,
+                                   device=dev)
+        a.out_state = out['state'].data_ptr()
+    if mean:
+        out['mean'] = torch.empty((nsave, save_nodes * E), dtype=torch.complex128, device=dev)
+        a.out_mean = out['mean'].data_ptr()
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    a.status = status.data_ptr()
+    nbytes = ctypes.c_size_t(0)
+    lib = load()
+    _check(lib.qsx_heom_workspace_bytes(ctypes.byref(a), ctypes.byref(nbytes)),
+           'qsx_heom_workspace_bytes')
+    ws = torch.empty(max(nbytes.value, 1), dtype=torch.uint8, device=dev)
+    a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()
+    _check(lib.qsx_heom_rk4(ctypes.byref(a), _stream()), 'qsx_heom_rk4')
+    if check_finite and int(status.item()) & QSX_ERR_NONFINITE:
+        raise IntegratorError('non-finite state during HEOM integration')
+    out['status'] = status
+    return out

@@ -100,6 +100,10 @@ def integrate(f, y0, t, t0=None, method_name='rk4', f_params=None,
     None or a linear map from an operator (e.g. ``V.commutator``,
     ``V.expectation_value``).  A 2-D ``y0`` integrates every row.
     """
+    from ..dynamics.heom import HEOMEquationOfMotion
+    if isinstance(f, HEOMEquationOfMotion):
+        return _integrate_heom(f, y0, t, t0, save_func, precision, step,
+                               kwargs.pop('heom_nodes', None))
     if not isinstance(f, EquationOfMotion):
         raise TypeError('integrate needs an equation of motion returned by a '
                         'qspectra_gb300 model (got {!r})'.format(type(f)))
@@ -134,6 +138,44 @@ def integrate(f, y0, t, t0=None, method_name='rk4', f_params=None,
         state = state[0]
     else:
         state = state.reshape(tuple(y.shape[:-1]) + tuple(state.shape[1:]))
+    return state.cpu().numpy() if as_numpy else state
+
+
+def _integrate_heom(f, y0, t, t0, save_func, precision, step, heom_nodes):
+    """integrate() for the HEOM generator: uniform outputs, full state by
+    default (the reference returns every ADO), node 0 only with heom_nodes=1."""
+    t = np.asarray(t, float)
+    if t0 is None:
+        t0 = t[0]
+    if step is None:
+        step = (t[1] - t[0]) if len(t) > 1 else 1.0
+    steps = step_plan(t, t0, step)
+    if steps[0] != 0 or (len(steps) > 1 and np.any(np.diff(steps) != steps[1] - steps[0])):
+        raise ValueError('HEOM integration needs uniform output times starting at t0')
+    every = int(steps[1] - steps[0]) if len(steps) > 1 else 1
+    nsteps = every * (len(steps) - 1)
+    tb = f.tables
+    nodes = tb.nnodes if heom_nodes is None else int(heom_nodes)
+    as_numpy = not isinstance(y0, torch.Tensor)
+    y = torch.as_tensor(np.asarray(y0, dtype=complex) if as_numpy else y0,
+                        dtype=torch.complex128, device='cuda')
+    squeeze = y.dim() == 1
+    Y = y[None] if squeeze else y.reshape(-1, y.shape[-1])
+    B = Y.shape[0] if f.Hx.dim() == 2 else f.Hx.shape[0]
+    res = _native.heom_rk4(tb, f.Hx, f.Hy, Y if Y.shape[0] > 1 else Y[0], nsteps, step,
+                           f.model.unit_convert, batch=B, save_every=max(every, 1),
+                           save_nodes=nodes, precision=_precision(precision))
+    state = res['state']
+    if save_func is not None:
+        if not isinstance(save_func, LinearMap):
+            state_np = state.cpu().numpy()
+            out = np.asarray(save_func(state_np))
+            return out[0] if squeeze else out
+        state = state @ save_func.matrix.T
+        if save_func.scalar:
+            state = state[..., 0]
+    if squeeze:
+        state = state[0]
     return state.cpu().numpy() if as_numpy else state
 
 
