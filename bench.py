@@ -55,6 +55,9 @@ def parse_args():
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--fp64-steps', type=int, default=2)
     p.add_argument('--no-heom', action='store_true')
+    p.add_argument('--only-heom', action='store_true',
+                   help='run only the HEOM ring workload (for profiling)')
+    p.add_argument('--heom-samples', type=int, default=64)
     return p.parse_args()
 
 
@@ -355,6 +358,12 @@ def main():
     args = parse_args()
     if args.impl == 'reference':
         return reference_arm(args)
+    if args.only_heom:
+        import torch
+        import qspectra_gb300 as qg
+        from qspectra_gb300 import _native
+        print(json.dumps(heom_ring8(torch, qg, _native, samples=args.heom_samples)), flush=True)
+        return 0
     return our_arm(args)
 
 

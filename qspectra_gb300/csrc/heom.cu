@@ -36,63 +36,124 @@ struct HeomP {
   double uc, h;
 };
 
-// k = RHS(x) for nodes [n0, n0 + nodes_per_cta) of sample b, one thread per
-// element.  Shared: Hx, Hy of the sample and the CTA's node blocks of x.
-template <typename C>
-__device__ __forceinline__ void heom_rhs_elem(const HeomP& p, const C* x, int64_t b,
-                                              int node, int e, const C* sx, const double* sHx,
-                                              const double* sHy, C& out) {
-  using T = decltype(out.x);
+// Per-CTA tables in the working precision T (staged once so the element
+// loop issues no FP64 work in the FP32 form): H blocks, occupations, the
+// low-temperature weights and the term tables of the CTA's nodes.
+template <typename T>
+struct HeomSmem {
+  using C = typename cplx<T>::type;
+  T* Hx;      // nx * nx
+  T* Hy;      // ny * ny
+  T* ox;      // n_sites * nx
+  T* oy;      // n_sites * ny
+  T* W;       // E
+  T* shift;   // npc
+  C* al;      // npc * nterms
+  C* be;      // npc * nterms
+  int* nbr;   // npc * nterms
+  int* site;  // npc * nterms
+  C* x;       // npc * E, this CTA's node blocks of the input
+};
+
+template <typename T>
+__host__ __device__ inline size_t heom_smem_bytes(int nx, int ny, int n_sites, int E, int npc,
+                                                  int nterms) {
+  using C = typename cplx<T>::type;
+  size_t b = (size_t)npc * E * sizeof(C) + 2 * (size_t)npc * nterms * sizeof(C);
+  b += ((size_t)nx * nx + ny * ny + (size_t)n_sites * (nx + ny) + E + npc) * sizeof(T);
+  b += 2 * (size_t)npc * nterms * sizeof(int);
+  return b + 64;
+}
+
+template <typename T>
+__device__ __forceinline__ HeomSmem<T> heom_carve(unsigned char* raw, const HeomP& p, int npc) {
+  using C = typename cplx<T>::type;
+  HeomSmem<T> s;
+  s.x = (C*)raw;
+  s.al = s.x + npc * p.E;
+  s.be = s.al + npc * p.nterms;
+  s.Hx = (T*)(s.be + npc * p.nterms);
+  s.Hy = s.Hx + p.nx * p.nx;
+  s.ox = s.Hy + p.ny * p.ny;
+  s.oy = s.ox + p.n_sites * p.nx;
+  s.W = s.oy + p.n_sites * p.ny;
+  s.shift = s.W + p.E;
+  s.nbr = (int*)(s.shift + npc);
+  s.site = s.nbr + npc * p.nterms;
+  return s;
+}
+
+template <typename T>
+__device__ __forceinline__ void heom_stage_smem(const HeomP& p, const typename cplx<T>::type* x,
+                                                int64_t b, int n0, int npc, HeomSmem<T>& s) {
+  using C = typename cplx<T>::type;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < p.nx * p.nx; i += nt) s.Hx[i] = (T)p.Hx[b * p.Hx_stride + i];
+  for (int i = tid; i < p.ny * p.ny; i += nt) s.Hy[i] = (T)p.Hy[b * p.Hy_stride + i];
+  for (int i = tid; i < p.n_sites * p.nx; i += nt) s.ox[i] = (T)p.occx[i];
+  for (int i = tid; i < p.n_sites * p.ny; i += nt) s.oy[i] = (T)p.occy[i];
+  for (int i = tid; i < p.E; i += nt) s.W[i] = p.W ? (T)p.W[i] : (T)0;
+  const int nn = (npc < p.nnodes - n0 ? npc : p.nnodes - n0);
+  for (int i = tid; i < npc; i += nt) s.shift[i] = i < nn ? (T)p.shift[n0 + i] : (T)0;
+  for (int i = tid; i < npc * p.nterms; i += nt) {
+    const bool ok = i < nn * p.nterms;
+    const int g = n0 * p.nterms + i;
+    s.nbr[i] = ok ? p.nbr[g] : -1;
+    s.site[i] = ok ? p.site[g] : 0;
+    const double2 a = ok ? p.alpha[g] : make_double2(0.0, 0.0);
+    const double2 c = ok ? p.beta[g] : make_double2(0.0, 0.0);
+    s.al[i] = cmk((T)a.x, (T)a.y);
+    s.be[i] = cmk((T)c.x, (T)c.y);
+  }
+  const C* xb = x + (b * p.nnodes + n0) * (int64_t)p.E;
+  for (int i = tid; i < nn * p.E; i += nt) s.x[i] = xb[i];
+  __syncthreads();
+}
+
+// k = RHS(x) for element e of local node `local` (global `node`) of sample b.
+template <typename T>
+__device__ __forceinline__ void heom_rhs_elem(const HeomP& p, const typename cplx<T>::type* x,
+                                              int64_t b, int local, int e, const HeomSmem<T>& s,
+                                              typename cplx<T>::type& out) {
+  using C = typename cplx<T>::type;
   const int a = e % p.nx, bb = e / p.nx;
+  const C* xs = s.x + local * p.E;
   // commutator: -i (Hx x - x Hy)[a][bb]
   T cr = 0, ci = 0;
   for (int c = 0; c < p.nx; ++c) {
-    const T hv = (T)sHx[a * p.nx + c];
-    const C v = sx[c + p.nx * bb];
+    const T hv = s.Hx[a * p.nx + c];
+    const C v = xs[c + p.nx * bb];
     cr = fma(hv, v.x, cr);
     ci = fma(hv, v.y, ci);
   }
   for (int c = 0; c < p.ny; ++c) {
-    const T hv = (T)sHy[c * p.ny + bb];
-    const C v = sx[a + p.nx * c];
+    const T hv = s.Hy[c * p.ny + bb];
+    const C v = xs[a + p.nx * c];
     cr = fma(-hv, v.x, cr);
     ci = fma(-hv, v.y, ci);
   }
   // -i (cr + i ci) = ci - i cr
-  const C self = sx[e];
+  const C self = xs[e];
   T orr = ci, oi = -cr;
-  const T sh = (T)p.shift[node] + (p.W ? (T)p.W[e] : (T)0);
+  const T sh = s.shift[local] + s.W[e];
   orr = fma(-sh, self.x, orr);
   oi = fma(-sh, self.y, oi);
-  const int base = node * p.nterms;
-  const size_t nodesz = (size_t)p.E;
   const C* xb = x + b * (int64_t)p.nnodes * p.E;
+  const int base = local * p.nterms;
   for (int t = 0; t < p.nterms; ++t) {
-    const int nb = p.nbr[base + t];
+    const int nb = s.nbr[base + t];
     if (nb < 0) continue;
-    const int j = p.site[base + t];
-    const double2 al = p.alpha[base + t], be = p.beta[base + t];
-    const double oa = p.occx[j * p.nx + a], ob = p.occy[j * p.ny + bb];
-    const T fr = (T)(al.x * oa + be.x * ob), fi = (T)(al.y * oa + be.y * ob);
-    const C v = xb[nb * nodesz + e];
+    const int j = s.site[base + t];
+    const C al = s.al[base + t], be = s.be[base + t];
+    const T oa = s.ox[j * p.nx + a], ob = s.oy[j * p.ny + bb];
+    const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
+    const C v = xb[(int64_t)nb * p.E + e];
     orr = fma(fr, v.x, fma(-fi, v.y, orr));
     oi = fma(fr, v.y, fma(fi, v.x, oi));
   }
-  out.x = (T)p.uc * orr;
-  out.y = (T)p.uc * oi;
-}
-
-// Shared staging of H and the CTA's node blocks; returns false if this CTA
-// has no nodes.  blockDim = nodes_per_cta * E (rounded up to a warp).
-template <typename C>
-__device__ __forceinline__ void heom_stage_smem(const HeomP& p, const C* x, int64_t b,
-                                                int n0, int npc, C* sx, double* sHx, double* sHy) {
-  for (int i = threadIdx.x; i < p.nx * p.nx; i += blockDim.x) sHx[i] = p.Hx[b * p.Hx_stride + i];
-  for (int i = threadIdx.x; i < p.ny * p.ny; i += blockDim.x) sHy[i] = p.Hy[b * p.Hy_stride + i];
-  const C* xb = x + (b * p.nnodes + n0) * (int64_t)p.E;
-  const int cnt = (npc < p.nnodes - n0 ? npc : p.nnodes - n0) * p.E;
-  for (int i = threadIdx.x; i < cnt; i += blockDim.x) sx[i] = xb[i];
-  __syncthreads();
+  const T uc = (T)p.uc;
+  out.x = uc * orr;
+  out.y = uc * oi;
 }
 
 // One RK4 stage (see qsx_heom_rk4): k = RHS(in); stage 0..2 write the next
@@ -105,17 +166,15 @@ __global__ void __launch_bounds__(256)
                       typename cplx<T>::type* __restrict__ next, int npc) {
   using C = typename cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
-  double* sHx = (double*)smraw;
-  double* sHy = sHx + p.nx * p.nx;
-  C* sx = (C*)(sHy + p.ny * p.ny + ((p.nx * p.nx + p.ny * p.ny) & 1));
+  HeomSmem<T> sm = heom_carve<T>(smraw, p, npc);
   const int64_t b = blockIdx.y;
   const int n0 = blockIdx.x * npc;
-  heom_stage_smem(p, in, b, n0, npc, sx, sHx, sHy);
+  heom_stage_smem<T>(p, in, b, n0, npc, sm);
   const int local = threadIdx.x / p.E, e = threadIdx.x % p.E;
   const int node = n0 + local;
   if (local >= npc || node >= p.nnodes) return;
   C k;
-  heom_rhs_elem(p, in, b, node, e, sx + local * p.E, sHx, sHy, k);
+  heom_rhs_elem<T>(p, in, b, local, e, sm, k);
   const int64_t idx = (b * p.nnodes + node) * (int64_t)p.E + e;
   const T h = (T)p.h;
   if (stage == 0) {
@@ -150,17 +209,15 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     heom_rhs_kernel(HeomP p, const double2* __restrict__ x, double2* __restrict__ out, int npc) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  double* sHx = (double*)smraw;
-  double* sHy = sHx + p.nx * p.nx;
-  double2* sx = (double2*)(sHy + p.ny * p.ny + ((p.nx * p.nx + p.ny * p.ny) & 1));
+  HeomSmem<double> sm = heom_carve<double>(smraw, p, npc);
   const int64_t b = blockIdx.y;
   const int n0 = blockIdx.x * npc;
-  heom_stage_smem(p, x, b, n0, npc, sx, sHx, sHy);
+  heom_stage_smem<double>(p, x, b, n0, npc, sm);
   const int local = threadIdx.x / p.E, e = threadIdx.x % p.E;
   const int node = n0 + local;
   if (local >= npc || node >= p.nnodes) return;
   double2 k;
-  heom_rhs_elem(p, x, b, node, e, sx + local * p.E, sHx, sHy, k);
+  heom_rhs_elem<double>(p, x, b, local, e, sm, k);
   out[(b * p.nnodes + node) * (int64_t)p.E + e] = k;
 }
 
@@ -288,7 +345,11 @@ int qsx_heom_rhs(const qsx_heom_args* a, const double* x, double* out, void* str
   HeomP p = heom_params(a);
   const int npc = std::max(1, 256 / p.E);
   const int threads = ((npc * p.E + 31) / 32) * 32;
-  const size_t smem = (p.nx * p.nx + p.ny * p.ny + 1) * sizeof(double) + npc * p.E * sizeof(double2);
+  const size_t smem = heom_smem_bytes<double>(p.nx, p.ny, p.n_sites, p.E, npc, p.nterms);
+  QSX_CHECK_ARG(smem <= 227 * 1024, "qsx_heom_rhs: node tables too large for shared memory");
+  cudaError_t ce = cudaFuncSetAttribute(heom_rhs_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (ce != cudaSuccess) return cuda_status(ce, "qsx_heom_rhs");
   dim3 grid((unsigned)((p.nnodes + npc - 1) / npc), (unsigned)p.batch);
   heom_rhs_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(p, (const double2*)x,
                                                                  (double2*)out, npc);
@@ -327,7 +388,11 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
     C* s1 = s0 + n;
     double2* saves = (double2*)(((size_t)(s1 + n) + 255) & ~(size_t)255);
     if (!node0) node0 = saves;
-    const size_t smem = (p.nx * p.nx + p.ny * p.ny + 1) * sizeof(double) + npc * p.E * sizeof(C);
+    const size_t smem = heom_smem_bytes<T>(p.nx, p.ny, p.n_sites, p.E, npc, p.nterms);
+    QSX_CHECK_ARG(smem <= 227 * 1024, "qsx_heom_rk4: node tables too large for shared memory");
+    cudaError_t ce = cudaFuncSetAttribute(heom_stage_kernel<T>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (ce != cudaSuccess) return cuda_status(ce, "qsx_heom_rk4");
     heom_init_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
         (const double2*)a->y0, a->y0_stride ? per : 0, per, p.batch, yh, yl);
     QSX_LAUNCH_CHECK("qsx_heom_rk4 init");
