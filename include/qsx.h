@@ -269,6 +269,70 @@ int qsx_heom_rk4(const qsx_heom_args* args, void* stream);
 size_t qsx_heom_args_bytes(void);
 
 /*
+ * Two-exciton (f) manifold in operator form, for third_order_response
+ * (qspectra/simulate/response.py:267-337) at site counts where the dense
+ * 'gef' Redfield tensor (qspectra/dynamics/redfield.py:9-74, n^4 entries)
+ * cannot be built.  N sites, P = N(N-1)/2 pair states (k < l, the
+ * all_states order of qspectra/operator_tools.py:122-152).
+ *
+ * qsx_fblock_tensor: the eigenbasis tensor of the f manifold,
+ *   Y_i[c][d] = uc * (U^T diag(occ_i) U)[c][d] * C(E_d - E_c)
+ * (the per-manifold restriction of redfield.py:41-69), so that
+ * M_i^f = U Y_i U^T.  E float64 [batch][P] and U float64 [batch][P][P]
+ * (columns = eigenvectors) of the f-block Hamiltonian; site_pairs int32
+ * [N][N-1] lists the pair states containing each site.  Y is written in the
+ * working precision (FP32 or FP64) as [batch][P][2N][P]: planes 0..N-1 hold
+ * Re Y_i, planes N..2N-1 hold Im Y_i.
+ */
+int qsx_fblock_tensor(const double* E, const double* U, int P, int N,
+                      const int* site_pairs, int64_t batch, double temperature,
+                      double reorg_energy, double cutoff_freq, int matsubara_cutoff,
+                      int discard_imag_corr, double unit_convert, int precision,
+                      void* Y, void* stream);
+
+/*
+ * qsx_fe_generator: column operators of the 'fe' Liouville block,
+ *   Q[s][q][b][r] = M_b^f[q][r] - G^f[q][r] - i uc H^f[q][r],
+ * G^f = sum_i diag(occ_i) M_i^f.  M in the plane layout of
+ * qsx_fblock_tensor (after both basis transforms), H float64 [batch][P][P]
+ * rotating-frame f-block Hamiltonian, pair_sites int32 [P][2].  Q complex in
+ * the working precision, [batch][P][N][P].
+ */
+int qsx_fe_generator(const void* M, const double* H, int P, int N, int64_t batch,
+                     const int* pair_sites, double unit_convert, int precision,
+                     void* Q, void* stream);
+
+/*
+ * qsx_fe_heisenberg_rk4: fixed-step RK4 of the Heisenberg-picture 'fe' block
+ * (the plain transpose of L restricted to 'fe', liouville_space.py:316-341),
+ * as integrate() runs it for the t3 leg of the excited-state-absorption
+ * pathways (response.py:323-336).  Q from qsx_fe_generator; Ae = G^e + i uc
+ * H^e complex [batch][N][N] and Me complex [batch][N][N][N] (Me[i] = M_i^e,
+ * site basis, including uc) in the working precision.  y0 complex128
+ * [batch][P*N] with stride y0_stride (0 = shared), column-stacked over the
+ * block.  out complex128 [batch][nsteps+1][P*N]: the state at every step.
+ * FP32 keeps a split-word (hi + lo) state.  Workspace:
+ * qsx_fe_heisenberg_workspace_bytes.  status: QSX_ERR_NONFINITE on NaN/Inf.
+ */
+size_t qsx_fe_heisenberg_workspace_bytes(int P, int N, int64_t batch, int precision);
+int qsx_fe_heisenberg_rk4(const void* Q, const void* Ae, const void* Me,
+                          const int* pair_sites, int P, int N, int64_t batch,
+                          int precision, const double* y0, int64_t y0_stride,
+                          int nsteps, double h, double* out, void* workspace,
+                          size_t workspace_bytes, int32_t* status, void* stream);
+
+/*
+ * qsx_csr_map_batched: out[b][r] = sum_k vals[k] * in[b][cols[k]] over
+ * rowptr[r] <= k < rowptr[r+1]: a sparse dipole super-operator
+ * (LiouvilleSpaceOperator.commutator, liouville_space.py:151-209) applied to
+ * a batch of Liouville vectors.  in complex128 [batch][n_in], out complex128
+ * [batch][n_out], vals complex128, rowptr/cols int32.
+ */
+int qsx_csr_map_batched(const double* in, int64_t n_in, int64_t batch,
+                        const int* rowptr, const int* cols, const double* vals,
+                        int n_out, double* out, void* stream);
+
+/*
  * Direct discrete Fourier transform of uniformly sampled signals,
  *   X[b][k] = dt * sum_n x[b][n] exp(i * sign * (freqs[k] - rw_freq) * uc * t_n),
  * t_n = t0 + n dt.  With freqs on the FFT grid this equals fourier_transform

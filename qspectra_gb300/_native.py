@@ -101,6 +101,18 @@ _PROTOS = {
     'qsx_dft_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
                                  _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_probe_fma': (_c_int, [_c_int, _c_i64, _c_int, _c_int, _c_vp, _c_vp]),
+    'qsx_fblock_tensor': (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_vp, _c_i64, _c_dbl,
+                                   _c_dbl, _c_dbl, _c_int, _c_int, _c_dbl, _c_int,
+                                   _c_vp, _c_vp]),
+    'qsx_fe_generator': (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_i64, _c_vp, _c_dbl,
+                                  _c_int, _c_vp, _c_vp]),
+    'qsx_fe_heisenberg_workspace_bytes': (ctypes.c_size_t, [_c_int, _c_int, _c_i64,
+                                                            _c_int]),
+    'qsx_fe_heisenberg_rk4': (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_i64,
+                                       _c_int, _c_vp, _c_i64, _c_int, _c_dbl, _c_vp,
+                                       _c_vp, ctypes.c_size_t, _c_vp, _c_vp]),
+    'qsx_csr_map_batched': (_c_int, [_c_vp, _c_i64, _c_i64, _c_vp, _c_vp, _c_vp, _c_int,
+                                     _c_vp, _c_vp]),
 }
 
 _LIB = None
@@ -470,3 +482,105 @@ def heom_rk4(tables, Hx, Hy, y0, nsteps, h, unit_convert, batch=None, save_every
         raise IntegratorError('non-finite state during HEOM integration')
     out['status'] = status
     return out
+
+
+# ------------------------------------------------- two-exciton (f) manifold
+def _real_dtype(precision):
+    return torch.float32 if precision == QSX_FP32 else torch.float64
+
+
+def _cplx_dtype(precision):
+    return torch.complex64 if precision == QSX_FP32 else torch.complex128
+
+
+def fblock_tensor(E, U, n_sites, site_pairs, bath, unit_convert, precision=QSX_FP64,
+                  discard_imag_corr=False, matsubara_cutoff=1000):
+    """Eigenbasis f-manifold tensor planes Y (B, P, 2N, P) in the working precision."""
+    require_gpu()
+    _need(E, torch.float64, 'E', 2)
+    _need(U, torch.float64, 'U', 3)
+    _need(site_pairs, torch.int32, 'site_pairs', 2)
+    B, P = E.shape
+    Y = torch.empty((B, P, 2 * n_sites, P), dtype=_real_dtype(precision), device=E.device)
+    _check(load().qsx_fblock_tensor(
+        _p(E), _p(U), P, n_sites, _p(site_pairs), B, bath.temperature, bath.reorg_energy,
+        bath.cutoff_freq, matsubara_cutoff, int(discard_imag_corr), unit_convert,
+        precision, _p(Y), _stream()), 'qsx_fblock_tensor')
+    return Y
+
+
+def fe_generator(M, H, pair_sites, unit_convert, precision=QSX_FP64):
+    """Column operators Q (B, P, N, P) of the 'fe' block from the site-basis planes M."""
+    require_gpu()
+    _need(M, _real_dtype(precision), 'M', 4)
+    _need(H, torch.float64, 'H', 3)
+    _need(pair_sites, torch.int32, 'pair_sites', 2)
+    B, P, twoN, _ = M.shape
+    N = twoN // 2
+    Q = torch.empty((B, P, N, P), dtype=_cplx_dtype(precision), device=M.device)
+    _check(load().qsx_fe_generator(_p(M), _p(H), P, N, B, _p(pair_sites), unit_convert,
+                                   precision, _p(Q), _stream()), 'qsx_fe_generator')
+    return Q
+
+
+def fe_heisenberg_rk4(Q, Ae, Me, pair_sites, y0, nsteps, h, precision=QSX_FP64,
+                      check_finite=True):
+    """States (B, nsteps+1, P*N) complex128 of the Heisenberg 'fe' RK4 loop."""
+    require_gpu()
+    cd = _cplx_dtype(precision)
+    _need(Q, cd, 'Q', 4)
+    _need(Ae, cd, 'Ae', 3)
+    _need(Me, cd, 'Me', 4)
+    _need(pair_sites, torch.int32, 'pair_sites', 2)
+    B, P, N, _ = Q.shape
+    y0 = y0.to(torch.complex128).contiguous()
+    if y0.shape[-1] != P * N:
+        raise ValueError('y0 must have P*N = {} components'.format(P * N))
+    stride = 0 if y0.dim() == 1 else P * N
+    lib = load()
+    ws_bytes = lib.qsx_fe_heisenberg_workspace_bytes(P, N, B, precision)
+    ws = torch.empty(max(int(ws_bytes), 1), dtype=torch.uint8, device=Q.device)
+    out = torch.empty((B, nsteps + 1, P * N), dtype=torch.complex128, device=Q.device)
+    status = torch.zeros(1, dtype=torch.int32, device=Q.device)
+    _check(lib.qsx_fe_heisenberg_rk4(_p(Q), _p(Ae), _p(Me), _p(pair_sites), P, N, B,
+                                     precision, _p(y0), stride, int(nsteps), float(h),
+                                     _p(out), _p(ws), ws.numel(), _p(status), _stream()),
+           'qsx_fe_heisenberg_rk4')
+    if check_finite and int(status.item()) & QSX_ERR_NONFINITE:
+        raise IntegratorError('non-finite state in the fe propagation')
+    return out
+
+
+class CsrMap:
+    """A sparse Liouville-space map (rows = outputs) resident on the GPU."""
+
+    def __init__(self, dense, device='cuda'):
+        dense = np.asarray(dense, dtype=complex)
+        self.shape = dense.shape
+        rows, cols = np.nonzero(dense)
+        order = np.lexsort((cols, rows))
+        rows, cols = rows[order], cols[order]
+        rowptr = np.zeros(dense.shape[0] + 1, dtype=np.int32)
+        np.add.at(rowptr, rows + 1, 1)
+        rowptr = np.cumsum(rowptr).astype(np.int32)
+        vals = dense[rows, cols]
+        if len(vals) == 0:  # keep valid pointers for an all-zero map
+            cols = np.zeros(1, dtype=np.int64)
+            vals = np.zeros(1, dtype=complex)
+        self.rowptr = torch.as_tensor(rowptr, device=device)
+        self.cols = torch.as_tensor(cols.astype(np.int32), device=device)
+        self.vals = torch.as_tensor(vals, dtype=torch.complex128, device=device)
+
+    def __call__(self, x):
+        """x (..., n_in) complex128 CUDA -> (..., n_out)."""
+        require_gpu()
+        n_out, n_in = self.shape
+        if x.shape[-1] != n_in:
+            raise ValueError('map takes {} components (got {})'.format(n_in, x.shape[-1]))
+        lead = x.shape[:-1]
+        xb = x.to(torch.complex128).reshape(-1, n_in).contiguous()
+        out = torch.empty((xb.shape[0], n_out), dtype=torch.complex128, device=x.device)
+        _check(load().qsx_csr_map_batched(_p(xb), n_in, xb.shape[0], _p(self.rowptr),
+                                          _p(self.cols), _p(self.vals), n_out, _p(out),
+                                          _stream()), 'qsx_csr_map_batched')
+        return out.reshape(tuple(lead) + (n_out,))

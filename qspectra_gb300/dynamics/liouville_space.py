@@ -159,8 +159,20 @@ class LiouvilleSpaceOperator(SystemOperator):
             self._maps[key] = LinearMap(build(), scalar)
         return self._maps[key]
 
+    def _restricted(self, side):
+        """kron(I, V) (side 'left') or kron(V^T, I) ('right') restricted to
+        to x from indices, without forming the n^2 x n^2 super-operator:
+        element (a + n b, c + n d) is V[a, c] [b == d] or V[d, b] [a == c]."""
+        V = np.asarray(self.operator)
+        n = len(V)
+        ta, tb = self.to_indices % n, self.to_indices // n
+        fc, fd = self.from_indices % n, self.from_indices // n
+        if side == 'left':
+            return V[np.ix_(ta, fc)] * (tb[:, None] == fd[None, :])
+        return V[np.ix_(fd, tb)].T * (ta[:, None] == fc[None, :])
+
     def _left(self):
-        return super_left_matrix(self.operator)[self.super_op_mesh]
+        return self._restricted('left')
 
     @property
     def left_multiply(self):
@@ -168,15 +180,21 @@ class LiouvilleSpaceOperator(SystemOperator):
 
     @property
     def right_multiply(self):
-        return self._map('right', lambda: super_right_matrix(self.operator)[self.super_op_mesh])
+        return self._map('right', lambda: self._restricted('right'))
 
     @property
     def commutator(self):
-        return self._map('comm', lambda: super_commutator_matrix(self.operator)[self.super_op_mesh])
+        return self._map('comm', lambda: self.commutator_matrix)
+
+    @property
+    def commutator_matrix(self):
+        """Host (to x from) matrix of the restricted commutator [V, .]."""
+        return self._restricted('left') - self._restricted('right')
 
     @property
     def expectation_row(self):
-        tr = np.identity(len(self.operator)).reshape(-1)[self.to_indices]
+        n = len(self.operator)
+        tr = (self.to_indices % n == self.to_indices // n).astype(float)
         return tr.dot(self._left())
 
     @property

@@ -86,12 +86,17 @@ def operator_extend(operator1, subspace='gef'):
 def transition_operator(n, n_sites, subspace='gef', include_transitions='-+'):
     """Create ('+') and/or annihilate ('-') an excitation on site n (operator_tools.py:238-270)."""
     states = all_states(n_sites, subspace)
+    where = {tuple(st): k for k, st in enumerate(states)}
     out = np.zeros((len(states), len(states)))
-    for r, si in enumerate(states):
-        for c, sj in enumerate(states):
-            create = '+' in include_transitions and si == sorted(sj + [n])
-            destroy = '-' in include_transitions and sorted(si + [n]) == sj
-            if create or destroy:
+    for c, sj in enumerate(states):
+        # create: the state with site n added; destroy: the state with n removed
+        if '+' in include_transitions and n not in sj:
+            r = where.get(tuple(sorted(sj + [n])))
+            if r is not None:
+                out[r, c] = 1
+        if '-' in include_transitions and n in sj:
+            r = where.get(tuple(x for x in sj if x != n))
+            if r is not None:
                 out[r, c] = 1
     return out
 

@@ -175,9 +175,22 @@ def third_order_response(dynamical_model, coherence_time_max,
                          ensemble_size=None, ensemble_random_orientations=False,
                          exact_isotropic_average=False, precision='fp64',
                          **integrate_kwargs):
-    """Third-order response function under the RWA (response.py:340-427)."""
+    """Third-order response function under the RWA (response.py:340-427).
+
+    Non-secular site-basis Redfield models on 'gef' with geometry '-++' or
+    '+-+' run on the batched engine (simulate/third_order.py): every sample
+    of an ensemble in one pass, the two-exciton block in operator form.
+    Other models and geometries integrate each pathway's dense blocks.
+    """
     if exact_isotropic_average or ensemble_random_orientations:
         raise NotImplementedError('isotropic averaging is not on the accelerated path')
+    from .third_order import supports, third_order_ensemble
+    if supports(dynamical_model, geometry) and not integrate_kwargs:
+        if population_times is None:
+            population_times = np.arange(0, population_time_max, dynamical_model.time_step)
+        return third_order_ensemble(dynamical_model, coherence_time_max, population_times,
+                                    geometry, polarization, include_signal, ensemble_size,
+                                    precision)
     if ensemble_size is None:
         return _single_third_order(dynamical_model, coherence_time_max,
                                    population_time_max, population_times, geometry,
