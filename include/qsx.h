@@ -269,6 +269,39 @@ int qsx_heom_rk4(const qsx_heom_args* args, void* stream);
 size_t qsx_heom_args_bytes(void);
 
 /*
+ * Batched FP64 symmetric eigensolver for n up to 2048 (the two-exciton
+ * block; the reference calls scipy.linalg.eigh per sample,
+ * qspectra/hamiltonian.py:310-328): Householder tridiagonalisation, then
+ * implicit QL, one CTA per matrix.  H float64 [batch][n][n] symmetric;
+ * E float64 [batch][n] ascending; U float64 [batch][n][n], column k the
+ * eigenvector of E[k].  Workspace: qsx_eigh_large_workspace_bytes.
+ * status: QSX_ERR_NONFINITE when a QL iteration fails to converge.
+ */
+size_t qsx_eigh_large_workspace_bytes(int n, int64_t batch);
+int qsx_eigh_large_batched(const double* H, int n, int64_t batch, double* E,
+                           double* U, void* workspace, size_t workspace_bytes,
+                           int32_t* status, void* stream);
+
+/*
+ * Adjoint of the ensemble-mean projected RK4 loop (no reference
+ * counterpart: the reference has no gradients; this differentiates the
+ * linear_response / absorption_spectra path, qspectra/simulate/
+ * response.py:15-154, averaged over the ensemble, decorators.py:40-64).
+ * Forward: y_{k+1} = (I + D_s) y_k, x_n = scale * sum_s c^T y_{s,n}.
+ * Given cotangents g[n] (complex128 [nsteps+1], PyTorch's convention for
+ * complex tensors), writes gradD complex128 [batch][m][m] =
+ * sum_k lam_{k+1} y_k^H with lam_N = scale g_N conj(c) and
+ * lam_k = (I + D)^H lam_{k+1} + scale g_k conj(c), and, when grady0 is not
+ * NULL, lam_0 per sample (complex128 [batch][m]).  checkpoints complex128
+ * [batch][nck][m] hold y at steps 0, ck_every, 2 ck_every, ... (nck *
+ * ck_every >= nsteps); each segment is recomputed on the device.  m <= 32.
+ */
+int qsx_rk4_adjoint_batched(const double* D, int m, int64_t batch, int nsteps,
+                            const double* checkpoints, int ck_every, int nck,
+                            const double* c, const double* g, double scale,
+                            double* gradD, double* grady0, void* stream);
+
+/*
  * Two-exciton (f) manifold in operator form, for third_order_response
  * (qspectra/simulate/response.py:267-337) at site counts where the dense
  * 'gef' Redfield tensor (qspectra/dynamics/redfield.py:9-74, n^4 entries)

@@ -113,6 +113,11 @@ _PROTOS = {
                                        _c_vp, ctypes.c_size_t, _c_vp, _c_vp]),
     'qsx_csr_map_batched': (_c_int, [_c_vp, _c_i64, _c_i64, _c_vp, _c_vp, _c_vp, _c_int,
                                      _c_vp, _c_vp]),
+    'qsx_eigh_large_workspace_bytes': (ctypes.c_size_t, [_c_int, _c_i64]),
+    'qsx_eigh_large_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_vp, _c_vp, _c_vp,
+                                        ctypes.c_size_t, _c_vp, _c_vp]),
+    'qsx_rk4_adjoint_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_vp, _c_int,
+                                         _c_int, _c_vp, _c_vp, _c_dbl, _c_vp, _c_vp, _c_vp]),
 }
 
 _LIB = None
@@ -584,3 +589,43 @@ class CsrMap:
                                           _p(self.cols), _p(self.vals), n_out, _p(out),
                                           _stream()), 'qsx_csr_map_batched')
         return out.reshape(tuple(lead) + (n_out,))
+
+
+def rk4_adjoint(D, checkpoints, ck_every, nsteps, c, g, scale, want_y0=False):
+    """grad of sum_n Re(conj(g_n) x_n) w.r.t. D (and y0) for the mean projected
+    RK4 loop (qsx_rk4_adjoint_batched).  D (B, m, m) complex128; checkpoints
+    (B, nck, m) complex128; c (m,), g (nsteps+1,) complex128."""
+    require_gpu()
+    _need(D, torch.complex128, 'D', 3)
+    _need(checkpoints, torch.complex128, 'checkpoints', 3)
+    c = _need(c.to(torch.complex128).contiguous(), torch.complex128, 'c', 1)
+    g = _need(g.to(torch.complex128).contiguous(), torch.complex128, 'g', 1)
+    B, m, _ = D.shape
+    if g.numel() != nsteps + 1 or c.numel() != m:
+        raise ValueError('g needs nsteps+1 entries and c m entries')
+    gradD = torch.empty_like(D)
+    gy = torch.empty((B, m), dtype=torch.complex128, device=D.device) if want_y0 else None
+    _check(load().qsx_rk4_adjoint_batched(_p(D), m, B, int(nsteps), _p(checkpoints),
+                                          int(ck_every), checkpoints.shape[1], _p(c), _p(g),
+                                          float(scale), _p(gradD), _p(gy), _stream()),
+           'qsx_rk4_adjoint_batched')
+    return (gradD, gy) if want_y0 else gradD
+
+
+def eigh_large(H):
+    """Batched FP64 eigensolver (Householder + implicit QL) for any n <= 2048.
+    H (B, n, n) float64 CUDA, symmetric.  Returns E ascending and U."""
+    require_gpu()
+    _need(H, torch.float64, 'H', 3)
+    B, n, _ = H.shape
+    lib = load()
+    ws = torch.empty(max(int(lib.qsx_eigh_large_workspace_bytes(n, B)), 1), dtype=torch.uint8,
+                     device=H.device)
+    E = torch.empty((B, n), dtype=torch.float64, device=H.device)
+    U = torch.empty((B, n, n), dtype=torch.float64, device=H.device)
+    status = torch.zeros(1, dtype=torch.int32, device=H.device)
+    _check(lib.qsx_eigh_large_batched(_p(H), n, B, _p(E), _p(U), _p(ws), ws.numel(),
+                                      _p(status), _stream()), 'qsx_eigh_large_batched')
+    if int(status.item()):
+        raise QsxError('qsx_eigh_large_batched: QL iteration did not converge')
+    return E, U

@@ -30,8 +30,11 @@ class SampleBatch:
         ham = model.hamiltonian
         if offsets is None:
             offsets = ham.disorder_offsets(size, start)
-        self.offsets = torch.as_tensor(np.asarray(offsets, float),
-                                       dtype=torch.float64).cuda()
+        if isinstance(offsets, torch.Tensor):
+            self.offsets = offsets.to(device='cuda', dtype=torch.float64)
+        else:
+            self.offsets = torch.as_tensor(np.asarray(offsets, float),
+                                           dtype=torch.float64).cuda()
 
     def H(self, subspace):
         ham = self.model.hamiltonian

@@ -9,7 +9,8 @@ block-diagonal over the g/e/f manifolds, so this engine never forms the
 
 * g and e blocks come from a 'ge' Redfield build (batched FP64 Jacobi
   eigensolve and operator-form tensor, one CTA per sample);
-* the f manifold is diagonalised per sample (FP64), its eigenbasis tensor
+* the f manifold is diagonalised per sample (FP64 Householder + QL kernel),
+  its eigenbasis tensor
   Kt_i o C is built in FP64 by ``qsx_fblock_tensor``, and two batched GEMMs
   bring M_i^f to the site basis in the working precision;
 * t1 and the 'eg' t3 leg run in the batched RK4 kernels; the t2 leg applies
@@ -165,8 +166,7 @@ class ThirdOrderEngine:
         self._pair_sites = torch.as_tensor(pair_sites).cuda()
         sp = torch.as_tensor(site_pairs).cuda()
         Hf = batch.H('f')
-        Ef, Uf = torch.linalg.eigh(Hf)
-        Ef, Uf = Ef.contiguous(), Uf.contiguous()
+        Ef, Uf = _native.eigh_large(Hf)
         Y = _native.fblock_tensor(Ef, Uf, N, sp, ham.bath, model.unit_convert, self.prec,
                                   model.discard_imag_corr,
                                   ham.bath.matsubara_cutoff)
@@ -190,8 +190,7 @@ class ThirdOrderEngine:
         cdt = torch.complex64 if prec == _native.QSX_FP32 else torch.complex128
         uc, dt = model.unit_convert, self.dt
         pol = self.polarization
-        offsets = torch.as_tensor(offsets, dtype=torch.float64).cuda()
-        S = offsets.shape[0]
+        S = len(offsets)
         batch = SampleBatch(model, S, offsets=offsets)
         ham = model.hamiltonian
         _tick(events, 'build')
