@@ -58,6 +58,12 @@ def parse_args():
     p.add_argument('--only-heom', action='store_true',
                    help='run only the HEOM ring workload (for profiling)')
     p.add_argument('--heom-samples', type=int, default=64)
+    p.add_argument('--no-third', action='store_true')
+    p.add_argument('--no-adjoint', action='store_true')
+    p.add_argument('--only', choices=['heom', 'third', 'adjoint'],
+                   help='run one auxiliary workload alone and print its JSON')
+    p.add_argument('--third-samples', type=int, default=256)
+    p.add_argument('--adjoint-samples', type=int, default=1024)
     return p.parse_args()
 
 
@@ -217,6 +223,145 @@ def heom_ring8(torch, qg, native, samples=64, nsteps=1999):
     return out
 
 
+def third_order_chain24(torch, qg, samples=256, fp64_samples=8, reps=2):
+    """Third-order response: 24-site chain (E ~ N(12300, 100^2), -80 / +15
+    cm^-1 couplings, seed 2024), Debye bath lambda = 40, gamma = 100, 300 K,
+    non-secular Redfield on 'gef' (276 two-exciton states), t1 = t3 = 128 x
+    2 fs, t2 in {0, 200, 500} fs, rephasing and non-rephasing geometries
+    (GSB + ESE + ESA each), 256 disorder samples (SD 60 cm^-1), FP32 bulk."""
+    from qspectra_gb300 import workloads as wl
+    from qspectra_gb300.simulate.third_order import ThirdOrderEngine
+    H = wl.chain_hamiltonian(n_sites=24, seed=2024)
+    extra = wl.energy_spread_for_dt(H, 2.0, qg.CM_FS)
+    ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 300, 40, 100),
+                                   dipoles=[[1, 0, 0]] * 24, disorder=wl.fwhm_for_sd(60.0),
+                                   random_seed=3, energy_spread_extra=extra)
+    m = qg.RedfieldModel(ham, hilbert_subspace='gef', unit_convert=qg.CM_FS, secular=False)
+    offs = m.hamiltonian.disorder_offsets(samples)
+    eng = ThirdOrderEngine(m, 256.0, [0.0, 200.0, 500.0], precision='fp32')
+    eng.run(offs)
+    torch.cuda.synchronize()
+    best, phases = None, None
+    for _ in range(reps):
+        ev = {}
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = eng.run(offs, events=ev)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if best is None or ms < best:
+            mk = ev['marks']
+            best = ms
+            phases = {mk[i][0]: mk[i][1].elapsed_time(mk[i + 1][1]) for i in range(len(mk) - 1)}
+    sub = offs[:fp64_samples]
+    r64 = ThirdOrderEngine(m, 256.0, [0.0, 200.0, 500.0], precision='fp64').run(sub)
+    r32 = ThirdOrderEngine(m, 256.0, [0.0, 200.0, 500.0], precision='fp32').run(sub)
+    err = max(float((r32[g] - r64[g]).abs().max() / r64[g].abs().max()) for g in r64)
+    return {'workload': '24-site chain third-order response, 276 two-exciton states, '
+                        't1 = t3 = 128 x 2 fs, t2 = 0/200/500 fs, both geometries, '
+                        '{} samples (SD 60 cm^-1), FP32 bulk'.format(samples),
+            'ms_per_ensemble': best, 'ensembles_per_s': 1000.0 / best,
+            'phases_ms': phases,
+            'fp32_vs_fp64_rel_err': err, 'fp64_check_samples': fp64_samples,
+            'output_shape': list(out['-++'].shape)}
+
+
+def adjoint_fmo7(torch, qg, samples=1024, adam_steps=200):
+    """Gradient of the absorption misfit (1024 frequencies, 11800-13000 cm^-1)
+    of the 7-site model's 1024-sample ensemble (SD 80 cm^-1) w.r.t. 7 site
+    energies, 21 couplings and lambda; 2048 points at 1 fs, checkpoints every
+    64 steps.  Adjoint time vs forward time, FD and autograd checks, Adam."""
+    from qspectra_gb300 import workloads as wl
+    from qspectra_gb300.simulate.adjoint import AbsorptionFit
+    H7, extra, fwhm = fmo7_inputs()
+    ham = qg.ElectronicHamiltonian(H7, bath=qg.DebyeBath(qg.CM_K * 77, 35, 106),
+                                   dipoles=[[1, 0, 0]] * 7, disorder=fwhm, random_seed=1,
+                                   energy_spread_extra=extra)
+    m = qg.RedfieldModel(ham, hilbert_subspace='ge', unit_convert=qg.CM_FS, secular=False)
+    freqs = np.linspace(11800.0, 13000.0, 1024)
+    fit = AbsorptionFit(7, ham.disorder_offsets(samples), freqs, rw_freq=m.rw_freq, dt=1.0,
+                        nsteps=2047, ck_every=64)
+    theta_true = fit.pack(H7, 35.0)
+    target = fit.spectrum(theta_true).detach()
+    rng = np.random.RandomState(11)
+    theta0 = theta_true.clone()
+    theta0[:7] += torch.as_tensor(rng.randn(7) * 8.0).cuda()
+    theta0[7:-1] += torch.as_tensor(rng.randn(21) * 4.0).cuda()
+    theta0[-1] += 5.0
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) * 1000.0
+            best = dt if best is None else min(best, dt)
+        return best
+
+    def forward():
+        with torch.no_grad():
+            return fit.misfit(theta0, target)
+
+    holder = {}
+
+    def fwd_graph():
+        th = theta0.clone().requires_grad_(True)
+        holder['th'] = th
+        holder['loss'] = fit.misfit(th, target)
+
+    def bwd():
+        holder['loss'].backward()
+
+    fwd_ms = timed(forward)
+    fwdg_ms = timed(fwd_graph)
+    bwd_samples = []
+    for _ in range(5):
+        fwd_graph()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bwd()
+        torch.cuda.synchronize()
+        bwd_samples.append((time.perf_counter() - t0) * 1000.0)
+    bwd_ms = min(bwd_samples)
+    g_adj = holder['th'].grad.detach().cpu().numpy()
+    th2 = theta0.clone().requires_grad_(True)
+    fit.misfit(th2, target, impl='autograd').backward()
+    g_ref = th2.grad.detach().cpu().numpy()
+    h = 1e-3
+    fd = np.zeros_like(g_adj)
+    with torch.no_grad():
+        for i in range(len(fd)):
+            e = torch.zeros_like(theta0)
+            e[i] = h
+            fd[i] = ((fit.misfit(theta0 + e, target) - fit.misfit(theta0 - e, target))
+                     / (2 * h)).item()
+    rel = lambda a, b: float(np.abs(a - b).max() / np.abs(b).max())  # noqa: E731
+    t0 = time.perf_counter()
+    theta_fit, hist = fit.fit(theta0, target, steps=adam_steps, lr=0.5)
+    torch.cuda.synchronize()
+    adam_s = time.perf_counter() - t0
+    err0 = (theta0 - theta_true).abs()
+    err1 = (theta_fit - theta_true).abs()
+    return {'workload': '7-site Redfield absorption misfit on 1024 frequencies '
+                        '(11800-13000 cm^-1), {} disorder samples (SD 80 cm^-1), 2048 x '
+                        '1 fs, checkpoints every 64 steps, 29 parameters'.format(samples),
+            'forward_ms': fwd_ms, 'forward_with_graph_ms': fwdg_ms, 'adjoint_ms': bwd_ms,
+            'adjoint_over_forward': bwd_ms / fwd_ms,
+            'grad_rel_err_vs_central_fd_h1e-3': rel(g_adj, fd),
+            'grad_rel_err_vs_fp64_autograd_rk4': rel(g_adj, g_ref),
+            'adam': {'steps': adam_steps, 'lr': 0.5, 'seconds': adam_s,
+                     'misfit_start': hist[0], 'misfit_end': hist[-1],
+                     'max_abs_err_start_cm': float(err0.max()),
+                     'max_abs_err_end_cm': float(err1.max()),
+                     'site_energy_err_end_cm': float(err1[:7].max()),
+                     'coupling_err_end_cm': float(err1[7:-1].max()),
+                     'lambda_end': float(theta_fit[-1])}}
+
+
 def ncu_traffic(path=os.path.join(ROOT, 'profiles', 'rk4_block_f32_fmo7.md')):
     try:
         txt = open(path).read()
@@ -308,6 +453,10 @@ def our_arm(args):
     err_pop = float((P32 - P64).abs().max() / P64.abs().max())
 
     heom = heom_ring8(torch, qg, _native) if rank == 0 and not args.no_heom else None
+    third = (third_order_chain24(torch, qg, samples=args.third_samples)
+             if rank == 0 and not args.no_third else None)
+    adj = (adjoint_fmo7(torch, qg, samples=args.adjoint_samples)
+           if rank == 0 and not args.no_adjoint else None)
     if rank != 0:
         return 0
     peak = fma_peak_tflops(torch, _native)
@@ -344,6 +493,11 @@ def our_arm(args):
         'gpu_launches': 12 * args.steps,
         'clocks': clocks,
     }
+    if adj is not None:
+        line['adjoint'] = adj
+        line['adjoint_over_forward'] = adj['adjoint_over_forward']
+    if third is not None:
+        line['third_order_chain24'] = third
     if heom is not None:
         line['heom_ring8'] = heom
     if base is not None:
@@ -359,10 +513,18 @@ def main():
     if args.impl == 'reference':
         return reference_arm(args)
     if args.only_heom:
+        args.only = 'heom'
+    if args.only:
         import torch
         import qspectra_gb300 as qg
         from qspectra_gb300 import _native
-        print(json.dumps(heom_ring8(torch, qg, _native, samples=args.heom_samples)), flush=True)
+        if args.only == 'heom':
+            out = heom_ring8(torch, qg, _native, samples=args.heom_samples)
+        elif args.only == 'third':
+            out = third_order_chain24(torch, qg, samples=args.third_samples)
+        else:
+            out = adjoint_fmo7(torch, qg, samples=args.adjoint_samples)
+        print(json.dumps(out), flush=True)
         return 0
     return our_arm(args)
 

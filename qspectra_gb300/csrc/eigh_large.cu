@@ -33,7 +33,7 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return t;
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(1024)
     eigh_tql_kernel(const double* __restrict__ A, int n, double* W, double* Zw,
                     double* __restrict__ E, double* __restrict__ U, int* status) {
   extern __shared__ __align__(16) double sm[];
@@ -156,16 +156,21 @@ __global__ void __launch_bounds__(256)
           bool split = false;
           for (int i = m - 1; i >= l; --i) {
             const double f = s * e[i], bb = c * e[i];
-            r = hypot(f, g);
-            e[i + 1] = r;
-            if (r == 0.0) {
+            // Givens rotation from one reciprocal square root (entries are
+            // far from the FP64 overflow range, so no hypot scaling)
+            const double rr = fma(f, f, g * g);
+            if (rr == 0.0) {
+              e[i + 1] = 0.0;
               d[i + 1] -= p;
               e[m] = 0.0;
               split = true;
               break;
             }
-            s = f / r;
-            c = g / r;
+            const double rinv = rsqrt(rr);
+            r = rr * rinv;
+            e[i + 1] = r;
+            s = f * rinv;
+            c = g * rinv;
             g = d[i + 1] - p;
             r = (d[i] - g) * s + 2.0 * c * bb;
             p = s * r;
@@ -191,12 +196,21 @@ __global__ void __launch_bounds__(256)
       // rotations on columns (i, i+1), i = m-1, m-2, ...: carry column i+1
       for (int r = tid; r < n; r += bd) {
         double x = Q[(int64_t)m * n + r];
-        for (int j = 0; j < nrot; ++j) {
-          const int i = m - 1 - j;
-          const double c = rc[j], s = rs[j];
-          const double zi = Q[(int64_t)i * n + r];
-          Q[(int64_t)(i + 1) * n + r] = s * zi + c * x;
-          x = c * zi - s * x;
+        constexpr int PF = 8;  // columns fetched ahead of the carried rotation chain
+        for (int j0 = 0; j0 < nrot; j0 += PF) {
+          double z[PF];
+#pragma unroll
+          for (int t = 0; t < PF; ++t)
+            z[t] = j0 + t < nrot ? Q[(int64_t)(m - 1 - j0 - t) * n + r] : 0.0;
+#pragma unroll
+          for (int t = 0; t < PF; ++t) {
+            if (j0 + t < nrot) {
+              const int i = m - 1 - j0 - t;
+              const double c = rc[j0 + t], s = rs[j0 + t];
+              Q[(int64_t)(i + 1) * n + r] = s * z[t] + c * x;
+              x = c * z[t] - s * x;
+            }
+          }
         }
         if (nrot > 0) Q[(int64_t)(m - nrot) * n + r] = x;
       }
@@ -246,8 +260,9 @@ extern "C" int qsx_eigh_large_batched(const double* H, int n, int64_t batch, dou
   if (e != cudaSuccess) return cuda_status(e, "qsx_eigh_large_batched");
   double* W = (double*)workspace;
   double* Z = W + (size_t)n * n * batch;
-  eigh_tql_kernel<<<(unsigned)batch, 256, smem, (cudaStream_t)stream>>>(H, n, W, Z, E, U,
-                                                                        status);
+  const int threads = n >= 1024 ? 1024 : ((n + 31) / 32) * 32;
+  eigh_tql_kernel<<<(unsigned)batch, threads, smem, (cudaStream_t)stream>>>(H, n, W, Z, E, U,
+                                                                            status);
   QSX_LAUNCH_CHECK("qsx_eigh_large_batched");
   return QSX_OK;
 }

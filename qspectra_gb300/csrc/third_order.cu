@@ -161,17 +161,28 @@ __global__ void __launch_bounds__(512)
   __syncthreads();
   const int row = threadIdx.x;
   if (row >= P) return;
-  const C* qcol = (const C*)p.Q + (s * P * N + b) * (int64_t)P + row;
+  const C* __restrict__ qcol = (const C*)p.Q + (s * P * N + b) * (int64_t)P + row;
   const int64_t qstride = (int64_t)N * P;
   const C* xb = sX + (size_t)b * P;
-  C k0 = cmk((T)0, (T)0), k1 = k0;
+  C k0 = cmk((T)0, (T)0), k1 = k0, k2 = k0, k3 = k0;
   int q = 0;
-#pragma unroll 4
-  for (; q + 1 < P; q += 2) {
-    cfma(k0, qcol[(int64_t)q * qstride], xb[q]);
-    cfma(k1, qcol[(int64_t)(q + 1) * qstride], xb[q + 1]);
+  // eight independent streaming loads in flight per thread
+  for (; q + 7 < P; q += 8) {
+    C a[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) a[t] = __ldg(qcol + (int64_t)(q + t) * qstride);
+    cfma(k0, a[0], xb[q]);
+    cfma(k1, a[1], xb[q + 1]);
+    cfma(k2, a[2], xb[q + 2]);
+    cfma(k3, a[3], xb[q + 3]);
+    cfma(k0, a[4], xb[q + 4]);
+    cfma(k1, a[5], xb[q + 5]);
+    cfma(k2, a[6], xb[q + 6]);
+    cfma(k3, a[7], xb[q + 7]);
   }
-  if (q < P) cfma(k0, qcol[(int64_t)q * qstride], xb[q]);
+  for (; q < P; ++q) cfma(k0, __ldg(qcol + (int64_t)q * qstride), xb[q]);
+  k0 = cmk(k0.x + k2.x, k0.y + k2.y);
+  k1 = cmk(k1.x + k3.x, k1.y + k3.y);
   const int kk = p.pair_sites[2 * row], ll = p.pair_sites[2 * row + 1];
   for (int c = 0; c < N; ++c) {
     const C ra = sR[kk * N + c], rb = sR[ll * N + c];

@@ -141,7 +141,7 @@ class Dft(torch.autograd.Function):
         (f,) = ctx.saved_tensors
         nt, dt, rw, uc = ctx.args
         f = f.numpy()
-        df = f[1] - f[0]
+        df = (f[-1] - f[0]) / (len(f) - 1)
         t = torch.arange(nt, dtype=torch.float64) * dt
         gx = _native.dft(g.contiguous(), f[0] - rw, df, t, 0.0, uc, -1) * (dt / df)
         return gx, None, None, None, None
@@ -151,7 +151,7 @@ class Dft(torch.autograd.Function):
 class AbsorptionFit:
     """Misfit of a disorder-averaged absorption spectrum on a frequency grid.
 
-    Parameters theta (float64, 2N + N(N-1)/2 - N + 1 entries): N site
+    Parameters theta (float64, N + N(N-1)/2 + 1 entries): N site
     energies, N(N-1)/2 couplings (upper triangle, row major) and lambda.
     ``offsets`` (S, N) are the disorder samples' site-energy shifts.
     """
@@ -163,8 +163,11 @@ class AbsorptionFit:
         self.offsets = torch.as_tensor(np.asarray(offsets, float)).cuda()
         self.freqs = np.asarray(freqs, float)
         df = np.diff(self.freqs)
-        if not np.allclose(df, df[0], rtol=1e-12, atol=0):
+        if len(self.freqs) < 2 or not np.allclose(df, df[0], rtol=1e-9, atol=0):
             raise ValueError('the frequency grid must be uniform')
+        # exactly f_0 + k df, the grid the transposed transform assumes
+        f = self.freqs
+        self.freqs = f[0] + np.arange(len(f)) * ((f[-1] - f[0]) / (len(f) - 1))
         self.T = CM_K * temperature_K
         self.gamma = cutoff_freq
         self.rw = rw_freq
@@ -232,3 +235,16 @@ class AbsorptionFit:
         """Relative L2 misfit |S(theta) - target|^2 / |target|^2."""
         s = self.spectrum(theta, impl)
         return ((s - target) ** 2).sum() / (target ** 2).sum()
+
+    def fit(self, theta0, target, steps=200, lr=1.0, impl='adjoint'):
+        """Adam on the misfit from theta0; returns (theta, misfit history)."""
+        theta = theta0.clone().requires_grad_(True)
+        opt = torch.optim.Adam([theta], lr=lr)
+        hist = []
+        for _ in range(steps):
+            opt.zero_grad()
+            loss = self.misfit(theta, target, impl)
+            loss.backward()
+            opt.step()
+            hist.append(float(loss.detach()))
+        return theta.detach(), hist
