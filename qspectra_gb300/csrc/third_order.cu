@@ -125,7 +125,9 @@ __global__ void fe_generator_kernel(const T* __restrict__ M, const double* __res
 // transpose, the Heisenberg-picture generator, is
 //   (L^T X)[:, b] = Q_b^T X[:, b] + sum_c X[:, c] R_p[c][b]  (row p),
 // so column b reads Q_b[q][r] along r: coalesced in the layout Q[s][q][b][r].
-// One CTA per (column b, sample), one thread per row.
+// One CTA per (column b, sample), one thread per row; Q is streamed once per
+// stage (the kernel's HBM traffic), X column b and the row operators sit in
+// shared memory.
 struct FeP {
   int P, N;
   const void* Q;          // [batch][P][N][P] complex (T)
@@ -135,8 +137,10 @@ struct FeP {
   double h;
 };
 
+constexpr int FE_THREADS = 320;
+
 template <typename T>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(FE_THREADS, sizeof(T) == 4 ? 4 : 2)
     fe_stage_kernel(FeP p, int stage, const typename cplx<T>::type* in,
                     typename cplx<T>::type* yh, typename cplx<T>::type* yl,
                     typename cplx<T>::type* acc, typename cplx<T>::type* next) {
@@ -145,11 +149,13 @@ __global__ void __launch_bounds__(512)
   const int P = p.P, N = p.N;
   const int b = blockIdx.x;
   const int64_t s = blockIdx.y;
-  C* sX = (C*)smraw;              // [N][P]: the whole sample state
-  C* sR = sX + (size_t)N * P;     // [N][N]: conj(Me[i][c][b] - Ae[c][b] / 2)
+  // shared: column b of X (the column term) and the row operators for
+  // column b; each thread reads its own row of X from global memory
+  C* sxb = (C*)smraw;          // [P]
+  C* sR = sxb + P;             // [N][N]: conj(Me[i][c][b] - Ae[c][b] / 2)
   const int64_t per = (int64_t)P * N;
   const C* x = in + s * per;
-  for (int64_t i = threadIdx.x; i < per; i += blockDim.x) sX[i] = x[i];
+  for (int i = threadIdx.x; i < P; i += blockDim.x) sxb[i] = x[(int64_t)b * P + i];
   const C* me = (const C*)p.Me + s * (int64_t)N * N * N;
   const C* ae = (const C*)p.Ae + s * (int64_t)N * N;
   for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
@@ -159,36 +165,49 @@ __global__ void __launch_bounds__(512)
     sR[i] = cmk(m.x - (T)0.5 * a.x, -(m.y - (T)0.5 * a.y));
   }
   __syncthreads();
-  const int row = threadIdx.x;
-  if (row >= P) return;
+  for (int row = threadIdx.x; row < P; row += blockDim.x) {
   const C* __restrict__ qcol = (const C*)p.Q + (s * P * N + b) * (int64_t)P + row;
   const int64_t qstride = (int64_t)N * P;
-  const C* xb = sX + (size_t)b * P;
   C k0 = cmk((T)0, (T)0), k1 = k0, k2 = k0, k3 = k0;
+  // column term sum_q Q_b[q][row] X[q][b], software-pipelined: the next
+  // U rows of Q are in flight while the current U are consumed
+  constexpr int U = 4;
+  C a[U], nx[U];
   int q = 0;
-  // eight independent streaming loads in flight per thread
-  for (; q + 7 < P; q += 8) {
-    C a[8];
+  if (P >= U) {
 #pragma unroll
-    for (int t = 0; t < 8; ++t) a[t] = __ldg(qcol + (int64_t)(q + t) * qstride);
-    cfma(k0, a[0], xb[q]);
-    cfma(k1, a[1], xb[q + 1]);
-    cfma(k2, a[2], xb[q + 2]);
-    cfma(k3, a[3], xb[q + 3]);
-    cfma(k0, a[4], xb[q + 4]);
-    cfma(k1, a[5], xb[q + 5]);
-    cfma(k2, a[6], xb[q + 6]);
-    cfma(k3, a[7], xb[q + 7]);
+    for (int t = 0; t < U; ++t) a[t] = __ldg(qcol + (int64_t)t * qstride);
+    for (; q + 2 * U <= P; q += U) {
+#pragma unroll
+      for (int t = 0; t < U; ++t) nx[t] = __ldg(qcol + (int64_t)(q + U + t) * qstride);
+#pragma unroll
+      for (int t = 0; t < U; t += 4) {
+        cfma(k0, a[t], sxb[q + t]);
+        cfma(k1, a[t + 1], sxb[q + t + 1]);
+        cfma(k2, a[t + 2], sxb[q + t + 2]);
+        cfma(k3, a[t + 3], sxb[q + t + 3]);
+      }
+#pragma unroll
+      for (int t = 0; t < U; ++t) a[t] = nx[t];
+    }
+#pragma unroll
+    for (int t = 0; t < U; t += 4) {
+      cfma(k0, a[t], sxb[q + t]);
+      cfma(k1, a[t + 1], sxb[q + t + 1]);
+      cfma(k2, a[t + 2], sxb[q + t + 2]);
+      cfma(k3, a[t + 3], sxb[q + t + 3]);
+    }
+    q += U;
   }
-  for (; q < P; ++q) cfma(k0, __ldg(qcol + (int64_t)q * qstride), xb[q]);
-  k0 = cmk(k0.x + k2.x, k0.y + k2.y);
-  k1 = cmk(k1.x + k3.x, k1.y + k3.y);
+  for (; q < P; ++q) cfma(k0, __ldg(qcol + (int64_t)q * qstride), sxb[q]);
+  // row term sum_c X[row][c] (T_k + T_l)[c]
   const int kk = p.pair_sites[2 * row], ll = p.pair_sites[2 * row + 1];
+  const C* xr = x + row;
   for (int c = 0; c < N; ++c) {
     const C ra = sR[kk * N + c], rb = sR[ll * N + c];
-    cfma(k1, sX[(size_t)c * P + row], cmk(ra.x + rb.x, ra.y + rb.y));
+    cfma(k1, xr[(int64_t)c * P], cmk(ra.x + rb.x, ra.y + rb.y));
   }
-  const C k = cmk(k0.x + k1.x, k0.y + k1.y);
+  const C k = cmk(k0.x + k1.x + k2.x + k3.x, k0.y + k1.y + k2.y + k3.y);
   const int64_t idx = s * per + (int64_t)b * P + row;
   const T h = (T)p.h;
   if (stage == 0) {
@@ -196,15 +215,15 @@ __global__ void __launch_bounds__(512)
     const C y = yh[idx];
     next[idx] = cmk(y.x + (T)0.5 * h * k.x, y.y + (T)0.5 * h * k.y);
   } else if (stage < 3) {
-    const C a = acc[idx];
-    acc[idx] = cmk(a.x + (T)2 * k.x, a.y + (T)2 * k.y);
+    const C a0 = acc[idx];
+    acc[idx] = cmk(a0.x + (T)2 * k.x, a0.y + (T)2 * k.y);
     const C y = yh[idx];
     const T cst = stage == 1 ? (T)0.5 * h : h;
     next[idx] = cmk(y.x + cst * k.x, y.y + cst * k.y);
   } else {
-    const C a = acc[idx];
+    const C a0 = acc[idx];
     const T s6 = h / (T)6;
-    const T ix = s6 * (a.x + k.x), iy = s6 * (a.y + k.y);
+    const T ix = s6 * (a0.x + k.x), iy = s6 * (a0.y + k.y);
     const C y = yh[idx];
     if (yl) {
       // split-word state: hi + lo with a TwoSum update
@@ -217,6 +236,7 @@ __global__ void __launch_bounds__(512)
     } else {
       yh[idx] = cmk(y.x + ix, y.y + iy);
     }
+  }
   }
 }
 
@@ -343,8 +363,8 @@ extern "C" int qsx_fe_heisenberg_rk4(const void* Q, const void* Ae, const void* 
                                      int precision, const double* y0, int64_t y0_stride,
                                      int nsteps, double h, double* out, void* workspace,
                                      size_t workspace_bytes, int32_t* status, void* stream) {
-  QSX_CHECK_ARG(N >= 2 && N <= 64 && P == N * (N - 1) / 2 && P <= 512,
-                "qsx_fe_heisenberg_rk4: P=%d, N=%d (P must be N(N-1)/2 <= 512)", P, N);
+  QSX_CHECK_ARG(N >= 2 && N <= 64 && P == N * (N - 1) / 2,
+                "qsx_fe_heisenberg_rk4: P=%d must be N(N-1)/2 for N=%d sites", P, N);
   QSX_CHECK_ARG(batch >= 0 && batch <= 65535 && nsteps >= 0,
                 "qsx_fe_heisenberg_rk4: batch or step count out of range");
   QSX_CHECK_ARG(precision == QSX_FP32 || precision == QSX_FP64,
@@ -368,7 +388,7 @@ extern "C" int qsx_fe_heisenberg_rk4(const void* Q, const void* Ae, const void* 
   const int64_t per = (int64_t)P * N;
   const int64_t n = per * batch;
   const dim3 grid((unsigned)N, (unsigned)batch);
-  const int threads = ((P + 31) / 32) * 32;
+  const int threads = P >= FE_THREADS ? FE_THREADS : ((P + 31) / 32) * 32;
   const unsigned eg = (unsigned)((n + 255) / 256);
   auto run = [&](auto tag) -> int {
     using T = decltype(tag);
@@ -378,9 +398,9 @@ extern "C" int qsx_fe_heisenberg_rk4(const void* Q, const void* Ae, const void* 
     C* acc = yh + (sizeof(T) == 4 ? 2 : 1) * n;
     C* s0 = acc + n;
     C* s1 = s0 + n;
-    const size_t smem = ((size_t)N * P + (size_t)N * N) * sizeof(C);
+    const size_t smem = ((size_t)P + (size_t)N * N) * sizeof(C);
     QSX_CHECK_ARG(smem <= 227 * 1024,
-                  "qsx_fe_heisenberg_rk4: state of %zu bytes exceeds shared memory", smem);
+                  "qsx_fe_heisenberg_rk4: %zu bytes of column state exceed shared memory", smem);
     cudaError_t e = cudaFuncSetAttribute(fe_stage_kernel<T>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "qsx_fe_heisenberg_rk4");

@@ -226,15 +226,19 @@ class ThirdOrderEngine:
         _tick(events, 't2')
         # ---- t2 propagator powers on the 'ee' block
         gaps = [int(k) for k in self.gaps]
-        Pk = None
-        if W is not None:
+        # P^g - I for g = gcd of the gaps; each gap then applies it gap/g
+        # times to the (S, T1, N^2) block of t1 states (a matrix-block product
+        # costs T1/N^2 of a matrix-matrix product)
+        base = int(np.gcd.reduce([k for k in gaps if k] or [1]))
+        Xg = None
+        if W is not None and any(gaps):
             Lee = build.block(self._idx('ee'))
             A = (dt * Lee).to(cdt)
             del Lee
             A2 = A @ A
             D = A + 0.5 * A2 + A2 @ (A / 6 + A2 / 24)
             del A, A2
-            Pk = powers_minus_identity(D, gaps)
+            Xg = powers_minus_identity(D, [base])[base].transpose(1, 2).contiguous()
             del D
         Dgg = build.propagator(self._idx('gg'), dt, prec)[:, 0, 0] if g3 is not None else None
         _tick(events, 't1')
@@ -252,8 +256,8 @@ class ThirdOrderEngine:
                 r = self._csr(sub1 + '->ee', pol[1], geo[1])(rho1).to(cdt)  # (S, T1, N^2)
                 Wt = W.to(cdt).transpose(1, 2)                           # (S, N^2, T3)
                 for j, k in enumerate(gaps):
-                    if k:
-                        r = r + r @ Pk[k].transpose(1, 2)
+                    for _ in range(k // base):
+                        r = r + torch.bmm(r, Xg)
                     total[:, j, :] += torch.bmm(r, Wt).to(torch.complex128).sum(0)
             if g3 is not None:
                 rgg = self._csr(sub1 + '->gg', pol[1], geo[1])(rho1)[..., 0]  # (S, T1)
