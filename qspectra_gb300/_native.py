@@ -47,6 +47,7 @@ class Rk4Args(ctypes.Structure):
         ('mean_scale', ctypes.c_double),
         ('workspace', _c_vp), ('workspace_bytes', ctypes.c_size_t),
         ('status', _c_vp),
+        ('variant', ctypes.c_int32), ('reserved', ctypes.c_int32),
     ]
 
 
@@ -304,7 +305,7 @@ def rk4_block_matrix(D, K, select):
 
 def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
         state=False, proj=None, select=None, per_sample=True, mean=False,
-        check_finite=True, workspace=None, block_k=0):
+        check_finite=True, workspace=None, block_k=0, variant=0):
     """Batched RK4 time loop (see qsx_rk4_args in include/qsx.h).
 
     matrix: (B, m, m) complex64 (FP32) / complex128 (FP64), or (m, m) shared.
@@ -338,6 +339,7 @@ def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
     a.matrix = matrix.data_ptr()
     a.matrix_stride = rows * m if matrix.dim() == 3 else 0
     a.block_k = block_k
+    a.variant = int(variant)
     a.h = h
     a.y0 = y0.data_ptr()
     a.y0_stride = m if y0.dim() == 2 else 0

@@ -3,18 +3,21 @@
 // The reference diagonalises each sample's Hamiltonian with scipy.linalg.eigh
 // (qspectra/hamiltonian.py:310-328).
 //
-// One CTA per matrix, three phases over a global-memory workspace:
+// One CTA per matrix, four phases over a global-memory workspace:
 //   1. Householder reduction to tridiagonal form, A = Q T Q^T: for each
 //      column k, v with (I - tau v v^T) x = alpha e_1 and the two-sided
 //      update B <- B - v w^T - w v^T, w = p - (tau/2)(v^T p) v, p = tau B v.
-//   2. Q = H_0 H_1 ... H_{n-3} accumulated backwards from the identity.
-//   3. Implicit QL iterations with Wilkinson-type shifts on T; thread 0 runs
-//      each sweep's scalar recurrence and records its Givens rotations, then
-//      every thread applies them to its row of Q (Q stored column-major so a
-//      rotation touches consecutive addresses across threads).
-// Eigenvalues are returned ascending with U[:, k] the k-th eigenvector.
-// Every loop is bounded: a QL that does not converge in 60 sweeps per
-// eigenvalue stops and reports QSX_ERR_NONFINITE in *status.
+//   2. Eigenvalues of T by implicit QL with Wilkinson-type shifts, without
+//      vectors (one thread; O(n^2)).
+//   3. Eigenvectors of T by inverse iteration: LU with partial pivoting of
+//      T - lambda I, three solves from a vector of ones; eigenvalues closer
+//      than 1e-3 |T| form a cluster handled by one thread with modified
+//      Gram-Schmidt against the cluster's earlier vectors.
+//   4. Back-transform by the Householder reflectors, U = H_0 ... H_{n-3} Z.
+// This keeps the FP64 work near 2 n^3 multiply-adds per matrix (no Givens
+// rotations accumulated into Q).  Eigenvalues are returned ascending with
+// U[:, k] the k-th eigenvector.  Every loop is bounded: a QL that does not
+// converge in 60 sweeps per eigenvalue stops and reports QSX_ERR_NONFINITE.
 #include <cfloat>
 
 #include "qsx_common.cuh"
@@ -33,8 +36,48 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return t;
 }
 
-__global__ void __launch_bounds__(1024)
-    eigh_tql_kernel(const double* __restrict__ A, int n, double* W, double* Zw,
+// sum_j x[j * ld] v[j]: four independent chains, eight loads in flight
+__device__ __forceinline__ double col_dot(const double* __restrict__ x, int ld,
+                                          const double* __restrict__ v, int m) {
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int j = 0;
+  for (; j + 7 < m; j += 8) {
+    double t[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t[q] = x[(int64_t)(j + q) * ld];
+    a0 = fma(t[0], v[j], a0);
+    a1 = fma(t[1], v[j + 1], a1);
+    a2 = fma(t[2], v[j + 2], a2);
+    a3 = fma(t[3], v[j + 3], a3);
+    a0 = fma(t[4], v[j + 4], a0);
+    a1 = fma(t[5], v[j + 5], a1);
+    a2 = fma(t[6], v[j + 6], a2);
+    a3 = fma(t[7], v[j + 7], a3);
+  }
+  for (; j < m; ++j) a0 = fma(x[(int64_t)j * ld], v[j], a0);
+  return (a0 + a1) + (a2 + a3);
+}
+
+// x[i * ld] -= a[i] * bc + b[i] * ac for i < m, eight rows loaded before
+// any is stored (the shared vectors a, b cannot alias x)
+__device__ __forceinline__ void col_rank2(double* __restrict__ x, int ld,
+                                          const double* __restrict__ a,
+                                          const double* __restrict__ b, double bc, double ac,
+                                          int m) {
+  int i = 0;
+  for (; i + 7 < m; i += 8) {
+    double t[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t[q] = x[(int64_t)(i + q) * ld];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      x[(int64_t)(i + q) * ld] = fma(-a[i + q], bc, fma(-b[i + q], ac, t[q]));
+  }
+  for (; i < m; ++i) x[(int64_t)i * ld] = fma(-a[i], bc, fma(-b[i], ac, x[(int64_t)i * ld]));
+}
+
+__global__ void __launch_bounds__(512)
+    eigh_tql_kernel(const double* __restrict__ A, int n, double* W, double* Zw, double* Sw,
                     double* __restrict__ E, double* __restrict__ U, int* status) {
   extern __shared__ __align__(16) double sm[];
   double* d = sm;          // [n] diagonal
@@ -82,21 +125,14 @@ __global__ void __launch_bounds__(1024)
       // p = tau B v (B symmetric: column r read across threads)
       double vp = 0.0;
       for (int r = tid; r < m; r += bd) {
-        double acc = 0.0;
-        for (int j = 0; j < m; ++j) acc = fma(B[(int64_t)j * n + r], v[j], acc);
-        w[r] = tau * acc;
-        vp += v[r] * w[r];
+        const double wr = tau * col_dot(B + r, n, v, m);
+        w[r] = wr;
+        vp += v[r] * wr;
       }
       const double K = 0.5 * tau * block_sum(vp, red);
       for (int r = tid; r < m; r += bd) w[r] -= K * v[r];
       __syncthreads();
-      for (int c = tid; c < m; c += bd) {
-        const double vc = v[c], wc = w[c];
-        for (int i = 0; i < m; ++i) {
-          double* x = B + (int64_t)i * n + c;
-          *x = fma(-v[i], wc, fma(-w[i], vc, *x));
-        }
-      }
+      for (int c = tid; c < m; c += bd) col_rank2(B + c, n, v, w, v[c], w[c], m);
     } else {
       if (tid == 0) e[k] = x0;
     }
@@ -114,124 +150,183 @@ __global__ void __launch_bounds__(1024)
     d[n - 1] = Wm[(int64_t)(n - 1) * n + n - 1];
     e[n - 1] = 0.0;
   }
-  // ---- 2. Q = H_0 ... H_{n-3}, row-major in Z
-  for (int64_t i = tid; i < nn; i += bd) Z[i] = (i / n == i % n) ? 1.0 : 0.0;
+  // ---- 2. eigenvalues: implicit QL on (d, e) without vectors, one thread
+  double* dv = rs;  // QL works on copies; d and e stay for inverse iteration
+  double* ev = rc;
+  for (int i = tid; i < n; i += bd) {
+    dv[i] = d[i];
+    ev[i] = e[i];
+  }
   __syncthreads();
+  if (tid == 0) {
+    int bad = 0;
+    for (int l = 0; l < n; ++l) {
+      for (int iter = 0;; ++iter) {
+        int m = l;
+        for (; m < n - 1; ++m) {
+          const double dd = fabs(dv[m]) + fabs(dv[m + 1]);
+          if (fabs(ev[m]) <= DBL_EPSILON * dd) break;
+        }
+        if (m == l) break;
+        if (iter >= 60) {
+          bad = 1;
+          break;
+        }
+        double g = (dv[l + 1] - dv[l]) / (2.0 * ev[l]);
+        double r = hypot(g, 1.0);
+        g = dv[m] - dv[l] + ev[l] / (g + copysign(r, g));
+        double s = 1.0, c = 1.0, p = 0.0;
+        bool split = false;
+        for (int i = m - 1; i >= l; --i) {
+          const double f = s * ev[i], bb = c * ev[i];
+          const double rr = fma(f, f, g * g);
+          if (rr == 0.0) {
+            dv[i + 1] -= p;
+            ev[m] = 0.0;
+            split = true;
+            break;
+          }
+          const double rinv = rsqrt(rr);
+          r = rr * rinv;
+          ev[i + 1] = r;
+          s = f * rinv;
+          c = g * rinv;
+          g = dv[i + 1] - p;
+          r = (dv[i] - g) * s + 2.0 * c * bb;
+          p = s * r;
+          dv[i + 1] = g + p;
+          g = c * r - bb;
+        }
+        if (!split) {
+          dv[l] -= p;
+          ev[l] = g;
+          ev[m] = 0.0;
+        }
+      }
+    }
+    ctl[2] = bad;
+  }
+  __syncthreads();
+  // ascending order (ties by index)
+  for (int i = tid; i < n; i += bd) {
+    int rk = 0;
+    const double di = dv[i];
+    for (int j = 0; j < n; ++j) rk += (dv[j] < di) || (dv[j] == di && j < i);
+    rank[i] = rk;
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += bd) w[rank[i]] = dv[i];  // sorted eigenvalues
+  __syncthreads();
+  // ---- 3. eigenvectors of T by inverse iteration, row-major in Z (column j
+  // = eigenvector of the j-th smallest eigenvalue).  Eigenvalues closer than
+  // 1e-3 |T| form a cluster, handled by one thread in order with modified
+  // Gram-Schmidt against the cluster's earlier vectors.
+  double tnorm = 0.0;
+  for (int i = 0; i < n; ++i)
+    tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : 0.0));
+  const double ortol = 1e-3 * tnorm;
+  const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
+  for (int j = tid; j < n; j += bd) {
+    if (j > 0 && w[j] - w[j - 1] < ortol) continue;  // not the first of its cluster
+    int jend = j + 1;
+    while (jend < n && w[jend] - w[jend - 1] < ortol) ++jend;
+    double* sc = Sw + ((int64_t)b * n + j) * 5 * (int64_t)n;  // this thread's scratch
+    double* u1 = sc;
+    double* u2 = sc + n;
+    double* u3 = sc + 2 * n;
+    double* lm = sc + 3 * n;
+    double* x = sc + 4 * n;
+    for (int jj = j; jj < jend; ++jj) {
+      // eigenvalues of a cluster are separated by a small multiple of the
+      // tolerance so that each factorisation differs
+      const double lam = w[jj] + (jj - j) * 10.0 * tiny;
+      // LU with partial pivoting of T - lam I: u1, u2, u3 the three diagonals
+      // of U, lm the multipliers (|l| <= 1; l + 4 where rows i, i+1 swapped)
+      double pp = d[0] - lam, qq = n > 1 ? e[0] : 0.0;
+      for (int i = 0; i < n - 1; ++i) {
+        const double sub = e[i];
+        const double an = d[i + 1] - lam, en = (i + 1 < n - 1) ? e[i + 1] : 0.0;
+        if (fabs(pp) >= fabs(sub)) {
+          if (pp == 0.0) pp = tiny;
+          const double l = sub / pp;
+          u1[i] = pp;
+          u2[i] = qq;
+          u3[i] = 0.0;
+          lm[i] = l;
+          pp = an - l * qq;
+          qq = en;
+        } else {
+          const double l = pp / sub;
+          u1[i] = sub;
+          u2[i] = an;
+          u3[i] = en;
+          lm[i] = l + 4.0;  // rows swapped: multipliers lie in [-1, 1], so l + 4 flags it
+          const double np = qq - l * an;
+          qq = -l * en;
+          pp = np;
+        }
+      }
+      u1[n - 1] = pp == 0.0 ? tiny : pp;
+      // start vector: all ones (the first solve uses U only)
+      for (int i = 0; i < n; ++i) x[i] = 1.0;
+      for (int it = 0; it < 3; ++it) {
+        if (it > 0) {
+          // apply the row interchanges and multipliers (L^{-1} P)
+          for (int i = 0; i < n - 1; ++i) {
+            const double t = lm[i];
+            if (t > 2.0) {
+              const double l = t - 4.0;
+              const double xi = x[i];
+              x[i] = x[i + 1];
+              x[i + 1] = xi - l * x[i];
+            } else {
+              x[i + 1] -= t * x[i];
+            }
+          }
+        }
+        // U x = x
+        for (int i = n - 1; i >= 0; --i) {
+          double v = x[i];
+          if (i + 1 < n) v -= u2[i] * x[i + 1];
+          if (i + 2 < n) v -= u3[i] * x[i + 2];
+          double piv = u1[i];
+          if (fabs(piv) < tiny) piv = copysign(tiny, piv);
+          x[i] = v / piv;
+        }
+        // orthogonalise against the cluster's earlier vectors, normalise
+        for (int k = j; k < jj; ++k) {
+          double dot = 0.0;
+          for (int i = 0; i < n; ++i) dot = fma(Z[(int64_t)i * n + k], x[i], dot);
+          for (int i = 0; i < n; ++i) x[i] -= dot * Z[(int64_t)i * n + k];
+        }
+        double nrm = 0.0;
+        for (int i = 0; i < n; ++i) nrm = fma(x[i], x[i], nrm);
+        const double inv = nrm > 0.0 ? rsqrt(nrm) : 0.0;
+        for (int i = 0; i < n; ++i) x[i] *= inv;
+      }
+      for (int i = 0; i < n; ++i) Z[(int64_t)i * n + jj] = x[i];
+    }
+  }
+  __syncthreads();
+  // ---- 4. back-transform U = H_0 H_1 ... H_{n-3} Z (reflector k acts on
+  // rows k+1 ..), applied from k = n-3 down to 0
   for (int k = n - 3; k >= 0; --k) {
     const double tau = Wm[(int64_t)k * n + k];
     if (tau == 0.0) continue;
     const int m = n - k - 1;
     for (int i = tid; i < m; i += bd) v[i] = Wm[(int64_t)k * n + k + 1 + i];
     __syncthreads();
-    double* Zb = Z + (int64_t)(k + 1) * n + k + 1;
-    for (int c = tid; c < m; c += bd) {
-      double u = 0.0;
-      for (int r = 0; r < m; ++r) u = fma(v[r], Zb[(int64_t)r * n + c], u);
-      u *= tau;
-      for (int r = 0; r < m; ++r) Zb[(int64_t)r * n + c] -= v[r] * u;
+    double* Zb = Z + (int64_t)(k + 1) * n;
+    for (int c = tid; c < n; c += bd) {
+      const double u = tau * col_dot(Zb + c, n, v, m);
+      col_rank2(Zb + c, n, v, v, u, 0.0, m);
     }
     __syncthreads();
   }
-  // column-major copy of Q into the (now free) reduction workspace
-  for (int64_t i = tid; i < nn; i += bd) Wm[(i % n) * n + i / n] = Z[i];
-  __syncthreads();
-  double* Q = Wm;  // Q[col * n + row]
-  // ---- 3. implicit QL
-  if (tid == 0) ctl[2] = 0;
-  for (int l = 0; l < n; ++l) {
-    for (int iter = 0;; ++iter) {
-      __syncthreads();  // every thread has read the previous round's ctl, rc, rs
-      if (tid == 0) {
-        int m = l;
-        for (; m < n - 1; ++m) {
-          const double dd = fabs(d[m]) + fabs(d[m + 1]);
-          if (fabs(e[m]) <= DBL_EPSILON * dd) break;
-        }
-        int nrot = 0;
-        if (m != l && iter < 60) {
-          double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-          double r = hypot(g, 1.0);
-          g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-          double s = 1.0, c = 1.0, p = 0.0;
-          bool split = false;
-          for (int i = m - 1; i >= l; --i) {
-            const double f = s * e[i], bb = c * e[i];
-            // Givens rotation from one reciprocal square root (entries are
-            // far from the FP64 overflow range, so no hypot scaling)
-            const double rr = fma(f, f, g * g);
-            if (rr == 0.0) {
-              e[i + 1] = 0.0;
-              d[i + 1] -= p;
-              e[m] = 0.0;
-              split = true;
-              break;
-            }
-            const double rinv = rsqrt(rr);
-            r = rr * rinv;
-            e[i + 1] = r;
-            s = f * rinv;
-            c = g * rinv;
-            g = d[i + 1] - p;
-            r = (d[i] - g) * s + 2.0 * c * bb;
-            p = s * r;
-            d[i + 1] = g + p;
-            g = c * r - bb;
-            rc[nrot] = c;
-            rs[nrot] = s;
-            ++nrot;
-          }
-          if (!split) {
-            d[l] -= p;
-            e[l] = g;
-            e[m] = 0.0;
-          }
-        }
-        if (m != l && iter >= 60) ctl[2] = 1;
-        ctl[0] = m;
-        ctl[1] = (m == l || iter >= 60) ? -1 : nrot;
-      }
-      __syncthreads();
-      const int m = ctl[0], nrot = ctl[1];
-      if (nrot < 0) break;
-      // rotations on columns (i, i+1), i = m-1, m-2, ...: carry column i+1
-      for (int r = tid; r < n; r += bd) {
-        double x = Q[(int64_t)m * n + r];
-        constexpr int PF = 8;  // columns fetched ahead of the carried rotation chain
-        for (int j0 = 0; j0 < nrot; j0 += PF) {
-          double z[PF];
-#pragma unroll
-          for (int t = 0; t < PF; ++t)
-            z[t] = j0 + t < nrot ? Q[(int64_t)(m - 1 - j0 - t) * n + r] : 0.0;
-#pragma unroll
-          for (int t = 0; t < PF; ++t) {
-            if (j0 + t < nrot) {
-              const int i = m - 1 - j0 - t;
-              const double c = rc[j0 + t], s = rs[j0 + t];
-              Q[(int64_t)(i + 1) * n + r] = s * z[t] + c * x;
-              x = c * z[t] - s * x;
-            }
-          }
-        }
-        if (nrot > 0) Q[(int64_t)(m - nrot) * n + r] = x;
-      }
-    }
-  }
-  __syncthreads();
   if (tid == 0 && ctl[2] && status) atomicOr(status, QSX_ERR_NONFINITE);
-  // ---- ascending order: rank of each eigenvalue (ties by index)
-  for (int i = tid; i < n; i += bd) {
-    int rk = 0;
-    const double di = d[i];
-    for (int j = 0; j < n; ++j) rk += (d[j] < di) || (d[j] == di && j < i);
-    rank[i] = rk;
-  }
-  __syncthreads();
-  for (int i = tid; i < n; i += bd) E[b * n + rank[i]] = d[i];
+  for (int i = tid; i < n; i += bd) E[b * n + i] = w[i];
   double* u = U + b * nn;
-  for (int64_t idx = tid; idx < nn; idx += bd) {
-    const int col = (int)(idx / n), row = (int)(idx % n);
-    u[(int64_t)row * n + rank[col]] = Q[idx];
-  }
+  for (int64_t idx = tid; idx < nn; idx += bd) u[idx] = Z[idx];
 }
 
 }  // namespace qsx
@@ -240,7 +335,8 @@ using namespace qsx;
 
 extern "C" size_t qsx_eigh_large_workspace_bytes(int n, int64_t batch) {
   if (n < 1 || batch < 0) return 0;
-  return (size_t)2 * n * n * (size_t)batch * sizeof(double);
+  // reduction matrix, eigenvectors, and 5 n doubles of scratch per eigenvalue
+  return (size_t)7 * n * n * (size_t)batch * sizeof(double);
 }
 
 extern "C" int qsx_eigh_large_batched(const double* H, int n, int64_t batch, double* E,
@@ -260,9 +356,10 @@ extern "C" int qsx_eigh_large_batched(const double* H, int n, int64_t batch, dou
   if (e != cudaSuccess) return cuda_status(e, "qsx_eigh_large_batched");
   double* W = (double*)workspace;
   double* Z = W + (size_t)n * n * batch;
-  const int threads = n >= 1024 ? 1024 : ((n + 31) / 32) * 32;
-  eigh_tql_kernel<<<(unsigned)batch, threads, smem, (cudaStream_t)stream>>>(H, n, W, Z, E, U,
-                                                                            status);
+  double* Sw = Z + (size_t)n * n * batch;
+  const int threads = n >= 512 ? 512 : ((n + 31) / 32) * 32;
+  eigh_tql_kernel<<<(unsigned)batch, threads, smem, (cudaStream_t)stream>>>(H, n, W, Z, Sw, E,
+                                                                            U, status);
   QSX_LAUNCH_CHECK("qsx_eigh_large_batched");
   return QSX_OK;
 }

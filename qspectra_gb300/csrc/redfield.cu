@@ -393,39 +393,72 @@ __global__ void liouvillian_kernel(const double* __restrict__ H, int64_t H_strid
 // C = A * B for m x m complex tiles in shared memory.  Each thread owns a 4 x 4
 // block of C (8 shared loads per 16 complex MACs); `store(e, acc)` writes the
 // result element e = row * m + col.
+template <int TR, int TC, typename C, typename Store>
+__device__ __forceinline__ void cgemm_tiled(const C* __restrict__ A, const C* __restrict__ B,
+                                            int m, Store store) {
+  // Thread (r', c') owns rows r' + i nbr (i < TR) and columns c' + j nbc
+  // (j < TC): consecutive threads read consecutive B columns (conflict-free)
+  // and share A rows (broadcast).
+  using T = decltype(A[0].x);
+  const int nbr = (m + TR - 1) / TR, nbc = (m + TC - 1) / TC;
+  for (int blk = threadIdx.x; blk < nbr * nbc; blk += blockDim.x) {
+    const int r0 = blk / nbc, c0 = blk % nbc;
+    C acc[TR][TC];
+#pragma unroll
+    for (int i = 0; i < TR; ++i)
+#pragma unroll
+      for (int j = 0; j < TC; ++j) acc[i][j] = cmk((T)0, (T)0);
+    for (int k = 0; k < m; ++k) {
+      C a[TR], b[TC];
+#pragma unroll
+      for (int i = 0; i < TR; ++i)
+        a[i] = (r0 + i * nbr < m) ? A[(r0 + i * nbr) * m + k] : cmk((T)0, (T)0);
+#pragma unroll
+      for (int j = 0; j < TC; ++j)
+        b[j] = (c0 + j * nbc < m) ? B[k * m + c0 + j * nbc] : cmk((T)0, (T)0);
+#pragma unroll
+      for (int i = 0; i < TR; ++i)
+#pragma unroll
+        for (int j = 0; j < TC; ++j) cfma(acc[i][j], a[i], b[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < TR; ++i)
+#pragma unroll
+      for (int j = 0; j < TC; ++j)
+        if (r0 + i * nbr < m && c0 + j * nbc < m)
+          store((r0 + i * nbr) * m + c0 + j * nbc, acc[i][j]);
+  }
+}
+
+// C = A B for m x m complex tiles in shared memory, results handed to
+// store(index, value).  The register tile TR x TC is chosen per m to keep
+// every thread busy: estimated issue cost per k = passes * (4 TR TC FMA +
+// TR + TC loads), e.g. 5 x 2 tiles (250 threads) at m = 49, 4 x 4 at m = 64.
 template <typename C, typename Store>
 __device__ __forceinline__ void smem_cgemm(const C* __restrict__ A, const C* __restrict__ B,
                                            int m, Store store) {
-  // Thread (r', c') owns rows r' + i nb and columns c' + j nb (i, j < 4,
-  // nb = ceil(m / 4)): consecutive threads read consecutive B columns
-  // (conflict-free) and share A rows (broadcast).
-  using T = decltype(A[0].x);
-  const int nb = (m + 3) / 4;
-  for (int blk = threadIdx.x; blk < nb * nb; blk += blockDim.x) {
-    const int r0 = blk / nb, c0 = blk % nb;
-    C acc[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) acc[i][j] = cmk((T)0, (T)0);
-    for (int k = 0; k < m; ++k) {
-      C a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-        a[i] = (r0 + i * nb < m) ? A[(r0 + i * nb) * m + k] : cmk((T)0, (T)0);
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-        b[j] = (c0 + j * nb < m) ? B[k * m + c0 + j * nb] : cmk((T)0, (T)0);
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], b[j]);
+  constexpr int NC = 8;
+  const int tr[NC] = {1, 2, 2, 3, 4, 3, 4, 5};
+  const int tc[NC] = {1, 1, 2, 2, 2, 3, 4, 2};
+  int best = 0, bestc = 0x7fffffff;
+  const int nt = blockDim.x;
+  for (int i = 0; i < NC; ++i) {
+    const int tiles = ((m + tr[i] - 1) / tr[i]) * ((m + tc[i] - 1) / tc[i]);
+    const int cost = ((tiles + nt - 1) / nt) * (4 * tr[i] * tc[i] + tr[i] + tc[i]);
+    if (cost < bestc) {
+      bestc = cost;
+      best = i;
     }
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-        if (r0 + i * nb < m && c0 + j * nb < m) store((r0 + i * nb) * m + c0 + j * nb, acc[i][j]);
+  }
+  switch (best) {
+    case 0: cgemm_tiled<1, 1>(A, B, m, store); break;
+    case 1: cgemm_tiled<2, 1>(A, B, m, store); break;
+    case 2: cgemm_tiled<2, 2>(A, B, m, store); break;
+    case 3: cgemm_tiled<3, 2>(A, B, m, store); break;
+    case 4: cgemm_tiled<4, 2>(A, B, m, store); break;
+    case 5: cgemm_tiled<3, 3>(A, B, m, store); break;
+    case 6: cgemm_tiled<4, 4>(A, B, m, store); break;
+    default: cgemm_tiled<5, 2>(A, B, m, store); break;
   }
 }
 
@@ -550,20 +583,18 @@ __global__ void __launch_bounds__(256)
   using C = typename cplx<T>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int mm = m * m;
-  C* sD = (C*)smraw;  // D
-  C* sBase = sD + mm;
-  C* sRes = sBase + mm;
-  C* sTmp = sRes + mm;
-  C* sR = sTmp + mm;              // current selected rows R_k  [nsel][m]
+  C* bufs[3];
+  bufs[0] = (C*)smraw;             // D, then a rotating buffer
+  bufs[1] = bufs[0] + mm;
+  bufs[2] = bufs[1] + mm;
+  C* sR = bufs[2] + mm;            // current selected rows R_k  [nsel][m]
   C* sR2 = sR + nsel * m;          // next selected rows
+  const C* sD = bufs[0];
   const int64_t b = blockIdx.x;
   const int rows = m + nsel * (K - 1);
   const C* d = D + b * mm;
   C* o = out + b * (int64_t)rows * m;
-  for (int e = threadIdx.x; e < mm; e += blockDim.x) {
-    sD[e] = d[e];
-    sBase[e] = d[e];
-  }
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) bufs[0][e] = d[e];
   for (int e = threadIdx.x; e < nsel * m; e += blockDim.x) {
     const int q = e / m, c = e % m;
     int r = sel[q];
@@ -572,47 +603,64 @@ __global__ void __launch_bounds__(256)
     if (K > 1) o[(int64_t)(m + q) * m + c] = d[r * m + c];
   }
   __syncthreads();
-  // selected rows of D_2 .. D_{K-1}
+  // selected rows of D_2 .. D_{K-1}: R_{k+1} = R_k + R_1 + R_k D
   for (int k = 2; k < K; ++k) {
     for (int e = threadIdx.x; e < nsel * m; e += blockDim.x) {
       const int q = e / m, c = e % m;
       int r = sel[q];
       r = (r >= 0 && r < m) ? r : 0;
-      C acc = cadd2(sR[e], sD[r * m + c]);
-      for (int j = 0; j < m; ++j) cfma(acc, sR[q * m + j], sD[j * m + c]);
-      sR2[e] = acc;
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < nsel * m; e += blockDim.x) {
-      sR[e] = sR2[e];
-      o[(int64_t)(m + (k - 1) * nsel + e / m) * m + e % m] = sR2[e];
-    }
-    __syncthreads();
-  }
-  // D_K by binary powering
-  bool have = false;
-  for (int kk = K; kk > 0; kk >>= 1) {
-    if (kk & 1) {
-      if (!have) {
-        for (int e = threadIdx.x; e < mm; e += blockDim.x) sRes[e] = sBase[e];
-        have = true;
-      } else {
-        smem_cgemm(sRes, sBase, m, [&](int e, C v) { sTmp[e] = v; });
-        __syncthreads();
-        for (int e = threadIdx.x; e < mm; e += blockDim.x)
-          sRes[e] = cadd2(cadd2(sRes[e], sBase[e]), sTmp[e]);
+      const C* rq = sR + q * m;
+      C a0 = cadd2(sR[e], sD[r * m + c]), a1 = cmk((T)0, (T)0), a2 = a1, a3 = a1;
+      int j = 0;
+      for (; j + 3 < m; j += 4) {
+        cfma(a0, rq[j], sD[j * m + c]);
+        cfma(a1, rq[j + 1], sD[(j + 1) * m + c]);
+        cfma(a2, rq[j + 2], sD[(j + 2) * m + c]);
+        cfma(a3, rq[j + 3], sD[(j + 3) * m + c]);
       }
-      __syncthreads();
+      for (; j < m; ++j) cfma(a0, rq[j], sD[j * m + c]);
+      const C v = cadd2(cadd2(a0, a1), cadd2(a2, a3));
+      sR2[e] = v;
+      o[(int64_t)(m + (k - 1) * nsel + q) * m + c] = v;
+    }
+    __syncthreads();
+    C* t = sR;
+    sR = sR2;
+    sR2 = t;
+  }
+  // D_K = P^K - I by binary powering over three rotating shared buffers;
+  // each product folds (I + X)(I + Y) - I = X + Y + X Y into its store
+  int res = -1, base = 0;
+  for (int kk = K; kk > 0; kk >>= 1) {
+    const bool last = (kk >> 1) == 0;
+    if (kk & 1) {
+      if (res < 0) {
+        res = base;
+        if (last)
+          for (int e = threadIdx.x; e < mm; e += blockDim.x) o[e] = bufs[res][e];
+      } else {
+        const C* X = bufs[res];
+        const C* Y = bufs[base];
+        if (last) {
+          smem_cgemm(X, Y, m, [&](int e, C v) { o[e] = cadd2(cadd2(X[e], Y[e]), v); });
+        } else {
+          const int f = 3 - res - base;
+          C* Z = bufs[f];
+          smem_cgemm(X, Y, m, [&](int e, C v) { Z[e] = cadd2(cadd2(X[e], Y[e]), v); });
+          __syncthreads();
+          res = f;
+        }
+      }
     }
     if (kk > 1) {
-      smem_cgemm(sBase, sBase, m, [&](int e, C v) { sTmp[e] = v; });
+      const int f = (res != 1 && base != 1) ? 1 : ((res != 2 && base != 2) ? 2 : 0);
+      const C* X = bufs[base];
+      C* Z = bufs[f];
+      smem_cgemm(X, X, m, [&](int e, C v) { Z[e] = cadd2(cadd2(X[e], X[e]), v); });
       __syncthreads();
-      for (int e = threadIdx.x; e < mm; e += blockDim.x)
-        sBase[e] = cadd2(cadd2(sBase[e], sBase[e]), sTmp[e]);
-      __syncthreads();
+      base = f;
     }
   }
-  for (int e = threadIdx.x; e < mm; e += blockDim.x) o[e] = sRes[e];
 }
 
 }  // namespace qsx
@@ -786,7 +834,7 @@ int qsx_rk4_block_matrix_batched(const void* D, int m, int64_t batch, int precis
   QSX_CHECK_ARG(D && out && (nselect == 0 || select),
                 "qsx_rk4_block_matrix_batched: null pointer");
   const size_t cs = precision == QSX_FP32 ? sizeof(float2) : sizeof(double2);
-  const size_t smem = (4 * (size_t)m * m + 2 * (size_t)nselect * m) * cs;
+  const size_t smem = (3 * (size_t)m * m + 2 * (size_t)nselect * m) * cs;
   if (smem > 227 * 1024) {
     set_error("qsx_rk4_block_matrix_batched: %zu bytes of shared memory needed", smem);
     return QSX_ERR_UNSUPPORTED;

@@ -51,6 +51,10 @@ __host__ __device__ constexpr int lanes_per_sample() {
   return M == 1 ? 1 : (M == 2 ? 2 : 4);
 }
 
+__host__ __device__ constexpr int lanes_per_sample_rt(int m) {
+  return m == 1 ? 1 : (m == 2 ? 2 : 4);
+}
+
 constexpr int LANES_MAXPROJ = 4;
 
 template <int M>
@@ -141,25 +145,26 @@ __global__ void __launch_bounds__(128) rk4_lanes_f32(Rk4P p) {
   };
   save(0);
   for (int step = 1; step <= p.nsteps; ++step) {
-    float zx[R], zy[R];
+    // two partial sums per row (even / odd j) halve the dependent FMA chain
+    float zx[R][2], zy[R][2];
 #pragma unroll
-    for (int i = 0; i < R; ++i) zx[i] = zy[i] = 0.f;
+    for (int i = 0; i < R; ++i) zx[i][0] = zy[i][0] = zx[i][1] = zy[i][1] = 0.f;
 #pragma unroll
     for (int j = 0; j < M; ++j) {
       const float vx = __shfl_sync(0xffffffffu, yh[j % R][0], base + j / R);
       const float vy = __shfl_sync(0xffffffffu, yh[j % R][1], base + j / R);
 #pragma unroll
       for (int i = 0; i < R; ++i) {
-        zx[i] = fmaf(D[i][j].x, vx, zx[i]);
-        zx[i] = fmaf(-D[i][j].y, vy, zx[i]);
-        zy[i] = fmaf(D[i][j].x, vy, zy[i]);
-        zy[i] = fmaf(D[i][j].y, vx, zy[i]);
+        zx[i][j & 1] = fmaf(D[i][j].x, vx, zx[i][j & 1]);
+        zx[i][j & 1] = fmaf(-D[i][j].y, vy, zx[i][j & 1]);
+        zy[i][j & 1] = fmaf(D[i][j].x, vy, zy[i][j & 1]);
+        zy[i][j & 1] = fmaf(D[i][j].y, vx, zy[i][j & 1]);
       }
     }
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      dd_add(yh[i][0], yl[i][0], zx[i]);
-      dd_add(yh[i][1], yl[i][1], zy[i]);
+      dd_add(yh[i][0], yl[i][0], zx[i][0] + zx[i][1]);
+      dd_add(yh[i][1], yl[i][1], zy[i][0] + zy[i][1]);
     }
     if (step % p.save_every == 0) save(step / p.save_every);
   }
@@ -393,6 +398,136 @@ __global__ void __launch_bounds__(256, 2) rk4_block_f32(Rk4P p, int64_t ngroups,
   }
 }
 
+// rk4_block2_f32<M, LPR>: the same K-step blocked loop with each row split
+// over LPR lanes of one warp (lanes l, l ^ 8, l ^ 16, ... holding column
+// pairs [part HP, (part + 1) HP)): 1/LPR of the register-resident matrix row
+// and of the dependent FMA chain per thread, log2(LPR) shuffles to combine.
+// Rows of a sample fill whole warps (32 / LPR rows per warp), G samples per
+// CTA.
+template <int M, int LPR>
+__global__ void __launch_bounds__(448, 2) rk4_block2_f32(Rk4P p, int64_t ngroups, int G, int K) {
+  constexpr int ST = rows_stride(M);
+  constexpr int MP = (M % 2) ? M + 1 : M;
+  constexpr int NPAIR = MP / 2;
+  constexpr int HP = (NPAIR + LPR - 1) / LPR;  // column pairs per lane
+  constexpr int RPW = 32 / LPR;                // rows per warp
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2* ybuf = (float2*)smraw;             // [2][G][ST]
+  float2* stash = ybuf + 2 * G * ST;         // [2][K][G][nsel]
+  const int nsel = p.nselect;
+  const int RT = M + nsel * (K - 1);
+  const int wps = (RT + RPW - 1) / RPW;      // warps per sample
+  const int tid = threadIdx.x, lane = tid & 31, wi = tid >> 5;
+  const int g = wi / wps;
+  const int r = (wi % wps) * RPW + (lane % RPW);
+  const int part = lane / RPW;
+  const bool active = g < G && r < RT;
+  const bool main_row = active && r < M;
+  const bool writer = active && part == 0;
+  const int kx = main_row ? K : (active ? (r - M) / nsel + 1 : 0);
+  const int qx = (active && !main_row) ? (r - M) % nsel : -1;
+  int myq = -1;
+  if (main_row)
+    for (int q = 0; q < nsel; ++q)
+      if (p.select[q] == r) { myq = q; break; }
+  const int selr = (active && !main_row) ? p.select[qx] : 0;
+  for (int e = tid; e < 2 * G * ST; e += blockDim.x) ybuf[e] = make_float2(0.f, 0.f);
+  __syncthreads();
+  auto stash_at = [&](int par, int k, int gg, int q) -> float2& {
+    return stash[((par * K + k) * G + gg) * nsel + q];
+  };
+  const int gs = active ? g : 0;
+  int parity = 0;
+  for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const int64_t s = grp * G + gs;
+    const bool valid = active && s < p.batch;
+    float2 drow[2 * HP];
+    const float2* dm = (const float2*)p.matrix + (valid ? s * p.matrix_stride + (int64_t)r * M : 0);
+#pragma unroll
+    for (int t = 0; t < 2 * HP; ++t) {
+      const int j = part * 2 * HP + t;
+      drow[t] = (valid && j < M) ? dm[j] : make_float2(0.f, 0.f);
+    }
+    float yhx = 0.f, yhy = 0.f, ylx = 0.f, yly = 0.f;
+    if (valid && main_row) {
+      double2 v = p.y0[s * p.y0_stride + r];
+      yhx = (float)v.x;
+      yhy = (float)v.y;
+      ylx = (float)(v.x - (double)yhx);
+      yly = (float)(v.y - (double)yhy);
+    }
+    if (main_row && part == 0) ybuf[g * ST + r] = make_float2(yhx, yhy);
+    if (myq >= 0 && part == 0) {
+      stash_at(parity, 0, g, myq) = make_float2(yhx, yhy);
+      if (p.out_proj && valid)
+        p.out_proj[(s * p.nsave) * p.nout + myq] =
+            make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
+    }
+    __syncthreads();
+    if (p.partial)
+      for (int q = tid; q < nsel; q += blockDim.x) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int gg = 0; gg < G; ++gg) acc = cadd2(acc, stash_at(parity, 0, gg, q));
+        double2* dst = p.partial + ((int64_t)blockIdx.x * p.nsave) * p.nout + q;
+        atomicAdd(&dst->x, (double)acc.x);
+        atomicAdd(&dst->y, (double)acc.y);
+      }
+    parity ^= 1;
+    const int nblk = p.nsteps / K;
+    for (int bs = 0; bs < nblk; ++bs) {
+      const float2* cur = ybuf + ((bs & 1) * G + gs) * ST;
+      float2 a0 = make_float2(0.f, 0.f), a1 = a0;
+#pragma unroll
+      for (int t = 0; t < HP; ++t) {
+        const int pr = part * HP + t;
+        if (pr < NPAIR) {
+          const float4 v = *reinterpret_cast<const float4*>(&cur[2 * pr]);
+          cfma(a0, drow[2 * t], make_float2(v.x, v.y));
+          cfma(a1, drow[2 * t + 1], make_float2(v.z, v.w));
+        }
+      }
+      float sx = a0.x + a1.x, sy = a0.y + a1.y;
+#pragma unroll
+      for (int o = 16; o >= RPW; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+      }
+      const int step0 = bs * K;
+      if (writer && main_row) {
+        dd_add(yhx, ylx, sx);
+        dd_add(yhy, yly, sy);
+        ybuf[(((bs + 1) & 1) * G + g) * ST + r] = make_float2(yhx, yhy);
+        if (myq >= 0) {
+          stash_at(parity, K - 1, g, myq) = valid ? make_float2(yhx, yhy) : make_float2(0.f, 0.f);
+          if (p.out_proj && valid)
+            p.out_proj[(s * p.nsave + step0 + K) * p.nout + myq] =
+                make_double2((double)yhx + (double)ylx, (double)yhy + (double)yly);
+        }
+      } else if (writer) {
+        const float2 base = cur[selr];
+        const float2 v = valid ? make_float2(base.x + sx, base.y + sy) : make_float2(0.f, 0.f);
+        stash_at(parity, kx - 1, g, qx) = v;
+        if (p.out_proj && valid)
+          p.out_proj[(s * p.nsave + step0 + kx) * p.nout + qx] = make_double2(v.x, v.y);
+      }
+      __syncthreads();
+      if (p.partial)
+        for (int e = tid; e < K * nsel; e += blockDim.x) {
+          const int k = e / nsel, q = e % nsel;
+          float2 acc = make_float2(0.f, 0.f);
+          for (int gg = 0; gg < G; ++gg) acc = cadd2(acc, stash_at(parity, k, gg, q));
+          double2* dst = p.partial + ((int64_t)blockIdx.x * p.nsave + step0 + k + 1) * p.nout + q;
+          atomicAdd(&dst->x, (double)acc.x);
+          atomicAdd(&dst->y, (double)acc.y);
+        }
+      parity ^= 1;
+    }
+    if (valid && main_row && part == 0 && p.status && !(isfinite(yhx) && isfinite(yhy)))
+      atomicOr(p.status, QSX_ERR_NONFINITE);
+    __syncthreads();
+  }
+}
+
 // -------------------------------------------------------------- generic
 constexpr int GEN_MAXR = 4;  // rows per thread (M <= 4 * 1024)
 
@@ -596,6 +731,7 @@ enum Kind { K_SMALL = 0, K_ROWS = 1, K_GENERIC = 2, K_BLOCK = 3 };
 struct Plan {
   Kind kind;
   int G;
+  int lpr;  // K_BLOCK: lanes per matrix row (1: rk4_block_f32, 2: rk4_block2_f32)
   int64_t nslots;
   int64_t grid;
   int threads;
@@ -655,19 +791,35 @@ static int make_plan(const qsx_rk4_args* a, Plan* pl) {
                   "nsteps %% block_k == 0 and m in {9,16,25,36,49,64}");
     const int RT = m + a->nselect * (K - 1);
     QSX_CHECK_ARG(RT <= 256, "qsx_rk4: block_k rows per sample exceed 256");
-    G = std::max(1, 256 / RT);
+    QSX_CHECK_ARG(a->variant >= 0 && a->variant <= 4, "qsx_rk4: variant must be 0, 1, 2 or 4");
+    // lanes per row: the planner's default, or the variant an autotuner picked
+    QSX_CHECK_ARG(a->variant != 3, "qsx_rk4: variant must be 0, 1, 2 or 4");
+    const int lpr = a->variant ? a->variant : 1;
+    int threads;
+    if (lpr > 1) {
+      const int wps = (RT + 32 / lpr - 1) / (32 / lpr);
+      G = std::max(1, 448 / (wps * 32));
+      threads = G * wps * 32;
+    } else {
+      G = std::max(1, 256 / RT);
+      threads = ((G * RT + 31) / 32) * 32;
+    }
     int dev = 0, sms = 0, occ = 0;
     pl->smem = (2 * (size_t)G * 66 + 2 * (size_t)K * G * a->nselect) * sizeof(float2);
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = ((G * RT + 31) / 32) * 32;
-#define X(MM, GG, BB)                                                                    \
-  if (e == cudaSuccess && m == MM)                                                       \
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rk4_block_f32<MM>, threads, \
-                                                      pl->smem);
+#define X(MM, GG, BB)                                                                      \
+  if (e == cudaSuccess && m == MM)                                                         \
+    e = lpr == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                          \
+                       &occ, rk4_block2_f32<MM, 4>, threads, pl->smem)                     \
+        : lpr == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                          \
+                       &occ, rk4_block2_f32<MM, 2>, threads, pl->smem)                     \
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rk4_block_f32<MM>, \
+                                                                   threads, pl->smem);
     QSX_ROWS_TABLE(X)
 #undef X
     if (e != cudaSuccess) return cuda_status(e, "qsx_rk4 plan");
+    pl->lpr = lpr;
     pl->kind = K_BLOCK;
     pl->G = G;
     pl->threads = threads;
@@ -680,7 +832,7 @@ static int make_plan(const qsx_rk4_args* a, Plan* pl) {
   (void)nsave;
   if (a->precision == QSX_FP32 && a->form == 0 && m <= 8 && a->nproj <= LANES_MAXPROJ &&
       a->nselect <= LANES_MAXPROJ) {
-    const int lps = m == 1 ? 1 : (m == 2 ? 2 : 4);
+    const int lps = lanes_per_sample_rt(m);
     const int64_t threads = a->batch * lps;
     pl->kind = K_SMALL;
     pl->threads = 128;
@@ -812,8 +964,15 @@ int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
     case K_BLOCK: {
 #define X(MM, GG, BB)                                                                   \
   if (a->m == MM)                                                                       \
-    rk4_block_f32<MM><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(p, pl.ngroups, pl.G, \
-                                                                    a->block_k);
+    if (pl.lpr == 4)                                                                    \
+      rk4_block2_f32<MM, 4><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(             \
+          p, pl.ngroups, pl.G, a->block_k);                                             \
+    else if (pl.lpr == 2)                                                               \
+      rk4_block2_f32<MM, 2><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(             \
+          p, pl.ngroups, pl.G, a->block_k);                                             \
+    else                                                                                \
+      rk4_block_f32<MM><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(p, pl.ngroups, pl.G, \
+                                                                      a->block_k);
       QSX_ROWS_TABLE(X)
 #undef X
       break;
@@ -942,9 +1101,17 @@ extern "C" int qsx_rk4_block_mean_noalloc(const qsx_rk4_args* a, void* stream) {
   p.partial32 = nullptr;
   p.status = a->status;
 #define X(MM, GG, BB)                                                                    \
-  if (a->m == MM)                                                                        \
-    rk4_block_f32<MM><<<(unsigned)grid, pl.threads, pl.smem, s>>>(p, pl.ngroups, pl.G,   \
-                                                                  a->block_k);
+  if (a->m == MM) {                                                                      \
+    if (pl.lpr == 4)                                                                     \
+      rk4_block2_f32<MM, 4><<<(unsigned)grid, pl.threads, pl.smem, s>>>(p, pl.ngroups,    \
+                                                                        pl.G, a->block_k); \
+    else if (pl.lpr == 2)                                                                \
+      rk4_block2_f32<MM, 2><<<(unsigned)grid, pl.threads, pl.smem, s>>>(p, pl.ngroups,    \
+                                                                        pl.G, a->block_k); \
+    else                                                                                 \
+      rk4_block_f32<MM><<<(unsigned)grid, pl.threads, pl.smem, s>>>(p, pl.ngroups, pl.G,  \
+                                                                    a->block_k);         \
+  }
   QSX_ROWS_TABLE(X)
 #undef X
   QSX_LAUNCH_CHECK("qsx_rk4_block_mean_noalloc");

@@ -110,10 +110,12 @@ def test_fused_redfield_propagator_matches_two_step_path(golden):
             assert rel_err(fused, ref) < tol
 
 
+@pytest.mark.parametrize('variant', [0, 1, 2, 4])
 @pytest.mark.parametrize('M,B,K,nsteps', [(9, 13, 3, 30), (49, 11, 9, 54), (25, 7, 4, 40),
-                                          (64, 5, 2, 10)])
-def test_block_k_matches_step_by_step(M, B, K, nsteps):
-    """K-step blocking gives the same RK4 iterates as the step-by-step loop."""
+                                          (64, 5, 2, 10), (36, 40, 9, 27), (16, 33, 5, 25)])
+def test_block_k_matches_step_by_step(M, B, K, nsteps, variant):
+    """K-step blocking gives the same RK4 iterates as the step-by-step loop,
+    for every kernel variant (one, two or four lanes per matrix row)."""
     L = random_generators(B, M, seed=M + K)
     rng = np.random.RandomState(K)
     y0 = rng.randn(B, M) + 1j * rng.randn(B, M)
@@ -123,7 +125,7 @@ def test_block_k_matches_step_by_step(M, B, K, nsteps):
     blk = _native.rk4_block_matrix(D, K, sel)
     assert blk.shape == (B, M + len(sel) * (K - 1), M)
     out = _native.rk4(blk, torch.as_tensor(y0).cuda(), nsteps, 1, select=sel, mean=True,
-                      block_k=K)
+                      block_k=K, variant=variant)
     assert rel_err(out['proj'].cpu().numpy(), ref[:, :, sel]) < 1e-5
     assert rel_err(out['mean'].cpu().numpy(), ref[:, :, sel].mean(0)) < 1e-5
 
