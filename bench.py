@@ -47,7 +47,7 @@ CONFIG = {'workload': 'fmo7 Redfield ensemble: 7 sites, 16384 disorder samples '
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument('--gpus', type=int, default=1)
-    p.add_argument('--steps', type=int, default=10)
+    p.add_argument('--steps', type=int, default=30)
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     p.add_argument('--samples', type=int, default=N_SAMPLES)
@@ -67,6 +67,10 @@ def parse_args():
     p.add_argument('--third-fp64-samples', type=int, default=8,
                    help='samples of the FP32-vs-FP64 check (0 skips it)')
     p.add_argument('--adjoint-samples', type=int, default=1024)
+    p.add_argument('--adjoint-adam-steps', type=int, default=200)
+    p.add_argument('--no-adjoint-checks', action='store_true',
+                   help='skip the finite-difference and autograd gradient checks')
+    p.add_argument('--heom-steps', type=int, default=1999)
     return p.parse_args()
 
 
@@ -82,7 +86,7 @@ def fmo7_inputs():
 def clocks_start(index=0):
     try:
         return subprocess.Popen(['nvidia-smi', '--query-gpu=' + CLOCK_QUERY,
-                                 '--format=csv,noheader,nounits', '-lms', '200',
+                                 '--format=csv,noheader,nounits', '-lms', '50',
                                  '-i', str(index)],
                                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
                                 text=True)
@@ -199,10 +203,11 @@ def heom_ring8(torch, qg, native, samples=64, nsteps=1999):
     Hb = torch.as_tensor(np.array([base + np.diag(o) for o in offs])).cuda()
     y0 = torch.zeros(m.ado_count * 64, dtype=torch.complex128, device='cuda')
     y0[0] = 1.0
-    out = {'workload': 'HEOM 8-site ring, K=0, depth 4 (495 nodes), 64 samples, '
-                       '1999 RK4 steps at 0.5 fs', 'nodes': m.ado_count}
+    out = {'workload': 'HEOM 8-site ring, K=0, depth 4 (495 nodes), {} samples, '
+                       '{} RK4 steps at 0.5 fs'.format(samples, nsteps), 'nodes': m.ado_count}
     res = {}
-    for name, prec, steps in (('fp32', native.QSX_FP32, nsteps), ('fp64', native.QSX_FP64, 200)):
+    for name, prec, steps in (('fp32', native.QSX_FP32, nsteps),
+                              ('fp64', native.QSX_FP64, min(200, nsteps))):
         native.heom_rk4(tb, Hb, Hb, y0, 10, 0.5, qg.CM_FS, batch=samples, save_every=10,
                         precision=prec, per_sample=False, mean=True)
         torch.cuda.synchronize()
@@ -218,11 +223,13 @@ def heom_ring8(torch, qg, native, samples=64, nsteps=1999):
         out[name + '_steps_timed'] = steps
     k = res['fp64'].shape[0]
     a, b = res['fp32'][:k], res['fp64']
-    out['fp32_vs_fp64_rel_err_first_200_steps'] = float((a - b).abs().max() / b.abs().max())
+    out['fp32_vs_fp64_rel_err_first_{}_steps'.format(k - 1)] = float(
+        (a - b).abs().max() / b.abs().max())
     # structured generator: 495 nodes x (2 x 8^3 commutator + coupling terms) per RHS
     flops = 8.0 * samples * 4 * nsteps * m.ado_count * (2 * 8 ** 3 + 64 * tb.nterms)
     out['fp32_tflops_executed_form'] = flops / (out['fp32_ms'] * 1e-3) / 1e12
-    out['fp64_ms_note'] = 'FP64 timed over 200 steps and scaled to 1999'
+    out['fp64_ms_note'] = 'FP64 timed over {} steps and scaled to {}'.format(min(200, nsteps),
+                                                                             nsteps)
     return out
 
 
@@ -273,7 +280,7 @@ def third_order_chain24(torch, qg, samples=256, fp64_samples=8, reps=2, warm=Tru
             'output_shape': list(out['-++'].shape)}
 
 
-def adjoint_fmo7(torch, qg, samples=1024, adam_steps=200):
+def adjoint_fmo7(torch, qg, samples=1024, adam_steps=200, checks=True):
     """Gradient of the absorption misfit (1024 frequencies, 11800-13000 cm^-1)
     of the 7-site model's 1024-sample ensemble (SD 80 cm^-1) w.r.t. 7 site
     energies, 21 couplings and lambda; 2048 points at 1 fs, checkpoints every
@@ -334,38 +341,41 @@ def adjoint_fmo7(torch, qg, samples=1024, adam_steps=200):
         bwd_samples.append((time.perf_counter() - t0) * 1000.0)
     bwd_ms = min(bwd_samples)
     g_adj = holder['th'].grad.detach().cpu().numpy()
-    th2 = theta0.clone().requires_grad_(True)
-    fit.misfit(th2, target, impl='autograd').backward()
-    g_ref = th2.grad.detach().cpu().numpy()
-    h = 1e-3
-    fd = np.zeros_like(g_adj)
-    with torch.no_grad():
-        for i in range(len(fd)):
-            e = torch.zeros_like(theta0)
-            e[i] = h
-            fd[i] = ((fit.misfit(theta0 + e, target) - fit.misfit(theta0 - e, target))
-                     / (2 * h)).item()
     rel = lambda a, b: float(np.abs(a - b).max() / np.abs(b).max())  # noqa: E731
-    t0 = time.perf_counter()
-    theta_fit, hist = fit.fit(theta0, target, steps=adam_steps, lr=0.5)
-    torch.cuda.synchronize()
-    adam_s = time.perf_counter() - t0
-    err0 = (theta0 - theta_true).abs()
-    err1 = (theta_fit - theta_true).abs()
-    return {'workload': '7-site Redfield absorption misfit on 1024 frequencies '
+    out = {}
+    if checks:
+        th2 = theta0.clone().requires_grad_(True)
+        fit.misfit(th2, target, impl='autograd').backward()
+        g_ref = th2.grad.detach().cpu().numpy()
+        h = 1e-3
+        fd = np.zeros_like(g_adj)
+        with torch.no_grad():
+            for i in range(len(fd)):
+                e = torch.zeros_like(theta0)
+                e[i] = h
+                fd[i] = ((fit.misfit(theta0 + e, target) - fit.misfit(theta0 - e, target))
+                         / (2 * h)).item()
+        out['grad_rel_err_vs_central_fd_h1e-3'] = rel(g_adj, fd)
+        out['grad_rel_err_vs_fp64_autograd_rk4'] = rel(g_adj, g_ref)
+    if adam_steps:
+        t0 = time.perf_counter()
+        theta_fit, hist = fit.fit(theta0, target, steps=adam_steps, lr=0.5)
+        torch.cuda.synchronize()
+        adam_s = time.perf_counter() - t0
+        err0 = (theta0 - theta_true).abs()
+        err1 = (theta_fit - theta_true).abs()
+        out['adam'] = {'steps': adam_steps, 'lr': 0.5, 'seconds': adam_s,
+                       'misfit_start': hist[0], 'misfit_end': hist[-1],
+                       'max_abs_err_start_cm': float(err0.max()),
+                       'max_abs_err_end_cm': float(err1.max()),
+                       'site_energy_err_end_cm': float(err1[:7].max()),
+                       'coupling_err_end_cm': float(err1[7:-1].max()),
+                       'lambda_end': float(theta_fit[-1])}
+    return dict({'workload': '7-site Redfield absorption misfit on 1024 frequencies '
                         '(11800-13000 cm^-1), {} disorder samples (SD 80 cm^-1), 2048 x '
                         '1 fs, checkpoints every 64 steps, 29 parameters'.format(samples),
             'forward_ms': fwd_ms, 'forward_with_graph_ms': fwdg_ms, 'adjoint_ms': bwd_ms,
-            'adjoint_over_forward': bwd_ms / fwd_ms,
-            'grad_rel_err_vs_central_fd_h1e-3': rel(g_adj, fd),
-            'grad_rel_err_vs_fp64_autograd_rk4': rel(g_adj, g_ref),
-            'adam': {'steps': adam_steps, 'lr': 0.5, 'seconds': adam_s,
-                     'misfit_start': hist[0], 'misfit_end': hist[-1],
-                     'max_abs_err_start_cm': float(err0.max()),
-                     'max_abs_err_end_cm': float(err1.max()),
-                     'site_energy_err_end_cm': float(err1[:7].max()),
-                     'coupling_err_end_cm': float(err1[7:-1].max()),
-                     'lambda_end': float(theta_fit[-1])}}
+            'adjoint_over_forward': bwd_ms / fwd_ms}, **out)
 
 
 def ncu_traffic(path=os.path.join(ROOT, 'profiles', 'rk4_block_f32_fmo7.md')):
@@ -413,6 +423,8 @@ def our_arm(args):
         work.run(off, 'fp32')
     barrier()
     clk = clocks_start(local) if rank == 0 else None
+    if clk is not None:
+        time.sleep(0.6)  # the sampler's first reading lands inside the timed region
     events = {}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -525,13 +537,16 @@ def main():
         import qspectra_gb300 as qg
         from qspectra_gb300 import _native
         if args.only == 'heom':
-            out = heom_ring8(torch, qg, _native, samples=args.heom_samples)
+            out = heom_ring8(torch, qg, _native, samples=args.heom_samples,
+                             nsteps=args.heom_steps)
         elif args.only == 'third':
             out = third_order_chain24(torch, qg, samples=args.third_samples,
                                       fp64_samples=args.third_fp64_samples,
                                       reps=args.third_reps, warm=args.third_reps > 1)
         else:
-            out = adjoint_fmo7(torch, qg, samples=args.adjoint_samples)
+            out = adjoint_fmo7(torch, qg, samples=args.adjoint_samples,
+                               adam_steps=args.adjoint_adam_steps,
+                               checks=not args.no_adjoint_checks)
         print(json.dumps(out), flush=True)
         return 0
     return our_arm(args)

@@ -76,7 +76,7 @@ __device__ __forceinline__ void col_rank2(double* __restrict__ x, int ld,
   for (; i < m; ++i) x[(int64_t)i * ld] = fma(-a[i], bc, fma(-b[i], ac, x[(int64_t)i * ld]));
 }
 
-__global__ void __launch_bounds__(512)
+__global__ void __maxnreg__(112)
     eigh_tql_kernel(const double* __restrict__ A, int n, double* W, double* Zw, double* Sw,
                     double* __restrict__ E, double* __restrict__ U, int* status) {
   extern __shared__ __align__(16) double sm[];
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(512)
       const double K = 0.5 * tau * block_sum(vp, red);
       for (int r = tid; r < m; r += bd) w[r] -= K * v[r];
       __syncthreads();
-      for (int c = tid; c < m; c += bd) col_rank2(B + c, n, v, w, v[c], w[c], m);
+      for (int c = tid; c < m; c += bd) col_rank2(B + c, n, v, w, w[c], v[c], m);
     } else {
       if (tid == 0) e[k] = x0;
     }
