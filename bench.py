@@ -378,6 +378,25 @@ def adjoint_fmo7(torch, qg, samples=1024, adam_steps=200, checks=True):
             'adjoint_over_forward': bwd_ms / fwd_ms}, **out)
 
 
+def measured_hbm_gbs():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return float(json.load(f)['hbm_gbs']), 'measured (MEASURED_PEAKS.json)'
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 'fallback (6.8 TB/s)'
+
+
+def hbm_view(traffic, launch_ms):
+    """The same kernel against the HBM roofline: ncu DRAM bytes per launch
+    over the CUDA-event launch time, as a fraction of the measured copy
+    bandwidth."""
+    peak, src = measured_hbm_gbs()
+    if not traffic or not launch_ms:
+        return {'peak_gbs': peak, 'peak_source': src, 'achieved_gbs': None, 'frac': None}
+    gbs = traffic / (launch_ms * 1e-3) / 1e9
+    return {'achieved_gbs': gbs, 'peak_gbs': peak, 'frac': gbs / peak, 'peak_source': src}
+
+
 def ncu_traffic(path=os.path.join(ROOT, 'profiles', 'rk4_block_f32_fmo7.md')):
     try:
         txt = open(path).read()
@@ -507,7 +526,8 @@ def our_arm(args):
                      'peak_source': 'measured live by qsx_probe_fma (FP32 FMA); '
                                     'MEASURED_PEAKS.json has no CUDA-core figure',
                      'flops_per_launch': flops_dyn, 'launch_ms': dyn_ms,
-                     'traffic': traffic},
+                     'traffic': traffic,
+                     'hbm': hbm_view(traffic, dyn_ms)},
         'gpu_launches': 12 * args.steps,
         'clocks': clocks,
     }

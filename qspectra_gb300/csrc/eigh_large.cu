@@ -3,17 +3,20 @@
 // The reference diagonalises each sample's Hamiltonian with scipy.linalg.eigh
 // (qspectra/hamiltonian.py:310-328).
 //
-// One CTA per matrix, four phases over a global-memory workspace:
-//   1. Householder reduction to tridiagonal form, A = Q T Q^T: for each
+// Four kernels over a global-memory workspace:
+//   1. Householder reduction to tridiagonal form (one CTA per matrix),
+//      A = Q T Q^T: for each
 //      column k, v with (I - tau v v^T) x = alpha e_1 and the two-sided
 //      update B <- B - v w^T - w v^T, w = p - (tau/2)(v^T p) v, p = tau B v.
 //   2. Eigenvalues of T by implicit QL with Wilkinson-type shifts, without
-//      vectors (one thread; O(n^2)).
-//   3. Eigenvectors of T by inverse iteration: LU with partial pivoting of
+//      vectors (one thread per matrix; O(n^2)).
+//   3. Eigenvectors of T by inverse iteration (one thread per eigenvalue of
+//      every matrix): LU with partial pivoting of
 //      T - lambda I, three solves from a vector of ones; eigenvalues closer
 //      than 1e-3 |T| form a cluster handled by one thread with modified
 //      Gram-Schmidt against the cluster's earlier vectors.
-//   4. Back-transform by the Householder reflectors, U = H_0 ... H_{n-3} Z.
+//   4. Back-transform by the Householder reflectors, U = H_0 ... H_{n-3} Z
+//      (one CTA per matrix).
 // This keeps the FP64 work near 2 n^3 multiply-adds per matrix (no Givens
 // rotations accumulated into Q).  Eigenvalues are returned ascending with
 // U[:, k] the k-th eigenvector.  Every loop is bounded: a QL that does not
@@ -76,28 +79,27 @@ __device__ __forceinline__ void col_rank2(double* __restrict__ x, int ld,
   for (; i < m; ++i) x[(int64_t)i * ld] = fma(-a[i], bc, fma(-b[i], ac, x[(int64_t)i * ld]));
 }
 
-__global__ void __maxnreg__(112)
-    eigh_tql_kernel(const double* __restrict__ A, int n, double* W, double* Zw, double* Sw,
-                    double* __restrict__ E, double* __restrict__ U, int* status) {
+constexpr int TQ_THREADS = 320;
+
+// ---- A. Householder tridiagonalisation: one CTA per matrix.  Writes the
+// diagonal and sub-diagonal to de[b] = {d[0..n), e[0..n)} and keeps, in the
+// work matrix W, each reflector v_k in row k right of the diagonal with
+// tau_k on the diagonal.
+__global__ void __launch_bounds__(TQ_THREADS, 2)
+    eigh_tridiag_kernel(const double* __restrict__ A, int n, double* W, double* de) {
   extern __shared__ __align__(16) double sm[];
-  double* d = sm;          // [n] diagonal
-  double* e = d + n;       // [n] sub-diagonal
-  double* v = e + n;       // [n] Householder vector
+  double* v = sm;          // [n] Householder vector
   double* w = v + n;       // [n]
-  double* rc = w + n;      // [n] rotation cosines
-  double* rs = rc + n;     // [n] rotation sines
-  double* red = rs + n;    // [32]
-  int* ctl = (int*)(red + 32);  // [4] m, nrot, stop
-  int* rank = ctl + 4;     // [n]
+  double* red = w + n;     // [32]
   const int tid = threadIdx.x, bd = blockDim.x;
   const int64_t b = blockIdx.x;
   const int64_t nn = (int64_t)n * n;
   const double* a = A + b * nn;
   double* Wm = W + b * nn;
-  double* Z = Zw + b * nn;
+  double* d = de + b * 2 * (int64_t)n;
+  double* e = d + n;
   for (int64_t i = tid; i < nn; i += bd) Wm[i] = a[i];
   __syncthreads();
-  // ---- 1. tridiagonalisation (full symmetric trailing block, row k = column k)
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;
     const double* rowk = Wm + (int64_t)k * n + k + 1;
@@ -137,7 +139,6 @@ __global__ void __maxnreg__(112)
       if (tid == 0) e[k] = x0;
     }
     __syncthreads();
-    // keep v (row k, right of the diagonal) and tau (on the diagonal) for phase 2
     for (int i = tid; i < m; i += bd) Wm[(int64_t)k * n + k + 1 + i] = tau != 0.0 ? v[i] : 0.0;
     if (tid == 0) Wm[(int64_t)k * n + k] = tau;
     __syncthreads();
@@ -149,184 +150,204 @@ __global__ void __maxnreg__(112)
     }
     d[n - 1] = Wm[(int64_t)(n - 1) * n + n - 1];
     e[n - 1] = 0.0;
+    if (n >= 2) Wm[(int64_t)(n - 2) * n + n - 2] = 0.0;  // no reflector for k = n-2
   }
-  // ---- 2. eigenvalues: implicit QL on (d, e) without vectors, one thread
-  double* dv = rs;  // QL works on copies; d and e stay for inverse iteration
-  double* ev = rc;
-  for (int i = tid; i < n; i += bd) {
-    dv[i] = d[i];
-    ev[i] = e[i];
-  }
-  __syncthreads();
-  if (tid == 0) {
-    int bad = 0;
-    for (int l = 0; l < n; ++l) {
-      for (int iter = 0;; ++iter) {
-        int m = l;
-        for (; m < n - 1; ++m) {
-          const double dd = fabs(dv[m]) + fabs(dv[m + 1]);
-          if (fabs(ev[m]) <= DBL_EPSILON * dd) break;
-        }
-        if (m == l) break;
-        if (iter >= 60) {
-          bad = 1;
+}
+
+// ---- B. eigenvalues by implicit QL without vectors, one thread per matrix,
+// then sorted ascending into ws[b].
+__global__ void eigh_ql_kernel(const double* __restrict__ de, int n, int64_t batch,
+                               double* work, double* ws, int* status) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  double* dv = work + b * 2 * (int64_t)n;
+  double* ev = dv + n;
+  const double* d0 = de + b * 2 * (int64_t)n;
+  for (int i = 0; i < 2 * n; ++i) dv[i] = d0[i];
+  int bad = 0;
+  for (int l = 0; l < n; ++l) {
+    for (int iter = 0;; ++iter) {
+      int m = l;
+      for (; m < n - 1; ++m) {
+        const double dd = fabs(dv[m]) + fabs(dv[m + 1]);
+        if (fabs(ev[m]) <= DBL_EPSILON * dd) break;
+      }
+      if (m == l) break;
+      if (iter >= 60) {
+        bad = 1;
+        break;
+      }
+      double g = (dv[l + 1] - dv[l]) / (2.0 * ev[l]);
+      double r = hypot(g, 1.0);
+      g = dv[m] - dv[l] + ev[l] / (g + copysign(r, g));
+      double s = 1.0, c = 1.0, p = 0.0;
+      bool split = false;
+      for (int i = m - 1; i >= l; --i) {
+        const double f = s * ev[i], bb = c * ev[i];
+        const double rr = fma(f, f, g * g);
+        if (rr == 0.0) {
+          dv[i + 1] -= p;
+          ev[m] = 0.0;
+          split = true;
           break;
         }
-        double g = (dv[l + 1] - dv[l]) / (2.0 * ev[l]);
-        double r = hypot(g, 1.0);
-        g = dv[m] - dv[l] + ev[l] / (g + copysign(r, g));
-        double s = 1.0, c = 1.0, p = 0.0;
-        bool split = false;
-        for (int i = m - 1; i >= l; --i) {
-          const double f = s * ev[i], bb = c * ev[i];
-          const double rr = fma(f, f, g * g);
-          if (rr == 0.0) {
-            dv[i + 1] -= p;
-            ev[m] = 0.0;
-            split = true;
-            break;
-          }
-          const double rinv = rsqrt(rr);
-          r = rr * rinv;
-          ev[i + 1] = r;
-          s = f * rinv;
-          c = g * rinv;
-          g = dv[i + 1] - p;
-          r = (dv[i] - g) * s + 2.0 * c * bb;
-          p = s * r;
-          dv[i + 1] = g + p;
-          g = c * r - bb;
-        }
-        if (!split) {
-          dv[l] -= p;
-          ev[l] = g;
-          ev[m] = 0.0;
-        }
+        const double rinv = rsqrt(rr);
+        r = rr * rinv;
+        ev[i + 1] = r;
+        s = f * rinv;
+        c = g * rinv;
+        g = dv[i + 1] - p;
+        r = (dv[i] - g) * s + 2.0 * c * bb;
+        p = s * r;
+        dv[i + 1] = g + p;
+        g = c * r - bb;
+      }
+      if (!split) {
+        dv[l] -= p;
+        ev[l] = g;
+        ev[m] = 0.0;
       }
     }
-    ctl[2] = bad;
   }
-  __syncthreads();
-  // ascending order (ties by index)
-  for (int i = tid; i < n; i += bd) {
-    int rk = 0;
-    const double di = dv[i];
-    for (int j = 0; j < n; ++j) rk += (dv[j] < di) || (dv[j] == di && j < i);
-    rank[i] = rk;
+  if (bad && status) atomicOr(status, QSX_ERR_NONFINITE);
+  // insertion sort (n <= 2048, once per matrix)
+  double* w = ws + b * (int64_t)n;
+  for (int i = 0; i < n; ++i) {
+    const double x = dv[i];
+    int j = i;
+    while (j > 0 && w[j - 1] > x) {
+      w[j] = w[j - 1];
+      --j;
+    }
+    w[j] = x;
   }
-  __syncthreads();
-  for (int i = tid; i < n; i += bd) w[rank[i]] = dv[i];  // sorted eigenvalues
-  __syncthreads();
-  // ---- 3. eigenvectors of T by inverse iteration, row-major in Z (column j
-  // = eigenvector of the j-th smallest eigenvalue).  Eigenvalues closer than
-  // 1e-3 |T| form a cluster, handled by one thread in order with modified
-  // Gram-Schmidt against the cluster's earlier vectors.
+}
+
+// ---- C. eigenvectors of T by inverse iteration, one thread per eigenvalue
+// of every matrix; eigenvalues closer than 1e-3 |T| form a cluster handled
+// by its first thread in order, with modified Gram-Schmidt against the
+// cluster's earlier vectors.  Z[b] row-major, column j for eigenvalue j.
+__global__ void eigh_invit_kernel(const double* __restrict__ de, const double* __restrict__ ws,
+                                  int n, int64_t batch, double* Z, double* scratch) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= batch * n) return;
+  const int64_t b = t / n;
+  const int j = (int)(t % n);
+  const double* d = de + b * 2 * (int64_t)n;
+  const double* e = d + n;
+  const double* w = ws + b * (int64_t)n;
+  double* z = Z + b * (int64_t)n * n;
   double tnorm = 0.0;
   for (int i = 0; i < n; ++i)
     tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]) + (i ? fabs(e[i - 1]) : 0.0));
   const double ortol = 1e-3 * tnorm;
   const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
-  for (int j = tid; j < n; j += bd) {
-    if (j > 0 && w[j] - w[j - 1] < ortol) continue;  // not the first of its cluster
-    int jend = j + 1;
-    while (jend < n && w[jend] - w[jend - 1] < ortol) ++jend;
-    double* sc = Sw + ((int64_t)b * n + j) * 5 * (int64_t)n;  // this thread's scratch
-    double* u1 = sc;
-    double* u2 = sc + n;
-    double* u3 = sc + 2 * n;
-    double* lm = sc + 3 * n;
-    double* x = sc + 4 * n;
-    for (int jj = j; jj < jend; ++jj) {
-      // eigenvalues of a cluster are separated by a small multiple of the
-      // tolerance so that each factorisation differs
-      const double lam = w[jj] + (jj - j) * 10.0 * tiny;
-      // LU with partial pivoting of T - lam I: u1, u2, u3 the three diagonals
-      // of U, lm the multipliers (|l| <= 1; l + 4 where rows i, i+1 swapped)
-      double pp = d[0] - lam, qq = n > 1 ? e[0] : 0.0;
-      for (int i = 0; i < n - 1; ++i) {
-        const double sub = e[i];
-        const double an = d[i + 1] - lam, en = (i + 1 < n - 1) ? e[i + 1] : 0.0;
-        if (fabs(pp) >= fabs(sub)) {
-          if (pp == 0.0) pp = tiny;
-          const double l = sub / pp;
-          u1[i] = pp;
-          u2[i] = qq;
-          u3[i] = 0.0;
-          lm[i] = l;
-          pp = an - l * qq;
-          qq = en;
-        } else {
-          const double l = pp / sub;
-          u1[i] = sub;
-          u2[i] = an;
-          u3[i] = en;
-          lm[i] = l + 4.0;  // rows swapped: multipliers lie in [-1, 1], so l + 4 flags it
-          const double np = qq - l * an;
-          qq = -l * en;
-          pp = np;
-        }
+  if (j > 0 && w[j] - w[j - 1] < ortol) return;  // not the first of its cluster
+  int jend = j + 1;
+  while (jend < n && w[jend] - w[jend - 1] < ortol) ++jend;
+  double* sc = scratch + t * 5 * (int64_t)n;
+  double* u1 = sc;
+  double* u2 = sc + n;
+  double* u3 = sc + 2 * n;
+  double* lm = sc + 3 * n;
+  double* x = sc + 4 * n;
+  for (int jj = j; jj < jend; ++jj) {
+    // equal eigenvalues of a cluster are pulled apart slightly so that each
+    // factorisation differs
+    const double lam = w[jj] + (jj - j) * 10.0 * tiny;
+    // LU with partial pivoting of T - lam I: u1, u2, u3 the three diagonals
+    // of U, lm the multipliers (|l| <= 1; l + 4 where rows i, i+1 swapped)
+    double pp = d[0] - lam, qq = n > 1 ? e[0] : 0.0;
+    for (int i = 0; i < n - 1; ++i) {
+      const double sub = e[i];
+      const double an = d[i + 1] - lam, en = (i + 1 < n - 1) ? e[i + 1] : 0.0;
+      if (fabs(pp) >= fabs(sub)) {
+        if (pp == 0.0) pp = tiny;
+        const double l = sub / pp;
+        u1[i] = pp;
+        u2[i] = qq;
+        u3[i] = 0.0;
+        lm[i] = l;
+        pp = an - l * qq;
+        qq = en;
+      } else {
+        const double l = pp / sub;
+        u1[i] = sub;
+        u2[i] = an;
+        u3[i] = en;
+        lm[i] = l + 4.0;
+        const double np = qq - l * an;
+        qq = -l * en;
+        pp = np;
       }
-      u1[n - 1] = pp == 0.0 ? tiny : pp;
-      // start vector: all ones (the first solve uses U only)
-      for (int i = 0; i < n; ++i) x[i] = 1.0;
-      for (int it = 0; it < 3; ++it) {
-        if (it > 0) {
-          // apply the row interchanges and multipliers (L^{-1} P)
-          for (int i = 0; i < n - 1; ++i) {
-            const double t = lm[i];
-            if (t > 2.0) {
-              const double l = t - 4.0;
-              const double xi = x[i];
-              x[i] = x[i + 1];
-              x[i + 1] = xi - l * x[i];
-            } else {
-              x[i + 1] -= t * x[i];
-            }
+    }
+    u1[n - 1] = pp == 0.0 ? tiny : pp;
+    for (int i = 0; i < n; ++i) x[i] = 1.0;  // the first solve uses U only
+    for (int it = 0; it < 3; ++it) {
+      if (it > 0) {
+        for (int i = 0; i < n - 1; ++i) {
+          const double tt = lm[i];
+          if (tt > 2.0) {
+            const double l = tt - 4.0;
+            const double xi = x[i];
+            x[i] = x[i + 1];
+            x[i + 1] = xi - l * x[i];
+          } else {
+            x[i + 1] -= tt * x[i];
           }
         }
-        // U x = x
-        for (int i = n - 1; i >= 0; --i) {
-          double v = x[i];
-          if (i + 1 < n) v -= u2[i] * x[i + 1];
-          if (i + 2 < n) v -= u3[i] * x[i + 2];
-          double piv = u1[i];
-          if (fabs(piv) < tiny) piv = copysign(tiny, piv);
-          x[i] = v / piv;
-        }
-        // orthogonalise against the cluster's earlier vectors, normalise
-        for (int k = j; k < jj; ++k) {
-          double dot = 0.0;
-          for (int i = 0; i < n; ++i) dot = fma(Z[(int64_t)i * n + k], x[i], dot);
-          for (int i = 0; i < n; ++i) x[i] -= dot * Z[(int64_t)i * n + k];
-        }
-        double nrm = 0.0;
-        for (int i = 0; i < n; ++i) nrm = fma(x[i], x[i], nrm);
-        const double inv = nrm > 0.0 ? rsqrt(nrm) : 0.0;
-        for (int i = 0; i < n; ++i) x[i] *= inv;
       }
-      for (int i = 0; i < n; ++i) Z[(int64_t)i * n + jj] = x[i];
+      for (int i = n - 1; i >= 0; --i) {
+        double vv = x[i];
+        if (i + 1 < n) vv -= u2[i] * x[i + 1];
+        if (i + 2 < n) vv -= u3[i] * x[i + 2];
+        double piv = u1[i];
+        if (fabs(piv) < tiny) piv = copysign(tiny, piv);
+        x[i] = vv / piv;
+      }
+      for (int k = j; k < jj; ++k) {
+        double dot = 0.0;
+        for (int i = 0; i < n; ++i) dot = fma(z[(int64_t)i * n + k], x[i], dot);
+        for (int i = 0; i < n; ++i) x[i] -= dot * z[(int64_t)i * n + k];
+      }
+      double nrm = 0.0;
+      for (int i = 0; i < n; ++i) nrm = fma(x[i], x[i], nrm);
+      const double inv = nrm > 0.0 ? rsqrt(nrm) : 0.0;
+      for (int i = 0; i < n; ++i) x[i] *= inv;
     }
+    for (int i = 0; i < n; ++i) z[(int64_t)i * n + jj] = x[i];
   }
-  __syncthreads();
-  // ---- 4. back-transform U = H_0 H_1 ... H_{n-3} Z (reflector k acts on
-  // rows k+1 ..), applied from k = n-3 down to 0
+}
+
+// ---- D. back-transform U = H_0 H_1 ... H_{n-3} Z (reflector k acts on rows
+// k+1 ..), applied from k = n-3 down to 0; writes E and U.
+__global__ void __launch_bounds__(TQ_THREADS, 2)
+    eigh_backtransform_kernel(const double* __restrict__ W, const double* __restrict__ ws,
+                              int n, double* Z, double* __restrict__ E,
+                              double* __restrict__ U) {
+  extern __shared__ __align__(16) double sm[];
+  double* v = sm;  // [n]
+  const int tid = threadIdx.x, bd = blockDim.x;
+  const int64_t b = blockIdx.x;
+  const int64_t nn = (int64_t)n * n;
+  const double* Wm = W + b * nn;
+  double* z = Z + b * nn;
   for (int k = n - 3; k >= 0; --k) {
     const double tau = Wm[(int64_t)k * n + k];
     if (tau == 0.0) continue;
     const int m = n - k - 1;
     for (int i = tid; i < m; i += bd) v[i] = Wm[(int64_t)k * n + k + 1 + i];
     __syncthreads();
-    double* Zb = Z + (int64_t)(k + 1) * n;
+    double* Zb = z + (int64_t)(k + 1) * n;
     for (int c = tid; c < n; c += bd) {
       const double u = tau * col_dot(Zb + c, n, v, m);
       col_rank2(Zb + c, n, v, v, u, 0.0, m);
     }
     __syncthreads();
   }
-  if (tid == 0 && ctl[2] && status) atomicOr(status, QSX_ERR_NONFINITE);
-  for (int i = tid; i < n; i += bd) E[b * n + i] = w[i];
+  for (int i = tid; i < n; i += bd) E[b * n + i] = ws[b * n + i];
   double* u = U + b * nn;
-  for (int64_t idx = tid; idx < nn; idx += bd) u[idx] = Z[idx];
+  for (int64_t idx = tid; idx < nn; idx += bd) u[idx] = z[idx];
 }
 
 }  // namespace qsx
@@ -335,8 +356,9 @@ using namespace qsx;
 
 extern "C" size_t qsx_eigh_large_workspace_bytes(int n, int64_t batch) {
   if (n < 1 || batch < 0) return 0;
-  // reduction matrix, eigenvectors, and 5 n doubles of scratch per eigenvalue
-  return (size_t)7 * n * n * (size_t)batch * sizeof(double);
+  // reduction matrix and eigenvectors (n^2 each), inverse-iteration scratch
+  // (5 n per eigenvalue), d/e, their QL copies and the sorted eigenvalues
+  return ((size_t)7 * n * n + (size_t)5 * n) * (size_t)batch * sizeof(double);
 }
 
 extern "C" int qsx_eigh_large_batched(const double* H, int n, int64_t batch, double* E,
@@ -350,16 +372,28 @@ extern "C" int qsx_eigh_large_batched(const double* H, int n, int64_t batch, dou
   QSX_CHECK_ARG(workspace && workspace_bytes >= need,
                 "qsx_eigh_large_batched: workspace of %zu bytes needed (got %zu)", need,
                 workspace_bytes);
-  const size_t smem = ((size_t)6 * n + 32) * sizeof(double) + ((size_t)4 + n) * sizeof(int);
-  cudaError_t e = cudaFuncSetAttribute(eigh_tql_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return cuda_status(e, "qsx_eigh_large_batched");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t nnb = (size_t)n * n * batch;
   double* W = (double*)workspace;
-  double* Z = W + (size_t)n * n * batch;
-  double* Sw = Z + (size_t)n * n * batch;
-  const int threads = n >= 512 ? 512 : ((n + 31) / 32) * 32;
-  eigh_tql_kernel<<<(unsigned)batch, threads, smem, (cudaStream_t)stream>>>(H, n, W, Z, Sw, E,
-                                                                            U, status);
+  double* Z = W + nnb;
+  double* scratch = Z + nnb;
+  double* de = scratch + 5 * nnb;
+  double* work = de + 2 * (size_t)n * batch;
+  double* ws = work + 2 * (size_t)n * batch;
+  const int threads = n >= TQ_THREADS ? TQ_THREADS : ((n + 31) / 32) * 32;
+  const size_t smemA = ((size_t)2 * n + 32) * sizeof(double);
+  const size_t smemD = (size_t)n * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(eigh_tridiag_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemA);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(eigh_backtransform_kernel,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemD);
+  if (e != cudaSuccess) return cuda_status(e, "qsx_eigh_large_batched");
+  eigh_tridiag_kernel<<<(unsigned)batch, threads, smemA, s>>>(H, n, W, de);
+  eigh_ql_kernel<<<(unsigned)((batch + 63) / 64), 64, 0, s>>>(de, n, batch, work, ws, status);
+  const int64_t nt = batch * n;
+  eigh_invit_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(de, ws, n, batch, Z, scratch);
+  eigh_backtransform_kernel<<<(unsigned)batch, threads, smemD, s>>>(W, ws, n, Z, E, U);
   QSX_LAUNCH_CHECK("qsx_eigh_large_batched");
   return QSX_OK;
 }

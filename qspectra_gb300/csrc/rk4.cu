@@ -43,16 +43,19 @@ __device__ __forceinline__ float2 f2(double2 v) { return make_float2((float)v.x,
 // ---------------------------------------------------------------- small M
 // rk4_lanes_f32<M>: M <= 8.  LPS lanes per sample (a power of two dividing
 // 32), lane q holding rows [q*R, q*R + R) of D and of the state in registers.
+// One lane per sample (the default) keeps the whole M x M matrix and state in
+// the lane's registers: no gather shuffles, 32 samples per warp, so the loop
+// issues a few instructions per sample-step instead of the shuffle traffic.
 // Each step gathers the M state values with shuffles, updates its rows in
 // split-word FP32 and, at save steps, folds the projections of all samples
 // of the warp into one FP32 partial sum per warp (slot = warp).
 template <int M>
 __host__ __device__ constexpr int lanes_per_sample() {
-  return M == 1 ? 1 : (M == 2 ? 2 : 4);
+  return M == 8 ? 2 : 1;  // M = 8 on one lane would exceed the register budget
 }
 
 __host__ __device__ constexpr int lanes_per_sample_rt(int m) {
-  return m == 1 ? 1 : (m == 2 ? 2 : 4);
+  return m == 8 ? 2 : 1;
 }
 
 constexpr int LANES_MAXPROJ = 4;
@@ -151,8 +154,9 @@ __global__ void __launch_bounds__(128) rk4_lanes_f32(Rk4P p) {
     for (int i = 0; i < R; ++i) zx[i][0] = zy[i][0] = zx[i][1] = zy[i][1] = 0.f;
 #pragma unroll
     for (int j = 0; j < M; ++j) {
-      const float vx = __shfl_sync(0xffffffffu, yh[j % R][0], base + j / R);
-      const float vy = __shfl_sync(0xffffffffu, yh[j % R][1], base + j / R);
+      // one lane per sample holds the whole state; otherwise gather it
+      const float vx = LPS == 1 ? yh[j][0] : __shfl_sync(0xffffffffu, yh[j % R][0], base + j / R);
+      const float vy = LPS == 1 ? yh[j][1] : __shfl_sync(0xffffffffu, yh[j % R][1], base + j / R);
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         zx[i][j & 1] = fmaf(D[i][j].x, vx, zx[i][j & 1]);

@@ -8,7 +8,8 @@ the bath reorganisation energy of a Redfield model (redfield.py:9-152).
 
 * The Heisenberg-picture 'eg' generator of every sample is built in FP64
   torch ops so that autograd carries d L / d theta: eigh of the
-  rotating-frame one-exciton Hamiltonian, the Debye correlation function
+  rotating-frame one-exciton Hamiltonian (the Jacobi kernel with an
+  analytic backward), the Debye correlation function
   (bath.py:84-102, the reference's truncated Matsubara sum, with its
   derivative), and the operator-form Redfield tensor.
 * The RK4 time loop and its adjoint are hand-written kernels behind
@@ -67,21 +68,51 @@ class DebyeCorr(torch.autograd.Function):
         return gx, glam, None, None, None
 
 
+# --------------------------------------------------------------- eigensolve
+class SymmetricEigh(torch.autograd.Function):
+    """E, U of a batch of real symmetric matrices by the batched Jacobi
+    kernel (qsx_eigh_batched, FP64, n <= 32), with the analytic backward
+    gA = U (diag(gE) + F o (U^T gU)) U^T, F_ij = 1 / (E_j - E_i) (i != j),
+    symmetrised."""
+
+    @staticmethod
+    def forward(ctx, A):
+        A = A.detach().contiguous()
+        n = A.shape[-1]
+        E, U = _native.eigh(A, [0, n])
+        ctx.save_for_backward(E, U)
+        return E, U
+
+    @staticmethod
+    def backward(ctx, gE, gU):
+        E, U = ctx.saved_tensors
+        inner = torch.zeros_like(U)
+        if gU is not None:
+            diff = E[:, None, :] - E[:, :, None]          # E_j - E_i
+            F = torch.where(diff.abs() > 0, 1.0 / torch.where(diff == 0, 1.0, diff), 0.0)
+            inner = F * (U.transpose(1, 2) @ gU)
+        if gE is not None:
+            inner = inner + torch.diag_embed(gE)
+        gA = U @ inner @ U.transpose(1, 2)
+        return 0.5 * (gA + gA.transpose(1, 2))
+
+
 # --------------------------------------------------------------- generator
 def eg_heisenberg_generator(H1, lam, temperature, cutoff_freq, rw_freq, unit_convert,
-                            matsubara_cutoff=1000):
+                            matsubara_cutoff=1000, eigh=None):
     """Heisenberg-picture 'eg' Redfield generator L^T (S, N, N) complex128.
 
     H1 (S, N, N) float64 one-exciton Hamiltonians (not rotating).  In the
     site basis L_eg = -(G + i uc H) with H the rotating-frame Hamiltonian and
     G[a][b] = uc sum_{c,d} U[a][c]^2 C(E_d - E_c) U[a][d] U[b][d], the e block
     of sum_i diag(occ_i) U (Kt_i o C) U^T (redfield.py:41-104,
-    liouville_space.py:316-341).
+    liouville_space.py:316-341).  ``eigh`` defaults to the GPU Jacobi kernel
+    (SymmetricEigh); a caller working on host tensors passes its own.
     """
     N = H1.shape[-1]
     eye = torch.eye(N, dtype=torch.float64, device=H1.device)
     H = H1 - rw_freq * eye
-    E, U = torch.linalg.eigh(H)
+    E, U = (eigh or SymmetricEigh.apply)(H)
     x = E[:, None, :] - E[:, :, None]                 # x[c][d] = E_d - E_c
     C = DebyeCorr.apply(x, lam, temperature, cutoff_freq, matsubara_cutoff)
     Uc = U.to(torch.complex128)

@@ -49,7 +49,8 @@ def test_eg_generator_matches_dense_oracle_block():
     om = orc.RedfieldSpec(oham, bath, 'ge', orc.CM_FS, secular=False)
     LH = om.eom_matrix('eg', heisenberg_picture=True)
     L = eg_heisenberg_generator(torch.as_tensor(H1)[None], torch.tensor(35.0, dtype=torch.float64),
-                                orc.CM_K * 77, 106.0, oham.rw_freq, orc.CM_FS)
+                                orc.CM_K * 77, 106.0, oham.rw_freq, orc.CM_FS,
+                                eigh=torch.linalg.eigh)
     assert rel_err(L[0].numpy(), LH) < 1e-12
 
 

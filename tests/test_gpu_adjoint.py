@@ -110,3 +110,24 @@ def test_adjoint_checkpoint_validation():
     g = torch.ones(21, dtype=torch.complex128, device='cuda')
     with pytest.raises(_native.QsxError):
         _native.rk4_adjoint(D, ck, 4, 20, c, g, 0.5)  # 2 checkpoints x 4 < 20 steps
+
+
+def test_symmetric_eigh_backward_matches_torch():
+    """Jacobi eigensolver + analytic backward against torch.linalg.eigh on a
+    sign-invariant function of the eigenpairs."""
+    from qspectra_gb300.simulate.adjoint import SymmetricEigh
+    rng = np.random.RandomState(5)
+    A0 = rng.randn(6, 7, 7) * 40
+    A0 = A0 + A0.transpose(0, 2, 1)
+    wE = torch.as_tensor(rng.randn(6, 7)).cuda()
+    R = torch.as_tensor(rng.randn(6, 7, 7)).cuda()
+
+    def f(E, U):
+        return (E * wE).sum() + ((U * U) * R).sum()
+
+    A1 = torch.as_tensor(A0).cuda().requires_grad_(True)
+    f(*SymmetricEigh.apply(A1)).backward()
+    A2 = torch.as_tensor(A0).cuda().requires_grad_(True)
+    f(*torch.linalg.eigh(A2)).backward()
+    g2 = 0.5 * (A2.grad + A2.grad.transpose(1, 2))
+    assert rel_err(A1.grad.cpu().numpy(), g2.cpu().numpy()) < 1e-10
