@@ -182,8 +182,10 @@ typedef struct {
   size_t workspace_bytes;
   int32_t* status;        /* device int: set to QSX_ERR_NONFINITE on NaN/Inf */
   int32_t variant;        /* kernel variant, 0 = the planner's choice; with block_k:
-                             1 = one thread per matrix row, 2 = two lanes per row
-                             (an autotuner times both and passes the faster) */
+                             1 = one thread per matrix row, 2 / 4 = that many lanes
+                             per row, 3 / 5 = two rows per thread over two / four
+                             lanes (an autotuner times them and passes the
+                             fastest) */
   int32_t reserved;       /* must be 0 */
 } qsx_rk4_args;
 /* nsave = nsteps / save_every + 1; nout = nproj if nproj > 0 else nselect.

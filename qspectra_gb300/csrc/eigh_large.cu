@@ -21,6 +21,7 @@
 // rotations accumulated into Q).  Eigenvalues are returned ascending with
 // U[:, k] the k-th eigenvector.  Every loop is bounded: a QL that does not
 // converge in 60 sweeps per eigenvalue stops and reports QSX_ERR_NONFINITE.
+#include <algorithm>
 #include <cfloat>
 
 #include "qsx_common.cuh"
@@ -154,13 +155,15 @@ __global__ void __launch_bounds__(TQ_THREADS, 2)
   }
 }
 
-// ---- B. eigenvalues by implicit QL without vectors, one thread per matrix,
-// then sorted ascending into ws[b].
+// ---- B. eigenvalues by implicit QL without vectors, one thread per matrix
+// (the recurrence is serial), its diagonal and sub-diagonal in shared memory
+// (row stride 2n + 1 doubles), then sorted ascending into ws[b].
 __global__ void eigh_ql_kernel(const double* __restrict__ de, int n, int64_t batch,
-                               double* work, double* ws, int* status) {
+                               double* ws, int* status) {
+  extern __shared__ __align__(16) double qsm[];
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= batch) return;
-  double* dv = work + b * 2 * (int64_t)n;
+  double* dv = qsm + (int64_t)threadIdx.x * (2 * n + 1);
   double* ev = dv + n;
   const double* d0 = de + b * 2 * (int64_t)n;
   for (int i = 0; i < 2 * n; ++i) dv[i] = d0[i];
@@ -378,8 +381,7 @@ extern "C" int qsx_eigh_large_batched(const double* H, int n, int64_t batch, dou
   double* Z = W + nnb;
   double* scratch = Z + nnb;
   double* de = scratch + 5 * nnb;
-  double* work = de + 2 * (size_t)n * batch;
-  double* ws = work + 2 * (size_t)n * batch;
+  double* ws = de + 4 * (size_t)n * batch;
   const int threads = n >= TQ_THREADS ? TQ_THREADS : ((n + 31) / 32) * 32;
   const size_t smemA = ((size_t)2 * n + 32) * sizeof(double);
   const size_t smemD = (size_t)n * sizeof(double);
@@ -390,7 +392,15 @@ extern "C" int qsx_eigh_large_batched(const double* H, int n, int64_t batch, dou
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemD);
   if (e != cudaSuccess) return cuda_status(e, "qsx_eigh_large_batched");
   eigh_tridiag_kernel<<<(unsigned)batch, threads, smemA, s>>>(H, n, W, de);
-  eigh_ql_kernel<<<(unsigned)((batch + 63) / 64), 64, 0, s>>>(de, n, batch, work, ws, status);
+  const size_t per_thread = (2 * (size_t)n + 1) * sizeof(double);
+  int tpb = (int)std::min<size_t>(32, (200 * 1024) / per_thread);
+  tpb = std::max(tpb, 1);
+  const size_t smemB = per_thread * tpb;
+  e = cudaFuncSetAttribute(eigh_ql_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smemB);
+  if (e != cudaSuccess) return cuda_status(e, "qsx_eigh_large_batched");
+  eigh_ql_kernel<<<(unsigned)((batch + tpb - 1) / tpb), tpb, smemB, s>>>(de, n, batch, ws,
+                                                                          status);
   const int64_t nt = batch * n;
   eigh_invit_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(de, ws, n, batch, Z, scratch);
   eigh_backtransform_kernel<<<(unsigned)batch, threads, smemD, s>>>(W, ws, n, Z, E, U);

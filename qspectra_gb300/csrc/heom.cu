@@ -34,6 +34,17 @@ struct HeomP {
   const double2* alpha;  // [nnodes][nterms]
   const double2* beta;   // [nnodes][nterms]
   double uc, h;
+  // FP32 copies of the tables, made once per qsx_heom_rk4 call so the FP32
+  // stage kernel stages them without FP64 conversions (null for FP64)
+  const float* Hx32;
+  const float* Hy32;
+  const float* occx32;
+  const float* occy32;
+  const float* W32;
+  const float* shift32;
+  const float2* alpha32;
+  const float2* beta32;
+  float uc32, h32;
 };
 
 // Per-CTA tables in the working precision T (staged once so the element
@@ -88,22 +99,34 @@ __device__ __forceinline__ void heom_stage_smem(const HeomP& p, const typename c
                                                 int64_t b, int n0, int npc, HeomSmem<T>& s) {
   using C = typename cplx<T>::type;
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int i = tid; i < p.nx * p.nx; i += nt) s.Hx[i] = (T)p.Hx[b * p.Hx_stride + i];
-  for (int i = tid; i < p.ny * p.ny; i += nt) s.Hy[i] = (T)p.Hy[b * p.Hy_stride + i];
-  for (int i = tid; i < p.n_sites * p.nx; i += nt) s.ox[i] = (T)p.occx[i];
-  for (int i = tid; i < p.n_sites * p.ny; i += nt) s.oy[i] = (T)p.occy[i];
-  for (int i = tid; i < p.E; i += nt) s.W[i] = p.W ? (T)p.W[i] : (T)0;
   const int nn = (npc < p.nnodes - n0 ? npc : p.nnodes - n0);
-  for (int i = tid; i < npc; i += nt) s.shift[i] = i < nn ? (T)p.shift[n0 + i] : (T)0;
+  if constexpr (sizeof(T) == 4) {
+    for (int i = tid; i < p.nx * p.nx; i += nt) s.Hx[i] = p.Hx32[b * p.Hx_stride + i];
+    for (int i = tid; i < p.ny * p.ny; i += nt) s.Hy[i] = p.Hy32[b * p.Hy_stride + i];
+    for (int i = tid; i < p.n_sites * p.nx; i += nt) s.ox[i] = p.occx32[i];
+    for (int i = tid; i < p.n_sites * p.ny; i += nt) s.oy[i] = p.occy32[i];
+    for (int i = tid; i < p.E; i += nt) s.W[i] = p.W32 ? p.W32[i] : 0.f;
+    for (int i = tid; i < npc; i += nt) s.shift[i] = i < nn ? p.shift32[n0 + i] : 0.f;
+  } else {
+    for (int i = tid; i < p.nx * p.nx; i += nt) s.Hx[i] = p.Hx[b * p.Hx_stride + i];
+    for (int i = tid; i < p.ny * p.ny; i += nt) s.Hy[i] = p.Hy[b * p.Hy_stride + i];
+    for (int i = tid; i < p.n_sites * p.nx; i += nt) s.ox[i] = p.occx[i];
+    for (int i = tid; i < p.n_sites * p.ny; i += nt) s.oy[i] = p.occy[i];
+    for (int i = tid; i < p.E; i += nt) s.W[i] = p.W ? p.W[i] : 0.0;
+    for (int i = tid; i < npc; i += nt) s.shift[i] = i < nn ? p.shift[n0 + i] : 0.0;
+  }
   for (int i = tid; i < npc * p.nterms; i += nt) {
     const bool ok = i < nn * p.nterms;
     const int g = n0 * p.nterms + i;
     s.nbr[i] = ok ? p.nbr[g] : -1;
     s.site[i] = ok ? p.site[g] : 0;
-    const double2 a = ok ? p.alpha[g] : make_double2(0.0, 0.0);
-    const double2 c = ok ? p.beta[g] : make_double2(0.0, 0.0);
-    s.al[i] = cmk((T)a.x, (T)a.y);
-    s.be[i] = cmk((T)c.x, (T)c.y);
+    if constexpr (sizeof(T) == 4) {
+      s.al[i] = ok ? p.alpha32[g] : make_float2(0.f, 0.f);
+      s.be[i] = ok ? p.beta32[g] : make_float2(0.f, 0.f);
+    } else {
+      s.al[i] = ok ? p.alpha[g] : make_double2(0.0, 0.0);
+      s.be[i] = ok ? p.beta[g] : make_double2(0.0, 0.0);
+    }
   }
   const C* xb = x + (b * p.nnodes + n0) * (int64_t)p.E;
   for (int i = tid; i < nn * p.E; i += nt) s.x[i] = xb[i];
@@ -151,7 +174,11 @@ __device__ __forceinline__ void heom_rhs_elem(const HeomP& p, const typename cpl
     orr = fma(fr, v.x, fma(-fi, v.y, orr));
     oi = fma(fr, v.y, fma(fi, v.x, oi));
   }
-  const T uc = (T)p.uc;
+  T uc;
+  if constexpr (sizeof(T) == 4)
+    uc = p.uc32;
+  else
+    uc = p.uc;
   out.x = uc * orr;
   out.y = uc * oi;
 }
@@ -176,7 +203,11 @@ __global__ void __launch_bounds__(256)
   C k;
   heom_rhs_elem<T>(p, in, b, local, e, sm, k);
   const int64_t idx = (b * p.nnodes + node) * (int64_t)p.E + e;
-  const T h = (T)p.h;
+  T h;
+  if constexpr (sizeof(T) == 4)
+    h = p.h32;
+  else
+    h = p.h;
   if (stage == 0) {
     acc[idx] = k;
     const C y = yh[idx];
@@ -307,11 +338,43 @@ static HeomP heom_params(const qsx_heom_args* a) {
   p.beta = (const double2*)a->beta;
   p.uc = a->unit_convert;
   p.h = a->h;
+  p.uc32 = (float)a->unit_convert;
+  p.h32 = (float)a->h;
+  p.Hx32 = p.Hy32 = p.occx32 = p.occy32 = p.W32 = p.shift32 = nullptr;
+  p.alpha32 = p.beta32 = nullptr;
   return p;
 }
 
 static size_t heom_state_elems(const qsx_heom_args* a) {
   return (size_t)a->batch * a->nnodes * a->nx * a->ny;
+}
+
+__global__ void f64_to_f32_kernel(const double* __restrict__ src, float* __restrict__ dst,
+                                  int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+
+// element counts of the FP32 table copies: Hx, Hy, occx, occy, W, shift,
+// alpha and beta (the last two as floats, two per complex entry)
+static void heom_table_counts(const qsx_heom_args* a, int64_t c[8]) {
+  const int64_t hb = a->H_stride ? a->batch : 1;
+  c[0] = hb * a->nx * a->nx;
+  c[1] = hb * a->ny * a->ny;
+  c[2] = (int64_t)a->n_sites * a->nx;
+  c[3] = (int64_t)a->n_sites * a->ny;
+  c[4] = a->W ? (int64_t)a->nx * a->ny : 0;
+  c[5] = a->nnodes;
+  c[6] = 2 * (int64_t)a->nnodes * a->nterms;
+  c[7] = c[6];
+}
+
+static size_t heom_table_bytes(const qsx_heom_args* a) {
+  int64_t c[8];
+  heom_table_counts(a, c);
+  size_t b = 0;
+  for (int i = 0; i < 8; ++i) b += ((size_t)c[i] * sizeof(float) + 255) & ~(size_t)255;
+  return b;
 }
 
 }  // namespace qsx
@@ -333,7 +396,8 @@ int qsx_heom_workspace_bytes(const qsx_heom_args* a, size_t* bytes) {
   const size_t states = (a->precision == QSX_FP32 ? 5 : 4) * n * cs;
   const size_t saves =
       a->out_mean ? (size_t)a->batch * nsave * a->save_nodes * a->nx * a->ny * sizeof(double2) : 0;
-  *bytes = states + saves + 256;
+  const size_t tables = a->precision == QSX_FP32 ? heom_table_bytes(a) + 256 : 0;
+  *bytes = states + saves + 256 + tables;
   return QSX_OK;
 }
 
@@ -388,6 +452,34 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
     C* s1 = s0 + n;
     double2* saves = (double2*)(((size_t)(s1 + n) + 255) & ~(size_t)255);
     if (!node0) node0 = saves;
+    if constexpr (sizeof(T) == 4) {
+      // FP32 copies of the tables after the saves
+      const int nsave_ = p.nsave;
+      const size_t save_bytes =
+          a->out_mean ? (size_t)p.batch * nsave_ * keep * p.E * sizeof(double2) : 0;
+      unsigned char* tp =
+          (unsigned char*)((((size_t)saves + save_bytes) + 255) & ~(size_t)255);
+      int64_t c[8];
+      heom_table_counts(a, c);
+      const double* src[8] = {a->Hx, a->Hy, a->occx, a->occy, a->W, a->shift, a->alpha,
+                              a->beta};
+      float* dst[8];
+      for (int i = 0; i < 8; ++i) {
+        dst[i] = (float*)tp;
+        tp += ((size_t)c[i] * sizeof(float) + 255) & ~(size_t)255;
+        if (c[i] > 0 && src[i])
+          f64_to_f32_kernel<<<(unsigned)((c[i] + 255) / 256), 256, 0, s>>>(src[i], dst[i], c[i]);
+      }
+      QSX_LAUNCH_CHECK("qsx_heom_rk4 tables");
+      p.Hx32 = dst[0];
+      p.Hy32 = dst[1];
+      p.occx32 = dst[2];
+      p.occy32 = dst[3];
+      p.W32 = a->W ? dst[4] : nullptr;
+      p.shift32 = dst[5];
+      p.alpha32 = (const float2*)dst[6];
+      p.beta32 = (const float2*)dst[7];
+    }
     const size_t smem = heom_smem_bytes<T>(p.nx, p.ny, p.n_sites, p.E, npc, p.nterms);
     QSX_CHECK_ARG(smem <= 227 * 1024, "qsx_heom_rk4: node tables too large for shared memory");
     cudaError_t ce = cudaFuncSetAttribute(heom_stage_kernel<T>,

@@ -255,7 +255,11 @@ __global__ void __launch_bounds__(256)
   double* sU = (double*)(sT1 + nn);  // nn
   double* sUt = sU + nn;             // nn, U^T
   double* sKt = sUt + nn;            // nn
-  double* sE = sKt + nn;             // n (<= 32)
+  double* sE = sKt + nn;             // n (<= 32), then 32 coupling weights of eigenvectors
+  // occupied states of each site (occ != 0), found once per CTA so the
+  // element loops below issue no FP64 compares
+  int* sOccN = (int*)(sE + 64);      // [n_sites]
+  int* sOccS = sOccN + 32;           // [n_sites][n] state indices
   const int64_t b = blockIdx.x;
   const double* u = U + b * nn;
   for (int e = threadIdx.x; e < nn; e += blockDim.x) {
@@ -265,22 +269,34 @@ __global__ void __launch_bounds__(256)
     sUt[c * n + r] = v;
     sGS[e] = cmk(0.0, 0.0);
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    sE[i] = E[b * n + i];
-    double w = 0.0;  // total bath coupling weight of site-basis state i
-    for (int k = 0; k < n_sites; ++k) w += occ[k * n + i];
-    sE[32 + i] = w;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sE[i] = E[b * n + i];
+  for (int i = threadIdx.x; i < n_sites; i += blockDim.x) {
+    int cnt = 0;
+    for (int st = 0; st < n; ++st)
+      if (occ[i * n + st] != 0.0) sOccS[i * n + cnt++] = st;
+    sOccN[i] = cnt;
   }
   __syncthreads();
-  // correlation function only where some Kt_i[c][d] can be non-zero; the
-  // pair (c, d), (d, c) shares one Matsubara evaluation (C(E_d - E_c) and
-  // C(E_c - E_d)), computed by the thread with c <= d.
+  // coupling weight of eigenvector c: sum_s U[s][c]^2 (sum_i occ_i(s)^2)
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    double wsum = 0.0;
+    for (int i = 0; i < n_sites; ++i)
+      for (int k = 0; k < sOccN[i]; ++k) {
+        const int st = sOccS[i * n + k];
+        const double o = occ[i * n + st], x = sU[st * n + c];
+        wsum = fma(o * o, x * x, wsum);
+      }
+    sE[32 + c] = wsum;
+  }
+  __syncthreads();
+  // correlation function only for pairs of bath-coupled eigenvectors (any
+  // Kt_i[c][d] vanishes otherwise); the pair (c, d), (d, c) shares one
+  // Matsubara evaluation (C(E_d - E_c) and C(E_c - E_d)), computed by the
+  // thread with c <= d.
   for (int e = threadIdx.x; e < nn; e += blockDim.x) {
     int c = e / n, d = e % n;
     if (c > d) continue;
-    double need = 0.0;
-    for (int s = 0; s < n; ++s) need += fabs(sU[s * n + c] * sU[s * n + d]) * sE[32 + s];
-    if (need > 0.0) {
+    if (sE[32 + c] > 0.0 && sE[32 + d] > 0.0) {
       double2 cp, cn;
       debye_corr_pair(bath, sE[d] - sE[c], cp, cn);
       sC[e] = cp;
@@ -293,12 +309,14 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   for (int i = 0; i < n_sites; ++i) {
     const double* oc = occ + i * n;
+    const int cnt = sOccN[i];
+    const int* ost = sOccS + i * n;
     for (int e = threadIdx.x; e < nn; e += blockDim.x) {
       int c = e / n, d = e % n;
       double acc = 0.0;
-      for (int s = 0; s < n; ++s) {
-        double o = oc[s];
-        if (o != 0.0) acc = fma(sU[s * n + c] * o, sU[s * n + d], acc);
+      for (int k = 0; k < cnt; ++k) {
+        const int st = ost[k];
+        acc = fma(sU[st * n + c] * oc[st], sU[st * n + d], acc);
       }
       sKt[e] = acc;
       double2 cw = sC[e];
@@ -312,10 +330,12 @@ __global__ void __launch_bounds__(256)
       smem_matmul_crT(sT1, sU, sMt, n);        // Mt_i <- T1 U^T (site basis)
       __syncthreads();
       // G_site = sum_i diag(occ_i) M_i: row s of G gathers row s of every M_i
-      for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-        Mi[e] = cscale(sMt[e], uc);
-        const double o = oc[e / n];
-        if (o != 0.0) sGS[e] = cadd(sGS[e], cscale(sMt[e], o));
+      for (int e = threadIdx.x; e < nn; e += blockDim.x) Mi[e] = cscale(sMt[e], uc);
+      for (int k = 0; k < cnt; ++k) {
+        const int st = ost[k];
+        const double o = oc[st];
+        for (int c = threadIdx.x; c < n; c += blockDim.x)
+          sGS[st * n + c] = cadd(sGS[st * n + c], cscale(sMt[st * n + c], o));
       }
     } else {
       smem_matmul_rc(sKt, sMt, sGS, n, true);  // GS += Kt_i Mt_i (eigenbasis)
@@ -743,7 +763,8 @@ int qsx_redfield_operators_batched(const double* E, const double* U, int n,
   DebyeParams p = make_debye(temperature, reorg_energy, cutoff_freq, matsubara_cutoff,
                              discard_imag_corr);
   const size_t nn = (size_t)n * n;
-  const size_t smem = (3 * nn + 64) * sizeof(double) + 4 * nn * sizeof(double2);
+  const size_t smem = (3 * nn + 64) * sizeof(double) + 4 * nn * sizeof(double2) +
+                      (32 + (size_t)n_sites * n) * sizeof(int);
   cudaError_t e = cudaFuncSetAttribute(redfield_operators_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);

@@ -532,6 +532,170 @@ __global__ void __launch_bounds__(448, 2) rk4_block2_f32(Rk4P p, int64_t ngroups
   }
 }
 
+// rk4_block3_f32<M, LPR>: the K-step blocked loop with each thread holding
+// TWO rows over 1/LPR of the columns (lanes l, l ^ 8, l ^ 16, ... split the
+// columns): every state value read from shared memory feeds two rows,
+// halving the shared-memory traffic per FMA of rk4_block_f32, with
+// log2(LPR) shuffles to combine.  Row pairs of a sample fill whole warps
+// (32 / LPR pairs per warp), G samples per CTA.
+template <int M, int LPR>
+__global__ void __launch_bounds__(256, 2) rk4_block3_f32(Rk4P p, int64_t ngroups, int G, int K) {
+  constexpr int ST = rows_stride(M);
+  constexpr int MP = (M % 2) ? M + 1 : M;
+  constexpr int NPAIR = MP / 2;
+  constexpr int HP = (NPAIR + LPR - 1) / LPR;  // column pairs per lane
+  constexpr int RPW = 32 / LPR;                // row pairs per warp
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2* ybuf = (float2*)smraw;             // [2][G][ST]
+  float2* stash = ybuf + 2 * G * ST;         // [2][K][G][nsel]
+  const int nsel = p.nselect;
+  const int RT = M + nsel * (K - 1);
+  const int NRP = (RT + 1) / 2;              // row pairs per sample
+  const int wps = (NRP + RPW - 1) / RPW;     // warps per sample
+  const int tid = threadIdx.x, lane = tid & 31, wi = tid >> 5;
+  const int g = wi / wps;
+  const int rp = (wi % wps) * RPW + (lane % RPW);
+  const int part = lane / RPW;
+  const int gs = g < G ? g : 0;
+  int r2[2];
+  bool act[2], mrow[2];
+  int kx[2], qx[2], myq[2], selr[2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int r = 2 * rp + u;
+    r2[u] = r;
+    act[u] = g < G && rp < NRP && r < RT;
+    mrow[u] = act[u] && r < M;
+    kx[u] = mrow[u] ? K : (act[u] ? (r - M) / nsel + 1 : 0);
+    qx[u] = (act[u] && !mrow[u]) ? (r - M) % nsel : -1;
+    myq[u] = -1;
+    if (mrow[u])
+      for (int q = 0; q < nsel; ++q)
+        if (p.select[q] == r) { myq[u] = q; break; }
+    selr[u] = (act[u] && !mrow[u]) ? p.select[qx[u]] : 0;
+  }
+  for (int e = tid; e < 2 * G * ST; e += blockDim.x) ybuf[e] = make_float2(0.f, 0.f);
+  __syncthreads();
+  auto stash_at = [&](int par, int k, int gg, int q) -> float2& {
+    return stash[((par * K + k) * G + gg) * nsel + q];
+  };
+  int parity = 0;
+  for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const int64_t s = grp * G + gs;
+    const bool svalid = g < G && s < p.batch;
+    float2 drow[2][2 * HP];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const bool v = svalid && act[u];
+      const float2* dm = (const float2*)p.matrix + (v ? s * p.matrix_stride + (int64_t)r2[u] * M : 0);
+#pragma unroll
+      for (int t = 0; t < 2 * HP; ++t) {
+        const int j = part * 2 * HP + t;
+        drow[u][t] = (v && j < M) ? dm[j] : make_float2(0.f, 0.f);
+      }
+    }
+    float yhx[2] = {0.f, 0.f}, yhy[2] = {0.f, 0.f}, ylx[2] = {0.f, 0.f}, yly[2] = {0.f, 0.f};
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (svalid && mrow[u]) {
+        double2 v = p.y0[s * p.y0_stride + r2[u]];
+        yhx[u] = (float)v.x;
+        yhy[u] = (float)v.y;
+        ylx[u] = (float)(v.x - (double)yhx[u]);
+        yly[u] = (float)(v.y - (double)yhy[u]);
+      }
+      if (mrow[u] && part == 0) ybuf[g * ST + r2[u]] = make_float2(yhx[u], yhy[u]);
+      if (myq[u] >= 0 && part == 0) {
+        stash_at(parity, 0, g, myq[u]) = make_float2(yhx[u], yhy[u]);
+        if (p.out_proj && svalid)
+          p.out_proj[(s * p.nsave) * p.nout + myq[u]] =
+              make_double2((double)yhx[u] + (double)ylx[u], (double)yhy[u] + (double)yly[u]);
+      }
+    }
+    __syncthreads();
+    if (p.partial)
+      for (int q = tid; q < nsel; q += blockDim.x) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int gg = 0; gg < G; ++gg) acc = cadd2(acc, stash_at(parity, 0, gg, q));
+        double2* dst = p.partial + ((int64_t)blockIdx.x * p.nsave) * p.nout + q;
+        atomicAdd(&dst->x, (double)acc.x);
+        atomicAdd(&dst->y, (double)acc.y);
+      }
+    parity ^= 1;
+    const int nblk = p.nsteps / K;
+    for (int bs = 0; bs < nblk; ++bs) {
+      const float2* cur = ybuf + ((bs & 1) * G + gs) * ST;
+      float2 a0[2], a1[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) a0[u] = a1[u] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int t = 0; t < HP; ++t) {
+        const int pr = part * HP + t;
+        if (pr < NPAIR) {
+          const float4 v = *reinterpret_cast<const float4*>(&cur[2 * pr]);
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            cfma(a0[u], drow[u][2 * t], make_float2(v.x, v.y));
+            cfma(a1[u], drow[u][2 * t + 1], make_float2(v.z, v.w));
+          }
+        }
+      }
+      const int step0 = bs * K;
+      float sx[2], sy[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        sx[u] = a0[u].x + a1[u].x;
+        sy[u] = a0[u].y + a1[u].y;
+#pragma unroll
+        for (int o = 16; o >= RPW; o >>= 1) {
+          sx[u] += __shfl_xor_sync(0xffffffffu, sx[u], o);
+          sy[u] += __shfl_xor_sync(0xffffffffu, sy[u], o);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (part != 0 || !act[u]) continue;
+        if (mrow[u]) {
+          dd_add(yhx[u], ylx[u], sx[u]);
+          dd_add(yhy[u], yly[u], sy[u]);
+          ybuf[(((bs + 1) & 1) * G + g) * ST + r2[u]] = make_float2(yhx[u], yhy[u]);
+          if (myq[u] >= 0) {
+            stash_at(parity, K - 1, g, myq[u]) =
+                svalid ? make_float2(yhx[u], yhy[u]) : make_float2(0.f, 0.f);
+            if (p.out_proj && svalid)
+              p.out_proj[(s * p.nsave + step0 + K) * p.nout + myq[u]] = make_double2(
+                  (double)yhx[u] + (double)ylx[u], (double)yhy[u] + (double)yly[u]);
+          }
+        } else {
+          const float2 base = cur[selr[u]];
+          const float2 v = svalid ? make_float2(base.x + sx[u], base.y + sy[u])
+                                  : make_float2(0.f, 0.f);
+          stash_at(parity, kx[u] - 1, g, qx[u]) = v;
+          if (p.out_proj && svalid)
+            p.out_proj[(s * p.nsave + step0 + kx[u]) * p.nout + qx[u]] = make_double2(v.x, v.y);
+        }
+      }
+      __syncthreads();
+      if (p.partial)
+        for (int e = tid; e < K * nsel; e += blockDim.x) {
+          const int k = e / nsel, q = e % nsel;
+          float2 acc = make_float2(0.f, 0.f);
+          for (int gg = 0; gg < G; ++gg) acc = cadd2(acc, stash_at(parity, k, gg, q));
+          double2* dst = p.partial + ((int64_t)blockIdx.x * p.nsave + step0 + k + 1) * p.nout + q;
+          atomicAdd(&dst->x, (double)acc.x);
+          atomicAdd(&dst->y, (double)acc.y);
+        }
+      parity ^= 1;
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      if (svalid && mrow[u] && part == 0 && p.status &&
+          !(isfinite(yhx[u]) && isfinite(yhy[u])))
+        atomicOr(p.status, QSX_ERR_NONFINITE);
+    __syncthreads();
+  }
+}
+
 // -------------------------------------------------------------- generic
 constexpr int GEN_MAXR = 4;  // rows per thread (M <= 4 * 1024)
 
@@ -795,12 +959,19 @@ static int make_plan(const qsx_rk4_args* a, Plan* pl) {
                   "nsteps %% block_k == 0 and m in {9,16,25,36,49,64}");
     const int RT = m + a->nselect * (K - 1);
     QSX_CHECK_ARG(RT <= 256, "qsx_rk4: block_k rows per sample exceed 256");
-    QSX_CHECK_ARG(a->variant >= 0 && a->variant <= 4, "qsx_rk4: variant must be 0, 1, 2 or 4");
-    // lanes per row: the planner's default, or the variant an autotuner picked
-    QSX_CHECK_ARG(a->variant != 3, "qsx_rk4: variant must be 0, 1, 2 or 4");
+    QSX_CHECK_ARG(a->variant >= 0, "qsx_rk4: variant must be 0..5");
+    // the planner's default, or the variant an autotuner picked: 1 = one
+    // thread per row, 2 / 4 = that many lanes per row, 3 / 5 = two rows per
+    // thread over two / four lanes
+    QSX_CHECK_ARG(a->variant <= 5, "qsx_rk4: variant must be 0..5");
     const int lpr = a->variant ? a->variant : 1;
     int threads;
-    if (lpr > 1) {
+    if (lpr == 3 || lpr == 5) {
+      const int rpw = lpr == 3 ? 16 : 8;  // row pairs per warp
+      const int wps = ((RT + 1) / 2 + rpw - 1) / rpw;
+      G = std::max(1, 256 / (wps * 32));
+      threads = G * wps * 32;
+    } else if (lpr > 1) {
       const int wps = (RT + 32 / lpr - 1) / (32 / lpr);
       G = std::max(1, 448 / (wps * 32));
       threads = G * wps * 32;
@@ -814,7 +985,11 @@ static int make_plan(const qsx_rk4_args* a, Plan* pl) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 #define X(MM, GG, BB)                                                                      \
   if (e == cudaSuccess && m == MM)                                                         \
-    e = lpr == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                          \
+    e = lpr == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                          \
+                       &occ, rk4_block3_f32<MM, 2>, threads, pl->smem)                     \
+        : lpr == 5 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                          \
+                       &occ, rk4_block3_f32<MM, 4>, threads, pl->smem)                     \
+        : lpr == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                          \
                        &occ, rk4_block2_f32<MM, 4>, threads, pl->smem)                     \
         : lpr == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                          \
                        &occ, rk4_block2_f32<MM, 2>, threads, pl->smem)                     \
@@ -968,7 +1143,13 @@ int qsx_rk4_batched(const qsx_rk4_args* a, void* stream) {
     case K_BLOCK: {
 #define X(MM, GG, BB)                                                                   \
   if (a->m == MM)                                                                       \
-    if (pl.lpr == 4)                                                                    \
+    if (pl.lpr == 3)                                                                    \
+      rk4_block3_f32<MM, 2><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(             \
+          p, pl.ngroups, pl.G, a->block_k);                                             \
+    else if (pl.lpr == 5)                                                               \
+      rk4_block3_f32<MM, 4><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(             \
+          p, pl.ngroups, pl.G, a->block_k);                                             \
+    else if (pl.lpr == 4)                                                               \
       rk4_block2_f32<MM, 4><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(             \
           p, pl.ngroups, pl.G, a->block_k);                                             \
     else if (pl.lpr == 2)                                                               \
@@ -1106,7 +1287,13 @@ extern "C" int qsx_rk4_block_mean_noalloc(const qsx_rk4_args* a, void* stream) {
   p.status = a->status;
 #define X(MM, GG, BB)                                                                    \
   if (a->m == MM) {                                                                      \
-    if (pl.lpr == 4)                                                                     \
+    if (pl.lpr == 3)                                                                     \
+      rk4_block3_f32<MM, 2><<<(unsigned)grid, pl.threads, pl.smem, s>>>(p, pl.ngroups,     \
+                                                                        pl.G, a->block_k); \
+    else if (pl.lpr == 5)                                                                \
+      rk4_block3_f32<MM, 4><<<(unsigned)grid, pl.threads, pl.smem, s>>>(p, pl.ngroups,     \
+                                                                        pl.G, a->block_k); \
+    else if (pl.lpr == 4)                                                                \
       rk4_block2_f32<MM, 4><<<(unsigned)grid, pl.threads, pl.smem, s>>>(p, pl.ngroups,    \
                                                                         pl.G, a->block_k); \
     else if (pl.lpr == 2)                                                                \

@@ -110,7 +110,7 @@ def test_fused_redfield_propagator_matches_two_step_path(golden):
             assert rel_err(fused, ref) < tol
 
 
-@pytest.mark.parametrize('variant', [0, 1, 2, 4])
+@pytest.mark.parametrize('variant', [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize('M,B,K,nsteps', [(9, 13, 3, 30), (49, 11, 9, 54), (25, 7, 4, 40),
                                           (64, 5, 2, 10), (36, 40, 9, 27), (16, 33, 5, 25)])
 def test_block_k_matches_step_by_step(M, B, K, nsteps, variant):
