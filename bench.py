@@ -518,8 +518,12 @@ def our_arm(args):
         'e2e': {'value': world * 1000.0 / e2e_ms, 'unit': UNIT,
                 'h2d_bytes_per_step': int(off_host.numel() * 8),
                 'd2h_bytes_per_step': int((nf + Ph.size + 1) * 8)},
-        'roofline': {'kernel': 'rk4_block_f32<49> (ee populations, K={} step blocking)'.format(
-                         events['dyn_block_k']),
+        'roofline': {'kernel': '{} (ee populations, K={} step blocking, autotuned variant {})'.format(
+                         {1: 'rk4_block_f32<49>', 2: 'rk4_block2_f32<49,2>',
+                          3: 'rk4_block3_f32<49,2>', 4: 'rk4_block2_f32<49,4>',
+                          5: 'rk4_block3_f32<49,4>'}.get(events.get('dyn_variant', 1),
+                                                         'rk4_block_f32<49>'),
+                         events['dyn_block_k'], events.get('dyn_variant', 1)),
                      'dense_step_equivalent_tflops': dense_equiv / (dyn_ms * 1e-3) / 1e12,
                      'bound': 'fp32_fma', 'achieved': achieved, 'peak': peak,
                      'unit': 'TFLOP/s', 'frac': achieved / peak,

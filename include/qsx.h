@@ -277,11 +277,12 @@ size_t qsx_heom_args_bytes(void);
 /*
  * Batched FP64 symmetric eigensolver for n up to 2048 (the two-exciton
  * block; the reference calls scipy.linalg.eigh per sample,
- * qspectra/hamiltonian.py:310-328): Householder tridiagonalisation, then
- * implicit QL, one CTA per matrix.  H float64 [batch][n][n] symmetric;
+ * qspectra/hamiltonian.py:310-328): Householder tridiagonalisation (one CTA
+ * per matrix), bisection on Sturm counts and inverse iteration (one thread
+ * per eigenvalue), back-transform by the reflectors.  H float64 [batch][n][n] symmetric;
  * E float64 [batch][n] ascending; U float64 [batch][n][n], column k the
  * eigenvector of E[k].  Workspace: qsx_eigh_large_workspace_bytes.
- * status: QSX_ERR_NONFINITE when a QL iteration fails to converge.
+ * status: QSX_ERR_NONFINITE when an eigenvalue comes out non-finite.
  */
 size_t qsx_eigh_large_workspace_bytes(int n, int64_t batch);
 int qsx_eigh_large_batched(const double* H, int n, int64_t batch, double* E,

@@ -629,5 +629,5 @@ def eigh_large(H):
     _check(lib.qsx_eigh_large_batched(_p(H), n, B, _p(E), _p(U), _p(ws), ws.numel(),
                                       _p(status), _stream()), 'qsx_eigh_large_batched')
     if int(status.item()):
-        raise QsxError('qsx_eigh_large_batched: QL iteration did not converge')
+        raise QsxError('qsx_eigh_large_batched: non-finite eigenvalue (non-finite input?)')
     return E, U

@@ -8,8 +8,8 @@
 //      A = Q T Q^T: for each
 //      column k, v with (I - tau v v^T) x = alpha e_1 and the two-sided
 //      update B <- B - v w^T - w v^T, w = p - (tau/2)(v^T p) v, p = tau B v.
-//   2. Eigenvalues of T by implicit QL with Wilkinson-type shifts, without
-//      vectors (one thread per matrix; O(n^2)).
+//   2. Eigenvalues of T by bisection on Sturm counts (one thread per
+//      eigenvalue of every matrix; O(n) per count, about 50 counts).
 //   3. Eigenvectors of T by inverse iteration (one thread per eigenvalue of
 //      every matrix): LU with partial pivoting of
 //      T - lambda I, three solves from a vector of ones; eigenvalues closer
@@ -19,8 +19,8 @@
 //      (one CTA per matrix).
 // This keeps the FP64 work near 2 n^3 multiply-adds per matrix (no Givens
 // rotations accumulated into Q).  Eigenvalues are returned ascending with
-// U[:, k] the k-th eigenvector.  Every loop is bounded: a QL that does not
-// converge in 60 sweeps per eigenvalue stops and reports QSX_ERR_NONFINITE.
+// U[:, k] the k-th eigenvector.  Every loop is bounded (bisection stops after
+// 128 halvings, inverse iteration runs three solves).
 #include <algorithm>
 #include <cfloat>
 
@@ -155,75 +155,53 @@ __global__ void __launch_bounds__(TQ_THREADS, 2)
   }
 }
 
-// ---- B. eigenvalues by implicit QL without vectors, one thread per matrix
-// (the recurrence is serial), its diagonal and sub-diagonal in shared memory
-// (row stride 2n + 1 doubles), then sorted ascending into ws[b].
-__global__ void eigh_ql_kernel(const double* __restrict__ de, int n, int64_t batch,
-                               double* ws, int* status) {
-  extern __shared__ __align__(16) double qsm[];
-  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= batch) return;
-  double* dv = qsm + (int64_t)threadIdx.x * (2 * n + 1);
-  double* ev = dv + n;
-  const double* d0 = de + b * 2 * (int64_t)n;
-  for (int i = 0; i < 2 * n; ++i) dv[i] = d0[i];
-  int bad = 0;
-  for (int l = 0; l < n; ++l) {
-    for (int iter = 0;; ++iter) {
-      int m = l;
-      for (; m < n - 1; ++m) {
-        const double dd = fabs(dv[m]) + fabs(dv[m + 1]);
-        if (fabs(ev[m]) <= DBL_EPSILON * dd) break;
-      }
-      if (m == l) break;
-      if (iter >= 60) {
-        bad = 1;
-        break;
-      }
-      double g = (dv[l + 1] - dv[l]) / (2.0 * ev[l]);
-      double r = hypot(g, 1.0);
-      g = dv[m] - dv[l] + ev[l] / (g + copysign(r, g));
-      double s = 1.0, c = 1.0, p = 0.0;
-      bool split = false;
-      for (int i = m - 1; i >= l; --i) {
-        const double f = s * ev[i], bb = c * ev[i];
-        const double rr = fma(f, f, g * g);
-        if (rr == 0.0) {
-          dv[i + 1] -= p;
-          ev[m] = 0.0;
-          split = true;
-          break;
-        }
-        const double rinv = rsqrt(rr);
-        r = rr * rinv;
-        ev[i + 1] = r;
-        s = f * rinv;
-        c = g * rinv;
-        g = dv[i + 1] - p;
-        r = (dv[i] - g) * s + 2.0 * c * bb;
-        p = s * r;
-        dv[i + 1] = g + p;
-        g = c * r - bb;
-      }
-      if (!split) {
-        dv[l] -= p;
-        ev[l] = g;
-        ev[m] = 0.0;
-      }
-    }
-  }
-  if (bad && status) atomicOr(status, QSX_ERR_NONFINITE);
-  // insertion sort (n <= 2048, once per matrix)
-  double* w = ws + b * (int64_t)n;
+// ---- B. eigenvalues by bisection on Sturm counts, one thread per
+// eigenvalue of every matrix (FP64 instructions of a serial recurrence are
+// slow on this part; these threads fill whole warps).  Eigenvalue j is the
+// point where the count of eigenvalues below x steps from j to j + 1; the
+// LDL^T recurrence q_i = (d_i - x) - e_{i-1}^2 / q_{i-1} counts negative
+// pivots, with |q| kept above pivmin = eps |T|.  Results land sorted in ws.
+__global__ void eigh_bisect_kernel(const double* __restrict__ de, int n, int64_t batch,
+                                   double* ws, int* status) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= batch * n) return;
+  const int64_t b = t / n;
+  const int j = (int)(t % n);
+  const double* d = de + b * 2 * (int64_t)n;
+  const double* e = d + n;
+  // Gershgorin interval and |T|
+  double lo = d[0], hi = d[0], tnorm = 0.0;
   for (int i = 0; i < n; ++i) {
-    const double x = dv[i];
-    int j = i;
-    while (j > 0 && w[j - 1] > x) {
-      w[j] = w[j - 1];
-      --j;
-    }
-    w[j] = x;
+    const double r = (i ? fabs(e[i - 1]) : 0.0) + fabs(e[i]);
+    lo = fmin(lo, d[i] - r);
+    hi = fmax(hi, d[i] + r);
+    tnorm = fmax(tnorm, fabs(d[i]) + r);
   }
+  const double pivmin = DBL_EPSILON * fmax(tnorm, DBL_MIN);
+  lo -= 2.0 * pivmin;
+  hi += 2.0 * pivmin;
+  for (int it = 0; it < 128; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + pivmin || mid <= lo ||
+        mid >= hi)
+      break;
+    int cnt = 0;
+    double q = d[0] - mid;
+    if (fabs(q) < pivmin) q = -pivmin;
+    cnt += q < 0.0;
+    for (int i = 1; i < n; ++i) {
+      q = (d[i] - mid) - e[i - 1] * e[i - 1] * __drcp_rn(q);
+      if (fabs(q) < pivmin) q = -pivmin;
+      cnt += q < 0.0;
+    }
+    if (cnt > j)
+      hi = mid;
+    else
+      lo = mid;
+  }
+  const double lam = 0.5 * (lo + hi);
+  if (!isfinite(lam) && status) atomicOr(status, QSX_ERR_NONFINITE);
+  ws[b * n + j] = lam;
 }
 
 // ---- C. eigenvectors of T by inverse iteration, one thread per eigenvalue
@@ -392,16 +370,8 @@ extern "C" int qsx_eigh_large_batched(const double* H, int n, int64_t batch, dou
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemD);
   if (e != cudaSuccess) return cuda_status(e, "qsx_eigh_large_batched");
   eigh_tridiag_kernel<<<(unsigned)batch, threads, smemA, s>>>(H, n, W, de);
-  const size_t per_thread = (2 * (size_t)n + 1) * sizeof(double);
-  int tpb = (int)std::min<size_t>(32, (200 * 1024) / per_thread);
-  tpb = std::max(tpb, 1);
-  const size_t smemB = per_thread * tpb;
-  e = cudaFuncSetAttribute(eigh_ql_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smemB);
-  if (e != cudaSuccess) return cuda_status(e, "qsx_eigh_large_batched");
-  eigh_ql_kernel<<<(unsigned)((batch + tpb - 1) / tpb), tpb, smemB, s>>>(de, n, batch, ws,
-                                                                          status);
   const int64_t nt = batch * n;
+  eigh_bisect_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(de, n, batch, ws, status);
   eigh_invit_kernel<<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(de, ws, n, batch, Z, scratch);
   eigh_backtransform_kernel<<<(unsigned)batch, threads, smemD, s>>>(W, ws, n, Z, E, U);
   QSX_LAUNCH_CHECK("qsx_eigh_large_batched");

@@ -68,6 +68,41 @@ def pick_block_k(nsteps, m, nselect, max_k=9):
     return 1
 
 
+# Autotuned time-loop variants (qsx_rk4_args.variant) per (m, K, selected
+# components, batch-size octave): each candidate is timed once on the first
+# call's own inputs and the fastest is kept for the process.
+BLOCK_VARIANTS = (1, 2, 5)
+_TUNED = {}
+_PINNED = None
+
+
+def set_block_variant(variant=None):
+    """Pin the blocked time-loop variant (1..5), or None to autotune."""
+    global _PINNED
+    _PINNED = variant
+
+
+def tuned_block_variant(mat, y0, nsteps, select, K):
+    if _PINNED is not None:
+        return _PINNED
+    key = (int(mat.shape[-1]), int(K), len(select), int(np.log2(max(int(mat.shape[0]), 1))))
+    if key not in _TUNED:
+        best, best_ms = 1, None
+        for v in BLOCK_VARIANTS:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _native.rk4(mat, y0, nsteps, 1, select=select, per_sample=False, mean=True,
+                        check_finite=False, block_k=K, variant=v)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            if best_ms is None or ms < best_ms:
+                best, best_ms = v, ms
+        _TUNED[key] = best
+    return _TUNED[key]
+
+
 def propagate_selected_mean(D, y0, nsteps, select, precision, events=None):
     """Ensemble mean of the selected components at every step (GPU).
 
@@ -79,11 +114,12 @@ def propagate_selected_mean(D, y0, nsteps, select, precision, events=None):
     B, m = D.shape[0], D.shape[-1]
     mat = _native.rk4_block_matrix(D, K, select) if K > 1 else D
     rows = mat.shape[-2]
+    variant = tuned_block_variant(mat, y0, nsteps, select, K) if K > 1 else 0
     if events is not None:
         e0 = torch.cuda.Event(enable_timing=True)
         e0.record()
     out = _native.rk4(mat, y0, nsteps, 1, select=select, per_sample=False, mean=True,
-                      check_finite=False, block_k=K if K > 1 else 0)
+                      check_finite=False, block_k=K if K > 1 else 0, variant=variant)
     if events is not None:
         e1 = torch.cuda.Event(enable_timing=True)
         e1.record()
@@ -91,6 +127,7 @@ def propagate_selected_mean(D, y0, nsteps, select, precision, events=None):
         # complex multiply-adds of the executed form, 8 real flops each
         events['dyn_flops'] = 8.0 * B * (nsteps // K) * rows * m
         events['dyn_block_k'] = K
+        events['dyn_variant'] = variant
     return out
 
 
