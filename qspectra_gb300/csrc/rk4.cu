@@ -979,6 +979,13 @@ static int make_plan(const qsx_rk4_args* a, Plan* pl) {
       G = std::max(1, 256 / RT);
       threads = ((G * RT + 31) / 32) * 32;
     }
+    // each variant is compiled for a maximum block size
+    const int max_threads = (lpr == 2 || lpr == 4) ? 448 : 256;
+    if (threads > max_threads) {
+      set_error("qsx_rk4: variant %d needs %d threads for %d blocked rows (at most %d)", lpr,
+                threads, RT, max_threads);
+      return QSX_ERR_UNSUPPORTED;
+    }
     int dev = 0, sms = 0, occ = 0;
     pl->smem = (2 * (size_t)G * 66 + 2 * (size_t)K * G * a->nselect) * sizeof(float2);
     cudaError_t e = cudaGetDevice(&dev);

@@ -92,8 +92,11 @@ def tuned_block_variant(mat, y0, nsteps, select, K):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
-            _native.rk4(mat, y0, nsteps, 1, select=select, per_sample=False, mean=True,
-                        check_finite=False, block_k=K, variant=v)
+            try:
+                _native.rk4(mat, y0, nsteps, 1, select=select, per_sample=False, mean=True,
+                            check_finite=False, block_k=K, variant=v)
+            except _native.QsxError:
+                continue  # a variant this shape cannot launch is never chosen
             e1.record()
             e1.synchronize()
             ms = e0.elapsed_time(e1)
@@ -267,14 +270,28 @@ class RedfieldEnsembleWorkload:
         H = self.H_base.expand(S, -1, -1).clone()
         H[:, self.e_idx, self.e_idx] += offsets
         build = self.model.build_batch(H)
-        D_eg = build.propagator(self.idx_eg, self.dt, prec, transpose=True)
-        sig = _native.rk4(D_eg, self.y_abs, len(self.t_abs) - 1, 1, proj=self.proj,
-                          per_sample=False, mean=True, check_finite=False)
-        X = _native.dft(-sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
-                        self.model.rw_freq, self.model.unit_convert, 1)
+        # the absorption leg (eg propagator, time loop, DFT) runs on a side
+        # stream, overlapping the population leg on the caller's stream
+        main = torch.cuda.current_stream()
+        if getattr(self, '_side', None) is None:
+            self._side = torch.cuda.Stream()
+        ready = torch.cuda.Event()
+        ready.record(main)
+        with torch.cuda.stream(self._side):
+            self._side.wait_event(ready)
+            D_eg = build.propagator(self.idx_eg, self.dt, prec, transpose=True)
+            sig = _native.rk4(D_eg, self.y_abs, len(self.t_abs) - 1, 1, proj=self.proj,
+                              per_sample=False, mean=True, check_finite=False)
+            X = _native.dft(-sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
+                            self.model.rw_freq, self.model.unit_convert, 1)
         D_ee = build.propagator(self.idx_ee, self.dt, prec)
         pop = propagate_selected_mean(D_ee, self.y_dyn, len(self.t_dyn) - 1, self.select,
                                       prec, events)
+        main.wait_stream(self._side)
+        for t in (X, sig['status']):
+            t.record_stream(main)
+        for t in (build.G, build.M, build.E, build.U, build.occ, H):
+            t.record_stream(self._side)
         status = sig['status'] | pop['status']
         return X.real, pop['mean'].real, status
 

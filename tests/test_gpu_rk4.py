@@ -142,3 +142,18 @@ def test_block_matrix_powers_fp64():
         for k in range(1, 5):
             Pk = np.linalg.matrix_power(P, k) - np.eye(16)
             assert rel_err(blk[b, 16 + (k - 1) * 2:16 + k * 2], Pk[sel]) < 1e-13
+
+
+def test_block_variant_too_wide_is_rejected():
+    """A variant whose block would exceed its compiled size is refused (the
+    planner's default and the autotuner fall back to the others)."""
+    M, B, K = 49, 3, 3
+    L = random_generators(B, M, seed=1)
+    D = _native.rk4_propagator(torch.as_tensor(L).cuda(), 1.0, _native.QSX_FP32)
+    sel = list(range(M))
+    blk = _native.rk4_block_matrix(D, K, sel)
+    y0 = torch.ones(M, dtype=torch.complex128, device='cuda')
+    with pytest.raises(_native.QsxError):
+        _native.rk4(blk, y0, 9, 1, select=sel, mean=True, block_k=K, variant=5)
+    out = _native.rk4(blk, y0, 9, 1, select=sel, mean=True, block_k=K)
+    assert torch.isfinite(out['mean'].real).all()
