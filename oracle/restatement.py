@@ -677,6 +677,63 @@ def third_order_response(model, coherence_time_max, population_times,
     return (t1, t2, t3), total
 
 
+class GaussianPulseSpec:
+    """E(t) = scale exp(i fc (carrier - rw)(t - t_peak) - (t - t_peak)^2 / 2 sigma^2)
+    on [t_peak - 3 sigma, t_peak + 3 sigma], sigma = fwhm GAUSSIAN_SD_FWHM
+    (pulse.py:74-113)."""
+
+    def __init__(self, carrier_freq, fwhm, t_peak=0.0, scale=1.0, freq_convert=1.0,
+                 t_limits_multiple=3):
+        sigma = GAUSSIAN_SD_FWHM * fwhm
+        self.two_sigma_squared = 2 * sigma ** 2
+        self.t_init = t_peak - t_limits_multiple * sigma
+        self.t_final = t_peak + t_limits_multiple * sigma
+        self.t_peak, self.carrier_freq = t_peak, carrier_freq
+        self.scale, self.freq_convert = scale, freq_convert
+
+    def __call__(self, t, rw_freq):
+        d = t - self.t_peak
+        return self.scale * np.exp(1j * self.freq_convert * (self.carrier_freq - rw_freq) * d
+                                   - d ** 2 / self.two_sigma_squared)
+
+
+def simulate_with_fields(model, pulses, geometry='-+', polarization='xx', time_extra=0.0,
+                         times=None, liouville_subspace='gg,ge,eg,ee', dt=None):
+    """RK4 form of _simulate_with_fields (eom.py:77-105): dy/dt = L y +
+    sum_p (-i E_p(t)^(*)) [V_p, y], from the thermal state at the first
+    pulse's start, outputs on arange(t0, tf + time_extra, time_step)."""
+    dt = model.time_step if dt is None else dt
+    L = model.eom_matrix(liouville_subspace)
+    C = [model.dipole(liouville_subspace, pol, tr).commutator_matrix
+         for pol, tr in zip(polarization, geometry)]
+
+    def f(t, y):
+        d = L @ y
+        for pulse, tr, Cp in zip(pulses, geometry, C):
+            E = pulse(t, model.ham.rw_freq)
+            if tr == '+':
+                E = np.conj(E)
+            d = d + (-1j * E) * (Cp @ y)
+        return d
+
+    y = np.array(model.thermal_state(liouville_subspace), dtype=complex)
+    t0 = min(p.t_init for p in pulses)
+    tf = max(p.t_final for p in pulses)
+    t = (np.arange(t0, tf + time_extra, model.time_step) if times is None
+         else tf + np.asarray(times, float))
+    out, cur = [], t0
+    for ti in t:
+        for _ in range(int(round((ti - cur) / dt))):
+            k1 = f(cur, y)
+            k2 = f(cur + dt / 2, y + dt / 2 * k1)
+            k3 = f(cur + dt / 2, y + dt / 2 * k2)
+            k4 = f(cur + dt, y + dt * k3)
+            y = y + dt / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+            cur = cur + dt
+        out.append(y.copy())
+    return t, np.array(out)
+
+
 def ensemble_average(model, n_samples, func, *args, **kw):
     """Serial ensemble loop then mean (decorators.py:40-64)."""
     acc = None

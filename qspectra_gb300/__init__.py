@@ -18,7 +18,8 @@ from .hamiltonian import ElectronicHamiltonian, HamiltonianError
 from .operator_tools import (SubspaceError, all_states, basis_transform_operator,
                              basis_transform_vector, n_excitations, unit_vec)
 from .polarization import check_polarizations, polarization_vector
-from .simulate.eom import simulate_dynamics
+from .pulse import CustomPulse, GaussianPulse, Pulse
+from .simulate.eom import simulate_dynamics, simulate_pump, simulate_with_fields
 from .simulate.response import (PUMP_PROBE_PATHWAYS, THIRD_ORDER_PATHWAYS,
                                 absorption_spectra, impulsive_probe,
                                 linear_response, third_order_response,
@@ -35,7 +36,8 @@ __all__ = [
     'ElectronicHamiltonian', 'HamiltonianError', 'SubspaceError', 'all_states',
     'basis_transform_operator', 'basis_transform_vector', 'n_excitations',
     'unit_vec', 'check_polarizations', 'polarization_vector',
-    'simulate_dynamics', 'PUMP_PROBE_PATHWAYS', 'THIRD_ORDER_PATHWAYS',
+    'simulate_dynamics', 'simulate_with_fields', 'simulate_pump', 'Pulse', 'CustomPulse',
+    'GaussianPulse', 'PUMP_PROBE_PATHWAYS', 'THIRD_ORDER_PATHWAYS',
     'absorption_spectra', 'impulsive_probe', 'linear_response',
     'third_order_response', 'two_dimensional_spectra', 'IntegratorError',
     'bound_signal', 'fourier_transform', 'integrate', 'QsxError',

@@ -1,5 +1,8 @@
 """Free time evolution (qspectra/simulate/eom.py:11-74)."""
 import numpy as np
+import torch
+
+from .. import _native
 
 from .ensemble import ensemble_populations
 from .utils import integrate
@@ -38,3 +41,90 @@ def simulate_dynamics(dynamical_model, initial_state, duration=None, times=None,
     states = integrate(eom, y0, t, save_func=save_func, precision=precision, step=step,
                        **integrate_kwargs)
     return t, dynamical_model.state_vector_to_density_matrix(states)
+
+
+def _field_table(pulses, geometry, rw_freq, t0, nsteps, h):
+    """a_p at t_n, t_n + h/2, t_n + h: -i E_p(t), conjugated for '+'."""
+    tn = t0 + h * np.arange(nsteps)
+    ts = np.stack([tn, tn + h / 2, tn + h], axis=1)            # (nsteps, 3)
+    cols = []
+    for pulse, trans in zip(pulses, geometry):
+        E = np.asarray(pulse(ts, rw_freq), dtype=complex)
+        if trans == '+':
+            E = np.conj(E)
+        cols.append(-1j * E)
+    return np.stack(cols, axis=-1)                              # (nsteps, 3, npulses)
+
+
+def simulate_with_fields(dynamical_model, pulses, geometry='-+', polarization='xx',
+                         time_extra=0, times=None, liouville_subspace='gg,ge,eg,ee',
+                         save_func=None, ensemble_size=None,
+                         ensemble_random_orientations=False, precision='fp64',
+                         **integrate_kwargs):
+    """Time evolution under pulses in the rotating-wave approximation
+    (eom.py:77-170), fixed-step RK4 on the GPU (qsx_rk4_field_batched).
+
+    Returns (t, states) with states (T, M) (or save_func of them), averaged
+    over ``ensemble_size`` disorder samples when given.
+    """
+    from .ensemble import SampleBatch
+    from .utils import PRECISIONS, step_plan
+    if ensemble_random_orientations:
+        raise NotImplementedError('random ensemble orientations are not on the '
+                                  'accelerated path')
+    if save_func is not None and not hasattr(save_func, 'matrix'):
+        raise TypeError('save_func must be a linear operator map')
+    model = dynamical_model
+    prec = PRECISIONS[precision]
+    h = integrate_kwargs.pop('step', model.time_step)
+    t0 = min(p.t_init for p in pulses)
+    tf = max(p.t_final for p in pulses)
+    t = (np.arange(t0, tf + time_extra, model.time_step) if times is None
+         else tf + np.asarray(times, float))
+    steps = step_plan(t, t0, h)
+    every = int(steps[1] - steps[0]) if len(steps) > 1 else 1
+    if steps[0] % max(every, 1) or np.any(np.diff(steps) != every):
+        raise ValueError('output times must be evenly spaced on the RK4 step grid from '
+                         'the first pulse')
+    first = int(steps[0])
+    nsteps = int(steps[-1])
+    idx = model.liouville_subspace_index(liouville_subspace)
+    V = [model.dipole_operator(liouville_subspace, pol, tr)
+         for pol, tr in zip(polarization, geometry)]
+    dev = torch.device('cuda', torch.cuda.current_device())
+    C = torch.as_tensor(np.array([v.commutator_matrix for v in V], dtype=complex),
+                        device=dev)
+    coef = torch.as_tensor(_field_table(pulses, geometry, model.rw_freq, t0, nsteps, h),
+                           device=dev)
+    y0 = torch.as_tensor(np.asarray(model.thermal_state(liouville_subspace), dtype=complex),
+                         device=dev)
+    if ensemble_size is None:
+        L = model.equation_of_motion(liouville_subspace).matrix
+    else:
+        batch = SampleBatch(model, ensemble_size)
+        L = model.build_batch(batch.H(model.hilbert_subspace)).block(idx)
+    save_every = max(every, 1) if nsteps else 1
+    states = _native.rk4_field(L, C, coef, y0, nsteps, h, save_every, prec)
+    states = states[:, first // save_every:]
+    if ensemble_size is not None:
+        states = states.mean(0)
+    else:
+        states = states[0]
+    if save_func is not None:
+        states = states @ save_func.matrix.T
+        if save_func.scalar:
+            states = states[..., 0]
+    return t, states.cpu().numpy()
+
+
+def simulate_pump(dynamical_model, pump, polarization='x', time_extra=0, times=None,
+                  liouville_subspace='gg,ge,eg,ee', save_func=None, ensemble_size=None,
+                  ensemble_random_orientations=False, exact_isotropic_average=False,
+                  precision='fp64', **integrate_kwargs):
+    """A pump pulse acting twice ('-+') (eom.py:173-227)."""
+    if exact_isotropic_average:
+        raise NotImplementedError('isotropic averaging is not on the accelerated path')
+    return simulate_with_fields(dynamical_model, [pump, pump], '-+',
+                                [polarization, polarization], time_extra, times,
+                                liouville_subspace, save_func, ensemble_size,
+                                ensemble_random_orientations, precision, **integrate_kwargs)

@@ -134,6 +134,22 @@ def main(ref_root):
     t, rhos = qs.simulate_dynamics(m7, psi, duration=1000.0, ensemble_size=8)
     out['fmo7_ens8_pops'] = np.einsum('tii->ti', rhos).real
 
+    # field-driven propagation (eom.py:77-227): a Gaussian pump, and two
+    # different pulses with a 3-sample ensemble
+    pump = qs.GaussianPulse(carrier_freq=12350.0, fwhm=20.0, t_peak=0.0, scale=1e-2,
+                            freq_convert=qs.CM_FS)
+    t, st = qs.simulate_pump(m7, pump, polarization='x', time_extra=60.0)
+    out['fields_pump_t'] = t
+    out['fields_pump_states'] = st
+    p1 = qs.GaussianPulse(carrier_freq=12250.0, fwhm=15.0, t_peak=-10.0, scale=5e-3,
+                          freq_convert=qs.CM_FS)
+    p2 = qs.GaussianPulse(carrier_freq=12450.0, fwhm=25.0, t_peak=20.0, scale=8e-3,
+                          freq_convert=qs.CM_FS)
+    t, st = qs.simulate_with_fields(m7, [p1, p2], geometry='-+', polarization='xy',
+                                    time_extra=40.0, ensemble_size=3)
+    out['fields_two_t'] = t
+    out['fields_two_states'] = st
+
     # tight zvode for the integrator gap (reference as shipped)
     qeom.integrate = qutils.integrate
     qresp.integrate = qutils.integrate

@@ -134,3 +134,24 @@ def test_heom_trajectory(golden):
     y0[0] = 1
     traj = orc.rk4_integrate_sparse(L, y0, 199, 0.5)
     assert rel_err(traj[:, :9], golden['heom3_traj_node0']) < 1e-12
+
+
+def test_fields_oracle_matches_reference(golden):
+    """Field-driven propagation (eom.py:77-227) against the reference's own
+    simulate_pump / simulate_with_fields driven by the RK4 harness."""
+    H7 = golden['fmo7_H']
+    bath = orc.DebyeBathSpec(orc.CM_K * 77, 35, 106)
+    oham = orc.ElectronicHamiltonianSpec(H7, dipoles=[[1, 0, 0]] * 7,
+                                         disorder=wl.fwhm_for_sd(80.0), random_seed=1,
+                                         energy_spread_extra=float(golden['fmo7_extra']),
+                                         bath=bath)
+    om = orc.RedfieldSpec(oham, bath, 'ge', orc.CM_FS, secular=False)
+    pump = orc.GaussianPulseSpec(12350.0, 20.0, 0.0, 1e-2, orc.CM_FS)
+    t, st = orc.simulate_with_fields(om, [pump, pump], '-+', 'xx', 60.0)
+    assert np.allclose(t, golden['fields_pump_t'], rtol=0, atol=1e-12)
+    assert rel_err(st, golden['fields_pump_states']) < 1e-12
+    p1 = orc.GaussianPulseSpec(12250.0, 15.0, -10.0, 5e-3, orc.CM_FS)
+    p2 = orc.GaussianPulseSpec(12450.0, 25.0, 20.0, 8e-3, orc.CM_FS)
+    ticks, st = orc.ensemble_average(om, 3, orc.simulate_with_fields, [p1, p2], '-+', 'xy',
+                                     40.0)
+    assert rel_err(st, golden['fields_two_states']) < 1e-12
