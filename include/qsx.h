@@ -282,13 +282,15 @@ size_t qsx_heom_args_bytes(void);
  * at every stage time: coef complex [nsteps][3][npulses] for t_n,
  * t_n + h/2 and t_n + h.  L complex [batch][m][m] (L_stride elements per
  * sample, 0 = shared), C complex [npulses][m][m] (the restricted commutator
- * maps of the pulses' dipole operators), all in the working precision
+ * maps of the pulses' dipole operators; C_stride elements per sample, 0 =
+ * shared, per-sample maps carry randomly oriented dipoles), all in the working precision
  * (complex64 for QSX_FP32, which keeps a split-word state; complex128 for
  * QSX_FP64).  y0 complex128 [batch][m] (y0_stride 0 = shared); out_state
  * complex128 [batch][nsteps / save_every + 1][m].  m <= 1024 and the
  * generator plus field maps must fit in 227 KB of shared memory.
  */
-int qsx_rk4_field_batched(const void* L, int64_t L_stride, const void* C, int npulses,
+int qsx_rk4_field_batched(const void* L, int64_t L_stride, const void* C,
+                          int64_t C_stride, int npulses,
                           const void* coef, int m, int64_t batch, int nsteps, double h,
                           const double* y0, int64_t y0_stride, int save_every,
                           int precision, double* out_state, int32_t* status,

@@ -130,6 +130,60 @@ def polarization_vector(p):
     return p
 
 
+def random_rotation_matrix(rng):
+    """Uniformly distributed rotation from three uniforms (polarization.py:87-102;
+    Arvo, Graphics Gems III, 1992): a rotation by 2 pi x1 about z, then the
+    reflection through the plane normal to v(x2, x3), negated."""
+    x1, x2, x3 = rng.rand(3)
+    th, ph = 2 * np.pi * x1, 2 * np.pi * x2
+    Rz = np.array([[np.cos(th), np.sin(th), 0.0],
+                   [-np.sin(th), np.cos(th), 0.0],
+                   [0.0, 0.0, 1.0]])
+    v = np.array([np.cos(ph) * np.sqrt(x3), np.sin(ph) * np.sqrt(x3), np.sqrt(1 - x3)])
+    return -(np.eye(3) - 2 * np.outer(v, v)) @ Rz
+
+
+FOURTH_ORDER_PAIRINGS = (((0, 1), (2, 3)), ((0, 2), (1, 3)), ((0, 3), (1, 2)))
+
+
+def isotropic_weights_4th(polarization):
+    """Weights of the three fourth-rank invariants (polarization.py:55-70):
+    (1/30)(5 I - 1) applied to the products of polarization dot products in
+    each pairing (Hochstrasser 2001)."""
+    e = np.array([polarization_vector(p) for p in polarization])
+    c = e @ e.T
+    prod = np.array([c[a] * c[b] for a, b in FOURTH_ORDER_PAIRINGS])
+    return (5 * np.eye(3) - np.ones((3, 3))) @ prod / 30
+
+
+def isotropic_average_4th(func, polarization, *args, **kw):
+    """Exact isotropic average of a third-order signal (decorators.py:67-92):
+    each invariant whose weight exceeds 1e-8 adds its weight times the sum of
+    the signals over the nine lab polarizations whose paired indices agree."""
+    signals, total, ticks = {}, 0, None
+    for pairing, w in zip(FOURTH_ORDER_PAIRINGS, isotropic_weights_4th(polarization)):
+        if w <= 1e-8:
+            continue
+        for p in itertools.product('xyz', repeat=4):
+            if all(p[a] == p[b] for a, b in pairing):
+                key = ''.join(p)
+                if key not in signals:
+                    ticks, signals[key] = func(*args, polarization=key, **kw)
+                total = total + w * signals[key]
+    return ticks, total
+
+
+def isotropic_average_2nd(func, polarization, *args, **kw):
+    """Exact isotropic average of a second-order signal (decorators.py:95-125):
+    (e1 . e2) / 3 times the sum of the 'xx', 'yy' and 'zz' signals."""
+    e = [polarization_vector(p) for p in polarization]
+    total, ticks = 0, None
+    for p in ('xx', 'yy', 'zz'):
+        ticks, sig = func(*args, polarization=p, **kw)
+        total = total + sig
+    return ticks, total * (np.dot(e[0], e[1]) / 3.0)
+
+
 def dipole_operator(dipoles, subspace, polarization, transitions='-+'):
     """Σ_n T_n (d_n · e) (hamiltonian.py:580-591)."""
     dipoles = np.asarray(dipoles, float)
@@ -229,8 +283,10 @@ class ElectronicHamiltonianSpec:
             rw_freq = float(np.mean(scipy.linalg.eigh(self.H1)[0]))
         self.rw_freq = rw_freq
 
-    def sample(self, n):
-        """hamiltonian.py:233-274 and :552-578 (diagonal Gaussian disorder)."""
+    def sample(self, n, random_orientations=False):
+        """hamiltonian.py:233-274 and :552-578 (diagonal Gaussian disorder,
+        then, with random_orientations, a uniform rotation of the dipoles
+        drawn from the same RandomState)."""
         seed = list(np.atleast_1d(self.random_seed)) + [n]
         rng = np.random.RandomState(seed)
         if self.disorder is None:
@@ -238,8 +294,12 @@ class ElectronicHamiltonianSpec:
         else:
             shift = np.diag((self.disorder * GAUSSIAN_SD_FWHM)
                             * rng.randn(self.n_sites))
+        dipoles = self.dipoles
+        if random_orientations:
+            R = random_rotation_matrix(rng)
+            dipoles = np.array([R @ d for d in self.dipoles])
         out = ElectronicHamiltonianSpec(
-            self.H1 + shift, self.dipoles, self.rw_freq, self.disorder,
+            self.H1 + shift, dipoles, self.rw_freq, self.disorder,
             seed, self.energy_spread_extra, self.bath)
         out._unsampled = self._unsampled
         return out
@@ -390,8 +450,8 @@ class RedfieldSpec:
     def n_sites(self):
         return self.ham.n_sites
 
-    def sample(self, n):
-        return RedfieldSpec(self.ham.sample(n), self.bath,
+    def sample(self, n, random_orientations=False):
+        return RedfieldSpec(self.ham.sample(n, random_orientations), self.bath,
                             self.hilbert_subspace, self.unit_convert,
                             self.secular, self.discard_imag_corr,
                             self.evolve_basis)
@@ -734,12 +794,12 @@ def simulate_with_fields(model, pulses, geometry='-+', polarization='xx', time_e
     return t, np.array(out)
 
 
-def ensemble_average(model, n_samples, func, *args, **kw):
+def ensemble_average(model, n_samples, func, *args, random_orientations=False, **kw):
     """Serial ensemble loop then mean (decorators.py:40-64)."""
     acc = None
     ticks = None
     for n in range(n_samples):
-        ticks, sig = func(model.sample(n), *args, **kw)
+        ticks, sig = func(model.sample(n, random_orientations), *args, **kw)
         acc = sig if acc is None else acc + sig
     return ticks, acc / n_samples
 

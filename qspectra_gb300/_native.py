@@ -114,7 +114,8 @@ _PROTOS = {
                                        _c_vp, ctypes.c_size_t, _c_vp, _c_vp]),
     'qsx_csr_map_batched': (_c_int, [_c_vp, _c_i64, _c_i64, _c_vp, _c_vp, _c_vp, _c_int,
                                      _c_vp, _c_vp]),
-    'qsx_rk4_field_batched': (_c_int, [_c_vp, _c_i64, _c_vp, _c_int, _c_vp, _c_int, _c_i64,
+    'qsx_rk4_field_batched': (_c_int, [_c_vp, _c_i64, _c_vp, _c_i64, _c_int, _c_vp, _c_int,
+                                       _c_i64,
                                        _c_int, _c_dbl, _c_vp, _c_i64, _c_int, _c_int, _c_vp,
                                        _c_vp, _c_vp]),
     'qsx_eigh_large_workspace_bytes': (ctypes.c_size_t, [_c_int, _c_i64]),
@@ -640,24 +641,35 @@ def rk4_field(L, C, coef, y0, nsteps, h, save_every=1, precision=QSX_FP64,
               check_finite=True):
     """States (B, nsteps/save_every + 1, m) complex128 of the field-driven RK4
     loop (qsx_rk4_field_batched).  L (B, m, m) or (m, m) complex128, C
-    (npulses, m, m) complex128, coef (nsteps, 3, npulses) complex128."""
+    (npulses, m, m) or per sample (B, npulses, m, m) complex128, coef
+    (nsteps, 3, npulses) complex128."""
     require_gpu()
     cd = torch.complex64 if precision == QSX_FP32 else torch.complex128
     Lm = L if L.dim() == 3 else L[None]
     m = Lm.shape[-1]
     y0 = y0.to(torch.complex128).contiguous()
-    B = Lm.shape[0] if L.dim() == 3 else (y0.shape[0] if y0.dim() == 2 else 1)
+    per_C = C is not None and C.dim() == 4
+    if L.dim() == 3:
+        B = Lm.shape[0]
+    elif per_C:
+        B = C.shape[0]
+    else:
+        B = y0.shape[0] if y0.dim() == 2 else 1
+    for name, n in (('C', C.shape[0] if per_C else B), ('y0', y0.shape[0] if y0.dim() == 2 else B)):
+        if n != B:
+            raise ValueError('{} batch does not match'.format(name))
     Lw = Lm.to(cd).contiguous()
-    np_ = int(C.shape[0]) if C is not None else 0
+    np_ = int(C.shape[-3]) if C is not None else 0
     Cw = C.to(cd).contiguous() if np_ else None
     cw = coef.to(cd).contiguous() if np_ else None
     out = torch.empty((B, nsteps // save_every + 1, m), dtype=torch.complex128,
                       device=Lw.device)
     status = torch.zeros(1, dtype=torch.int32, device=Lw.device)
     _check(load().qsx_rk4_field_batched(
-        _p(Lw), m * m if L.dim() == 3 else 0, _p(Cw), np_, _p(cw), m, B, int(nsteps),
-        float(h), _p(y0), m if y0.dim() == 2 else 0, int(save_every), precision, _p(out),
-        _p(status), _stream()), 'qsx_rk4_field_batched')
+        _p(Lw), m * m if L.dim() == 3 else 0, _p(Cw), np_ * m * m if per_C else 0, np_,
+        _p(cw), m, B, int(nsteps), float(h), _p(y0), m if y0.dim() == 2 else 0,
+        int(save_every), precision, _p(out), _p(status), _stream()),
+        'qsx_rk4_field_batched')
     if check_finite and int(status.item()) & QSX_ERR_NONFINITE:
         raise IntegratorError('non-finite state in the field-driven propagation')
     return out

@@ -18,7 +18,8 @@ struct FieldP {
   int64_t batch;
   const void* L;     // [batch][m][m] complex (T), stride L_stride elements (0 = shared)
   int64_t L_stride;
-  const void* C;     // [np][m][m] complex (T), shared
+  const void* C;     // [np][m][m] complex (T), stride C_stride elements (0 = shared)
+  int64_t C_stride;
   const void* coef;  // [nsteps][3][np] complex (T)
   double h;
   const double2* y0;
@@ -38,7 +39,7 @@ __global__ void __launch_bounds__(1024) rk4_field_kernel(FieldP p) {
   Cx* sa = sCT + (size_t)np * m * m;     // [np] stage coefficients
   const int64_t s = blockIdx.x;
   const Cx* L = (const Cx*)p.L + s * p.L_stride;
-  const Cx* C = (const Cx*)p.C;
+  const Cx* C = (const Cx*)p.C + s * p.C_stride;
   for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
     const int r = e / m, c = e % m;
     sLT[c * m + r] = L[e];
@@ -123,7 +124,8 @@ __global__ void __launch_bounds__(1024) rk4_field_kernel(FieldP p) {
 using namespace qsx;
 
 extern "C" int qsx_rk4_field_batched(const void* L, int64_t L_stride, const void* C,
-                                     int npulses, const void* coef, int m, int64_t batch,
+                                     int64_t C_stride, int npulses, const void* coef,
+                                     int m, int64_t batch,
                                      int nsteps, double h, const double* y0,
                                      int64_t y0_stride, int save_every, int precision,
                                      double* out_state, int32_t* status, void* stream) {
@@ -152,6 +154,7 @@ extern "C" int qsx_rk4_field_batched(const void* L, int64_t L_stride, const void
   p.L = L;
   p.L_stride = L_stride;
   p.C = C;
+  p.C_stride = npulses ? C_stride : 0;
   p.coef = coef;
   p.h = h;
   p.y0 = (const double2*)y0;

@@ -304,3 +304,21 @@ class ElectronicHamiltonian:
         for k, n in enumerate(range(start, start + ensemble_size)):
             out[k] = scale * np.random.RandomState(base._seed_for(n)).randn(self.n_sites)
         return out
+
+    def orientation_rotations(self, ensemble_size, start=0):
+        """(ensemble_size, 3, 3) rotations applied to the dipoles of samples
+        start..start+ensemble_size-1 when ``random_orientations`` is set.
+
+        The same draws as ``sample(n, random_orientations=True)``
+        (hamiltonian.py:552-575): RandomState(list(seed) + [n]) draws the
+        disorder first, then the three uniforms of the rotation.  Sample n's
+        dipoles are R_n d_i, so its response to lab polarization e equals the
+        unrotated system's response to R_n^T e.
+        """
+        base = self._not_sampled
+        out = np.empty((ensemble_size, 3, 3))
+        for k, n in enumerate(range(start, start + ensemble_size)):
+            rs = np.random.RandomState(base._seed_for(n))
+            base._disorder_for(rs)
+            out[k] = random_rotation_matrix(rs)
+        return out

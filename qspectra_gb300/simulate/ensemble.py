@@ -140,10 +140,23 @@ def redfield_batch_build(model, batch):
     return model.build_batch(batch.H(model.hilbert_subspace))
 
 
+def sample_polarizations(polarization, rotations):
+    """(S, k, 3) per-sample polarization vectors R_s^T e for lab polarizations
+    ``polarization`` (k of them) and dipole rotations (S, 3, 3)."""
+    from ..polarization import polarization_vector
+    pols = np.array([polarization_vector(p) for p in polarization], float)
+    return np.einsum('sji,kj->ski', np.asarray(rotations, float), pols)
+
+
 def ensemble_linear_signal(model, time_max, ensemble_size, polarization='xx',
                            precision='fp32', path='gg->eg->gg', start=0,
-                           offsets=None, return_build=False):
+                           offsets=None, return_build=False, rotations=None):
     """Disorder-averaged Heisenberg-picture linear response (response.py:15-43).
+
+    ``rotations`` (S, 3, 3) rotates each sample's dipoles (random ensemble
+    orientations, decorators.py:40-64): the dipole operators are linear in
+    the polarization vector, so sample s uses R_s^T e in place of e, as a
+    per-sample initial state and projection of the same batched time loop.
 
     Returns (t, mean signal) with the signal on the GPU (complex128).
     """
@@ -155,14 +168,26 @@ def ensemble_linear_signal(model, time_max, ensemble_size, polarization='xx',
     batch = SampleBatch(model, ensemble_size, start, offsets)
     build = redfield_batch_build(model, batch)
     rho0 = model.thermal_state(subs[0])
+    q = None if rotations is None else torch.as_tensor(
+        sample_polarizations(polarization, rotations)).cuda()      # (S, 2, 3)
     total = None
     for sim in subs[1].split(','):
-        V0 = model.dipole_operator('{}->{}'.format(subs[0], sim), polarization[0], '+')
-        V1 = model.dipole_operator('{}->{}'.format(sim, subs[2]), polarization[1], '-')
-        v_rho0 = V0.commutator(rho0)
+        sp0, sp1 = '{}->{}'.format(subs[0], sim), '{}->{}'.format(sim, subs[2])
         D = build.propagator(model.liouville_subspace_index(sim), dt, prec, transpose=True)
-        y0 = torch.as_tensor(-V1.bra_vector, dtype=torch.complex128).cuda()
-        proj = torch.as_tensor(np.asarray(v_rho0)[None, :], dtype=torch.complex128).cuda()
+        if q is None:
+            V0 = model.dipole_operator(sp0, polarization[0], '+')
+            V1 = model.dipole_operator(sp1, polarization[1], '-')
+            y0 = torch.as_tensor(-V1.bra_vector, dtype=torch.complex128).cuda()
+            proj = torch.as_tensor(np.asarray(V0.commutator(rho0))[None, :],
+                                   dtype=torch.complex128).cuda()
+        else:
+            axes = np.eye(3)
+            P0 = np.array([model.dipole_operator(sp0, a, '+').commutator(rho0) for a in axes])
+            Y1 = np.array([-model.dipole_operator(sp1, a, '-').bra_vector for a in axes])
+            P0 = torch.as_tensor(P0, dtype=torch.complex128).cuda()
+            Y1 = torch.as_tensor(Y1, dtype=torch.complex128).cuda()
+            y0 = torch.einsum('sa,am->sm', q[:, 1].to(Y1.dtype), Y1).contiguous()
+            proj = torch.einsum('sa,am->sm', q[:, 0].to(P0.dtype), P0)[:, None, :].contiguous()
         steps = step_plan(t, 0.0, dt)
         out = _native.rk4(D, y0, int(steps[-1]), 1,
                           proj=proj, per_sample=False, mean=True, check_finite=False)

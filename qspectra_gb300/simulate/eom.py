@@ -15,16 +15,29 @@ def simulate_dynamics(dynamical_model, initial_state, duration=None, times=None,
     """Density matrices ρ(t) with no applied field (eom.py:29-74).
 
     Returns (t, rhos) with rhos (T, N, N) like the reference.  With
-    ``ensemble_size`` the disorder average is one batched GPU run.
+    ``ensemble_size`` the disorder average of a Redfield model is one batched
+    GPU run; other models integrate the samples one after another.  Random
+    orientations rotate only the dipoles, which free dynamics never reads, so
+    ``ensemble_random_orientations`` leaves the result unchanged (the
+    reference draws the rotation after the disorder: hamiltonian.py:552-575).
     """
+    from ..dynamics.redfield import RedfieldModel
     if ensemble_size is not None:
-        if times is not None or save_func is not None:
-            raise NotImplementedError('ensemble dynamics take duration and no save_func')
-        t, mean = ensemble_populations(dynamical_model, initial_state, duration,
-                                       ensemble_size, liouville_subspace, precision,
-                                       full_state=True)
-        rhos = dynamical_model.state_vector_to_density_matrix(mean.cpu().numpy())
-        return t, rhos
+        if (isinstance(dynamical_model, RedfieldModel) and times is None
+                and save_func is None and not integrate_kwargs):
+            t, mean = ensemble_populations(dynamical_model, initial_state, duration,
+                                           ensemble_size, liouville_subspace, precision,
+                                           full_state=True)
+            rhos = dynamical_model.state_vector_to_density_matrix(mean.cpu().numpy())
+            return t, rhos
+        total = 0
+        for m in dynamical_model.sample_ensemble(ensemble_size,
+                                                 ensemble_random_orientations):
+            t, rhos = simulate_dynamics(m, initial_state, duration, times,
+                                        liouville_subspace, save_func,
+                                        precision=precision, **integrate_kwargs)
+            total = total + rhos
+        return t, total / ensemble_size
     from ..dynamics.heom import HEOMModel
     eom = dynamical_model.equation_of_motion(liouville_subspace)
     rho0 = np.asarray(initial_state)
@@ -65,13 +78,13 @@ def simulate_with_fields(dynamical_model, pulses, geometry='-+', polarization='x
     (eom.py:77-170), fixed-step RK4 on the GPU (qsx_rk4_field_batched).
 
     Returns (t, states) with states (T, M) (or save_func of them), averaged
-    over ``ensemble_size`` disorder samples when given.
+    over ``ensemble_size`` disorder samples when given.  With
+    ``ensemble_random_orientations`` each sample's field maps carry its
+    rotated dipoles (hamiltonian.py:552-575): the commutator maps are linear
+    in the polarization vector, so sample s gets sum_a (R_s^T e)_a C(e_a).
     """
-    from .ensemble import SampleBatch
+    from .ensemble import SampleBatch, sample_polarizations
     from .utils import PRECISIONS, step_plan
-    if ensemble_random_orientations:
-        raise NotImplementedError('random ensemble orientations are not on the '
-                                  'accelerated path')
     if save_func is not None and not hasattr(save_func, 'matrix'):
         raise TypeError('save_func must be a linear operator map')
     model = dynamical_model
@@ -89,11 +102,19 @@ def simulate_with_fields(dynamical_model, pulses, geometry='-+', polarization='x
     first = int(steps[0])
     nsteps = int(steps[-1])
     idx = model.liouville_subspace_index(liouville_subspace)
-    V = [model.dipole_operator(liouville_subspace, pol, tr)
-         for pol, tr in zip(polarization, geometry)]
     dev = torch.device('cuda', torch.cuda.current_device())
-    C = torch.as_tensor(np.array([v.commutator_matrix for v in V], dtype=complex),
-                        device=dev)
+    if ensemble_size is not None and ensemble_random_orientations:
+        rot = model.hamiltonian.orientation_rotations(ensemble_size)
+        q = torch.as_tensor(sample_polarizations(polarization, rot), device=dev)
+        basis = torch.as_tensor(np.array(
+            [[model.dipole_operator(liouville_subspace, a, tr).commutator_matrix
+              for a in np.eye(3)] for tr in geometry], dtype=complex), device=dev)
+        C = torch.einsum('spa,pamn->spmn', q.to(basis.dtype), basis)
+    else:
+        V = [model.dipole_operator(liouville_subspace, pol, tr)
+             for pol, tr in zip(polarization, geometry)]
+        C = torch.as_tensor(np.array([v.commutator_matrix for v in V], dtype=complex),
+                            device=dev)
     coef = torch.as_tensor(_field_table(pulses, geometry, model.rw_freq, t0, nsteps, h),
                            device=dev)
     y0 = torch.as_tensor(np.asarray(model.thermal_state(liouville_subspace), dtype=complex),
@@ -121,9 +142,24 @@ def simulate_pump(dynamical_model, pump, polarization='x', time_extra=0, times=N
                   liouville_subspace='gg,ge,eg,ee', save_func=None, ensemble_size=None,
                   ensemble_random_orientations=False, exact_isotropic_average=False,
                   precision='fp64', **integrate_kwargs):
-    """A pump pulse acting twice ('-+') (eom.py:173-227)."""
+    """A pump pulse acting twice ('-+') (eom.py:173-227).
+
+    ``exact_isotropic_average`` sums the 'xx', 'yy' and 'zz' runs with weight
+    (e . e) / 3 (decorators.py:95-125).
+    """
     if exact_isotropic_average:
-        raise NotImplementedError('isotropic averaging is not on the accelerated path')
+        from ..polarization import check_polarizations
+        e = check_polarizations([polarization, polarization], 2)
+        weight = float(np.dot(*e))
+        total, t = 0, None
+        for p in 'xyz':
+            t, st = simulate_with_fields(dynamical_model, [pump, pump], '-+', [p, p],
+                                         time_extra, times, liouville_subspace,
+                                         save_func, ensemble_size,
+                                         ensemble_random_orientations, precision,
+                                         **integrate_kwargs)
+            total = total + st
+        return t, total * (weight / 3.0)
     return simulate_with_fields(dynamical_model, [pump, pump], '-+',
                                 [polarization, polarization], time_extra, times,
                                 liouville_subspace, save_func, ensemble_size,

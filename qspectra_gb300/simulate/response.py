@@ -7,7 +7,8 @@ average as one batched GPU pipeline instead of a serial loop.
 import numpy as np
 import torch
 
-from ..polarization import check_polarizations
+from ..polarization import (FOURTH_ORDER_INVARIANTS, check_polarizations,
+                             invariant_polarizations, invariant_weights_4th_order)
 from .ensemble import ensemble_linear_signal
 from .utils import fourier_transform, integrate
 
@@ -78,18 +79,35 @@ def linear_response(dynamical_model, liouv_space_path, time_max,
                     ensemble_random_orientations=False,
                     exact_isotropic_average=False, precision='fp64',
                     **integrate_kwargs):
-    """Linear response function under the RWA (response.py:46-100)."""
-    if ensemble_random_orientations:
-        raise NotImplementedError('random ensemble orientations are not on the '
-                                  'accelerated path')
+    """Linear response function under the RWA (response.py:46-100).
+
+    With ``ensemble_size`` a Redfield model runs every disorder sample in one
+    batched pipeline; other models integrate the samples one after another.
+    ``ensemble_random_orientations`` rotates each sample's dipoles with the
+    reference's draws (hamiltonian.py:552-575).
+    """
+    from ..dynamics.redfield import RedfieldModel
+    rotations = None
+    if ensemble_size is not None and ensemble_random_orientations:
+        rotations = dynamical_model.hamiltonian.orientation_rotations(ensemble_size)
+    batched = (ensemble_size is not None and isinstance(dynamical_model, RedfieldModel)
+               and initial_state is None and not integrate_kwargs)
 
     def one(pol):
-        if ensemble_size is not None:
-            if initial_state is not None:
-                raise NotImplementedError('ensemble runs start from the thermal state')
+        if batched:
             t, sig = ensemble_linear_signal(dynamical_model, time_max, ensemble_size,
-                                            pol, precision, path=liouv_space_path)
+                                            pol, precision, path=liouv_space_path,
+                                            rotations=rotations)
             return t, sig.cpu().numpy()
+        if ensemble_size is not None:
+            total = 0
+            for m in dynamical_model.sample_ensemble(ensemble_size,
+                                                     ensemble_random_orientations):
+                t, sig = _single_linear_response(m, liouv_space_path, time_max,
+                                                 initial_state, pol, precision,
+                                                 **integrate_kwargs)
+                total = total + sig
+            return t, total / ensemble_size
         return _single_linear_response(dynamical_model, liouv_space_path, time_max,
                                        initial_state, pol, precision,
                                        **integrate_kwargs)
@@ -181,27 +199,47 @@ def third_order_response(dynamical_model, coherence_time_max,
     '+-+' run on the batched engine (simulate/third_order.py): every sample
     of an ensemble in one pass, the two-exciton block in operator form.
     Other models and geometries integrate each pathway's dense blocks.
+
+    ``exact_isotropic_average`` sums the lab polarizations of the three
+    fourth-rank invariants with the reference's weights (decorators.py:67-92;
+    invariants whose weight is not above 1e-8 are left out, as there);
+    ``ensemble_random_orientations`` rotates each sample's dipoles.  The
+    engine evaluates both from shared legs in one pass.
     """
-    if exact_isotropic_average or ensemble_random_orientations:
-        raise NotImplementedError('isotropic averaging is not on the accelerated path')
     from .third_order import supports, third_order_ensemble
     if supports(dynamical_model, geometry) and not integrate_kwargs:
         if population_times is None:
             population_times = np.arange(0, population_time_max, dynamical_model.time_step)
         return third_order_ensemble(dynamical_model, coherence_time_max, population_times,
                                     geometry, polarization, include_signal, ensemble_size,
-                                    precision)
-    if ensemble_size is None:
-        return _single_third_order(dynamical_model, coherence_time_max,
-                                   population_time_max, population_times, geometry,
-                                   polarization, include_signal, precision,
-                                   **integrate_kwargs)
-    total = 0
-    ticks = None
-    for m in dynamical_model.sample_ensemble(ensemble_size):
-        ticks, s = _single_third_order(m, coherence_time_max, population_time_max,
+                                    precision, isotropic=exact_isotropic_average,
+                                    random_orientations=ensemble_random_orientations)
+
+    def one(model):
+        if not exact_isotropic_average:
+            return _single_third_order(model, coherence_time_max, population_time_max,
                                        population_times, geometry, polarization,
                                        include_signal, precision, **integrate_kwargs)
+        weights = invariant_weights_4th_order(polarization)
+        signals = {}
+        total, ticks = 0, None
+        for inv, w in zip(FOURTH_ORDER_INVARIANTS, weights):
+            if w > 1e-8:
+                for p in invariant_polarizations(inv):
+                    if p not in signals:
+                        ticks, signals[p] = _single_third_order(
+                            model, coherence_time_max, population_time_max,
+                            population_times, geometry, p, include_signal, precision,
+                            **integrate_kwargs)
+                    total = total + w * signals[p]
+        return ticks, total
+
+    if ensemble_size is None:
+        return one(dynamical_model)
+    total = 0
+    ticks = None
+    for m in dynamical_model.sample_ensemble(ensemble_size, ensemble_random_orientations):
+        ticks, s = one(m)
         total = total + s
     return ticks, total / ensemble_size
 

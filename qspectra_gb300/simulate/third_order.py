@@ -24,6 +24,17 @@ block-diagonal over the g/e/f manifolds, so this engine never forms the
 
 Rephasing ('-++') and non-rephasing ('+-+') geometries share the t3 leg and
 are evaluated together.
+
+Orientation averages reuse the legs.  The response is linear in each
+pulse's polarization vector, so it is written over lab-frame channels:
+R = sum T[a, b, c, d] R(e_a, e_b, e_c, e_d).  A fixed polarization is one
+channel per pulse; random ensemble orientations make that channel's vector
+per sample (R_s^T e); the exact isotropic average (decorators.py:67-92)
+takes the three axes per pulse with T the invariant weights.  The t1 leg
+then runs once per first-pulse channel, the t3 legs once per last-pulse
+channel, and only the nine (a, b) t2 products meet the nine (c, d) t3
+states, where the reference re-runs all pathways for each of up to 21
+polarizations.
 """
 import numpy as np
 import torch
@@ -32,6 +43,7 @@ from .. import _native
 from ..dynamics.redfield import RedfieldBuild, RedfieldModel
 from ..operator_tools import occupation_table
 from ..dynamics.liouville_space import liouville_subspace_index
+from ..polarization import check_polarizations, isotropic_tensor_4th_order
 from .ensemble import SampleBatch
 from .utils import PRECISIONS, step_plan
 
@@ -102,11 +114,13 @@ class ThirdOrderEngine:
     ``run(offsets)`` returns {geometry: (T1, T2, T3) complex128 tensor}, the
     sum over samples of each sample's response (response.py:297-336 summed
     over the selected pathways); divide by the sample count for the mean.
+    ``isotropic`` evaluates the exact isotropic average for the given lab
+    polarizations; ``run(offsets, rotations)`` rotates each sample's dipoles.
     """
 
     def __init__(self, model, coherence_time_max, population_times,
                  polarization='xxxx', include_signal=None, precision='fp32',
-                 geometries=ENGINE_GEOMETRIES):
+                 geometries=ENGINE_GEOMETRIES, isotropic=False):
         for g in geometries:
             if not supports(model, g):
                 raise NotImplementedError(
@@ -122,6 +136,13 @@ class ThirdOrderEngine:
         steps2 = step_plan(self.t2, 0.0, self.dt)
         self.gaps = np.diff(np.concatenate([[0], steps2])).astype(np.int64)
         self.polarization = polarization
+        pols = check_polarizations(polarization, 4)
+        if isotropic:
+            self.lab = None
+            self.coupling = isotropic_tensor_4th_order(polarization)
+        else:
+            self.lab = pols
+            self.coupling = np.ones((1, 1, 1, 1))
         if include_signal is None:
             include_signal = ('GSB', 'ESE', 'ESA')
         elif isinstance(include_signal, str):
@@ -143,7 +164,7 @@ class ThirdOrderEngine:
     def _op(self, spec, pol, tr):
         key = (spec, pol, tr)
         if key not in self._maps:
-            self._maps[key] = self.model.dipole_operator(spec, pol, tr)
+            self._maps[key] = self.model.dipole_operator(spec, np.asarray(pol, float), tr)
         return self._maps[key]
 
     def _csr(self, spec, pol, tr, transpose=False):
@@ -153,9 +174,52 @@ class ThirdOrderEngine:
             self._maps[key] = _native.CsrMap(m.T if transpose else m)
         return self._maps[key]
 
-    def _bra(self, spec, pol, tr):
-        v = self._op(spec, pol, tr).bra_vector
-        return torch.as_tensor(np.asarray(v, dtype=complex), dtype=torch.complex128).cuda()
+    def _channels(self, S, rotations):
+        """Per pulse, its channels' polarization vectors: a shared tuple, or an
+        (S, 3) CUDA tensor when the dipoles are rotated per sample."""
+        axes = np.eye(3) if self.lab is None else None
+        out = []
+        for k in range(4):
+            vecs = axes if axes is not None else self.lab[k:k + 1]
+            if rotations is None:
+                out.append([tuple(float(x) for x in v) for v in vecs])
+            else:
+                q = np.einsum('sji,cj->csi', rotations, vecs)          # (C, S, 3)
+                out.append([torch.as_tensor(qc).cuda() for qc in q])
+        return out
+
+    def _apply(self, spec, tr, vec, x, transpose=False):
+        """Map of polarization ``vec`` applied to x (S, ..., n_in): one CSR map
+        for a shared vector, a per-sample mix of the three axis maps otherwise."""
+        if isinstance(vec, tuple):
+            return self._csr(spec, vec, tr, transpose)(x)
+        out = None
+        shape = (x.shape[0],) + (1,) * (x.dim() - 1)
+        for a in range(3):
+            y = self._csr(spec, tuple(np.eye(3)[a]), tr, transpose)(x)
+            y = y * vec[:, a].view(shape)
+            out = y if out is None else out + y
+        return out
+
+    def _bra(self, spec, vec, tr, S):
+        """Bra vector of the dipole operator: (n,) shared or (S, n) per sample."""
+        if isinstance(vec, tuple):
+            v = self._op(spec, vec, tr).bra_vector
+            return torch.as_tensor(np.asarray(v, dtype=complex),
+                                   dtype=torch.complex128).cuda()
+        basis = torch.as_tensor(np.array(
+            [np.asarray(self._op(spec, tuple(np.eye(3)[a]), tr).bra_vector, dtype=complex)
+             for a in range(3)]), dtype=torch.complex128).cuda()
+        return torch.einsum('sa,an->sn', vec.to(basis.dtype), basis).contiguous()
+
+    def _ket0(self, spec, vec, tr):
+        """Dipole commutator on the ground state: (n,) or (S, n)."""
+        rho0 = torch.ones(1, dtype=torch.complex128, device='cuda')
+        if isinstance(vec, tuple):
+            return self._csr(spec, vec, tr)(rho0)
+        basis = torch.stack([self._csr(spec, tuple(np.eye(3)[a]), tr)(rho0)
+                             for a in range(3)])
+        return torch.einsum('sa,an->sn', vec.to(basis.dtype), basis).contiguous()
 
     # -------------------------------------------------------------- builds
     def _f_operators(self, batch, build_e, cdt):
@@ -181,16 +245,25 @@ class ThirdOrderEngine:
         return Q
 
     # ----------------------------------------------------------------- run
-    def run(self, offsets, events=None):
+    def run(self, offsets, events=None, rotations=None):
         """Summed response over the samples with the given site-energy offsets
-        ((S, N) float64, CUDA or host)."""
+        ((S, N) float64, CUDA or host); ``rotations`` (S, 3, 3) rotates each
+        sample's dipoles."""
         _native.require_gpu()
         model, N = self.model, self.N
         prec = self.prec
         cdt = torch.complex64 if prec == _native.QSX_FP32 else torch.complex128
         uc, dt = model.unit_convert, self.dt
-        pol = self.polarization
         S = len(offsets)
+        ch = self._channels(S, None if rotations is None else np.asarray(rotations, float))
+        Tw = self.coupling
+        # (a, b) x (c, d) channel pairs that meet with a nonzero weight
+        left = [(a, b) for a in range(Tw.shape[0]) for b in range(Tw.shape[1])
+                if np.any(Tw[a, b])]
+        right = sorted({(c, d) for a, b in left for c in range(Tw.shape[2])
+                        for d in range(Tw.shape[3]) if Tw[a, b, c, d]})
+        ch0 = sorted({a for a, _ in left})
+        ch3 = sorted({d for _, d in right})
         batch = SampleBatch(model, S, offsets=offsets)
         ham = model.hamiltonian
         _tick(events, 'build')
@@ -205,33 +278,51 @@ class ThirdOrderEngine:
         _tick(events, 't3')
         # ---- t3 legs (Heisenberg picture), shared by the geometries
         T3 = len(self.t3)
-        y_eg = self._bra('eg->gg', pol[3], '-')
         D3 = build.propagator(self._idx('eg'), dt, prec, transpose=True)
-        v_eg = _native.rk4(D3, y_eg, T3 - 1, 1, h=dt, precision=prec,
-                           state=True)['state']                       # (S, T3, N)
-        W = None
-        if 'ESE' in self.signals:
-            W = self._csr('ee->eg', pol[2], '+', transpose=True)(v_eg)  # (S, T3, N^2)
+        v_eg, v_fe = {}, {}
+        for d in ch3:
+            y_eg = self._bra('eg->gg', ch[3][d], '-', S)
+            v_eg[d] = _native.rk4(D3, y_eg, T3 - 1, 1, h=dt, precision=prec,
+                                  state=True)['state']                    # (S, T3, N)
+            if need_fe:
+                y_fe = self._bra('fe->ee', ch[3][d], '-', S)
+                v_fe[d] = _native.fe_heisenberg_rk4(Q, Ae, Me, self._pair_sites, y_fe,
+                                                    T3 - 1, dt, prec)     # (S, T3, P N)
         if need_fe:
-            y_fe = self._bra('fe->ee', pol[3], '-')
-            v_fe = _native.fe_heisenberg_rk4(Q, Ae, Me, self._pair_sites, y_fe, T3 - 1, dt,
-                                             prec)                     # (S, T3, P N)
             del Q
-            w = self._csr('ee->fe', pol[2], '+', transpose=True)(v_fe)
-            del v_fe
-            W = w if W is None else W + w
-        g3 = None
-        if 'GSB' in self.signals:
-            g3 = self._csr('gg->eg', pol[2], '+', transpose=True)(v_eg)[..., 0]  # (S, T3)
+        W, g3 = {}, {}
+        for c, d in right:
+            w = None
+            if 'ESE' in self.signals:
+                w = self._apply('ee->eg', '+', ch[2][c], v_eg[d], transpose=True)
+            if need_fe:
+                wf = self._apply('ee->fe', '+', ch[2][c], v_fe[d], transpose=True)
+                w = wf if w is None else w + wf
+            if w is not None:
+                W[c, d] = w                                               # (S, T3, N^2)
+            if 'GSB' in self.signals:
+                g3[c, d] = self._apply('gg->eg', '+', ch[2][c], v_eg[d],
+                                       transpose=True)[..., 0]            # (S, T3)
+        del v_fe
+        # t3 states of each (a, b) channel pair, weighted by the coupling
+        Wc, gc = [], []
+        for a, b in left:
+            terms = [(Tw[a, b, c, d], cd) for cd in right for c, d in [cd] if Tw[a, b, c, d]]
+            if W:
+                Wc.append(sum(float(t) * W[cd] for t, cd in terms).to(cdt).transpose(1, 2))
+            if g3:
+                gc.append(sum(float(t) * g3[cd] for t, cd in terms))
+        del W
+        Wt = torch.stack(Wc, 1).contiguous() if Wc else None          # (S, L, N^2, T3)
         _tick(events, 't2')
         # ---- t2 propagator powers on the 'ee' block
         gaps = [int(k) for k in self.gaps]
         # P^g - I for g = gcd of the gaps; each gap then applies it gap/g
-        # times to the (S, T1, N^2) block of t1 states (a matrix-block product
-        # costs T1/N^2 of a matrix-matrix product)
+        # times to the (S, L T1, N^2) block of t1 states (a matrix-block
+        # product costs L T1/N^2 of a matrix-matrix product)
         base = int(np.gcd.reduce([k for k in gaps if k] or [1]))
         Xg = None
-        if W is not None and any(gaps):
+        if Wt is not None and any(gaps):
             Lee = build.block(self._idx('ee'))
             A = (dt * Lee).to(cdt)
             del Lee
@@ -240,31 +331,37 @@ class ThirdOrderEngine:
             del A, A2
             Xg = powers_minus_identity(D, [base])[base].transpose(1, 2).contiguous()
             del D
-        Dgg = build.propagator(self._idx('gg'), dt, prec)[:, 0, 0] if g3 is not None else None
+        Dgg = build.propagator(self._idx('gg'), dt, prec)[:, 0, 0] if gc else None
         _tick(events, 't1')
         out = {}
         T1 = len(self.t1)
+        nL = len(left)
         for geo in self.geometries:
             sub1 = 'ge' if geo == '-++' else 'eg'
-            rho0 = torch.ones(1, dtype=torch.complex128, device='cuda')
-            v0 = self._csr('gg->' + sub1, pol[0], geo[0])(rho0)         # (N,)
             D1 = build.propagator(self._idx(sub1), dt, prec)
-            rho1 = _native.rk4(D1, v0, T1 - 1, 1, h=dt, precision=prec,
-                               state=True)['state']                     # (S, T1, N)
+            rho1 = {}
+            for a in ch0:
+                v0 = self._ket0('gg->' + sub1, ch[0][a], geo[0])          # (N,) / (S, N)
+                rho1[a] = _native.rk4(D1, v0, T1 - 1, 1, h=dt, precision=prec,
+                                      state=True)['state']                 # (S, T1, N)
             total = torch.zeros((T1, len(gaps), T3), dtype=torch.complex128, device='cuda')
-            if W is not None:
-                r = self._csr(sub1 + '->ee', pol[1], geo[1])(rho1).to(cdt)  # (S, T1, N^2)
-                Wt = W.to(cdt).transpose(1, 2)                           # (S, N^2, T3)
+            if Wt is not None:
+                r = torch.stack([self._apply(sub1 + '->ee', geo[1], ch[1][b], rho1[a])
+                                 for a, b in left], 1).to(cdt)             # (S, L, T1, N^2)
+                r = r.view(S, nL * T1, N * N)
+                Wv = Wt.view(S * nL, N * N, T3)
                 for j, k in enumerate(gaps):
                     for _ in range(k // base):
                         r = r + torch.bmm(r, Xg)
-                    total[:, j, :] += torch.bmm(r, Wt).to(torch.complex128).sum(0)
-            if g3 is not None:
-                rgg = self._csr(sub1 + '->gg', pol[1], geo[1])(rho1)[..., 0]  # (S, T1)
-                for j, k in enumerate(gaps):
-                    if k:
-                        rgg = rgg * (1 + Dgg[:, None]) ** k
-                    total[:, j, :] += torch.einsum('sa,sc->ac', rgg, g3)
+                    part = torch.bmm(r.view(S * nL, T1, N * N), Wv)
+                    total[:, j, :] += part.to(torch.complex128).sum(0)
+            if gc:
+                for (a, b), g in zip(left, gc):
+                    rgg = self._apply(sub1 + '->gg', geo[1], ch[1][b], rho1[a])[..., 0]
+                    for j, k in enumerate(gaps):
+                        if k:
+                            rgg = rgg * (1 + Dgg[:, None]) ** k
+                        total[:, j, :] += torch.einsum('sa,sc->ac', rgg, g)
             out[geo] = total
         _tick(events, 'end')
         return out
@@ -279,21 +376,29 @@ def _tick(events, name):
 
 def third_order_ensemble(model, coherence_time_max, population_times, geometry='-++',
                          polarization='xxxx', include_signal=None, ensemble_size=None,
-                         precision='fp64', chunk=None):
+                         precision='fp64', chunk=None, isotropic=False,
+                         random_orientations=False):
     """(t1, t2, t3), mean response of one geometry over the disorder samples
-    0 .. ensemble_size-1 (or of the model itself when ensemble_size is None)."""
+    0 .. ensemble_size-1 (or of the model itself when ensemble_size is None).
+    ``isotropic`` gives the exact isotropic average; ``random_orientations``
+    rotates each sample's dipoles with the reference's draws."""
     eng = ThirdOrderEngine(model, coherence_time_max, population_times, polarization,
-                           include_signal, precision, geometries=(geometry,))
+                           include_signal, precision, geometries=(geometry,),
+                           isotropic=isotropic)
     ham = model.hamiltonian
+    rotations = None
     if ensemble_size is None:
         offsets = np.zeros((1, ham.n_sites))
         count = 1
     else:
         offsets = ham.disorder_offsets(ensemble_size)
         count = ensemble_size
+        if random_orientations:
+            rotations = ham.orientation_rotations(ensemble_size)
     chunk = chunk or len(offsets)
     total = None
     for s0 in range(0, len(offsets), chunk):
-        part = eng.run(offsets[s0:s0 + chunk])[geometry]
+        rot = None if rotations is None else rotations[s0:s0 + chunk]
+        part = eng.run(offsets[s0:s0 + chunk], rotations=rot)[geometry]
         total = part if total is None else total + part
     return (eng.t1, eng.t2, eng.t3), (total / count).cpu().numpy()

@@ -52,7 +52,23 @@ def rk4_harness(step):
     return integrate
 
 
+def python3_shims():
+    """The reference's decorators call inspect.getargspec, which Python 3.11
+    removed; give it back as a view of getfullargspec (same fields, with
+    ``keywords`` named ``varkw`` there) so the reference runs unmodified."""
+    import inspect
+    from collections import namedtuple
+    if not hasattr(inspect, 'getargspec'):
+        ArgSpec = namedtuple('ArgSpec', 'args varargs keywords defaults')
+
+        def getargspec(func):
+            spec = inspect.getfullargspec(func)
+            return ArgSpec(spec.args, spec.varargs, spec.varkw, spec.defaults)
+        inspect.getargspec = getargspec
+
+
 def main(ref_root):
+    python3_shims()
     sys.path.insert(0, ref_root)
     sys.path.insert(0, ROOT)
     warnings.simplefilter('ignore')
@@ -150,6 +166,46 @@ def main(ref_root):
     out['fields_two_t'] = t
     out['fields_two_states'] = st
 
+    # orientation averages on a 4-site model with non-parallel dipoles:
+    # random ensemble orientations (hamiltonian.py:552-575) and exact
+    # isotropic averages (decorators.py:67-125)
+    H4 = wl.chain_hamiltonian(n_sites=4, seed=11)
+    extra4 = wl.energy_spread_for_dt(H4, 1.0, qs.CM_FS)
+    dip4 = [[1.0, 0, 0], [0.3, 0.9, 0.1], [-0.5, 0.4, 0.7], [0.2, -0.6, 0.5]]
+    ham4 = qs.ElectronicHamiltonian(H4, bath=bath77, dipoles=dip4,
+                                    disorder=wl.fwhm_for_sd(40.0), random_seed=3,
+                                    energy_spread_extra=extra4)
+    m4 = qs.RedfieldModel(ham4, hilbert_subspace='ge', unit_convert=qs.CM_FS,
+                          secular=False)
+    assert m4.time_step == 1.0, m4.time_step
+    out['ori4_H'] = H4
+    out['ori4_extra'] = extra4
+    out['ori4_dipoles'] = np.array(dip4)
+    out['ori4_sample_dipoles'] = np.array(
+        [h.dipoles for h in ham4.sample_ensemble(4, random_orientations=True)])
+    f, X = qs.absorption_spectra(m4, 512.0, ensemble_size=4,
+                                 ensemble_random_orientations=True)
+    out['ori4_abs_f'] = f
+    out['ori4_abs_rand'] = X
+    f, X = qs.absorption_spectra(m4, 512.0, polarization=[0.3, 'x'],
+                                 exact_isotropic_average=True)
+    out['ori4_abs_iso'] = X
+    f, X = qs.absorption_spectra(m4, 512.0, ensemble_size=3,
+                                 ensemble_random_orientations=True,
+                                 exact_isotropic_average=True)
+    out['ori4_abs_iso_rand'] = X
+    pump4 = qs.GaussianPulse(carrier_freq=float(np.mean(np.diag(H4))), fwhm=20.0,
+                             t_peak=0.0, scale=1e-2, freq_convert=qs.CM_FS)
+    t, st = qs.simulate_pump(m4, pump4, polarization=0.5, time_extra=30.0,
+                             exact_isotropic_average=True)
+    out['ori4_pump_iso_t'] = t
+    out['ori4_pump_iso'] = st
+    t, st = qs.simulate_with_fields(m4, [p1, p2], geometry='-+', polarization='xy',
+                                    time_extra=30.0, ensemble_size=3,
+                                    ensemble_random_orientations=True)
+    out['ori4_fields_rand_t'] = t
+    out['ori4_fields_rand'] = st
+
     # tight zvode for the integrator gap (reference as shipped)
     qeom.integrate = qutils.integrate
     qresp.integrate = qutils.integrate
@@ -179,6 +235,32 @@ def main(ref_root):
             geometry=geo)
         out['chain3_3rd_' + geo] = S
     out['chain3_t1'] = t1
+    dip3 = [[1.0, 0, 0], [0.4, 0.8, 0.0], [-0.3, 0.5, 0.6]]
+    ham3o = qs.ElectronicHamiltonian(H3, bath=bath300, dipoles=dip3,
+                                     disorder=wl.fwhm_for_sd(30.0), random_seed=5,
+                                     energy_spread_extra=extra3)
+    m3o = qs.RedfieldModel(ham3o, hilbert_subspace='gef', unit_convert=qs.CM_FS,
+                           secular=False)
+    assert m3o.time_step == 2.0
+    out['ori3_dipoles'] = np.array(dip3)
+    t2s = [0.0, 20.0, 50.0]
+    _, S = qs.third_order_response(m3o, coherence_time_max=40.0, population_times=t2s,
+                                   geometry='-++', polarization=[0, 0, 0.5, 0.5],
+                                   exact_isotropic_average=True)
+    out['ori3_3rd_iso_-++'] = S
+    _, S = qs.third_order_response(m3o, coherence_time_max=40.0, population_times=t2s,
+                                   geometry='+-+', polarization='xxyy',
+                                   exact_isotropic_average=True)
+    out['ori3_3rd_isoxxyy_+-+'] = S
+    _, S = qs.third_order_response(m3o, coherence_time_max=40.0, population_times=t2s,
+                                   geometry='-++', polarization='xyxz', ensemble_size=3,
+                                   ensemble_random_orientations=True)
+    out['ori3_3rd_rand_-++'] = S
+    _, S = qs.third_order_response(m3o, coherence_time_max=40.0, population_times=t2s,
+                                   geometry='+-+', polarization='xxxx', ensemble_size=2,
+                                   ensemble_random_orientations=True,
+                                   exact_isotropic_average=True)
+    out['ori3_3rd_iso_rand_+-+'] = S
 
     # ---- HEOM generators (heom.py:298-443) --------------------------------
     H2 = np.array([[12400., -100], [-100, 12480]])

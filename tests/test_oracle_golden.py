@@ -155,3 +155,92 @@ def test_fields_oracle_matches_reference(golden):
     ticks, st = orc.ensemble_average(om, 3, orc.simulate_with_fields, [p1, p2], '-+', 'xy',
                                      40.0)
     assert rel_err(st, golden['fields_two_states']) < 1e-12
+
+
+def ori4_model(golden):
+    bath = orc.DebyeBathSpec(orc.CM_K * 77, 35, 106)
+    ham = orc.ElectronicHamiltonianSpec(golden['ori4_H'], dipoles=golden['ori4_dipoles'],
+                                        disorder=wl.fwhm_for_sd(40.0), random_seed=3,
+                                        energy_spread_extra=float(golden['ori4_extra']),
+                                        bath=bath)
+    return orc.RedfieldSpec(ham, bath, 'ge', CM_FS, secular=False)
+
+
+def test_random_orientation_draws(golden):
+    """Sample n's dipoles are R_n d_i with R_n drawn after the disorder
+    (hamiltonian.py:552-575, polarization.py:87-102)."""
+    m = ori4_model(golden)
+    dips = np.array([m.sample(n, True).ham.dipoles for n in range(4)])
+    assert np.abs(dips - golden['ori4_sample_dipoles']).max() < 1e-14
+
+
+def test_orientation_averaged_absorption(golden):
+    """Random ensemble orientations and the exact second-order isotropic
+    average of the absorption spectrum (decorators.py:40-64, 95-125)."""
+    m = ori4_model(golden)
+
+    def spectrum(x):
+        t = orc.time_grid(512.0, m.time_step)
+        return orc.fourier_transform(t, -x, rw_freq=m.ham.rw_freq,
+                                     unit_convert=m.unit_convert)[1].real
+
+    _, x = orc.ensemble_average(m, 4, orc.linear_response, 512.0, random_orientations=True)
+    assert rel_err(spectrum(x), golden['ori4_abs_rand']) < 1e-11
+    _, x = orc.isotropic_average_2nd(orc.linear_response, [0.3, 'x'], m, 512.0)
+    assert rel_err(spectrum(x), golden['ori4_abs_iso']) < 1e-11
+
+    def iso(model, time_max):
+        return orc.isotropic_average_2nd(orc.linear_response, 'xx', model, time_max)
+    _, x = orc.ensemble_average(m, 3, iso, 512.0, random_orientations=True)
+    assert rel_err(spectrum(x), golden['ori4_abs_iso_rand']) < 1e-11
+
+
+def test_orientation_averaged_fields(golden):
+    m = ori4_model(golden)
+    pump = orc.GaussianPulseSpec(float(np.mean(np.diag(golden['ori4_H']))), 20.0, 0.0,
+                                 1e-2, orc.CM_FS)
+
+    def pumped(model, polarization):
+        return orc.simulate_with_fields(model, [pump, pump], '-+', polarization, 30.0)
+    t, st = orc.isotropic_average_2nd(pumped, [0.5, 0.5], m)
+    assert np.allclose(t, golden['ori4_pump_iso_t'], rtol=0, atol=1e-12)
+    assert rel_err(st, golden['ori4_pump_iso']) < 1e-12
+    p1 = orc.GaussianPulseSpec(12250.0, 15.0, -10.0, 5e-3, orc.CM_FS)
+    p2 = orc.GaussianPulseSpec(12450.0, 25.0, 20.0, 8e-3, orc.CM_FS)
+    t, st = orc.ensemble_average(m, 3, orc.simulate_with_fields, [p1, p2], '-+', 'xy',
+                                 30.0, random_orientations=True)
+    assert np.allclose(t, golden['ori4_fields_rand_t'], rtol=0, atol=1e-12)
+    assert rel_err(st, golden['ori4_fields_rand']) < 1e-12
+
+
+def ori3_model(golden):
+    bath = orc.DebyeBathSpec(orc.CM_K * 300, 40, 100)
+    ham = orc.ElectronicHamiltonianSpec(golden['chain3_H'], dipoles=golden['ori3_dipoles'],
+                                        disorder=wl.fwhm_for_sd(30.0), random_seed=5,
+                                        energy_spread_extra=float(golden['chain3_extra']),
+                                        bath=bath)
+    return orc.RedfieldSpec(ham, bath, 'gef', CM_FS, secular=False)
+
+
+@pytest.mark.parametrize('key,geo,pol,ens,rand,iso', [
+    ('ori3_3rd_iso_-++', '-++', [0, 0, 0.5, 0.5], None, False, True),
+    ('ori3_3rd_isoxxyy_+-+', '+-+', 'xxyy', None, False, True),
+    ('ori3_3rd_rand_-++', '-++', 'xyxz', 3, True, False),
+    ('ori3_3rd_iso_rand_+-+', '+-+', 'xxxx', 2, True, True)])
+def test_orientation_averaged_third_order(golden, key, geo, pol, ens, rand, iso):
+    """Fourth-order isotropic average (decorators.py:67-92, invariants with
+    weight <= 1e-8 dropped as there) and random ensemble orientations."""
+    m = ori3_model(golden)
+    t2 = [0.0, 20.0, 50.0]
+
+    def one(model, polarization):
+        if iso:
+            return orc.isotropic_average_4th(orc.third_order_response, polarization, model,
+                                             40.0, t2, geometry=geo)
+        return orc.third_order_response(model, 40.0, t2, geometry=geo,
+                                        polarization=polarization)
+    if ens is None:
+        _, S = one(m, pol)
+    else:
+        _, S = orc.ensemble_average(m, ens, one, pol, random_orientations=rand)
+    assert rel_err(S, golden[key]) < 1e-11
