@@ -297,6 +297,60 @@ int qsx_rk4_field_batched(const void* L, int64_t L_stride, const void* C,
                           void* stream);
 
 /*
+ * ZOFE master equation (qspectra/dynamics/zofe.py:121-229), the time loop of
+ * a ZOFEModel, optionally under applied fields (simulate/eom.py:77-105).
+ * The state vector is the reference's: rho (n x n, column-major) followed by
+ * the auxiliary operators O (npm, n_sites, n, n) in column-major order, i.e.
+ * O[pm][s][k][l] at n*n + pm + npm (s + n_sites (k + n l)).  The right-hand
+ * side (unit_convert times)
+ *   rho' = b rho + sum_s L_s rho S_s^H + rho (i H - a^H) + sum_s S_s rho L_s^H
+ *   O'   = Gamma[pm][s] L_s - w[pm][s] O + b O - O b
+ * with S_s = sum_pm O[pm][s], a = sum_s L_s^H S_s, b = -i H - a, L_s =
+ * diag(Ld[s]) (the system-bath couplings carrying the ZOFE sign: minus the
+ * site number operators), plus sum_p a_p(t) [V_p, .] on rho and on every O
+ * for pulses, not scaled by unit_convert (a_p tabulated at t_n, t_n + h/2, t_n + h as for
+ * qsx_rk4_field_batched).  Fixed-step RK4; FP32 keeps a split-word state.
+ * One thread-block cluster per sample splits the pseudomodes over its CTAs
+ * (cluster 0 = chosen by the library); n <= 32 and at most 4096 state
+ * elements per CTA.
+ */
+typedef struct {
+  int32_t precision;     /* QSX_FP64 or QSX_FP32 */
+  int32_t n;             /* Hilbert-space states */
+  int32_t n_sites;       /* sites (couplings L_s) */
+  int32_t npm;           /* pseudomodes */
+  int32_t nsteps;        /* RK4 steps */
+  int32_t save_every;    /* output every save_every steps */
+  int32_t npulses;       /* field terms, 0 = free evolution */
+  int32_t nproj;         /* projections of rho saved instead of (or beside) states */
+  int32_t mode;          /* 0: RK4 loop; 1: evaluate the right-hand side at y0 once */
+  int32_t cluster;       /* CTAs per sample, 0 = library's choice, else 1..8 */
+  int64_t batch;         /* samples */
+  const double* H;       /* real [n][n] rotating-frame Hamiltonian */
+  int64_t H_stride;      /* elements between samples, 0 = shared */
+  const double* Ld;      /* real [n_sites][n] diagonals of L_s */
+  const double* Gamma;   /* complex128 [npm][n_sites], Omega^2 huang */
+  const double* w;       /* complex128 [npm][n_sites], i Omega + gamma */
+  const double* V;       /* complex128 [npulses][n][n] row-major dipole operators */
+  int64_t V_stride;      /* elements between samples, 0 = shared */
+  const double* coef;    /* complex128 [nsteps][3][npulses] (mode 1: [1][3][npulses]) */
+  const double* proj;    /* complex128 [nproj][n*n] rows over rho (column-major) */
+  double unit_convert;
+  double h;              /* RK4 step */
+  const double* y0;      /* complex128 [batch][M], M = n^2 + npm n_sites n^2 */
+  int64_t y0_stride;     /* elements between samples, 0 = shared */
+  double* out_state;     /* complex128 [batch][nsteps/save_every + 1][M] or NULL;
+                            mode 1: [batch][M], the right-hand side */
+  double* out_proj;      /* complex128 [batch][nsteps/save_every + 1][nproj] or NULL */
+  int32_t* status;       /* device int: QSX_ERR_NONFINITE on NaN/Inf */
+  int32_t reserved;      /* must be 0 */
+  int32_t pad;
+} qsx_zofe_args;
+
+size_t qsx_zofe_args_bytes(void);
+int qsx_zofe_rk4(const qsx_zofe_args* args, void* stream);
+
+/*
  * Batched FP64 symmetric eigensolver for n up to 2048 (the two-exciton
  * block; the reference calls scipy.linalg.eigh per sample,
  * qspectra/hamiltonian.py:310-328): Householder tridiagonalisation (one CTA

@@ -965,3 +965,146 @@ def rk4_integrate_sparse(L, y0, nsteps, h, save_every=1):
         if s % save_every == 0:
             out.append(y.copy())
     return np.array(out)
+
+
+# --------------------------------------------------------------------------
+# ZOFE master equation (qspectra/dynamics/zofe.py)
+# --------------------------------------------------------------------------
+class ZOFESpec:
+    """ZOFE model with one pseudomode bath per site (zofe.py:44-229).
+
+    The state is rho (n x n) followed by the auxiliary operators
+    O (npm, n_sites, n, n), both flattened column-major (zofe.py:101-119).
+    ``Omega``, ``gamma``, ``huang`` are (npm, n_sites).
+    """
+
+    def __init__(self, ham, Omega, gamma, huang, hilbert_subspace='ge', unit_convert=1.0):
+        self.ham = ham
+        self.Omega = np.asarray(Omega, complex)
+        self.gamma = np.asarray(gamma, complex)
+        self.huang = np.asarray(huang, complex)
+        self.hilbert_subspace = hilbert_subspace
+        self.unit_convert = unit_convert
+        self.npm = self.Omega.shape[0]
+        self.n = len(site_states(ham.n_sites, hilbert_subspace))
+        self.oop_shape = (self.npm, ham.n_sites, self.n, self.n)
+
+    def sample(self, n, random_orientations=False):
+        return ZOFESpec(self.ham.sample(n, random_orientations), self.Omega, self.gamma,
+                        self.huang, self.hilbert_subspace, self.unit_convert)
+
+    @property
+    def time_step(self):
+        return self.ham.time_step(self.unit_convert)
+
+    def split(self, y):
+        n2 = self.n * self.n
+        return (y[:n2].reshape((self.n, self.n), order='F'),
+                y[n2:].reshape(self.oop_shape, order='F'))
+
+    def join(self, rho, oop):
+        return np.concatenate([rho.reshape(-1, order='F'), oop.reshape(-1, order='F')])
+
+    def rhs(self, y):
+        """zofe.py:121-202 (rho_hermit = ham_hermit = False), times
+        unit_convert; L_n = -(number operators) (zofe.py:219-222)."""
+        rho, oop = self.split(y)
+        H = self.ham.H(self.hilbert_subspace)
+        L = -np.array([np.diag(o) for o in occupations(self.ham.n_sites,
+                                                        self.hilbert_subspace)])
+        Gamma = self.Omega ** 2 * self.huang
+        w = 1j * self.Omega + self.gamma
+        S = oop.sum(axis=0)
+        Lh = np.conj(np.transpose(L, (0, 2, 1)))
+        a = np.einsum('sij,sjk->ik', Lh, S)
+        b = -1j * H - a
+        c = np.einsum('sij,jk,smk->im', L, rho, np.conj(S))
+        big = np.einsum('sij,jk,skm->im', S, rho, Lh)
+        rhodot = b @ rho + c + rho @ (1j * H - a.conj().T) + big
+        oopdot = (Gamma[:, :, None, None] * L[None]
+                  - w[:, :, None, None] * oop
+                  + np.einsum('kj,psjl->pskl', b, oop)
+                  - np.einsum('pskj,jl->pskl', oop, b))
+        return self.unit_convert * self.join(rhodot, oopdot)
+
+    def thermal_state(self, _=None):
+        """Ground state (a pseudomode bath has no temperature,
+        hamiltonian.py:164-175) with zero auxiliary operators."""
+        H = extend_operator(self.ham.H1, self.hilbert_subspace)
+        E, U = scipy.linalg.eigh(H)
+        rho = np.outer(U[:, 0], U[:, 0].conj())
+        return self.join(rho.astype(complex), np.zeros(self.oop_shape, complex))
+
+    def dipole(self, polarization, transitions):
+        return dipole_operator(self.ham.dipoles, self.hilbert_subspace, polarization,
+                               transitions)
+
+    def commutator(self, A, y):
+        """[A, .] on rho and on every auxiliary operator (zofe.py:22-33)."""
+        rho, oop = self.split(y)
+        return self.join(A @ rho - rho @ A, A @ oop - oop @ A)
+
+    def expectation(self, A, y):
+        rho, _ = self.split(y)
+        return np.trace(A @ rho)
+
+
+def rk4_nonlinear(f, y0, t, t0=None, h=None):
+    """Fixed-step RK4 for dy/dt = f(t, y), outputs at t (simulate/utils.py:16-109)."""
+    t = np.asarray(t, float)
+    y = np.array(y0, dtype=complex)
+    t0 = t[0] if t0 is None else t0
+    h = (t[1] - t[0]) if h is None else h
+    out, cur = [], t0
+    for ti in t:
+        for _ in range(int(round((ti - cur) / h))):
+            k1 = f(cur, y)
+            k2 = f(cur + h / 2, y + h / 2 * k1)
+            k3 = f(cur + h / 2, y + h / 2 * k2)
+            k4 = f(cur + h, y + h * k3)
+            y = y + h / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+            cur = cur + h
+        out.append(y.copy())
+    return np.array(out)
+
+
+def zofe_dynamics(model, psi_or_rho, duration):
+    """simulate_dynamics for a ZOFE model (eom.py:11-26): rho(t) (T, n, n)."""
+    rho0 = np.asarray(psi_or_rho)
+    if rho0.ndim == 1:
+        rho0 = np.outer(rho0.conj(), rho0)
+    y0 = model.join(rho0.astype(complex), np.zeros(model.oop_shape, complex))
+    t = time_grid(duration, model.time_step)
+    ys = rk4_nonlinear(lambda _, y: model.rhs(y), y0, t)
+    return t, np.array([model.split(y)[0] for y in ys])
+
+
+def zofe_linear_response(model, time_max, polarization='xx'):
+    """_linear_response without a Heisenberg picture (response.py:15-43):
+    -tr(V1 rho(t)) from rho(0) = [V0, rho_thermal] (the ZOFE maps ignore
+    Liouville subspaces, zofe.py:98-99)."""
+    t = time_grid(time_max, model.time_step)
+    V0 = model.dipole(polarization[0], '+')
+    V1 = model.dipole(polarization[1], '-')
+    y0 = model.commutator(V0, model.thermal_state())
+    ys = rk4_nonlinear(lambda _, y: model.rhs(y), y0, t)
+    return t, -np.array([model.expectation(V1, y) for y in ys])
+
+
+def zofe_with_fields(model, pulses, geometry='-+', polarization='xx', time_extra=0.0):
+    """_simulate_with_fields for a ZOFE model (eom.py:77-105)."""
+    V = [model.dipole(p, tr) for p, tr in zip(polarization, geometry)]
+    rw = model.ham.rw_freq
+
+    def f(t, y):
+        d = model.rhs(y)
+        for pulse, tr, A in zip(pulses, geometry, V):
+            E = pulse(t, rw)
+            if tr == '+':
+                E = np.conj(E)
+            d = d + (-1j * E) * model.commutator(A, y)
+        return d
+    t0 = min(p.t_init for p in pulses)
+    tf = max(p.t_final for p in pulses)
+    t = np.arange(t0, tf + time_extra, model.time_step)
+    return t, rk4_nonlinear(f, model.thermal_state(), t, t0=t0, h=model.time_step)

@@ -6,7 +6,7 @@ simulate_dynamics / linear_response / absorption_spectra /
 third_order_response, disorder ensembles and the Fourier transform, all
 computed by hand-written sm_103a kernels behind the C ABI in include/qsx.h.
 """
-from .bath import DebyeBath
+from .bath import DebyeBath, PseudomodeBath
 from .constants import CM_FS, CM_FS_LINEAR, CM_K, GAUSSIAN_SD_FWHM
 from .dynamics.base import DynamicalModel, SystemOperator
 from .dynamics.liouville_space import (EquationOfMotion, LiouvilleSpaceModel,
@@ -14,6 +14,7 @@ from .dynamics.liouville_space import (EquationOfMotion, LiouvilleSpaceModel,
                                        matrix_to_bra_vec, matrix_to_ket_vec)
 from .dynamics.heom import HEOMModel
 from .dynamics.redfield import RedfieldModel
+from .dynamics.zofe import ZOFEModel
 from .hamiltonian import ElectronicHamiltonian, HamiltonianError
 from .operator_tools import (SubspaceError, all_states, basis_transform_operator,
                              basis_transform_vector, n_excitations, unit_vec)
@@ -29,7 +30,7 @@ from .simulate.utils import (IntegratorError, bound_signal, fourier_transform,
 from ._native import QsxError
 
 __all__ = [
-    'DebyeBath', 'CM_FS', 'CM_FS_LINEAR', 'CM_K', 'GAUSSIAN_SD_FWHM',
+    'DebyeBath', 'PseudomodeBath', 'ZOFEModel', 'CM_FS', 'CM_FS_LINEAR', 'CM_K', 'GAUSSIAN_SD_FWHM',
     'DynamicalModel', 'SystemOperator', 'EquationOfMotion',
     'LiouvilleSpaceModel', 'LiouvilleSpaceOperator', 'ket_vec_to_matrix',
     'matrix_to_bra_vec', 'matrix_to_ket_vec', 'RedfieldModel', 'HEOMModel',

@@ -68,6 +68,21 @@ class HeomArgs(ctypes.Structure):
     ]
 
 
+class ZofeArgs(ctypes.Structure):
+    _fields_ = [
+        ('precision', ctypes.c_int32), ('n', ctypes.c_int32), ('n_sites', ctypes.c_int32),
+        ('npm', ctypes.c_int32), ('nsteps', ctypes.c_int32), ('save_every', ctypes.c_int32),
+        ('npulses', ctypes.c_int32), ('nproj', ctypes.c_int32), ('mode', ctypes.c_int32),
+        ('cluster', ctypes.c_int32), ('batch', ctypes.c_int64),
+        ('H', _c_vp), ('H_stride', ctypes.c_int64), ('Ld', _c_vp), ('Gamma', _c_vp),
+        ('w', _c_vp), ('V', _c_vp), ('V_stride', ctypes.c_int64), ('coef', _c_vp),
+        ('proj', _c_vp), ('unit_convert', ctypes.c_double), ('h', ctypes.c_double),
+        ('y0', _c_vp), ('y0_stride', ctypes.c_int64), ('out_state', _c_vp),
+        ('out_proj', _c_vp), ('status', _c_vp), ('reserved', ctypes.c_int32),
+        ('pad', ctypes.c_int32),
+    ]
+
+
 _PROTOS = {
     'qsx_last_error_string': (ctypes.c_char_p, []),
     'qsx_version': (_c_int, []),
@@ -95,6 +110,8 @@ _PROTOS = {
     'qsx_rk4_batched': (_c_int, [ctypes.POINTER(Rk4Args), _c_vp]),
     'qsx_rk4_block_mean_noalloc': (_c_int, [ctypes.POINTER(Rk4Args), _c_vp]),
     'qsx_heom_args_bytes': (ctypes.c_size_t, []),
+    'qsx_zofe_args_bytes': (ctypes.c_size_t, []),
+    'qsx_zofe_rk4': (_c_int, [ctypes.POINTER(ZofeArgs), _c_vp]),
     'qsx_heom_workspace_bytes': (_c_int, [ctypes.POINTER(HeomArgs),
                                           ctypes.POINTER(ctypes.c_size_t)]),
     'qsx_heom_rhs': (_c_int, [ctypes.POINTER(HeomArgs), _c_vp, _c_vp, _c_vp]),
@@ -673,3 +690,78 @@ def rk4_field(L, C, coef, y0, nsteps, h, save_every=1, precision=QSX_FP64,
     if check_finite and int(status.item()) & QSX_ERR_NONFINITE:
         raise IntegratorError('non-finite state in the field-driven propagation')
     return out
+
+
+def zofe_rk4(H, Ld, Gamma, w, y0, nsteps, h, unit_convert, save_every=1,
+             precision=QSX_FP64, V=None, coef=None, proj=None, state=True, mode=0,
+             cluster=0, check_finite=True):
+    """ZOFE time loop (qsx_zofe_rk4).
+
+    H (n, n) or (B, n, n) float64; Ld (n_sites, n) float64; Gamma, w
+    (npm, n_sites) complex128; y0 (M,) or (B, M) complex128 in the reference's
+    state layout; V (np, n, n) or (B, np, n, n) and coef (nsteps, 3, np)
+    complex128 for pulses; proj (P, n*n) complex128 rows over rho.  Returns a
+    dict with 'state' (B, nsave, M) and/or 'proj' (B, nsave, P); mode 1
+    returns the right-hand side at y0 as 'rhs' (B, M).
+    """
+    require_gpu()
+    dev = y0.device
+    H = H.to(device=dev, dtype=torch.float64).contiguous()
+    Ld = Ld.to(device=dev, dtype=torch.float64).contiguous()
+    Gamma = Gamma.to(device=dev, dtype=torch.complex128).contiguous()
+    w = w.to(device=dev, dtype=torch.complex128).contiguous()
+    y0 = y0.to(torch.complex128).contiguous()
+    n = H.shape[-1]
+    npm, N = Gamma.shape
+    M = n * n + npm * N * n * n
+    if y0.shape[-1] != M:
+        raise ValueError('y0 must have {} components (n^2 + npm n_sites n^2)'.format(M))
+    if tuple(Ld.shape) != (N, n) or tuple(w.shape) != (npm, N):
+        raise ValueError('Ld must be (n_sites, n) and w (npm, n_sites)')
+    batches = [t.shape[0] for t, d in ((H, 3), (y0, 2)) if t.dim() == d]
+    if V is not None and V.dim() == 4:
+        batches.append(V.shape[0])
+    B = batches[0] if batches else 1
+    if any(b != B for b in batches):
+        raise ValueError('batch sizes do not match')
+    if nsteps % save_every:
+        raise ValueError('nsteps must be a multiple of save_every')
+    nsave = 1 if mode == 1 else nsteps // save_every + 1
+    keep = [H, Ld, Gamma, w, y0]
+    a = ZofeArgs()
+    a.precision, a.n, a.n_sites, a.npm = precision, n, N, npm
+    a.nsteps, a.save_every, a.mode, a.cluster = int(nsteps), int(save_every), int(mode), int(cluster)
+    a.batch = B
+    a.H, a.H_stride = H.data_ptr(), (n * n if H.dim() == 3 else 0)
+    a.Ld, a.Gamma, a.w = Ld.data_ptr(), Gamma.data_ptr(), w.data_ptr()
+    if V is not None:
+        V = V.to(device=dev, dtype=torch.complex128).contiguous()
+        coef = coef.to(device=dev, dtype=torch.complex128).contiguous()
+        a.npulses = V.shape[-3]
+        a.V, a.coef = V.data_ptr(), coef.data_ptr()
+        a.V_stride = a.npulses * n * n if V.dim() == 4 else 0
+        keep += [V, coef]
+    a.unit_convert, a.h = float(unit_convert), float(h)
+    a.y0, a.y0_stride = y0.data_ptr(), (M if y0.dim() == 2 else 0)
+    out = {}
+    if mode == 1:
+        out['rhs'] = torch.empty((B, M), dtype=torch.complex128, device=dev)
+        a.out_state = out['rhs'].data_ptr()
+    else:
+        if state:
+            out['state'] = torch.empty((B, nsave, M), dtype=torch.complex128, device=dev)
+            a.out_state = out['state'].data_ptr()
+        if proj is not None:
+            proj = proj.to(device=dev, dtype=torch.complex128).contiguous()
+            a.nproj = proj.shape[0]
+            a.proj = proj.data_ptr()
+            keep.append(proj)
+            out['proj'] = torch.empty((B, nsave, a.nproj), dtype=torch.complex128, device=dev)
+            a.out_proj = out['proj'].data_ptr()
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    a.status = status.data_ptr()
+    _check(load().qsx_zofe_rk4(ctypes.byref(a), _stream()), 'qsx_zofe_rk4')
+    if check_finite and int(status.item()) & QSX_ERR_NONFINITE:
+        raise IntegratorError('non-finite state in the ZOFE propagation')
+    return out
+

@@ -56,3 +56,19 @@ class DebyeBath:
     def corr_func_real(self, x):
         """(n(x)+1) J_anti(x) (bath.py:17-31)."""
         return self._corr(x, True)
+
+
+class PseudomodeBath:
+    """Bath given by pseudomodes, Lorentzians in the bath correlation spectrum
+    (bath.py:105-146): frequencies ``Omega``, widths ``gamma`` and couplings
+    ``huang``, each (numb_pm, n_sites) when the sites have separate baths.
+    Used by the ZOFE master equation."""
+
+    def __init__(self, numb_pm, Omega, gamma, huang):
+        self.numb_pm = numb_pm
+        self.Omega = Omega
+        self.gamma = gamma
+        self.huang = huang
+
+    def __repr__(self):
+        return 'PseudomodeBath(numb_pm={!r})'.format(self.numb_pm)

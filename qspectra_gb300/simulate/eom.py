@@ -22,6 +22,11 @@ def simulate_dynamics(dynamical_model, initial_state, duration=None, times=None,
     reference draws the rotation after the disorder: hamiltonian.py:552-575).
     """
     from ..dynamics.redfield import RedfieldModel
+    from ..dynamics.zofe import ZOFEModel
+    if (isinstance(dynamical_model, ZOFEModel) and save_func is None
+            and not integrate_kwargs.get('heom_nodes')):
+        return _zofe_dynamics(dynamical_model, initial_state, duration, times,
+                              ensemble_size, precision, integrate_kwargs.pop('step', None))
     if ensemble_size is not None:
         if (isinstance(dynamical_model, RedfieldModel) and times is None
                 and save_func is None and not integrate_kwargs):
@@ -56,6 +61,32 @@ def simulate_dynamics(dynamical_model, initial_state, duration=None, times=None,
     return t, dynamical_model.state_vector_to_density_matrix(states)
 
 
+def _zofe_dynamics(model, initial_state, duration, times, ensemble_size, precision, step):
+    """ZOFE free dynamics: only rho is read back (the projections of rho onto
+    its own entries), averaged over the samples in the same launch."""
+    from ..dynamics.zofe import ensemble_inputs
+    from .utils import PRECISIONS, uniform_save_plan
+    step = model.time_step if step is None else step
+    t = np.arange(0, duration, step) if times is None else np.asarray(times, float)
+    nsteps, every, first = uniform_save_plan(t, 0.0, step)
+    rho0 = np.asarray(initial_state)
+    if rho0.ndim == 1:
+        rho0 = np.outer(rho0.conj(), rho0)
+    dev = torch.device('cuda', torch.cuda.current_device())
+    y0 = torch.as_tensor(model.density_matrix_to_state_vector(rho0), device=dev)
+    if ensemble_size is None:
+        H = model.equation_of_motion().H
+    else:
+        H, _ = ensemble_inputs(model, ensemble_size)
+    n = model.n_states
+    Ld, G, w = model.zofe_tables()
+    eye = torch.eye(n * n, dtype=torch.complex128, device=dev)
+    out = _native.zofe_rk4(H, Ld, G, w, y0, nsteps, step, model.unit_convert, every,
+                           PRECISIONS[precision], proj=eye, state=False)['proj']
+    vec = out[:, first:].mean(0).cpu().numpy()          # (T, n*n), column-major rho
+    return t, vec.reshape(len(vec), n, n).transpose(0, 2, 1)
+
+
 def _field_table(pulses, geometry, rw_freq, t0, nsteps, h):
     """a_p at t_n, t_n + h/2, t_n + h: -i E_p(t), conjugated for '+'."""
     tn = t0 + h * np.arange(nsteps)
@@ -85,9 +116,11 @@ def simulate_with_fields(dynamical_model, pulses, geometry='-+', polarization='x
     """
     from .ensemble import SampleBatch, sample_polarizations
     from .utils import PRECISIONS, step_plan
-    if save_func is not None and not hasattr(save_func, 'matrix'):
-        raise TypeError('save_func must be a linear operator map')
+    from ..dynamics.zofe import ZOFEModel
     model = dynamical_model
+    if (save_func is not None and not hasattr(save_func, 'matrix')
+            and not isinstance(model, ZOFEModel)):
+        raise TypeError('save_func must be a linear operator map')
     prec = PRECISIONS[precision]
     h = integrate_kwargs.pop('step', model.time_step)
     t0 = min(p.t_init for p in pulses)
@@ -101,8 +134,21 @@ def simulate_with_fields(dynamical_model, pulses, geometry='-+', polarization='x
                          'the first pulse')
     first = int(steps[0])
     nsteps = int(steps[-1])
-    idx = model.liouville_subspace_index(liouville_subspace)
     dev = torch.device('cuda', torch.cuda.current_device())
+    coef = torch.as_tensor(_field_table(pulses, geometry, model.rw_freq, t0, nsteps, h),
+                           device=dev)
+    save_every = max(every, 1) if nsteps else 1
+    if isinstance(model, ZOFEModel):
+        states = _zofe_fields(model, polarization, geometry, coef, nsteps, h, save_every,
+                              ensemble_size, ensemble_random_orientations, prec)
+        states = states[:, first // save_every:]
+        states = states.mean(0) if ensemble_size is not None else states[0]
+        if save_func is not None:
+            states = save_func(states)
+        if isinstance(states, torch.Tensor):
+            states = states.cpu().numpy()
+        return t, states
+    idx = model.liouville_subspace_index(liouville_subspace)
     if ensemble_size is not None and ensemble_random_orientations:
         rot = model.hamiltonian.orientation_rotations(ensemble_size)
         q = torch.as_tensor(sample_polarizations(polarization, rot), device=dev)
@@ -115,8 +161,6 @@ def simulate_with_fields(dynamical_model, pulses, geometry='-+', polarization='x
              for pol, tr in zip(polarization, geometry)]
         C = torch.as_tensor(np.array([v.commutator_matrix for v in V], dtype=complex),
                             device=dev)
-    coef = torch.as_tensor(_field_table(pulses, geometry, model.rw_freq, t0, nsteps, h),
-                           device=dev)
     y0 = torch.as_tensor(np.asarray(model.thermal_state(liouville_subspace), dtype=complex),
                          device=dev)
     if ensemble_size is None:
@@ -124,7 +168,6 @@ def simulate_with_fields(dynamical_model, pulses, geometry='-+', polarization='x
     else:
         batch = SampleBatch(model, ensemble_size)
         L = model.build_batch(batch.H(model.hilbert_subspace)).block(idx)
-    save_every = max(every, 1) if nsteps else 1
     states = _native.rk4_field(L, C, coef, y0, nsteps, h, save_every, prec)
     states = states[:, first // save_every:]
     if ensemble_size is not None:
@@ -136,6 +179,36 @@ def simulate_with_fields(dynamical_model, pulses, geometry='-+', polarization='x
         if save_func.scalar:
             states = states[..., 0]
     return t, states.cpu().numpy()
+
+
+def _zofe_fields(model, polarization, geometry, coef, nsteps, h, save_every,
+                 ensemble_size, random_orientations, prec):
+    """States (B, nsave, M) of a ZOFE model under pulses (qsx_zofe_rk4 with
+    the dipole operators folded into its small operators)."""
+    from ..dynamics.zofe import ensemble_inputs
+    from .ensemble import sample_polarizations
+    dev = coef.device
+    if ensemble_size is None:
+        H = model.equation_of_motion().H
+        y0 = torch.as_tensor(model.thermal_state(), device=dev)
+    else:
+        H, y0 = ensemble_inputs(model, ensemble_size)
+    sub = model.hilbert_subspace
+    ham = model.hamiltonian
+    if ensemble_size is not None and random_orientations:
+        q = torch.as_tensor(sample_polarizations(
+            polarization, ham.orientation_rotations(ensemble_size)), device=dev)
+        basis = torch.as_tensor(np.array(
+            [[ham.dipole_operator(sub, a, tr) for a in np.eye(3)] for tr in geometry],
+            dtype=complex), device=dev)
+        V = torch.einsum('spa,pamn->spmn', q.to(basis.dtype), basis)
+    else:
+        V = torch.as_tensor(np.array([ham.dipole_operator(sub, p, tr)
+                                      for p, tr in zip(polarization, geometry)],
+                                     dtype=complex), device=dev)
+    Ld, G, w = model.zofe_tables()
+    return _native.zofe_rk4(H, Ld, G, w, y0, nsteps, h, model.unit_convert, save_every,
+                            prec, V=V, coef=coef)['state']
 
 
 def simulate_pump(dynamical_model, pump, polarization='x', time_extra=0, times=None,

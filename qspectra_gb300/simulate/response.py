@@ -9,6 +9,7 @@ import torch
 
 from ..polarization import (FOURTH_ORDER_INVARIANTS, check_polarizations,
                              invariant_polarizations, invariant_weights_4th_order)
+from .. import _native
 from .ensemble import ensemble_linear_signal
 from .utils import fourier_transform, integrate
 
@@ -63,6 +64,45 @@ def _single_linear_response(model, liouv_space_path, time_max, initial_state,
     return t, signal
 
 
+def _zofe_linear(model, time_max, ensemble_size, polarization, precision, rotations):
+    """Linear response of a ZOFE model (response.py:15-43; no Heisenberg
+    picture, zofe.py:211-213): -tr(V1 rho(t)) from rho(0) = [V0, rho_thermal],
+    every disorder sample in one launch, tr(V1 rho) reduced on the GPU."""
+    from ..dynamics.zofe import ZOFESpaceOperator, ensemble_inputs
+    from .ensemble import sample_polarizations
+    from .utils import PRECISIONS, uniform_save_plan
+    step = model.time_step
+    t = np.arange(0, time_max, step)
+    nsteps, every, first = uniform_save_plan(t, 0.0, step)
+    dev = torch.device('cuda', torch.cuda.current_device())
+    if ensemble_size is None:
+        H = model.equation_of_motion().H
+        y_th = torch.as_tensor(model.thermal_state(), device=dev)[None]
+    else:
+        H, y_th = ensemble_inputs(model, ensemble_size)
+    ham, sub = model.hamiltonian, model.hilbert_subspace
+    if rotations is None:
+        A0 = ZOFESpaceOperator(ham.dipole_operator(sub, polarization[0], '+'), None, model)
+        y0 = A0.commutator(y_th)
+        proj = torch.as_tensor(ham.dipole_operator(sub, polarization[1], '-').reshape(1, -1),
+                               dtype=torch.complex128, device=dev)
+    else:
+        q = torch.as_tensor(sample_polarizations(polarization, rotations), device=dev)
+        y0 = sum(q[:, 0, a, None] * ZOFESpaceOperator(
+            ham.dipole_operator(sub, np.eye(3)[a], '+'), None, model).commutator(y_th)
+            for a in range(3))
+        proj = torch.as_tensor(np.array([ham.dipole_operator(sub, np.eye(3)[a], '-').reshape(-1)
+                                         for a in range(3)]),
+                               dtype=torch.complex128, device=dev)
+    Ld, G, w = model.zofe_tables()
+    out = _native.zofe_rk4(H, Ld, G, w, y0.contiguous(), nsteps, step, model.unit_convert,
+                           every, PRECISIONS[precision], proj=proj, state=False)['proj']
+    out = out[:, first:]
+    if rotations is not None:
+        out = (out * q[:, None, 1, :].to(out.dtype)).sum(-1, keepdim=True)
+    return t, -out[..., 0].mean(0).cpu().numpy()
+
+
 def _isotropic(fn, polarization, order=2):
     pols = check_polarizations(polarization, order)
     weight = np.dot(*pols)
@@ -87,13 +127,19 @@ def linear_response(dynamical_model, liouv_space_path, time_max,
     reference's draws (hamiltonian.py:552-575).
     """
     from ..dynamics.redfield import RedfieldModel
+    from ..dynamics.zofe import ZOFEModel
     rotations = None
     if ensemble_size is not None and ensemble_random_orientations:
         rotations = dynamical_model.hamiltonian.orientation_rotations(ensemble_size)
     batched = (ensemble_size is not None and isinstance(dynamical_model, RedfieldModel)
                and initial_state is None and not integrate_kwargs)
+    zofe = (isinstance(dynamical_model, ZOFEModel) and initial_state is None
+            and not integrate_kwargs and ',' not in liouv_space_path.split('->')[1])
 
     def one(pol):
+        if zofe:
+            return _zofe_linear(dynamical_model, time_max, ensemble_size, pol, precision,
+                                rotations)
         if batched:
             t, sig = ensemble_linear_signal(dynamical_model, time_max, ensemble_size,
                                             pol, precision, path=liouv_space_path,

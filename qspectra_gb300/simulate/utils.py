@@ -101,9 +101,12 @@ def integrate(f, y0, t, t0=None, method_name='rk4', f_params=None,
     ``V.expectation_value``).  A 2-D ``y0`` integrates every row.
     """
     from ..dynamics.heom import HEOMEquationOfMotion
+    from ..dynamics.zofe import ZOFEEquationOfMotion
     if isinstance(f, HEOMEquationOfMotion):
         return _integrate_heom(f, y0, t, t0, save_func, precision, step,
                                kwargs.pop('heom_nodes', None))
+    if isinstance(f, ZOFEEquationOfMotion):
+        return _integrate_zofe(f, y0, t, t0, save_func, precision, step)
     if not isinstance(f, EquationOfMotion):
         raise TypeError('integrate needs an equation of motion returned by a '
                         'qspectra_gb300 model (got {!r})'.format(type(f)))
@@ -177,6 +180,63 @@ def _integrate_heom(f, y0, t, t0, save_func, precision, step, heom_nodes):
     if squeeze:
         state = state[0]
     return state.cpu().numpy() if as_numpy else state
+
+
+def uniform_save_plan(t, t0, step):
+    """(nsteps, save_every, first) for outputs on a uniform grid of RK4 steps
+    from t0: the kernel saves every save_every steps and the outputs start at
+    save index first."""
+    steps = step_plan(np.asarray(t, float), t0, step)
+    every = int(steps[1] - steps[0]) if len(steps) > 1 else max(int(steps[0]), 1)
+    every = max(every, 1)
+    if steps[0] % every or (len(steps) > 1 and np.any(np.diff(steps) != every)):
+        raise ValueError('output times must be evenly spaced on the RK4 step grid from t0')
+    return int(steps[-1]), every, int(steps[0]) // every
+
+
+def _integrate_zofe(f, y0, t, t0, save_func, precision, step):
+    """integrate() for the ZOFE master equation (qsx_zofe_rk4): uniform
+    outputs; an operator's expectation value is reduced on the GPU, other
+    save functions are applied to the saved states."""
+    from ..dynamics.zofe import ZOFESpaceOperator
+    t = np.asarray(t, float)
+    if t0 is None:
+        t0 = t[0]
+    if step is None:
+        step = (t[1] - t[0]) if len(t) > 1 else 1.0
+    nsteps, every, first = uniform_save_plan(t, t0, step)
+    as_numpy = not isinstance(y0, torch.Tensor)
+    y = torch.as_tensor(np.asarray(y0, dtype=complex) if as_numpy else y0,
+                        dtype=torch.complex128, device='cuda')
+    squeeze = y.dim() == 1
+    Y = y[None] if squeeze else y.reshape(-1, y.shape[-1])
+    Ld, G, w = f.model.zofe_tables()
+    owner = getattr(save_func, '__self__', None)
+    expect = (isinstance(owner, ZOFESpaceOperator)
+              and getattr(save_func, '__func__', None) is ZOFESpaceOperator.expectation_value)
+    proj = None
+    if expect:
+        proj = torch.as_tensor(owner.expectation_row[None], dtype=torch.complex128,
+                               device=Y.device)
+    res = _native.zofe_rk4(f.H, Ld, G, w, Y if Y.shape[0] > 1 else Y[0], nsteps, step,
+                           f.model.unit_convert, save_every=every,
+                           precision=_precision(precision), proj=proj, state=not expect)
+    if expect:
+        out = res['proj'][:, first:, 0]
+    else:
+        out = res['state'][:, first:]
+        if save_func is not None:
+            if isinstance(save_func, LinearMap):
+                out = out @ save_func.matrix.T
+                if save_func.scalar:
+                    out = out[..., 0]
+            else:
+                out = save_func(out)
+    if squeeze:
+        out = out[0]
+    else:
+        out = out.reshape(tuple(y.shape[:-1]) + tuple(out.shape[1:]))
+    return out.cpu().numpy() if as_numpy else out
 
 
 def is_constant(x, atol=1e-7, positive=None):

@@ -262,6 +262,59 @@ def main(ref_root):
                                    exact_isotropic_average=True)
     out['ori3_3rd_iso_rand_+-+'] = S
 
+    # ---- ZOFE master equation (dynamics/zofe.py) on a 3-site chain ---------
+    Hz = wl.chain_hamiltonian(n_sites=3, seed=13)
+    extraz = wl.energy_spread_for_dt(Hz, 2.0, qs.CM_FS)
+    zpm = dict(Omega=[-200.0, 30.0, 250.0], gamma=[100.0, 50.0, 150.0],
+               huang=[-5e-3, 0.8, 1e-2])
+    on = np.ones(3, complex)
+    pmb = qs.PseudomodeBath(3, np.array([x * on for x in zpm['Omega']]),
+                            np.array([x * on for x in zpm['gamma']]),
+                            np.array([x * on for x in zpm['huang']]))
+    dipz = [[1.0, 0, 0], [0.4, 0.8, 0.0], [-0.3, 0.5, 0.6]]
+    hamz = qs.ElectronicHamiltonian(Hz, bath=pmb, dipoles=dipz,
+                                    disorder=wl.fwhm_for_sd(30.0), random_seed=9,
+                                    energy_spread_extra=extraz)
+    mz = qs.ZOFEModel(hamz, hilbert_subspace='ge', unit_convert=qs.CM_FS)
+    assert mz.time_step == 2.0, mz.time_step
+    out['zofe3_H'] = Hz
+    out['zofe3_extra'] = extraz
+    out['zofe3_dipoles'] = np.array(dipz)
+    for k, v in zpm.items():
+        out['zofe3_' + k] = np.array(v)
+    qeom.integrate = rk4_harness(2.0)
+    qresp.integrate = rk4_harness(2.0)
+    t, rho = qs.simulate_dynamics(mz, [0, 1, 0, 0], 400.0)
+    out['zofe3_dyn_t'] = t
+    out['zofe3_dyn_rho'] = rho
+    mze = qs.ZOFEModel(hamz, hilbert_subspace='e', unit_convert=qs.CM_FS)
+    t, st = qs.simulate_dynamics(mze, [1, 0, 0], 200.0)
+    out['zofe3e_dyn_rho'] = st
+    t, x = qs.linear_response(mz, 'gg->eg->gg', 256.0)
+    out['zofe3_lin'] = x
+    f, X = qs.absorption_spectra(mz, 256.0)
+    out['zofe3_abs_X'] = X
+    f, X = qs.absorption_spectra(mz, 256.0, ensemble_size=3,
+                                 ensemble_random_orientations=True)
+    out['zofe3_abs_rand_X'] = X
+    pumpz = qs.GaussianPulse(carrier_freq=float(np.mean(np.diag(Hz))), fwhm=20.0,
+                             t_peak=0.0, scale=1e-2, freq_convert=qs.CM_FS)
+    t, st = qs.simulate_pump(mz, pumpz, polarization='x', time_extra=60.0)
+    out['zofe3_pump_t'] = t
+    out['zofe3_pump'] = st
+    mzf = qs.ZOFEModel(qs.ElectronicHamiltonian(Hz[:2, :2], bath=qs.PseudomodeBath(
+        3, np.array([x * on[:2] for x in zpm['Omega']]),
+        np.array([x * on[:2] for x in zpm['gamma']]),
+        np.array([x * on[:2] for x in zpm['huang']])), dipoles=dipz[:2],
+        energy_spread_extra=extraz), hilbert_subspace='gef', unit_convert=qs.CM_FS)
+    out['zofe2f_time_step'] = np.array(mzf.time_step)
+    qeom.integrate = rk4_harness(mzf.time_step)
+    qresp.integrate = rk4_harness(mzf.time_step)
+    _, S = qs.third_order_response(mzf, coherence_time_max=12 * mzf.time_step,
+                                   population_times=[0.0, 4 * mzf.time_step],
+                                   geometry='-++')
+    out['zofe2f_3rd'] = S
+
     # ---- HEOM generators (heom.py:298-443) --------------------------------
     H2 = np.array([[12400., -100], [-100, 12480]])
     hamh = qs.ElectronicHamiltonian(H2, bath=qs.DebyeBath(qs.CM_K * 300, 35, 106),

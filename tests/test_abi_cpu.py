@@ -55,3 +55,14 @@ def test_argument_validation_without_gpu(lib):
 def test_rk4_args_layout_matches_library(lib):
     assert ctypes.sizeof(_native.Rk4Args) == lib.qsx_rk4_args_bytes()
     assert _native.Rk4Args.batch.offset == 16
+
+
+def test_zofe_args_layout_matches_library(lib):
+    assert ctypes.sizeof(_native.ZofeArgs) == lib.qsx_zofe_args_bytes()
+    assert _native.ZofeArgs.batch.offset == 40
+    a = _native.ZofeArgs()
+    a.precision, a.n, a.n_sites, a.npm, a.nsteps, a.save_every = 0, 40, 2, 2, 4, 1
+    a.batch = 1
+    assert lib.qsx_zofe_rk4(ctypes.byref(a), None) == 1
+    assert b'bad sizes' in lib.qsx_last_error_string()
+

@@ -244,3 +244,40 @@ def test_orientation_averaged_third_order(golden, key, geo, pol, ens, rand, iso)
     else:
         _, S = orc.ensemble_average(m, ens, one, pol, random_orientations=rand)
     assert rel_err(S, golden[key]) < 1e-11
+
+
+def zofe3_model(golden, subspace='ge', sites=3):
+    ham = orc.ElectronicHamiltonianSpec(golden['zofe3_H'][:sites, :sites],
+                                        dipoles=golden['zofe3_dipoles'][:sites],
+                                        disorder=wl.fwhm_for_sd(30.0) if sites == 3 else None,
+                                        random_seed=9,
+                                        energy_spread_extra=float(golden['zofe3_extra']))
+    pm = [np.outer(golden['zofe3_' + k], np.ones(sites)) for k in ('Omega', 'gamma', 'huang')]
+    return orc.ZOFESpec(ham, *pm, hilbert_subspace=subspace, unit_convert=CM_FS)
+
+
+def test_zofe_oracle_matches_reference(golden):
+    """ZOFE master equation (zofe.py:121-229): free dynamics on 'ge' and 'e',
+    linear response, absorption with random orientations, a pump pulse."""
+    m = zofe3_model(golden)
+    assert m.time_step == 2.0
+    t, rho = orc.zofe_dynamics(m, [0, 1, 0, 0], 400.0)
+    assert np.allclose(t, golden['zofe3_dyn_t'])
+    assert rel_err(rho, golden['zofe3_dyn_rho']) < 1e-12
+    _, rho = orc.zofe_dynamics(zofe3_model(golden, 'e'), [1, 0, 0], 200.0)
+    assert rel_err(rho, golden['zofe3e_dyn_rho']) < 1e-12
+    t, x = orc.zofe_linear_response(m, 256.0)
+    assert rel_err(x, golden['zofe3_lin']) < 1e-12
+
+    def spectrum(x):
+        return orc.fourier_transform(t, -x, rw_freq=m.ham.rw_freq,
+                                     unit_convert=CM_FS)[1].real
+    assert rel_err(spectrum(x), golden['zofe3_abs_X']) < 1e-12
+    _, x = orc.ensemble_average(m, 3, orc.zofe_linear_response, 256.0,
+                                random_orientations=True)
+    assert rel_err(spectrum(x), golden['zofe3_abs_rand_X']) < 1e-12
+    pump = orc.GaussianPulseSpec(float(np.mean(np.diag(golden['zofe3_H']))), 20.0, 0.0,
+                                 1e-2, CM_FS)
+    t, st = orc.zofe_with_fields(m, [pump, pump], '-+', 'xx', 60.0)
+    assert np.allclose(t, golden['zofe3_pump_t'])
+    assert rel_err(st, golden['zofe3_pump']) < 1e-12
