@@ -60,7 +60,9 @@ def parse_args():
     p.add_argument('--heom-samples', type=int, default=64)
     p.add_argument('--no-third', action='store_true')
     p.add_argument('--no-adjoint', action='store_true')
-    p.add_argument('--only', choices=['heom', 'third', 'adjoint'],
+    p.add_argument('--no-zofe', action='store_true')
+    p.add_argument('--zofe-samples', type=int, default=152)
+    p.add_argument('--only', choices=['heom', 'third', 'adjoint', 'zofe'],
                    help='run one auxiliary workload alone and print its JSON')
     p.add_argument('--third-samples', type=int, default=256)
     p.add_argument('--third-reps', type=int, default=2)
@@ -230,6 +232,69 @@ def heom_ring8(torch, qg, native, samples=64, nsteps=1999):
     out['fp32_tflops_executed_form'] = flops / (out['fp32_ms'] * 1e-3) / 1e12
     out['fp64_ms_note'] = 'FP64 timed over {} steps and scaled to {}'.format(min(200, nsteps),
                                                                              nsteps)
+    return out
+
+
+def zofe_fmo7(torch, qg, native, samples=152, reps=2):
+    """ZOFE workload: 7 sites with 16 pseudomodes per site (seeded
+    parameters), dt = 1 fs.  Single-model calls through the public API, timed
+    end to end (wall clock, after a warm-up call): 'e' dynamics for 1000 fs
+    (5537 state components), a pump pulse on 'ge' over 1000 fs after it
+    (7232 components) and the 'ge' absorption spectrum from 2000 fs; then the
+    disorder-averaged spectrum of ``samples`` samples in one launch."""
+    from qspectra_gb300 import workloads as wl
+    H = wl.fmo7_hamiltonian()
+    extra = wl.energy_spread_for_dt(H, 1.0, qg.CM_FS)
+    bath = qg.PseudomodeBath(16, *wl.pseudomode_parameters(7, 16))
+    ham = qg.ElectronicHamiltonian(H, bath=bath, dipoles=wl.unit_dipoles(7),
+                                   disorder=wl.fwhm_for_sd(80.0), random_seed=1,
+                                   energy_spread_extra=extra)
+    m_e = qg.ZOFEModel(ham, hilbert_subspace='e', unit_convert=qg.CM_FS)
+    m_ge = qg.ZOFEModel(ham, hilbert_subspace='ge', unit_convert=qg.CM_FS)
+    pump = qg.GaussianPulse(12500.0, 50.0, scale=1e-3, freq_convert=qg.CM_FS)
+    psi = np.zeros(7)
+    psi[0] = 1.0
+    calls = {
+        'dynamics_e_1000fs': lambda p: qg.simulate_dynamics(m_e, psi, 1000.0, precision=p),
+        'pump_ge_1000fs': lambda p: qg.simulate_pump(m_ge, pump, 'x', 1000.0, precision=p),
+        'absorption_ge_2000fs': lambda p: qg.absorption_spectra(m_ge, 2000.0, precision=p),
+    }
+    out = {'workload': 'ZOFE 7 sites x 16 pseudomodes, dt 1 fs; single-model calls end to '
+                       'end, plus a {}-sample ensemble absorption in one launch'.format(samples)}
+    res = {}
+    for name, fn in calls.items():
+        for prec in ('fp64', 'fp32'):
+            fn(prec)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                r = fn(prec)
+            torch.cuda.synchronize()
+            out['{}_{}_ms'.format(name, prec)] = (time.perf_counter() - t0) * 1e3 / reps
+            res[name, prec] = np.asarray(r[1])
+        a, b = res[name, 'fp32'], res[name, 'fp64']
+        out[name + '_fp32_vs_fp64_rel_err'] = float(np.abs(a - b).max() / np.abs(b).max())
+    # CPU baseline: the oracle's NumPy restatement of the same 'e' dynamics on
+    # one host thread, 200 of the 1000 steps, scaled
+    import oracle
+    om = oracle.ZOFESpec(oracle.ElectronicHamiltonianSpec(H, dipoles=wl.unit_dipoles(7),
+                                                          energy_spread_extra=extra),
+                         *wl.pseudomode_parameters(7, 16), hilbert_subspace='e',
+                         unit_convert=qg.CM_FS)
+    t0 = time.perf_counter()
+    oracle.zofe_dynamics(om, psi, 200.0)
+    out['cpu_baseline'] = {'value': (time.perf_counter() - t0) * 1e3 * 5, 'unit': 'ms',
+                           'cores': 1, 'kind': 'port',
+                           'sample': "dynamics_e_1000fs: 200 of 1000 RK4 steps, scaled"}
+    for prec in ('fp32', 'fp64'):
+        qg.absorption_spectra(m_ge, 2000.0, ensemble_size=samples, precision=prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        qg.absorption_spectra(m_ge, 2000.0, ensemble_size=samples, precision=prec)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3
+        out['ensemble_absorption_{}_ms'.format(prec)] = ms
+        out['ensemble_absorption_{}_spectra_per_s'.format(prec)] = samples / (ms * 1e-3)
     return out
 
 
@@ -494,6 +559,8 @@ def our_arm(args):
              if rank == 0 and not args.no_third else None)
     adj = (adjoint_fmo7(torch, qg, samples=args.adjoint_samples)
            if rank == 0 and not args.no_adjoint else None)
+    zofe = (zofe_fmo7(torch, qg, _native, samples=args.zofe_samples)
+            if rank == 0 and not args.no_zofe else None)
     if rank != 0:
         return 0
     peak = fma_peak_tflops(torch, _native)
@@ -542,6 +609,8 @@ def our_arm(args):
         line['third_order_chain24'] = third
     if heom is not None:
         line['heom_ring8'] = heom
+    if zofe is not None:
+        line['zofe_fmo7'] = zofe
     if base is not None:
         line['cpu_baseline'] = base
     print(json.dumps(line), flush=True)
@@ -563,6 +632,8 @@ def main():
         if args.only == 'heom':
             out = heom_ring8(torch, qg, _native, samples=args.heom_samples,
                              nsteps=args.heom_steps)
+        elif args.only == 'zofe':
+            out = zofe_fmo7(torch, qg, _native, samples=args.zofe_samples)
         elif args.only == 'third':
             out = third_order_chain24(torch, qg, samples=args.third_samples,
                                       fp64_samples=args.third_fp64_samples,

@@ -339,12 +339,13 @@ typedef struct {
   double h;              /* RK4 step */
   const double* y0;      /* complex128 [batch][M], M = n^2 + npm n_sites n^2 */
   int64_t y0_stride;     /* elements between samples, 0 = shared */
-  double* out_state;     /* complex128 [batch][nsteps/save_every + 1][M] or NULL;
+  double* out_state;     /* complex128 [batch][nsteps/save_every + 1][M] or NULL
+                            ([...][n*n], rho only, with save_rho_only);
                             mode 1: [batch][M], the right-hand side */
   double* out_proj;      /* complex128 [batch][nsteps/save_every + 1][nproj] or NULL */
   int32_t* status;       /* device int: QSX_ERR_NONFINITE on NaN/Inf */
   int32_t reserved;      /* must be 0 */
-  int32_t pad;
+  int32_t save_rho_only; /* 1: out_state keeps rho only (mode 0) */
 } qsx_zofe_args;
 
 size_t qsx_zofe_args_bytes(void);

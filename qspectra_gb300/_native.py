@@ -79,7 +79,7 @@ class ZofeArgs(ctypes.Structure):
         ('proj', _c_vp), ('unit_convert', ctypes.c_double), ('h', ctypes.c_double),
         ('y0', _c_vp), ('y0_stride', ctypes.c_int64), ('out_state', _c_vp),
         ('out_proj', _c_vp), ('status', _c_vp), ('reserved', ctypes.c_int32),
-        ('pad', ctypes.c_int32),
+        ('save_rho_only', ctypes.c_int32),
     ]
 
 
@@ -701,8 +701,9 @@ def zofe_rk4(H, Ld, Gamma, w, y0, nsteps, h, unit_convert, save_every=1,
     (npm, n_sites) complex128; y0 (M,) or (B, M) complex128 in the reference's
     state layout; V (np, n, n) or (B, np, n, n) and coef (nsteps, 3, np)
     complex128 for pulses; proj (P, n*n) complex128 rows over rho.  Returns a
-    dict with 'state' (B, nsave, M) and/or 'proj' (B, nsave, P); mode 1
-    returns the right-hand side at y0 as 'rhs' (B, M).
+    dict with 'state' (B, nsave, M) and/or 'proj' (B, nsave, P); with
+    state='rho' the states hold rho only, (B, nsave, n*n) column-major; mode
+    1 returns the right-hand side at y0 as 'rhs' (B, M).
     """
     require_gpu()
     dev = y0.device
@@ -749,7 +750,9 @@ def zofe_rk4(H, Ld, Gamma, w, y0, nsteps, h, unit_convert, save_every=1,
         a.out_state = out['rhs'].data_ptr()
     else:
         if state:
-            out['state'] = torch.empty((B, nsave, M), dtype=torch.complex128, device=dev)
+            width = n * n if state == 'rho' else M
+            a.save_rho_only = 1 if state == 'rho' else 0
+            out['state'] = torch.empty((B, nsave, width), dtype=torch.complex128, device=dev)
             a.out_state = out['state'].data_ptr()
         if proj is not None:
             proj = proj.to(device=dev, dtype=torch.complex128).contiguous()

@@ -33,7 +33,7 @@ namespace qsx {
 
 struct ZofeP {
   int n, N, npm, pmc, csize;  // states, sites, pseudomodes, pseudomodes per CTA, cluster
-  int nsteps, save_every, nsave, np, nproj, mode;
+  int nsteps, save_every, nsave, np, nproj, mode, rho_only;
   int64_t batch, H_stride, V_stride, y0_stride;
   int64_t M;                  // n^2 + npm N n^2
   const double* H;            // real [n][n], rotating frame
@@ -60,16 +60,17 @@ __device__ __forceinline__ void zofe_save(const ZofeP& p, int k, int64_t smp, in
                                           typename cplx<T>::type* sx) {
   const int n2 = p.n * p.n, tid = threadIdx.x, bd = blockDim.x;
   if (p.out_state) {
+    const int64_t row = p.rho_only ? (int64_t)n2 : p.M;
 #pragma unroll
     for (int u = 0; u < EPT; ++u) {
       const int e = tid + u * bd;
-      if (gidx[u] < 0 || (e < n2 && rank != 0)) continue;
+      if (gidx[u] < 0 || (e < n2 && rank != 0) || (p.rho_only && e >= n2)) continue;
       double vx = (double)yh[u].x, vy = (double)yh[u].y;
       if (sizeof(T) == 4) {
         vx += (double)yl[u].x;
         vy += (double)yl[u].y;
       }
-      p.out_state[(smp * p.nsave + k) * p.M + gidx[u]] = make_double2(vx, vy);
+      p.out_state[(smp * p.nsave + k) * row + gidx[u]] = make_double2(vx, vy);
     }
   }
   if (p.out_proj && rank == 0) {
@@ -184,11 +185,14 @@ __global__ void __launch_bounds__(EPT >= 4 ? 512 : 1024, 1)
       }
       cluster.sync();  // partials published cluster-wide
       for (int q = tid; q < Q; q += bd) {
-        Cx z = cmk((T)0, (T)0);
-        for (int r = 0; r < C; ++r) {
-          const Cx* peer = cluster.map_shared_rank(part, r);
-          z = cadd2(z, peer[q]);
-        }
+        // issue every peer's load before adding (they are independent)
+        Cx v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+          v[r] = r < C ? cluster.map_shared_rank(part, r)[q] : cmk((T)0, (T)0);
+        Cx z = v[0];
+#pragma unroll
+        for (int r = 1; r < 8; ++r) z = cadd2(z, v[r]);
         sS[q] = z;
       }
       __syncthreads();
@@ -198,9 +202,14 @@ __global__ void __launch_bounds__(EPT >= 4 ? 512 : 1024, 1)
         Cx aik = cmk((T)0, (T)0), aki = aik, fv = aik;
         for (int s = 0; s < N; ++s) {
           const T li = sLd[s * n + i], lk = sLd[s * n + k];
-          const Cx Sik = sS[s + N * (i + n * k)], Ski = sS[s + N * (k + n * i)];
-          aik = cmk(aik.x + li * Sik.x, aik.y + li * Sik.y);
-          aki = cmk(aki.x + lk * Ski.x, aki.y + lk * Ski.y);
+          if (li != (T)0) {
+            const Cx Sik = sS[s + N * (i + n * k)];
+            aik = cmk(aik.x + li * Sik.x, aik.y + li * Sik.y);
+          }
+          if (lk != (T)0) {
+            const Cx Ski = sS[s + N * (k + n * i)];
+            aki = cmk(aki.x + lk * Ski.x, aki.y + lk * Ski.y);
+          }
         }
         for (int q = 0; q < np; ++q) cfma(fv, sa[q], sV[(size_t)q * n2 + e]);
         // the field term is not scaled by unit_convert: fold it in divided by it
@@ -222,15 +231,22 @@ __global__ void __launch_bounds__(EPT >= 4 ? 512 : 1024, 1)
             cfma(d, sB[i * n + j], sx[j + n * m]);
             cfma(d, sx[i + n * j], sR[j * n + m]);
           }
+          // the couplings are site number operators: most L_s[i] vanish
           for (int s = 0; s < N; ++s) {
-            Cx cs = cmk((T)0, (T)0), bs = cs;
-            for (int k = 0; k < n; ++k) {
-              const Cx Smk = sS[s + N * (m + n * k)];
-              cfma(cs, sx[i + n * k], cmk(Smk.x, -Smk.y));
-              cfma(bs, sS[s + N * (i + n * k)], sx[k + n * m]);
-            }
             const T li = sLd[s * n + i], lm = sLd[s * n + m];
-            d = cmk(d.x + li * cs.x + lm * bs.x, d.y + li * cs.y + lm * bs.y);
+            if (li != (T)0) {
+              Cx cs = cmk((T)0, (T)0);
+              for (int k = 0; k < n; ++k) {
+                const Cx Smk = sS[s + N * (m + n * k)];
+                cfma(cs, sx[i + n * k], cmk(Smk.x, -Smk.y));
+              }
+              d = cmk(d.x + li * cs.x, d.y + li * cs.y);
+            }
+            if (lm != (T)0) {
+              Cx bs = cmk((T)0, (T)0);
+              for (int k = 0; k < n; ++k) cfma(bs, sS[s + N * (i + n * k)], sx[k + n * m]);
+              d = cmk(d.x + lm * bs.x, d.y + lm * bs.y);
+            }
           }
         } else {
           const int qq = e - n2, pmL = qq % P, q = qq / P;
@@ -326,7 +342,7 @@ extern "C" int qsx_zofe_rk4(const qsx_zofe_args* a, void* stream) {
                     a->npulses >= 0 && a->nproj >= 0 && a->batch >= 0 && a->nsteps >= 0 &&
                     a->save_every >= 1 && a->nsteps % a->save_every == 0 &&
                     (a->mode == 0 || a->mode == 1) && a->cluster >= 0 && a->cluster <= 8 &&
-                    a->reserved == 0,
+                    a->reserved == 0 && (a->save_rho_only == 0 || a->save_rho_only == 1),
                 "qsx_zofe_rk4: bad sizes (n=%d, sites=%d, pseudomodes=%d, steps=%d)", a->n,
                 a->n_sites, a->npm, a->nsteps);
   if (a->batch == 0) return QSX_OK;
@@ -355,7 +371,9 @@ extern "C" int qsx_zofe_rk4(const qsx_zofe_args* a, void* stream) {
               Mloc, n, N, a->npm, C);
     return QSX_ERR_UNSUPPORTED;
   }
-  int ept = Mloc <= 1024 ? 1 : (Mloc <= 2048 ? 2 : 8);
+  const bool f32 = a->precision == QSX_FP32;
+  // elements per thread: FP64 keeps 128 registers a thread above one element
+  const int ept = Mloc <= 1024 ? 1 : (Mloc <= 2048 ? (f32 ? 2 : 4) : 8);
   const int maxthr = ept >= 4 ? 512 : 1024;
   int threads = (Mloc + ept - 1) / ept;
   threads = ((threads + 31) / 32) * 32;
@@ -380,6 +398,7 @@ extern "C" int qsx_zofe_rk4(const qsx_zofe_args* a, void* stream) {
   p.np = np;
   p.nproj = a->nproj;
   p.mode = a->mode;
+  p.rho_only = a->save_rho_only;
   p.batch = a->batch;
   p.H_stride = a->H_stride;
   p.V_stride = np ? a->V_stride : 0;
@@ -401,11 +420,12 @@ extern "C" int qsx_zofe_rk4(const qsx_zofe_args* a, void* stream) {
   p.status = a->status;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e;
-  const bool f32 = a->precision == QSX_FP32;
   if (ept == 1)
     e = f32 ? launch_zofe<float, 1>(p, threads, smem, s) : launch_zofe<double, 1>(p, threads, smem, s);
   else if (ept == 2)
-    e = f32 ? launch_zofe<float, 2>(p, threads, smem, s) : launch_zofe<double, 2>(p, threads, smem, s);
+    e = launch_zofe<float, 2>(p, threads, smem, s);
+  else if (ept == 4)
+    e = launch_zofe<double, 4>(p, threads, smem, s);
   else
     e = f32 ? launch_zofe<float, 8>(p, threads, smem, s) : launch_zofe<double, 8>(p, threads, smem, s);
   if (e != cudaSuccess) return cuda_status(e, "qsx_zofe_rk4");

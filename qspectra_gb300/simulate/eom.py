@@ -62,8 +62,8 @@ def simulate_dynamics(dynamical_model, initial_state, duration=None, times=None,
 
 
 def _zofe_dynamics(model, initial_state, duration, times, ensemble_size, precision, step):
-    """ZOFE free dynamics: only rho is read back (the projections of rho onto
-    its own entries), averaged over the samples in the same launch."""
+    """ZOFE free dynamics: only rho is written back, averaged over the
+    samples of the same launch."""
     from ..dynamics.zofe import ensemble_inputs
     from .utils import PRECISIONS, uniform_save_plan
     step = model.time_step if step is None else step
@@ -80,9 +80,8 @@ def _zofe_dynamics(model, initial_state, duration, times, ensemble_size, precisi
         H, _ = ensemble_inputs(model, ensemble_size)
     n = model.n_states
     Ld, G, w = model.zofe_tables()
-    eye = torch.eye(n * n, dtype=torch.complex128, device=dev)
     out = _native.zofe_rk4(H, Ld, G, w, y0, nsteps, step, model.unit_convert, every,
-                           PRECISIONS[precision], proj=eye, state=False)['proj']
+                           PRECISIONS[precision], state='rho')['state']
     vec = out[:, first:].mean(0).cpu().numpy()          # (T, n*n), column-major rho
     return t, vec.reshape(len(vec), n, n).transpose(0, 2, 1)
 

@@ -54,6 +54,26 @@ def ring_hamiltonian(n_sites=8, seed=4321, mean=12400.0, sd=80.0,
     return H
 
 
+def pseudomode_parameters(n_sites=7, numb_pm=16, seed=77):
+    """Seeded pseudomode bath (Omega, gamma, huang), each (numb_pm, n_sites):
+    Lorentzians at Omega in [-500, 1500] cm^-1 with widths 40..500 cm^-1 and
+    couplings Omega^2 huang of 20..400 cm^-1, one low-frequency mode near
+    zero; the same set on every site."""
+    rng = np.random.RandomState(seed)
+    Om = np.sort(rng.uniform(-500.0, 1500.0, numb_pm))
+    Om[np.argmin(np.abs(Om))] = 1.0
+    ga = rng.uniform(40.0, 500.0, numb_pm)
+    hu = rng.uniform(20.0, 400.0, numb_pm) / (Om ** 2 + 100.0)
+    on = np.ones(n_sites, complex)
+    return tuple(np.array([x * on for x in v]) for v in (Om, ga, hu))
+
+
+def unit_dipoles(n_sites=7, seed=99):
+    """Random unit transition dipoles."""
+    d = np.random.RandomState(seed).randn(n_sites, 3)
+    return d / np.linalg.norm(d, axis=1, keepdims=True)
+
+
 def fwhm_for_sd(sd):
     """Disorder argument (a FWHM) that gives Gaussian SD ``sd`` (hamiltonian.py:458-461)."""
     return sd / GAUSSIAN_SD_FWHM
