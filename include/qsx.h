@@ -141,6 +141,59 @@ int qsx_rk4_block_matrix_batched(const void* D, int m, int64_t batch,
                                  int nselect, void* out, void* stream);
 
 /*
+ * Real form of Hermitian Liouville blocks (no reference counterpart: an
+ * exact change of coordinates).  A Redfield generator with a real symmetric
+ * Hamiltonian maps Hermitian density matrices to Hermitian ones, so on a
+ * diagonal block (n x n states, m = n^2, column-stacked) its RK4 propagator
+ * is a real m x m matrix in the coordinates
+ *   x[a + n b] = Re rho_ab (a <= b),  Im rho_ba (a > b),
+ * with the populations x[a + n a] = rho_aa among them; each step then costs
+ * m^2 real multiply-adds instead of m^2 complex ones.
+ *
+ * qsx_hermitian_real_form: complex [batch][m][m] (complex64 for QSX_FP32,
+ * complex128 for QSX_FP64) -> real [batch][m][m] (float / double).
+ * qsx_redfield_propagator_hermitian_batched: as
+ * qsx_redfield_propagator_batched for the diagonal block of the nb states
+ * `states` (Hilbert indices, nb <= 8, m = nb^2), writing the real
+ * D_r = P_r - I [batch][m][m].  The real generator is given as a sparse
+ * linear map (CSR rowptr [m*m + 1], cols, vals; rows = entries r * m + c)
+ * of the sources [Re B[s]_xy, Im B[s]_xy for s, x, y < nb] ++
+ * [uc H_xy for x, y < nb], B[s] = G - sum_i occ_is M_i on the block; the
+ * map depends on nb only and is built once by the caller.
+ * qsx_rk4_block_matrix_real_batched: qsx_rk4_block_matrix_batched on real
+ * matrices; each sample's (m + nselect (K - 1)) x m output starts at a
+ * multiple of 4 values (sample stride = that size rounded up to 4).
+ * qsx_rk4_real_block_mean: the K-step blocked loop on FP32 real matrices
+ * [batch][m + nselect (K - 1)][m] in that padded layout (m in
+ * {9,16,25,36,49,64}, at most 512
+ * rows), split-word FP32 state from y0 (double [batch][m], y0_stride 0 =
+ * shared); out_mean (double [nsteps + 1][nselect]) is the ensemble mean of
+ * the selected coordinates at every step; workspace of
+ * qsx_rk4_real_block_workspace_bytes() bytes.  group = samples per CTA
+ * (0 = the library's choice, one).
+ */
+int qsx_hermitian_real_form(const void* A, int n, int64_t batch, int precision,
+                            void* R, void* stream);
+int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
+                                              const double* G, const double* M,
+                                              const double* occ, int n, int n_sites,
+                                              int64_t batch, double unit_convert,
+                                              const int* states, int nb,
+                                              const int* rowptr, const int* cols,
+                                              const float* vals, double h,
+                                              int precision, void* D, void* stream);
+int qsx_rk4_block_matrix_real_batched(const void* D, int m, int64_t batch,
+                                      int precision, int K, const int* select,
+                                      int nselect, void* out, void* stream);
+size_t qsx_rk4_real_block_workspace_bytes(int m, int64_t batch, int K, int nsteps,
+                                          int nselect, int group);
+int qsx_rk4_real_block_mean(const float* matrix, int m, int64_t batch, int K,
+                            int nsteps, const double* y0, int64_t y0_stride,
+                            const int* select, int nselect, int group,
+                            double* out_mean, void* workspace, size_t workspace_bytes,
+                            int32_t* status, void* stream);
+
+/*
  * RK4 propagator D = P - I with P = sum_{k<=4} (hL)^k / k!, i.e. exactly one
  * classical RK4 step of dy/dt = L y (the step inside the integrate loop,
  * qspectra/simulate/utils.py:44-49, with zvode replaced by RK4).

@@ -102,6 +102,17 @@ _PROTOS = {
         _c_int, _c_int, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_rk4_block_matrix_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int,
                                               _c_vp, _c_int, _c_vp, _c_vp]),
+    'qsx_hermitian_real_form': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_vp, _c_vp]),
+    'qsx_redfield_propagator_hermitian_batched': (_c_int, [
+        _c_vp, _c_i64, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_i64, _c_dbl, _c_vp,
+        _c_int, _c_vp, _c_vp, _c_vp, _c_dbl, _c_int, _c_vp, _c_vp]),
+    'qsx_rk4_block_matrix_real_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int,
+                                                   _c_vp, _c_int, _c_vp, _c_vp]),
+    'qsx_rk4_real_block_workspace_bytes': (ctypes.c_size_t, [_c_int, _c_i64, _c_int, _c_int,
+                                                             _c_int, _c_int]),
+    'qsx_rk4_real_block_mean': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int, _c_vp, _c_i64,
+                                         _c_vp, _c_int, _c_int, _c_vp, _c_vp, ctypes.c_size_t,
+                                         _c_vp, _c_vp]),
     'qsx_rk4_propagator_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl,
                                             _c_int, _c_vp, _c_vp]),
     'qsx_rk4_args_bytes': (ctypes.c_size_t, []),
@@ -295,6 +306,158 @@ def redfield_propagator(H, G, M, occ, idx, unit_convert, h, precision=QSX_FP64,
     return D
 
 
+def hermitian_real_form(A, n):
+    """Real form (B, m, m) of complex (B, m, m) Hermiticity-preserving maps on
+    n x n matrices (qsx_hermitian_real_form; float32 from complex64)."""
+    require_gpu()
+    prec = QSX_FP32 if A.dtype == torch.complex64 else QSX_FP64
+    A = _need(A.contiguous(), A.dtype, 'A', 3)
+    B, m, _ = A.shape
+    if m != n * n:
+        raise ValueError('matrix size must be n^2')
+    R = torch.empty((B, m, m), dtype=torch.float32 if prec == QSX_FP32 else torch.float64,
+                    device=A.device)
+    _check(load().qsx_hermitian_real_form(_p(A), n, B, prec, _p(R), _stream()),
+           'qsx_hermitian_real_form')
+    return R
+
+
+_CONSTS = {}
+
+
+def const_tensor(values, dtype, device):
+    """A small host array as a device tensor, uploaded once and cached by
+    content.  Index tables and selections are the same on every call of a
+    workload; uploading a pageable host array blocks the host until the
+    stream reaches the copy, so repeated uploads would serialise the host's
+    launches with the GPU's work."""
+    arr = np.ascontiguousarray(values)
+    key = (arr.tobytes(), arr.shape, arr.dtype.str, str(dtype), str(device))
+    t = _CONSTS.get(key)
+    if t is None:
+        if len(_CONSTS) > 512:
+            _CONSTS.clear()
+        t = torch.as_tensor(arr).to(dtype=dtype, device=device).contiguous()
+        _CONSTS[key] = t
+    return t
+
+
+_RECIPES = {}
+
+
+def hermitian_recipe(nb, device):
+    """CSR map (rowptr, cols, vals) from the sources [Re B, Im B (nb, nb, nb),
+    uc H (nb, nb)] to the real form of the Redfield generator block
+    L[(a,b),(c,d)] = d_bd (-B[b]_ac - i uc H_ac) + d_ac (-conj(B[a]_bd) + i uc H_db)
+    on a diagonal block of nb states (row-major over the m^2 entries)."""
+    key = (nb, str(device))
+    if key in _RECIPES:
+        return _RECIPES[key]
+    m = nb * nb
+    nsrc = 2 * nb ** 3 + m
+    S = np.eye(nsrc)
+    Bs = (S[:, :nb ** 3] + 1j * S[:, nb ** 3:2 * nb ** 3]).reshape(nsrc, nb, nb, nb)
+    uH = S[:, 2 * nb ** 3:].reshape(nsrc, nb, nb)
+    I = np.eye(nb)
+    L4 = (np.einsum('bd,nbac->nabcd', I, -Bs) + np.einsum('bd,nac->nabcd', I, -1j * uH)
+          + np.einsum('ac,nabd->nabcd', I, -Bs.conj()) + np.einsum('ac,ndb->nabcd', I, 1j * uH))
+    L = L4.transpose(0, 2, 1, 4, 3).reshape(nsrc, m, m)      # k = a + nb b, l = c + nb d
+    # real form: R[k, l] = coordinate k of L applied to Hermitian basis matrix l
+    k = np.arange(m)
+    a, b = k % nb, k // nb
+    row = np.where(a <= b, a + nb * b, b + nb * a)
+    c, d = a, b
+    cols_re = np.where(c <= d, c + nb * d, d + nb * c)
+    cols_tr = np.where(c <= d, d + nb * c, c + nb * d)
+    Lr = L[:, row, :]                                         # (nsrc, m rows k, m)
+    V = np.where(c == d, Lr[:, :, k],
+                 np.where(c < d, Lr[:, :, cols_re] + Lr[:, :, cols_tr],
+                          1j * (Lr[:, :, d + nb * c] - Lr[:, :, c + nb * d])))
+    R = np.where((a <= b)[None, :, None], V.real, V.imag)     # (nsrc, m, m)
+    J = R.reshape(nsrc, m * m).T                              # (m^2, nsrc)
+    rows, cols = np.nonzero(J)
+    rowptr = np.zeros(m * m + 1, dtype=np.int32)
+    np.add.at(rowptr, rows + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    out = (torch.as_tensor(rowptr, device=device),
+           torch.as_tensor(cols.astype(np.int32), device=device),
+           torch.as_tensor(J[rows, cols].astype(np.float32), device=device))
+    _RECIPES[key] = out
+    return out
+
+
+def redfield_propagator_hermitian(H, G, M, occ, states, unit_convert, h, precision=QSX_FP32):
+    """Real one-step propagator D_r = P_r - I (B, nb^2, nb^2) of the diagonal
+    block of Hilbert states ``states`` (qsx_redfield_propagator_hermitian_batched)."""
+    require_gpu()
+    _need(G, torch.complex128, 'G', 3)
+    _need(M, torch.complex128, 'M', 4)
+    _need(occ, torch.float64, 'occ', 2)
+    B, n, _ = G.shape
+    N = M.shape[1]
+    H = _need(H, torch.float64, 'H')
+    h_stride = 0 if H.dim() == 2 else n * n
+    st = const_tensor(np.asarray(states, dtype=np.int32), torch.int32, G.device)
+    nb = st.numel()
+    rowptr, cols, vals = hermitian_recipe(nb, G.device)
+    m = nb * nb
+    dt = torch.float32 if precision == QSX_FP32 else torch.float64
+    D = torch.empty((B, m, m), dtype=dt, device=G.device)
+    _check(load().qsx_redfield_propagator_hermitian_batched(
+        _p(H), h_stride, _p(G), _p(M), _p(occ), n, N, B, unit_convert, _p(st), nb, _p(rowptr),
+        _p(cols), _p(vals), h, precision, _p(D), _stream()),
+        'qsx_redfield_propagator_hermitian_batched')
+    return D
+
+
+def rk4_block_matrix_real(D, K, select):
+    """(B, m + len(select) (K-1), m) real K-step blocked matrix from a real D."""
+    require_gpu()
+    prec = QSX_FP32 if D.dtype == torch.float32 else QSX_FP64
+    _need(D, D.dtype, 'D', 3)
+    B, m, _ = D.shape
+    sel_np = np.asarray(select, dtype=np.int64).reshape(-1)
+    if sel_np.size == 0 or sel_np.min() < 0 or sel_np.max() >= m:
+        raise ValueError('select indices must lie in [0, {})'.format(m))
+    sel = const_tensor(sel_np.astype(np.int32), torch.int32, D.device)
+    rows = m + sel.numel() * (K - 1)
+    stride = (rows * m + 3) // 4 * 4   # samples start on 16-byte boundaries
+    flat = torch.empty((B, stride), dtype=D.dtype, device=D.device)
+    _check(load().qsx_rk4_block_matrix_real_batched(_p(D), m, B, prec, K, _p(sel), sel.numel(),
+                                                    _p(flat), _stream()),
+           'qsx_rk4_block_matrix_real_batched')
+    return flat[:, :rows * m].view(B, rows, m)
+
+
+def rk4_real_block_mean(mat, y0, nsteps, select, K, check_finite=True, group=0):
+    """Ensemble mean (nsteps + 1, len(select)) float64 of the selected real
+    coordinates (qsx_rk4_real_block_mean).  mat (B, m + nsel (K-1), m)
+    float32; y0 (m,) or (B, m) float64."""
+    require_gpu()
+    if mat.dtype != torch.float32 or mat.dim() != 3 or not mat.is_cuda:
+        raise TypeError('mat must be a (B, rows, m) float32 CUDA tensor')
+    B, rows, m = mat.shape
+    if mat.stride(2) != 1 or mat.stride(1) != m or mat.stride(0) != (rows * m + 3) // 4 * 4:
+        raise ValueError('mat must use the padded sample layout of rk4_block_matrix_real')
+    y0 = y0.to(device=mat.device, dtype=torch.float64).contiguous()
+    sel = const_tensor(np.asarray(select, dtype=np.int32), torch.int32, mat.device)
+    nsel = sel.numel()
+    if rows != m + nsel * (K - 1):
+        raise ValueError('matrix rows do not match K and select')
+    lib = load()
+    ws_bytes = lib.qsx_rk4_real_block_workspace_bytes(m, B, K, int(nsteps), nsel, int(group))
+    ws = torch.empty(max(int(ws_bytes), 8), dtype=torch.uint8, device=mat.device)
+    out = torch.empty((nsteps + 1, nsel), dtype=torch.float64, device=mat.device)
+    status = torch.zeros(1, dtype=torch.int32, device=mat.device)
+    _check(lib.qsx_rk4_real_block_mean(_p(mat), m, B, K, int(nsteps), _p(y0),
+                                       m if y0.dim() == 2 else 0, _p(sel), nsel, int(group),
+                                       _p(out), _p(ws), ws.numel(), _p(status), _stream()),
+           'qsx_rk4_real_block_mean')
+    if check_finite and int(status.item()) & QSX_ERR_NONFINITE:
+        raise IntegratorError('non-finite state in the blocked real loop')
+    return out, status
+
+
 def rk4_propagator(L, h, precision=QSX_FP64):
     require_gpu()
     _need(L, torch.complex128, 'L', 3)
@@ -316,7 +479,7 @@ def rk4_block_matrix(D, K, select):
     sel_np = np.asarray(select, dtype=np.int64).reshape(-1)
     if sel_np.size == 0 or sel_np.min() < 0 or sel_np.max() >= m:
         raise ValueError('select indices must lie in [0, {})'.format(m))
-    sel = torch.as_tensor(sel_np, dtype=torch.int32, device=D.device)
+    sel = const_tensor(sel_np.astype(np.int32), torch.int32, D.device)
     out = torch.empty((B, m + sel.numel() * (K - 1), m), dtype=D.dtype, device=D.device)
     _check(load().qsx_rk4_block_matrix_batched(_p(D), m, B, prec, K, _p(sel), sel.numel(),
                                                _p(out), _stream()),
@@ -380,7 +543,7 @@ def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
             raise ValueError('select indices must lie in [0, {})'.format(m))
         if len(np.unique(sel_np)) != sel_np.size:
             raise ValueError('select indices must be distinct')
-        sel = torch.as_tensor(sel_np, dtype=torch.int32).to(dev).contiguous()
+        sel = const_tensor(sel_np.astype(np.int32), torch.int32, dev)
         a.nselect = sel.numel()
         a.select = sel.data_ptr()
         nout = a.nselect

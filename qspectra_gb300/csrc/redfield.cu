@@ -5,6 +5,8 @@
 #include <cmath>
 
 #include "qsx_bath.cuh"
+#include <type_traits>
+
 #include "qsx_common.cuh"
 
 namespace qsx {
@@ -482,6 +484,103 @@ __device__ __forceinline__ void smem_cgemm(const C* __restrict__ A, const C* __r
   }
 }
 
+// C = A B for real matrices in shared memory with row stride ld (a multiple
+// of 4, columns beyond the data zero): A has `rows` rows (a multiple of 4),
+// B is ld x ld.  Each thread owns a 4 x 4 block of C and per four k reads four
+// float4 of A rows and four float4 of B rows (64 FMA per 8 vector loads, no
+// bounds tests in the loop); store(r0, c0, acc) receives the block.
+struct Quad {
+  float x, y, z, w;
+};
+struct QuadD {
+  double x, y, z, w;
+};
+// four consecutive values from 16-byte aligned shared memory
+__device__ __forceinline__ Quad load4(const float* p) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ QuadD load4(const double* p) {
+  const double2 a = *reinterpret_cast<const double2*>(p);
+  const double2 b = *reinterpret_cast<const double2*>(p + 2);
+  return {a.x, a.y, b.x, b.y};
+}
+
+template <typename T, typename Store>
+__device__ __forceinline__ void rgemm_4x4(const T* __restrict__ A, const T* __restrict__ B,
+                                          int ld, int rows, Store store) {
+  using V4 = typename std::conditional<sizeof(T) == 4, Quad, QuadD>::type;
+  const int nct = ld / 4;
+  const int ntiles = (rows / 4) * nct;
+  for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
+    const int r0 = (t / nct) * 4, c0 = (t % nct) * 4;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = (T)0;
+    for (int k = 0; k < ld; k += 4) {
+      V4 a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = load4(A + (r0 + i) * ld + k);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) b[q] = load4(B + (k + q) * ld + c0);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const T av[4] = {a[i].x, a[i].y, a[i].z, a[i].w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          acc[i][0] = fma(av[q], b[q].x, acc[i][0]);
+          acc[i][1] = fma(av[q], b[q].y, acc[i][1]);
+          acc[i][2] = fma(av[q], b[q].z, acc[i][2]);
+          acc[i][3] = fma(av[q], b[q].w, acc[i][3]);
+        }
+      }
+    }
+    store(r0, c0, acc);
+  }
+}
+
+// (I + X)(I + Y) - I = X + Y + X Y for padded ld x ld shared matrices (rows
+// of X: `rows`); Z may be global (ldz, only the first m rows/cols written)
+// or shared.
+template <typename T>
+__device__ __forceinline__ void compose_into(const T* X, const T* Y, int ld, int rows, int m,
+                                             T* Z, int ldz) {
+  rgemm_4x4<T>(X, Y, ld, rows, [&](int r0, int c0, T (&acc)[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int r = r0 + i, c = c0 + j;
+        if (r < m && c < m) Z[r * ldz + c] = (X[r * ld + c] + Y[r * ld + c]) + acc[i][j];
+      }
+  });
+}
+
+// Real form of a Hermiticity-preserving map on n x n matrices (m = n^2,
+// column-stacked).  Coordinates of a Hermitian rho: x[a + n b] = Re rho_ab
+// for a <= b and Im rho_ba for a > b.  Input coordinate l = c + n d is the
+// Hermitian basis matrix E_cc (c = d), E_cd + E_dc (c < d) or
+// i E_dc - i E_cd (c > d); R[k][l] is coordinate k of A applied to it.
+template <typename C>
+__device__ __forceinline__ auto hermitian_entry(const C* __restrict__ A, int lda, int n, int k,
+                                                int l) -> decltype(A[0].x) {
+  const int a = k % n, b = k / n, c = l % n, d = l / n;
+  const int row = a <= b ? a + n * b : b + n * a;
+  const C* Ar = A + (size_t)row * lda;
+  C v;
+  if (c == d) {
+    v = Ar[l];
+  } else if (c < d) {
+    v = cadd2(Ar[c + n * d], Ar[d + n * c]);
+  } else {  // i (A[:, d + n c] - A[:, c + n d])
+    const C u = Ar[d + n * c], w = Ar[c + n * d];
+    v = cmk(-(u.y - w.y), u.x - w.x);
+  }
+  return a <= b ? v.x : v.y;
+}
+
 // D = P - I for one RK4 step, P = sum_{k<=4} A^k / k!, A = h L, evaluated
 // Paterson-Stockmeyer style with two products:
 //   A2 = A A,   D = A + A2 / 2 + A2 (A / 6 + A2 / 24).
@@ -512,7 +611,7 @@ __device__ void rk4_polynomial(typename cplx<T>::type* sA, typename cplx<T>::typ
 //   L[(a,b),(c,d)] = d_bd (-B[b]_ac - i uc H_ac) + d_ac (-conj(B[a]_bd) + i uc H_db),
 // which is the K == NULL branch of liouvillian_kernel regrouped.
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
     redfield_propagator_kernel(const double* __restrict__ H, int64_t H_stride,
                                const double2* __restrict__ G, const double2* __restrict__ Mo,
                                const double* __restrict__ occ, int n, int n_sites, double uc,
@@ -527,17 +626,30 @@ __global__ void __launch_bounds__(256)
   C* sX = sL + m * m;
   C* sY = sX + m * m;
   int* sIdx = (int*)(sY + m * m);     // m
+  C* sGM = (C*)(sIdx + ((m + 3) & ~3));  // (1 + n_sites) n^2: G, M_i (16-byte aligned)
+  T* sOcc = (T*)(sGM + (size_t)(1 + n_sites) * nn);  // n_sites n
   const int64_t b = blockIdx.x;
   const double2* g = G + b * nn;
   const double2* mo = Mo + b * (int64_t)n_sites * nn;
+  // every FP64 operator entry is converted once
+  for (int e = threadIdx.x; e < (1 + n_sites) * nn; e += blockDim.x) {
+    const double2 v = e < nn ? g[e] : mo[e - nn];
+    sGM[e] = cmk((T)v.x, (T)v.y);
+  }
+  for (int e = threadIdx.x; e < n_sites * n; e += blockDim.x) sOcc[e] = (T)occ[e];
+  __syncthreads();
+  // B[s] = G - sum_i occ_is M_i
   for (int e = threadIdx.x; e < n * nn; e += blockDim.x) {
     const int st = e / nn, xy = e % nn;
-    double2 v = g[xy];
+    C v = sGM[xy];
     for (int i = 0; i < n_sites; ++i) {
-      const double o = occ[i * n + st];
-      if (o != 0.0) v = csub(v, cscale(mo[i * nn + xy], o));
+      const T o = sOcc[i * n + st];
+      if (o != (T)0) {
+        const C mv = sGM[(1 + i) * nn + xy];
+        v = cmk(v.x - o * mv.x, v.y - o * mv.y);
+      }
     }
-    sB[e] = cmk((T)v.x, (T)v.y);
+    sB[e] = v;
   }
   for (int e = threadIdx.x; e < nn; e += blockDim.x) sHs[e] = cmk((T)0, (T)(uc * H[b * H_stride + e]));
   for (int e = threadIdx.x; e < m; e += blockDim.x) {
@@ -683,11 +795,257 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Real one-step propagator D_r = P_r - I of a Hermitian diagonal block of nb
+// states (m = nb^2) from the per-sample operators.  The real generator is a
+// fixed sparse linear map of the sources
+//   S = [Re B[s]_xy, Im B[s]_xy (s, x, y < nb)], [uc H_xy (x, y < nb)],
+// B[s] = G - sum_i occ_is M_i restricted to the block, given as CSR
+// (rowptr, cols, vals) over the m^2 entries (row-major) and built once by
+// the host; so the assembly is nb^3 operator sums in the working precision
+// plus one short sparse dot product per entry, no index arithmetic.
+template <typename T>
+__global__ void __launch_bounds__(256, 2)
+    hermitian_propagator_kernel(const double* __restrict__ H, int64_t H_stride,
+                                const double2* __restrict__ G, const double2* __restrict__ Mo,
+                                const double* __restrict__ occ, int n, int n_sites,
+                                const int* __restrict__ states, int nb,
+                                const int* __restrict__ rowptr, const int* __restrict__ cols,
+                                const float* __restrict__ vals, double uc, double h,
+                                T* __restrict__ D) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int m = nb * nb, ld = (m + 3) & ~3, nb3 = nb * m;
+  T* rA = (T*)smraw;
+  T* rB = rA + ld * ld;
+  T* rC = rB + ld * ld;
+  T* src = rC + ld * ld;               // [2 nb^3 + nb^2]
+  int* st = (int*)(src + 2 * nb3 + m); // [nb]
+  const int64_t b = blockIdx.x;
+  const double2* g = G + b * (int64_t)n * n;
+  const double2* mo = Mo + b * (int64_t)n_sites * n * n;
+  for (int e = threadIdx.x; e < 3 * ld * ld; e += blockDim.x) rA[e] = (T)0;
+  for (int e = threadIdx.x; e < nb; e += blockDim.x) st[e] = states[e];
+  __syncthreads();
+  for (int e = threadIdx.x; e < nb3; e += blockDim.x) {
+    const int s = e / m, xy = e % m;
+    const int fx = st[xy / nb], fy = st[xy % nb], fs = st[s];
+    const int f = fx * n + fy;
+    const double2 g0 = g[f];
+    T vx = (T)g0.x, vy = (T)g0.y;
+    for (int i = 0; i < n_sites; ++i) {
+      const double o = occ[i * n + fs];
+      if (o != 0.0) {
+        const double2 mv = mo[(int64_t)i * n * n + f];
+        vx -= (T)o * (T)mv.x;
+        vy -= (T)o * (T)mv.y;
+      }
+    }
+    src[e] = vx;
+    src[nb3 + e] = vy;
+  }
+  for (int e = threadIdx.x; e < m; e += blockDim.x)
+    src[2 * nb3 + e] = (T)(uc * H[b * H_stride + st[e / nb] * n + st[e % nb]]);
+  __syncthreads();
+  const T ht = (T)h;
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+    T acc = (T)0;
+    for (int q = rowptr[e]; q < rowptr[e + 1]; ++q) acc += (T)vals[q] * src[cols[q]];
+    rA[(e / m) * ld + e % m] = ht * acc;
+  }
+  __syncthreads();
+  rgemm_4x4<T>(rA, rA, ld, ld, [&](int r0, int c0, T (&acc)[4][4]) {  // A2
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) rB[(r0 + i) * ld + c0 + j] = acc[i][j];
+  });
+  __syncthreads();
+  const T c6 = (T)(1.0 / 6.0), c24 = (T)(1.0 / 24.0), c2 = (T)0.5;
+  for (int e = threadIdx.x; e < ld * ld; e += blockDim.x) rC[e] = c6 * rA[e] + c24 * rB[e];
+  __syncthreads();
+  T* Dr = D + b * (int64_t)m * m;
+  rgemm_4x4<T>(rB, rC, ld, ld, [&](int r0, int c0, T (&acc)[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int r = r0 + i, c = c0 + j;
+        if (r < m && c < m) Dr[r * m + c] = rA[r * ld + c] + c2 * rB[r * ld + c] + acc[i][j];
+      }
+  });
+}
+
+// Real counterpart of block_matrix_kernel for the Hermitian real form:
+// out rows 0..m-1 = D_K = P^K - I, then the selected rows R_k of D_k for
+// k = 1..K-1 (row m + (k-1) nsel + q = row sel[q] of D_k).
+// Shared memory holds the squares D_{2^j} (padded to ld = 4 ceil(m/4)), two
+// accumulators for the binary powering of D_K, and the selected rows, built
+// by doubling: R_{i+b} = R_i + R_b + R_i D_b for b = 2^j, so every product is
+// a 4 x 4-tiled GEMM against a square already in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    block_matrix_real_kernel(const T* __restrict__ D, int m, int K, const int* __restrict__ sel,
+                             int nsel, T* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ld = (m + 3) & ~3;
+  const int mm = ld * ld;
+  int J = 0;
+  while ((2 << J) <= K) ++J;                 // squares D_{2^0} .. D_{2^J}
+  T* sq = (T*)smraw;                          // [J + 1][ld][ld]
+  T* acc0 = sq + (size_t)(J + 1) * mm;        // [ld][ld]
+  T* acc1 = acc0 + mm;
+  const int rrows = ((nsel * (K - 1) + 3) & ~3) + 4;
+  T* sR = acc1 + mm;                          // [rrows][ld] selected rows R_1 .. R_{K-1}
+  const int64_t b = blockIdx.x;
+  const int rows = m + nsel * (K - 1);
+  const T* d = D + b * (int64_t)m * m;
+  // samples are padded to a multiple of four values, so every sample starts
+  // on a 16-byte boundary (the time loop prefetches them with 16-byte copies)
+  T* o = out + b * (((int64_t)rows * m + 3) & ~(int64_t)3);
+  // zero everything first: the padding rows and columns of every matrix
+  // must stay zero because the tiled products read them
+  const int total = (J + 3) * mm + rrows * ld;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) sq[e] = (T)0;
+  __syncthreads();
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) sq[(e / m) * ld + e % m] = d[e];
+  __syncthreads();
+  for (int j = 1; j <= J; ++j) {
+    const T* X = sq + (size_t)(j - 1) * mm;
+    compose_into<T>(X, X, ld, ld, m, sq + (size_t)j * mm, ld);
+    __syncthreads();
+  }
+  // selected rows: R_1 = rows of D, then doubling
+  for (int e = threadIdx.x; e < nsel * ld; e += blockDim.x) {
+    const int q = e / ld, c = e % ld;
+    int r = sel[q];
+    r = (r >= 0 && r < m) ? r : 0;
+    sR[e] = sq[r * ld + c];
+  }
+  __syncthreads();
+  int have = 1;  // R_1 .. R_have are in sR
+  for (int j = 0; have < K - 1; ++j) {
+    const int bpow = 1 << j;  // have == bpow here
+    const int add = min(bpow, K - 1 - have);
+    const T* Db = sq + (size_t)j * mm;
+    const int arows = ((add * nsel + 3) & ~3);
+    T* dst = sR + (size_t)have * nsel * ld;
+    const T* Rb = sR + (size_t)(bpow - 1) * nsel * ld;  // rows of D_b
+    rgemm_4x4<T>(sR, Db, ld, arows, [&](int r0, int c0, T (&acc)[4][4]) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const int r = r0 + i, c = c0 + jj;
+          if (r < add * nsel && c < m)
+            dst[r * ld + c] = (sR[r * ld + c] + Rb[(r % nsel) * ld + c]) + acc[i][jj];
+        }
+    });
+    __syncthreads();
+    have += add;
+  }
+  for (int e = threadIdx.x; e < nsel * (K - 1) * m; e += blockDim.x) {
+    const int rr = e / m, c = e % m;
+    o[(int64_t)(m + rr) * m + c] = sR[rr * ld + c];
+  }
+  // D_K by binary powering over the squares
+  const T* cur = nullptr;
+  T* bufs[2] = {acc0, acc1};
+  int nb = 0;
+  int bits = K, j = 0, remaining = 0;
+  for (int t = K; t; t &= t - 1) ++remaining;
+  for (; bits; bits >>= 1, ++j) {
+    if (!(bits & 1)) continue;
+    const T* S = sq + (size_t)j * mm;
+    --remaining;
+    if (cur == nullptr) {
+      cur = S;
+      if (remaining == 0)
+        for (int e = threadIdx.x; e < m * m; e += blockDim.x) o[e] = S[(e / m) * ld + e % m];
+    } else if (remaining == 0) {
+      compose_into<T>(cur, S, ld, ld, m, o, m);
+    } else {
+      T* Z = bufs[nb];
+      nb ^= 1;
+      compose_into<T>(cur, S, ld, ld, m, Z, ld);
+      __syncthreads();
+      cur = Z;
+    }
+  }
+}
+
+// Real form of every sample's complex matrix (a Hermiticity-preserving map
+// on n x n matrices), one thread per entry.
+template <typename T>
+__global__ void hermitian_form_kernel(const typename cplx<T>::type* __restrict__ A, int n,
+                                      int64_t batch, T* __restrict__ R) {
+  const int m = n * n;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= batch * m * m) return;
+  const int64_t b = t / ((int64_t)m * m);
+  const int e = (int)(t % ((int64_t)m * m));
+  R[t] = hermitian_entry(A + b * (int64_t)m * m, m, n, e / m, e % m);
+}
+
 }  // namespace qsx
 
 using namespace qsx;
 
 extern "C" {
+
+int qsx_hermitian_real_form(const void* A, int n, int64_t batch, int precision, void* R,
+                            void* stream) {
+  QSX_CHECK_ARG(n >= 1 && n <= 32 && batch >= 0 && (precision == QSX_FP32 || precision == QSX_FP64),
+                "qsx_hermitian_real_form: bad arguments (n=%d)", n);
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(A && R, "qsx_hermitian_real_form: null pointer");
+  const int64_t total = batch * (int64_t)n * n * n * n;
+  const unsigned grid = (unsigned)((total + 255) / 256);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (precision == QSX_FP32)
+    hermitian_form_kernel<float><<<grid, 256, 0, s>>>((const float2*)A, n, batch, (float*)R);
+  else
+    hermitian_form_kernel<double><<<grid, 256, 0, s>>>((const double2*)A, n, batch, (double*)R);
+  QSX_LAUNCH_CHECK("qsx_hermitian_real_form");
+  return QSX_OK;
+}
+
+int qsx_rk4_block_matrix_real_batched(const void* D, int m, int64_t batch, int precision, int K,
+                                      const int* select, int nselect, void* out, void* stream) {
+  QSX_CHECK_ARG(m >= 1 && m <= 64 && K >= 1 && K <= 64 && nselect >= 0 && nselect <= m,
+                "qsx_rk4_block_matrix_real_batched: need m <= 64, 1 <= K <= 64, nselect <= m");
+  QSX_CHECK_ARG(batch >= 0 && batch <= 0x7fffffff, "qsx_rk4_block_matrix_real_batched: bad batch");
+  QSX_CHECK_ARG(precision == QSX_FP32 || precision == QSX_FP64,
+                "qsx_rk4_block_matrix_real_batched: bad precision");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(D && out && (nselect == 0 || select),
+                "qsx_rk4_block_matrix_real_batched: null pointer");
+  const size_t rs = precision == QSX_FP32 ? sizeof(float) : sizeof(double);
+  const size_t ld = ((size_t)m + 3) & ~(size_t)3;
+  int J = 0;
+  while ((2 << J) <= K) ++J;
+  const size_t rrows = (((size_t)nselect * (K - 1) + 3) & ~(size_t)3) + 4;
+  const size_t smem = ((size_t)(J + 3) * ld * ld + rrows * ld) * rs;
+  if (smem > 227 * 1024) {
+    set_error("qsx_rk4_block_matrix_real_batched: %zu bytes of shared memory needed", smem);
+    return QSX_ERR_UNSUPPORTED;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e;
+  if (precision == QSX_FP32) {
+    e = cudaFuncSetAttribute(block_matrix_real_kernel<float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_block_matrix_real_batched");
+    block_matrix_real_kernel<float><<<(unsigned)batch, 256, smem, s>>>(
+        (const float*)D, m, K, select, nselect, (float*)out);
+  } else {
+    e = cudaFuncSetAttribute(block_matrix_real_kernel<double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_block_matrix_real_batched");
+    block_matrix_real_kernel<double><<<(unsigned)batch, 256, smem, s>>>(
+        (const double*)D, m, K, select, nselect, (double*)out);
+  }
+  QSX_LAUNCH_CHECK("qsx_rk4_block_matrix_real_batched");
+  return QSX_OK;
+}
 
 int qsx_debye_corr(const double* x, int64_t n, double temperature,
                    double reorg_energy, double cutoff_freq, int matsubara_cutoff,
@@ -800,6 +1158,44 @@ int qsx_redfield_liouvillian_batched(const double* H, int64_t H_stride, const do
   return QSX_OK;
 }
 
+
+int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
+                                              const double* G, const double* M,
+                                              const double* occ, int n, int n_sites,
+                                              int64_t batch, double unit_convert,
+                                              const int* states, int nb, const int* rowptr,
+                                              const int* cols, const float* vals, double h,
+                                              int precision, void* D, void* stream) {
+  QSX_CHECK_ARG(nb >= 1 && nb <= 8 && n >= nb && n_sites >= 1 && batch >= 0 &&
+                    (precision == QSX_FP32 || precision == QSX_FP64),
+                "qsx_redfield_propagator_hermitian_batched: bad sizes (n=%d, nb=%d)", n, nb);
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(H && G && M && occ && states && rowptr && cols && vals && D,
+                "qsx_redfield_propagator_hermitian_batched: null pointer");
+  const int m = nb * nb, ld = (m + 3) & ~3;
+  const size_t rs = precision == QSX_FP32 ? sizeof(float) : sizeof(double);
+  const size_t smem = (3 * (size_t)ld * ld + 2 * (size_t)nb * m + m) * rs + nb * sizeof(int);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e;
+  if (precision == QSX_FP32) {
+    e = cudaFuncSetAttribute(hermitian_propagator_kernel<float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_hermitian_batched");
+    hermitian_propagator_kernel<float><<<(unsigned)batch, 256, smem, s>>>(
+        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, states, nb, rowptr,
+        cols, vals, unit_convert, h, (float*)D);
+  } else {
+    e = cudaFuncSetAttribute(hermitian_propagator_kernel<double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_hermitian_batched");
+    hermitian_propagator_kernel<double><<<(unsigned)batch, 256, smem, s>>>(
+        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, states, nb, rowptr,
+        cols, vals, unit_convert, h, (double*)D);
+  }
+  QSX_LAUNCH_CHECK("qsx_redfield_propagator_hermitian_batched");
+  return QSX_OK;
+}
+
 int qsx_redfield_propagator_batched(const double* H, int64_t H_stride, const double* G,
                                     const double* M, const double* occ, int n, int n_sites,
                                     int64_t batch, double unit_convert, const int* idx, int m,
@@ -817,7 +1213,10 @@ int qsx_redfield_propagator_batched(const double* H, int64_t H_stride, const dou
                 "qsx_redfield_propagator_batched: null pointer");
   const size_t nn = (size_t)n * n;
   const size_t cs = precision == QSX_FP32 ? sizeof(float2) : sizeof(double2);
-  const size_t smem = ((size_t)n * nn + nn + 3 * (size_t)m * m) * cs + (size_t)m * sizeof(int);
+  const size_t smem = ((size_t)n * nn + nn + 3 * (size_t)m * m) * cs +
+                      (((size_t)m + 3) & ~(size_t)3) * sizeof(int) +
+                      (1 + (size_t)n_sites) * nn * cs +
+                      (size_t)n_sites * n * (cs / 2);
   if (smem > 227 * 1024) {
     set_error("qsx_redfield_propagator_batched: %zu bytes of shared memory needed; use "
               "qsx_redfield_liouvillian_batched + qsx_rk4_propagator_batched", smem);

@@ -44,7 +44,8 @@ class RedfieldBuild:
         self.unit_convert = unit_convert
         self.secular = secular
         self.evolve_basis = evolve_basis
-        self.occ = torch.as_tensor(occ, dtype=torch.float64, device=H.device).contiguous()
+        self.occ = _native.const_tensor(np.asarray(occ, dtype=np.float64), torch.float64,
+                                        H.device)
         bounds = manifold_bounds(n_sites, hilbert_subspace)
         if self.n <= EIGH_JACOBI_MAX:
             self.E, self.U = _native.eigh(H, bounds)
@@ -66,17 +67,29 @@ class RedfieldBuild:
         the block first.
         """
         if self.site_ops and len(idx) <= 64:
-            idx_t = torch.as_tensor(np.asarray(idx), dtype=torch.int32, device=self.H.device)
+            idx_t = _native.const_tensor(np.asarray(idx, dtype=np.int32), torch.int32,
+                                         self.H.device)
             D = _native.redfield_propagator(self.H, self.G, self.M, self.occ, idx_t,
                                             self.unit_convert, h, precision, transpose)
             if D is not None:
                 return D
         return _native.rk4_propagator(self.block(idx, transpose), h, precision)
 
+    def hermitian_propagator(self, idx, nb, h, precision=_native.QSX_FP32):
+        """(S, nb^2, nb^2) real one-step propagator D_r = P_r - I of the
+        diagonal block of nb x nb states ``idx`` (column-stacked), in the
+        Hermitian coordinates of ``hermitian_coordinates``."""
+        if self.site_ops and len(idx) <= 64:
+            states = np.asarray(idx)[:nb] % self.n
+            return _native.redfield_propagator_hermitian(self.H, self.G, self.M, self.occ,
+                                                         states, self.unit_convert, h,
+                                                         precision)
+        return _native.hermitian_real_form(self.propagator(idx, h, precision), nb)
+
     def block(self, idx, transpose=False):
         """(S, m, m) complex128 generator on the column-stacked indices ``idx``."""
         idx_np = np.asarray(idx, dtype=np.int64)
-        idx_t = torch.as_tensor(idx_np, dtype=torch.int32, device=self.H.device)
+        idx_t = _native.const_tensor(idx_np.astype(np.int32), torch.int32, self.H.device)
         uc = self.unit_convert
         if self.site_ops:
             return _native.redfield_liouvillian(self.H, self.G, self.M, idx_t, uc,

@@ -134,6 +134,132 @@ def propagate_selected_mean(D, y0, nsteps, select, precision, events=None):
     return out
 
 
+# The real (Hermitian) form of diagonal population blocks: on by default for
+# FP32 ensembles; set_hermitian_form(False) keeps the complex blocked loop.
+_HERMITIAN = True
+
+
+def set_hermitian_form(enabled=True):
+    global _HERMITIAN
+    _HERMITIAN = bool(enabled)
+
+
+def hermitian_coordinates(y, n):
+    """Real coordinates x[a + n b] = Re rho_ab (a <= b), Im rho_ba (a > b) of
+    column-stacked n x n Hermitian matrices y (..., n^2) (numpy or torch)."""
+    a, b = np.divmod(np.arange(n * n), n)[::-1]
+    src = np.where(a <= b, a + n * b, b + n * a)
+    take_re = a <= b
+    if isinstance(y, torch.Tensor):
+        v = y[..., _native.const_tensor(src, torch.int64, y.device)]
+        return torch.where(_native.const_tensor(take_re, torch.bool, y.device), v.real, v.imag)
+    v = np.asarray(y)[..., src]
+    return np.where(take_re, v.real, v.imag)
+
+
+def from_hermitian_coordinates(x, n):
+    """Column-stacked complex matrices from Hermitian coordinates (inverse of
+    hermitian_coordinates); x (..., n^2) real, numpy or torch."""
+    a, b = np.divmod(np.arange(n * n), n)[::-1]
+    lo, hi = np.minimum(a, b), np.maximum(a, b)
+    re_idx = lo + n * hi
+    im_idx = hi + n * lo
+    sign = np.where(a < b, 1.0, np.where(a > b, -1.0, 0.0))
+    if isinstance(x, torch.Tensor):
+        dev = x.device
+        re = x[..., _native.const_tensor(re_idx, torch.int64, dev)]
+        im = (x[..., _native.const_tensor(im_idx, torch.int64, dev)]
+              * _native.const_tensor(sign, x.dtype, dev))
+        return torch.complex(re, im)
+    x = np.asarray(x)
+    return x[..., re_idx] + 1j * sign * x[..., im_idx]
+
+
+def pick_block_k_real(nsteps, m, nselect, max_k=64):
+    """K minimising the executed work of the real blocked loop: per block-step
+    (m + nsel (K-1)) m multiply-adds (weighted twice: the loop is the
+    latency-bound part), plus the block build, nsel m^2 (K-2) for the
+    selected rows and m^3 per product of the binary powering."""
+    best, best_cost = 1, None
+    for K in range(2, max_k + 1):
+        if nsteps % K or m + nselect * (K - 1) > 512:
+            continue
+        products = bin(K).count('1') - 1 + K.bit_length() - 1
+        cost = (2.0 * (nsteps // K) * (m + nselect * (K - 1)) * m
+                + nselect * m * m * max(K - 2, 0) + products * m ** 3)
+        if best_cost is None or cost < best_cost:
+            best, best_cost = K, cost
+    return best
+
+
+def hermitian_block_size(idx, n_total):
+    """nb when the column-stacked indices ``idx`` form one diagonal block of
+    nb x nb states (e.g. 'ee'), else None."""
+    idx = np.asarray(idx)
+    rows, cols = idx % n_total, idx // n_total
+    states = np.unique(rows)
+    nb = len(states)
+    if nb * nb != len(idx) or not np.array_equal(np.unique(cols), states):
+        return None
+    expect = (states[None, :] + n_total * states[:, None]).reshape(-1)
+    return nb if np.array_equal(np.sort(idx), np.sort(expect)) else None
+
+
+def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None):
+    """FP32 ensemble mean of the selected components of a Hermitian diagonal
+    block through its real form: real propagator, real K-step blocked matrix
+    and real blocked loop.  Returns {'mean': (nsteps + 1, len(select))
+    complex128, 'status'} like propagate_selected_mean."""
+    m = nb * nb
+    sel = np.asarray(select, dtype=np.int64)
+    a, b = sel % nb, sel // nb
+    partner = np.where(a == b, sel, b + nb * a)
+    coords = np.unique(np.concatenate([sel, partner]))
+    Dr = build.hermitian_propagator(idx, nb, h)
+    K = pick_block_k_real(nsteps, m, len(coords))
+    mat = _native.rk4_block_matrix_real(Dr, K, coords)
+    del Dr
+    x0 = hermitian_coordinates(y0, nb)
+    if events is not None:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+    if K > 1:
+        xm, status = _native.rk4_real_block_mean(mat, x0, nsteps, coords, K, check_finite=False)
+    else:
+        raise NotImplementedError('the real blocked loop needs a block size K > 1')
+    if events is not None:
+        e1 = torch.cuda.Event(enable_timing=True)
+        e1.record()
+        events.setdefault('dyn', []).append((e0, e1))
+        events['dyn_flops'] = 2.0 * mat.shape[0] * (nsteps // K) * mat.shape[1] * m
+        events['dyn_block_k'] = K
+        events['dyn_variant'] = 'real'
+    full = torch.zeros((xm.shape[0], m), dtype=torch.float64, device=xm.device)
+    full[:, _native.const_tensor(coords, torch.int64, xm.device)] = xm
+    y = from_hermitian_coordinates(full, nb)
+    return {'mean': y[:, _native.const_tensor(sel, torch.int64, xm.device)], 'status': status}
+
+
+def can_use_hermitian(precision, idx, n_total, y0, nsteps):
+    """Whether the real Hermitian form applies: FP32, a diagonal block of
+    3..8 states, a Hermitian initial state and at least one K > 1."""
+    if not _HERMITIAN or precision != _native.QSX_FP32:
+        return None
+    nb = hermitian_block_size(idx, n_total)
+    if nb is None or not 3 <= nb <= 8:
+        return None
+    y = y0.detach().cpu().numpy() if isinstance(y0, torch.Tensor) else np.asarray(y0)
+    if y.ndim != 1:
+        return None
+    rho = y.reshape(nb, nb, order='F')
+    if np.abs(rho - rho.conj().T).max() > 1e-14 * max(np.abs(rho).max(), 1e-300):
+        return None
+    m = nb * nb
+    if pick_block_k_real(nsteps, m, m) == 1 and pick_block_k_real(nsteps, m, nb) == 1:
+        return None
+    return nb
+
+
 def redfield_batch_build(model, batch):
     if not isinstance(model, RedfieldModel):
         raise NotImplementedError('batched ensembles need a RedfieldModel')
@@ -219,7 +345,6 @@ def ensemble_populations(model, initial_state, duration, ensemble_size,
         rho0 = np.outer(rho0.conj(), rho0)
     y0 = model.density_matrix_to_state_vector(rho0, liouville_subspace)
     idx = model.liouville_subspace_index(liouville_subspace)
-    D = build.propagator(idx, dt, prec)
     M = len(idx)
     if full_state:
         select = list(range(M))
@@ -227,7 +352,13 @@ def ensemble_populations(model, initial_state, duration, ensemble_size,
         nn = int(round(np.sqrt(M)))
         select = [i * nn + i for i in range(nn)]
     y0t = torch.as_tensor(y0, dtype=torch.complex128).cuda()
-    out = propagate_selected_mean(D, y0t, len(t) - 1, select, prec)
+    n_total = model.hamiltonian.n_states(model.hilbert_subspace)
+    nb = can_use_hermitian(prec, idx, n_total, y0, len(t) - 1)
+    if nb is not None:
+        out = propagate_hermitian_mean(build, idx, nb, dt, y0t, len(t) - 1, select)
+    else:
+        out = propagate_selected_mean(build.propagator(idx, dt, prec), y0t, len(t) - 1,
+                                      select, prec)
     if int(out['status'].item()) & _native.QSX_ERR_NONFINITE:
         raise _native.IntegratorError('non-finite state in ensemble propagation')
     return t, out['mean']
@@ -273,8 +404,8 @@ class RedfieldEnsembleWorkload:
         rho = np.asarray(initial_state)
         if rho.ndim == 1:
             rho = np.outer(rho.conj(), rho)
-        self.y_dyn = torch.as_tensor(model.density_matrix_to_state_vector(rho, 'ee'),
-                                     dtype=torch.complex128, device=dev)
+        self.y_dyn_np = np.asarray(model.density_matrix_to_state_vector(rho, 'ee'), complex)
+        self.y_dyn = torch.as_tensor(self.y_dyn_np, dtype=torch.complex128, device=dev)
         self.select = [i * self.n_sites + i for i in range(self.n_sites)]
         self.freqs_np = (fft_frequencies(self.t_abs, model.rw_freq, model.unit_convert)
                          if freqs is None else np.asarray(freqs, float))
@@ -309,9 +440,15 @@ class RedfieldEnsembleWorkload:
                               per_sample=False, mean=True, check_finite=False)
             X = _native.dft(-sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
                             self.model.rw_freq, self.model.unit_convert, 1)
-        D_ee = build.propagator(self.idx_ee, self.dt, prec)
-        pop = propagate_selected_mean(D_ee, self.y_dyn, len(self.t_dyn) - 1, self.select,
-                                      prec, events)
+        nb = can_use_hermitian(prec, self.idx_ee, self.n_sites + 1, self.y_dyn_np,
+                               len(self.t_dyn) - 1)
+        if nb is not None:
+            pop = propagate_hermitian_mean(build, self.idx_ee, nb, self.dt, self.y_dyn,
+                                           len(self.t_dyn) - 1, self.select, events)
+        else:
+            D_ee = build.propagator(self.idx_ee, self.dt, prec)
+            pop = propagate_selected_mean(D_ee, self.y_dyn, len(self.t_dyn) - 1, self.select,
+                                          prec, events)
         main.wait_stream(self._side)
         for t in (X, sig['status']):
             t.record_stream(main)

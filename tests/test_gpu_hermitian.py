@@ -1,0 +1,122 @@
+"""Real (Hermitian) form of diagonal population blocks: the coordinate map,
+the fused real propagator, the real K-step blocked matrix and loop, and the
+ensemble drivers that use them, against the complex path and the oracle."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as orc
+import qspectra_gb300 as qg
+from conftest import rel_err
+from qspectra_gb300 import _native
+from qspectra_gb300 import workloads as wl
+from qspectra_gb300.simulate import ensemble as ens
+
+pytestmark = pytest.mark.gpu
+
+
+def lindblad_maps(n, B, seed):
+    """Random Hermiticity-preserving generators -i[H, .] + K . K^+ - {K^+K, .}/2."""
+    rng = np.random.RandomState(seed)
+    I = np.eye(n)
+    out = []
+    for _ in range(B):
+        H = rng.randn(n, n)
+        H = H + H.T
+        K = rng.randn(n, n) + 1j * rng.randn(n, n)
+        KK = K.conj().T @ K
+        out.append(-1j * (np.kron(I, H) - np.kron(H.T, I)) + np.kron(K.conj(), K)
+                   - 0.5 * (np.kron(I, KK) + np.kron(KK.T, I)))
+    return np.array(out)
+
+
+def real_form_np(L, n):
+    x = np.eye(n * n)
+    cols = ens.from_hermitian_coordinates(x, n)              # basis matrices as columns
+    return np.array([ens.hermitian_coordinates((Lb @ cols.T).T, n).T for Lb in L])
+
+
+@pytest.mark.parametrize('n', [3, 5, 7])
+def test_real_form_kernel(n):
+    L = lindblad_maps(n, 4, seed=n)
+    ref = real_form_np(L, n)
+    for dt, tol in ((torch.complex128, 1e-14), (torch.complex64, 1e-6)):
+        R = _native.hermitian_real_form(torch.as_tensor(L).to(dt).cuda(), n).cpu().numpy()
+        assert rel_err(R, ref) < tol
+
+
+def fmo_build(S=6, nsites=7):
+    H = wl.fmo7_hamiltonian(nsites)
+    ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 77, 35, 106),
+                                   dipoles=[[1, 0, 0]] * nsites, disorder=wl.fwhm_for_sd(80.0),
+                                   random_seed=1,
+                                   energy_spread_extra=wl.energy_spread_for_dt(H, 1.0, qg.CM_FS))
+    m = qg.RedfieldModel(ham, hilbert_subspace='ge', unit_convert=qg.CM_FS, secular=False)
+    batch = ens.SampleBatch(m, S)
+    return m, m.build_batch(batch.H('ge'))
+
+
+@pytest.mark.parametrize('precision,tol', [(_native.QSX_FP64, 1e-12), (_native.QSX_FP32, 2e-5)])
+def test_fused_real_propagator_matches_complex(precision, tol):
+    m, build = fmo_build()
+    idx = m.liouville_subspace_index('ee')
+    D = build.propagator(idx, 1.0, _native.QSX_FP64)
+    ref = _native.hermitian_real_form(D, 7).cpu().numpy()
+    Dr = build.hermitian_propagator(idx, 7, 1.0, precision).cpu().numpy()
+    assert rel_err(Dr, ref) < tol
+
+
+def test_real_block_matrix_and_loop_match_numpy():
+    rng = np.random.RandomState(3)
+    n, B, K, nsteps = 4, 5, 4, 24
+    m = n * n
+    L = 0.05 * real_form_np(lindblad_maps(n, B, seed=9), n)
+    P = np.array([np.eye(m) + Lb + Lb @ Lb / 2 for Lb in L])      # any real propagator
+    D = P - np.eye(m)
+    sel = [0, 5, 10, 15, 3]
+    mat = _native.rk4_block_matrix_real(torch.as_tensor(D).cuda(), K, sel).cpu().numpy()
+    for b in range(B):
+        assert rel_err(mat[b, :m], np.linalg.matrix_power(P[b], K) - np.eye(m)) < 1e-13
+        for k in range(1, K):
+            Dk = np.linalg.matrix_power(P[b], k) - np.eye(m)
+            assert rel_err(mat[b, m + (k - 1) * len(sel):m + k * len(sel)], Dk[sel]) < 1e-13
+    mat32 = _native.rk4_block_matrix_real(torch.as_tensor(D).float().cuda(), K, sel)
+    x0 = rng.randn(B, m)
+    mean, _ = _native.rk4_real_block_mean(mat32, torch.as_tensor(x0).cuda(), nsteps, sel, K)
+    xs = np.array([[np.linalg.matrix_power(P[b], t) @ x0[b] for t in range(nsteps + 1)]
+                   for b in range(B)])
+    assert rel_err(mean.cpu().numpy(), xs.mean(0)[:, sel]) < 2e-6
+
+
+@pytest.mark.parametrize('full_state', [False, True])
+def test_ensemble_populations_real_form_matches_complex_and_fp64(full_state):
+    m, _ = fmo_build()
+    psi = np.zeros(7)
+    psi[2] = 1.0
+    args = (m, psi, 600.0, 64, 'ee')
+    t, r64 = ens.ensemble_populations(*args, precision='fp64', full_state=full_state)
+    _, r32 = ens.ensemble_populations(*args, precision='fp32', full_state=full_state)
+    ens.set_hermitian_form(False)
+    try:
+        _, c32 = ens.ensemble_populations(*args, precision='fp32', full_state=full_state)
+    finally:
+        ens.set_hermitian_form(True)
+    r64, r32, c32 = (x.cpu().numpy() for x in (r64, r32, c32))
+    assert rel_err(r32, r64) < 1e-5
+    assert rel_err(c32, r64) < 1e-5
+
+
+def test_workload_uses_real_form_and_matches_fp64():
+    from qspectra_gb300.simulate.ensemble import RedfieldEnsembleWorkload
+    m, _ = fmo_build()
+    psi = np.zeros(7)
+    psi[0] = 1.0
+    work = RedfieldEnsembleWorkload(m, 512.0, 1000.0, psi)
+    offs = torch.as_tensor(m.hamiltonian.disorder_offsets(256)).cuda()
+    ev = {}
+    X32, P32, st = work.run(offs, 'fp32', ev)
+    X64, P64, _ = work.run(offs, 'fp64')
+    assert ev['dyn_variant'] == 'real'
+    assert int(st.item()) == 0
+    assert rel_err(P32.cpu().numpy(), P64.cpu().numpy()) < 1e-5
+    assert rel_err(X32.cpu().numpy(), X64.cpu().numpy()) < 1e-5
