@@ -74,6 +74,9 @@ int qsx_eigh_batched(const double* H, int n, int64_t batch, int nblocks,
  *   E [batch][n], U [batch][n][n], occ [n_sites][n] (shared),
  *   G complex128 [batch][n][n], M complex128 [batch][n_sites][n][n],
  *   K real [batch][n_sites][n][n].  n <= 32, n_sites <= 32.
+ * precision QSX_FP64 evaluates everything in FP64; QSX_FP32 evaluates the
+ * same formulas in FP32 (for generators that feed the FP32 split-word
+ * propagation), with the outputs still stored as complex128 / double.
  */
 int qsx_redfield_operators_batched(const double* E, const double* U, int n,
                                    int64_t batch, const double* occ,
@@ -81,7 +84,7 @@ int qsx_redfield_operators_batched(const double* E, const double* U, int n,
                                    double reorg_energy, double cutoff_freq,
                                    int matsubara_cutoff, int discard_imag_corr,
                                    double unit_convert, int site_basis,
-                                   double* G, double* M, double* K,
+                                   int precision, double* G, double* M, double* K,
                                    void* stream);
 
 /*

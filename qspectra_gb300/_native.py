@@ -93,7 +93,7 @@ _PROTOS = {
                                   _c_vp]),
     'qsx_redfield_operators_batched': (_c_int, [
         _c_vp, _c_vp, _c_int, _c_i64, _c_vp, _c_int, _c_dbl, _c_dbl, _c_dbl,
-        _c_int, _c_int, _c_dbl, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
+        _c_int, _c_int, _c_dbl, _c_int, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
     'qsx_redfield_liouvillian_batched': (_c_int, [
         _c_vp, _c_i64, _c_vp, _c_vp, _c_vp, _c_i64, _c_vp, _c_int, _c_int,
         _c_i64, _c_dbl, _c_vp, _c_int, _c_int, _c_int, _c_vp, _c_vp]),
@@ -236,7 +236,7 @@ def eigh(H, block_starts):
 
 
 def redfield_operators(E, U, occ, bath, unit_convert, discard_imag_corr=False,
-                       site_basis=True, matsubara_cutoff=1000):
+                       site_basis=True, matsubara_cutoff=1000, precision=QSX_FP64):
     require_gpu()
     _need(E, torch.float64, 'E', 2)
     _need(U, torch.float64, 'U', 3)
@@ -251,7 +251,7 @@ def redfield_operators(E, U, occ, bath, unit_convert, discard_imag_corr=False,
     _check(load().qsx_redfield_operators_batched(
         _p(E), _p(U), n, B, _p(occ), N, bath.temperature, bath.reorg_energy,
         bath.cutoff_freq, matsubara_cutoff, int(discard_imag_corr), unit_convert,
-        int(site_basis), _p(G), _p(M), _p(K), _stream()),
+        int(site_basis), int(precision), _p(G), _p(M), _p(K), _stream()),
         'qsx_redfield_operators_batched')
     return G, M, K
 

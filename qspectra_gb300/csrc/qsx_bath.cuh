@@ -119,6 +119,87 @@ __device__ __forceinline__ void debye_corr_pair(const DebyeParams& p, double x, 
   cneg = debye_from_matsubara(p, -x, cconj(S));
 }
 
+// Single-precision form of the same closed form, for builds whose generator
+// feeds the FP32 split-word propagation: the series, logarithm and arctangent
+// evaluated in FP32 (relative error a few units in 1e-7).
+__device__ __forceinline__ float2 digamma_asymptotic_f(float2 z) {
+  const float c1 = 1.0f / 12.0f, c2 = -1.0f / 120.0f, c3 = 1.0f / 252.0f,
+              c4 = -1.0f / 240.0f, c5 = 1.0f / 132.0f, c6 = -691.0f / 32760.0f,
+              c7 = 1.0f / 12.0f;
+  const float2 zi = crecip(z);
+  const float2 zi2 = cmul(zi, zi);
+  float2 s = cmk(c7, 0.0f);
+  s = cadd(cmul(s, zi2), cmk(c6, 0.0f));
+  s = cadd(cmul(s, zi2), cmk(c5, 0.0f));
+  s = cadd(cmul(s, zi2), cmk(c4, 0.0f));
+  s = cadd(cmul(s, zi2), cmk(c3, 0.0f));
+  s = cadd(cmul(s, zi2), cmk(c2, 0.0f));
+  s = cadd(cmul(s, zi2), cmk(c1, 0.0f));
+  s = cmul(s, zi2);
+  const float2 lz = cmk(logf(hypotf(z.x, z.y)), atan2f(z.y, z.x));
+  return csub(csub(lz, cscale(zi, 0.5f)), s);
+}
+
+__device__ __forceinline__ float2 debye_matsubara_f(const DebyeParams& p, float x) {
+  const float c = (float)(2.0 * M_PI * p.T);
+  const float a = (float)p.gamma / c;
+  const float y = x / c;
+  const float2 amb = cmk(a, -y), apb = cmk(a, y);
+  const float2 A = cscale(crecip(amb), 0.5f);
+  const float2 B = cscale(crecip(apb), -0.5f);
+  const float2 D = cscale(cdiv(cmk(0.0f, y), cmul(amb, apb)), -1.0f);
+  float2 g = cmk(0.0f, 0.0f);
+  const int K = p.matsubara;
+  const int kmax = K < 9 ? K : 8;
+  for (int k = 1; k < kmax; ++k) {
+    const float inv = 1.0f / fmaf((float)k, (float)k, y * y);
+    g.x = fmaf((float)k, inv, g.x);
+    g.y = fmaf(y, inv, g.y);
+  }
+  if (K >= 9)
+    g = cadd(g, csub(digamma_asymptotic_f(cmk((float)K, -y)), digamma_asymptotic_f(cmk(8.0f, -y))));
+  const float2 S = cadd(cadd(cscale(A, (float)p.fa), cscale(B, (float)p.fb)), cmul(D, g));
+  return cscale(S, 1.0f / (c * c));
+}
+
+__device__ __forceinline__ float2 debye_from_matsubara_f(const DebyeParams& p, float x, float2 S) {
+  const float2 first = cdiv(cmk((float)p.cot_term, -1.0f), cmk((float)p.gamma, -x));
+  return cscale(cadd(first, cscale(S, (float)(4.0 * p.T))), (float)(p.lam * p.gamma));
+}
+
+__device__ __forceinline__ float2 debye_real_f(const DebyeParams& p, float x) {
+  const float lam = (float)p.lam, gam = (float)p.gamma, T = (float)p.T;
+  if (x == 0.0f) return cmk(T * 2.0f * lam / gam, 0.0f);
+  const float J = 2.0f * lam * gam * x / (gam * gam + x * x);
+  return cmk((1.0f / expm1f(x / T) + 1.0f) * J, 0.0f);
+}
+
+__device__ __forceinline__ void debye_corr_pair_f(const DebyeParams& p, float x, float2& cpos,
+                                                  float2& cneg) {
+  if (p.real_only) {
+    cpos = debye_real_f(p, x);
+    cneg = debye_real_f(p, -x);
+    return;
+  }
+  if (x == 0.0f) {
+    cpos = cneg = cmk((float)(p.lam * (2.0 * p.T / p.gamma)), (float)-p.lam);
+    return;
+  }
+  const float2 S = debye_matsubara_f(p, x);
+  cpos = debye_from_matsubara_f(p, x, S);
+  cneg = debye_from_matsubara_f(p, -x, cconj(S));
+}
+
+// precision dispatch used by templated builds
+__device__ __forceinline__ void debye_corr_pair_t(const DebyeParams& p, double x, double2& cp,
+                                                  double2& cn) {
+  debye_corr_pair(p, x, cp, cn);
+}
+__device__ __forceinline__ void debye_corr_pair_t(const DebyeParams& p, float x, float2& cp,
+                                                  float2& cn) {
+  debye_corr_pair_f(p, x, cp, cn);
+}
+
 // Host-side constants of the closed form (depend on T and gamma only).
 inline DebyeParams make_debye(double T, double lam, double gamma, int K,
                               int real_only) {

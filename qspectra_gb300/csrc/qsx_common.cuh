@@ -51,6 +51,24 @@ __host__ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
   }
 }
 __host__ __device__ __forceinline__ double2 crecip(double2 b) { return cdiv(cmk(1.0, 0.0), b); }
+// single-precision counterparts
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return cmk(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return cmk(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return cmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ float2 cconj(float2 a) { return cmk(a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return cmk(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ float2 cdiv(float2 a, float2 b) {
+  if (fabsf(b.x) >= fabsf(b.y)) {
+    float r = b.y / b.x, d = b.x + b.y * r;
+    return cmk((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  } else {
+    float r = b.x / b.y, d = b.y + b.x * r;
+    return cmk((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+  }
+}
+__host__ __device__ __forceinline__ float2 crecip(float2 b) { return cdiv(cmk(1.0f, 0.0f), b); }
 
 // acc += a * b  (complex multiply-accumulate, 4 FMAs)
 __device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {

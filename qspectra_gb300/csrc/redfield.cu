@@ -211,15 +211,19 @@ __global__ void __launch_bounds__(32 * EIGH_WARPS)
 // ------------------------------------------------- Redfield operator form
 // One CTA per sample.  Shared layout (n <= 32): U, Kt real; Cw, Mt, GS, T1
 // complex.  See qsx_redfield_operators_batched in qsx.h for the algebra.
-__device__ __forceinline__ void smem_matmul_rc(const double* A, const double2* B,
-                                               double2* C, int n, bool accumulate) {
+// T = double is the FP64 build; T = float evaluates the same formulas in FP32
+// for generators that feed the FP32 split-word propagation (outputs are
+// stored as complex128 either way).
+template <typename T>
+__device__ __forceinline__ void smem_matmul_rc(const T* A, const typename cplx<T>::type* B,
+                                               typename cplx<T>::type* C, int n, bool accumulate) {
   // C = A (real) * B (complex)
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     int r = e / n, c = e % n;
-    double2 acc = accumulate ? C[e] : cmk(0.0, 0.0);
+    typename cplx<T>::type acc = accumulate ? C[e] : cmk((T)0, (T)0);
     for (int k = 0; k < n; ++k) {
-      double a = A[r * n + k];
-      double2 bb = B[k * n + c];
+      const T a = A[r * n + k];
+      const typename cplx<T>::type bb = B[k * n + c];
       acc.x = fma(a, bb.x, acc.x);
       acc.y = fma(a, bb.y, acc.y);
     }
@@ -227,15 +231,16 @@ __device__ __forceinline__ void smem_matmul_rc(const double* A, const double2* B
   }
 }
 
-__device__ __forceinline__ void smem_matmul_crT(const double2* A, const double* B,
-                                                double2* C, int n) {
+template <typename T>
+__device__ __forceinline__ void smem_matmul_crT(const typename cplx<T>::type* A, const T* B,
+                                                typename cplx<T>::type* C, int n) {
   // C = A (complex) * B^T (real)
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     int r = e / n, c = e % n;
-    double2 acc = cmk(0.0, 0.0);
+    typename cplx<T>::type acc = cmk((T)0, (T)0);
     for (int k = 0; k < n; ++k) {
-      double bb = B[c * n + k];
-      double2 a = A[r * n + k];
+      const T bb = B[c * n + k];
+      const typename cplx<T>::type a = A[r * n + k];
       acc.x = fma(a.x, bb, acc.x);
       acc.y = fma(a.y, bb, acc.y);
     }
@@ -243,35 +248,39 @@ __device__ __forceinline__ void smem_matmul_crT(const double2* A, const double* 
   }
 }
 
+template <typename T>
 __global__ void __launch_bounds__(256)
     redfield_operators_kernel(const double* __restrict__ E, const double* __restrict__ U,
                               int n, int64_t batch, const double* __restrict__ occ,
                               int n_sites, DebyeParams bath, double uc, int site_basis,
                               double2* G, double2* M, double* K) {
-  extern __shared__ double2 smem2[];
+  using Cx = typename cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
   const int nn = n * n;
-  double2* sC = smem2;               // nn   (16-byte arrays first)
-  double2* sMt = sC + nn;            // nn
-  double2* sGS = sMt + nn;           // nn
-  double2* sT1 = sGS + nn;           // nn
-  double* sU = (double*)(sT1 + nn);  // nn
-  double* sUt = sU + nn;             // nn, U^T
-  double* sKt = sUt + nn;            // nn
-  double* sE = sKt + nn;             // n (<= 32), then 32 coupling weights of eigenvectors
+  Cx* sC = (Cx*)smraw;               // nn   (complex arrays first)
+  Cx* sMt = sC + nn;                 // nn
+  Cx* sGS = sMt + nn;                // nn
+  Cx* sT1 = sGS + nn;                // nn
+  T* sU = (T*)(sT1 + nn);            // nn
+  T* sUt = sU + nn;                  // nn, U^T
+  T* sKt = sUt + nn;                 // nn
+  T* sE = sKt + nn;                  // n (<= 32), then 32 coupling weights of eigenvectors
+  T* sOcc = sE + 64;                 // [n_sites][n]
   // occupied states of each site (occ != 0), found once per CTA so the
-  // element loops below issue no FP64 compares
-  int* sOccN = (int*)(sE + 64);      // [n_sites]
-  int* sOccS = sOccN + 32;           // [n_sites][n] state indices
+  // element loops below issue no compares on the occupations
+  int* sOccN = (int*)(sOcc + n_sites * n);  // [n_sites]
+  int* sOccS = sOccN + 32;                   // [n_sites][n] state indices
   const int64_t b = blockIdx.x;
   const double* u = U + b * nn;
   for (int e = threadIdx.x; e < nn; e += blockDim.x) {
     int r = e / n, c = e % n;
-    double v = u[e];
+    const T v = (T)u[e];
     sU[e] = v;
     sUt[c * n + r] = v;
-    sGS[e] = cmk(0.0, 0.0);
+    sGS[e] = cmk((T)0, (T)0);
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) sE[i] = E[b * n + i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sE[i] = (T)E[b * n + i];
+  for (int e = threadIdx.x; e < n_sites * n; e += blockDim.x) sOcc[e] = (T)occ[e];
   for (int i = threadIdx.x; i < n_sites; i += blockDim.x) {
     int cnt = 0;
     for (int st = 0; st < n; ++st)
@@ -281,11 +290,11 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   // coupling weight of eigenvector c: sum_s U[s][c]^2 (sum_i occ_i(s)^2)
   for (int c = threadIdx.x; c < n; c += blockDim.x) {
-    double wsum = 0.0;
+    T wsum = (T)0;
     for (int i = 0; i < n_sites; ++i)
       for (int k = 0; k < sOccN[i]; ++k) {
         const int st = sOccS[i * n + k];
-        const double o = occ[i * n + st], x = sU[st * n + c];
+        const T o = sOcc[i * n + st], x = sU[st * n + c];
         wsum = fma(o * o, x * x, wsum);
       }
     sE[32 + c] = wsum;
@@ -298,60 +307,63 @@ __global__ void __launch_bounds__(256)
   for (int e = threadIdx.x; e < nn; e += blockDim.x) {
     int c = e / n, d = e % n;
     if (c > d) continue;
-    if (sE[32 + c] > 0.0 && sE[32 + d] > 0.0) {
-      double2 cp, cn;
-      debye_corr_pair(bath, sE[d] - sE[c], cp, cn);
+    if (sE[32 + c] > (T)0 && sE[32 + d] > (T)0) {
+      Cx cp, cn;
+      debye_corr_pair_t(bath, sE[d] - sE[c], cp, cn);
       sC[e] = cp;
       sC[d * n + c] = cn;
     } else {
-      sC[e] = cmk(0.0, 0.0);
-      sC[d * n + c] = cmk(0.0, 0.0);
+      sC[e] = cmk((T)0, (T)0);
+      sC[d * n + c] = cmk((T)0, (T)0);
     }
   }
   __syncthreads();
+  const T uct = (T)uc;
   for (int i = 0; i < n_sites; ++i) {
-    const double* oc = occ + i * n;
+    const T* oc = sOcc + i * n;
     const int cnt = sOccN[i];
     const int* ost = sOccS + i * n;
     for (int e = threadIdx.x; e < nn; e += blockDim.x) {
       int c = e / n, d = e % n;
-      double acc = 0.0;
+      T acc = (T)0;
       for (int k = 0; k < cnt; ++k) {
         const int st = ost[k];
         acc = fma(sU[st * n + c] * oc[st], sU[st * n + d], acc);
       }
       sKt[e] = acc;
-      double2 cw = sC[e];
+      const Cx cw = sC[e];
       sMt[e] = cmk(acc * cw.x, acc * cw.y);
     }
     __syncthreads();
     double2* Mi = M + (b * n_sites + i) * nn;
     if (site_basis) {
-      smem_matmul_rc(sU, sMt, sT1, n, false);  // T1 = U Mt_i
+      smem_matmul_rc<T>(sU, sMt, sT1, n, false);  // T1 = U Mt_i
       __syncthreads();
-      smem_matmul_crT(sT1, sU, sMt, n);        // Mt_i <- T1 U^T (site basis)
+      smem_matmul_crT<T>(sT1, sU, sMt, n);        // Mt_i <- T1 U^T (site basis)
       __syncthreads();
       // G_site = sum_i diag(occ_i) M_i: row s of G gathers row s of every M_i
-      for (int e = threadIdx.x; e < nn; e += blockDim.x) Mi[e] = cscale(sMt[e], uc);
+      for (int e = threadIdx.x; e < nn; e += blockDim.x)
+        Mi[e] = make_double2((double)(sMt[e].x * uct), (double)(sMt[e].y * uct));
       for (int k = 0; k < cnt; ++k) {
         const int st = ost[k];
-        const double o = oc[st];
+        const T o = oc[st];
         for (int c = threadIdx.x; c < n; c += blockDim.x)
           sGS[st * n + c] = cadd(sGS[st * n + c], cscale(sMt[st * n + c], o));
       }
     } else {
-      smem_matmul_rc(sKt, sMt, sGS, n, true);  // GS += Kt_i Mt_i (eigenbasis)
+      smem_matmul_rc<T>(sKt, sMt, sGS, n, true);  // GS += Kt_i Mt_i (eigenbasis)
       __syncthreads();
       double* Ki = K + (b * n_sites + i) * nn;
       for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-        Mi[e] = cscale(sMt[e], uc);
-        Ki[e] = sKt[e];
+        Mi[e] = make_double2((double)(sMt[e].x * uct), (double)(sMt[e].y * uct));
+        Ki[e] = (double)sKt[e];
       }
     }
     __syncthreads();
   }
   double2* g = G + b * nn;
-  for (int e = threadIdx.x; e < nn; e += blockDim.x) g[e] = cscale(sGS[e], uc);
+  for (int e = threadIdx.x; e < nn; e += blockDim.x)
+    g[e] = make_double2((double)(sGS[e].x * uct), (double)(sGS[e].y * uct));
 }
 
 // ----------------------------------------------- dense Liouvillian block
@@ -1106,8 +1118,10 @@ int qsx_redfield_operators_batched(const double* E, const double* U, int n,
                                    double temperature, double reorg_energy,
                                    double cutoff_freq, int matsubara_cutoff,
                                    int discard_imag_corr, double unit_convert,
-                                   int site_basis, double* G, double* M, double* K,
-                                   void* stream) {
+                                   int site_basis, int precision, double* G, double* M,
+                                   double* K, void* stream) {
+  QSX_CHECK_ARG(precision == QSX_FP32 || precision == QSX_FP64,
+                "qsx_redfield_operators_batched: bad precision");
   QSX_CHECK_ARG(n >= 1 && n <= 32 && n_sites >= 1 && n_sites <= 32,
                 "qsx_redfield_operators_batched: need 1 <= n, n_sites <= 32 (got %d, %d)",
                 n, n_sites);
@@ -1121,17 +1135,25 @@ int qsx_redfield_operators_batched(const double* E, const double* U, int n,
   DebyeParams p = make_debye(temperature, reorg_energy, cutoff_freq, matsubara_cutoff,
                              discard_imag_corr);
   const size_t nn = (size_t)n * n;
-  const size_t smem = (3 * nn + 64) * sizeof(double) + 4 * nn * sizeof(double2) +
+  const size_t rs = precision == QSX_FP32 ? sizeof(float) : sizeof(double);
+  const size_t smem = (3 * nn + 64 + (size_t)n_sites * n) * rs + 4 * nn * 2 * rs +
                       (32 + (size_t)n_sites * n) * sizeof(int);
-  cudaError_t e = cudaFuncSetAttribute(redfield_operators_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_operators_batched");
   // one thread per matrix element (n^2 <= 1024), rounded to whole warps
   const int threads = std::min(256, (int)((nn + 31) / 32) * 32);
-  redfield_operators_kernel<<<(unsigned)batch, threads, smem, (cudaStream_t)stream>>>(
-      E, U, n, batch, occ, n_sites, p, unit_convert, site_basis, (double2*)G,
-      (double2*)M, K);
+  cudaError_t e;
+  if (precision == QSX_FP32) {
+    e = cudaFuncSetAttribute(redfield_operators_kernel<float>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_operators_batched");
+    redfield_operators_kernel<float><<<(unsigned)batch, threads, smem, (cudaStream_t)stream>>>(
+        E, U, n, batch, occ, n_sites, p, unit_convert, site_basis, (double2*)G, (double2*)M, K);
+  } else {
+    e = cudaFuncSetAttribute(redfield_operators_kernel<double>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_operators_batched");
+    redfield_operators_kernel<double><<<(unsigned)batch, threads, smem, (cudaStream_t)stream>>>(
+        E, U, n, batch, occ, n_sites, p, unit_convert, site_basis, (double2*)G, (double2*)M, K);
+  }
   QSX_LAUNCH_CHECK("qsx_redfield_operators_batched");
   return QSX_OK;
 }

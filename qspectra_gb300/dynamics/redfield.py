@@ -37,7 +37,8 @@ class RedfieldBuild:
     """
 
     def __init__(self, H, n_sites, hilbert_subspace, occ, bath, unit_convert,
-                 secular=False, discard_imag_corr=False, evolve_basis='site'):
+                 secular=False, discard_imag_corr=False, evolve_basis='site',
+                 precision=_native.QSX_FP64):
         self.H = H
         self.n = H.shape[-1]
         self.n_sites = n_sites
@@ -57,7 +58,8 @@ class RedfieldBuild:
         self.site_ops = evolve_basis == 'site' and not secular
         self.G, self.M, self.K = _native.redfield_operators(
             self.E, self.U, self.occ, bath, unit_convert, discard_imag_corr,
-            site_basis=self.site_ops, matsubara_cutoff=bath.matsubara_cutoff)
+            site_basis=self.site_ops, matsubara_cutoff=bath.matsubara_cutoff,
+            precision=precision)
 
     def propagator(self, idx, h, precision=_native.QSX_FP64, transpose=False):
         """(S, m, m) RK4 propagator D = P - I of the block ``idx`` (m <= 64).
@@ -130,13 +132,15 @@ class RedfieldModel(LiouvilleSpaceModel):
             self.hilbert_subspace, self.unit_convert, self.secular,
             self.discard_imag_corr, self.evolve_basis)
 
-    def build_batch(self, H):
-        """RedfieldBuild for a (S, n, n) batch of rotating-frame Hamiltonians."""
+    def build_batch(self, H, precision=_native.QSX_FP64):
+        """RedfieldBuild for a (S, n, n) batch of rotating-frame Hamiltonians;
+        precision QSX_FP32 evaluates the operator build in FP32 (for FP32
+        propagation)."""
         ham = self.hamiltonian
         return RedfieldBuild(H, ham.n_sites, self.hilbert_subspace,
                              ham.occupation_table(self.hilbert_subspace), ham.bath,
                              self.unit_convert, self.secular, self.discard_imag_corr,
-                             self.evolve_basis)
+                             self.evolve_basis, precision)
 
     def _build(self):
         if 'build' not in self._cache:

@@ -260,10 +260,10 @@ def can_use_hermitian(precision, idx, n_total, y0, nsteps):
     return nb
 
 
-def redfield_batch_build(model, batch):
+def redfield_batch_build(model, batch, precision=_native.QSX_FP64):
     if not isinstance(model, RedfieldModel):
         raise NotImplementedError('batched ensembles need a RedfieldModel')
-    return model.build_batch(batch.H(model.hilbert_subspace))
+    return model.build_batch(batch.H(model.hilbert_subspace), precision)
 
 
 def sample_polarizations(polarization, rotations):
@@ -292,7 +292,7 @@ def ensemble_linear_signal(model, time_max, ensemble_size, polarization='xx',
     dt = model.time_step
     t = np.arange(0, time_max, dt)
     batch = SampleBatch(model, ensemble_size, start, offsets)
-    build = redfield_batch_build(model, batch)
+    build = redfield_batch_build(model, batch, prec)
     rho0 = model.thermal_state(subs[0])
     q = None if rotations is None else torch.as_tensor(
         sample_polarizations(polarization, rotations)).cuda()      # (S, 2, 3)
@@ -339,7 +339,7 @@ def ensemble_populations(model, initial_state, duration, ensemble_size,
     dt = model.time_step
     t = np.arange(0, duration, dt)
     batch = SampleBatch(model, ensemble_size, start, offsets)
-    build = redfield_batch_build(model, batch)
+    build = redfield_batch_build(model, batch, prec)
     rho0 = np.asarray(initial_state)
     if rho0.ndim == 1:
         rho0 = np.outer(rho0.conj(), rho0)
@@ -425,7 +425,7 @@ class RedfieldEnsembleWorkload:
         S = offsets.shape[0]
         H = self.H_base.expand(S, -1, -1).clone()
         H[:, self.e_idx, self.e_idx] += offsets
-        build = self.model.build_batch(H)
+        build = self.model.build_batch(H, prec)
         # the absorption leg (eg propagator, time loop, DFT) runs on a side
         # stream, overlapping the population leg on the caller's stream
         main = torch.cuda.current_stream()
