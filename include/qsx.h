@@ -61,6 +61,12 @@ int qsx_debye_corr(const double* x, int64_t n, double temperature,
 int qsx_eigh_batched(const double* H, int n, int64_t batch, int nblocks,
                      const int* block_starts, double* E, double* U,
                      void* stream);
+/* As qsx_eigh_batched; precision QSX_FP32 runs the block Jacobi sweeps of
+ * blocks up to 8 states in FP32 (builds that feed FP32 propagation), the
+ * outputs still double.  Larger blocks always run in FP64. */
+int qsx_eigh_batched_prec(const double* H, int n, int64_t batch, int nblocks,
+                          const int* block_starts, int precision, double* E,
+                          double* U, void* stream);
 
 /*
  * Redfield operators per disorder sample, FP64.  Replaces redfield_tensor

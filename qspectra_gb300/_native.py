@@ -91,6 +91,9 @@ _PROTOS = {
     'qsx_eigh_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int,
                                   ctypes.POINTER(ctypes.c_int), _c_vp, _c_vp,
                                   _c_vp]),
+    'qsx_eigh_batched_prec': (_c_int, [_c_vp, _c_int, _c_i64, _c_int,
+                                       ctypes.POINTER(ctypes.c_int), _c_int, _c_vp, _c_vp,
+                                       _c_vp]),
     'qsx_redfield_operators_batched': (_c_int, [
         _c_vp, _c_vp, _c_int, _c_i64, _c_vp, _c_int, _c_dbl, _c_dbl, _c_dbl,
         _c_int, _c_int, _c_dbl, _c_int, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
@@ -222,16 +225,18 @@ def debye_corr(x, temperature, reorg_energy, cutoff_freq, matsubara_cutoff=1000,
     return out
 
 
-def eigh(H, block_starts):
-    """Batched Jacobi eigensolver; H (B, n, n) float64 CUDA."""
+def eigh(H, block_starts, precision=QSX_FP64):
+    """Batched Jacobi eigensolver; H (B, n, n) float64 CUDA.  precision
+    QSX_FP32 runs blocks of up to 8 states in FP32."""
     require_gpu()
     _need(H, torch.float64, 'H', 3)
     B, n, _ = H.shape
     E = torch.empty((B, n), dtype=torch.float64, device=H.device)
     U = torch.empty((B, n, n), dtype=torch.float64, device=H.device)
     blk = (ctypes.c_int * len(block_starts))(*[int(v) for v in block_starts])
-    _check(load().qsx_eigh_batched(_p(H), n, B, len(block_starts) - 1, blk,
-                                   _p(E), _p(U), _stream()), 'qsx_eigh_batched')
+    _check(load().qsx_eigh_batched_prec(_p(H), n, B, len(block_starts) - 1, blk,
+                                        int(precision), _p(E), _p(U), _stream()),
+           'qsx_eigh_batched')
     return E, U
 
 

@@ -46,58 +46,69 @@ __device__ __forceinline__ void jacobi_rotation(double app, double aqq, double a
   double t;
   jacobi_rotation(app, aqq, apq, c, s, t);
 }
+__device__ __forceinline__ void jacobi_rotation(float app, float aqq, float apq, float& c,
+                                                float& s, float& t) {
+  const float tau = (aqq - app) / (2.0f * apq);
+  t = fabsf(tau) < 1e18f ? (tau >= 0.0f ? 1.0f : -1.0f) / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.0f)))
+                         : 0.5f / tau;
+  c = rsqrtf(fmaf(t, t, 1.0f));
+  s = t * c;
+}
 
 // One thread per matrix for a diagonal block of size NB <= 8 starting at
 // row/column `off` of each n x n input: the upper triangle of the block and
 // its eigenvectors live in registers (fully unrolled sweeps, compile-time
 // indices).  Symmetric update: a_pp -= t a_pq, a_qq += t a_pq, and for
 // k != p, q the pair (a_kp, a_kq) rotates by (c, s).
-template <int NB>
+// T = float runs the same sweeps in FP32 (for builds feeding FP32
+// propagation; stops at off-diagonal mass below 1e-13 of the diagonal).
+template <typename T, int NB>
 __global__ void __launch_bounds__(64)
     eigh_block_kernel(const double* __restrict__ H, int n, int off, int64_t batch,
                       double* E, double* U) {
 #define AS(i, j) A[(i) < (j) ? (i) : (j)][(i) < (j) ? (j) : (i)]
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= batch) return;
-  double A[NB][NB], V[NB][NB];
+  T A[NB][NB], V[NB][NB];
   const double* h = H + b * n * n;
+  const T tol = sizeof(T) == 4 ? (T)1e-13 : (T)1e-32;
 #pragma unroll
   for (int i = 0; i < NB; ++i)
 #pragma unroll
     for (int j = 0; j < NB; ++j) {
-      if (j >= i) A[i][j] = h[(off + i) * n + off + j];
-      V[i][j] = i == j ? 1.0 : 0.0;
+      if (j >= i) A[i][j] = (T)h[(off + i) * n + off + j];
+      V[i][j] = i == j ? (T)1 : (T)0;
     }
   for (int sweep = 0; sweep < 30; ++sweep) {
-    double offd = 0.0, dia = 0.0;
+    T offd = (T)0, dia = (T)0;
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
       dia = fma(A[i][i], A[i][i], dia);
 #pragma unroll
       for (int j = i + 1; j < NB; ++j) offd = fma(A[i][j], A[i][j], offd);
     }
-    if (!(offd > 1e-32 * dia)) break;
+    if (!(offd > tol * dia)) break;
 #pragma unroll
     for (int p = 0; p < NB - 1; ++p) {
 #pragma unroll
       for (int q = p + 1; q < NB; ++q) {
-        const double apq = A[p][q];
-        if (apq != 0.0) {
-          double c, s, t;
+        const T apq = A[p][q];
+        if (apq != (T)0) {
+          T c, s, t;
           jacobi_rotation(A[p][p], A[q][q], apq, c, s, t);
           A[p][p] = fma(-t, apq, A[p][p]);
           A[q][q] = fma(t, apq, A[q][q]);
-          A[p][q] = 0.0;
+          A[p][q] = (T)0;
 #pragma unroll
           for (int k = 0; k < NB; ++k) {
             if (k == p || k == q) continue;
-            const double g = AS(k, p), hh = AS(k, q);
+            const T g = AS(k, p), hh = AS(k, q);
             AS(k, p) = c * g - s * hh;
             AS(k, q) = s * g + c * hh;
           }
 #pragma unroll
           for (int k = 0; k < NB; ++k) {  // V <- V J
-            const double vkp = V[k][p], vkq = V[k][q];
+            const T vkp = V[k][p], vkq = V[k][q];
             V[k][p] = c * vkp - s * vkq;
             V[k][q] = s * vkp + c * vkq;
           }
@@ -112,9 +123,9 @@ __global__ void __launch_bounds__(64)
 #pragma unroll
     for (int j = 0; j < NB; ++j)
       rank += (A[j][j] < A[i][i] || (A[j][j] == A[i][i] && j < i)) ? 1 : 0;
-    E[b * n + off + rank] = A[i][i];
+    E[b * n + off + rank] = (double)A[i][i];
 #pragma unroll
-    for (int r = 0; r < NB; ++r) U[b * n * n + (off + r) * n + off + rank] = V[r][i];
+    for (int r = 0; r < NB; ++r) U[b * n * n + (off + r) * n + off + rank] = (double)V[r][i];
   }
 #undef AS
 }
@@ -1076,6 +1087,14 @@ int qsx_debye_corr(const double* x, int64_t n, double temperature,
 
 int qsx_eigh_batched(const double* H, int n, int64_t batch, int nblocks,
                      const int* block_starts, double* E, double* U, void* stream) {
+  return qsx_eigh_batched_prec(H, n, batch, nblocks, block_starts, QSX_FP64, E, U, stream);
+}
+
+int qsx_eigh_batched_prec(const double* H, int n, int64_t batch, int nblocks,
+                          const int* block_starts, int precision, double* E, double* U,
+                          void* stream) {
+  QSX_CHECK_ARG(precision == QSX_FP32 || precision == QSX_FP64,
+                "qsx_eigh_batched_prec: bad precision");
   QSX_CHECK_ARG(n >= 1 && n <= EIGH_NMAX, "qsx_eigh_batched: need 1 <= n <= %d (got %d)",
                 EIGH_NMAX, n);
   QSX_CHECK_ARG(batch >= 0 && nblocks >= 1 && nblocks <= n && block_starts,
@@ -1104,7 +1123,13 @@ int qsx_eigh_batched(const double* H, int n, int64_t batch, int nblocks,
   for (int k = 0; k < nblocks; ++k) {
     const int off = block_starts[k], nb = block_starts[k + 1] - off;
     switch (nb) {
-#define B(NB) case NB: eigh_block_kernel<NB><<<grid, 64, 0, st>>>(H, n, off, batch, E, U); break;
+#define B(NB)                                                                        \
+  case NB:                                                                           \
+    if (precision == QSX_FP32)                                                       \
+      eigh_block_kernel<float, NB><<<grid, 64, 0, st>>>(H, n, off, batch, E, U);     \
+    else                                                                             \
+      eigh_block_kernel<double, NB><<<grid, 64, 0, st>>>(H, n, off, batch, E, U);    \
+    break;
       B(1) B(2) B(3) B(4) B(5) B(6) B(7) B(8)
 #undef B
     }

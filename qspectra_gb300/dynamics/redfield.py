@@ -49,7 +49,7 @@ class RedfieldBuild:
                                         H.device)
         bounds = manifold_bounds(n_sites, hilbert_subspace)
         if self.n <= EIGH_JACOBI_MAX:
-            self.E, self.U = _native.eigh(H, bounds)
+            self.E, self.U = _native.eigh(H, bounds, precision)
         else:
             raise _native.QsxError(
                 'Hilbert space of {} states exceeds the {}-state Redfield '
