@@ -164,11 +164,13 @@ int qsx_rk4_block_matrix_batched(const void* D, int m, int64_t batch,
  * qsx_redfield_propagator_hermitian_batched: as
  * qsx_redfield_propagator_batched for the diagonal block of the nb states
  * `states` (Hilbert indices, nb <= 8, m = nb^2), writing the real
- * D_r = P_r - I [batch][m][m].  The real generator is given as a sparse
- * linear map (CSR rowptr [m*m + 1], cols, vals; rows = entries r * m + c)
+ * D_r = P_r - I [batch][m][m].  The real generator is a sparse linear map
  * of the sources [Re B[s]_xy, Im B[s]_xy for s, x, y < nb] ++
- * [uc H_xy for x, y < nb], B[s] = G - sum_i occ_is M_i on the block; the
- * map depends on nb only and is built once by the caller.
+ * [uc H_xy for x, y < nb], B[s] = G - sum_i occ_is M_i on the block, given
+ * per entry r * m + c as four int32 (16-byte aligned): two 16-bit source
+ * indices in each of the first two, four signed 8-bit coefficients in the
+ * third, the fourth unused; it depends on nb only and is built once by the
+ * caller.
  * qsx_rk4_block_matrix_real_batched: qsx_rk4_block_matrix_batched on real
  * matrices; each sample's (m + nselect (K - 1)) x m output starts at a
  * multiple of 4 values (sample stride = that size rounded up to 4).
@@ -188,8 +190,7 @@ int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
                                               const double* occ, int n, int n_sites,
                                               int64_t batch, double unit_convert,
                                               const int* states, int nb,
-                                              const int* rowptr, const int* cols,
-                                              const float* vals, double h,
+                                              const int* recipe, double h,
                                               int precision, void* D, void* stream);
 int qsx_rk4_block_matrix_real_batched(const void* D, int m, int64_t batch,
                                       int precision, int K, const int* select,
@@ -282,6 +283,27 @@ int qsx_rk4_batched(const qsx_rk4_args* args, void* stream);
  * array and clears the part it uses: calls that overlap on the GPU race.
  */
 int qsx_rk4_block_mean_noalloc(const qsx_rk4_args* args, void* stream);
+
+/*
+ * K-step blocked loop for projected signals of small blocks (m <= 8, up to
+ * 4 projections), the time loop of the Heisenberg-picture linear response.
+ * qsx_rk4_proj_block_build: from D = P - I (complex64 [batch][m][m]) and the
+ * projections proj (complex128 [nproj][m], shared) write, per sample, the
+ * complex64 (m + nproj K) x m matrix: rows 0..m-1 = P^K - I, row
+ * m + k nproj + p = proj_p P^k (k = 0..K-1).
+ * qsx_rk4_proj_block_mean: out_mean (complex128 [nsteps + 1][nproj]) = the
+ * ensemble mean over samples of proj_p . y_n with y_{n+1} = P y_n from y0
+ * (complex128 [batch][m], y0_stride 0 = shared), nsteps % K == 0; split-word
+ * FP32 state; workspace of qsx_rk4_proj_block_workspace_bytes() bytes.
+ */
+int qsx_rk4_proj_block_build(const void* D, int m, int64_t batch, int K,
+                             const double* proj, int nproj, void* out, void* stream);
+size_t qsx_rk4_proj_block_workspace_bytes(int m, int64_t batch, int K, int nsteps,
+                                          int nproj);
+int qsx_rk4_proj_block_mean(const void* matrix, int m, int64_t batch, int K, int nsteps,
+                            const double* y0, int64_t y0_stride, int nproj,
+                            double* out_mean, void* workspace, size_t workspace_bytes,
+                            int32_t* status, void* stream);
 
 /*
  * Hierarchical equations of motion (HEOM).  Replaces HEOMModel.HEOM_tensor

@@ -106,9 +106,15 @@ _PROTOS = {
     'qsx_rk4_block_matrix_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int,
                                               _c_vp, _c_int, _c_vp, _c_vp]),
     'qsx_hermitian_real_form': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_vp, _c_vp]),
+    'qsx_rk4_proj_block_build': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_vp, _c_int, _c_vp,
+                                          _c_vp]),
+    'qsx_rk4_proj_block_workspace_bytes': (ctypes.c_size_t, [_c_int, _c_i64, _c_int, _c_int,
+                                                             _c_int]),
+    'qsx_rk4_proj_block_mean': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int, _c_vp, _c_i64,
+                                         _c_int, _c_vp, _c_vp, ctypes.c_size_t, _c_vp, _c_vp]),
     'qsx_redfield_propagator_hermitian_batched': (_c_int, [
         _c_vp, _c_i64, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_i64, _c_dbl, _c_vp,
-        _c_int, _c_vp, _c_vp, _c_vp, _c_dbl, _c_int, _c_vp, _c_vp]),
+        _c_int, _c_vp, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_rk4_block_matrix_real_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int,
                                                    _c_vp, _c_int, _c_vp, _c_vp]),
     'qsx_rk4_real_block_workspace_bytes': (ctypes.c_size_t, [_c_int, _c_i64, _c_int, _c_int,
@@ -351,7 +357,7 @@ _RECIPES = {}
 
 
 def hermitian_recipe(nb, device):
-    """CSR map (rowptr, cols, vals) from the sources [Re B, Im B (nb, nb, nb),
+    """Packed (m^2, 4) int32 map from the sources [Re B, Im B (nb, nb, nb),
     uc H (nb, nb)] to the real form of the Redfield generator block
     L[(a,b),(c,d)] = d_bd (-B[b]_ac - i uc H_ac) + d_ac (-conj(B[a]_bd) + i uc H_db)
     on a diagonal block of nb states (row-major over the m^2 entries)."""
@@ -384,9 +390,24 @@ def hermitian_recipe(nb, device):
     rowptr = np.zeros(m * m + 1, dtype=np.int32)
     np.add.at(rowptr, rows + 1, 1)
     rowptr = np.cumsum(rowptr).astype(np.int32)
-    out = (torch.as_tensor(rowptr, device=device),
-           torch.as_tensor(cols.astype(np.int32), device=device),
-           torch.as_tensor(J[rows, cols].astype(np.float32), device=device))
+    coefs = J[rows, cols]
+    if np.diff(rowptr).max(initial=0) > 4 or nsrc > 65535 or np.any(
+            np.abs(coefs - np.round(coefs)) > 0) or np.abs(coefs).max(initial=0) > 127:
+        raise ValueError('generator recipe does not fit the packed 4-term form')
+    # packed per entry: sources (16 bits) in words 0-1, int8 coefficients in word 2
+    src = np.zeros((m * m, 4), dtype=np.int64)
+    cf = np.zeros((m * m, 4), dtype=np.int64)
+    for e in range(m * m):
+        k = rowptr[e + 1] - rowptr[e]
+        src[e, :k] = cols[rowptr[e]:rowptr[e + 1]]
+        cf[e, :k] = np.round(coefs[rowptr[e]:rowptr[e + 1]])
+    packed = np.zeros((m * m, 4), dtype=np.int64)
+    packed[:, 0] = src[:, 0] | (src[:, 1] << 16)
+    packed[:, 1] = src[:, 2] | (src[:, 3] << 16)
+    packed[:, 2] = ((cf[:, 0] & 0xff) | ((cf[:, 1] & 0xff) << 8) | ((cf[:, 2] & 0xff) << 16)
+                    | ((cf[:, 3] & 0xff) << 24))
+    packed = packed.astype(np.uint32).view(np.int32)
+    out = torch.as_tensor(np.ascontiguousarray(packed), device=device)
     _RECIPES[key] = out
     return out
 
@@ -404,13 +425,13 @@ def redfield_propagator_hermitian(H, G, M, occ, states, unit_convert, h, precisi
     h_stride = 0 if H.dim() == 2 else n * n
     st = const_tensor(np.asarray(states, dtype=np.int32), torch.int32, G.device)
     nb = st.numel()
-    rowptr, cols, vals = hermitian_recipe(nb, G.device)
+    recipe = hermitian_recipe(nb, G.device)
     m = nb * nb
     dt = torch.float32 if precision == QSX_FP32 else torch.float64
     D = torch.empty((B, m, m), dtype=dt, device=G.device)
     _check(load().qsx_redfield_propagator_hermitian_batched(
-        _p(H), h_stride, _p(G), _p(M), _p(occ), n, N, B, unit_convert, _p(st), nb, _p(rowptr),
-        _p(cols), _p(vals), h, precision, _p(D), _stream()),
+        _p(H), h_stride, _p(G), _p(M), _p(occ), n, N, B, unit_convert, _p(st), nb,
+        _p(recipe), h, precision, _p(D), _stream()),
         'qsx_redfield_propagator_hermitian_batched')
     return D
 
@@ -460,6 +481,41 @@ def rk4_real_block_mean(mat, y0, nsteps, select, K, check_finite=True, group=0):
            'qsx_rk4_real_block_mean')
     if check_finite and int(status.item()) & QSX_ERR_NONFINITE:
         raise IntegratorError('non-finite state in the blocked real loop')
+    return out, status
+
+
+def proj_block_k(nsteps, m, nproj, max_k=64):
+    """Largest K <= max_k dividing nsteps with m + nproj K <= 256 (1: none)."""
+    for K in range(min(max_k, (256 - m) // nproj), 1, -1):
+        if nsteps % K == 0:
+            return K
+    return 1
+
+
+def rk4_proj_block_mean(D, y0, proj, nsteps, K, check_finite=True):
+    """Ensemble mean (nsteps + 1, nproj) complex128 of proj . y_n for
+    y_{n+1} = (I + D) y_n (qsx_rk4_proj_block_build + qsx_rk4_proj_block_mean).
+    D (B, m, m) complex64; y0 (m,) or (B, m); proj (nproj, m) shared."""
+    require_gpu()
+    _need(D, torch.complex64, 'D', 3)
+    B, m, _ = D.shape
+    proj = proj.to(device=D.device, dtype=torch.complex128).contiguous()
+    P = proj.shape[0]
+    y0 = y0.to(device=D.device, dtype=torch.complex128).contiguous()
+    lib = load()
+    mat = torch.empty((B, m + P * K, m), dtype=torch.complex64, device=D.device)
+    _check(lib.qsx_rk4_proj_block_build(_p(D), m, B, K, _p(proj), P, _p(mat), _stream()),
+           'qsx_rk4_proj_block_build')
+    ws_bytes = lib.qsx_rk4_proj_block_workspace_bytes(m, B, K, int(nsteps), P)
+    ws = torch.empty(max(int(ws_bytes), 16), dtype=torch.uint8, device=D.device)
+    out = torch.empty((nsteps + 1, P), dtype=torch.complex128, device=D.device)
+    status = torch.zeros(1, dtype=torch.int32, device=D.device)
+    _check(lib.qsx_rk4_proj_block_mean(_p(mat), m, B, K, int(nsteps), _p(y0),
+                                       m if y0.dim() == 2 else 0, P, _p(out), _p(ws),
+                                       ws.numel(), _p(status), _stream()),
+           'qsx_rk4_proj_block_mean')
+    if check_finite and int(status.item()) & QSX_ERR_NONFINITE:
+        raise IntegratorError('non-finite state in the projected blocked loop')
     return out, status
 
 

@@ -822,18 +822,19 @@ __global__ void __launch_bounds__(256)
 // states (m = nb^2) from the per-sample operators.  The real generator is a
 // fixed sparse linear map of the sources
 //   S = [Re B[s]_xy, Im B[s]_xy (s, x, y < nb)], [uc H_xy (x, y < nb)],
-// B[s] = G - sum_i occ_is M_i restricted to the block, given as CSR
-// (rowptr, cols, vals) over the m^2 entries (row-major) and built once by
-// the host; so the assembly is nb^3 operator sums in the working precision
-// plus one short sparse dot product per entry, no index arithmetic.
+// B[s] = G - sum_i occ_is M_i restricted to the block; every entry of the
+// real generator combines at most four sources with coefficients in
+// {0, +-1, +-2}, given per entry (row-major) as one int4: source indices
+// (16 bits each) in .x, .y and four signed 8-bit coefficients in .z, built
+// once by the host.  So the assembly is nb^3 operator sums in the working
+// precision plus one 16-byte load and four multiply-adds per entry.
 template <typename T>
 __global__ void __launch_bounds__(256, 2)
     hermitian_propagator_kernel(const double* __restrict__ H, int64_t H_stride,
                                 const double2* __restrict__ G, const double2* __restrict__ Mo,
                                 const double* __restrict__ occ, int n, int n_sites,
                                 const int* __restrict__ states, int nb,
-                                const int* __restrict__ rowptr, const int* __restrict__ cols,
-                                const float* __restrict__ vals, double uc, double h,
+                                const int4* __restrict__ recipe, double uc, double h,
                                 T* __restrict__ D) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int m = nb * nb, ld = (m + 3) & ~3, nb3 = nb * m;
@@ -870,8 +871,12 @@ __global__ void __launch_bounds__(256, 2)
   __syncthreads();
   const T ht = (T)h;
   for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-    T acc = (T)0;
-    for (int q = rowptr[e]; q < rowptr[e + 1]; ++q) acc += (T)vals[q] * src[cols[q]];
+    const int4 rq = recipe[e];
+    const int cz = rq.z;
+    T acc = (T)(signed char)(cz & 0xff) * src[rq.x & 0xffff];
+    acc = fma((T)(signed char)((cz >> 8) & 0xff), src[(rq.x >> 16) & 0xffff], acc);
+    acc = fma((T)(signed char)((cz >> 16) & 0xff), src[rq.y & 0xffff], acc);
+    acc = fma((T)(signed char)((cz >> 24) & 0xff), src[(rq.y >> 16) & 0xffff], acc);
     rA[(e / m) * ld + e % m] = ht * acc;
   }
   __syncthreads();
@@ -897,13 +902,44 @@ __global__ void __launch_bounds__(256, 2)
   });
 }
 
+// One 4 x 4 tile of C = A B (row stride ld for A, B), accumulators returned.
+template <typename T>
+__device__ __forceinline__ void rtile_4x4(const T* __restrict__ A, const T* __restrict__ B,
+                                          int ld, int r0, int c0, T (&acc)[4][4]) {
+  using V4 = typename std::conditional<sizeof(T) == 4, Quad, QuadD>::type;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = (T)0;
+  for (int k = 0; k < ld; k += 4) {
+    V4 a[4], bq[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = load4(A + (r0 + i) * ld + k);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) bq[q] = load4(B + (k + q) * ld + c0);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const T av[4] = {a[i].x, a[i].y, a[i].z, a[i].w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        acc[i][0] = fma(av[q], bq[q].x, acc[i][0]);
+        acc[i][1] = fma(av[q], bq[q].y, acc[i][1]);
+        acc[i][2] = fma(av[q], bq[q].z, acc[i][2]);
+        acc[i][3] = fma(av[q], bq[q].w, acc[i][3]);
+      }
+    }
+  }
+}
+
 // Real counterpart of block_matrix_kernel for the Hermitian real form:
 // out rows 0..m-1 = D_K = P^K - I, then the selected rows R_k of D_k for
 // k = 1..K-1 (row m + (k-1) nsel + q = row sel[q] of D_k).
 // Shared memory holds the squares D_{2^j} (padded to ld = 4 ceil(m/4)), two
-// accumulators for the binary powering of D_K, and the selected rows, built
-// by doubling: R_{i+b} = R_i + R_b + R_i D_b for b = 2^j, so every product is
-// a 4 x 4-tiled GEMM against a square already in shared memory.
+// accumulators for the binary powering of D_K, and the selected rows.  Phase
+// j forms, from D_{2^j}, both the next square D_{2^{j+1}} = 2 D + D D and the
+// rows R_{i + 2^j} = R_i + R_{2^j} + R_i D_{2^j} (i <= 2^j), the two products'
+// 4 x 4 tiles spread over the whole CTA between one pair of barriers; D_K
+// then follows from the squares by composition over the set bits of K.
 template <typename T>
 __global__ void __launch_bounds__(256)
     block_matrix_real_kernel(const T* __restrict__ D, int m, int K, const int* __restrict__ sel,
@@ -911,6 +947,7 @@ __global__ void __launch_bounds__(256)
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ld = (m + 3) & ~3;
   const int mm = ld * ld;
+  const int nct = ld / 4;
   int J = 0;
   while ((2 << J) <= K) ++J;                 // squares D_{2^0} .. D_{2^J}
   T* sq = (T*)smraw;                          // [J + 1][ld][ld]
@@ -931,12 +968,6 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   for (int e = threadIdx.x; e < m * m; e += blockDim.x) sq[(e / m) * ld + e % m] = d[e];
   __syncthreads();
-  for (int j = 1; j <= J; ++j) {
-    const T* X = sq + (size_t)(j - 1) * mm;
-    compose_into<T>(X, X, ld, ld, m, sq + (size_t)j * mm, ld);
-    __syncthreads();
-  }
-  // selected rows: R_1 = rows of D, then doubling
   for (int e = threadIdx.x; e < nsel * ld; e += blockDim.x) {
     const int q = e / ld, c = e % ld;
     int r = sel[q];
@@ -945,23 +976,42 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   int have = 1;  // R_1 .. R_have are in sR
-  for (int j = 0; have < K - 1; ++j) {
-    const int bpow = 1 << j;  // have == bpow here
-    const int add = min(bpow, K - 1 - have);
-    const T* Db = sq + (size_t)j * mm;
-    const int arows = ((add * nsel + 3) & ~3);
+  for (int j = 0; j < J || have < K - 1; ++j) {
+    const T* Dj = sq + (size_t)j * mm;
+    const bool square = j < J;                       // D_{2^{j+1}} still needed
+    const int add = have < K - 1 ? min(1 << j, K - 1 - have) : 0;
+    const int arows = (add * nsel + 3) & ~3;
+    const int nsq = square ? nct * nct : 0;
+    const int ntiles = nsq + (arows / 4) * nct;
+    T* Z = sq + (size_t)(j + 1) * mm;
     T* dst = sR + (size_t)have * nsel * ld;
-    const T* Rb = sR + (size_t)(bpow - 1) * nsel * ld;  // rows of D_b
-    rgemm_4x4<T>(sR, Db, ld, arows, [&](int r0, int c0, T (&acc)[4][4]) {
+    const T* Rb = sR + (size_t)((1 << j) - 1) * nsel * ld;  // rows of D_{2^j}
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
+      T acc[4][4];
+      if (t < nsq) {
+        const int r0 = (t / nct) * 4, c0 = (t % nct) * 4;
+        rtile_4x4<T>(Dj, Dj, ld, r0, c0, acc);
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const int r = r0 + i, c = c0 + jj;
-          if (r < add * nsel && c < m)
-            dst[r * ld + c] = (sR[r * ld + c] + Rb[(r % nsel) * ld + c]) + acc[i][jj];
-        }
-    });
+          for (int jj = 0; jj < 4; ++jj) {
+            const int r = r0 + i, c = c0 + jj;
+            if (r < m && c < m) Z[r * ld + c] = (Dj[r * ld + c] + Dj[r * ld + c]) + acc[i][jj];
+          }
+      } else {
+        const int tt = t - nsq;
+        const int r0 = (tt / nct) * 4, c0 = (tt % nct) * 4;
+        rtile_4x4<T>(sR, Dj, ld, r0, c0, acc);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            const int r = r0 + i, c = c0 + jj;
+            if (r < add * nsel && c < m)
+              dst[r * ld + c] = (sR[r * ld + c] + Rb[(r % nsel) * ld + c]) + acc[i][jj];
+          }
+      }
+    }
     __syncthreads();
     have += add;
   }
@@ -1210,14 +1260,13 @@ int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
                                               const double* G, const double* M,
                                               const double* occ, int n, int n_sites,
                                               int64_t batch, double unit_convert,
-                                              const int* states, int nb, const int* rowptr,
-                                              const int* cols, const float* vals, double h,
-                                              int precision, void* D, void* stream) {
+                                              const int* states, int nb, const int* recipe,
+                                              double h, int precision, void* D, void* stream) {
   QSX_CHECK_ARG(nb >= 1 && nb <= 8 && n >= nb && n_sites >= 1 && batch >= 0 &&
                     (precision == QSX_FP32 || precision == QSX_FP64),
                 "qsx_redfield_propagator_hermitian_batched: bad sizes (n=%d, nb=%d)", n, nb);
   if (batch == 0) return QSX_OK;
-  QSX_CHECK_ARG(H && G && M && occ && states && rowptr && cols && vals && D,
+  QSX_CHECK_ARG(H && G && M && occ && states && recipe && D,
                 "qsx_redfield_propagator_hermitian_batched: null pointer");
   const int m = nb * nb, ld = (m + 3) & ~3;
   const size_t rs = precision == QSX_FP32 ? sizeof(float) : sizeof(double);
@@ -1229,15 +1278,15 @@ int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_hermitian_batched");
     hermitian_propagator_kernel<float><<<(unsigned)batch, 256, smem, s>>>(
-        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, states, nb, rowptr,
-        cols, vals, unit_convert, h, (float*)D);
+        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, states, nb,
+        (const int4*)recipe, unit_convert, h, (float*)D);
   } else {
     e = cudaFuncSetAttribute(hermitian_propagator_kernel<double>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_hermitian_batched");
     hermitian_propagator_kernel<double><<<(unsigned)batch, 256, smem, s>>>(
-        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, states, nb, rowptr,
-        cols, vals, unit_convert, h, (double*)D);
+        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, states, nb,
+        (const int4*)recipe, unit_convert, h, (double*)D);
   }
   QSX_LAUNCH_CHECK("qsx_redfield_propagator_hermitian_batched");
   return QSX_OK;

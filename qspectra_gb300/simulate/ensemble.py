@@ -260,6 +260,21 @@ def can_use_hermitian(precision, idx, n_total, y0, nsteps):
     return nb
 
 
+def projected_mean(D, y0, proj, nsteps):
+    """Ensemble mean of proj . y_n (n = 0..nsteps) for y_{n+1} = (I + D) y_n:
+    the K-step blocked projection loop for FP32 blocks of up to 8 states and
+    a shared projection, else the step-by-step batched loop."""
+    m = D.shape[-1]
+    P = proj.shape[-2]
+    K = _native.proj_block_k(nsteps, m, P) if (D.dtype == torch.complex64 and m <= 8
+                                               and proj.dim() == 2 and P <= 4) else 1
+    if K > 1:
+        mean, status = _native.rk4_proj_block_mean(D, y0, proj, nsteps, K, check_finite=False)
+        return {'mean': mean, 'status': status}
+    return _native.rk4(D, y0, nsteps, 1, proj=proj, per_sample=False, mean=True,
+                       check_finite=False)
+
+
 def redfield_batch_build(model, batch, precision=_native.QSX_FP64):
     if not isinstance(model, RedfieldModel):
         raise NotImplementedError('batched ensembles need a RedfieldModel')
@@ -315,8 +330,7 @@ def ensemble_linear_signal(model, time_max, ensemble_size, polarization='xx',
             y0 = torch.einsum('sa,am->sm', q[:, 1].to(Y1.dtype), Y1).contiguous()
             proj = torch.einsum('sa,am->sm', q[:, 0].to(P0.dtype), P0)[:, None, :].contiguous()
         steps = step_plan(t, 0.0, dt)
-        out = _native.rk4(D, y0, int(steps[-1]), 1,
-                          proj=proj, per_sample=False, mean=True, check_finite=False)
+        out = projected_mean(D, y0, proj, int(steps[-1]))
         sig = out['mean'][:, 0]
         total = sig if total is None else total + sig
         if int(out['status'].item()) & _native.QSX_ERR_NONFINITE:
@@ -436,8 +450,7 @@ class RedfieldEnsembleWorkload:
         with torch.cuda.stream(self._side):
             self._side.wait_event(ready)
             D_eg = build.propagator(self.idx_eg, self.dt, prec, transpose=True)
-            sig = _native.rk4(D_eg, self.y_abs, len(self.t_abs) - 1, 1, proj=self.proj,
-                              per_sample=False, mean=True, check_finite=False)
+            sig = projected_mean(D_eg, self.y_abs, self.proj, len(self.t_abs) - 1)
             X = _native.dft(-sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
                             self.model.rw_freq, self.model.unit_convert, 1)
         nb = can_use_hermitian(prec, self.idx_ee, self.n_sites + 1, self.y_dyn_np,

@@ -120,3 +120,28 @@ def test_workload_uses_real_form_and_matches_fp64():
     assert int(st.item()) == 0
     assert rel_err(P32.cpu().numpy(), P64.cpu().numpy()) < 1e-5
     assert rel_err(X32.cpu().numpy(), X64.cpu().numpy()) < 1e-5
+
+
+@pytest.mark.parametrize('m,P,nsteps', [(7, 1, 2047), (3, 2, 120), (8, 1, 96), (5, 3, 64)])
+def test_projection_blocked_loop_matches_stepwise(m, P, nsteps):
+    """The K-step projection loop (qsx_rk4_proj_block_*) against the
+    step-by-step batched loop and an FP64 NumPy recurrence."""
+    rng = np.random.RandomState(m + P)
+    B = 37
+    A = 0.005 * (rng.randn(B, m, m) + 1j * rng.randn(B, m, m)) - 0.03 * np.eye(m)[None]
+    D = torch.as_tensor(A).to(torch.complex64).cuda()
+    y0 = torch.as_tensor(rng.randn(m) + 1j * rng.randn(m)).cuda()
+    proj = torch.as_tensor(rng.randn(P, m) + 1j * rng.randn(P, m)).cuda()
+    K = _native.proj_block_k(nsteps, m, P)
+    assert K > 1
+    blk, _ = _native.rk4_proj_block_mean(D, y0, proj, nsteps, K)
+    ref = _native.rk4(D, y0, nsteps, 1, proj=proj, per_sample=False, mean=True)['mean']
+    Pm = np.eye(m)[None] + D.cpu().numpy().astype(np.complex128)
+    y = np.repeat(y0.cpu().numpy()[None], B, 0)
+    exact = []
+    for _ in range(nsteps + 1):
+        exact.append((y @ proj.cpu().numpy().T).mean(0))
+        y = np.einsum('bij,bj->bi', Pm, y)
+    exact = np.array(exact)
+    assert rel_err(blk.cpu().numpy(), exact) < 2e-6
+    assert rel_err(ref.cpu().numpy(), exact) < 2e-6
