@@ -941,7 +941,7 @@ __device__ __forceinline__ void rtile_4x4(const T* __restrict__ A, const T* __re
 // 4 x 4 tiles spread over the whole CTA between one pair of barriers; D_K
 // then follows from the squares by composition over the set bits of K.
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
     block_matrix_real_kernel(const T* __restrict__ D, int m, int K, const int* __restrict__ sel,
                              int nsel, T* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -950,11 +950,13 @@ __global__ void __launch_bounds__(256)
   const int nct = ld / 4;
   int J = 0;
   while ((2 << J) <= K) ++J;                 // squares D_{2^0} .. D_{2^J}
+  // composition buffers are needed only when K has more than two set bits
+  const int nacc = __popc(K) > 2 ? 2 : 0;
   T* sq = (T*)smraw;                          // [J + 1][ld][ld]
-  T* acc0 = sq + (size_t)(J + 1) * mm;        // [ld][ld]
+  T* acc0 = sq + (size_t)(J + 1) * mm;        // [nacc][ld][ld]
   T* acc1 = acc0 + mm;
   const int rrows = ((nsel * (K - 1) + 3) & ~3) + 4;
-  T* sR = acc1 + mm;                          // [rrows][ld] selected rows R_1 .. R_{K-1}
+  T* sR = acc0 + (size_t)nacc * mm;           // [rrows][ld] selected rows R_1 .. R_{K-1}
   const int64_t b = blockIdx.x;
   const int rows = m + nsel * (K - 1);
   const T* d = D + b * (int64_t)m * m;
@@ -963,7 +965,7 @@ __global__ void __launch_bounds__(256)
   T* o = out + b * (((int64_t)rows * m + 3) & ~(int64_t)3);
   // zero everything first: the padding rows and columns of every matrix
   // must stay zero because the tiled products read them
-  const int total = (J + 3) * mm + rrows * ld;
+  const int total = (J + 1 + nacc) * mm + rrows * ld;
   for (int e = threadIdx.x; e < total; e += blockDim.x) sq[e] = (T)0;
   __syncthreads();
   for (int e = threadIdx.x; e < m * m; e += blockDim.x) sq[(e / m) * ld + e % m] = d[e];
@@ -1096,7 +1098,10 @@ int qsx_rk4_block_matrix_real_batched(const void* D, int m, int64_t batch, int p
   int J = 0;
   while ((2 << J) <= K) ++J;
   const size_t rrows = (((size_t)nselect * (K - 1) + 3) & ~(size_t)3) + 4;
-  const size_t smem = ((size_t)(J + 3) * ld * ld + rrows * ld) * rs;
+  int bits = 0;
+  for (int t = K; t; t &= t - 1) ++bits;
+  const size_t nacc = bits > 2 ? 2 : 0;
+  const size_t smem = ((size_t)(J + 1 + nacc) * ld * ld + rrows * ld) * rs;
   if (smem > 227 * 1024) {
     set_error("qsx_rk4_block_matrix_real_batched: %zu bytes of shared memory needed", smem);
     return QSX_ERR_UNSUPPORTED;
