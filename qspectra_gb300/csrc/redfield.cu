@@ -829,7 +829,7 @@ __global__ void __launch_bounds__(256)
 // once by the host.  So the assembly is nb^3 operator sums in the working
 // precision plus one 16-byte load and four multiply-adds per entry.
 template <typename T>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
     hermitian_propagator_kernel(const double* __restrict__ H, int64_t H_stride,
                                 const double2* __restrict__ G, const double2* __restrict__ Mo,
                                 const double* __restrict__ occ, int n, int n_sites,
@@ -842,32 +842,39 @@ __global__ void __launch_bounds__(256, 2)
   T* rB = rA + ld * ld;
   T* rC = rB + ld * ld;
   T* src = rC + ld * ld;               // [2 nb^3 + nb^2]
-  int* st = (int*)(src + 2 * nb3 + m); // [nb]
+  T* gm = src + 2 * nb3 + m;           // [1 + n_sites][2][nb^2]: G, M_i on the block
+  T* so = gm + 2 * (1 + n_sites) * m;  // [n_sites][nb] occupations of the block states
+  int* st = (int*)(so + n_sites * nb); // [nb]
   const int64_t b = blockIdx.x;
   const double2* g = G + b * (int64_t)n * n;
   const double2* mo = Mo + b * (int64_t)n_sites * n * n;
   for (int e = threadIdx.x; e < 3 * ld * ld; e += blockDim.x) rA[e] = (T)0;
   for (int e = threadIdx.x; e < nb; e += blockDim.x) st[e] = states[e];
   __syncthreads();
+  // every FP64 operator entry of the block is converted once
+  for (int e = threadIdx.x; e < (1 + n_sites) * m; e += blockDim.x) {
+    const int i = e / m, xy = e % m;
+    const int f = st[xy / nb] * n + st[xy % nb];
+    const double2 v = i == 0 ? g[f] : mo[(int64_t)(i - 1) * n * n + f];
+    gm[2 * i * m + xy] = (T)v.x;
+    gm[(2 * i + 1) * m + xy] = (T)v.y;
+  }
+  for (int e = threadIdx.x; e < n_sites * nb; e += blockDim.x)
+    so[e] = (T)occ[(e / nb) * n + st[e % nb]];
+  for (int e = threadIdx.x; e < m; e += blockDim.x)
+    src[2 * nb3 + e] = (T)(uc * H[b * H_stride + st[e / nb] * n + st[e % nb]]);
+  __syncthreads();
   for (int e = threadIdx.x; e < nb3; e += blockDim.x) {
     const int s = e / m, xy = e % m;
-    const int fx = st[xy / nb], fy = st[xy % nb], fs = st[s];
-    const int f = fx * n + fy;
-    const double2 g0 = g[f];
-    T vx = (T)g0.x, vy = (T)g0.y;
+    T vx = gm[xy], vy = gm[m + xy];
     for (int i = 0; i < n_sites; ++i) {
-      const double o = occ[i * n + fs];
-      if (o != 0.0) {
-        const double2 mv = mo[(int64_t)i * n * n + f];
-        vx -= (T)o * (T)mv.x;
-        vy -= (T)o * (T)mv.y;
-      }
+      const T o = so[i * nb + s];
+      vx = fma(-o, gm[2 * (i + 1) * m + xy], vx);
+      vy = fma(-o, gm[(2 * (i + 1) + 1) * m + xy], vy);
     }
     src[e] = vx;
     src[nb3 + e] = vy;
   }
-  for (int e = threadIdx.x; e < m; e += blockDim.x)
-    src[2 * nb3 + e] = (T)(uc * H[b * H_stride + st[e / nb] * n + st[e % nb]]);
   __syncthreads();
   const T ht = (T)h;
   for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
@@ -1275,7 +1282,9 @@ int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
                 "qsx_redfield_propagator_hermitian_batched: null pointer");
   const int m = nb * nb, ld = (m + 3) & ~3;
   const size_t rs = precision == QSX_FP32 ? sizeof(float) : sizeof(double);
-  const size_t smem = (3 * (size_t)ld * ld + 2 * (size_t)nb * m + m) * rs + nb * sizeof(int);
+  const size_t smem = (3 * (size_t)ld * ld + 2 * (size_t)nb * m + m +
+                       2 * (1 + (size_t)n_sites) * m + (size_t)n_sites * nb) * rs +
+                      nb * sizeof(int);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e;
   if (precision == QSX_FP32) {
