@@ -526,6 +526,8 @@ def our_arm(args):
         raise _native.IntegratorError('non-finite state in the timed run')
     value = world * 1000.0 / ms
     dyn_ms = statistics.mean(a.elapsed_time(b) for a, b in events['dyn'])
+    bb_ms = (statistics.mean(a.elapsed_time(b) for a, b in events['blockbuild'])
+             if events.get('blockbuild') else None)
 
     # end to end through the library call with host buffers
     for _ in range(2):
@@ -567,7 +569,10 @@ def our_arm(args):
     flops_dyn = events['dyn_flops']  # executed form (K-step blocked rows)
     dense_equiv = float(S) * (DYN_TIME - 1) * 49 * 49 * 8  # one 49x49 GEMV per step
     achieved = flops_dyn / (dyn_ms * 1e-3) / 1e12
-    traffic = ncu_traffic()
+    traffic = ncu_traffic(os.path.join(ROOT, 'profiles', 'rk4_hblock_f32_fmo7.md'))
+    bb_traffic = ncu_traffic(os.path.join(ROOT, 'profiles', 'block_matrix_real_fmo7.md'))
+    bb_flops = events.get('blockbuild_flops')
+    bb_achieved = bb_flops / (bb_ms * 1e-3) / 1e12 if bb_ms else None
     base = None
     if world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(H, extra, fwhm, args.cpu_samples_per_core, S)
@@ -576,7 +581,8 @@ def our_arm(args):
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'c64 split-word (FP32 bulk, FP64 Redfield build)',
+        'dtype': 'f32/c64 split-word (FP32 build and propagation; populations in the '
+                 'real Hermitian form)',
         'data': 'synthetic (seeded Hamiltonians and disorder draws)',
         'config': dict(CONFIG, parallelism='replicas (weak: each GPU runs its own '
                                            '16384-sample ensemble)' if world > 1 else 'single GPU'),
@@ -585,21 +591,24 @@ def our_arm(args):
         'e2e': {'value': world * 1000.0 / e2e_ms, 'unit': UNIT,
                 'h2d_bytes_per_step': int(off_host.numel() * 8),
                 'd2h_bytes_per_step': int((nf + Ph.size + 1) * 8)},
-        'roofline': {'kernel': '{} (ee populations, K={} step blocking, autotuned variant {})'.format(
-                         {1: 'rk4_block_f32<49>', 2: 'rk4_block2_f32<49,2>',
-                          3: 'rk4_block3_f32<49,2>', 4: 'rk4_block2_f32<49,4>',
-                          5: 'rk4_block3_f32<49,4>'}.get(events.get('dyn_variant', 1),
-                                                         'rk4_block_f32<49>'),
-                         events['dyn_block_k'], events.get('dyn_variant', 1)),
-                     'dense_step_equivalent_tflops': dense_equiv / (dyn_ms * 1e-3) / 1e12,
-                     'bound': 'fp32_fma', 'achieved': achieved, 'peak': peak,
-                     'unit': 'TFLOP/s', 'frac': achieved / peak,
+        'roofline': {'kernel': 'block_matrix_real_kernel<float> (ee populations, real '
+                               'Hermitian form: K={} step blocked matrices, 4x4-tiled '
+                               'FP32 products)'.format(events['dyn_block_k']),
+                     'bound': 'fp32_fma', 'achieved': bb_achieved, 'peak': peak,
+                     'unit': 'TFLOP/s', 'frac': bb_achieved / peak if bb_achieved else None,
                      'peak_source': 'measured live by qsx_probe_fma (FP32 FMA); '
                                     'MEASURED_PEAKS.json has no CUDA-core figure',
-                     'flops_per_launch': flops_dyn, 'launch_ms': dyn_ms,
-                     'traffic': traffic,
-                     'hbm': hbm_view(traffic, dyn_ms)},
-        'gpu_launches': 12 * args.steps,
+                     'flops_per_launch': bb_flops, 'launch_ms': bb_ms,
+                     'traffic': bb_traffic, 'hbm': hbm_view(bb_traffic, bb_ms)},
+        'roofline_time_loop': {
+            'kernel': '{} (ee populations, K={} step blocking, variant {})'.format(
+                'rk4_hblock_f32<49>' if events.get('dyn_variant') == 'real'
+                else 'rk4_block_f32<49>', events['dyn_block_k'], events.get('dyn_variant')),
+            'dense_step_equivalent_tflops': dense_equiv / (dyn_ms * 1e-3) / 1e12,
+            'bound': 'fp32_fma', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
+            'frac': achieved / peak, 'flops_per_launch': flops_dyn, 'launch_ms': dyn_ms,
+            'traffic': traffic, 'hbm': hbm_view(traffic, dyn_ms)},
+        'gpu_launches': 13 * args.steps,
         'clocks': clocks,
     }
     if adj is not None:

@@ -217,7 +217,20 @@ def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None)
     coords = np.unique(np.concatenate([sel, partner]))
     Dr = build.hermitian_propagator(idx, nb, h)
     K = pick_block_k_real(nsteps, m, len(coords))
+    if events is not None:
+        b0 = torch.cuda.Event(enable_timing=True)
+        b0.record()
     mat = _native.rk4_block_matrix_real(Dr, K, coords)
+    if events is not None:
+        b1 = torch.cuda.Event(enable_timing=True)
+        b1.record()
+        events.setdefault('blockbuild', []).append((b0, b1))
+        # real multiply-adds of the unpadded products: the squares and the
+        # final composition of the binary powering (m^3 each) and the
+        # selected rows R_2 .. R_{K-1} (nsel m^2 each), 2 flops apiece
+        products = (K.bit_length() - 1) + (bin(K).count('1') - 1)
+        events['blockbuild_flops'] = 2.0 * Dr.shape[0] * (
+            products * m ** 3 + max(K - 2, 0) * len(coords) * m * m)
     del Dr
     x0 = hermitian_coordinates(y0, nb)
     if events is not None:
