@@ -451,6 +451,56 @@ def measured_hbm_gbs():
         return 6800.0, 'fallback (6.8 TB/s)'
 
 
+def measured_tf32_tflops():
+    """Dense TF32 tensor rate: half the measured cuBLAS bf16 burst rate (the
+    dense TF32 rate is half the bf16 rate on this part: 1.1 vs 2.25 PFLOP/s
+    nominal)."""
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return (float(json.load(f)['bf16_tflops']) / 2.0,
+                    'measured: MEASURED_PEAKS.json bf16_tflops / 2 (dense TF32 = half bf16)')
+    except (OSError, KeyError, ValueError):
+        return 1900.0 / 2.0, 'fallback: 1.9 PFLOP/s bf16 / 2'
+
+
+def block_roofline(events, bb_flops, bb_ms, fma_peak):
+    """Roofline of the FP32 K-step block build: the tcgen05 3xTF32 kernel
+    against the dense TF32 tensor rate, or the CUDA-core kernel against the
+    FP32 FMA rate.  `achieved` counts the algorithmic (unpadded) FLOPs;
+    `executed_tensor_tflops` the MMA work actually issued (three TF32
+    products of M = 128, N = NP, K = KP per chain)."""
+    bb_achieved = bb_flops / (bb_ms * 1e-3) / 1e12 if bb_ms else None
+    K = events['dyn_block_k']
+    if events.get('blockbuild_variant') == 'tcgen05':
+        B, m, K, nsel = events['blockbuild_shape']
+        kp, np_ = (m + 7) // 8 * 8, (m + 15) // 16 * 16
+        chains = (K.bit_length() - 1) + (0 if K & (K - 1) == 0 else 1)
+        executed = float(B) * chains * 3 * 2 * 128 * np_ * kp
+        traffic = ncu_traffic(os.path.join(ROOT, 'profiles', 'block_matrix_tc_fmo7.md'))
+        peak, src = measured_tf32_tflops()
+        ex = executed / (bb_ms * 1e-3) / 1e12 if bb_ms else None
+        return {'kernel': 'block_matrix_tc_kernel<32> (ee populations, real Hermitian form: '
+                          'K={} step blocked matrices, tcgen05 3xTF32 products in TMEM)'.format(K),
+                'bound': 'tensor', 'achieved': bb_achieved, 'peak': peak, 'unit': 'TFLOP/s',
+                'frac': bb_achieved / peak if bb_achieved else None, 'peak_source': src,
+                'executed_tensor_tflops': ex, 'executed_frac': ex / peak if ex else None,
+                'executed_flops_per_launch': executed,
+                'fp32_fma_view': {'peak': fma_peak, 'frac': bb_achieved / fma_peak
+                                  if bb_achieved else None,
+                                  'peak_source': 'measured live by qsx_probe_fma'},
+                'flops_per_launch': bb_flops, 'launch_ms': bb_ms,
+                'traffic': traffic, 'hbm': hbm_view(traffic, bb_ms)}
+    traffic = ncu_traffic(os.path.join(ROOT, 'profiles', 'block_matrix_real_fmo7.md'))
+    return {'kernel': 'block_matrix_real_kernel<float> (ee populations, real Hermitian form: '
+                      'K={} step blocked matrices, 4x4-tiled FP32 products)'.format(K),
+            'bound': 'fp32_fma', 'achieved': bb_achieved, 'peak': fma_peak, 'unit': 'TFLOP/s',
+            'frac': bb_achieved / fma_peak if bb_achieved else None,
+            'peak_source': 'measured live by qsx_probe_fma (FP32 FMA); '
+                           'MEASURED_PEAKS.json has no CUDA-core figure',
+            'flops_per_launch': bb_flops, 'launch_ms': bb_ms,
+            'traffic': traffic, 'hbm': hbm_view(traffic, bb_ms)}
+
+
 def hbm_view(traffic, launch_ms):
     """The same kernel against the HBM roofline: ncu DRAM bytes per launch
     over the CUDA-event launch time, as a fraction of the measured copy
@@ -570,9 +620,7 @@ def our_arm(args):
     dense_equiv = float(S) * (DYN_TIME - 1) * 49 * 49 * 8  # one 49x49 GEMV per step
     achieved = flops_dyn / (dyn_ms * 1e-3) / 1e12
     traffic = ncu_traffic(os.path.join(ROOT, 'profiles', 'rk4_hblock_f32_fmo7.md'))
-    bb_traffic = ncu_traffic(os.path.join(ROOT, 'profiles', 'block_matrix_real_fmo7.md'))
     bb_flops = events.get('blockbuild_flops')
-    bb_achieved = bb_flops / (bb_ms * 1e-3) / 1e12 if bb_ms else None
     base = None
     if world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(H, extra, fwhm, args.cpu_samples_per_core, S)
@@ -591,15 +639,7 @@ def our_arm(args):
         'e2e': {'value': world * 1000.0 / e2e_ms, 'unit': UNIT,
                 'h2d_bytes_per_step': int(off_host.numel() * 8),
                 'd2h_bytes_per_step': int((nf + Ph.size + 1) * 8)},
-        'roofline': {'kernel': 'block_matrix_real_kernel<float> (ee populations, real '
-                               'Hermitian form: K={} step blocked matrices, 4x4-tiled '
-                               'FP32 products)'.format(events['dyn_block_k']),
-                     'bound': 'fp32_fma', 'achieved': bb_achieved, 'peak': peak,
-                     'unit': 'TFLOP/s', 'frac': bb_achieved / peak if bb_achieved else None,
-                     'peak_source': 'measured live by qsx_probe_fma (FP32 FMA); '
-                                    'MEASURED_PEAKS.json has no CUDA-core figure',
-                     'flops_per_launch': bb_flops, 'launch_ms': bb_ms,
-                     'traffic': bb_traffic, 'hbm': hbm_view(bb_traffic, bb_ms)},
+        'roofline': block_roofline(events, bb_flops, bb_ms, peak),
         'roofline_time_loop': {
             'kernel': '{} (ee populations, K={} step blocking, variant {})'.format(
                 'rk4_hblock_f32<49>' if events.get('dyn_variant') == 'real'

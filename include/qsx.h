@@ -195,6 +195,20 @@ int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
 int qsx_rk4_block_matrix_real_batched(const void* D, int m, int64_t batch,
                                       int precision, int K, const int* select,
                                       int nselect, void* out, void* stream);
+/* The same real blocked matrices (FP32) on the tensor cores: each phase is
+ * one M = 128 x N = 16 ceil(m/16) x K = 8 ceil(m/8) tcgen05.mma chain in
+ * 3xTF32 (hi/lo TF32 split of both operands, FP32 accumulation in tensor
+ * memory) computing the next square and the next selected rows together;
+ * persistent CTAs, two per SM.  Supported when
+ * qsx_rk4_block_matrix_real_tc_supported(m, K, nselect): m <= 64,
+ * K = 2^J or 2^J + 1, at most 64 selected rows entering a product.  D
+ * [batch][m][m] contiguous, 4-byte aligned; out as for the batched form
+ * (per-sample stride rounded up to 4 floats); status (device int, may be
+ * NULL) receives QSX_ERR_CUDA if a completion wait times out. */
+int qsx_rk4_block_matrix_real_tc_supported(int m, int K, int nselect);
+int qsx_rk4_block_matrix_real_tc(const float* D, int m, int64_t batch, int K,
+                                 const int* select, int nselect, float* out,
+                                 int32_t* status, void* stream);
 size_t qsx_rk4_real_block_workspace_bytes(int m, int64_t batch, int K, int nsteps,
                                           int nselect, int group);
 int qsx_rk4_real_block_mean(const float* matrix, int m, int64_t batch, int K,

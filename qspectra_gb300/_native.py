@@ -117,6 +117,9 @@ _PROTOS = {
         _c_int, _c_vp, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_rk4_block_matrix_real_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int,
                                                    _c_vp, _c_int, _c_vp, _c_vp]),
+    'qsx_rk4_block_matrix_real_tc_supported': (_c_int, [_c_int, _c_int, _c_int]),
+    'qsx_rk4_block_matrix_real_tc': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_vp, _c_int,
+                                              _c_vp, _c_vp, _c_vp]),
     'qsx_rk4_real_block_workspace_bytes': (ctypes.c_size_t, [_c_int, _c_i64, _c_int, _c_int,
                                                              _c_int, _c_int]),
     'qsx_rk4_real_block_mean': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int, _c_vp, _c_i64,
@@ -453,6 +456,34 @@ def rk4_block_matrix_real(D, K, select):
                                                     _p(flat), _stream()),
            'qsx_rk4_block_matrix_real_batched')
     return flat[:, :rows * m].view(B, rows, m)
+
+
+def rk4_block_matrix_real_tc_supported(m, K, nselect):
+    """Whether the tcgen05 block build takes this shape
+    (qsx_rk4_block_matrix_real_tc_supported)."""
+    return bool(load().qsx_rk4_block_matrix_real_tc_supported(int(m), int(K), int(nselect)))
+
+
+def rk4_block_matrix_real_tc(D, K, select):
+    """As rk4_block_matrix_real for FP32, on the tensor cores (3xTF32
+    tcgen05 products; qsx_rk4_block_matrix_real_tc).  Returns None when the
+    shape is not supported."""
+    require_gpu()
+    _need(D, torch.float32, 'D', 3)
+    B, m, _ = D.shape
+    sel_np = np.asarray(select, dtype=np.int64).reshape(-1)
+    lib = load()
+    if not lib.qsx_rk4_block_matrix_real_tc_supported(m, int(K), sel_np.size):
+        return None
+    sel = const_tensor(sel_np.astype(np.int32), torch.int32, D.device)
+    rows = m + sel.numel() * (K - 1)
+    stride = (rows * m + 3) // 4 * 4
+    flat = torch.empty((B, stride), dtype=torch.float32, device=D.device)
+    status = torch.zeros(1, dtype=torch.int32, device=D.device)
+    _check(lib.qsx_rk4_block_matrix_real_tc(_p(D), m, B, int(K), _p(sel), sel.numel(), _p(flat),
+                                            _p(status), _stream()),
+           'qsx_rk4_block_matrix_real_tc')
+    return flat[:, :rows * m].view(B, rows, m), status
 
 
 def rk4_real_block_mean(mat, y0, nsteps, select, K, check_finite=True, group=0):

@@ -175,18 +175,22 @@ def from_hermitian_coordinates(x, n):
     return x[..., re_idx] + 1j * sign * x[..., im_idx]
 
 
-def pick_block_k_real(nsteps, m, nselect, max_k=64):
+def pick_block_k_real(nsteps, m, nselect, max_k=64, tensor_core=None):
     """K minimising the executed work of the real blocked loop: per block-step
     (m + nsel (K-1)) m multiply-adds (weighted twice: the loop is the
     latency-bound part), plus the block build, nsel m^2 (K-2) for the
-    selected rows and m^3 per product of the binary powering."""
+    selected rows and m^3 per product of the binary powering.  Where
+    ``tensor_core(K)`` says the tcgen05 build takes K, the build terms weigh
+    0.6 (its measured time against the CUDA-core build at K = 9)."""
     best, best_cost = 1, None
     for K in range(2, max_k + 1):
         if nsteps % K or m + nselect * (K - 1) > 512:
             continue
         products = bin(K).count('1') - 1 + K.bit_length() - 1
-        cost = (2.0 * (nsteps // K) * (m + nselect * (K - 1)) * m
-                + nselect * m * m * max(K - 2, 0) + products * m ** 3)
+        build = nselect * m * m * max(K - 2, 0) + products * m ** 3
+        if tensor_core is not None and tensor_core(K):
+            build *= 0.6
+        cost = 2.0 * (nsteps // K) * (m + nselect * (K - 1)) * m + build
         if best_cost is None or cost < best_cost:
             best, best_cost = K, cost
     return best
@@ -205,10 +209,15 @@ def hermitian_block_size(idx, n_total):
     return nb if np.array_equal(np.sort(idx), np.sort(expect)) else None
 
 
+# FP32 blocked matrices on the tensor cores (3xTF32 tcgen05 products) where
+# the shape allows; the CUDA-core kernel otherwise.
+_TENSOR_CORE_BLOCKS = True
+
+
 def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None):
     """FP32 ensemble mean of the selected components of a Hermitian diagonal
     block through its real form: real propagator, real K-step blocked matrix
-    and real blocked loop.  Returns {'mean': (nsteps + 1, len(select))
+    (tcgen05 3xTF32 products when the shape allows) and real blocked loop.  Returns {'mean': (nsteps + 1, len(select))
     complex128, 'status'} like propagate_selected_mean."""
     m = nb * nb
     sel = np.asarray(select, dtype=np.int64)
@@ -216,15 +225,25 @@ def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None)
     partner = np.where(a == b, sel, b + nb * a)
     coords = np.unique(np.concatenate([sel, partner]))
     Dr = build.hermitian_propagator(idx, nb, h)
-    K = pick_block_k_real(nsteps, m, len(coords))
+    use_tc = _TENSOR_CORE_BLOCKS and Dr.dtype == torch.float32
+    K = pick_block_k_real(
+        nsteps, m, len(coords),
+        tensor_core=(lambda k: _native.rk4_block_matrix_real_tc_supported(m, k, len(coords)))
+        if use_tc else None)
     if events is not None:
         b0 = torch.cuda.Event(enable_timing=True)
         b0.record()
-    mat = _native.rk4_block_matrix_real(Dr, K, coords)
+    tc = _native.rk4_block_matrix_real_tc(Dr, K, coords) if use_tc else None
+    if tc is not None:
+        mat, tc_status = tc
+    else:
+        mat, tc_status = _native.rk4_block_matrix_real(Dr, K, coords), None
     if events is not None:
         b1 = torch.cuda.Event(enable_timing=True)
         b1.record()
         events.setdefault('blockbuild', []).append((b0, b1))
+        events['blockbuild_variant'] = 'tcgen05' if tc is not None else 'cuda_core'
+        events['blockbuild_shape'] = (Dr.shape[0], m, K, len(coords))
         # real multiply-adds of the unpadded products: the squares and the
         # final composition of the binary powering (m^3 each) and the
         # selected rows R_2 .. R_{K-1} (nsel m^2 each), 2 flops apiece
@@ -240,6 +259,8 @@ def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None)
         xm, status = _native.rk4_real_block_mean(mat, x0, nsteps, coords, K, check_finite=False)
     else:
         raise NotImplementedError('the real blocked loop needs a block size K > 1')
+    if tc_status is not None:
+        status = status | tc_status
     if events is not None:
         e1 = torch.cuda.Event(enable_timing=True)
         e1.record()

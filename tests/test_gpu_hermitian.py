@@ -117,9 +117,34 @@ def test_workload_uses_real_form_and_matches_fp64():
     X32, P32, st = work.run(offs, 'fp32', ev)
     X64, P64, _ = work.run(offs, 'fp64')
     assert ev['dyn_variant'] == 'real'
+    assert ev['blockbuild_variant'] == 'tcgen05'
     assert int(st.item()) == 0
     assert rel_err(P32.cpu().numpy(), P64.cpu().numpy()) < 1e-5
     assert rel_err(X32.cpu().numpy(), X64.cpu().numpy()) < 1e-5
+
+
+def test_tensor_core_and_cuda_core_block_builds_agree_in_the_ensemble(monkeypatch):
+    """The ensemble populations through the tcgen05 block build equal those
+    through the CUDA-core FP32 build to FP32 rounding."""
+    m, _ = fmo_build()
+    psi = np.zeros(7)
+    psi[4] = 1.0
+    args = (m, psi, 513.0, 300, 'ee')     # 512 steps
+    calls = []
+    real_tc = _native.rk4_block_matrix_real_tc
+
+    def counting(D, K, select):
+        res = real_tc(D, K, select)
+        calls.append((K, res is not None))
+        return res
+
+    monkeypatch.setattr(_native, 'rk4_block_matrix_real_tc', counting)
+    _, tc = ens.ensemble_populations(*args, precision='fp32')
+    assert calls and all(ok for _, ok in calls)
+    monkeypatch.setattr(ens, '_TENSOR_CORE_BLOCKS', False)
+    _, cc = ens.ensemble_populations(*args, precision='fp32')
+    assert len(calls) == 1 or all(ok for _, ok in calls)
+    assert rel_err(tc.cpu().numpy(), cc.cpu().numpy()) < 2e-6
 
 
 @pytest.mark.parametrize('m,P,nsteps', [(7, 1, 2047), (3, 2, 120), (8, 1, 96), (5, 3, 64)])
@@ -145,3 +170,38 @@ def test_projection_blocked_loop_matches_stepwise(m, P, nsteps):
     exact = np.array(exact)
     assert rel_err(blk.cpu().numpy(), exact) < 2e-6
     assert rel_err(ref.cpu().numpy(), exact) < 2e-6
+
+
+@pytest.mark.parametrize('m,K,sel', [(49, 9, [i * 7 + i for i in range(7)]),
+                                     (49, 8, [0, 8, 16, 24, 32, 40, 48]),
+                                     (16, 5, [0, 5, 10, 15]),
+                                     (25, 3, list(range(20))),
+                                     (64, 2, [3, 9])])
+def test_tensor_core_block_matrix_matches(m, K, sel):
+    """3xTF32 tcgen05 form of the real blocked matrices against FP64 powers
+    and the CUDA-core FP32 kernel."""
+    rng = np.random.RandomState(m + K)
+    B = 9
+    D = 0.02 * rng.randn(B, m, m) - 0.01 * np.eye(m)[None]
+    D32 = torch.as_tensor(D).float().cuda()
+    res = _native.rk4_block_matrix_real_tc(D32, K, sel)
+    assert res is not None
+    tc, status = res
+    assert int(status.item()) == 0
+    ref32 = _native.rk4_block_matrix_real(D32, K, sel).cpu().numpy()
+    tc = tc.cpu().numpy()
+    Dd = D32.cpu().numpy().astype(np.float64)
+    for b in range(B):
+        P = np.eye(m) + Dd[b]
+        exact = [np.linalg.matrix_power(P, K) - np.eye(m)]
+        for k in range(1, K):
+            exact.append((np.linalg.matrix_power(P, k) - np.eye(m))[sel])
+        exact = np.concatenate(exact)
+        assert rel_err(tc[b], exact) < 2e-6
+        assert rel_err(tc[b], ref32[b]) < 2e-6
+
+
+def test_tensor_core_block_matrix_unsupported_shapes():
+    D = torch.zeros((2, 49, 49), dtype=torch.float32, device='cuda')
+    assert _native.rk4_block_matrix_real_tc(D, 7, [0, 8]) is None      # K = 7
+    assert _native.rk4_block_matrix_real_tc(D, 9, list(range(49))) is None  # 4 x 49 rows
