@@ -185,23 +185,542 @@ __global__ void __launch_bounds__(512, 1) rk4_hblock_f32(HbP p, int64_t ngroups,
   }
 }
 
-// out[e] = scale * sum over slots of partial[slot][e], slots in order.
-__global__ void hblock_reduce_kernel(const double* __restrict__ partial, int64_t nslots,
-                                     int64_t per, double scale, double* __restrict__ out) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= per) return;
-  double acc = 0.0;
-  for (int64_t sl = 0; sl < nslots; ++sl) acc += partial[sl * per + e];
-  out[e] = acc * scale;
+// Warp-specialised form of the same loop (the default).  Warp 0 holds the M
+// state rows (P^K - I), two per lane (rows l and l + 32), and runs the
+// sequential chain alone: each block-step is one pass over the state (each
+// 16-byte load feeds both rows' paired FMA), the split-word update of the
+// lane's own coordinates and a __syncwarp, with no CTA barrier.  The
+// block-start states go into a ring of 2 CH + 1 slots in shared memory.  The
+// following warps hold the nsel (K - 1) selected rows, 64 per warp, and trail
+// the chain by one chunk of CH block-steps: for each block-start state of the
+// previous chunk they form their selected coordinates at the K - 1
+// intermediate steps, again with no barrier inside the chunk.  Every (step,
+// coordinate) of the CTA's partial sums has one owning thread, which adds to
+// it in shared memory directly; the two sides meet at one CTA barrier per
+// chunk.  Each thread loads its rows from global memory into registers at the
+// start of a sample; the next sample's matrices are prefetched into L2.
+template <int M>
+__device__ __forceinline__ void dot2_rows(const float* __restrict__ cur,
+                                          const float2 (&ra)[((M + 3) & ~3) / 2],
+                                          const float2 (&rb)[((M + 3) & ~3) / 2], float& sa,
+                                          float& sb) {
+  constexpr int MP = (M + 3) & ~3;
+  float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
+  float2 b0 = a0, b1 = a0, b2 = a0, b3 = a0;
+#pragma unroll
+  for (int j = 0; j < MP; j += 4) {
+    const float4 v = *reinterpret_cast<const float4*>(cur + j);
+    const float2 lo = make_float2(v.x, v.y), hi = make_float2(v.z, v.w);
+    if ((j / 4) % 2 == 0) {
+      ffma2(a0, ra[j / 2], lo);
+      ffma2(a1, ra[j / 2 + 1], hi);
+      ffma2(b0, rb[j / 2], lo);
+      ffma2(b1, rb[j / 2 + 1], hi);
+    } else {
+      ffma2(a2, ra[j / 2], lo);
+      ffma2(a3, ra[j / 2 + 1], hi);
+      ffma2(b2, rb[j / 2], lo);
+      ffma2(b3, rb[j / 2 + 1], hi);
+    }
+  }
+  sa = ((a0.x + a0.y) + (a1.x + a1.y)) + ((a2.x + a2.y) + (a3.x + a3.y));
+  sb = ((b0.x + b0.y) + (b1.x + b1.y)) + ((b2.x + b2.y) + (b3.x + b3.y));
 }
+
+template <int M>
+__device__ __forceinline__ void load_row(const float* __restrict__ src, bool act,
+                                         float2 (&d)[((M + 3) & ~3) / 2]) {
+  constexpr int MP = (M + 3) & ~3;
+#pragma unroll
+  for (int j = 0; j < MP; j += 2)
+    d[j / 2] = make_float2((act && j < M) ? __ldg(src + j) : 0.f,
+                           (act && j + 1 < M) ? __ldg(src + j + 1) : 0.f);
+}
+
+template <int M, int MAXT>
+__global__ void __launch_bounds__(MAXT, MAXT == 64 ? 6 : 1)
+    rk4_hblock_ws_f32(HbP p, int K, int chunk) {
+  constexpr int MP = (M + 3) & ~3;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nsel = p.nselect;
+  const int nR = nsel * (K - 1);
+  const int RT = M + nR;
+  const int64_t sstride = ((int64_t)RT * M + 3) & ~(int64_t)3;
+  const int nslot = 2 * chunk + 1;
+  float* __restrict__ ring = reinterpret_cast<float*>(smraw);   // [nslot][MP] block-start states
+  float* __restrict__ lsum = ring + nslot * MP;                 // [nsave][nsel] partial sums
+  const int tid = threadIdx.x, lane = tid & 31;
+  const bool mainw = tid < 32;
+  // this lane's two rows: state rows lane, lane + 32; or selected rows i, i + 32
+  const int ia = mainw ? lane : 64 * ((tid >> 5) - 1) + lane, ib = ia + 32;
+  const bool acta = mainw ? ia < M : ia < nR, actb = mainw ? ib < M : ib < nR;
+  const int rowa = mainw ? ia : M + ia, rowb = mainw ? ib : M + ib;
+  int qa = -1, qb = -1, sela = 0, selb = 0;
+  if (mainw) {
+    for (int q = 0; q < nsel; ++q) {
+      if (acta && p.select[q] == ia) qa = q;
+      if (actb && p.select[q] == ib) qb = q;
+    }
+  } else {
+    if (acta) sela = p.select[ia % nsel];
+    if (actb) selb = p.select[ib % nsel];
+    sela = (sela >= 0 && sela < M) ? sela : 0;
+    selb = (selb >= 0 && selb < M) ? selb : 0;
+  }
+  // threads 32 .. 32 + nsel - 1 also own the selected coordinates at the
+  // block boundaries (steps (b + 1) K)
+  const int bq = (tid >= 32 && tid - 32 < nsel) ? tid - 32 : -1;
+  int bsel = bq >= 0 ? p.select[bq] : 0;
+  bsel = (bsel >= 0 && bsel < M) ? bsel : 0;
+  for (int e = tid; e < nslot * MP; e += blockDim.x) ring[e] = 0.f;
+  for (int e = tid; e < p.nsave * nsel; e += blockDim.x) lsum[e] = 0.f;
+  __syncthreads();
+  const int nblk = p.nsteps / K;
+  const int nch = (nblk + chunk - 1) / chunk;
+  // output slots: state rows at steps (b + 1) K, selected rows at b K + k;
+  // both advance by K nsel per block-step
+  float* const owna = lsum + (mainw ? max(qa, 0) : (ia / nsel + 1) * nsel + ia % nsel);
+  float* const ownb = lsum + (mainw ? max(qb, 0) : (ib / nsel + 1) * nsel + ib % nsel);
+  const bool wa = mainw ? qa >= 0 : acta, wb = mainw ? qb >= 0 : actb;
+  for (int64_t s = blockIdx.x; s < p.batch; s += gridDim.x) {
+    if (tid == 0 && s + gridDim.x < p.batch) {
+      const float* nxt = p.matrix + (s + gridDim.x) * sstride;
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(nxt),
+                   "r"((unsigned)(sstride * 4))
+                   : "memory");
+    }
+    float2 da[MP / 2], db[MP / 2];
+    {
+      const float* src = p.matrix + s * sstride;
+      load_row<M>(src + (int64_t)rowa * M, acta, da);
+      load_row<M>(src + (int64_t)rowb * M, actb, db);
+    }
+    float xha = 0.f, xla = 0.f, xhb = 0.f, xlb = 0.f;
+    if (mainw) {
+      const double* y0 = p.y0 + s * p.y0_stride;
+      if (acta) {
+        const double v = y0[ia];
+        xha = (float)v;
+        xla = (float)(v - (double)xha);
+        ring[ia] = xha;
+        if (wa) owna[0] += xha;
+      }
+      if (actb) {
+        const double v = y0[ib];
+        xhb = (float)v;
+        xlb = (float)(v - (double)xhb);
+        ring[ib] = xhb;
+        if (wb) ownb[0] += xhb;
+      }
+    }
+    __syncthreads();
+    for (int c = 0; c <= nch; ++c) {
+      if (mainw) {
+        if (c < nch) {
+          const int b0 = c * chunk, b1 = min(b0 + chunk, nblk);
+          int slot = b0 % nslot;
+          for (int b = b0; b < b1; ++b) {
+            float sa, sb;
+            dot2_rows<M>(ring + slot * MP, da, db, sa, sb);
+            slot = slot + 1 == nslot ? 0 : slot + 1;
+            float* nxt = ring + slot * MP;
+            if (acta) {
+              dd_add(xha, xla, sa);
+              nxt[ia] = xha;
+            }
+            if (actb) {
+              dd_add(xhb, xlb, sb);
+              nxt[ib] = xhb;
+            }
+            __syncwarp();
+          }
+        }
+      } else if (c >= 1) {
+        const int b0 = (c - 1) * chunk, b1 = min(b0 + chunk, nblk);
+        int slot = b0 % nslot;
+        int64_t off = (int64_t)b0 * K * nsel;
+        for (int b = b0; b < b1; ++b) {
+          const float* cur = ring + slot * MP;
+          float sa, sb;
+          dot2_rows<M>(cur, da, db, sa, sb);
+          if (wa) owna[off] += cur[sela] + sa;
+          if (wb) ownb[off] += cur[selb] + sb;
+          off += K * nsel;
+          slot = slot + 1 == nslot ? 0 : slot + 1;
+          // the selected coordinates of the next block-start state (step
+          // (b + 1) K), written by the chain in this chunk
+          if (bq >= 0) lsum[(int64_t)(b + 1) * K * nsel + bq] += ring[slot * MP + bsel];
+        }
+      }
+      __syncthreads();
+    }
+    if (mainw && p.status && ((acta && !isfinite(xha)) || (actb && !isfinite(xhb))))
+      atomicOr(p.status, QSX_ERR_NONFINITE);
+  }
+  // every (step, coordinate) was last updated by its owner before the final
+  // barrier; write this CTA's slice
+  double* dst = p.partial + (int64_t)blockIdx.x * p.nsave * nsel;
+  for (int e = tid; e < p.nsave * nsel; e += blockDim.x) dst[e] = (double)lsum[e];
+}
+
+// out[e] = scale * sum over slots of partial[slot][e].  One CTA per 32
+// consecutive e: warp w adds slots w, w + 8, ... (each load a coalesced
+// 256-byte row), then warp 0 adds the eight warp sums in warp order, so the
+// summation order is fixed and results are reproducible.
+__global__ void __launch_bounds__(256) hblock_reduce_kernel(const double* __restrict__ partial,
+                                                            int64_t nslots, int64_t per,
+                                                            double scale,
+                                                            double* __restrict__ out) {
+  __shared__ double red[8][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t e = (int64_t)blockIdx.x * 32 + lane;
+  double acc = 0.0;
+  if (e < per)
+    for (int64_t sl = warp; sl < nslots; sl += 8) acc += partial[sl * per + e];
+  red[warp][lane] = acc;
+  __syncthreads();
+  if (warp == 0 && e < per) {
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t += red[w][lane];
+    out[e] = t * scale;
+  }
+}
+
+// Two-pass form of the loop.
+//
+// Pass 1 (rk4_hchain_f32): the state chain alone, one warp per sample and
+// two state rows per lane (rows l, l + 32) in registers, so each SM holds
+// about twelve independent chains.  Each block-step forms x_{b+1} =
+// x_b + (P^K - I) x_b in split-word FP32 and stores the leading word of
+// x_{b+1} both to a two-slot ring in shared memory (the next step's input)
+// and to Y[s][b + 1] in global memory; no CTA barrier, one __syncwarp.
+//
+// Pass 2 (rk4_hcontract_f32): the selected coordinates at the intermediate
+// steps, out[b K + k][q] = x_b[sel_q] + (row R_k,q) . x_b, summed over the
+// samples.  For one sample this is the product of the nsel (K - 1) x M
+// selected rows and the M x nblk states; each thread owns a 4-row x 8-state
+// tile of it and keeps that tile's ensemble sums in registers across all
+// its CTA's samples.  The block-boundary coordinates x_b[sel_q] (steps b K)
+// are summed by the threads of the tiles' first CTA row into shared memory.
+// The sample's selected rows and states are staged in shared memory with
+// cp.async, one sample ahead.
+template <int M>
+__global__ void __launch_bounds__(32, 12)
+    rk4_hchain_f32(const float* __restrict__ matrix, int64_t sstride, const double* __restrict__ y0,
+                   int64_t y0_stride, int64_t batch, int nblk, float* __restrict__ Y,
+                   int* status) {
+  constexpr int MP = (M + 3) & ~3;
+  __shared__ __align__(16) float ring[2][MP];
+  const int lane = threadIdx.x;
+  const int ia = lane, ib = lane + 32;
+  const bool acta = ia < M, actb = ib < M;
+  for (int e = lane; e < 2 * MP; e += 32) (&ring[0][0])[e] = 0.f;
+  __syncwarp();
+  const int64_t ystride = (int64_t)(nblk + 1) * MP;
+  for (int64_t s = blockIdx.x; s < batch; s += gridDim.x) {
+    if (lane == 0 && s + gridDim.x < batch) {
+      const float* nxt = matrix + (s + gridDim.x) * sstride;
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(nxt),
+                   "r"((unsigned)((int64_t)M * M * 4 + 15) & ~15u)
+                   : "memory");
+    }
+    float2 da[MP / 2], db[MP / 2];
+    const float* src = matrix + s * sstride;
+    load_row<M>(src + (int64_t)ia * M, acta, da);
+    load_row<M>(src + (int64_t)ib * M, actb, db);
+    float* ys = Y + s * ystride;
+    float xha = 0.f, xla = 0.f, xhb = 0.f, xlb = 0.f;
+    if (acta) {
+      const double v = y0[s * y0_stride + ia];
+      xha = (float)v;
+      xla = (float)(v - (double)xha);
+      ring[0][ia] = xha;
+    }
+    if (ia < MP) ys[ia] = xha;
+    if (actb) {
+      const double v = y0[s * y0_stride + ib];
+      xhb = (float)v;
+      xlb = (float)(v - (double)xhb);
+      ring[0][ib] = xhb;
+    }
+    if (ib < MP) ys[ib] = xhb;   // the padding columns of the stored states are zero
+    __syncwarp();
+    int cur = 0;
+    for (int b = 0; b < nblk; ++b) {
+      float sa, sb;
+      dot2_rows<M>(ring[cur], da, db, sa, sb);
+      cur ^= 1;
+      float* yn = ys + (int64_t)(b + 1) * MP;
+      if (acta) {
+        dd_add(xha, xla, sa);
+        ring[cur][ia] = xha;
+      }
+      if (ia < MP) yn[ia] = xha;
+      if (actb) {
+        dd_add(xhb, xlb, sb);
+        ring[cur][ib] = xhb;
+      }
+      if (ib < MP) yn[ib] = xhb;
+      __syncwarp();
+    }
+    if (status && ((acta && !isfinite(xha)) || (actb && !isfinite(xhb))))
+      atomicOr(status, QSX_ERR_NONFINITE);
+  }
+}
+
+constexpr int HC_THREADS = 256, HC_TR = 4, HC_TB = 8;
+
+// floats of one pass-2 stage: the selected rows [nR][MP] and the states
+// [nblk + 1][MP] of one sample
+__host__ __device__ inline size_t hcontract_stage_floats(int MP, int nR, int nblk) {
+  return (size_t)(nR + nblk + 1) * MP;
+}
+
+// pass 2 applies when every 4 x 8 tile of one sample's product has its own
+// thread in one CTA
+inline bool hcontract_fits(int nR, int nblk) {
+  return (int64_t)((nR + HC_TR - 1) / HC_TR) * ((nblk + HC_TB - 1) / HC_TB) <= HC_THREADS;
+}
+
+template <int M>
+__global__ void __launch_bounds__(HC_THREADS, 2)
+    rk4_hcontract_f32(const float* __restrict__ matrix, int64_t sstride,
+                      const float* __restrict__ Y, int64_t batch, int nblk, int K,
+                      const int* __restrict__ select, int nsel, double* __restrict__ partial,
+                      int nsave) {
+  constexpr int MP = (M + 3) & ~3;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nR = nsel * (K - 1);
+  const int nrt = (nR + HC_TR - 1) / HC_TR;   // row tiles
+  const int ntiles = nrt * ((nblk + HC_TB - 1) / HC_TB);
+  const int stage = (int)hcontract_stage_floats(MP, nR, nblk);
+  float* buf0 = reinterpret_cast<float*>(smraw);
+  float* bpart = buf0 + 2 * stage;            // [nblk + 1][nsel] boundary sums
+  const int tid = threadIdx.x;
+  const bool owner = tid < ntiles;
+  // interleaved tiles: rows rt + i nrt and states bt + j nbt, so that
+  // neighbouring lanes read neighbouring rows (distinct bank quads at the
+  // row stride MP)
+  const int nbt = (nblk + HC_TB - 1) / HC_TB;
+  const int rt = owner ? tid % nrt : 0, bt = owner ? tid / nrt : 0;
+  int selr[HC_TR];
+#pragma unroll
+  for (int i = 0; i < HC_TR; ++i) {
+    const int row = rt + i * nrt;
+    const int q = row < nR ? select[row % nsel] : 0;
+    selr[i] = (q >= 0 && q < M) ? q : 0;
+  }
+  for (int e = tid; e < (nblk + 1) * nsel; e += HC_THREADS) bpart[e] = 0.f;
+  float acc[HC_TR][HC_TB];
+#pragma unroll
+  for (int i = 0; i < HC_TR; ++i)
+#pragma unroll
+    for (int j = 0; j < HC_TB; ++j) acc[i][j] = 0.f;
+  const int64_t ystride = (int64_t)(nblk + 1) * MP;
+  // one sample into a stage: selected rows re-strided to MP (4-byte copies),
+  // states 0 .. nblk (16-byte copies)
+  auto load = [&](int64_t s, float* st) {
+    const float* rsrc = matrix + s * sstride + (int64_t)M * M;
+    for (int row = tid >> 5; row < nR; row += HC_THREADS / 32)
+      for (int c = tid & 31; c < M; c += 32) {
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(st + row * MP + c);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst),
+                     "l"(rsrc + row * M + c)
+                     : "memory");
+      }
+    const float* ysrc = Y + s * ystride;
+    const unsigned ydst = (unsigned)__cvta_generic_to_shared(st + nR * MP);
+    for (int v = tid; v < (nblk + 1) * MP / 4; v += HC_THREADS)
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(ydst + 16u * v),
+                   "l"(ysrc + 4 * v)
+                   : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  // the padding columns of the re-strided rows stay zero
+  for (int e = tid; e < 2 * stage; e += HC_THREADS) buf0[e] = 0.f;
+  __syncthreads();
+  int par = 0;
+  if (blockIdx.x < batch) load(blockIdx.x, buf0);
+  for (int64_t s = blockIdx.x; s < batch; s += gridDim.x) {
+    if (s + gridDim.x < batch) {
+      load(s + gridDim.x, buf0 + (par ^ 1) * stage);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();
+    const float* R = buf0 + par * stage;
+    const float* X = R + nR * MP;   // X[b][MP], b = 0 .. nblk
+    if (owner) {
+#pragma unroll 1
+      for (int k4 = 0; k4 < MP; k4 += 4) {
+        float4 rv[HC_TR];
+#pragma unroll
+        for (int i = 0; i < HC_TR; ++i)
+          rv[i] = rt + i * nrt < nR ? *reinterpret_cast<const float4*>(R + (rt + i * nrt) * MP + k4)
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < HC_TB; ++j) {
+          const float4 xv = bt + j * nbt < nblk
+                                ? *reinterpret_cast<const float4*>(X + (bt + j * nbt) * MP + k4)
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int i = 0; i < HC_TR; ++i) {
+            float a = acc[i][j];
+            a = fmaf(rv[i].x, xv.x, a);
+            a = fmaf(rv[i].y, xv.y, a);
+            a = fmaf(rv[i].z, xv.z, a);
+            a = fmaf(rv[i].w, xv.w, a);
+            acc[i][j] = a;
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < HC_TB; ++j)
+        if (bt + j * nbt < nblk)
+#pragma unroll
+          for (int i = 0; i < HC_TR; ++i) acc[i][j] += X[(bt + j * nbt) * MP + selr[i]];
+    }
+    // the selected coordinates at the block boundaries, steps b K, b = 0 .. nblk
+    for (int e = tid; e < (nblk + 1) * nsel; e += HC_THREADS) {
+      const int bb = e / nsel, q = e - bb * nsel;
+      int sq = select[q];
+      sq = (sq >= 0 && sq < M) ? sq : 0;
+      bpart[e] += X[bb * MP + sq];
+    }
+    __syncthreads();   // this stage is free for the sample after next
+    par ^= 1;
+  }
+  // every (step, coordinate) of the slice has one writer: the tiles cover
+  // steps b K + k (k = 1 .. K-1), the boundary sums steps b K
+  double* dst = partial + (int64_t)blockIdx.x * nsave * nsel;
+  if (owner) {
+#pragma unroll
+    for (int j = 0; j < HC_TB; ++j) {
+      const int b = bt + j * nbt;
+      if (b < nblk)
+#pragma unroll
+        for (int i = 0; i < HC_TR; ++i) {
+          const int row = rt + i * nrt;
+          if (row < nR) {
+            const int k = row / nsel + 1, q = row - (k - 1) * nsel;
+            dst[((int64_t)b * K + k) * nsel + q] = (double)acc[i][j];
+          }
+        }
+    }
+  }
+  for (int e = tid; e < (nblk + 1) * nsel; e += HC_THREADS) {
+    const int bb = e / nsel;
+    dst[(int64_t)bb * K * nsel + (e - bb * nsel)] = (double)bpart[e];
+  }
+}
+
+#define QSX_HBLOCK_SIZES(X) X(9) X(16) X(25) X(36) X(49) X(64)
 
 struct HbPlan {
   int G, threads, local_sums;
-  int64_t ngroups, grid;
+  int ws, chunk;   // warp-specialised kernel and its chunk of block-steps
+  int tp;          // two-pass form: chain, then contraction
+  int64_t ngroups, grid, chain_grid;
   size_t smem;
+  size_t ybytes;   // two-pass: the block-start states, after the partial slices
 };
 
-#define QSX_HBLOCK_SIZES(X) X(9) X(16) X(25) X(36) X(49) X(64)
+// launch configuration of the two-pass form, if it applies
+static cudaError_t hblock_tp_plan(int m, int64_t batch, int K, int nsteps, int nselect, int group,
+                                  HbPlan* pl, bool* ok) {
+  *ok = false;
+  const int nR = nselect * (K - 1);
+  const int nblk = nsteps / K;
+  if (group > 1 || !hcontract_fits(nR, nblk)) return cudaSuccess;
+  const int MP = (m + 3) & ~3;
+  const size_t smem = (2 * hcontract_stage_floats(MP, nR, nblk) + (size_t)(nblk + 1) * nselect) *
+                      sizeof(float);
+  if (smem > 110 * 1024) return cudaSuccess;
+  int dev = 0, sms = 0, occ_c = 0, occ_h = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+#define X(MM)                                                                                 \
+  if (e == cudaSuccess && m == MM) {                                                          \
+    e = cudaFuncSetAttribute(rk4_hcontract_f32<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             (int)smem);                                                      \
+    if (e == cudaSuccess)                                                                     \
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_h, rk4_hcontract_f32<MM>,        \
+                                                        HC_THREADS, smem);                   \
+    if (e == cudaSuccess)                                                                     \
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, rk4_hchain_f32<MM>, 32, 0);   \
+  }
+  QSX_HBLOCK_SIZES(X)
+#undef X
+  if (e != cudaSuccess) return e;
+  pl->tp = 1;
+  pl->ws = 0;
+  pl->G = 1;
+  pl->smem = smem;
+  pl->local_sums = 1;
+  pl->ngroups = batch;
+  pl->grid = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)sms * std::max(occ_h, 1)));
+  pl->chain_grid = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)sms * std::max(occ_c, 1)));
+  pl->ybytes = (size_t)batch * (nblk + 1) * MP * sizeof(float);
+  *ok = true;
+  return cudaSuccess;
+}
+
+// launch configuration of the warp-specialised kernel, if it applies:
+// one sample per CTA, partial sums in shared memory, at most 448 selected rows
+static bool hblock_ws_plan(int m, int K, int nsteps, int nselect, int group, HbPlan* pl) {
+  const int nR = nselect * (K - 1);
+  if (group > 1 || nR > 448 || nselect > 224) return false;
+  const int MP = (m + 3) & ~3;
+  const size_t lsum = (size_t)(nsteps + 1) * nselect * sizeof(float);
+  for (int chunk = 16; chunk >= 2; chunk /= 2) {
+    const size_t smem = (size_t)(2 * chunk + 1) * MP * sizeof(float) + lsum;
+    if (smem <= 96 * 1024) {
+      pl->ws = 1;
+      pl->chunk = chunk;
+      pl->G = 1;
+      // warp 0 runs the chain; the others hold 64 selected rows each and
+      // own the nsel block-boundary outputs (at least one such warp)
+      pl->threads = 32 + 32 * std::max(std::max((nR + 63) / 64, (nselect + 31) / 32), 1);
+      pl->smem = smem;
+      pl->local_sums = 1;
+      return true;
+    }
+  }
+  return false;
+}
+
+template <int M>
+static cudaError_t hblock_ws_occupancy(const HbPlan& pl, int* occ) {
+  cudaError_t e;
+  if (pl.threads <= 64) {
+    e = cudaFuncSetAttribute(rk4_hblock_ws_f32<M, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pl.smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(rk4_hblock_ws_f32<M, 64>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, rk4_hblock_ws_f32<M, 64>,
+                                                        pl.threads, pl.smem);
+  } else {
+    e = cudaFuncSetAttribute(rk4_hblock_ws_f32<M, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pl.smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, rk4_hblock_ws_f32<M, 256>,
+                                                        pl.threads, pl.smem);
+  }
+  return e;
+}
+
+template <int M>
+static void hblock_ws_launch(const HbPlan& pl, const HbP& p, int K, cudaStream_t s) {
+  if (pl.threads <= 64)
+    rk4_hblock_ws_f32<M, 64><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(p, K, pl.chunk);
+  else
+    rk4_hblock_ws_f32<M, 256><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(p, K, pl.chunk);
+}
+
 
 static int hblock_plan(int m, int64_t batch, int K, int nsteps, int nselect, int group,
                        HbPlan* pl) {
@@ -209,6 +728,30 @@ static int hblock_plan(int m, int64_t batch, int K, int nsteps, int nselect, int
   QSX_CHECK_ARG(RT <= 512, "qsx_rk4_real_block_mean: %d blocked rows per sample exceed 512", RT);
   QSX_CHECK_ARG(group >= 0 && group * RT <= 512,
                 "qsx_rk4_real_block_mean: %d samples of %d rows exceed 512 threads", group, RT);
+  pl->ws = 0;
+  pl->chunk = 0;
+  pl->tp = 0;
+  pl->chain_grid = 0;
+  pl->ybytes = 0;
+  {
+    bool ok = false;
+    cudaError_t e = hblock_tp_plan(m, batch, K, nsteps, nselect, group, pl, &ok);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_real_block_mean plan");
+    if (ok) return QSX_OK;
+  }
+  if (hblock_ws_plan(m, K, nsteps, nselect, group, pl)) {
+    pl->ngroups = batch;
+    int dev = 0, sms = 0, occ = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+#define X(MM) \
+    if (e == cudaSuccess && m == MM) e = hblock_ws_occupancy<MM>(*pl, &occ);
+    QSX_HBLOCK_SIZES(X)
+#undef X
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_real_block_mean plan");
+    pl->grid = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)sms * std::max(occ, 1)));
+    return QSX_OK;
+  }
   // one sample per CTA by default: each CTA is an independent pipeline with
   // its own barrier, several resident per SM
   pl->G = group ? group : 1;
@@ -254,12 +797,17 @@ static int hblock_check(int m, int64_t batch, int K, int nsteps, int nselect) {
 
 using namespace qsx;
 
+// the CTA partial slices, rounded up to 256 bytes (the two-pass states follow)
+static size_t hblock_partial_bytes(const HbPlan& pl, int nsteps, int nselect) {
+  return ((size_t)pl.grid * (nsteps + 1) * nselect * sizeof(double) + 255) & ~(size_t)255;
+}
+
 extern "C" size_t qsx_rk4_real_block_workspace_bytes(int m, int64_t batch, int K, int nsteps,
                                                      int nselect, int group) {
   if (hblock_check(m, batch, K, nsteps, nselect) != QSX_OK || batch == 0) return 0;
   HbPlan pl;
   if (hblock_plan(m, batch, K, nsteps, nselect, group, &pl) != QSX_OK) return 0;
-  return (size_t)pl.grid * (nsteps + 1) * nselect * sizeof(double);
+  return hblock_partial_bytes(pl, nsteps, nselect) + pl.ybytes;
 }
 
 extern "C" int qsx_rk4_real_block_mean(const float* matrix, int m, int64_t batch, int K,
@@ -276,24 +824,12 @@ extern "C" int qsx_rk4_real_block_mean(const float* matrix, int m, int64_t batch
   st = hblock_plan(m, batch, K, nsteps, nselect, group, &pl);
   if (st) return st;
   const int64_t per = (int64_t)(nsteps + 1) * nselect;
-  const size_t need = (size_t)pl.grid * per * sizeof(double);
+  const size_t need = hblock_partial_bytes(pl, nsteps, nselect) + pl.ybytes;
   QSX_CHECK_ARG(workspace_bytes >= need,
                 "qsx_rk4_real_block_mean: workspace of %zu bytes needed (got %zu)", need,
                 workspace_bytes);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e;
-  if (!pl.local_sums) {  // the FP64 atomics accumulate into zeroed slices
-    e = cudaMemsetAsync(workspace, 0, need, s);
-    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_real_block_mean memset");
-  }
-#define X(MM)                                                                          \
-  if (m == MM) {                                                                       \
-    e = cudaFuncSetAttribute(rk4_hblock_f32<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             (int)pl.smem);                                            \
-    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_real_block_mean");            \
-  }
-  QSX_HBLOCK_SIZES(X)
-#undef X
   HbP p;
   p.m = m;
   p.nsteps = nsteps;
@@ -307,13 +843,58 @@ extern "C" int qsx_rk4_real_block_mean(const float* matrix, int m, int64_t batch
   p.partial = (double*)workspace;
   p.status = status;
   p.local_sums = pl.local_sums;
+  if (pl.tp) {
+    const int nblk = nsteps / K;
+    const int MP = (m + 3) & ~3;
+    const int64_t sstride = ((int64_t)(m + nselect * (K - 1)) * m + 3) & ~(int64_t)3;
+    float* Y = reinterpret_cast<float*>(static_cast<char*>(workspace) +
+                                        hblock_partial_bytes(pl, nsteps, nselect));
+    (void)MP;
+#define X(MM)                                                                                  \
+    if (m == MM) {                                                                             \
+      rk4_hchain_f32<MM><<<(unsigned)pl.chain_grid, 32, 0, s>>>(matrix, sstride, y0, y0_stride, \
+                                                                batch, nblk, Y, status);       \
+      rk4_hcontract_f32<MM><<<(unsigned)pl.grid, HC_THREADS, pl.smem, s>>>(                    \
+          matrix, sstride, Y, batch, nblk, K, select, nselect, (double*)workspace, nsteps + 1); \
+    }
+    QSX_HBLOCK_SIZES(X)
+#undef X
+    QSX_LAUNCH_CHECK("qsx_rk4_real_block_mean");
+    hblock_reduce_kernel<<<(unsigned)((per + 31) / 32), 256, 0, s>>>(
+        (const double*)workspace, pl.grid, per, 1.0 / (double)batch, out_mean);
+    QSX_LAUNCH_CHECK("qsx_rk4_real_block_mean reduce");
+    return QSX_OK;
+  }
+  if (pl.ws) {
+#define X(MM) \
+    if (m == MM) hblock_ws_launch<MM>(pl, p, K, s);
+    QSX_HBLOCK_SIZES(X)
+#undef X
+    QSX_LAUNCH_CHECK("qsx_rk4_real_block_mean");
+    hblock_reduce_kernel<<<(unsigned)((per + 31) / 32), 256, 0, s>>>(
+        (const double*)workspace, pl.grid, per, 1.0 / (double)batch, out_mean);
+    QSX_LAUNCH_CHECK("qsx_rk4_real_block_mean reduce");
+    return QSX_OK;
+  }
+  if (!pl.local_sums) {  // the FP64 atomics accumulate into zeroed slices
+    e = cudaMemsetAsync(workspace, 0, need, s);
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_real_block_mean memset");
+  }
+#define X(MM)                                                                          \
+  if (m == MM) {                                                                       \
+    e = cudaFuncSetAttribute(rk4_hblock_f32<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             (int)pl.smem);                                            \
+    if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_real_block_mean");            \
+  }
+  QSX_HBLOCK_SIZES(X)
+#undef X
 #define X(MM)                                                                               \
   if (m == MM) rk4_hblock_f32<MM><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(p, pl.ngroups, \
                                                                                 pl.G, K);
   QSX_HBLOCK_SIZES(X)
 #undef X
   QSX_LAUNCH_CHECK("qsx_rk4_real_block_mean");
-  hblock_reduce_kernel<<<(unsigned)((per + 255) / 256), 256, 0, s>>>(
+  hblock_reduce_kernel<<<(unsigned)((per + 31) / 32), 256, 0, s>>>(
       (const double*)workspace, pl.grid, per, 1.0 / (double)batch, out_mean);
   QSX_LAUNCH_CHECK("qsx_rk4_real_block_mean reduce");
   return QSX_OK;
