@@ -19,6 +19,7 @@
 #include <algorithm>
 
 #include "qsx_common.cuh"
+#include "qsx_tc.cuh"
 
 namespace qsx {
 
@@ -43,7 +44,7 @@ __device__ __forceinline__ void ffma2(float2& acc, float2 a, float2 b) {
 template <int M>
 __global__ void __launch_bounds__(512, 1) rk4_hblock_f32(HbP p, int64_t ngroups, int G, int K) {
   constexpr int MP = (M + 3) & ~3;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   const int64_t sstride = ((int64_t)(M + p.nselect * (K - 1)) * M + 3) & ~(int64_t)3;
   float* mbuf = (float*)smraw;          // [G][sstride] next group's matrices (prefetched)
   float* xbuf = mbuf + G * sstride;     // [2][G][MP]
@@ -241,7 +242,7 @@ template <int M, int MAXT>
 __global__ void __launch_bounds__(MAXT, MAXT == 64 ? 6 : 1)
     rk4_hblock_ws_f32(HbP p, int K, int chunk) {
   constexpr int MP = (M + 3) & ~3;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   const int nsel = p.nselect;
   const int nR = nsel * (K - 1);
   const int RT = M + nR;
@@ -396,15 +397,9 @@ __global__ void __launch_bounds__(256) hblock_reduce_kernel(const double* __rest
 // x_{b+1} both to a two-slot ring in shared memory (the next step's input)
 // and to Y[s][b + 1] in global memory; no CTA barrier, one __syncwarp.
 //
-// Pass 2 (rk4_hcontract_f32): the selected coordinates at the intermediate
-// steps, out[b K + k][q] = x_b[sel_q] + (row R_k,q) . x_b, summed over the
-// samples.  For one sample this is the product of the nsel (K - 1) x M
-// selected rows and the M x nblk states; each thread owns a 4-row x 8-state
-// tile of it and keeps that tile's ensemble sums in registers across all
-// its CTA's samples.  The block-boundary coordinates x_b[sel_q] (steps b K)
-// are summed by the threads of the tiles' first CTA row into shared memory.
-// The sample's selected rows and states are staged in shared memory with
-// cp.async, one sample ahead.
+// Pass 2 (rk4_hcontract_tc, below): the selected coordinates at the
+// intermediate steps, out[b K + k][q] = x_b[sel_q] + (row R_k,q) . x_b,
+// summed over the samples, on the tensor cores.
 template <int M>
 __global__ void __launch_bounds__(32, 12)
     rk4_hchain_f32(const float* __restrict__ matrix, int64_t sstride, const double* __restrict__ y0,
@@ -469,151 +464,250 @@ __global__ void __launch_bounds__(32, 12)
   }
 }
 
-constexpr int HC_THREADS = 256, HC_TR = 4, HC_TB = 8;
+constexpr int HC_THREADS = 128;
 
-// floats of one pass-2 stage: the selected rows [nR][MP] and the states
-// [nblk + 1][MP] of one sample
-__host__ __device__ inline size_t hcontract_stage_floats(int MP, int nR, int nblk) {
-  return (size_t)(nR + nblk + 1) * MP;
+// Shapes and shared memory of pass 2: A = the nR selected rows (M = 128
+// accumulator rows, K = KP), B = the nblk block-start states (N = nblk
+// rounded up to 16, at most 128); hi/lo planes of both, the boundary sums
+// [nblk + 1][nsel], the mbarrier and the tensor-memory address.
+struct HcShape {
+  int kp, nb, tmem_cols, arows;
+  size_t smem;
+};
+
+// A planes hold `arows` rows: 64 when nR <= 64, since the MMA's rows 64..127
+// may then read whatever follows (their accumulator rows are never used),
+// else 128.  The staging scratch holds either the raw selected rows or the
+// raw states of one sample.
+inline size_t hcontract_scratch_floats(int m, int nR, int nblk) {
+  const size_t mp = (size_t)((m + 3) & ~3);
+  return std::max((size_t)nR * m, (size_t)(nblk + 1) * mp);
 }
 
-// pass 2 applies when every 4 x 8 tile of one sample's product has its own
-// thread in one CTA
-inline bool hcontract_fits(int nR, int nblk) {
-  return (int64_t)((nR + HC_TR - 1) / HC_TR) * ((nblk + HC_TB - 1) / HC_TB) <= HC_THREADS;
+inline bool hcontract_shape(int m, int nR, int nblk, int nsel, HcShape* sh) {
+  if (nR > tc::ROWS || nblk < 1 || nblk > 128) return false;
+  sh->kp = (m + 7) & ~7;
+  sh->nb = (nblk + 15) & ~15;
+  sh->arows = nR <= 64 ? 64 : tc::ROWS;
+  sh->tmem_cols = 32;
+  while (sh->tmem_cols < sh->nb) sh->tmem_cols *= 2;
+  const size_t planes = 2 * (size_t)sh->arows * sh->kp * 4 + 2 * (size_t)sh->nb * sh->kp * 4;
+  sh->smem = ((planes + hcontract_scratch_floats(m, nR, nblk) * 4 + (size_t)(nblk + 1) * nsel * 4 +
+               15) & ~(size_t)15) + 16;
+  // the A operand of each MMA spans 128 rows from its plane's start: with
+  // 64-row planes the lo plane's rows 64..127 end at 3 x 64 rows, which
+  // must lie inside the allocation
+  sh->smem = std::max(sh->smem, (size_t)3 * 64 * sh->kp * 4);
+  return sh->smem <= 227 * 1024;
 }
 
+// Pass 2 on the tensor cores.  Summed over the samples, the intermediate
+// coordinates are out[b K + k][q] = sum_s (R_s)_{k,q} . x^s_b + sum_s
+// x^s_b[sel_q]: the first term is the product of the stacked selected rows
+// [R_1 | R_2 | ...] with the stacked states [X_1; X_2; ...], i.e. one long-K
+// GEMM, which the tcgen05 accumulator forms by adding every sample's
+// 3xTF32 chain into the same TMEM tile.  Per sample the CTA loads the rows
+// and states into registers (ahead of the previous chain's completion),
+// splits them into TF32 hi/lo planes and issues one chain of 3 KP / 8 MMAs;
+// the second term (the block-boundary coordinates, also the outputs at steps
+// b K) is summed by the thread that stages state b.  Two CTAs share an SM so
+// that one stages while the other's chain runs; at the end the CTA writes
+// its slice from TMEM.  Every barrier wait is bounded.
 template <int M>
 __global__ void __launch_bounds__(HC_THREADS, 2)
-    rk4_hcontract_f32(const float* __restrict__ matrix, int64_t sstride,
-                      const float* __restrict__ Y, int64_t batch, int nblk, int K,
-                      const int* __restrict__ select, int nsel, double* __restrict__ partial,
-                      int nsave) {
+    rk4_hcontract_tc(const float* __restrict__ matrix, int64_t sstride, const float* __restrict__ Y,
+                     int64_t batch, int nblk, int K, const int* __restrict__ select, int nsel,
+                     int nb, int tmem_cols, int arows, double* __restrict__ partial, int nsave,
+                     int* status) {
+  using namespace tc;
   constexpr int MP = (M + 3) & ~3;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int KP = (M + 7) & ~7;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  const uint32_t sbo = KP * 32u;
+  const uint32_t PA = (uint32_t)arows * KP * 4, PB = (uint32_t)nb * KP * 4;
+  unsigned char* a_hi = smraw;
+  unsigned char* a_lo = a_hi + PA;
+  unsigned char* b_hi = a_lo + PA;
+  unsigned char* b_lo = b_hi + PB;
+  const int nR_ = nsel * (K - 1);
+  const int nsc = max(nR_ * M, (nblk + 1) * MP);
+  float* sc = reinterpret_cast<float*>(b_lo + PB);      // staging scratch [nsc]
+  float* bsum = sc + nsc;                               // [nblk + 1][nsel]
+  const uint32_t off_mbar =
+      (2 * PA + 2 * PB + (uint32_t)(nsc + (nblk + 1) * nsel) * 4 + 15) & ~15u;
+  uint64_t* mbar_p = reinterpret_cast<uint64_t*>(smraw + off_mbar);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar_p + 1);
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5;
   const int nR = nsel * (K - 1);
-  const int nrt = (nR + HC_TR - 1) / HC_TR;   // row tiles
-  const int ntiles = nrt * ((nblk + HC_TB - 1) / HC_TB);
-  const int stage = (int)hcontract_stage_floats(MP, nR, nblk);
-  float* buf0 = reinterpret_cast<float*>(smraw);
-  float* bpart = buf0 + 2 * stage;            // [nblk + 1][nsel] boundary sums
-  const int tid = threadIdx.x;
-  const bool owner = tid < ntiles;
-  // interleaved tiles: rows rt + i nrt and states bt + j nbt, so that
-  // neighbouring lanes read neighbouring rows (distinct bank quads at the
-  // row stride MP)
-  const int nbt = (nblk + HC_TB - 1) / HC_TB;
-  const int rt = owner ? tid % nrt : 0, bt = owner ? tid / nrt : 0;
-  int selr[HC_TR];
-#pragma unroll
-  for (int i = 0; i < HC_TR; ++i) {
-    const int row = rt + i * nrt;
-    const int q = row < nR ? select[row % nsel] : 0;
-    selr[i] = (q >= 0 && q < M) ? q : 0;
+  const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(mbar_p);
+  const uint64_t da_hi = smem_desc((uint32_t)__cvta_generic_to_shared(a_hi), sbo);
+  const uint64_t da_lo = smem_desc((uint32_t)__cvta_generic_to_shared(a_lo), sbo);
+  const uint64_t db_hi = smem_desc((uint32_t)__cvta_generic_to_shared(b_hi), sbo);
+  const uint64_t db_lo = smem_desc((uint32_t)__cvta_generic_to_shared(b_lo), sbo);
+  const uint32_t idesc = make_idesc(nb);
+  for (uint32_t e = tid; e < (2 * PA + 2 * PB) / 16; e += HC_THREADS)
+    reinterpret_cast<uint4*>(smraw)[e] = make_uint4(0, 0, 0, 0);
+  for (int e = tid; e < (nblk + 1) * nsel; e += HC_THREADS) bsum[e] = 0.f;
+  if (tid == 0) {
+    s_abort = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int e = tid; e < (nblk + 1) * nsel; e += HC_THREADS) bpart[e] = 0.f;
-  float acc[HC_TR][HC_TB];
-#pragma unroll
-  for (int i = 0; i < HC_TR; ++i)
-#pragma unroll
-    for (int j = 0; j < HC_TB; ++j) acc[i][j] = 0.f;
-  const int64_t ystride = (int64_t)(nblk + 1) * MP;
-  // one sample into a stage: selected rows re-strided to MP (4-byte copies),
-  // states 0 .. nblk (16-byte copies)
-  auto load = [&](int64_t s, float* st) {
-    const float* rsrc = matrix + s * sstride + (int64_t)M * M;
-    for (int row = tid >> 5; row < nR; row += HC_THREADS / 32)
-      for (int c = tid & 31; c < M; c += 32) {
-        const unsigned dst = (unsigned)__cvta_generic_to_shared(st + row * MP + c);
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst),
-                     "l"(rsrc + row * M + c)
-                     : "memory");
-      }
-    const float* ysrc = Y + s * ystride;
-    const unsigned ydst = (unsigned)__cvta_generic_to_shared(st + nR * MP);
-    for (int v = tid; v < (nblk + 1) * MP / 4; v += HC_THREADS)
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(ydst + 16u * v),
-                   "l"(ysrc + 4 * v)
-                   : "memory");
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  };
-  // the padding columns of the re-strided rows stay zero
-  for (int e = tid; e < 2 * stage; e += HC_THREADS) buf0[e] = 0.f;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(tmem_slot)),
+                 "r"(tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
   __syncthreads();
-  int par = 0;
-  if (blockIdx.x < batch) load(blockIdx.x, buf0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  // this thread's selected row (A row = TMEM lane = tid) and states b = tid,
+  // tid + 128 (B rows; the boundary sums also take b = nblk)
+  const bool arow = tid < nR;
+  const int64_t ystride = (int64_t)(nblk + 1) * MP;
+  uint32_t parity = 0;
+  bool first = true;
+  const bool brow = tid < nblk;   // this thread stages state b = tid
+  // per-sample loads, coalesced: the selected rows (nR x M floats, from a
+  // 4-byte-aligned start) and the states ((nblk + 1) x MP floats, 16-byte
+  // aligned), each thread taking every HC_THREADS-th element / vector
+  constexpr int RA = (128 * 64 + HC_THREADS - 1) / HC_THREADS;          // bound for nR M
+  constexpr int RY = ((129 * MP) / 4 + HC_THREADS - 1) / HC_THREADS;    // bound for (nblk + 1) MP / 4
+  const int na = nR * M, ny4 = (nblk + 1) * MP / 4;
   for (int64_t s = blockIdx.x; s < batch; s += gridDim.x) {
-    if (s + gridDim.x < batch) {
-      load(s + gridDim.x, buf0 + (par ^ 1) * stage);
-      asm volatile("cp.async.wait_group 1;" ::: "memory");
-    } else {
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (tid == 0 && s + gridDim.x < batch) {
+      // the next sample's selected rows and states into L2
+      const int64_t n = s + gridDim.x;
+      const uintptr_t r0 = reinterpret_cast<uintptr_t>(matrix + n * sstride + (int64_t)M * M) & ~(uintptr_t)15;
+      const uintptr_t r1 = (reinterpret_cast<uintptr_t>(matrix + n * sstride + (int64_t)(M + nR) * M) + 15) &
+                           ~(uintptr_t)15;
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(r0), "r"((unsigned)(r1 - r0))
+                   : "memory");
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(Y + n * ystride),
+                   "r"((unsigned)(ystride * 4))
+                   : "memory");
+    }
+    // this sample's data into registers while the previous chain runs
+    const float* rsrc = matrix + s * sstride + (int64_t)M * M;
+    const float4* ysrc = reinterpret_cast<const float4*>(Y + s * ystride);
+    float ra[RA];
+    float4 ry[RY];
+#pragma unroll
+    for (int j = 0; j < RA; ++j) {
+      const int e = tid + HC_THREADS * j;
+      ra[j] = e < na ? __ldg(rsrc + e) : 0.f;
+    }
+#pragma unroll
+    for (int j = 0; j < RY; ++j) {
+      const int e = tid + HC_THREADS * j;
+      ry[j] = e < ny4 ? __ldg(ysrc + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (!first) {
+      if (tid == 0 && !wait_parity(mbar, parity)) {
+        if (status) atomicOr(status, QSX_ERR_CUDA);
+        s_abort = 1;
+      }
+      __syncthreads();
+      if (s_abort) break;
+      parity ^= 1;
+    }
+    // selected rows: scratch (row-major, stride M), then each row's owner
+    // splits it into the A planes
+#pragma unroll
+    for (int j = 0; j < RA; ++j) {
+      const int e = tid + HC_THREADS * j;
+      if (e < na) sc[e] = ra[j];
     }
     __syncthreads();
-    const float* R = buf0 + par * stage;
-    const float* X = R + nR * MP;   // X[b][MP], b = 0 .. nblk
-    if (owner) {
-#pragma unroll 1
-      for (int k4 = 0; k4 < MP; k4 += 4) {
-        float4 rv[HC_TR];
+    if (arow) {
+      float a[KP];
 #pragma unroll
-        for (int i = 0; i < HC_TR; ++i)
-          rv[i] = rt + i * nrt < nR ? *reinterpret_cast<const float4*>(R + (rt + i * nrt) * MP + k4)
-                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int c = 0; c < KP; ++c) a[c] = c < M ? sc[tid * M + c] : 0.f;
 #pragma unroll
-        for (int j = 0; j < HC_TB; ++j) {
-          const float4 xv = bt + j * nbt < nblk
-                                ? *reinterpret_cast<const float4*>(X + (bt + j * nbt) * MP + k4)
-                                : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int g = 0; g < KP / 4; ++g)
+        st_split4(a_hi, a_lo, op_offset(tid, 4 * g, sbo), a[4 * g], a[4 * g + 1], a[4 * g + 2],
+                  a[4 * g + 3]);
+    }
+    __syncthreads();
+    // states: scratch ([nblk + 1][MP]), then state b = tid into the B planes
+    // and the boundary coordinates of states b = tid, tid + 128, ...
 #pragma unroll
-          for (int i = 0; i < HC_TR; ++i) {
-            float a = acc[i][j];
-            a = fmaf(rv[i].x, xv.x, a);
-            a = fmaf(rv[i].y, xv.y, a);
-            a = fmaf(rv[i].z, xv.z, a);
-            a = fmaf(rv[i].w, xv.w, a);
-            acc[i][j] = a;
-          }
-        }
+    for (int j = 0; j < RY; ++j) {
+      const int e = tid + HC_THREADS * j;
+      if (e < ny4) reinterpret_cast<float4*>(sc)[e] = ry[j];
+    }
+    __syncthreads();
+    if (brow) {
+      float x[KP];
+#pragma unroll
+      for (int c4 = 0; c4 < KP; c4 += 4) {
+        const float4 v = c4 < MP ? *reinterpret_cast<const float4*>(sc + tid * MP + c4)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+        x[c4] = v.x;
+        x[c4 + 1] = v.y;
+        x[c4 + 2] = v.z;
+        x[c4 + 3] = v.w;
       }
 #pragma unroll
-      for (int j = 0; j < HC_TB; ++j)
-        if (bt + j * nbt < nblk)
-#pragma unroll
-          for (int i = 0; i < HC_TR; ++i) acc[i][j] += X[(bt + j * nbt) * MP + selr[i]];
+      for (int g = 0; g < KP / 4; ++g)
+        st_split4(b_hi, b_lo, op_offset(tid, 4 * g, sbo), x[4 * g], x[4 * g + 1], x[4 * g + 2],
+                  x[4 * g + 3]);
     }
-    // the selected coordinates at the block boundaries, steps b K, b = 0 .. nblk
-    for (int e = tid; e < (nblk + 1) * nsel; e += HC_THREADS) {
-      const int bb = e / nsel, q = e - bb * nsel;
-      int sq = select[q];
-      sq = (sq >= 0 && sq < M) ? sq : 0;
-      bpart[e] += X[bb * MP + sq];
-    }
-    __syncthreads();   // this stage is free for the sample after next
-    par ^= 1;
+    for (int b = tid; b <= nblk; b += HC_THREADS)
+      for (int q = 0; q < nsel; ++q) {
+        int c = __ldg(select + q);
+        c = (c >= 0 && c < M) ? c : 0;
+        bsum[b * nsel + q] += sc[b * MP + c];
+      }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0)
+      issue_product(tmem, da_hi, da_lo, db_hi, db_lo, KP / 8, idesc, mbar, first ? 0u : 1u);
+    first = false;
   }
-  // every (step, coordinate) of the slice has one writer: the tiles cover
-  // steps b K + k (k = 1 .. K-1), the boundary sums steps b K
+  if (!first && !s_abort) {
+    if (tid == 0 && !wait_parity(mbar, parity)) {
+      if (status) atomicOr(status, QSX_ERR_CUDA);
+      s_abort = 1;
+    }
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   double* dst = partial + (int64_t)blockIdx.x * nsave * nsel;
-  if (owner) {
+  const int k = arow ? tid / nsel + 1 : 0, q = arow ? tid % nsel : 0;
+  if (!s_abort) {
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+    for (int c0 = 0; c0 < nb; c0 += 16) {
+      float v[16];
+      if (first) {
 #pragma unroll
-    for (int j = 0; j < HC_TB; ++j) {
-      const int b = bt + j * nbt;
-      if (b < nblk)
+        for (int j = 0; j < 16; ++j) v[j] = 0.f;
+      } else {
+        tmem_load(lane_addr + (uint32_t)c0, v);
+      }
 #pragma unroll
-        for (int i = 0; i < HC_TR; ++i) {
-          const int row = rt + i * nrt;
-          if (row < nR) {
-            const int k = row / nsel + 1, q = row - (k - 1) * nsel;
-            dst[((int64_t)b * K + k) * nsel + q] = (double)acc[i][j];
-          }
-        }
+      for (int j = 0; j < 16; ++j) {
+        const int b = c0 + j;
+        if (arow && b < nblk)
+          dst[((int64_t)b * K + k) * nsel + q] = (double)v[j] + (double)bsum[b * nsel + q];
+      }
     }
+    for (int e = tid; e < (nblk + 1) * nsel; e += HC_THREADS) {
+      const int bb = e / nsel;
+      dst[(int64_t)bb * K * nsel + (e - bb * nsel)] = (double)bsum[e];
+    }
+  } else if (tid == 0) {
+    wait_parity(mbar, parity);   // let an unfinished chain drain before freeing TMEM
   }
-  for (int e = tid; e < (nblk + 1) * nsel; e += HC_THREADS) {
-    const int bb = e / nsel;
-    dst[(int64_t)bb * K * nsel + (e - bb * nsel)] = (double)bpart[e];
-  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(tmem_cols)
+                 : "memory");
 }
 
 #define QSX_HBLOCK_SIZES(X) X(9) X(16) X(25) X(36) X(49) X(64)
@@ -622,6 +716,7 @@ struct HbPlan {
   int G, threads, local_sums;
   int ws, chunk;   // warp-specialised kernel and its chunk of block-steps
   int tp;          // two-pass form: chain, then contraction
+  int nb, tmem_cols, arows;   // two-pass: padded states, tensor-memory columns, A plane rows
   int64_t ngroups, grid, chain_grid;
   size_t smem;
   size_t ybytes;   // two-pass: the block-start states, after the partial slices
@@ -633,21 +728,19 @@ static cudaError_t hblock_tp_plan(int m, int64_t batch, int K, int nsteps, int n
   *ok = false;
   const int nR = nselect * (K - 1);
   const int nblk = nsteps / K;
-  if (group > 1 || !hcontract_fits(nR, nblk)) return cudaSuccess;
-  const int MP = (m + 3) & ~3;
-  const size_t smem = (2 * hcontract_stage_floats(MP, nR, nblk) + (size_t)(nblk + 1) * nselect) *
-                      sizeof(float);
-  if (smem > 110 * 1024) return cudaSuccess;
-  int dev = 0, sms = 0, occ_c = 0, occ_h = 0;
+  HcShape sh;
+  if (group > 1 || K < 2 || !hcontract_shape(m, nR, nblk, nselect, &sh)) return cudaSuccess;
+  int dev = 0, sms = 0, occ_c = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 #define X(MM)                                                                                 \
   if (e == cudaSuccess && m == MM) {                                                          \
-    e = cudaFuncSetAttribute(rk4_hcontract_f32<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             (int)smem);                                                      \
+    e = cudaFuncSetAttribute(rk4_hcontract_tc<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             (int)sh.smem);                                                   \
     if (e == cudaSuccess)                                                                     \
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_h, rk4_hcontract_f32<MM>,        \
-                                                        HC_THREADS, smem);                   \
+      e = cudaFuncSetAttribute(rk4_hcontract_tc<MM>,                                          \
+                               cudaFuncAttributePreferredSharedMemoryCarveout,                \
+                               (int)cudaSharedmemCarveoutMaxShared);                          \
     if (e == cudaSuccess)                                                                     \
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, rk4_hchain_f32<MM>, 32, 0);   \
   }
@@ -657,12 +750,18 @@ static cudaError_t hblock_tp_plan(int m, int64_t batch, int K, int nsteps, int n
   pl->tp = 1;
   pl->ws = 0;
   pl->G = 1;
-  pl->smem = smem;
+  pl->smem = sh.smem;
   pl->local_sums = 1;
   pl->ngroups = batch;
-  pl->grid = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)sms * std::max(occ_h, 1)));
+  pl->nb = sh.nb;
+  pl->tmem_cols = sh.tmem_cols;
+  pl->arows = sh.arows;
+  // two contraction CTAs per SM (one stages while the other's chain runs);
+  // the occupancy query can report fewer for tcgen05 kernels, and a second
+  // wave is harmless because every CTA strides over the samples on its own
+  pl->grid = std::max<int64_t>(1, std::min<int64_t>(batch, 2 * (int64_t)sms));
   pl->chain_grid = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)sms * std::max(occ_c, 1)));
-  pl->ybytes = (size_t)batch * (nblk + 1) * MP * sizeof(float);
+  pl->ybytes = (size_t)batch * (nblk + 1) * ((m + 3) & ~3) * sizeof(float);
   *ok = true;
   return cudaSuccess;
 }
@@ -854,8 +953,9 @@ extern "C" int qsx_rk4_real_block_mean(const float* matrix, int m, int64_t batch
     if (m == MM) {                                                                             \
       rk4_hchain_f32<MM><<<(unsigned)pl.chain_grid, 32, 0, s>>>(matrix, sstride, y0, y0_stride, \
                                                                 batch, nblk, Y, status);       \
-      rk4_hcontract_f32<MM><<<(unsigned)pl.grid, HC_THREADS, pl.smem, s>>>(                    \
-          matrix, sstride, Y, batch, nblk, K, select, nselect, (double*)workspace, nsteps + 1); \
+      rk4_hcontract_tc<MM><<<(unsigned)pl.grid, HC_THREADS, pl.smem, s>>>(                     \
+          matrix, sstride, Y, batch, nblk, K, select, nselect, pl.nb, pl.tmem_cols, pl.arows,   \
+          (double*)workspace, nsteps + 1, status);                                              \
     }
     QSX_HBLOCK_SIZES(X)
 #undef X
