@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(32, 12)
   }
 }
 
-constexpr int HC_THREADS = 128;
+constexpr int HC_THREADS = 128, HC_FLUSH = 4;
 
 // Shapes and shared memory of pass 2: A = the nR selected rows (M = 128
 // accumulator rows, K = KP), B = the nblk block-start states (N = nblk
@@ -489,8 +489,9 @@ inline bool hcontract_shape(int m, int nR, int nblk, int nsel, HcShape* sh) {
   sh->kp = (m + 7) & ~7;
   sh->nb = (nblk + 15) & ~15;
   sh->arows = nR <= 64 ? 64 : tc::ROWS;
+  // two tiles: the MMA tile and the running sum
   sh->tmem_cols = 32;
-  while (sh->tmem_cols < sh->nb) sh->tmem_cols *= 2;
+  while (sh->tmem_cols < 2 * sh->nb) sh->tmem_cols *= 2;
   const size_t planes = 2 * (size_t)sh->arows * sh->kp * 4 + 2 * (size_t)sh->nb * sh->kp * 4;
   sh->smem = ((planes + hcontract_scratch_floats(m, nR, nblk) * 4 + (size_t)(nblk + 1) * nsel * 4 +
                15) & ~(size_t)15) + 16;
@@ -570,7 +571,33 @@ __global__ void __launch_bounds__(HC_THREADS, 2)
   const int64_t ystride = (int64_t)(nblk + 1) * MP;
   uint32_t parity = 0;
   bool first = true;
+  int nacc = 0;   // samples summed in tensor memory since the last flush
   const bool brow = tid < nblk;   // this thread stages state b = tid
+  double* dst = partial + (int64_t)blockIdx.x * nsave * nsel;
+  const int k = arow ? tid / nsel + 1 : 0, q = arow ? tid % nsel : 0;
+  // Every HC_FLUSH samples the MMA tile (columns 0 .. nb) is added, in
+  // IEEE FP32, into a second tile (columns tmem_cols / 2 ..) that holds the
+  // running sum, so that at most HC_FLUSH x 3 KP / 8 MMAs add into the MMA
+  // tile before it restarts (the tensor-core accumulation is not rounded to
+  // nearest at every add).
+  const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+  const uint32_t long_addr = lane_addr + (uint32_t)(tmem_cols / 2);
+  bool have_long = false;
+  auto flush = [&]() {
+    for (int c0 = 0; c0 < nb; c0 += 16) {
+      float v[16];
+      tmem_load(lane_addr + (uint32_t)c0, v);
+      if (have_long) {
+        float w[16];
+        tmem_load(long_addr + (uint32_t)c0, w);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] += w[j];
+      }
+      tmem_store(long_addr + (uint32_t)c0, v);
+    }
+    have_long = true;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  };
   // per-sample loads, coalesced: the selected rows (nR x M floats, from a
   // 4-byte-aligned start) and the states ((nblk + 1) x MP floats, 16-byte
   // aligned), each thread taking every HC_THREADS-th element / vector
@@ -613,6 +640,11 @@ __global__ void __launch_bounds__(HC_THREADS, 2)
       __syncthreads();
       if (s_abort) break;
       parity ^= 1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (nacc == HC_FLUSH) {
+        flush();
+        nacc = 0;
+      }
     }
     // selected rows: scratch (row-major, stride M), then each row's owner
     // splits it into the A planes
@@ -665,8 +697,9 @@ __global__ void __launch_bounds__(HC_THREADS, 2)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0)
-      issue_product(tmem, da_hi, da_lo, db_hi, db_lo, KP / 8, idesc, mbar, first ? 0u : 1u);
+      issue_product(tmem, da_hi, da_lo, db_hi, db_lo, KP / 8, idesc, mbar, nacc > 0 ? 1u : 0u);
     first = false;
+    ++nacc;
   }
   if (!first && !s_abort) {
     if (tid == 0 && !wait_parity(mbar, parity)) {
@@ -676,17 +709,15 @@ __global__ void __launch_bounds__(HC_THREADS, 2)
   }
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  double* dst = partial + (int64_t)blockIdx.x * nsave * nsel;
-  const int k = arow ? tid / nsel + 1 : 0, q = arow ? tid % nsel : 0;
   if (!s_abort) {
-    const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+    if (nacc > 0) flush();
     for (int c0 = 0; c0 < nb; c0 += 16) {
       float v[16];
-      if (first) {
+      if (have_long) {
+        tmem_load(long_addr + (uint32_t)c0, v);
+      } else {
 #pragma unroll
         for (int j = 0; j < 16; ++j) v[j] = 0.f;
-      } else {
-        tmem_load(lane_addr + (uint32_t)c0, v);
       }
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
