@@ -619,7 +619,7 @@ def our_arm(args):
     flops_dyn = events['dyn_flops']  # executed form (K-step blocked rows)
     dense_equiv = float(S) * (DYN_TIME - 1) * 49 * 49 * 8  # one 49x49 GEMV per step
     achieved = flops_dyn / (dyn_ms * 1e-3) / 1e12
-    traffic = ncu_traffic(os.path.join(ROOT, 'profiles', 'rk4_hblock_f32_fmo7.md'))
+    traffic = ncu_traffic(os.path.join(ROOT, 'profiles', 'rk4_real_two_pass_fmo7.md'))
     bb_flops = events.get('blockbuild_flops')
     base = None
     if world == 1 and not args.no_cpu_baseline:
@@ -642,8 +642,11 @@ def our_arm(args):
         'roofline': block_roofline(events, bb_flops, bb_ms, peak),
         'roofline_time_loop': {
             'kernel': '{} (ee populations, K={} step blocking, variant {})'.format(
-                'rk4_hblock_f32<49>' if events.get('dyn_variant') == 'real'
-                else 'rk4_block_f32<49>', events['dyn_block_k'], events.get('dyn_variant')),
+                'rk4_hchain_f32<49> + rk4_hcontract_tc<49> + hblock_reduce_kernel (two-pass '
+                'real loop: the state chain on the CUDA cores, the ensemble contraction as one '
+                'long-K tcgen05 GEMM; times are the whole library call)'
+                if events.get('dyn_variant') == 'real' else 'rk4_block_f32<49>',
+                events['dyn_block_k'], events.get('dyn_variant')),
             'dense_step_equivalent_tflops': dense_equiv / (dyn_ms * 1e-3) / 1e12,
             'bound': 'fp32_fma', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
             'frac': achieved / peak, 'flops_per_launch': flops_dyn, 'launch_ms': dyn_ms,

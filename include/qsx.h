@@ -181,7 +181,13 @@ int qsx_rk4_block_matrix_batched(const void* D, int m, int64_t batch,
  * shared); out_mean (double [nsteps + 1][nselect]) is the ensemble mean of
  * the selected coordinates at every step; workspace of
  * qsx_rk4_real_block_workspace_bytes() bytes.  group = samples per CTA
- * (0 = the library's choice, one).
+ * (0 = the library's choice, one).  With group <= 1, when the selected
+ * rows fit 128 and the block-steps 128, the loop runs in two passes: the
+ * state chain (one warp per sample) writes every block-start state into the
+ * workspace (batch x (nsteps / K + 1) x 4 ceil(m / 4) floats after the
+ * partial sums), then the ensemble contraction runs on the tensor cores
+ * (3xTF32 tcgen05 products summed in tensor memory); status also receives
+ * QSX_ERR_CUDA if a tensor-core completion wait times out.
  */
 int qsx_hermitian_real_form(const void* A, int n, int64_t batch, int precision,
                             void* R, void* stream);

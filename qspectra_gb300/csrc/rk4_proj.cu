@@ -171,13 +171,27 @@ __global__ void __launch_bounds__(256) rk4_projblock_f32(PbP p, int64_t ngroups,
     dst[e] = make_double2((double)lsum[e].x, (double)lsum[e].y);
 }
 
-__global__ void projblock_reduce_kernel(const double2* __restrict__ partial, int64_t nslots,
-                                        int64_t per, double scale, double2* __restrict__ out) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= per) return;
+// One CTA per 32 consecutive e: warp w adds slots w, w + 8, ... (each load a
+// coalesced row), then warp 0 adds the eight warp sums in warp order, so the
+// summation order is fixed and results are reproducible.
+__global__ void __launch_bounds__(256) projblock_reduce_kernel(const double2* __restrict__ partial,
+                                                               int64_t nslots, int64_t per,
+                                                               double scale,
+                                                               double2* __restrict__ out) {
+  __shared__ double2 red[8][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t e = (int64_t)blockIdx.x * 32 + lane;
   double2 acc = make_double2(0.0, 0.0);
-  for (int64_t sl = 0; sl < nslots; ++sl) acc = cadd(acc, partial[sl * per + e]);
-  out[e] = cscale(acc, scale);
+  if (e < per)
+    for (int64_t sl = warp; sl < nslots; sl += 8) acc = cadd(acc, partial[sl * per + e]);
+  red[warp][lane] = acc;
+  __syncthreads();
+  if (warp == 0 && e < per) {
+    double2 t = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t = cadd(t, red[w][lane]);
+    out[e] = cscale(t, scale);
+  }
 }
 
 struct PbPlan {
@@ -275,7 +289,7 @@ extern "C" int qsx_rk4_proj_block_mean(const void* matrix, int m, int64_t batch,
   }
   if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_proj_block_mean");
   QSX_LAUNCH_CHECK("qsx_rk4_proj_block_mean");
-  projblock_reduce_kernel<<<(unsigned)((per + 255) / 256), 256, 0, s>>>(
+  projblock_reduce_kernel<<<(unsigned)((per + 31) / 32), 256, 0, s>>>(
       (const double2*)workspace, pl.grid, per, 1.0 / (double)batch, (double2*)out_mean);
   QSX_LAUNCH_CHECK("qsx_rk4_proj_block_mean reduce");
   return QSX_OK;
