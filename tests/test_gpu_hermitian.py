@@ -88,6 +88,38 @@ def test_real_block_matrix_and_loop_match_numpy():
     assert rel_err(mean.cpu().numpy(), xs.mean(0)[:, sel]) < 2e-6
 
 
+@pytest.mark.parametrize('n,K,nsteps,sel,group', [
+    (4, 4, 24, [0, 5, 10, 15, 3], 0),     # two-pass: chain + tensor-core contraction
+    (4, 2, 300, [0, 5, 10, 15], 0),       # 150 block-steps: fused warp-specialised loop
+    (4, 4, 24, [0, 5, 10, 15, 3], 2),     # two samples per CTA: grouped loop
+    (7, 9, 999, list(range(0, 49, 8)), 0),  # the fmo7 shape, two-pass
+    (3, 3, 90, [0, 4, 8, 1], 0),          # m = 9, two-pass
+])
+def test_real_loop_paths_match_numpy(n, K, nsteps, sel, group):
+    """Every execution path of qsx_rk4_real_block_mean against numpy powers
+    of the same FP32 propagators."""
+    rng = np.random.RandomState(n + K)
+    B = 40
+    m = n * n
+    L = 0.02 * real_form_np(lindblad_maps(n, B, seed=n + 1), n)
+    P = np.array([np.eye(m) + Lb + Lb @ Lb / 2 for Lb in L])
+    D32 = torch.as_tensor(P - np.eye(m)).float().cuda()
+    mat = _native.rk4_block_matrix_real(D32, K, sel)
+    x0 = rng.randn(B, m)
+    mean, st = _native.rk4_real_block_mean(mat, torch.as_tensor(x0).cuda(), nsteps, sel, K,
+                                           group=group)
+    assert int(st.item()) == 0
+    Pd = (D32.cpu().numpy().astype(np.float64) + np.eye(m))
+    ref = np.zeros((nsteps + 1, len(sel)))
+    for b in range(B):
+        x = x0[b].copy()
+        for t in range(nsteps + 1):
+            ref[t] += x[sel]
+            x = Pd[b] @ x
+    ref /= B
+    assert rel_err(mean.cpu().numpy(), ref) < 2e-5
+
+
 @pytest.mark.parametrize('full_state', [False, True])
 def test_ensemble_populations_real_form_matches_complex_and_fp64(full_state):
     m, _ = fmo_build()
