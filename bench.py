@@ -61,6 +61,8 @@ def parse_args():
     p.add_argument('--no-third', action='store_true')
     p.add_argument('--no-adjoint', action='store_true')
     p.add_argument('--no-zofe', action='store_true')
+    p.add_argument('--no-graph', action='store_true',
+                   help='time the eager launches only (no CUDA graph capture)')
     p.add_argument('--zofe-samples', type=int, default=152)
     p.add_argument('--only', choices=['heom', 'third', 'adjoint', 'zofe'],
                    help='run one auxiliary workload alone and print its JSON')
@@ -566,12 +568,33 @@ def our_arm(args):
         X32, P32, status = work.run(off, 'fp32', events)
     e1.record()
     barrier()
+    eager_ms = e0.elapsed_time(e1) / args.steps
+    # the same step as one CUDA graph launch (the library's capture/replay),
+    # timed beside the eager steps; `value` is the eager timing (the GPU
+    # already runs behind the launches there), while the end-to-end calls
+    # below go through run_host, which replays the graph
+    graph_ok = (not args.no_graph) and work.capture(off, 'fp32')
+    ms = eager_ms
+    graph_ms = None
+    if graph_ok:
+        for _ in range(args.warmup):
+            work.replay()
+        barrier()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record()
+        for _ in range(args.steps):
+            Xg, Pg, status = work.replay()
+        g1.record()
+        barrier()
+        graph_ms = g0.elapsed_time(g1) / args.steps
+        graph_vs_eager = max(float((Xg - X32).abs().max() / X32.abs().max()),
+                             float((Pg - P32).abs().max() / P32.abs().max()))
     clocks = clocks_stop(clk) if rank == 0 else None
-    ms = e0.elapsed_time(e1) / args.steps
     if world > 1:
-        t = torch.tensor([ms], device='cuda')
+        t = torch.tensor([ms, graph_ms or 0.0], device='cuda')
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = float(t[0].item())
+        graph_ms = float(t[1].item()) if graph_ok else None
     if int(status.item()) & _native.QSX_ERR_NONFINITE:
         raise _native.IntegratorError('non-finite state in the timed run')
     value = world * 1000.0 / ms
@@ -635,6 +658,10 @@ def our_arm(args):
         'config': dict(CONFIG, parallelism='replicas (weak: each GPU runs its own '
                                            '16384-sample ensemble)' if world > 1 else 'single GPU'),
         'fp32_vs_fp64_rel_err': {'spectrum': err_spec, 'populations': err_pop},
+        'step_launch': ({'value': 'eager launches', 'e2e': 'captured CUDA graph (run_host)',
+                         'graph_ms_per_step': graph_ms,
+                         'graph_vs_eager_rel_diff': graph_vs_eager}
+                        if graph_ok else {'value': 'eager launches', 'e2e': 'eager launches'}),
         'fp64_ms_per_step': fp64_ms, 'speedup_fp32_vs_fp64': fp64_ms / ms,
         'e2e': {'value': world * 1000.0 / e2e_ms, 'unit': UNIT,
                 'h2d_bytes_per_step': int(off_host.numel() * 8),
@@ -651,7 +678,7 @@ def our_arm(args):
             'bound': 'fp32_fma', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
             'frac': achieved / peak, 'flops_per_launch': flops_dyn, 'launch_ms': dyn_ms,
             'traffic': traffic, 'hbm': hbm_view(traffic, dyn_ms)},
-        'gpu_launches': 13 * args.steps,
+        'gpu_launches': 12 * args.steps,
         'clocks': clocks,
     }
     if adj is not None:

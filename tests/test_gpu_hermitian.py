@@ -155,6 +155,27 @@ def test_workload_uses_real_form_and_matches_fp64():
     assert rel_err(X32.cpu().numpy(), X64.cpu().numpy()) < 1e-5
 
 
+def test_workload_graph_replay_matches_eager():
+    """One captured step replayed (device input, then pinned host input
+    through run_host) gives the eager step's results."""
+    from qspectra_gb300.simulate.ensemble import RedfieldEnsembleWorkload
+    m, _ = fmo_build()
+    psi = np.zeros(7)
+    psi[1] = 1.0
+    work = RedfieldEnsembleWorkload(m, 512.0, 1000.0, psi)
+    offs = torch.as_tensor(m.hamiltonian.disorder_offsets(192))
+    X, P, st = work.run(offs.cuda(), 'fp32')
+    X, P = X.cpu().numpy(), P.cpu().numpy()
+    assert work.capture(offs.cuda(), 'fp32')
+    Xg, Pg, stg = work.replay()
+    assert int(stg.item()) == 0
+    assert rel_err(Xg.cpu().numpy(), X) < 1e-12 and rel_err(Pg.cpu().numpy(), P) < 1e-12
+    other = torch.as_tensor(m.hamiltonian.disorder_offsets(192, start=500)).pin_memory()
+    Xh, Ph = work.run_host(other, 'fp32')
+    X2, P2, _ = work.run(other.cuda(), 'fp32')
+    assert rel_err(Xh, X2.cpu().numpy()) < 1e-12 and rel_err(Ph, P2.cpu().numpy()) < 1e-12
+
+
 def test_tensor_core_and_cuda_core_block_builds_agree_in_the_ensemble(monkeypatch):
     """The ensemble populations through the tcgen05 block build equal those
     through the CUDA-core FP32 build to FP32 rounding."""
