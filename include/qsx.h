@@ -27,7 +27,7 @@ enum {
   QSX_OK = 0,
   QSX_ERR_INVALID_ARG = 1, /* bad shape, size, subspace index or pointer */
   QSX_ERR_CUDA = 2,        /* a CUDA runtime call or launch failed */
-  QSX_ERR_UNSUPPORTED = 3, /* valid request this build does not implement */
+  QSX_ERR_UNSUPPORTED = 3, /* valid request the library does not implement */
   QSX_ERR_NONFINITE = 4    /* a NaN/Inf was detected in a state */
 };
 
