@@ -1,0 +1,65 @@
+"""Host-side logic of the ensemble drivers (no GPU): block-size choice for
+the real blocked loop, Hermitian block detection and the coordinate map."""
+import numpy as np
+
+from qspectra_gb300.simulate import ensemble as ens
+
+
+def tc_supported(m, K, nsel):
+    """The shapes the tensor-core block build takes: m <= 64, K = 2^J or
+    2^J + 1, and at most 64 selected rows entering its last row product."""
+    if m > 64 or K < 2 or K > 64:
+        return False
+    if K & (K - 1) and ((K - 1) & (K - 2) or K <= 2):
+        return False
+    b = 1
+    while 2 * b < K - 1:
+        b *= 2
+    return b * nsel <= 64
+
+
+def test_block_size_divides_the_steps_and_prefers_cheap_builds():
+    for nsteps in (999, 512, 300, 2047, 1023, 24):
+        K = ens.pick_block_k_real(nsteps, 49, 7)
+        Kt = ens.pick_block_k_real(nsteps, 49, 7,
+                                   tensor_core=lambda k: tc_supported(49, k, 7))
+        for k in (K, Kt):
+            assert k == 1 or nsteps % k == 0
+            assert 49 + 7 * (k - 1) <= 512
+    # the fmo7 population run: 999 steps, K = 9 either way (a tensor-core shape)
+    assert ens.pick_block_k_real(999, 49, 7) == 9
+    assert tc_supported(49, 9, 7)
+    # a cheaper build only makes tensor-core shapes more attractive: when the
+    # plain choice is one, so is the weighted choice (possibly a larger K)
+    for nsteps in (512, 360, 720, 1000):
+        K = ens.pick_block_k_real(nsteps, 49, 7)
+        Kt = ens.pick_block_k_real(nsteps, 49, 7, tensor_core=lambda k: tc_supported(49, k, 7))
+        if tc_supported(49, K, 7):
+            assert tc_supported(49, Kt, 7) and Kt >= K
+
+
+def test_no_block_size_when_no_divisor_fits():
+    assert ens.pick_block_k_real(997, 49, 7) == 1        # prime, above the largest K
+
+
+def test_hermitian_block_detection():
+    n = 8   # ground + 7 sites
+    ee = np.array([a + n * b for b in range(1, n) for a in range(1, n)])
+    assert ens.hermitian_block_size(ee, n) == 7
+    eg = np.array([a + n * 0 for a in range(1, n)])
+    assert ens.hermitian_block_size(eg, n) is None
+
+
+def test_hermitian_coordinates_round_trip():
+    rng = np.random.RandomState(0)
+    nb = 5
+    A = rng.randn(nb, nb) + 1j * rng.randn(nb, nb)
+    rho = A + A.conj().T
+    y = rho.reshape(-1, order='F')
+    x = ens.hermitian_coordinates(y, nb)
+    assert x.dtype.kind == 'f' and x.shape == (nb * nb,)
+    # populations are coordinates
+    for a in range(nb):
+        assert x[a + nb * a] == rho[a, a].real
+    back = ens.from_hermitian_coordinates(x, nb)
+    assert np.allclose(back, y, atol=1e-14)
