@@ -66,3 +66,24 @@ def test_zofe_args_layout_matches_library(lib):
     assert lib.qsx_zofe_rk4(ctypes.byref(a), None) == 1
     assert b'bad sizes' in lib.qsx_last_error_string()
 
+
+
+def test_tensor_core_block_shapes(lib):
+    """The tcgen05 block build takes m <= 64, K = 2^J or 2^J + 1, and at most
+    64 selected rows entering its last row product (host logic, no GPU)."""
+    def expected(m, K, nsel):
+        if m < 1 or m > 64 or K < 2 or K > 64 or nsel < 1 or nsel > m:
+            return 0
+        pow2 = K & (K - 1) == 0
+        pow2p1 = K > 2 and (K - 1) & (K - 2) == 0
+        if not (pow2 or pow2p1):
+            return 0
+        b = 1
+        while 2 * b < K - 1:
+            b *= 2
+        return int(b * nsel <= 64)
+    for m in (9, 16, 25, 36, 49, 64, 65):
+        for K in (1, 2, 3, 4, 5, 6, 7, 8, 9, 16, 17, 27, 32, 33, 64, 65):
+            for nsel in (1, 4, 7, 8, 16, 49):
+                assert lib.qsx_rk4_block_matrix_real_tc_supported(m, K, nsel) == \
+                    expected(m, K, nsel), (m, K, nsel)
