@@ -171,6 +171,84 @@ __global__ void __launch_bounds__(256) rk4_projblock_f32(PbP p, int64_t ngroups,
     dst[e] = make_double2((double)lsum[e].x, (double)lsum[e].y);
 }
 
+// Warp-per-sample form (the default when the M + P K rows fit one warp):
+// lane l holds row l, the state goes through a two-slot ring in shared
+// memory with a __syncwarp per block-step and no CTA barrier, and each warp
+// keeps its own partial sums [nsave][P] in shared memory, every (step,
+// projection) owned by one lane.  At the end the warps' sums are added in
+// warp order into the CTA's slice, so results are reproducible.
+constexpr int PW_WARPS = 4;
+
+template <int M>
+__global__ void __launch_bounds__(32 * PW_WARPS) rk4_projblock_w_f32(PbP p, int K) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int P = p.P, RT = M + P * K;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float2* ybuf = reinterpret_cast<float2*>(smraw) + w * 16;          // [2][8] per warp
+  float2* lsum = reinterpret_cast<float2*>(smraw) + PW_WARPS * 16 +  // [nsave][P] per warp
+                 (size_t)w * p.nsave * P;
+  const bool main_row = lane < M, act = lane < RT;
+  const int kx = main_row ? 0 : (lane - M) / P, px = main_row ? 0 : (lane - M) % P;
+  for (int e = lane; e < p.nsave * P; e += 32) lsum[e] = cmk(0.f, 0.f);
+  if (lane < 16) ybuf[lane] = cmk(0.f, 0.f);
+  __syncwarp();
+  const int nblk = p.nsteps / K;
+  for (int64_t s = (int64_t)blockIdx.x * PW_WARPS + w; s < p.batch;
+       s += (int64_t)gridDim.x * PW_WARPS) {
+    float2 row[M];
+    const float2* dm = p.matrix + (s * RT + (act ? lane : 0)) * (int64_t)M;
+#pragma unroll
+    for (int j = 0; j < M; ++j) row[j] = act ? dm[j] : cmk(0.f, 0.f);
+    float yhx = 0.f, yhy = 0.f, ylx = 0.f, yly = 0.f;
+    if (main_row) {
+      const double2 v = p.y0[s * p.y0_stride + lane];
+      yhx = (float)v.x;
+      yhy = (float)v.y;
+      ylx = (float)(v.x - (double)yhx);
+      yly = (float)(v.y - (double)yhy);
+      ybuf[lane] = cmk(yhx, yhy);
+    }
+    __syncwarp();
+    for (int bs = 0; bs <= nblk; ++bs) {
+      const float2* cur = ybuf + (bs & 1) * 8;
+      const bool last = bs == nblk;  // only the step-nsteps signal remains
+      float2 a0 = cmk(0.f, 0.f), a1 = a0;
+#pragma unroll
+      for (int j = 0; j < M; j += 2) {
+        cfma(a0, row[j], cur[j]);
+        if (j + 1 < M) cfma(a1, row[j + 1], cur[j + 1]);
+      }
+      const float sx = a0.x + a1.x, sy = a0.y + a1.y;
+      if (main_row) {
+        if (!last) {
+          dd_add(yhx, ylx, sx);
+          dd_add(yhy, yly, sy);
+          ybuf[((bs + 1) & 1) * 8 + lane] = cmk(yhx, yhy);
+        }
+      } else if (act && (!last || kx == 0)) {
+        float2* l = lsum + ((int64_t)bs * K + kx) * P + px;
+        *l = cadd2(*l, cmk(sx, sy));
+      }
+      __syncwarp();
+    }
+    if (main_row && p.status && !(isfinite(yhx) && isfinite(yhy)))
+      atomicOr(p.status, QSX_ERR_NONFINITE);
+  }
+  __syncthreads();
+  const float2* all = reinterpret_cast<const float2*>(smraw) + PW_WARPS * 16;
+  double2* dst = p.partial + (int64_t)blockIdx.x * p.nsave * P;
+  for (int e = threadIdx.x; e < p.nsave * P; e += blockDim.x) {
+    double x = 0.0, y = 0.0;
+#pragma unroll
+    for (int ww = 0; ww < PW_WARPS; ++ww) {
+      const float2 v = all[(size_t)ww * p.nsave * P + e];
+      x += (double)v.x;
+      y += (double)v.y;
+    }
+    dst[e] = make_double2(x, y);
+  }
+}
+
 // One CTA per 32 consecutive e: warp w adds slots w, w + 8, ... (each load a
 // coalesced row), then warp 0 adds the eight warp sums in warp order, so the
 // summation order is fixed and results are reproducible.
@@ -195,7 +273,7 @@ __global__ void __launch_bounds__(256) projblock_reduce_kernel(const double2* __
 }
 
 struct PbPlan {
-  int G, threads;
+  int G, threads, warp_form;
   int64_t ngroups, grid;
   size_t smem;
 };
@@ -203,6 +281,37 @@ struct PbPlan {
 static int projblock_plan(int m, int64_t batch, int K, int nsteps, int P, PbPlan* pl) {
   const int RT = m + P * K;
   QSX_CHECK_ARG(RT <= 256, "qsx_rk4_proj_block_mean: %d rows per sample exceed 256", RT);
+  pl->warp_form = 0;
+  {
+    const size_t smem = ((size_t)PW_WARPS * 16 + (size_t)PW_WARPS * (nsteps + 1) * P) *
+                        sizeof(float2);
+    if (RT <= 32 && smem <= 110 * 1024) {
+      int dev = 0, sms = 0, occ = 0;
+      cudaError_t e = cudaGetDevice(&dev);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      switch (m) {
+#define C(MM)                                                                               \
+  case MM:                                                                                  \
+    if (e == cudaSuccess)                                                                   \
+      e = cudaFuncSetAttribute(rk4_projblock_w_f32<MM>,                                     \
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+    if (e == cudaSuccess)                                                                   \
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, rk4_projblock_w_f32<MM>,      \
+                                                        32 * PW_WARPS, smem);               \
+    break;
+        C(1) C(2) C(3) C(4) C(5) C(6) C(7) C(8)
+#undef C
+      }
+      if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_proj_block_mean plan");
+      pl->warp_form = 1;
+      pl->G = PW_WARPS;
+      pl->threads = 32 * PW_WARPS;
+      pl->smem = smem;
+      pl->ngroups = (batch + PW_WARPS - 1) / PW_WARPS;
+      pl->grid = std::max<int64_t>(1, std::min<int64_t>(pl->ngroups, (int64_t)sms * std::max(occ, 1)));
+      return QSX_OK;
+    }
+  }
   pl->G = std::max(1, 256 / RT);
   pl->threads = ((pl->G * RT + 31) / 32) * 32;
   pl->smem = ((size_t)2 * pl->G * m + 2 * (size_t)K * pl->G * P + (size_t)(nsteps + 1) * P) *
@@ -275,6 +384,21 @@ extern "C" int qsx_rk4_proj_block_mean(const void* matrix, int m, int64_t batch,
   p.status = status;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaSuccess;
+  if (pl.warp_form) {
+    switch (m) {
+#define C(MM)                                                                               \
+  case MM:                                                                                  \
+    rk4_projblock_w_f32<MM><<<(unsigned)pl.grid, pl.threads, pl.smem, s>>>(p, K);            \
+    break;
+      C(1) C(2) C(3) C(4) C(5) C(6) C(7) C(8)
+#undef C
+    }
+    QSX_LAUNCH_CHECK("qsx_rk4_proj_block_mean");
+    projblock_reduce_kernel<<<(unsigned)((per + 31) / 32), 256, 0, s>>>(
+        (const double2*)workspace, pl.grid, per, 1.0 / (double)batch, (double2*)out_mean);
+    QSX_LAUNCH_CHECK("qsx_rk4_proj_block_mean reduce");
+    return QSX_OK;
+  }
   switch (m) {
 #define C(MM)                                                                             \
   case MM:                                                                                \
