@@ -19,71 +19,84 @@
 namespace qsx {
 
 // ---------------------------------------------------------------- build
-// One CTA per sample: P = I + D (complex64, M x M) in shared memory, the
-// projection rows W_k = W_{k-1} P and D_K by binary powering with
-// (I + X)(I + Y) - I = X + Y + X Y.
-__global__ void __launch_bounds__(64)
-    proj_block_build_kernel(const float2* __restrict__ D, int M, int K,
-                            const double2* __restrict__ proj, int P, float2* __restrict__ out) {
-  __shared__ float2 sP[8 * 8], sX[8 * 8], sY[8 * 8], sZ[8 * 8], sW[2][8 * 8];
-  const int64_t b = blockIdx.x;
-  const int mm = M * M, rows = M + P * K, tid = threadIdx.x;
+// Per sample: P = I + D (complex64, M x M) in shared memory, the projection
+// rows W_k = W_{k-1} P and D_K by binary powering with
+// (I + X)(I + Y) - I = X + Y + X Y.  One warp per sample (eight samples per
+// CTA): each warp works in its own shared-memory slices and synchronises
+// with __syncwarp, so the ~K + 2 log2 K dependent small products need no CTA
+// barrier.
+constexpr int PBW_WARPS = 8;
+
+__global__ void __launch_bounds__(32 * PBW_WARPS)
+    proj_block_build_w_kernel(const float2* __restrict__ D, int M, int K,
+                              const double2* __restrict__ proj, int P, int64_t batch,
+                              float2* __restrict__ out) {
+  __shared__ float2 sm[PBW_WARPS][6][8 * 8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t b = (int64_t)blockIdx.x * PBW_WARPS + w;
+  if (b >= batch) return;   // whole warps only: no CTA barrier follows
+  float2* sP = sm[w][0];
+  float2* sX = sm[w][1];
+  float2* sY = sm[w][2];
+  float2* sZ = sm[w][3];
+  float2* sW[2] = {sm[w][4], sm[w][5]};
+  const int mm = M * M, rows = M + P * K;
   const float2* d = D + b * mm;
   float2* o = out + b * (int64_t)rows * M;
-  for (int e = tid; e < mm; e += blockDim.x) {
+  for (int e = lane; e < mm; e += 32) {
     sX[e] = d[e];
     sP[e] = cmk(d[e].x + ((e / M) == (e % M) ? 1.f : 0.f), d[e].y);
   }
-  for (int e = tid; e < P * M; e += blockDim.x) {
+  for (int e = lane; e < P * M; e += 32) {
     const double2 v = proj[e];
     sW[0][e] = cmk((float)v.x, (float)v.y);
     o[(int64_t)M * M + e] = sW[0][e];  // k = 0
   }
-  __syncthreads();
+  __syncwarp();
   for (int k = 1; k < K; ++k) {
     const float2* wprev = sW[(k - 1) & 1];
     float2* wnext = sW[k & 1];
-    for (int e = tid; e < P * M; e += blockDim.x) {
+    for (int e = lane; e < P * M; e += 32) {
       const int p = e / M, c = e % M;
       float2 acc = cmk(0.f, 0.f);
       for (int j = 0; j < M; ++j) cfma(acc, wprev[p * M + j], sP[j * M + c]);
       wnext[e] = acc;
       o[(int64_t)(M + k * P) * M + e] = acc;
     }
-    __syncthreads();
+    __syncwarp();
   }
   // D_K: base = D_{2^j} in sX, result accumulated in sY
   bool have = false;
   for (int kk = K; kk > 0; kk >>= 1) {
     if (kk & 1) {
       if (!have) {
-        for (int e = tid; e < mm; e += blockDim.x) sY[e] = sX[e];
+        for (int e = lane; e < mm; e += 32) sY[e] = sX[e];
         have = true;
       } else {
-        for (int e = tid; e < mm; e += blockDim.x) {
+        for (int e = lane; e < mm; e += 32) {
           const int r = e / M, c = e % M;
           float2 acc = cadd2(sY[e], sX[e]);
           for (int j = 0; j < M; ++j) cfma(acc, sY[r * M + j], sX[j * M + c]);
           sZ[e] = acc;
         }
-        __syncthreads();
-        for (int e = tid; e < mm; e += blockDim.x) sY[e] = sZ[e];
+        __syncwarp();
+        for (int e = lane; e < mm; e += 32) sY[e] = sZ[e];
       }
-      __syncthreads();
+      __syncwarp();
     }
     if (kk > 1) {
-      for (int e = tid; e < mm; e += blockDim.x) {
+      for (int e = lane; e < mm; e += 32) {
         const int r = e / M, c = e % M;
         float2 acc = cadd2(sX[e], sX[e]);
         for (int j = 0; j < M; ++j) cfma(acc, sX[r * M + j], sX[j * M + c]);
         sZ[e] = acc;
       }
-      __syncthreads();
-      for (int e = tid; e < mm; e += blockDim.x) sX[e] = sZ[e];
-      __syncthreads();
+      __syncwarp();
+      for (int e = lane; e < mm; e += 32) sX[e] = sZ[e];
+      __syncwarp();
     }
   }
-  for (int e = tid; e < mm; e += blockDim.x) o[e] = sY[e];
+  for (int e = lane; e < mm; e += 32) o[e] = sY[e];
 }
 
 // ----------------------------------------------------------------- loop
@@ -339,8 +352,10 @@ extern "C" int qsx_rk4_proj_block_build(const void* D, int m, int64_t batch, int
                 "qsx_rk4_proj_block_build: bad sizes (m=%d, K=%d, nproj=%d)", m, K, nproj);
   if (batch == 0) return QSX_OK;
   QSX_CHECK_ARG(D && proj && out, "qsx_rk4_proj_block_build: null pointer");
-  proj_block_build_kernel<<<(unsigned)batch, 64, 0, (cudaStream_t)stream>>>(
-      (const float2*)D, m, K, (const double2*)proj, nproj, (float2*)out);
+  proj_block_build_w_kernel<<<(unsigned)((batch + PBW_WARPS - 1) / PBW_WARPS), 32 * PBW_WARPS, 0,
+                              (cudaStream_t)stream>>>((const float2*)D, m, K,
+                                                      (const double2*)proj, nproj, batch,
+                                                      (float2*)out);
   QSX_LAUNCH_CHECK("qsx_rk4_proj_block_build");
   return QSX_OK;
 }
