@@ -704,6 +704,103 @@ __global__ void __launch_bounds__(256, 2)
   rk4_polynomial<T>(sL, sX, sY, m, h, D + b * (int64_t)m * m);
 }
 
+// The same propagator for small blocks (m <= 8, n <= 8), one warp per
+// sample and eight samples per CTA: the warp stages its operators in shared
+// memory (coalesced, converted once), forms each generator entry with its
+// B[s] sums on the fly, and evaluates the RK4 polynomial with __syncwarp
+// between the dependent products, no CTA barrier.
+constexpr int RPW_WARPS = 8;
+
+template <typename T>
+struct RpwSlice {
+  typename cplx<T>::type gm[9 * 64];   // G, M_i (i < n_sites <= 8) on n^2 <= 64 entries
+  typename cplx<T>::type hs[64];       // (0, uc H)
+  typename cplx<T>::type a[64], a2[64], c[64];
+  T occ[8 * 8];
+  int idx[8];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(32 * RPW_WARPS)
+    redfield_propagator_w_kernel(const double* __restrict__ H, int64_t H_stride,
+                                 const double2* __restrict__ G, const double2* __restrict__ Mo,
+                                 const double* __restrict__ occ, int n, int n_sites, double uc,
+                                 const int* __restrict__ idx, int m, int transpose, double h,
+                                 int64_t batch, typename cplx<T>::type* D) {
+  using C = typename cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t b = (int64_t)blockIdx.x * RPW_WARPS + w;
+  if (b >= batch) return;   // whole warps only: no CTA barrier follows
+  RpwSlice<T>& S = reinterpret_cast<RpwSlice<T>*>(smraw)[w];
+  const int nn = n * n, mm = m * m;
+  const double2* g = G + b * nn;
+  const double2* mo = Mo + b * (int64_t)n_sites * nn;
+  for (int e = lane; e < (1 + n_sites) * nn; e += 32) {
+    const double2 v = e < nn ? g[e] : mo[e - nn];
+    S.gm[e] = cmk((T)v.x, (T)v.y);
+  }
+  for (int e = lane; e < n_sites * n; e += 32) S.occ[e] = (T)occ[e];
+  for (int e = lane; e < nn; e += 32) S.hs[e] = cmk((T)0, (T)(uc * H[b * H_stride + e]));
+  if (lane < m) {
+    const int v = idx[lane];
+    S.idx[lane] = (v >= 0 && v < nn) ? v : -1;
+  }
+  __syncwarp();
+  // B[s]_xy = G_xy - sum_i occ_is M_i,xy, in the CTA kernel's order
+  auto bval = [&](int st, int xy) -> C {
+    C v = S.gm[xy];
+    for (int i = 0; i < n_sites; ++i) {
+      const T o = S.occ[i * n + st];
+      if (o != (T)0) {
+        const C mv = S.gm[(1 + i) * nn + xy];
+        v = cmk(v.x - o * mv.x, v.y - o * mv.y);
+      }
+    }
+    return v;
+  };
+  const T ht = (T)h;
+  for (int e = lane; e < mm; e += 32) {
+    int r = e / m, cc = e % m;
+    if (transpose) { const int t = r; r = cc; cc = t; }
+    const int ir = S.idx[r], ic = S.idx[cc];
+    C v = cmk((T)0, (T)0);
+    if (ir < 0 || ic < 0) {
+      v = cmk((T)nan(""), (T)nan(""));
+    } else {
+      const int a = ir % n, bb = ir / n, c = ic % n, d = ic / n;
+      if (bb == d) {  // -B[b]_ac - i uc H_ac
+        const C x = bval(bb, a * n + c), hh = S.hs[a * n + c];
+        v = cmk(v.x - x.x - hh.x, v.y - x.y - hh.y);
+      }
+      if (a == c) {  // -conj(B[a]_bd) + i uc H_db
+        const C x = bval(a, bb * n + d), hh = S.hs[d * n + bb];
+        v = cmk(v.x - x.x + hh.x, v.y + x.y + hh.y);
+      }
+    }
+    S.a[e] = cmk(ht * v.x, ht * v.y);
+  }
+  __syncwarp();
+  for (int e = lane; e < mm; e += 32) {  // A2 = A A
+    const int r = e / m, cc = e % m;
+    C acc = cmk((T)0, (T)0);
+    for (int j = 0; j < m; ++j) cfma(acc, S.a[r * m + j], S.a[j * m + cc]);
+    S.a2[e] = acc;
+  }
+  __syncwarp();
+  const T c6 = (T)(1.0 / 6.0), c24 = (T)(1.0 / 24.0), c2 = (T)0.5;
+  for (int e = lane; e < mm; e += 32)
+    S.c[e] = cmk(c6 * S.a[e].x + c24 * S.a2[e].x, c6 * S.a[e].y + c24 * S.a2[e].y);
+  __syncwarp();
+  C* Dr = D + b * (int64_t)mm;
+  for (int e = lane; e < mm; e += 32) {  // D = A + A2 / 2 + A2 (A / 6 + A2 / 24)
+    const int r = e / m, cc = e % m;
+    C z = cmk((T)0, (T)0);
+    for (int j = 0; j < m; ++j) cfma(z, S.a2[r * m + j], S.c[j * m + cc]);
+    Dr[e] = cmk(S.a[e].x + c2 * S.a2[e].x + z.x, S.a[e].y + c2 * S.a2[e].y + z.y);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256)
     propagator_kernel(const double2* __restrict__ L, int m, double h,
@@ -1334,6 +1431,29 @@ int qsx_redfield_propagator_batched(const double* H, int64_t H_stride, const dou
   }
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e;
+  if (m <= 8 && n <= 8 && n_sites <= 8) {
+    // small blocks: one warp per sample
+    const unsigned grid = (unsigned)((batch + RPW_WARPS - 1) / RPW_WARPS);
+    if (precision == QSX_FP32) {
+      const size_t sm = RPW_WARPS * sizeof(RpwSlice<float>);
+      e = cudaFuncSetAttribute(redfield_propagator_w_kernel<float>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_batched");
+      redfield_propagator_w_kernel<float><<<grid, 32 * RPW_WARPS, sm, s>>>(
+          H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, unit_convert, idx,
+          m, transpose, h, batch, (float2*)D);
+    } else {
+      const size_t sm = RPW_WARPS * sizeof(RpwSlice<double>);
+      e = cudaFuncSetAttribute(redfield_propagator_w_kernel<double>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_batched");
+      redfield_propagator_w_kernel<double><<<grid, 32 * RPW_WARPS, sm, s>>>(
+          H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, unit_convert, idx,
+          m, transpose, h, batch, (double2*)D);
+    }
+    QSX_LAUNCH_CHECK("qsx_redfield_propagator_batched");
+    return QSX_OK;
+  }
   if (precision == QSX_FP32) {
     e = cudaFuncSetAttribute(redfield_propagator_kernel<float>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
