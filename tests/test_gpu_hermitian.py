@@ -200,7 +200,10 @@ def test_tensor_core_and_cuda_core_block_builds_agree_in_the_ensemble(monkeypatc
     assert rel_err(tc.cpu().numpy(), cc.cpu().numpy()) < 2e-6
 
 
-@pytest.mark.parametrize('m,P,nsteps', [(7, 1, 2047), (3, 2, 120), (8, 1, 96), (5, 3, 64)])
+# (7, 1, 2047) and (4, 3, 679) fit one warp per sample (m + P K <= 32), the
+# others take the CTA-wide loop
+@pytest.mark.parametrize('m,P,nsteps', [(7, 1, 2047), (4, 3, 679), (3, 2, 120), (8, 1, 96),
+                                        (5, 3, 64)])
 def test_projection_blocked_loop_matches_stepwise(m, P, nsteps):
     """The K-step projection loop (qsx_rk4_proj_block_*) against the
     step-by-step batched loop and an FP64 NumPy recurrence."""
