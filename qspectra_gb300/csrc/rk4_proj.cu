@@ -8,10 +8,12 @@
 //   row  M + k P + p     W_{k,p} = proj_p P^k     (k = 0..K-1)
 // so one pass over the rows at step n yields the signals at steps
 // n .. n + K - 1 and the state at n + K: per K steps (M + P K) M complex
-// multiply-adds instead of K (M^2 + P M).  One thread per row, G samples
-// per CTA, persistent grid, split-word FP32 state; the ensemble mean is
-// accumulated per CTA in shared memory (each (step, projection) by one
-// thread in program order) and the CTA slices are summed in a fixed order.
+// multiply-adds instead of K (M^2 + P M).  One thread per row and a
+// split-word FP32 state: one sample per warp when the M + P K rows fit 32
+// (rk4_projblock_w_f32), else G samples per CTA (rk4_projblock_f32).  The
+// ensemble mean is accumulated in shared memory, each (step, projection) by
+// one thread in program order, and the CTA slices are summed in a fixed
+// order.
 #include <algorithm>
 
 #include "qsx_common.cuh"

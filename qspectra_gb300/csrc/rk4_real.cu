@@ -6,16 +6,22 @@
 // (a <= b), Im rho_ba (a > b): every step costs m^2 real multiply-adds
 // instead of m^2 complex ones (4 m^2).  The populations rho_aa are
 // coordinates themselves.  This loop is the real counterpart of the complex
-// blocked kernels in rk4.cu, fed by qsx_rk4_block_matrix_real_batched:
-// rows 0..m-1 of each sample's matrix advance K steps (P_r^K - I), the
-// following nsel (K - 1) rows give the selected coordinates at the K - 1
-// intermediate steps.  One thread per matrix row (the row in registers),
-// G samples per CTA, a persistent grid; the state is split-word FP32.  The
-// ensemble mean of the selected coordinates is accumulated per CTA, each
-// (step, coordinate) always by the same thread in program order: in FP32 in
-// shared memory when [nsteps + 1][nsel] fits there (written out once at the
-// end), else by FP64 atomics into the CTA's global slice.  The CTA slices
-// are summed in a fixed order, so results are reproducible.
+// blocked kernels in rk4.cu, fed by qsx_rk4_block_matrix_real_batched or
+// qsx_rk4_block_matrix_real_tc: rows 0..m-1 of each sample's matrix advance
+// K steps (P_r^K - I), the following nsel (K - 1) rows give the selected
+// coordinates at the K - 1 intermediate steps.  The state is split-word
+// FP32 throughout.  Three forms, chosen by the plan:
+//   - two passes (the default when the selected rows and block-steps fit
+//     128): rk4_hchain_f32 runs the state chain one warp per sample and
+//     stores every block-start state; rk4_hcontract_tc then forms the
+//     selected coordinates of all samples as one long-K tcgen05 GEMM summed
+//     in tensor memory;
+//   - rk4_hblock_ws_f32: one chain warp and trailing selected-row warps per
+//     sample in one kernel;
+//   - rk4_hblock_f32: one thread per row, G samples per CTA (any group size).
+// Each form keeps per-CTA partial sums of the selected coordinates, every
+// (step, coordinate) added by one owner in program order, and the CTA
+// slices are summed in a fixed order, so results are reproducible.
 #include <algorithm>
 
 #include "qsx_common.cuh"
