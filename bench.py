@@ -176,15 +176,30 @@ def reference_arm(args):
 
 
 # -------------------------------------------------------------- GPU arm
-def fma_peak_tflops(torch, native):
+def fma_peak_tflops(torch, native, precision=None):
+    """Measured CUDA-core FMA peak (TFLOP/s) from the benchmark's own probe
+    library (libqsx_probe.so, built beside libqsx.so)."""
+    import ctypes
+    from qspectra_gb300 import build as qbuild
+    if precision is None:
+        precision = native.QSX_FP32
+    probe = ctypes.CDLL(qbuild.PROBE_LIB)
+    probe.qsx_probe_fma.restype = ctypes.c_int
+    probe.qsx_probe_fma.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_void_p]
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    blocks, threads, iters = sms * 8, 256, 4000
-    out = torch.empty(blocks * threads, dtype=torch.float32, device='cuda')
+    fp32 = precision == native.QSX_FP32
+    blocks, threads, iters = sms * 8, 256, (4000 if fp32 else 250)
+    out = torch.empty(blocks * threads, dtype=torch.float32 if fp32 else torch.float64,
+                      device='cuda')
     best = 0.0
     for _ in range(3):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        native.probe_fma(native.QSX_FP32, blocks, threads, iters, out)
+        st = probe.qsx_probe_fma(precision, blocks, threads, iters, out.data_ptr(),
+                                 torch.cuda.current_stream().cuda_stream)
+        if st != 0:
+            raise RuntimeError('qsx_probe_fma failed with status {}'.format(st))
         e1.record()
         torch.cuda.synchronize()
         flops = 2.0 * blocks * threads * iters * 16 * 8
@@ -489,7 +504,7 @@ def block_roofline(events, bb_flops, bb_ms, fma_peak):
                 'executed_flops_per_launch': executed,
                 'fp32_fma_view': {'peak': fma_peak, 'frac': bb_achieved / fma_peak
                                   if bb_achieved else None,
-                                  'peak_source': 'measured live by qsx_probe_fma'},
+                                  'peak_source': 'measured live by the FMA probe (libqsx_probe.so)'},
                 'flops_per_launch': bb_flops, 'launch_ms': bb_ms,
                 'traffic': traffic, 'hbm': hbm_view(traffic, bb_ms)}
     traffic = ncu_traffic(os.path.join(ROOT, 'profiles', 'block_matrix_real_fmo7.md'))
@@ -497,7 +512,7 @@ def block_roofline(events, bb_flops, bb_ms, fma_peak):
                       'K={} step blocked matrices, 4x4-tiled FP32 products)'.format(K),
             'bound': 'fp32_fma', 'achieved': bb_achieved, 'peak': fma_peak, 'unit': 'TFLOP/s',
             'frac': bb_achieved / fma_peak if bb_achieved else None,
-            'peak_source': 'measured live by qsx_probe_fma (FP32 FMA); '
+            'peak_source': 'measured live by the FMA probe (libqsx_probe.so, FP32 FMA); '
                            'MEASURED_PEAKS.json has no CUDA-core figure',
             'flops_per_launch': bb_flops, 'launch_ms': bb_ms,
             'traffic': traffic, 'hbm': hbm_view(traffic, bb_ms)}

@@ -278,7 +278,10 @@ typedef struct {
  * matrix-vector pass advances K RK4 steps while still producing the selected
  * components at every step (same iterates y_{n+1} = P y_n, regrouped).
  * Needs QSX_FP32, form 0, nselect outputs only, save_every 1, no out_state,
- * nsteps % K == 0 and m in {9, 16, 25, 36, 49, 64}. */
+ * nsteps % K == 0 and m in {9, 16, 25, 36, 49, 64}.  The select entries must
+ * be distinct and in [0, m): the blocked kernels check the table on the
+ * device and, for a bad one, set QSX_ERR_INVALID_ARG in status and write
+ * nothing. */
 
 /* sizeof(qsx_rk4_args) as compiled into the library, for FFI bindings to
  * check their struct declaration against. */
@@ -299,8 +302,10 @@ int qsx_rk4_batched(const qsx_rk4_args* args, void* stream);
  * 16 MiB are rejected with QSX_ERR_INVALID_ARG; larger batches run with fewer
  * persistent CTAs so their partial sums fit.  The first call on each device
  * looks up the array's address (cudaGetSymbolAddress) with that device
- * current, so make it before any stream capture.  Every call shares the
- * array and clears the part it uses: calls that overlap on the GPU race.
+ * current, so make it before any stream capture; calls outside a capture
+ * look it up again, so the address stays right after a device reset.
+ * Every call shares the array and clears the part it uses: calls that
+ * overlap on the GPU race.
  */
 int qsx_rk4_block_mean_noalloc(const qsx_rk4_args* args, void* stream);
 
@@ -565,14 +570,6 @@ int qsx_csr_map_batched(const double* in, int64_t n_in, int64_t batch,
 int qsx_dft_batched(const double* x, int nt, int64_t batch, double t0,
                     double dt, const double* freqs, int nf, double rw_freq,
                     double unit_convert, int sign, double* X, void* stream);
-
-/*
- * Peak-throughput probes (no reference counterpart): each thread runs
- * `iters` iterations of 8 independent FMA chains (FP32 or FP64) and writes
- * one value to out[thread].  Used to measure the CUDA-core FMA roofline.
- */
-int qsx_probe_fma(int precision, int64_t blocks, int threads, int iters,
-                  void* out, void* stream);
 
 #ifdef __cplusplus
 }

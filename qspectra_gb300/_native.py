@@ -15,6 +15,9 @@ LIB_PATH = os.path.join(_HERE, '_lib', 'libqsx.so')
 
 QSX_FP64 = 0
 QSX_FP32 = 1
+# status-word bits set by the kernels (the QSX_ERR_* codes of include/qsx.h)
+QSX_ERR_INVALID_ARG = 1
+QSX_ERR_CUDA = 2
 QSX_ERR_NONFINITE = 4
 
 _c_int = ctypes.c_int
@@ -141,7 +144,6 @@ _PROTOS = {
     'qsx_heom_rk4': (_c_int, [ctypes.POINTER(HeomArgs), _c_vp]),
     'qsx_dft_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
                                  _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
-    'qsx_probe_fma': (_c_int, [_c_int, _c_i64, _c_int, _c_int, _c_vp, _c_vp]),
     'qsx_fblock_tensor': (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_vp, _c_i64, _c_dbl,
                                    _c_dbl, _c_dbl, _c_int, _c_int, _c_dbl, _c_int,
                                    _c_vp, _c_vp]),
@@ -667,7 +669,7 @@ def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
         st = int(status.item())
         if st & QSX_ERR_NONFINITE:
             raise IntegratorError('non-finite state during RK4 integration')
-        if st & 1:
+        if st & QSX_ERR_INVALID_ARG:
             raise QsxError('qsx_rk4_batched: index table out of range')
     out['status'] = status
     return out
@@ -688,11 +690,6 @@ def dft(x, t0, dt, freqs, rw_freq=0.0, unit_convert=1.0, sign=1):
                                   rw_freq, unit_convert, sign, _p(X), _stream()),
            'qsx_dft_batched')
     return X[0] if squeeze else X
-
-
-def probe_fma(precision, blocks, threads, iters, out):
-    _check(load().qsx_probe_fma(precision, blocks, threads, iters, _p(out),
-                                _stream()), 'qsx_probe_fma')
 
 
 def _heom_args(tables, Hx, Hy, unit_convert, batch, precision=QSX_FP64):

@@ -15,6 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 OUT_DIR = os.path.join(HERE, '_lib')
 LIB = os.path.join(OUT_DIR, 'libqsx.so')
+# the FMA-throughput probe the benchmark uses for its CUDA-core roofline
+# denominators: a separate library, not part of libqsx.so or include/qsx.h
+PROBE_SRC = os.path.join(CSRC, 'probe', 'fma_probe.cu')
+PROBE_LIB = os.path.join(OUT_DIR, 'libqsx_probe.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC',
          '--expt-relaxed-constexpr']
@@ -70,6 +74,12 @@ def build(verbose=False, force=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError('link failed:\n' + r.stderr)
+    if force or _stale(PROBE_LIB, [PROBE_SRC]):
+        cmd = [exe] + ARCH + FLAGS + ['-shared', '-cudart', 'static', PROBE_SRC,
+                                      '-o', PROBE_LIB]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError('nvcc failed on {}:\n{}'.format(PROBE_SRC, r.stderr))
     return LIB
 
 

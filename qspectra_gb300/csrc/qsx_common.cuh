@@ -106,4 +106,29 @@ __host__ __device__ __forceinline__ double2 cadd2(double2 a, double2 b) { return
 
 __device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 
+// Whether a select table can drive the blocked loops: every entry in
+// [0, m) and no entry twice (a repeated entry would leave an output slot
+// unfilled, an entry outside [0, m) would index past the state).  Every
+// thread of the CTA must call it (it ends in a barrier); the result is the
+// same in all threads, and a bad table sets QSX_ERR_INVALID_ARG in *status.
+__device__ __forceinline__ bool select_table_valid(const int* __restrict__ sel, int nsel, int m,
+                                                   int* status) {
+  int bad = 0;
+  for (int q = threadIdx.x; q < nsel; q += blockDim.x) {
+    const int v = sel[q];
+    if (v < 0 || v >= m) {
+      bad = 1;
+    } else {
+      for (int j = 0; j < q; ++j)
+        if (sel[j] == v) {
+          bad = 1;
+          break;
+        }
+    }
+  }
+  bad = __syncthreads_or(bad);
+  if (bad && threadIdx.x == 0 && status) atomicOr(status, QSX_ERR_INVALID_ARG);
+  return !bad;
+}
+
 }  // namespace qsx

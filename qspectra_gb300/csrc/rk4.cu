@@ -14,6 +14,7 @@
 // Ensemble means are reduced deterministically: every kernel writes partial
 // sums per "slot" (warp, CTA or sample) into caller workspace and
 // rk4_reduce_kernel sums the slots in a fixed order in FP64.
+#include <atomic>
 #include <algorithm>
 
 #include "qsx_common.cuh"
@@ -302,6 +303,7 @@ __global__ void __launch_bounds__(256, 2) rk4_block_f32(Rk4P p, int64_t ngroups,
   float2* ybuf = (float2*)smraw;             // [2][G][ST]
   float2* stash = ybuf + 2 * G * ST;         // [2][K][G][nsel]
   const int nsel = p.nselect;
+  if (!select_table_valid(p.select, nsel, M, p.status)) return;
   const int RT = M + nsel * (K - 1);
   const int tid = threadIdx.x;
   const int g = tid / RT, r = tid % RT;
@@ -419,6 +421,7 @@ __global__ void __launch_bounds__(448, 2) rk4_block2_f32(Rk4P p, int64_t ngroups
   float2* ybuf = (float2*)smraw;             // [2][G][ST]
   float2* stash = ybuf + 2 * G * ST;         // [2][K][G][nsel]
   const int nsel = p.nselect;
+  if (!select_table_valid(p.select, nsel, M, p.status)) return;
   const int RT = M + nsel * (K - 1);
   const int wps = (RT + RPW - 1) / RPW;      // warps per sample
   const int tid = threadIdx.x, lane = tid & 31, wi = tid >> 5;
@@ -549,6 +552,7 @@ __global__ void __launch_bounds__(256, 2) rk4_block3_f32(Rk4P p, int64_t ngroups
   float2* ybuf = (float2*)smraw;             // [2][G][ST]
   float2* stash = ybuf + 2 * G * ST;         // [2][K][G][nsel]
   const int nsel = p.nselect;
+  if (!select_table_valid(p.select, nsel, M, p.status)) return;
   const int RT = M + nsel * (K - 1);
   const int NRP = (RT + 1) / 2;              // row pairs per sample
   const int wps = (NRP + RPW - 1) / RPW;     // warps per sample
@@ -1221,24 +1225,36 @@ constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)16 << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
-static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+// per-device cache of the array's address; host threads may call
+// concurrently, so every access is atomic
+static std::atomic<void*> g_noalloc_ptr[NOALLOC_MAX_DEVICES];
 
 // Device address of g_noalloc_scratch on the current device (host code may
-// not take the address of a __device__ array directly).
-static int noalloc_scratch(void** out) {
+// not take the address of a __device__ array directly).  Outside a stream
+// capture the address is looked up on every call (cheap, and right after a
+// device reset); inside one the cached address of an earlier call is used.
+static int noalloc_scratch(cudaStream_t s, void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_block_mean_noalloc: cudaGetDevice");
   QSX_CHECK_ARG(dev >= 0 && dev < NOALLOC_MAX_DEVICES,
                 "qsx_rk4_block_mean_noalloc: device index %d not supported", dev);
-  if (g_noalloc_ptr[dev] == nullptr) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(s, &cap);
+  if (e != cudaSuccess)
+    return cuda_status(e, "qsx_rk4_block_mean_noalloc: cudaStreamIsCapturing");
+  if (cap == cudaStreamCaptureStatusNone) {
     void* ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess)
       return cuda_status(e, "qsx_rk4_block_mean_noalloc: cudaGetSymbolAddress");
-    g_noalloc_ptr[dev] = ptr;
+    g_noalloc_ptr[dev].store(ptr, std::memory_order_release);
   }
-  *out = g_noalloc_ptr[dev];
+  void* ptr = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  QSX_CHECK_ARG(ptr != nullptr,
+                "qsx_rk4_block_mean_noalloc: the first call on device %d was made inside a "
+                "stream capture; make one call before capturing", dev);
+  *out = ptr;
   return QSX_OK;
 }
 
@@ -1263,10 +1279,10 @@ extern "C" int qsx_rk4_block_mean_noalloc(const qsx_rk4_args* a, void* stream) {
   // fewer persistent CTAs when their slices would not all fit
   const int64_t grid = std::max<int64_t>(
       1, std::min<int64_t>(pl.grid, (int64_t)(NOALLOC_SCRATCH_BYTES / slice)));
-  void* scratch = nullptr;
-  st = noalloc_scratch(&scratch);
-  if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
+  void* scratch = nullptr;
+  st = noalloc_scratch(s, &scratch);
+  if (st) return st;
   cudaError_t e = cudaMemsetAsync(scratch, 0, (size_t)grid * slice, s);
   if (e != cudaSuccess) return cuda_status(e, "qsx_rk4_block_mean_noalloc: memset");
   Rk4P p;

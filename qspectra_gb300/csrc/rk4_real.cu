@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(512, 1) rk4_hblock_f32(HbP p, int64_t ngroups,
   // ([nsave][nsel] FP32) until the end instead of one FP64 atomic per step
   float* lsum = stash + 2 * K * G * p.nselect;
   const int nsel = p.nselect;
+  if (!select_table_valid(p.select, nsel, M, p.status)) return;
   const int RT = M + nsel * (K - 1);
   const int tid = threadIdx.x;
   const int g = tid / RT, r = tid % RT;
@@ -250,6 +251,7 @@ __global__ void __launch_bounds__(MAXT, MAXT == 64 ? 6 : 1)
   constexpr int MP = (M + 3) & ~3;
   extern __shared__ __align__(128) unsigned char smraw[];
   const int nsel = p.nselect;
+  if (!select_table_valid(p.select, nsel, M, p.status)) return;
   const int nR = nsel * (K - 1);
   const int RT = M + nR;
   const int64_t sstride = ((int64_t)RT * M + 3) & ~(int64_t)3;
@@ -553,6 +555,7 @@ __global__ void __launch_bounds__(HC_THREADS, 2)
   const uint64_t db_hi = smem_desc((uint32_t)__cvta_generic_to_shared(b_hi), sbo);
   const uint64_t db_lo = smem_desc((uint32_t)__cvta_generic_to_shared(b_lo), sbo);
   const uint32_t idesc = make_idesc(nb);
+  if (!select_table_valid(select, nsel, M, status)) return;   // before any TMEM is held
   for (uint32_t e = tid; e < (2 * PA + 2 * PB) / 16; e += HC_THREADS)
     reinterpret_cast<uint4*>(smraw)[e] = make_uint4(0, 0, 0, 0);
   for (int e = tid; e < (nblk + 1) * nsel; e += HC_THREADS) bsum[e] = 0.f;

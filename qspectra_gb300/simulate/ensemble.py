@@ -325,8 +325,12 @@ def sample_polarizations(polarization, rotations):
 
 def ensemble_linear_signal(model, time_max, ensemble_size, polarization='xx',
                            precision='fp32', path='gg->eg->gg', start=0,
-                           offsets=None, return_build=False, rotations=None):
+                           offsets=None, return_build=False, rotations=None,
+                           initial_state=None):
     """Disorder-averaged Heisenberg-picture linear response (response.py:15-43).
+
+    ``initial_state`` (a state vector on the path's first subspace, shared by
+    every sample) replaces the thermal state, as in linear_response.
 
     ``rotations`` (S, 3, 3) rotates each sample's dipoles (random ensemble
     orientations, decorators.py:40-64): the dipole operators are linear in
@@ -342,7 +346,8 @@ def ensemble_linear_signal(model, time_max, ensemble_size, polarization='xx',
     t = np.arange(0, time_max, dt)
     batch = SampleBatch(model, ensemble_size, start, offsets)
     build = redfield_batch_build(model, batch, prec)
-    rho0 = model.thermal_state(subs[0])
+    rho0 = (model.thermal_state(subs[0]) if initial_state is None
+            else np.asarray(initial_state))
     q = None if rotations is None else torch.as_tensor(
         sample_polarizations(polarization, rotations)).cuda()      # (S, 2, 3)
     total = None
@@ -367,8 +372,7 @@ def ensemble_linear_signal(model, time_max, ensemble_size, polarization='xx',
         out = projected_mean(D, y0, proj, int(steps[-1]))
         sig = out['mean'][:, 0]
         total = sig if total is None else total + sig
-        if int(out['status'].item()) & _native.QSX_ERR_NONFINITE:
-            raise _native.IntegratorError('non-finite state in ensemble propagation')
+        raise_for_status(int(out['status'].item()))
     if return_build:
         return t, total, build
     return t, total
@@ -407,9 +411,21 @@ def ensemble_populations(model, initial_state, duration, ensemble_size,
     else:
         out = propagate_selected_mean(build.propagator(idx, dt, prec), y0t, len(t) - 1,
                                       select, prec)
-    if int(out['status'].item()) & _native.QSX_ERR_NONFINITE:
-        raise _native.IntegratorError('non-finite state in ensemble propagation')
+    raise_for_status(int(out['status'].item()))
     return t, out['mean']
+
+
+def raise_for_status(status):
+    """Raise for a status word of the ensemble kernels: IntegratorError for a
+    non-finite state (integrate()'s error in the reference,
+    simulate/utils.py:12-13), QsxError for a bad index table or a timed-out
+    tensor-core wait."""
+    if status & _native.QSX_ERR_NONFINITE:
+        raise _native.IntegratorError('non-finite state in ensemble propagation')
+    if status & _native.QSX_ERR_INVALID_ARG:
+        raise _native.QsxError('ensemble propagation: index table out of range')
+    if status & _native.QSX_ERR_CUDA:
+        raise _native.QsxError('ensemble propagation: a tensor-core wait timed out')
 
 
 class RedfieldEnsembleWorkload:
@@ -552,6 +568,5 @@ class RedfieldEnsembleWorkload:
             X, pops, status = self.run(off, precision)
         out = torch.cat([X, pops.reshape(-1), status.to(torch.float64)]).to('cpu')
         n = X.numel()
-        if int(out[-1].item()) & _native.QSX_ERR_NONFINITE:
-            raise _native.IntegratorError('non-finite state in ensemble propagation')
+        raise_for_status(int(out[-1].item()))
         return out[:n].numpy(), out[n:-1].numpy().reshape(pops.shape)
