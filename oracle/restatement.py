@@ -670,10 +670,12 @@ def simulate_dynamics(model, psi_or_rho, duration, liouville_subspace='ee',
 
 
 def linear_response(model, time_max, polarization='xx', path='gg->eg->gg',
-                    dt=None):
-    """Heisenberg-picture linear response (response.py:15-43)."""
+                    dt=None, initial_state=None):
+    """Heisenberg-picture linear response (response.py:15-43); the initial
+    state defaults to the thermal state of the path's first subspace."""
     subs = path.split('->')
-    rho0 = model.thermal_state(subs[0])
+    rho0 = (model.thermal_state(subs[0]) if initial_state is None
+            else np.asarray(initial_state))
     dt = model.time_step if dt is None else dt
     t = time_grid(time_max, dt)
     signal = 0
@@ -685,6 +687,40 @@ def linear_response(model, time_max, polarization='xx', path='gg->eg->gg',
         v_gt = rk4_integrate(LH, -V1.bra_vector, t)
         signal = signal + v_gt @ v_rho0
     return t, signal
+
+
+PUMP_PROBE_PATHWAYS = {'GSB': 'gg->eg->gg', 'ESE': 'ee->eg->gg', 'ESA': 'ee->fe->ee'}
+"""Pump-probe Liouville pathways (response.py:157-160)."""
+
+
+def impulsive_probe(model, state, time_max, polarization='xx',
+                    initial_liouv_subspace='gg,ge,eg,ee', include_signal='GSB,ESE,ESA'):
+    """response.py:174-244: the state minus the thermal state, split over the
+    selected pump-probe pathways, each portion's linear response summed, then
+    the Fourier transform (sign +1, rw_freq added)."""
+    init = np.asarray(state) - model.thermal_state(initial_liouv_subspace)
+    total, t = 0, None
+    for name, path in PUMP_PROBE_PATHWAYS.items():
+        if name not in include_signal:
+            continue
+        first = path.split('->')[0]
+        portion = model.map_between_subspaces(init, initial_liouv_subspace, first)
+        t, sig = linear_response(model, time_max, polarization, path, initial_state=portion)
+        total = total + sig
+    return fourier_transform(t, total, rw_freq=model.ham.rw_freq,
+                             unit_convert=model.unit_convert)
+
+
+def two_dimensional_spectra(model, coherence_time_max, population_times, geometry='-++',
+                            polarization='xxxx', include_signal=None):
+    """response.py:430-455: the third-order response transformed over t1
+    (sign -1, axis 0) and then t3 (sign +1, axis 2)."""
+    (t1, t2, t3), X = third_order_response(model, coherence_time_max, population_times,
+                                           geometry, polarization, include_signal)
+    rw, uc = model.ham.rw_freq, model.unit_convert
+    f1, X1 = fourier_transform(t1, X, 0, rw_freq=rw, sign=-1, unit_convert=uc)
+    f3, X3 = fourier_transform(t3, X1, 2, rw_freq=rw, unit_convert=uc)
+    return (f1, t2, f3), X3
 
 
 def absorption_spectra(model, time_max, polarization='xx', dt=None,

@@ -132,7 +132,8 @@ def linear_response(dynamical_model, liouv_space_path, time_max,
     if ensemble_size is not None and ensemble_random_orientations:
         rotations = dynamical_model.hamiltonian.orientation_rotations(ensemble_size)
     batched = (ensemble_size is not None and isinstance(dynamical_model, RedfieldModel)
-               and initial_state is None and not integrate_kwargs)
+               and (initial_state is None or np.ndim(initial_state) == 1)
+               and not integrate_kwargs)
     zofe = (isinstance(dynamical_model, ZOFEModel) and initial_state is None
             and not integrate_kwargs and ',' not in liouv_space_path.split('->')[1])
 
@@ -143,7 +144,8 @@ def linear_response(dynamical_model, liouv_space_path, time_max,
         if batched:
             t, sig = ensemble_linear_signal(dynamical_model, time_max, ensemble_size,
                                             pol, precision, path=liouv_space_path,
-                                            rotations=rotations)
+                                            rotations=rotations,
+                                            initial_state=initial_state)
             return t, sig.cpu().numpy()
         if ensemble_size is not None:
             total = 0
@@ -183,9 +185,18 @@ def absorption_spectra(dynamical_model, time_max, correlation_decay_time=None,
 
 def impulsive_probe(dynamical_model, state, time_max, polarization='xx',
                     initial_liouv_subspace='gg,ge,eg,ee',
-                    include_signal='GSB,ESE,ESA', precision='fp64',
+                    include_signal='GSB,ESE,ESA', ensemble_size=None,
+                    ensemble_random_orientations=False,
+                    exact_isotropic_average=False, precision='fp64',
                     **integrate_kwargs):
-    """Impulsive probe of a 2nd-order state (response.py:174-244)."""
+    """Impulsive probe of a 2nd-order state (response.py:174-244).
+
+    The state minus the thermal state is split over the pump-probe pathways
+    (GSB, ESE, ESA) and each portion goes through ``linear_response`` with
+    the same ensemble and orientation options; the summed signal is Fourier
+    transformed.  With ``ensemble_size`` on a Redfield model every disorder
+    sample of a pathway runs in one batched pipeline.
+    """
     init = np.asarray(state) - dynamical_model.thermal_state(initial_liouv_subspace)
     total = 0
     t = None
@@ -194,8 +205,11 @@ def impulsive_probe(dynamical_model, state, time_max, polarization='xx',
         portion = np.apply_along_axis(
             lambda s: dynamical_model.map_between_subspaces(s, initial_liouv_subspace, first),
             -1, init)
-        t, sig = _single_linear_response(dynamical_model, path, time_max, portion,
-                                         polarization, precision, **integrate_kwargs)
+        t, sig = linear_response(dynamical_model, path, time_max, portion, polarization,
+                                 ensemble_size=ensemble_size,
+                                 ensemble_random_orientations=ensemble_random_orientations,
+                                 exact_isotropic_average=exact_isotropic_average,
+                                 precision=precision, **integrate_kwargs)
         total = total + sig
     return fourier_transform(t, total, rw_freq=dynamical_model.rw_freq,
                              unit_convert=dynamical_model.unit_convert)

@@ -1,9 +1,14 @@
 """Generate the golden fixtures in this folder by running the reference itself.
 
 Run from the repository root in a container where the reference checkout is
-available (read-only is fine):
+available (read-only is fine), giving the checkout's path:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <reference-checkout> [base|drivers|all]
+
+``base`` writes reference_golden.npz (generators, trajectories, spectra and
+small third-order cases); ``drivers`` writes reference_golden_drivers.npz
+(impulsive probe, 2D spectra, third order on the 128 x 3 x 128 grids at 6
+and 8 sites, and the 8-site 495-node HEOM trajectory).
 
 Every fixture comes from the reference's own code path.  Its adaptive
 ``zvode`` integrator is swapped for a fixed-step RK4 harness that drives the
@@ -351,5 +356,133 @@ def main(ref_root):
     print('wrote', len(out), 'arrays')
 
 
+def import_reference(ref_root):
+    python3_shims()
+    sys.path.insert(0, ref_root)
+    sys.path.insert(0, ROOT)
+    warnings.simplefilter('ignore')
+    import qspectra as qs
+    return qs
+
+
+def second_order_state(n_sites, seed):
+    """A Hermitian state on 'gg,ge,eg,ee' (column-stacked, the reference's
+    state_vector layout): the ground state plus small seeded coherences and
+    excited-state populations, as a pump would leave it."""
+    rng = np.random.RandomState(seed)
+    n = n_sites + 1
+    rho = np.zeros((n, n), complex)
+    rho[0, 0] = 0.9
+    c = 0.05 * (rng.randn(n_sites) + 1j * rng.randn(n_sites))
+    rho[1:, 0] = c
+    rho[0, 1:] = c.conj()
+    psi = rng.randn(n_sites) + 1j * rng.randn(n_sites)
+    psi *= np.sqrt(0.1) / np.linalg.norm(psi)
+    rho[1:, 1:] = np.outer(psi, psi.conj())
+    return rho
+
+
+def drivers_main(ref_root):
+    """Fixtures for the pump-probe and 2D drivers and for the configuration-
+    size third-order and HEOM checks."""
+    qs = import_reference(ref_root)
+    import qspectra.simulate.response as qresp
+    import qspectra.simulate.eom as qeom
+    from qspectra_gb300 import workloads as wl
+    out = {}
+
+    # ---- impulsive_probe (response.py:174-244) on a 3-site 'gef' chain -----
+    rk4 = rk4_harness(2.0)
+    qeom.integrate = rk4
+    qresp.integrate = rk4
+    H3 = wl.chain_hamiltonian(n_sites=3, seed=7)
+    bath300 = qs.DebyeBath(qs.CM_K * 300, 40, 100)
+    extra3 = wl.energy_spread_for_dt(H3, 2.0, qs.CM_FS)
+    dip3 = [[1.0, 0, 0], [0.4, 0.8, 0.0], [-0.3, 0.5, 0.6]]
+    ham3 = qs.ElectronicHamiltonian(H3, bath=bath300, dipoles=dip3,
+                                    disorder=wl.fwhm_for_sd(30.0), random_seed=5,
+                                    energy_spread_extra=extra3)
+    m3 = qs.RedfieldModel(ham3, hilbert_subspace='gef', unit_convert=qs.CM_FS,
+                          secular=False)
+    assert m3.time_step == 2.0
+    rho = second_order_state(3, seed=21)
+    state = m3.density_matrix_to_state_vector(rho, 'gg,ge,eg,ee')
+    out['probe3_H'] = H3
+    out['probe3_extra'] = extra3
+    out['probe3_dipoles'] = np.array(dip3)
+    out['probe3_state'] = state
+    for sig in ('GSB', 'ESE', 'ESA', 'GSB,ESE,ESA'):
+        f, X = qs.impulsive_probe(m3, state, 200.0, polarization='xy',
+                                  include_signal=sig)
+        out['probe3_{}'.format(sig.replace(',', '_'))] = X
+    out['probe3_f'] = f
+    _, X = qs.impulsive_probe(m3, state, 200.0, polarization='xx', ensemble_size=3)
+    out['probe3_ens3'] = X
+    _, X = qs.impulsive_probe(m3, state, 200.0, polarization='xy', ensemble_size=3,
+                              ensemble_random_orientations=True)
+    out['probe3_ens3_rand'] = X
+    _, X = qs.impulsive_probe(m3, state, 200.0, polarization=[0.4, 'x'],
+                              exact_isotropic_average=True)
+    out['probe3_iso'] = X
+
+    # ---- two_dimensional_spectra (response.py:430-455) ---------------------
+    for geo in ('-++', '+-+'):
+        (f1, t2, f3), X = qs.two_dimensional_spectra(
+            m3, coherence_time_max=40.0, population_times=[0.0, 20.0, 50.0], geometry=geo)
+        out['twod3_{}'.format(geo)] = X
+    out['twod3_f1'] = f1
+    out['twod3_f3'] = f3
+    (f1, t2, f3), X = qs.two_dimensional_spectra(
+        m3, coherence_time_max=40.0, population_times=[0.0, 30.0], geometry='-++',
+        polarization='xyxy', ensemble_size=2)
+    out['twod3_ens2_xyxy'] = X
+
+    # ---- third order on the 128 x 3 x 128 grids, chains of 6 and 8 sites ----
+    for N in (6, 8):
+        HN = wl.chain_hamiltonian(n_sites=N, seed=2024)
+        extraN = wl.energy_spread_for_dt(HN, 2.0, qs.CM_FS)
+        hamN = qs.ElectronicHamiltonian(HN, bath=bath300, dipoles=[[1, 0, 0]] * N,
+                                        disorder=wl.fwhm_for_sd(60.0), random_seed=3,
+                                        energy_spread_extra=extraN)
+        mN = qs.RedfieldModel(hamN, hilbert_subspace='gef', unit_convert=qs.CM_FS,
+                              secular=False)
+        assert mN.time_step == 2.0
+        out['chain{}_H'.format(N)] = HN
+        out['chain{}_extra'.format(N)] = extraN
+        for geo in ('-++', '+-+'):
+            (t1, t2, t3), S = qs.third_order_response(
+                mN, coherence_time_max=256.0, population_times=[0.0, 200.0, 500.0],
+                geometry=geo, ensemble_size=2)
+            out['chain{}_3rd_ens2_{}'.format(N, geo)] = S
+        print('chain', N, 'done', flush=True)
+
+    # ---- HEOM at the 8-site ring configuration: 495 nodes, 200 steps -------
+    HR = wl.ring_hamiltonian()
+    hamR = qs.ElectronicHamiltonian(HR, bath=qs.DebyeBath(qs.CM_K * 300, 35, 106),
+                                    disorder=wl.fwhm_for_sd(50.0), random_seed=7)
+    sample = 37
+    hs = hamR.sample(sample)
+    hm = qs.HEOMModel(hs, hilbert_subspace='e', unit_convert=qs.CM_FS, K=0,
+                      level_cutoff=5, low_temp_corr=True)
+    assert hm.ado_count == 495
+    eom = hm.equation_of_motion('ee')
+    y0 = np.zeros(495 * 64, complex)
+    y0[0] = 1.0
+    traj = rk4_harness(0.5)(eom, y0, np.arange(0, 100.5, 0.5))
+    out['ring8_H'] = HR
+    out['ring8_sample'] = np.array(sample)
+    out['ring8_sample_H'] = hs.H_1exc
+    out['ring8_traj_node0'] = traj[:, :64]
+    out['ring8_final_state'] = traj[-1]
+    np.savez_compressed(os.path.join(HERE, 'reference_golden_drivers.npz'), **out)
+    print('wrote', len(out), 'arrays')
+
+
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    if len(sys.argv) < 2:
+        sys.exit('usage: make_golden.py <reference-checkout> [base|drivers|all]')
+    what = sys.argv[2] if len(sys.argv) > 2 else 'all'
+    if what in ('base', 'all'):
+        main(sys.argv[1])
+    if what in ('drivers', 'all'):
+        drivers_main(sys.argv[1])

@@ -1,0 +1,116 @@
+"""The pump-probe and 2D drivers and the third-order engine on the full
+128 x 3 x 128 grids, against fixtures made by running the reference.
+
+* ``impulsive_probe`` (response.py:174-244): each pump-probe pathway alone and
+  all three, a disorder ensemble, random ensemble orientations and the exact
+  isotropic average, on a 3-site 'gef' chain;
+* ``two_dimensional_spectra`` (response.py:430-455): both engine geometries,
+  and a 2-sample ensemble with mixed polarizations;
+* ``third_order_response`` on disordered 6- and 8-site chains with the
+  third-order configuration's grids (t1 = t3 = 128 x 2 fs, t2 = 0 / 200 /
+  500 fs), both geometries, a 2-sample ensemble.
+
+FP64 must match to 1e-10 and FP32 to 1e-4 (max-abs relative).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import qspectra_gb300 as qg
+from conftest import ROOT, rel_err
+from qspectra_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+TOLS = [('fp64', 1e-10), ('fp32', 1e-4)]
+
+
+@pytest.fixture(scope='module')
+def drivers():
+    path = os.path.join(ROOT, 'tests', 'golden', 'reference_golden_drivers.npz')
+    with np.load(path) as z:
+        return {k: z[k] for k in z.files}
+
+
+def probe_model(g):
+    ham = qg.ElectronicHamiltonian(g['probe3_H'], bath=qg.DebyeBath(qg.CM_K * 300, 40, 100),
+                                   dipoles=g['probe3_dipoles'], disorder=wl.fwhm_for_sd(30.0),
+                                   random_seed=5, energy_spread_extra=float(g['probe3_extra']))
+    return qg.RedfieldModel(ham, hilbert_subspace='gef', unit_convert=qg.CM_FS, secular=False)
+
+
+@pytest.mark.parametrize('precision,tol', TOLS)
+@pytest.mark.parametrize('sig', ['GSB', 'ESE', 'ESA', 'GSB,ESE,ESA'])
+def test_impulsive_probe(drivers, sig, precision, tol):
+    m = probe_model(drivers)
+    f, X = qg.impulsive_probe(m, drivers['probe3_state'], 200.0, polarization='xy',
+                              include_signal=sig, precision=precision)
+    assert np.allclose(f, drivers['probe3_f'], rtol=0, atol=1e-9)
+    assert rel_err(X, drivers['probe3_' + sig.replace(',', '_')]) < tol
+
+
+@pytest.mark.parametrize('precision,tol', TOLS)
+def test_impulsive_probe_ensemble(drivers, precision, tol):
+    m = probe_model(drivers)
+    _, X = qg.impulsive_probe(m, drivers['probe3_state'], 200.0, polarization='xx',
+                              ensemble_size=3, precision=precision)
+    assert rel_err(X, drivers['probe3_ens3']) < tol
+
+
+@pytest.mark.parametrize('precision,tol', TOLS)
+def test_impulsive_probe_random_orientations(drivers, precision, tol):
+    m = probe_model(drivers)
+    _, X = qg.impulsive_probe(m, drivers['probe3_state'], 200.0, polarization='xy',
+                              ensemble_size=3, ensemble_random_orientations=True,
+                              precision=precision)
+    assert rel_err(X, drivers['probe3_ens3_rand']) < tol
+
+
+@pytest.mark.parametrize('precision,tol', TOLS)
+def test_impulsive_probe_isotropic(drivers, precision, tol):
+    m = probe_model(drivers)
+    _, X = qg.impulsive_probe(m, drivers['probe3_state'], 200.0, polarization=[0.4, 'x'],
+                              exact_isotropic_average=True, precision=precision)
+    assert rel_err(X, drivers['probe3_iso']) < tol
+
+
+@pytest.mark.parametrize('precision,tol', TOLS)
+@pytest.mark.parametrize('geo', ['-++', '+-+'])
+def test_two_dimensional_spectra(drivers, geo, precision, tol):
+    m = probe_model(drivers)
+    (f1, t2, f3), X = qg.two_dimensional_spectra(m, 40.0, population_times=[0.0, 20.0, 50.0],
+                                                 geometry=geo, precision=precision)
+    assert np.allclose(f1, drivers['twod3_f1'], rtol=0, atol=1e-9)
+    assert np.allclose(f3, drivers['twod3_f3'], rtol=0, atol=1e-9)
+    assert rel_err(X, drivers['twod3_' + geo]) < tol
+
+
+@pytest.mark.parametrize('precision,tol', TOLS)
+def test_two_dimensional_spectra_ensemble(drivers, precision, tol):
+    m = probe_model(drivers)
+    _, X = qg.two_dimensional_spectra(m, 40.0, population_times=[0.0, 30.0], geometry='-++',
+                                      polarization='xyxy', ensemble_size=2,
+                                      precision=precision)
+    assert rel_err(X, drivers['twod3_ens2_xyxy']) < tol
+
+
+def chain_model(g, N):
+    ham = qg.ElectronicHamiltonian(g['chain{}_H'.format(N)],
+                                   bath=qg.DebyeBath(qg.CM_K * 300, 40, 100),
+                                   dipoles=[[1, 0, 0]] * N, disorder=wl.fwhm_for_sd(60.0),
+                                   random_seed=3,
+                                   energy_spread_extra=float(g['chain{}_extra'.format(N)]))
+    return qg.RedfieldModel(ham, hilbert_subspace='gef', unit_convert=qg.CM_FS, secular=False)
+
+
+@pytest.mark.parametrize('precision,tol', TOLS)
+@pytest.mark.parametrize('N', [6, 8])
+def test_third_order_full_grids(drivers, N, precision, tol):
+    m = chain_model(drivers, N)
+    for geo in ('-++', '+-+'):
+        (t1, t2, t3), R = qg.third_order_response(m, 256.0, population_times=[0.0, 200.0, 500.0],
+                                                  geometry=geo, ensemble_size=2,
+                                                  precision=precision)
+        assert R.shape == (128, 3, 128)
+        assert rel_err(R, drivers['chain{}_3rd_ens2_{}'.format(N, geo)]) < tol
