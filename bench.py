@@ -51,7 +51,9 @@ def parse_args():
     p.add_argument('--warmup', type=int, default=3)
     p.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     p.add_argument('--samples', type=int, default=N_SAMPLES)
-    p.add_argument('--cpu-samples-per-core', type=int, default=24)
+    p.add_argument('--cpu-samples-per-core', type=int, default=4)
+    p.add_argument('--shipped-samples', type=int, default=16,
+                   help='disorder samples of the single-process reference timing')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--fp64-steps', type=int, default=2)
     p.add_argument('--no-heom', action='store_true')
@@ -131,28 +133,68 @@ def clocks_stop(proc):
 
 # ------------------------------------------------------------ CPU baseline
 def cpu_baseline(H, extra, fwhm, per_core, n_full=N_SAMPLES, steps=1, warmup=0):
-    """Oracle port of the reference path over a spawn pool of all host cores."""
+    """CPU baseline over a spawn pool of all host cores: the reference's own
+    per-sample calls (absorption_spectra + simulate_dynamics, zvode) when the
+    reference is installed under baseline/_ref, else the oracle port of the
+    same path.  Each measurement is a bounded sample of ``per_core`` samples
+    per core; spectra/s is extrapolated linearly to ``n_full`` samples."""
     import multiprocessing as mp
     from oracle import baseline as ob
+    from oracle import reference_shipped as rs
     cores = os.cpu_count() or 1
     n = per_core * cores
     ctx = mp.get_context('spawn')
     # one BLAS thread per worker process (spawned children read these at import)
     for var in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
         os.environ[var] = '1'
-    vals = []
+    ref = rs.available()
+    vals, walls = [], []
     with ctx.Pool(cores) as pool:
-        ob.time_fmo7_samples(H, extra, fwhm, cores, workers=cores, pool=pool)  # warm
+        if ref:
+            rs.time_pool(H, extra, fwhm, cores, pool, cores)   # warm (imports)
+        else:
+            ob.time_fmo7_samples(H, extra, fwhm, cores, workers=cores, pool=pool)
         for k in range(warmup + steps):
-            wall, _, _ = ob.time_fmo7_samples(H, extra, fwhm, n, workers=cores, pool=pool,
-                                              start=k * n)
+            if ref:
+                wall = rs.time_pool(H, extra, fwhm, n, pool, cores, start=k * n)
+            else:
+                wall, _, _ = ob.time_fmo7_samples(H, extra, fwhm, n, workers=cores, pool=pool,
+                                                  start=k * n)
             if k >= warmup:
                 vals.append(1.0 / (wall / n * n_full))
-    return {'value': float(np.mean(vals)), 'unit': UNIT, 'cores': cores, 'kind': 'port',
-            'sample': '{} disorder samples per measurement ({} per core) of the same '
-                      'workload, one sample at a time per process like the reference '
-                      'ensemble loop; spectra/s extrapolated linearly to {} samples'.format(
-                          n, per_core, n_full)}
+                walls.append(wall)
+    what = ("the reference's own absorption_spectra + simulate_dynamics calls (baseline/_ref, "
+            "zvode), one disorder sample at a time per process" if ref else
+            'the oracle port of the same path (RK4), one disorder sample at a time per process')
+    return {'value': float(np.mean(vals)), 'unit': UNIT, 'cores': cores,
+            'kind': 'reference' if ref else 'port',
+            'ms_per_measurement': 1000.0 * float(np.mean(walls)),
+            'sample': '{} disorder samples per measurement ({} per core): {}; spectra/s '
+                      'extrapolated linearly to {} samples'.format(n, per_core, what, n_full)}
+
+
+def reference_as_shipped(H, extra, fwhm, samples, n_full=N_SAMPLES, reps=1):
+    """The reference as shipped: one process, one BLAS thread, its own
+    ensemble loop (ensemble_size=samples) over absorption_spectra and
+    simulate_dynamics; run in a spawned child so the thread setting holds."""
+    import multiprocessing as mp
+    from oracle import reference_shipped as rs
+    if not rs.available():
+        return {'unavailable': 'baseline/_ref not installed (oracle/install_reference.sh)'}
+    for var in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+        os.environ[var] = '1'
+    ctx = mp.get_context('spawn')
+    with ctx.Pool(1) as pool:
+        pool.apply(rs.time_as_shipped, (H, extra, fwhm, 1))   # warm (imports)
+        walls = [pool.apply(rs.time_as_shipped, (H, extra, fwhm, samples))
+                 for _ in range(reps)]
+    wall = float(np.mean(walls))
+    return {'value': 1.0 / (wall / samples * n_full), 'unit': UNIT, 'cores': 1,
+            'kind': 'reference', 'ms_per_sample': 1000.0 * wall / samples,
+            'sample': 'absorption_spectra(model, 2048, ensemble_size={0}) + '
+                      'simulate_dynamics(model, psi, 1000, ensemble_size={0}) of the '
+                      'reference (baseline/_ref, zvode), one process, one BLAS thread; '
+                      'spectra/s extrapolated linearly to {1} samples'.format(samples, n_full)}
 
 
 def reference_arm(args):
@@ -165,10 +207,16 @@ def reference_arm(args):
     val = base['value']
     line = {'metric': METRIC, 'value': val, 'unit': UNIT, 'impl': 'reference',
             'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-            'ms_per_step': 1000.0 / val, 'higher_is_better': True,
+            'ms_per_step': base['ms_per_measurement'],
+            'ms_per_step_note': ('measured wall time of one step, a bounded sample of the '
+                                 'ensemble; value extrapolates it to the full {} samples'
+                                 .format(args.samples)),
+            'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'c128',
             'data': 'synthetic (seeded)', 'config': dict(CONFIG),
             'cpu_baseline': base,
+            'reference_as_shipped': reference_as_shipped(H, extra, fwhm,
+                                                         args.shipped_samples, args.samples),
             'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0}}
     print(json.dumps(line), flush=True)
@@ -665,7 +713,7 @@ def our_arm(args):
     bb_flops = events.get('blockbuild_flops')
     base = None
     if world == 1 and not args.no_cpu_baseline:
-        base = cpu_baseline(H, extra, fwhm, args.cpu_samples_per_core, S)
+        base = cpu_baseline(H, extra, fwhm, 4 * args.cpu_samples_per_core, S, steps=3)
     nf = Xh.size
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,

@@ -94,6 +94,30 @@ int qsx_redfield_operators_batched(const double* E, const double* U, int n,
                                    void* stream);
 
 /*
+ * FP64 build for one-exciton Hilbert spaces ('e', 'ge'; 2 <= n_sites <= 8),
+ * one warp per sample: the eigendecomposition of the rotating-frame H
+ * (Hamiltonian.eig, qspectra/hamiltonian.py:310-328) from approximate
+ * eigenvectors X: two FP64 Newton-Schulz steps make X orthonormal, then
+ * cyclic FP64 Jacobi sweeps diagonalise S = X^T H X, rotating X along (the
+ * low-precision-preconditioned Jacobi method); then the site-basis Redfield
+ * operators G and M_i of qsx_redfield_operators_batched (site_basis != 0),
+ * all in FP64.
+ * The coupled block is rows/columns [off, off + n_sites) of each n x n H
+ * (n <= 32); states outside it are uncoupled 1 x 1 blocks.  U_approx holds
+ * approximate eigenvectors of that block (e.g. from qsx_eigh_batched_prec
+ * with QSX_FP32) and may alias U.  Outputs: E [batch][n] (ascending inside
+ * the block), U [batch][n][n], G complex128 [batch][n][n], M complex128
+ * [batch][n_sites][n][n], scaled by unit_convert, zero outside the block.
+ */
+int qsx_redfield_build_w64(const double* H, int n, int off, int n_sites,
+                           int64_t batch, const double* U_approx,
+                           double temperature, double reorg_energy,
+                           double cutoff_freq, int matsubara_cutoff,
+                           int discard_imag_corr, double unit_convert,
+                           double* E, double* U, double* G, double* M,
+                           void* stream);
+
+/*
  * Dense Liouvillian block L[idx, idx] (transposed when transpose != 0, the
  * Heisenberg picture).  Replaces RedfieldModel.evolution_super_operator
  * (qspectra/dynamics/redfield.py:95-104, 146-152) sliced by
@@ -361,8 +385,9 @@ typedef struct {
   const double* occy;  /* [n_sites][ny] */
   const double* W;     /* [nx * ny] low-temperature weights, or NULL */
   const double* shift; /* [nnodes] */
-  const int32_t* nbr;  /* [nnodes][nterms] neighbour node, -1 = none */
-  const int32_t* site; /* [nnodes][nterms] */
+  const int32_t* nbr;  /* [nnodes][nterms] neighbour node, -1 = none (after the
+                          node's terms) */
+  const int32_t* site; /* [nnodes][nterms], ascending within each node */
   const double* alpha; /* complex128 [nnodes][nterms] */
   const double* beta;  /* complex128 [nnodes][nterms] */
   double unit_convert;

@@ -142,6 +142,9 @@ _PROTOS = {
                                           ctypes.POINTER(ctypes.c_size_t)]),
     'qsx_heom_rhs': (_c_int, [ctypes.POINTER(HeomArgs), _c_vp, _c_vp, _c_vp]),
     'qsx_heom_rk4': (_c_int, [ctypes.POINTER(HeomArgs), _c_vp]),
+    'qsx_redfield_build_w64': (_c_int, [_c_vp, _c_int, _c_int, _c_int, _c_i64, _c_vp, _c_dbl,
+                                        _c_dbl, _c_dbl, _c_int, _c_int, _c_dbl, _c_vp, _c_vp,
+                                        _c_vp, _c_vp, _c_vp]),
     'qsx_dft_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
                                  _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_fblock_tensor': (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_vp, _c_i64, _c_dbl,
@@ -270,6 +273,29 @@ def redfield_operators(E, U, occ, bath, unit_convert, discard_imag_corr=False,
         int(site_basis), int(precision), _p(G), _p(M), _p(K), _stream()),
         'qsx_redfield_operators_batched')
     return G, M, K
+
+
+def redfield_build_w64(H, U_approx, n_sites, off, bath, unit_convert, discard_imag_corr=False,
+                       matsubara_cutoff=1000):
+    """FP64 eigenpairs and site-basis Redfield operators of one-exciton
+    Hilbert spaces (qsx_redfield_build_w64): two FP64 refinement steps of
+    the approximate eigenvectors U_approx (e.g. the FP32 Jacobi's), then the
+    operator build in FP64.  H, U_approx (B, n, n) float64 CUDA; the coupled
+    block is [off, off + n_sites).  Returns E, U, G, M."""
+    require_gpu()
+    _need(H, torch.float64, 'H', 3)
+    _need(U_approx, torch.float64, 'U_approx', 3)
+    B, n, _ = H.shape
+    dev = H.device
+    E = torch.empty((B, n), dtype=torch.float64, device=dev)
+    U = torch.empty((B, n, n), dtype=torch.float64, device=dev)
+    G = torch.empty((B, n, n), dtype=torch.complex128, device=dev)
+    M = torch.empty((B, n_sites, n, n), dtype=torch.complex128, device=dev)
+    _check(load().qsx_redfield_build_w64(
+        _p(H), n, off, n_sites, B, _p(U_approx), bath.temperature, bath.reorg_energy,
+        bath.cutoff_freq, matsubara_cutoff, int(discard_imag_corr), unit_convert,
+        _p(E), _p(U), _p(G), _p(M), _stream()), 'qsx_redfield_build_w64')
+    return E, U, G, M
 
 
 def redfield_liouvillian(H, G, M, idx, unit_convert, K=None, occ=None,

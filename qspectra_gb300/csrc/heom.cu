@@ -63,6 +63,10 @@ struct HeomSmem {
   C* be;      // npc * nterms
   int* nbr;   // npc * nterms
   int* site;  // npc * nterms
+  int* tstart;  // npc * (n_sites + 1): each node's terms of site j are
+                // tstart[j] .. tstart[j + 1] - 1 (the host groups them by site)
+  int* sx;    // 2 * nx: the (at most two) sites occupied in x state a, -1 = none
+  int* sy;    // 2 * ny
   C* x;       // npc * E, this CTA's node blocks of the input
 };
 
@@ -73,6 +77,7 @@ __host__ __device__ inline size_t heom_smem_bytes(int nx, int ny, int n_sites, i
   size_t b = (size_t)npc * E * sizeof(C) + 2 * (size_t)npc * nterms * sizeof(C);
   b += ((size_t)nx * nx + ny * ny + (size_t)n_sites * (nx + ny) + E + npc) * sizeof(T);
   b += 2 * (size_t)npc * nterms * sizeof(int);
+  b += ((size_t)npc * (n_sites + 1) + 2 * (size_t)(nx + ny)) * sizeof(int);
   return b + 64;
 }
 
@@ -91,6 +96,9 @@ __device__ __forceinline__ HeomSmem<T> heom_carve(unsigned char* raw, const Heom
   s.shift = s.W + p.E;
   s.nbr = (int*)(s.shift + npc);
   s.site = s.nbr + npc * p.nterms;
+  s.tstart = s.site + npc * p.nterms;
+  s.sx = s.tstart + npc * (p.n_sites + 1);
+  s.sy = s.sx + 2 * p.nx;
   return s;
 }
 
@@ -131,6 +139,32 @@ __device__ __forceinline__ void heom_stage_smem(const HeomP& p, const typename c
   const C* xb = x + (b * p.nnodes + n0) * (int64_t)p.E;
   for (int i = tid; i < nn * p.E; i += nt) s.x[i] = xb[i];
   __syncthreads();
+  // per node, where each site's terms start (terms are grouped by site; a
+  // term whose site is out of range, or padding, belongs to no site)
+  for (int l = tid; l < npc; l += nt) {
+    int* ts = s.tstart + l * (p.n_sites + 1);
+    const int* st = s.site + l * p.nterms;
+    const int* nb = s.nbr + l * p.nterms;
+    int t = 0;
+    for (int j = 0; j <= p.n_sites; ++j) {
+      while (t < p.nterms && nb[t] >= 0 && st[t] < j) ++t;
+      ts[j] = t;
+    }
+  }
+  // the sites occupied in each state (number operators: at most two)
+  for (int i = tid; i < p.nx + p.ny; i += nt) {
+    const bool isx = i < p.nx;
+    const int st = isx ? i : i - p.nx;
+    const T* o = isx ? s.ox : s.oy;
+    const int n = isx ? p.nx : p.ny;
+    int found[2] = {-1, -1}, k = 0;
+    for (int j = 0; j < p.n_sites && k < 2; ++j)
+      if (o[j * n + st] != (T)0) found[k++] = j;
+    int* dst = isx ? s.sx + 2 * st : s.sy + 2 * st;
+    dst[0] = found[0];
+    dst[1] = found[1];
+  }
+  __syncthreads();
 }
 
 // k = RHS(x) for element e of local node `local` (global `node`) of sample b.
@@ -163,16 +197,24 @@ __device__ __forceinline__ void heom_rhs_elem(const HeomP& p, const typename cpl
   oi = fma(-sh, self.y, oi);
   const C* xb = x + b * (int64_t)p.nnodes * p.E;
   const int base = local * p.nterms;
-  for (int t = 0; t < p.nterms; ++t) {
-    const int nb = s.nbr[base + t];
-    if (nb < 0) continue;
-    const int j = s.site[base + t];
-    const C al = s.al[base + t], be = s.be[base + t];
+  const int* ts = s.tstart + local * (p.n_sites + 1);
+  // a term of site j weighs occ_j(a) alpha + occ_j(b) beta, so only the
+  // sites occupied in state a or state b contribute (each visited once)
+  const int js[4] = {s.sx[2 * a], s.sx[2 * a + 1], s.sy[2 * bb], s.sy[2 * bb + 1]};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = js[q];
+    if (j < 0) continue;
+    if (q >= 2 && (j == js[0] || j == js[1])) continue;
     const T oa = s.ox[j * p.nx + a], ob = s.oy[j * p.ny + bb];
-    const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
-    const C v = xb[(int64_t)nb * p.E + e];
-    orr = fma(fr, v.x, fma(-fi, v.y, orr));
-    oi = fma(fr, v.y, fma(fi, v.x, oi));
+    for (int t = base + ts[j]; t < base + ts[j + 1]; ++t) {
+      const int nb = s.nbr[t];
+      const C al = s.al[t], be = s.be[t];
+      const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
+      const C v = xb[(int64_t)nb * p.E + e];
+      orr = fma(fr, v.x, fma(-fi, v.y, orr));
+      oi = fma(fr, v.y, fma(fi, v.x, oi));
+    }
   }
   T uc;
   if constexpr (sizeof(T) == 4)

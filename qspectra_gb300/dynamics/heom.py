@@ -120,6 +120,9 @@ class HEOMTables:
                 for (m, j, a_, b_) in lst:
                     tt[m].append((n, j, a_, b_))
             terms = tt
+        # grouped by site (stable): the kernel visits only the sites a
+        # state occupies, through per-site ranges of this list
+        terms = [sorted(lst, key=lambda term: term[1]) for lst in terms]
         self.terms = terms
         nt = max(1, max(len(t) for t in terms))
         self.nterms = nt

@@ -38,7 +38,7 @@ class RedfieldBuild:
 
     def __init__(self, H, n_sites, hilbert_subspace, occ, bath, unit_convert,
                  secular=False, discard_imag_corr=False, evolve_basis='site',
-                 precision=_native.QSX_FP64):
+                 precision=_native.QSX_FP64, build_precision=None):
         self.H = H
         self.n = H.shape[-1]
         self.n_sites = n_sites
@@ -48,18 +48,36 @@ class RedfieldBuild:
         self.occ = _native.const_tensor(np.asarray(occ, dtype=np.float64), torch.float64,
                                         H.device)
         bounds = manifold_bounds(n_sites, hilbert_subspace)
-        if self.n <= EIGH_JACOBI_MAX:
-            self.E, self.U = _native.eigh(H, bounds, precision)
-        else:
+        if self.n > EIGH_JACOBI_MAX:
             raise _native.QsxError(
                 'Hilbert space of {} states exceeds the {}-state Redfield '
                 'build; use the operator-form third-order path'.format(
                     self.n, EIGH_JACOBI_MAX))
         self.site_ops = evolve_basis == 'site' and not secular
+        # the eigendecomposition and operator build run in FP64 unless an FP32
+        # build is asked for (it feeds only FP32 propagation)
+        if build_precision is None:
+            build_precision = _native.QSX_FP64
+        self.build_precision = build_precision
+        one_exciton = set(hilbert_subspace) <= set('ge') and 'e' in hilbert_subspace
+        off = 1 if 'g' in hilbert_subspace else 0
+        self.refined = (build_precision == _native.QSX_FP64 and precision == _native.QSX_FP32
+                        and self.site_ops and one_exciton and 2 <= n_sites <= 8
+                        and self.n == off + n_sites)
+        if self.refined:
+            # FP64 build for FP32 propagation: FP32 Jacobi, two FP64
+            # refinement steps, FP64 operators (qsx_redfield_build_w64)
+            _, U32 = _native.eigh(H, bounds, _native.QSX_FP32)
+            self.E, self.U, self.G, self.M = _native.redfield_build_w64(
+                H, U32, n_sites, off, bath, unit_convert, discard_imag_corr,
+                matsubara_cutoff=bath.matsubara_cutoff)
+            self.K = None
+            return
+        self.E, self.U = _native.eigh(H, bounds, build_precision)
         self.G, self.M, self.K = _native.redfield_operators(
             self.E, self.U, self.occ, bath, unit_convert, discard_imag_corr,
             site_basis=self.site_ops, matsubara_cutoff=bath.matsubara_cutoff,
-            precision=precision)
+            precision=build_precision)
 
     def propagator(self, idx, h, precision=_native.QSX_FP64, transpose=False):
         """(S, m, m) RK4 propagator D = P - I of the block ``idx`` (m <= 64).
@@ -132,15 +150,16 @@ class RedfieldModel(LiouvilleSpaceModel):
             self.hilbert_subspace, self.unit_convert, self.secular,
             self.discard_imag_corr, self.evolve_basis)
 
-    def build_batch(self, H, precision=_native.QSX_FP64):
-        """RedfieldBuild for a (S, n, n) batch of rotating-frame Hamiltonians;
-        precision QSX_FP32 evaluates the operator build in FP32 (for FP32
-        propagation)."""
+    def build_batch(self, H, precision=_native.QSX_FP64, build_precision=None):
+        """RedfieldBuild for a (S, n, n) batch of rotating-frame Hamiltonians.
+        ``precision`` is the propagation precision; the eigendecomposition
+        and operator build run in FP64 unless ``build_precision`` is
+        QSX_FP32 (an FP32 build, for FP32 propagation only)."""
         ham = self.hamiltonian
         return RedfieldBuild(H, ham.n_sites, self.hilbert_subspace,
                              ham.occupation_table(self.hilbert_subspace), ham.bath,
                              self.unit_convert, self.secular, self.discard_imag_corr,
-                             self.evolve_basis, precision)
+                             self.evolve_basis, precision, build_precision)
 
     def _build(self):
         if 'build' not in self._cache:

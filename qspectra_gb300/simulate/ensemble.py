@@ -309,10 +309,13 @@ def projected_mean(D, y0, proj, nsteps):
                        check_finite=False)
 
 
-def redfield_batch_build(model, batch, precision=_native.QSX_FP64):
+def redfield_batch_build(model, batch, precision=_native.QSX_FP64, build_precision=None):
+    """The batch's Redfield build: eigendecomposition and operators in FP64
+    (``build_precision`` QSX_FP32 asks for the FP32 build instead, valid for
+    FP32 propagation only)."""
     if not isinstance(model, RedfieldModel):
         raise NotImplementedError('batched ensembles need a RedfieldModel')
-    return model.build_batch(batch.H(model.hilbert_subspace), precision)
+    return model.build_batch(batch.H(model.hilbert_subspace), precision, build_precision)
 
 
 def sample_polarizations(polarization, rotations):
@@ -478,18 +481,29 @@ class RedfieldEnsembleWorkload:
         t_sym, _ = symmetric_grid(self.t_abs)
         self.dft_t0 = self.t_abs[0] - t_sym[t_sym.size // 2]
 
-    def run(self, offsets, precision='fp32', events=None):
-        """(spectrum (F,) float64, populations (T, n_sites) float64) on the GPU.
+    def run(self, offsets, precision='fp32', events=None, build_precision='fp64'):
+        """(spectrum (F,) float64, populations (T, n_sites) float64, status) on
+        the GPU.
 
-        ``offsets`` is a (S, n_sites) float64 CUDA tensor.  ``events`` (a dict)
-        collects CUDA events around the population propagation.
+        ``offsets`` is a (S, n_sites) float64 CUDA tensor.  ``precision`` is
+        the propagation precision; the eigendecomposition and Redfield build
+        run in ``build_precision`` ('fp64', or 'fp32' for an FP32 build
+        feeding FP32 propagation).  ``events`` (a dict) collects CUDA events
+        around the build and the population propagation.
         """
         from .utils import PRECISIONS
         prec = PRECISIONS[precision]
         S = offsets.shape[0]
         H = self.H_base.expand(S, -1, -1).clone()
         H[:, self.e_idx, self.e_idx] += offsets
-        build = self.model.build_batch(H, prec)
+        if events is not None:
+            a0 = torch.cuda.Event(enable_timing=True)
+            a0.record()
+        build = self.model.build_batch(H, prec, PRECISIONS[build_precision])
+        if events is not None:
+            a1 = torch.cuda.Event(enable_timing=True)
+            a1.record()
+            events.setdefault('build', []).append((a0, a1))
         # the absorption leg (eg propagator, time loop, DFT) runs on a side
         # stream, overlapping the population leg on the caller's stream
         main = torch.cuda.current_stream()
@@ -520,7 +534,7 @@ class RedfieldEnsembleWorkload:
         status = sig['status'] | pop['status']
         return X.real, pop['mean'].real, status
 
-    def capture(self, offsets, precision='fp32'):
+    def capture(self, offsets, precision='fp32', build_precision='fp64'):
         """Record one step as a CUDA graph on static buffers (a copy of
         ``offsets`` in, the outputs of ``run``), so that a step is one graph
         launch instead of some forty kernel launches and their host-side
@@ -533,16 +547,16 @@ class RedfieldEnsembleWorkload:
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.stream(side):
                 for _ in range(2):   # caches filled, workspaces allocated
-                    self.run(static_in, precision)
+                    self.run(static_in, precision, build_precision=build_precision)
             torch.cuda.current_stream().wait_stream(side)
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):
-                out = self.run(static_in, precision)
+                out = self.run(static_in, precision, build_precision=build_precision)
             torch.cuda.synchronize()
         except RuntimeError:
             torch.cuda.synchronize()
             return False
-        self._graph = (g, static_in, out, precision)
+        self._graph = (g, static_in, out, (precision, build_precision))
         return True
 
     def replay(self, offsets=None):
@@ -555,17 +569,17 @@ class RedfieldEnsembleWorkload:
         g.replay()
         return out
 
-    def run_host(self, offsets_host, precision='fp32'):
+    def run_host(self, offsets_host, precision='fp32', build_precision='fp64'):
         """End-to-end call with host buffers: pinned offsets in, numpy out
         (through the captured graph when one matches)."""
         dev = self.H_base.device
         graph = getattr(self, '_graph', None)
-        if (graph is not None and graph[3] == precision
+        if (graph is not None and graph[3] == (precision, build_precision)
                 and tuple(graph[1].shape) == tuple(offsets_host.shape)):
             X, pops, status = self.replay(offsets_host)
         else:
             off = offsets_host.to(dev, non_blocking=True)
-            X, pops, status = self.run(off, precision)
+            X, pops, status = self.run(off, precision, build_precision=build_precision)
         out = torch.cat([X, pops.reshape(-1), status.to(torch.float64)]).to('cpu')
         n = X.numel()
         raise_for_status(int(out[-1].item()))
