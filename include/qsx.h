@@ -376,7 +376,9 @@ typedef struct {
   int32_t nsteps;      /* RK4 steps */
   int32_t save_every;  /* output every save_every steps */
   int32_t save_nodes;  /* leading nodes saved per output (1 = physical rho) */
-  int32_t pad0;
+  int32_t variant;     /* 0: the library's choice (the persistent cluster form,
+                          one launch for the whole loop, when it fits); 1: one
+                          launch per RK4 stage */
   int64_t batch;       /* disorder samples */
   int64_t H_stride;    /* 0: Hx, Hy shared; else per sample [batch][n][n] */
   const double* Hx;    /* real [nx][nx], rotating frame */

@@ -59,7 +59,7 @@ class HeomArgs(ctypes.Structure):
         ('precision', ctypes.c_int32), ('nx', ctypes.c_int32), ('ny', ctypes.c_int32),
         ('nnodes', ctypes.c_int32), ('nterms', ctypes.c_int32), ('n_sites', ctypes.c_int32),
         ('nsteps', ctypes.c_int32), ('save_every', ctypes.c_int32),
-        ('save_nodes', ctypes.c_int32), ('pad0', ctypes.c_int32),
+        ('save_nodes', ctypes.c_int32), ('variant', ctypes.c_int32),
         ('batch', ctypes.c_int64), ('H_stride', ctypes.c_int64),
         ('Hx', _c_vp), ('Hy', _c_vp), ('occx', _c_vp), ('occy', _c_vp), ('W', _c_vp),
         ('shift', _c_vp), ('nbr', _c_vp), ('site', _c_vp), ('alpha', _c_vp), ('beta', _c_vp),
@@ -754,14 +754,17 @@ def heom_rhs(tables, Hx, Hy, x, unit_convert):
 
 def heom_rk4(tables, Hx, Hy, y0, nsteps, h, unit_convert, batch=None, save_every=1,
              save_nodes=1, precision=QSX_FP64, per_sample=True, mean=False,
-             check_finite=True):
-    """RK4 loop over the HEOM generator for all samples (qsx_heom_rk4)."""
+             check_finite=True, variant=0):
+    """RK4 loop over the HEOM generator for all samples (qsx_heom_rk4).
+    variant 0: the library's choice (one persistent cluster launch per call
+    when it fits); 1: one launch per RK4 stage."""
     require_gpu()
     y0 = _need(y0.to(torch.complex128).contiguous(), torch.complex128, 'y0')
     if batch is None:
         batch = Hx.shape[0] if Hx.dim() == 3 else (y0.shape[0] if y0.dim() == 2 else 1)
     a = _heom_args(tables, Hx, Hy, unit_convert, batch, precision)
     a.nsteps, a.save_every, a.save_nodes = nsteps, save_every, save_nodes
+    a.variant = int(variant)
     a.h = h
     a.y0, a.y0_stride = y0.data_ptr(), (1 if y0.dim() == 2 else 0)
     nsave = nsteps // save_every + 1

@@ -13,9 +13,13 @@
 // (-i m, +i m) and the down couplings (-i m c_k, +i m conj(c_k)).  The
 // transposed generator (Heisenberg picture) has the same form with the term
 // table transposed, which the host builds.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 
 #include "qsx_common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace qsx {
 
@@ -278,6 +282,226 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ------------------------------------------------ persistent cluster form
+// The whole RK4 loop in one launch: one thread-block cluster per disorder
+// sample, the hierarchy nodes split into contiguous ranges over its C CTAs.
+// Each CTA keeps the stage input of its nodes in shared memory, double
+// buffered, and its elements' state (split-word in FP32) and RK4
+// accumulator in registers; a node's commutator reads its own CTA's block,
+// the coupling terms read the neighbour nodes' blocks through distributed
+// shared memory.  One cluster barrier per stage publishes the stage input:
+// a CTA writes the next stage's input into the other buffer, which no peer
+// reads until after the next barrier.
+struct HeomCP {
+  int nx, ny, E, nnodes, nterms, n_sites, nsave, save_every, nsteps, keep;
+  int csize, npcta;
+  int64_t batch, Hx_stride, Hy_stride, y0_stride;
+  const double* Hx;
+  const double* Hy;
+  const double* occx;
+  const double* occy;
+  const double* W;
+  const double* shift;
+  const int* nbr;
+  const int* site;
+  const double2* alpha;
+  const double2* beta;
+  double uc, h;
+  const double2* y0;
+  double2* saves;   // [batch][nsave][keep * E]
+  int* status;
+};
+
+template <typename T>
+__host__ __device__ inline size_t heom_cluster_smem_bytes(int nx, int ny, int n_sites, int E,
+                                                          int npcta, int nterms) {
+  using C = typename cplx<T>::type;
+  size_t b = 2 * (size_t)npcta * E * sizeof(C);                        // stage inputs
+  b += 2 * (size_t)npcta * nterms * sizeof(C);                         // alpha, beta
+  b += ((size_t)nx * nx + ny * ny + (size_t)n_sites * (nx + ny) + E + npcta) * sizeof(T);
+  b += 2 * (size_t)npcta * nterms * sizeof(int);                       // nbr, site
+  b += ((size_t)npcta * (n_sites + 1) + 2 * (size_t)(nx + ny)) * sizeof(int);
+  return b + 64;
+}
+
+template <typename T, int EPT>
+__global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
+  using Cx = typename cplx<T>::type;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int64_t smp = blockIdx.x / p.csize;
+  const int E = p.E, nx = p.nx, ny = p.ny, N = p.n_sites, nt = p.nterms;
+  const int node0 = rank * p.npcta;
+  const int nloc = max(0, min(p.nnodes, node0 + p.npcta) - node0);
+  const int Mloc = nloc * E;
+  const int tid = threadIdx.x, bd = blockDim.x;
+
+  extern __shared__ __align__(16) unsigned char smraw[];
+  Cx* sx = (Cx*)smraw;                                  // [2][npcta E]
+  Cx* sal = sx + 2 * (size_t)p.npcta * E;               // [npcta nterms]
+  Cx* sbe = sal + (size_t)p.npcta * nt;
+  T* sHx = (T*)(sbe + (size_t)p.npcta * nt);
+  T* sHy = sHx + nx * nx;
+  T* sox = sHy + ny * ny;
+  T* soy = sox + N * nx;
+  T* sW = soy + N * ny;
+  T* ssh = sW + E;
+  int* snb = (int*)(ssh + p.npcta);
+  int* sst = snb + p.npcta * nt;
+  int* sts = sst + p.npcta * nt;                        // [npcta][N + 1]
+  int* ssx = sts + p.npcta * (N + 1);                   // [nx][2]
+  int* ssy = ssx + 2 * nx;                              // [ny][2]
+
+  const double* hx = p.Hx + smp * p.Hx_stride;
+  const double* hy = p.Hy + smp * p.Hy_stride;
+  for (int i = tid; i < nx * nx; i += bd) sHx[i] = (T)hx[i];
+  for (int i = tid; i < ny * ny; i += bd) sHy[i] = (T)hy[i];
+  for (int i = tid; i < N * nx; i += bd) sox[i] = (T)p.occx[i];
+  for (int i = tid; i < N * ny; i += bd) soy[i] = (T)p.occy[i];
+  for (int i = tid; i < E; i += bd) sW[i] = p.W ? (T)p.W[i] : (T)0;
+  for (int i = tid; i < p.npcta; i += bd) ssh[i] = i < nloc ? (T)p.shift[node0 + i] : (T)0;
+  for (int i = tid; i < p.npcta * nt; i += bd) {
+    const bool ok = i < nloc * nt;
+    const int g = node0 * nt + i;
+    snb[i] = ok ? p.nbr[g] : -1;
+    sst[i] = ok ? p.site[g] : 0;
+    const double2 a = ok ? p.alpha[g] : make_double2(0.0, 0.0);
+    const double2 b = ok ? p.beta[g] : make_double2(0.0, 0.0);
+    sal[i] = cmk((T)a.x, (T)a.y);
+    sbe[i] = cmk((T)b.x, (T)b.y);
+  }
+  __syncthreads();
+  for (int l = tid; l < p.npcta; l += bd) {
+    int t = 0;
+    for (int j = 0; j <= N; ++j) {
+      while (t < nt && snb[l * nt + t] >= 0 && sst[l * nt + t] < j) ++t;
+      sts[l * (N + 1) + j] = t;
+    }
+  }
+  for (int i = tid; i < nx + ny; i += bd) {
+    const bool isx = i < nx;
+    const int st = isx ? i : i - nx;
+    const T* o = isx ? sox : soy;
+    const int n = isx ? nx : ny;
+    int found[2] = {-1, -1}, k = 0;
+    for (int j = 0; j < N && k < 2; ++j)
+      if (o[j * n + st] != (T)0) found[k++] = j;
+    int* dst = isx ? ssx + 2 * st : ssy + 2 * st;
+    dst[0] = found[0];
+    dst[1] = found[1];
+  }
+
+  // this thread's elements: state (split-word in FP32) and RK4 accumulator
+  Cx yh[EPT], yl[EPT], acc[EPT];
+  const double2* y0 = p.y0 + smp * p.y0_stride;
+#pragma unroll
+  for (int u = 0; u < EPT; ++u) {
+    const int el = tid + u * bd;
+    yh[u] = yl[u] = acc[u] = cmk((T)0, (T)0);
+    if (el < Mloc) {
+      const double2 v = y0[(int64_t)node0 * E + el];
+      yh[u] = cmk((T)v.x, (T)v.y);
+      if (sizeof(T) == 4) yl[u] = cmk((T)(v.x - (double)yh[u].x), (T)(v.y - (double)yh[u].y));
+      sx[el] = yh[u];   // stage 0 input of step 0, buffer 0
+    }
+  }
+  const T h = (T)p.h, uc = (T)p.uc;
+  auto save = [&](int k) {
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) {
+      const int el = tid + u * bd;
+      const int node = node0 + el / E;
+      if (el >= Mloc || node >= p.keep) continue;
+      double vx = (double)yh[u].x, vy = (double)yh[u].y;
+      if (sizeof(T) == 4) {
+        vx += (double)yl[u].x;
+        vy += (double)yl[u].y;
+      }
+      if (p.status && !(isfinite(vx) && isfinite(vy))) atomicOr(p.status, QSX_ERR_NONFINITE);
+      p.saves[(smp * p.nsave + k) * (int64_t)p.keep * E + (int64_t)node * E + el % E] =
+          make_double2(vx, vy);
+    }
+  };
+  save(0);
+  for (int step = 0; step < p.nsteps; ++step) {
+    for (int stage = 0; stage < 4; ++stage) {
+      const int buf = stage & 1;   // 4 stages per step: the parity pattern repeats
+      cluster.sync();              // this stage's input is complete cluster-wide
+      const Cx* xin = sx + (size_t)buf * p.npcta * E;
+      Cx* xout = sx + (size_t)(buf ^ 1) * p.npcta * E;
+      const T cnext = stage == 2 ? h : (T)0.5 * h;
+      const T wg = (stage == 0 || stage == 3) ? (T)1 : (T)2;
+#pragma unroll
+      for (int u = 0; u < EPT; ++u) {
+        const int el = tid + u * bd;
+        if (el >= Mloc) continue;
+        const int l = el / E, e = el % E;
+        const int a = e % nx, bb = e / nx;
+        const Cx* xs = xin + l * E;
+        // -i (Hx x - x Hy)[a][bb]
+        T cr = 0, ci = 0;
+        for (int c = 0; c < nx; ++c) {
+          const T hv = sHx[a * nx + c];
+          const Cx v = xs[c + nx * bb];
+          cr = fma(hv, v.x, cr);
+          ci = fma(hv, v.y, ci);
+        }
+        for (int c = 0; c < ny; ++c) {
+          const T hv = sHy[c * ny + bb];
+          const Cx v = xs[a + nx * c];
+          cr = fma(-hv, v.x, cr);
+          ci = fma(-hv, v.y, ci);
+        }
+        const Cx self = xs[e];
+        T orr = ci, oi = -cr;
+        const T sh = ssh[l] + sW[e];
+        orr = fma(-sh, self.x, orr);
+        oi = fma(-sh, self.y, oi);
+        // couplings of the sites occupied in state a or state bb
+        const int* ts = sts + l * (N + 1);
+        const int js[4] = {ssx[2 * a], ssx[2 * a + 1], ssy[2 * bb], ssy[2 * bb + 1]};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int j = js[q];
+          if (j < 0) continue;
+          if (q >= 2 && (j == js[0] || j == js[1])) continue;
+          const T oa = sox[j * nx + a], ob = soy[j * ny + bb];
+          for (int t = l * nt + ts[j]; t < l * nt + ts[j + 1]; ++t) {
+            const int m = snb[t];
+            const int r = m / p.npcta, ml = m - r * p.npcta;
+            const Cx* src = r == rank ? xin : cluster.map_shared_rank(xin, r);
+            const Cx v = src[ml * E + e];
+            const Cx al = sal[t], be = sbe[t];
+            const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
+            orr = fma(fr, v.x, fma(-fi, v.y, orr));
+            oi = fma(fr, v.y, fma(fi, v.x, oi));
+          }
+        }
+        const Cx d = cmk(uc * orr, uc * oi);
+        acc[u] = stage == 0 ? d : cmk(acc[u].x + wg * d.x, acc[u].y + wg * d.y);
+        if (stage < 3) {
+          xout[el] = cmk(yh[u].x + cnext * d.x, yh[u].y + cnext * d.y);
+        } else {
+          const T s6 = h / (T)6;
+          if (sizeof(T) == 4) {
+            float hxv = (float)yh[u].x, lxv = (float)yl[u].x, hyv = (float)yh[u].y,
+                  lyv = (float)yl[u].y;
+            dd_add(hxv, lxv, (float)(s6 * acc[u].x));
+            dd_add(hyv, lyv, (float)(s6 * acc[u].y));
+            yh[u] = cmk((T)hxv, (T)hyv);
+            yl[u] = cmk((T)lxv, (T)lyv);
+          } else {
+            yh[u] = cmk(yh[u].x + s6 * acc[u].x, yh[u].y + s6 * acc[u].y);
+          }
+          xout[el] = yh[u];
+        }
+      }
+    }
+    if ((step + 1) % p.save_every == 0) save((step + 1) / p.save_every);
+  }
+  cluster.sync();  // peers may still read this CTA's buffers
+}
+
 // out = RHS(x) in FP64 (the equation of motion as a callable).
 __global__ void __launch_bounds__(256)
     heom_rhs_kernel(HeomP p, const double2* __restrict__ x, double2* __restrict__ out, int npc) {
@@ -387,6 +611,94 @@ static HeomP heom_params(const qsx_heom_args* a) {
   return p;
 }
 
+template <typename T, int EPT>
+static cudaError_t launch_heom_cluster(const HeomCP& p, size_t smem, cudaStream_t s,
+                                       int* clusters) {
+  auto kern = heom_cluster_kernel<T, EPT>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(p.batch * p.csize));
+  cfg.blockDim = dim3(512);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)p.csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  *clusters = 0;
+  e = cudaOccupancyMaxActiveClusters(clusters, kern, &cfg);
+  if (e != cudaSuccess || *clusters < 1) return e;
+  return cudaLaunchKernelEx(&cfg, kern, p);
+}
+
+// The persistent cluster form when the shapes allow it: returns 1 if it ran
+// (or failed with *st set), 0 to fall back to the per-stage kernels.
+template <typename T>
+static int heom_rk4_cluster(const qsx_heom_args* a, double2* saves, cudaStream_t s, int* st) {
+  const int E = a->nx * a->ny;
+  const int C = std::min(8, a->nnodes);
+  const int npcta = (a->nnodes + C - 1) / C;
+  const int ept = (npcta * E + 511) / 512;
+  const size_t smem =
+      heom_cluster_smem_bytes<T>(a->nx, a->ny, a->n_sites, E, npcta, std::max(a->nterms, 1));
+  if (ept > 16 || smem > 200 * 1024) return 0;
+  HeomCP p;
+  p.nx = a->nx;
+  p.ny = a->ny;
+  p.E = E;
+  p.nnodes = a->nnodes;
+  p.nterms = std::max(a->nterms, 0);
+  p.n_sites = a->n_sites;
+  p.nsave = a->nsteps / a->save_every + 1;
+  p.save_every = a->save_every;
+  p.nsteps = a->nsteps;
+  p.keep = a->save_nodes;
+  p.csize = C;
+  p.npcta = npcta;
+  p.batch = a->batch;
+  p.Hx_stride = a->H_stride ? (int64_t)a->nx * a->nx : 0;
+  p.Hy_stride = a->H_stride ? (int64_t)a->ny * a->ny : 0;
+  p.y0_stride = a->y0_stride ? (int64_t)a->nnodes * E : 0;
+  p.Hx = a->Hx;
+  p.Hy = a->Hy;
+  p.occx = a->occx;
+  p.occy = a->occy;
+  p.W = a->W;
+  p.shift = a->shift;
+  p.nbr = a->nbr;
+  p.site = a->site;
+  p.alpha = (const double2*)a->alpha;
+  p.beta = (const double2*)a->beta;
+  p.uc = a->unit_convert;
+  p.h = a->h;
+  p.y0 = (const double2*)a->y0;
+  p.saves = saves;
+  p.status = a->status;
+  int clusters = 0;
+  cudaError_t e;
+  if (ept <= 1)
+    e = launch_heom_cluster<T, 1>(p, smem, s, &clusters);
+  else if (ept <= 2)
+    e = launch_heom_cluster<T, 2>(p, smem, s, &clusters);
+  else if (ept <= 4)
+    e = launch_heom_cluster<T, 4>(p, smem, s, &clusters);
+  else if (ept <= 8)
+    e = launch_heom_cluster<T, 8>(p, smem, s, &clusters);
+  else
+    e = launch_heom_cluster<T, 16>(p, smem, s, &clusters);
+  if (e != cudaSuccess) {
+    *st = cuda_status(e, "qsx_heom_rk4 (cluster form)");
+    return 1;
+  }
+  if (clusters < 1) return 0;   // cannot be scheduled: per-stage kernels
+  return 1;
+}
+
 static size_t heom_state_elems(const qsx_heom_args* a) {
   return (size_t)a->batch * a->nnodes * a->nx * a->ny;
 }
@@ -487,6 +799,22 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
   auto run = [&](auto tag) -> int {
     using T = decltype(tag);
     using C = typename cplx<T>::type;
+    if (a->variant != 1) {
+      // the whole loop in one launch, one cluster per sample
+      double2* saves = (double2*)(((size_t)ws + 255) & ~(size_t)255);
+      double2* dst = node0 ? node0 : saves;
+      int cst = QSX_OK;
+      if (heom_rk4_cluster<T>(a, dst, s, &cst)) {
+        if (cst) return cst;
+        if (a->out_mean) {
+          const int64_t m = (int64_t)p.nsave * keep * p.E;
+          heom_mean_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(
+              dst, p.batch, m, 1.0 / (double)p.batch, (double2*)a->out_mean);
+          QSX_LAUNCH_CHECK("qsx_heom_rk4 mean");
+        }
+        return QSX_OK;
+      }
+    }
     C* yh = (C*)ws;
     C* yl = sizeof(T) == 4 ? yh + n : nullptr;
     C* acc = (sizeof(T) == 4 ? yl : yh) + n;

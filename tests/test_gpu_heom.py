@@ -72,3 +72,27 @@ def test_heom_fp32_split_word_and_batch():
         L = om.eom_matrix('ee')
         ref = orc.rk4_integrate_sparse(L, y0.cpu().numpy(), 400, 0.5, save_every=20)
         assert rel_err(r64['state'][s].cpu().numpy(), ref[:, :16]) < 1e-10
+
+
+@pytest.mark.parametrize('tag,kw', CASES)
+@pytest.mark.parametrize('heis', [False, True])
+@pytest.mark.parametrize('precision,tol', [(_native.QSX_FP64, 1e-12), (_native.QSX_FP32, 1e-5)])
+def test_heom_cluster_form_matches_per_stage_form(golden, tag, kw, heis, precision, tol):
+    """The persistent cluster kernel (whole loop in one launch, node ranges
+    over the cluster's CTAs, neighbours through distributed shared memory)
+    against the per-stage kernels, on every generator case, both pictures,
+    with per-sample Hamiltonians and all nodes saved."""
+    m = model2(golden, **kw)
+    tb = m.tables('ee', transpose=heis)
+    S = 3
+    base = m.hamiltonian.H('e')
+    rng = np.random.RandomState(4)
+    Hb = torch.as_tensor(np.array([base + np.diag(rng.randn(2) * 30) for _ in range(S)])).cuda()
+    E = tb.nx * tb.ny
+    y0 = torch.as_tensor(rng.randn(S, m.ado_count * E) + 1j * rng.randn(S, m.ado_count * E)).cuda()
+    out = []
+    for variant in (0, 1):
+        out.append(_native.heom_rk4(tb, Hb, Hb, y0, 60, 0.5, qg.CM_FS, batch=S, save_every=6,
+                                    save_nodes=m.ado_count, precision=precision,
+                                    variant=variant)['state'].cpu().numpy())
+    assert rel_err(out[0], out[1]) < tol
