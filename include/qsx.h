@@ -118,6 +118,28 @@ int qsx_redfield_build_w64(const double* H, int n, int off, int n_sites,
                            void* stream);
 
 /*
+ * Batched dense product C = alpha A B + beta Cin for the third-order
+ * engine's many-right-hand-side steps (the t2 integrate over len(t1) states
+ * and the einsum('ci,abi') contraction of qspectra/simulate/response.py:
+ * 321-336, and the operator transforms and propagator powers behind them).
+ * mode 0: real A, B, C; 1: complex A, B, C; 2: complex A, real B; 3: real A,
+ * complex B (C complex for modes 1-3).  Complex values are interleaved
+ * {re, im}.  A [batch][M][K] row-major with row stride lda and batch stride
+ * strideA (0 = shared), likewise B [K][N] and C, Cin [M][N]; strides count
+ * elements of the operand's own type.  Cin may be NULL (then beta is
+ * ignored) or C itself; C must not alias A or B.  QSX_FP32 runs on the
+ * tensor cores (tcgen05, 3xTF32 with FP32 accumulation; status, may be
+ * NULL, receives QSX_ERR_CUDA if a completion wait times out), QSX_FP64 on
+ * the CUDA cores.  batch <= 65535, K >= 1.
+ */
+int qsx_gemm_batched(int precision, int mode, int64_t batch, int M, int N, int K,
+                     const void* A, int64_t lda, int64_t strideA,
+                     const void* B, int64_t ldb, int64_t strideB,
+                     const void* Cin, int64_t ldcin, int64_t strideCin, double beta,
+                     void* C, int64_t ldc, int64_t strideC, double alpha,
+                     int32_t* status, void* stream);
+
+/*
  * Dense Liouvillian block L[idx, idx] (transposed when transpose != 0, the
  * Heisenberg picture).  Replaces RedfieldModel.evolution_super_operator
  * (qspectra/dynamics/redfield.py:95-104, 146-152) sliced by

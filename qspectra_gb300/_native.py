@@ -145,6 +145,9 @@ _PROTOS = {
     'qsx_redfield_build_w64': (_c_int, [_c_vp, _c_int, _c_int, _c_int, _c_i64, _c_vp, _c_dbl,
                                         _c_dbl, _c_dbl, _c_int, _c_int, _c_dbl, _c_vp, _c_vp,
                                         _c_vp, _c_vp, _c_vp]),
+    'qsx_gemm_batched': (_c_int, [_c_int, _c_int, _c_i64, _c_int, _c_int, _c_int, _c_vp,
+                                  _c_i64, _c_i64, _c_vp, _c_i64, _c_i64, _c_vp, _c_i64, _c_i64,
+                                  _c_dbl, _c_vp, _c_i64, _c_i64, _c_dbl, _c_vp, _c_vp]),
     'qsx_dft_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
                                  _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_fblock_tensor': (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_vp, _c_i64, _c_dbl,
@@ -273,6 +276,53 @@ def redfield_operators(E, U, occ, bath, unit_convert, discard_imag_corr=False,
         int(site_basis), int(precision), _p(G), _p(M), _p(K), _stream()),
         'qsx_redfield_operators_batched')
     return G, M, K
+
+
+def gemm(A, B, out=None, Cin=None, alpha=1.0, beta=1.0, status=None):
+    """Batched out = alpha A B (+ beta Cin) on the GPU (qsx_gemm_batched): FP32
+    operands on the tensor cores (3xTF32), FP64 on the CUDA cores.
+
+    A (S, M, K) and B (S, K, N), either of them 2-D to share it across the
+    batch; real or complex of one precision (float32/complex64 or
+    float64/complex128); the result is complex when either operand is.  The
+    last dimension of every operand must be contiguous.  ``out`` must not
+    overlap A or B; Cin may be ``out`` itself."""
+    require_gpu()
+    if A.dim() not in (2, 3) or B.dim() not in (2, 3):
+        raise ValueError('gemm operands must be 2-D or 3-D')
+    single = A.dtype in (torch.float32, torch.complex64)
+    if single != (B.dtype in (torch.float32, torch.complex64)):
+        raise TypeError('gemm operands must share one precision')
+    ca, cb = A.is_complex(), B.is_complex()
+    mode = {(False, False): 0, (True, True): 1, (True, False): 2, (False, True): 3}[(ca, cb)]
+    if A.stride(-1) != 1 or B.stride(-1) != 1:
+        raise ValueError('gemm operands need a contiguous last dimension')
+    S = max(A.shape[0] if A.dim() == 3 else 1, B.shape[0] if B.dim() == 3 else 1)
+    M, K = A.shape[-2], A.shape[-1]
+    if B.shape[-2] != K:
+        raise ValueError('gemm: inner sizes differ ({} vs {})'.format(K, B.shape[-2]))
+    N = B.shape[-1]
+    cdt = (torch.complex64 if single else torch.complex128) if (ca or cb) else A.dtype
+    if out is None:
+        out = torch.empty((S, M, N), dtype=cdt, device=A.device)
+    if out.dtype != cdt or out.shape[-2:] != (M, N) or out.stride(-1) != 1:
+        raise ValueError('gemm: bad output tensor')
+    sa = A.stride(0) if A.dim() == 3 else 0
+    sb = B.stride(0) if B.dim() == 3 else 0
+    so = out.stride(0) if out.dim() == 3 else 0
+    if Cin is not None:
+        if Cin.dtype != cdt or Cin.shape[-2:] != (M, N) or Cin.stride(-1) != 1:
+            raise ValueError('gemm: bad Cin tensor')
+        sc, ldc_in = (Cin.stride(0) if Cin.dim() == 3 else 0), Cin.stride(-2)
+    else:
+        sc, ldc_in, beta = 0, 0, 0.0
+    _check(load().qsx_gemm_batched(
+        QSX_FP32 if single else QSX_FP64, mode, S, M, N, K,
+        _p(A), A.stride(-2), sa, _p(B), B.stride(-2), sb,
+        _p(Cin) if Cin is not None else None, ldc_in, sc, float(beta),
+        _p(out), out.stride(-2), so, float(alpha),
+        _p(status) if status is not None else None, _stream()), 'qsx_gemm_batched')
+    return out
 
 
 def redfield_build_w64(H, U_approx, n_sites, off, bath, unit_convert, discard_imag_corr=False,

@@ -17,9 +17,10 @@ from qspectra_gb300.operator_tools import occupation_table
 pytestmark = pytest.mark.gpu
 
 
-def ge_hamiltonians(N, B, seed):
+def ge_hamiltonians(N, B, seed, degenerate=True):
     """(B, N + 1, N + 1) rotating-frame 'ge' Hamiltonians: ground state 0,
-    disordered one-exciton block."""
+    disordered one-exciton block; ``degenerate`` plants equal and nearly
+    equal eigenvalues in a few of them."""
     rng = np.random.RandomState(seed)
     H = np.zeros((B, N + 1, N + 1))
     J = np.triu(rng.normal(0, 50, (B, N, N)), 1)
@@ -28,13 +29,13 @@ def ge_hamiltonians(N, B, seed):
     H[:, idx, idx] = rng.uniform(-300, 300, (B, N))
     # exactly and nearly degenerate eigenvalues in a random eigenbasis, and
     # an exactly diagonal block
-    for k, gap in zip(range(1, min(B, 6)), (0.0, 1e-9, 1e-5, 1e-3, 1.0)):
+    for k, gap in zip(range(1, min(B, 6) if degenerate else 1), (0.0, 1e-9, 1e-5, 1e-3, 1.0)):
         lam = np.sort(rng.uniform(-300, 300, N))
         lam[1] = lam[0] + gap
         Q, _ = np.linalg.qr(rng.randn(N, N))
         blk = Q @ np.diag(lam) @ Q.T
         H[k, 1:, 1:] = 0.5 * (blk + blk.T)
-    if B > 6:
+    if B > 6 and degenerate:
         H[6, 1:, 1:] = np.diag(np.diag(H[6, 1:, 1:]))
     return H
 
@@ -51,15 +52,21 @@ def test_refined_eigenpairs_are_fp64_accurate(N):
     for b in range(B):
         A = Hn[b]
         scale = np.abs(A).max()
-        assert np.max(np.abs(E[b] - np.linalg.eigvalsh(A))) < 1e-13 * scale
+        # ascending inside each block: the ground state, then the one-exciton block
+        assert E[b, 0] == 0.0
+        assert np.max(np.abs(E[b, 1:] - np.linalg.eigvalsh(A[1:, 1:]))) < 1e-13 * scale
         assert np.max(np.abs(U[b] @ np.diag(E[b]) @ U[b].T - A)) < 1e-13 * scale
         assert np.max(np.abs(U[b].T @ U[b] - np.eye(N + 1))) < 1e-13
 
 
 @pytest.mark.parametrize('N,discard', [(7, False), (4, False), (6, True)])
 def test_fp64_build_matches_plain_fp64_build(N, discard):
+    """Generic (non-degenerate) spectra: the reference's correlation function
+    takes a separate value at exactly zero frequency (bath.py:84-102), so at
+    an exact degeneracy the operators depend on whether a difference of two
+    computed eigenvalues rounds to zero."""
     B = 300
-    H = torch.as_tensor(ge_hamiltonians(N, B, seed=10 + N)).cuda()
+    H = torch.as_tensor(ge_hamiltonians(N, B, seed=10 + N, degenerate=False)).cuda()
     bath = qg.DebyeBath(qg.CM_K * 77, 35, 106)
     occ = occupation_table(N, 'ge')
     ref = RedfieldBuild(H, N, 'ge', occ, bath, qg.CM_FS, discard_imag_corr=discard,
