@@ -56,6 +56,9 @@ def parse_args():
                    help='disorder samples of the single-process reference timing')
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--fp64-steps', type=int, default=2)
+    p.add_argument('--build', choices=['fp32', 'fp64'], default='fp32',
+                   help='precision of the eigendecomposition and Redfield build of the '
+                        'timed FP32 step (the other one is measured beside)')
     p.add_argument('--no-heom', action='store_true')
     p.add_argument('--only-heom', action='store_true',
                    help='run only the HEOM ring workload (for profiling)')
@@ -631,7 +634,7 @@ def our_arm(args):
         torch.cuda.synchronize()
 
     for _ in range(args.warmup):
-        work.run(off, 'fp32')
+        work.run(off, 'fp32', build_precision=args.build)
     barrier()
     clk = clocks_start(local) if rank == 0 else None
     if clk is not None:
@@ -640,7 +643,7 @@ def our_arm(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(args.steps):
-        X32, P32, status = work.run(off, 'fp32', events)
+        X32, P32, status = work.run(off, 'fp32', events, build_precision=args.build)
     e1.record()
     barrier()
     eager_ms = e0.elapsed_time(e1) / args.steps
@@ -649,7 +652,7 @@ def our_arm(args):
     # succeeds it is the timed form for `value`, and the end-to-end calls
     # below go through run_host, which replays it; the eager time is
     # reported beside
-    graph_ok = (not args.no_graph) and work.capture(off, 'fp32')
+    graph_ok = (not args.no_graph) and work.capture(off, 'fp32', build_precision=args.build)
     ms = eager_ms
     graph_ms = None
     if graph_ok:
@@ -683,11 +686,11 @@ def our_arm(args):
 
     # end to end through the library call with host buffers
     for _ in range(2):
-        work.run_host(off_host, 'fp32')
+        work.run_host(off_host, 'fp32', build_precision=args.build)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        Xh, Ph = work.run_host(off_host, 'fp32')
+        Xh, Ph = work.run_host(off_host, 'fp32', build_precision=args.build)
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
     if world > 1:
@@ -707,6 +710,35 @@ def our_arm(args):
     fp64_ms = f0.elapsed_time(f1) / args.fp64_steps
     err_spec = float((X32 - X64).abs().max() / X64.abs().max())
     err_pop = float((P32 - P64).abs().max() / P64.abs().max())
+    # the other build precision beside: the FP64 build (FP64 eigenpairs and
+    # Redfield operators feeding FP32 propagation) or the FP32 build
+    other = 'fp64' if args.build == 'fp32' else 'fp32'
+    for _ in range(2):
+        work.run(off, 'fp32', build_precision=other)
+    torch.cuda.synchronize()
+    o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev_other = {}
+    o0.record()
+    for _ in range(args.fp64_steps + 3):
+        Xo, Po, _ = work.run(off, 'fp32', ev_other, build_precision=other)
+    o1.record()
+    torch.cuda.synchronize()
+    other_ms = o0.elapsed_time(o1) / (args.fp64_steps + 3)
+    build_ms = {args.build: statistics.mean(a.elapsed_time(b) for a, b in events['build']),
+                other: statistics.mean(a.elapsed_time(b) for a, b in ev_other['build'])}
+    precision_forms = {
+        'value_form': {'build': args.build, 'propagation': 'fp32 split-word',
+                       'ms_per_step': ms, 'build_ms': build_ms[args.build],
+                       'rel_err_vs_fp64': {'spectrum': err_spec, 'populations': err_pop}},
+        'other_form': {'build': other, 'propagation': 'fp32 split-word',
+                       'ms_per_step_eager': other_ms, 'spectra_per_s_eager': 1000.0 / other_ms,
+                       'build_ms': build_ms[other],
+                       'rel_err_vs_fp64': {
+                           'spectrum': float((Xo - X64).abs().max() / X64.abs().max()),
+                           'populations': float((Po - P64).abs().max() / P64.abs().max())}},
+        'note': ('fp64 build = FP64 eigenpairs (FP32 Jacobi refined in FP64) and FP64 '
+                 'Redfield operators (qsx_redfield_build_w64); fp32 build = the same formulas '
+                 'in FP32; propagation FP32 split-word either way')}
 
     heom = heom_ring8(torch, qg, _native) if rank == 0 and not args.no_heom else None
     third = (third_order_chain24(torch, qg, samples=args.third_samples)
@@ -731,12 +763,14 @@ def our_arm(args):
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'f32/c64 split-word (FP32 build and propagation; populations in the '
-                 'real Hermitian form)',
+        'dtype': ('f32/c64 split-word propagation (populations in the real Hermitian form) '
+                  'after an {} eigendecomposition and Redfield build'.format(
+                      'FP64' if args.build == 'fp64' else 'FP32')),
         'data': 'synthetic (seeded Hamiltonians and disorder draws)',
         'config': dict(CONFIG, parallelism='replicas (weak: each GPU runs its own '
                                            '16384-sample ensemble)' if world > 1 else 'single GPU'),
         'fp32_vs_fp64_rel_err': {'spectrum': err_spec, 'populations': err_pop},
+        'precision_forms': precision_forms,
         'step_launch': ({'value': ('captured CUDA graph (replay)' if ms == graph_ms
                                    else 'eager launches (replay differed)'),
                          'e2e': 'captured CUDA graph (run_host)',

@@ -94,14 +94,23 @@ int qsx_redfield_operators_batched(const double* E, const double* U, int n,
                                    void* stream);
 
 /*
+ * Rotating-frame Hamiltonians of disorder samples: H[s] = base + diag of
+ * offsets[s] ([batch][n_sites]) on rows/columns [off, off + n_sites) of the
+ * shared n x n base (the site-energy shifts of Hamiltonian.sample,
+ * qspectra/hamiltonian.py:552-578).  H [batch][n][n] double.
+ */
+int qsx_disordered_hamiltonians(const double* base, int n, const double* offsets,
+                                int64_t batch, int n_sites, int off, double* H,
+                                void* stream);
+
+/*
  * FP64 build for one-exciton Hilbert spaces ('e', 'ge'; 2 <= n_sites <= 8),
  * one warp per sample: the eigendecomposition of the rotating-frame H
- * (Hamiltonian.eig, qspectra/hamiltonian.py:310-328) from approximate
- * eigenvectors X: two FP64 Newton-Schulz steps make X orthonormal, then
- * cyclic FP64 Jacobi sweeps diagonalise S = X^T H X, rotating X along (the
- * low-precision-preconditioned Jacobi method); then the site-basis Redfield
- * operators G and M_i of qsx_redfield_operators_batched (site_basis != 0),
- * all in FP64.
+ * (Hamiltonian.eig, qspectra/hamiltonian.py:310-328) refined to FP64 from
+ * approximate eigenvectors X (two Ogita-Aishima steps R = I - X^T X,
+ * S = X^T H X, X <- X + X F, with close pairs finished by FP64 Jacobi
+ * rotations), then the site-basis Redfield operators G and M_i of
+ * qsx_redfield_operators_batched (site_basis != 0), all in FP64.
  * The coupled block is rows/columns [off, off + n_sites) of each n x n H
  * (n <= 32); states outside it are uncoupled 1 x 1 blocks.  U_approx holds
  * approximate eigenvectors of that block (e.g. from qsx_eigh_batched_prec
@@ -113,9 +122,22 @@ int qsx_redfield_build_w64(const double* H, int n, int off, int n_sites,
                            int64_t batch, const double* U_approx,
                            double temperature, double reorg_energy,
                            double cutoff_freq, int matsubara_cutoff,
-                           int discard_imag_corr, double unit_convert,
+                           int discard_imag_corr, const double* corr_table,
+                           int corr_pieces, double corr_width, double unit_convert,
                            double* E, double* U, double* G, double* M,
                            void* stream);
+/* The Matsubara sum S(x) = sum_{k=1}^{K-1} nu_k / ((nu_k^2 - gamma^2)
+ * (nu_k - i x)), nu_k = 2 pi k T, of the Debye correlation function
+ * (qspectra/bath.py:95-102) as a piecewise Chebyshev table: piece j covers
+ * x in [j width, (j + 1) width) with qsx_debye_matsubara_table_degree()
+ * complex coefficients, fitted in FP64 to the direct sum; computed on the
+ * host into coef (host memory, [pieces][degree] complex128).  The FP64
+ * build takes it (device copy) as corr_table, corr_pieces, corr_width and
+ * evaluates C(x) there by Clenshaw's recurrence, using the closed form
+ * beyond the table or when corr_table is NULL. */
+int qsx_debye_matsubara_table(double temperature, double cutoff_freq, int matsubara_cutoff,
+                              int pieces, double width, double* coef);
+int qsx_debye_matsubara_table_degree(void);
 
 /*
  * Batched dense product C = alpha A B + beta Cin for the third-order

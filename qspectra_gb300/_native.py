@@ -143,8 +143,12 @@ _PROTOS = {
     'qsx_heom_rhs': (_c_int, [ctypes.POINTER(HeomArgs), _c_vp, _c_vp, _c_vp]),
     'qsx_heom_rk4': (_c_int, [ctypes.POINTER(HeomArgs), _c_vp]),
     'qsx_redfield_build_w64': (_c_int, [_c_vp, _c_int, _c_int, _c_int, _c_i64, _c_vp, _c_dbl,
-                                        _c_dbl, _c_dbl, _c_int, _c_int, _c_dbl, _c_vp, _c_vp,
-                                        _c_vp, _c_vp, _c_vp]),
+                                        _c_dbl, _c_dbl, _c_int, _c_int, _c_vp, _c_int, _c_dbl,
+                                        _c_dbl, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    'qsx_debye_matsubara_table': (_c_int, [_c_dbl, _c_dbl, _c_int, _c_int, _c_dbl, _c_vp]),
+    'qsx_debye_matsubara_table_degree': (_c_int, []),
+    'qsx_disordered_hamiltonians': (_c_int, [_c_vp, _c_int, _c_vp, _c_i64, _c_int, _c_int,
+                                             _c_vp, _c_vp]),
     'qsx_gemm_batched': (_c_int, [_c_int, _c_int, _c_i64, _c_int, _c_int, _c_int, _c_vp,
                                   _c_i64, _c_i64, _c_vp, _c_i64, _c_i64, _c_vp, _c_i64, _c_i64,
                                   _c_dbl, _c_vp, _c_i64, _c_i64, _c_dbl, _c_vp, _c_vp]),
@@ -278,6 +282,20 @@ def redfield_operators(E, U, occ, bath, unit_convert, discard_imag_corr=False,
     return G, M, K
 
 
+def disordered_hamiltonians(base, offsets, off):
+    """(S, n, n) float64: base (n, n) plus diag(offsets[s]) on rows/columns
+    off .. off + n_sites - 1 (qsx_disordered_hamiltonians)."""
+    require_gpu()
+    _need(base, torch.float64, 'base', 2)
+    _need(offsets, torch.float64, 'offsets', 2)
+    n = base.shape[0]
+    S, N = offsets.shape
+    H = torch.empty((S, n, n), dtype=torch.float64, device=base.device)
+    _check(load().qsx_disordered_hamiltonians(_p(base), n, _p(offsets), S, N, off, _p(H),
+                                              _stream()), 'qsx_disordered_hamiltonians')
+    return H
+
+
 def gemm(A, B, out=None, Cin=None, alpha=1.0, beta=1.0, status=None):
     """Batched out = alpha A B (+ beta Cin) on the GPU (qsx_gemm_batched): FP32
     operands on the tensor cores (3xTF32), FP64 on the CUDA cores.
@@ -325,13 +343,38 @@ def gemm(A, B, out=None, Cin=None, alpha=1.0, beta=1.0, status=None):
     return out
 
 
+_MATSUBARA_TABLES = {}
+
+
+def matsubara_table(bath, matsubara_cutoff, xmax=4096.0, device=None):
+    """(table, pieces, width): the piecewise Chebyshev table of the Debye
+    Matsubara sum (qsx_debye_matsubara_table) on [0, xmax], on the GPU,
+    computed once per bath.  Pieces are at most 64 cm^-1 wide and at most a
+    fifth of the first Matsubara frequency, so every piece's series
+    converges to FP64 rounding."""
+    T, g = float(bath.temperature), float(bath.cutoff_freq)
+    key = (T, g, int(matsubara_cutoff), float(xmax))
+    if key not in _MATSUBARA_TABLES:
+        width = min(64.0, 0.4 * np.pi * T)   # half-width <= nu_1 / 10
+        pieces = int(np.ceil(xmax / width))
+        deg = load().qsx_debye_matsubara_table_degree()
+        coef = np.zeros((pieces, deg, 2), dtype=np.float64)
+        _check(load().qsx_debye_matsubara_table(T, g, int(matsubara_cutoff), pieces, width,
+                                                coef.ctypes.data_as(_c_vp)),
+               'qsx_debye_matsubara_table')
+        dev = device or torch.device('cuda', torch.cuda.current_device())
+        _MATSUBARA_TABLES[key] = (torch.as_tensor(coef).to(dev), pieces, width)
+    return _MATSUBARA_TABLES[key]
+
+
 def redfield_build_w64(H, U_approx, n_sites, off, bath, unit_convert, discard_imag_corr=False,
                        matsubara_cutoff=1000):
     """FP64 eigenpairs and site-basis Redfield operators of one-exciton
-    Hilbert spaces (qsx_redfield_build_w64): two FP64 refinement steps of
-    the approximate eigenvectors U_approx (e.g. the FP32 Jacobi's), then the
-    operator build in FP64.  H, U_approx (B, n, n) float64 CUDA; the coupled
-    block is [off, off + n_sites).  Returns E, U, G, M."""
+    Hilbert spaces (qsx_redfield_build_w64): FP64 refinement of the
+    approximate eigenvectors U_approx (e.g. the FP32 Jacobi's), then the
+    operator build in FP64 with the tabulated correlation function.  H,
+    U_approx (B, n, n) float64 CUDA; the coupled block is [off, off +
+    n_sites).  Returns E, U, G, M."""
     require_gpu()
     _need(H, torch.float64, 'H', 3)
     _need(U_approx, torch.float64, 'U_approx', 3)
@@ -341,10 +384,11 @@ def redfield_build_w64(H, U_approx, n_sites, off, bath, unit_convert, discard_im
     U = torch.empty((B, n, n), dtype=torch.float64, device=dev)
     G = torch.empty((B, n, n), dtype=torch.complex128, device=dev)
     M = torch.empty((B, n_sites, n, n), dtype=torch.complex128, device=dev)
+    table, pieces, width = matsubara_table(bath, matsubara_cutoff, device=dev)
     _check(load().qsx_redfield_build_w64(
         _p(H), n, off, n_sites, B, _p(U_approx), bath.temperature, bath.reorg_energy,
-        bath.cutoff_freq, matsubara_cutoff, int(discard_imag_corr), unit_convert,
-        _p(E), _p(U), _p(G), _p(M), _stream()), 'qsx_redfield_build_w64')
+        bath.cutoff_freq, matsubara_cutoff, int(discard_imag_corr), _p(table), pieces, width,
+        unit_convert, _p(E), _p(U), _p(G), _p(M), _stream()), 'qsx_redfield_build_w64')
     return E, U, G, M
 
 

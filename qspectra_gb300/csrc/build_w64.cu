@@ -8,15 +8,26 @@
 // propagation.  GB300 issues FP64 at a small fraction of its FP32 rate, so
 // the kernel spends FP64 only where the result needs it:
 //
-// * Eigenpairs: Jacobi preconditioned in low precision (the mixed-precision
-//   Jacobi of Higham, Tisseur, Webb and Zhou, 2024).  The FP32 register
-//   Jacobi (eigh_block_kernel<float>) gives an approximate eigenbasis X; in
-//   FP64, two Newton-Schulz steps X <- X + X (I - X^T X) / 2 make it
-//   orthonormal, S = X^T A X is then diagonal up to the FP32 error, and
-//   cyclic FP64 Jacobi sweeps on S (rotating X along) finish the job: one
-//   sweep of small rotations, then a sweep that finds nothing to do.  Close
-//   and equal eigenvalues need no special case (a rotation zeroes the pair
-//   exactly), unlike a perturbative refinement.
+// * Eigenpairs: the FP32 register Jacobi (eigh_block_kernel<float>) gives an
+//   approximate eigenbasis X; two steps of the symmetric eigenvalue
+//   refinement of Ogita and Aishima (Japan J. Indust. Appl. Math. 35 (2018)
+//   1007-1035, Algorithm 1) bring it to FP64 accuracy, each step one
+//   quadratic improvement in orthogonality and diagonalisation, all lanes
+//   busy:
+//     R = I - X^T X,  S = X^T A X,  l_i = S_ii / (1 - R_ii),
+//     F_ij = (S_ij + l_j R_ij) / (l_j - l_i)  for well-separated pairs,
+//     F_ij = R_ij / 2 otherwise (and on the diagonal),  X <- X + X F.
+//   From an FP32 start two steps reach FP64 only for gaps above ~1% of the
+//   spectral radius, so closer pairs are treated as clusters (their common
+//   subspace is refined, the pair itself is not).  The eigenvalues are the
+//   diagonal of the final S = X^T A X; a pair still coupled there (a close
+//   pair, a few percent of disorder samples) gets FP64 Jacobi rotations
+//   inside its refined subspace (Golub & Van Loan, Alg. 8.4.3) on lane 0.
+// * Correlation function: C(x) = lam gamma [(cot(gamma / 2T) - i) /
+//   (gamma - i x) + 4 T S(x)] with the Matsubara sum S(x) from a piecewise
+//   Chebyshev table (qsx_debye_matsubara_table, FP64 coefficients fitted to
+//   the direct finite sum of bath.py:95-102), evaluated by Clenshaw's
+//   recurrence in FP64; beyond the table the closed form of qsx_bath.cuh.
 // * Operators (site basis, non-secular): with the number-operator couplings
 //   of one-exciton states, Kt_i[c][d] = X[i][c] X[i][d], so with
 //   Y_i[a][c] = X[a][c] X[i][c] and C[c][d] = C(l_d - l_c)
@@ -34,6 +45,18 @@
 namespace qsx {
 
 constexpr int BW_WARPS = 4;
+// pairs closer than this fraction of the largest |H| entry are clusters for
+// the refinement steps (two steps from an FP32 start resolve wider gaps)
+constexpr double BW_CLOSE = 1.5e-2;
+constexpr int CHEB_DEG = 18;   // Chebyshev terms per table piece
+
+// Piecewise Chebyshev table of the Matsubara sum S(x), x >= 0: piece j covers
+// [j width, (j + 1) width) with CHEB_DEG complex coefficients (NULL: none).
+struct ChebTable {
+  const double2* coef;
+  int pieces;
+  double width;
+};
 
 template <int NB>
 struct BwSmem {
@@ -68,9 +91,10 @@ __device__ __forceinline__ double warp_sum(double v) {
 template <int NB>
 __global__ void __launch_bounds__(32 * BW_WARPS)
     redfield_build_w64_kernel(const double* __restrict__ H, int n, int off, int64_t batch,
-                              const double* __restrict__ Uapprox, DebyeParams bath, double uc,
-                              double* __restrict__ E, double* __restrict__ U,
-                              double2* __restrict__ G, double2* __restrict__ M) {
+                              const double* __restrict__ Uapprox, DebyeParams bath,
+                              ChebTable ctab, double uc, double* __restrict__ E,
+                              double* __restrict__ U, double2* __restrict__ G,
+                              double2* __restrict__ M) {
   constexpr int NN = NB * NB;
   constexpr int NNN = NB * NB * NB;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -87,29 +111,73 @@ __global__ void __launch_bounds__(32 * BW_WARPS)
     sm.X[e] = u0[(off + r) * n + off + c];
   }
   __syncwarp();
-  // ---- FP64 orthonormalisation of the FP32 basis: two Newton-Schulz steps
-  // X <- X + X (I - X^T X) / 2 (each squares the orthogonality error)
-  for (int it = 0; it < 2; ++it) {
-    for (int e = lane; e < NN; e += 32) {   // R = I - X^T X
-      const int i = e / NB, j = e % NB;
-      double r = 0.0;
+  // ---- two refinement steps (Ogita-Aishima), close pairs as clusters ----
+  double amax = 0.0;
+  for (int e = lane; e < NN; e += 32) amax = fmax(amax, fabs(sm.A[e]));
 #pragma unroll
-      for (int k = 0; k < NB; ++k) r = fma(sm.X[k * NB + i], sm.X[k * NB + j], r);
-      sm.R[e] = (i == j ? 1.0 : 0.0) - r;
-    }
-    __syncwarp();
-    for (int e = lane; e < NN; e += 32) {   // X + X R / 2, into P
-      const int a = e / NB, j = e % NB;
+  for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  const double close = BW_CLOSE * amax;
+  for (int it = 0; it < 2; ++it) {
+    for (int e = lane; e < NN; e += 32) {   // P = A X
+      const int r = e / NB, c = e % NB;
       double acc = 0.0;
 #pragma unroll
-      for (int k = 0; k < NB; ++k) acc = fma(sm.X[a * NB + k], sm.R[k * NB + j], acc);
-      sm.P[e] = fma(0.5, acc, sm.X[e]);
+      for (int k = 0; k < NB; ++k) acc = fma(sm.A[r * NB + k], sm.X[k * NB + c], acc);
+      sm.P[e] = acc;
     }
     __syncwarp();
-    for (int e = lane; e < NN; e += 32) sm.X[e] = sm.P[e];
+    double nA = 0.0, nR = 0.0;
+    for (int e = lane; e < NN; e += 32) {   // S = X^T P, R = I - X^T X
+      const int i = e / NB, j = e % NB;
+      double sv = 0.0, r = 0.0;
+#pragma unroll
+      for (int k = 0; k < NB; ++k) {
+        const double xki = sm.X[k * NB + i];
+        sv = fma(xki, sm.P[k * NB + j], sv);
+        r = fma(xki, sm.X[k * NB + j], r);
+      }
+      r = (i == j ? 1.0 : 0.0) - r;
+      sm.S[e] = sv;
+      sm.R[e] = r;
+      nA = fma(sm.A[e], sm.A[e], nA);
+      nR = fma(r, r, nR);
+    }
+    __syncwarp();
+    if (lane < NB) sm.lam[lane] = sm.S[lane * NB + lane] / (1.0 - sm.R[lane * NB + lane]);
+    __syncwarp();
+    double nS = 0.0;
+    for (int e = lane; e < NN; e += 32) {
+      const int i = e / NB, j = e % NB;
+      const double d = sm.S[e] - (i == j ? sm.lam[i] : 0.0);
+      nS = fma(d, d, nS);
+    }
+    nA = warp_sum(nA);
+    nR = warp_sum(nR);
+    nS = warp_sum(nS);
+    const double thr = fmax(2.0 * (sqrt(nS) + sqrt(nA) * sqrt(nR)), close);
+    for (int e = lane; e < NN; e += 32) {   // F, into P
+      const int i = e / NB, j = e % NB;
+      const double gap = sm.lam[j] - sm.lam[i];
+      double f;
+      if (i != j && fabs(gap) > thr)
+        f = (sm.S[e] + sm.lam[j] * sm.R[e]) / gap;
+      else
+        f = 0.5 * sm.R[e];
+      sm.P[e] = f;
+    }
+    __syncwarp();
+    for (int e = lane; e < NN; e += 32) {   // X + X F, into S
+      const int a = e / NB, j = e % NB;
+      double acc = sm.X[e];
+#pragma unroll
+      for (int k = 0; k < NB; ++k) acc = fma(sm.X[a * NB + k], sm.P[k * NB + j], acc);
+      sm.S[e] = acc;
+    }
+    __syncwarp();
+    for (int e = lane; e < NN; e += 32) sm.X[e] = sm.S[e];
     __syncwarp();
   }
-  // ---- S = X^T A X (nearly diagonal), symmetrised ------------------------
+  // ---- final S = X^T A X; close pairs still coupled get Jacobi rotations --
   for (int e = lane; e < NN; e += 32) {
     const int r = e / NB, c = e % NB;
     double acc = 0.0;
@@ -134,49 +202,35 @@ __global__ void __launch_bounds__(32 * BW_WARPS)
     sm.S[e] = 0.5 * (sm.R[e] + sm.R[j * NB + i]);
   }
   __syncwarp();
-  // ---- cyclic FP64 Jacobi on S (Golub & Van Loan, Alg. 8.4.3), rotating the
-  // columns of X too; one sweep normally zeroes every pair, the next finds
-  // nothing above the tolerance.  Lane 0 forms each rotation, lane k < NB
-  // updates row/column k of S and row k of X.
   const double tol = 1e-15 * sqrt(asum);
-  for (int sweep = 0; sweep < 10; ++sweep) {
-    bool rotated = false;
-    for (int p = 0; p < NB - 1; ++p)
-      for (int q = p + 1; q < NB; ++q) {
-        const double apq = sm.S[p * NB + q];
-        if (!(fabs(apq) > tol)) continue;   // same value in every lane
-        rotated = true;
-        const double app = sm.S[p * NB + p], aqq = sm.S[q * NB + q];
-        double c = 1.0, sn = 0.0, t = 0.0;
-        if (lane == 0) jacobi_rotation_f64(app, aqq, apq, c, sn, t);
-        c = __shfl_sync(0xffffffffu, c, 0);
-        sn = __shfl_sync(0xffffffffu, sn, 0);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        __syncwarp();
-        if (lane < NB) {
-          const int k = lane;
-          if (k != p && k != q) {
-            const double g = sm.S[k * NB + p], hh = sm.S[k * NB + q];
-            const double np_ = c * g - sn * hh, nq = sn * g + c * hh;
-            sm.S[k * NB + p] = np_;
-            sm.S[p * NB + k] = np_;
-            sm.S[k * NB + q] = nq;
-            sm.S[q * NB + k] = nq;
-          } else if (k == p) {
-            sm.S[p * NB + p] = fma(-t, apq, app);
-            sm.S[p * NB + q] = 0.0;
-            sm.S[q * NB + p] = 0.0;
-          } else {
-            sm.S[q * NB + q] = fma(t, apq, aqq);
+  if (lane == 0) {
+    for (int sweep = 0; sweep < 10; ++sweep) {
+      bool rotated = false;
+      for (int p = 0; p < NB - 1; ++p)
+        for (int q = p + 1; q < NB; ++q) {
+          const double apq = sm.S[p * NB + q];
+          if (!(fabs(apq) > tol)) continue;
+          rotated = true;
+          double c, sn, t;
+          jacobi_rotation_f64(sm.S[p * NB + p], sm.S[q * NB + q], apq, c, sn, t);
+          sm.S[p * NB + p] = fma(-t, apq, sm.S[p * NB + p]);
+          sm.S[q * NB + q] = fma(t, apq, sm.S[q * NB + q]);
+          sm.S[p * NB + q] = sm.S[q * NB + p] = 0.0;
+          for (int k = 0; k < NB; ++k) {
+            if (k != p && k != q) {
+              const double g = sm.S[k * NB + p], hh = sm.S[k * NB + q];
+              sm.S[k * NB + p] = sm.S[p * NB + k] = c * g - sn * hh;
+              sm.S[k * NB + q] = sm.S[q * NB + k] = sn * g + c * hh;
+            }
+            const double xp = sm.X[k * NB + p], xq = sm.X[k * NB + q];
+            sm.X[k * NB + p] = c * xp - sn * xq;
+            sm.X[k * NB + q] = sn * xp + c * xq;
           }
-          const double xp = sm.X[k * NB + p], xq = sm.X[k * NB + q];
-          sm.X[k * NB + p] = c * xp - sn * xq;
-          sm.X[k * NB + q] = sn * xp + c * xq;
         }
-        __syncwarp();
-      }
-    if (!rotated) break;
+      if (!rotated) break;
+    }
   }
+  __syncwarp();
   if (lane < NB) sm.lam[lane] = sm.S[lane * NB + lane];
   __syncwarp();
   // ---- eigenpairs out, ascending inside the block (stable on ties) -------
@@ -206,7 +260,28 @@ __global__ void __launch_bounds__(32 * BW_WARPS)
     const int c = e / NB, d = e % NB;
     if (c > d) continue;
     double2 cp, cn;
-    debye_corr_pair(bath, sm.lam[d] - sm.lam[c], cp, cn);
+    const double x = sm.lam[d] - sm.lam[c];
+    const double ax = fabs(x);
+    const int piece = (int)(ax / ctab.width);
+    if (ctab.coef && !bath.real_only && x != 0.0 && piece < ctab.pieces) {
+      // Clenshaw on the piece's Chebyshev series of S(|x|); S(-x) = conj S(x)
+      const double2* cf = ctab.coef + (size_t)piece * CHEB_DEG;
+      const double t = (ax - (piece + 0.5) * ctab.width) * (2.0 / ctab.width);
+      const double t2 = 2.0 * t;
+      double2 b1 = cmk(0.0, 0.0), b2 = cmk(0.0, 0.0);
+      for (int k = CHEB_DEG - 1; k >= 1; --k) {
+        const double2 ck = cf[k];
+        const double2 b0 = cmk(fma(t2, b1.x, ck.x - b2.x), fma(t2, b1.y, ck.y - b2.y));
+        b2 = b1;
+        b1 = b0;
+      }
+      double2 Sx = cmk(fma(t, b1.x, cf[0].x - b2.x), fma(t, b1.y, cf[0].y - b2.y));
+      if (x < 0.0) Sx = cconj(Sx);
+      cp = debye_from_matsubara(bath, x, Sx);
+      cn = debye_from_matsubara(bath, -x, cconj(Sx));
+    } else {
+      debye_corr_pair(bath, x, cp, cn);
+    }
     sm.C[c * NB + d] = cp;
     sm.C[d * NB + c] = cn;
   }
@@ -264,26 +339,75 @@ __global__ void __launch_bounds__(32 * BW_WARPS)
 
 template <int NB>
 static cudaError_t launch_bw(const double* H, int n, int off, int64_t batch, const double* Ua,
-                             const DebyeParams& bath, double uc, double* E, double* U, double* G,
-                             double* M, cudaStream_t s) {
+                             const DebyeParams& bath, const ChebTable& ctab, double uc, double* E,
+                             double* U, double* G, double* M, cudaStream_t s) {
   const size_t smem = sizeof(BwSmem<NB>) * BW_WARPS;
   cudaError_t e = cudaFuncSetAttribute(redfield_build_w64_kernel<NB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int64_t grid = (batch + BW_WARPS - 1) / BW_WARPS;
   redfield_build_w64_kernel<NB><<<(unsigned)grid, 32 * BW_WARPS, smem, s>>>(
-      H, n, off, batch, Ua, bath, uc, E, U, (double2*)G, (double2*)M);
+      H, n, off, batch, Ua, bath, ctab, uc, E, U, (double2*)G, (double2*)M);
   return cudaGetLastError();
 }
 
 }  // namespace qsx
 
+// Host: Chebyshev coefficients of the Matsubara sum
+//   S(x) = sum_{k=1}^{K-1} nu_k / ((nu_k^2 - gamma^2)(nu_k - i x)),
+// nu_k = 2 pi k T (bath.py:95-102), on pieces [j w, (j + 1) w), x >= 0:
+// CHEB_DEG values at the Chebyshev points of each piece, summed directly in
+// FP64, then the discrete cosine transform.
+extern "C" int qsx_debye_matsubara_table(double temperature, double cutoff_freq,
+                                         int matsubara_cutoff, int pieces, double width,
+                                         double* coef) {
+  using namespace qsx;
+  QSX_CHECK_ARG(temperature > 0 && cutoff_freq > 0 && matsubara_cutoff >= 1 && pieces >= 1 &&
+                    width > 0 && coef,
+                "qsx_debye_matsubara_table: bad arguments");
+  const int D = CHEB_DEG;
+  const double pi = 3.14159265358979323846;
+  double fr[CHEB_DEG], fi[CHEB_DEG];
+  for (int j = 0; j < pieces; ++j) {
+    for (int q = 0; q < D; ++q) {
+      const double th = pi * (q + 0.5) / D;
+      const double x = (j + 0.5) * width + 0.5 * width * cos(th);
+      double sr = 0.0, si = 0.0;
+      for (int k = 1; k < matsubara_cutoff; ++k) {
+        const double nu = 2.0 * pi * k * temperature;
+        const double a = nu / (nu * nu - cutoff_freq * cutoff_freq);
+        // a / (nu - i x) = a (nu + i x) / (nu^2 + x^2)
+        const double den = nu * nu + x * x;
+        sr += a * nu / den;
+        si += a * x / den;
+      }
+      fr[q] = sr;
+      fi[q] = si;
+    }
+    for (int m = 0; m < D; ++m) {
+      double cr = 0.0, ci = 0.0;
+      for (int q = 0; q < D; ++q) {
+        const double w = cos(pi * m * (q + 0.5) / D);
+        cr += fr[q] * w;
+        ci += fi[q] * w;
+      }
+      const double scale = (m == 0 ? 1.0 : 2.0) / D;
+      coef[2 * ((size_t)j * D + m)] = cr * scale;
+      coef[2 * ((size_t)j * D + m) + 1] = ci * scale;
+    }
+  }
+  return QSX_OK;
+}
+
+extern "C" int qsx_debye_matsubara_table_degree(void) { return qsx::CHEB_DEG; }
+
 extern "C" int qsx_redfield_build_w64(const double* H, int n, int off, int n_sites,
                                       int64_t batch, const double* U_approx,
                                       double temperature, double reorg_energy,
                                       double cutoff_freq, int matsubara_cutoff,
-                                      int discard_imag_corr, double unit_convert, double* E,
-                                      double* U, double* G, double* M, void* stream) {
+                                      int discard_imag_corr, const double* corr_table,
+                                      int corr_pieces, double corr_width, double unit_convert,
+                                      double* E, double* U, double* G, double* M, void* stream) {
   using namespace qsx;
   QSX_CHECK_ARG(n_sites >= 2 && n_sites <= 8,
                 "qsx_redfield_build_w64: n_sites must be 2..8 (got %d)", n_sites);
@@ -295,18 +419,24 @@ extern "C" int qsx_redfield_build_w64(const double* H, int n, int off, int n_sit
   QSX_CHECK_ARG(H && U_approx && E && U && G && M, "qsx_redfield_build_w64: null pointer");
   QSX_CHECK_ARG(temperature > 0 && cutoff_freq > 0 && matsubara_cutoff >= 1,
                 "qsx_redfield_build_w64: bad bath parameters");
+  QSX_CHECK_ARG(corr_table == nullptr || (corr_pieces >= 1 && corr_width > 0),
+                "qsx_redfield_build_w64: bad correlation table");
   const DebyeParams bath = make_debye(temperature, reorg_energy, cutoff_freq, matsubara_cutoff,
                                       discard_imag_corr);
+  ChebTable ctab;
+  ctab.coef = (const double2*)corr_table;
+  ctab.pieces = corr_table ? corr_pieces : 0;
+  ctab.width = corr_table ? corr_width : 1.0;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaSuccess;
   switch (n_sites) {
-    case 2: e = launch_bw<2>(H, n, off, batch, U_approx, bath, unit_convert, E, U, G, M, s); break;
-    case 3: e = launch_bw<3>(H, n, off, batch, U_approx, bath, unit_convert, E, U, G, M, s); break;
-    case 4: e = launch_bw<4>(H, n, off, batch, U_approx, bath, unit_convert, E, U, G, M, s); break;
-    case 5: e = launch_bw<5>(H, n, off, batch, U_approx, bath, unit_convert, E, U, G, M, s); break;
-    case 6: e = launch_bw<6>(H, n, off, batch, U_approx, bath, unit_convert, E, U, G, M, s); break;
-    case 7: e = launch_bw<7>(H, n, off, batch, U_approx, bath, unit_convert, E, U, G, M, s); break;
-    default: e = launch_bw<8>(H, n, off, batch, U_approx, bath, unit_convert, E, U, G, M, s); break;
+    case 2: e = launch_bw<2>(H, n, off, batch, U_approx, bath, ctab, unit_convert, E, U, G, M, s); break;
+    case 3: e = launch_bw<3>(H, n, off, batch, U_approx, bath, ctab, unit_convert, E, U, G, M, s); break;
+    case 4: e = launch_bw<4>(H, n, off, batch, U_approx, bath, ctab, unit_convert, E, U, G, M, s); break;
+    case 5: e = launch_bw<5>(H, n, off, batch, U_approx, bath, ctab, unit_convert, E, U, G, M, s); break;
+    case 6: e = launch_bw<6>(H, n, off, batch, U_approx, bath, ctab, unit_convert, E, U, G, M, s); break;
+    case 7: e = launch_bw<7>(H, n, off, batch, U_approx, bath, ctab, unit_convert, E, U, G, M, s); break;
+    default: e = launch_bw<8>(H, n, off, batch, U_approx, bath, ctab, unit_convert, E, U, G, M, s); break;
   }
   if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_build_w64");
   return QSX_OK;

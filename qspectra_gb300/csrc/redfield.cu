@@ -1164,11 +1164,43 @@ __global__ void hermitian_form_kernel(const typename cplx<T>::type* __restrict__
   R[t] = hermitian_entry(A + b * (int64_t)m * m, m, n, e / m, e % m);
 }
 
+// H[s] = base + diag(offsets[s]) on rows/columns [off, off + n_sites):
+// the rotating-frame Hamiltonian of disorder sample s (Hamiltonian.sample,
+// hamiltonian.py:552-578, which shifts the site energies).
+__global__ void disordered_hamiltonians_kernel(const double* __restrict__ base, int n,
+                                               const double* __restrict__ offsets,
+                                               int64_t batch, int n_sites, int off,
+                                               double* __restrict__ H) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nn = n * n;
+  if (t >= batch * nn) return;
+  const int64_t s = t / nn;
+  const int e = (int)(t % nn), r = e / n, c = e % n;
+  double v = base[e];
+  if (r == c && r >= off && r < off + n_sites) v += offsets[s * n_sites + (r - off)];
+  H[t] = v;
+}
+
 }  // namespace qsx
 
 using namespace qsx;
 
 extern "C" {
+
+int qsx_disordered_hamiltonians(const double* base, int n, const double* offsets,
+                                int64_t batch, int n_sites, int off, double* H, void* stream) {
+  QSX_CHECK_ARG(n >= 1 && n_sites >= 0 && off >= 0 && off + n_sites <= n && batch >= 0,
+                "qsx_disordered_hamiltonians: bad sizes");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(base && H && (n_sites == 0 || offsets),
+                "qsx_disordered_hamiltonians: null pointer");
+  const int64_t total = batch * (int64_t)n * n;
+  disordered_hamiltonians_kernel<<<(unsigned)((total + 255) / 256), 256, 0,
+                                   (cudaStream_t)stream>>>(base, n, offsets, batch, n_sites, off,
+                                                           H);
+  QSX_LAUNCH_CHECK("qsx_disordered_hamiltonians");
+  return QSX_OK;
+}
 
 int qsx_hermitian_real_form(const void* A, int n, int64_t batch, int precision, void* R,
                             void* stream) {

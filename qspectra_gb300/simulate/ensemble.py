@@ -214,11 +214,15 @@ def hermitian_block_size(idx, n_total):
 _TENSOR_CORE_BLOCKS = True
 
 
-def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None):
+def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None, x0=None):
     """FP32 ensemble mean of the selected components of a Hermitian diagonal
     block through its real form: real propagator, real K-step blocked matrix
-    (tcgen05 3xTF32 products when the shape allows) and real blocked loop.  Returns {'mean': (nsteps + 1, len(select))
-    complex128, 'status'} like propagate_selected_mean."""
+    (tcgen05 3xTF32 products when the shape allows) and real blocked loop.
+    Returns {'mean': (nsteps + 1, len(select)) complex128, 'status'} like
+    propagate_selected_mean; when every selected component is a population
+    (diagonal), 'mean_real' holds the same values as float64 without the
+    complex reconstruction.  ``x0`` may pass the Hermitian coordinates of
+    y0 (hermitian_coordinates) when the caller keeps them."""
     m = nb * nb
     sel = np.asarray(select, dtype=np.int64)
     a, b = sel % nb, sel // nb
@@ -251,7 +255,8 @@ def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None)
         events['blockbuild_flops'] = 2.0 * Dr.shape[0] * (
             products * m ** 3 + max(K - 2, 0) * len(coords) * m * m)
     del Dr
-    x0 = hermitian_coordinates(y0, nb)
+    if x0 is None:
+        x0 = hermitian_coordinates(y0, nb)
     if events is not None:
         e0 = torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -268,6 +273,9 @@ def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None)
         events['dyn_flops'] = 2.0 * mat.shape[0] * (nsteps // K) * mat.shape[1] * m
         events['dyn_block_k'] = K
         events['dyn_variant'] = 'real'
+    if np.all(a == b) and np.array_equal(coords, sel):
+        # populations: the coordinates are the values themselves
+        return {'mean_real': xm, 'status': status}
     full = torch.zeros((xm.shape[0], m), dtype=torch.float64, device=xm.device)
     full[:, _native.const_tensor(coords, torch.int64, xm.device)] = xm
     y = from_hermitian_coordinates(full, nb)
@@ -411,6 +419,8 @@ def ensemble_populations(model, initial_state, duration, ensemble_size,
     nb = can_use_hermitian(prec, idx, n_total, y0, len(t) - 1)
     if nb is not None:
         out = propagate_hermitian_mean(build, idx, nb, dt, y0t, len(t) - 1, select)
+        if 'mean_real' in out:
+            out['mean'] = out['mean_real'].to(torch.complex128)
     else:
         out = propagate_selected_mean(build.propagator(idx, dt, prec), y0t, len(t) - 1,
                                       select, prec)
@@ -467,6 +477,9 @@ class RedfieldEnsembleWorkload:
         V1 = model.dipole_operator('eg->gg', polarization[1], '-')
         self.proj = torch.as_tensor(np.asarray(V0.commutator(rho0))[None, :],
                                     dtype=torch.complex128, device=dev)
+        # the spectrum transforms minus the signal (response.py:150-153):
+        # project with -proj so the loop yields it directly
+        self.proj_neg = (-self.proj).contiguous()
         self.y_abs = torch.as_tensor(-V1.bra_vector, dtype=torch.complex128, device=dev)
         rho = np.asarray(initial_state)
         if rho.ndim == 1:
@@ -474,6 +487,7 @@ class RedfieldEnsembleWorkload:
         self.y_dyn_np = np.asarray(model.density_matrix_to_state_vector(rho, 'ee'), complex)
         self.y_dyn = torch.as_tensor(self.y_dyn_np, dtype=torch.complex128, device=dev)
         self.select = [i * self.n_sites + i for i in range(self.n_sites)]
+        self.x_dyn = None   # Hermitian coordinates of y_dyn, made on first use
         self.freqs_np = (fft_frequencies(self.t_abs, model.rw_freq, model.unit_convert)
                          if freqs is None else np.asarray(freqs, float))
         self.freqs = torch.as_tensor(self.freqs_np, device=dev)
@@ -493,9 +507,7 @@ class RedfieldEnsembleWorkload:
         """
         from .utils import PRECISIONS
         prec = PRECISIONS[precision]
-        S = offsets.shape[0]
-        H = self.H_base.expand(S, -1, -1).clone()
-        H[:, self.e_idx, self.e_idx] += offsets
+        H = _native.disordered_hamiltonians(self.H_base, offsets.contiguous(), 1)
         if events is not None:
             a0 = torch.cuda.Event(enable_timing=True)
             a0.record()
@@ -514,14 +526,17 @@ class RedfieldEnsembleWorkload:
         with torch.cuda.stream(self._side):
             self._side.wait_event(ready)
             D_eg = build.propagator(self.idx_eg, self.dt, prec, transpose=True)
-            sig = projected_mean(D_eg, self.y_abs, self.proj, len(self.t_abs) - 1)
-            X = _native.dft(-sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
+            sig = projected_mean(D_eg, self.y_abs, self.proj_neg, len(self.t_abs) - 1)
+            X = _native.dft(sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
                             self.model.rw_freq, self.model.unit_convert, 1)
         nb = can_use_hermitian(prec, self.idx_ee, self.n_sites + 1, self.y_dyn_np,
                                len(self.t_dyn) - 1)
         if nb is not None:
+            if self.x_dyn is None:
+                self.x_dyn = hermitian_coordinates(self.y_dyn, nb).contiguous()
             pop = propagate_hermitian_mean(build, self.idx_ee, nb, self.dt, self.y_dyn,
-                                           len(self.t_dyn) - 1, self.select, events)
+                                           len(self.t_dyn) - 1, self.select, events,
+                                           x0=self.x_dyn)
         else:
             D_ee = build.propagator(self.idx_ee, self.dt, prec)
             pop = propagate_selected_mean(D_ee, self.y_dyn, len(self.t_dyn) - 1, self.select,
@@ -532,7 +547,8 @@ class RedfieldEnsembleWorkload:
         for t in (build.G, build.M, build.E, build.U, build.occ, H):
             t.record_stream(self._side)
         status = sig['status'] | pop['status']
-        return X.real, pop['mean'].real, status
+        pops = pop['mean_real'] if 'mean_real' in pop else pop['mean'].real
+        return X.real, pops, status
 
     def capture(self, offsets, precision='fp32', build_precision='fp64'):
         """Record one step as a CUDA graph on static buffers (a copy of

@@ -83,11 +83,17 @@ def pair_tables(n_sites):
     return pair_sites, site_pairs
 
 
-def powers_minus_identity(D, gaps):
+def _gemm_add(A, B, C):
+    return _native.gemm(A, B, Cin=C)
+
+
+def powers_minus_identity(D, gaps, mul_add=_gemm_add):
     """{k: P^k - I} for P = I + D (batched), sharing one squaring chain.
 
     (I + X)(I + Y) - I = X + Y + X Y keeps the small part of each factor, so
     the powers lose no accuracy to cancellation against the identity.
+    ``mul_add(A, B, C)`` returns A B + C; the default runs qsx_gemm_batched
+    (tensor cores for FP32).
     """
     out = {}
     todo = sorted({int(k) for k in gaps})
@@ -98,10 +104,11 @@ def powers_minus_identity(D, gaps):
     while bit <= top:
         for k in todo:
             if k & bit:
-                acc[k] = X if acc[k] is None else acc[k] + X + acc[k] @ X
+                # acc + X + acc X
+                acc[k] = X if acc[k] is None else mul_add(acc[k], X, acc[k] + X)
         bit <<= 1
         if bit <= top:
-            X = 2 * X + X @ X
+            X = mul_add(X, X, 2 * X)   # 2 X + X X
     for k in todo:
         out[k] = acc[k] if acc[k] is not None else torch.zeros_like(D)
     return out
@@ -210,7 +217,7 @@ class ThirdOrderEngine:
         basis = torch.as_tensor(np.array(
             [np.asarray(self._op(spec, tuple(np.eye(3)[a]), tr).bra_vector, dtype=complex)
              for a in range(3)]), dtype=torch.complex128).cuda()
-        return torch.einsum('sa,an->sn', vec.to(basis.dtype), basis).contiguous()
+        return (vec.to(basis.dtype)[:, :, None] * basis[None]).sum(1).contiguous()
 
     def _ket0(self, spec, vec, tr):
         """Dipole commutator on the ground state: (n,) or (S, n)."""
@@ -219,7 +226,7 @@ class ThirdOrderEngine:
             return self._csr(spec, vec, tr)(rho0)
         basis = torch.stack([self._csr(spec, tuple(np.eye(3)[a]), tr)(rho0)
                              for a in range(3)])
-        return torch.einsum('sa,an->sn', vec.to(basis.dtype), basis).contiguous()
+        return (vec.to(basis.dtype)[:, :, None] * basis[None]).sum(1).contiguous()
 
     # -------------------------------------------------------------- builds
     def _f_operators(self, batch, build_e, cdt):
@@ -235,10 +242,13 @@ class ThirdOrderEngine:
                                   model.discard_imag_corr,
                                   ham.bath.matsubara_cutoff)
         S = Y.shape[0]
-        U = Uf.to(Y.dtype)
-        T = torch.bmm(U, Y.view(S, P, 2 * N * P))
+        # M_q = U Y_q U^T for the 2N operators q: U (real) times all Y_q side
+        # by side, then every T_q times U^T (qsx_gemm_batched)
+        rdt = torch.float32 if Y.dtype == torch.complex64 else torch.float64
+        U = Uf.to(rdt).contiguous()
+        T = _native.gemm(U, Y.view(S, P, 2 * N * P))
         del Y
-        Mf = torch.bmm(T.view(S, P * 2 * N, P), U.transpose(1, 2))
+        Mf = _native.gemm(T.view(S, P * 2 * N, P), U.transpose(1, 2).contiguous())
         del T
         Q = _native.fe_generator(Mf.view(S, P, 2 * N, P).contiguous(), Hf.contiguous(),
                                  self._pair_sites, model.unit_convert, self.prec)
@@ -326,8 +336,9 @@ class ThirdOrderEngine:
             Lee = build.block(self._idx('ee'))
             A = (dt * Lee).to(cdt)
             del Lee
-            A2 = A @ A
-            D = A + 0.5 * A2 + A2 @ (A / 6 + A2 / 24)
+            A2 = _native.gemm(A, A)
+            # D = A + A^2 / 2 + A^2 (A / 6 + A^2 / 24), one step of RK4
+            D = _native.gemm(A2, A / 6 + A2 / 24, Cin=A + 0.5 * A2)
             del A, A2
             Xg = powers_minus_identity(D, [base])[base].transpose(1, 2).contiguous()
             del D
@@ -352,8 +363,8 @@ class ThirdOrderEngine:
                 Wv = Wt.view(S * nL, N * N, T3)
                 for j, k in enumerate(gaps):
                     for _ in range(k // base):
-                        r = r + torch.bmm(r, Xg)
-                    part = torch.bmm(r.view(S * nL, T1, N * N), Wv)
+                        r = _native.gemm(r, Xg, Cin=r)          # r (I + X_g)
+                    part = _native.gemm(r.view(S * nL, T1, N * N), Wv)
                     total[:, j, :] += part.to(torch.complex128).sum(0)
             if gc:
                 for (a, b), g in zip(left, gc):
@@ -361,7 +372,9 @@ class ThirdOrderEngine:
                     for j, k in enumerate(gaps):
                         if k:
                             rgg = rgg * (1 + Dgg[:, None]) ** k
-                        total[:, j, :] += torch.einsum('sa,sc->ac', rgg, g)
+                        # sum over samples of rgg[s, a] g[s, c]
+                        total[:, j, :] += _native.gemm(rgg.t().contiguous(),
+                                                       g.contiguous())[0]
             out[geo] = total
         _tick(events, 'end')
         return out

@@ -36,7 +36,9 @@ def test_gemm_matches_fp64_product(ca, cb, S, M, K, N, single):
     out = _native.gemm(At, Bt, status=status)
     torch.cuda.synchronize()
     assert int(status.item()) == 0
-    tol = 2e-6 if single else 1e-13
+    # 3xTF32 drops the lo*lo term (about 2^-22 of each product) and sums in
+    # FP32: a few 1e-6 relative at K = 576 (FP32-level accuracy)
+    tol = 1e-5 if single else 1e-13
     assert rel_err(out.cpu().numpy(), ref) < tol
     # accumulate in place: out = 0.5 A B + 2 C0
     Ct = torch.as_tensor(C0).to(out.dtype).cuda()
@@ -51,7 +53,7 @@ def test_gemm_shared_operand(single):
     B = rand((96, 40), True, rng)
     dt = torch.complex64 if single else torch.complex128
     out = _native.gemm(torch.as_tensor(A).to(dt).cuda(), torch.as_tensor(B).to(dt).cuda())
-    assert rel_err(out.cpu().numpy(), A @ B) < (2e-6 if single else 1e-13)
+    assert rel_err(out.cpu().numpy(), A @ B) < (1e-5 if single else 1e-13)
     out = _native.gemm(torch.as_tensor(B.T.copy()).to(dt).cuda(),
                        torch.as_tensor(A.transpose(0, 2, 1).copy()).to(dt).cuda())
-    assert rel_err(out.cpu().numpy(), B.T @ A.transpose(0, 2, 1)) < (2e-6 if single else 1e-13)
+    assert rel_err(out.cpu().numpy(), B.T @ A.transpose(0, 2, 1)) < (1e-5 if single else 1e-13)

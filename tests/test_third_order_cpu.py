@@ -78,7 +78,7 @@ def test_powers_minus_identity():
     rng = np.random.RandomState(0)
     D = 0.05 * (rng.randn(3, 6, 6) + 1j * rng.randn(3, 6, 6))
     gaps = [0, 1, 7, 100, 150]
-    out = powers_minus_identity(torch.as_tensor(D), gaps)
+    out = powers_minus_identity(torch.as_tensor(D), gaps, mul_add=lambda A, B, C: A @ B + C)
     for k in gaps:
         ref = np.array([np.linalg.matrix_power(np.eye(6) + d, k) - np.eye(6) for d in D])
         assert np.max(np.abs(out[k].numpy() - ref)) < 1e-12 * max(1, np.abs(ref).max())
