@@ -313,8 +313,9 @@ def gemm(A, B, out=None, Cin=None, alpha=1.0, beta=1.0, status=None):
         raise TypeError('gemm operands must share one precision')
     ca, cb = A.is_complex(), B.is_complex()
     mode = {(False, False): 0, (True, True): 1, (True, False): 2, (False, True): 3}[(ca, cb)]
-    if A.stride(-1) != 1 or B.stride(-1) != 1:
-        raise ValueError('gemm operands need a contiguous last dimension')
+    for t in (A, B):
+        if t.shape[-1] > 1 and t.stride(-1) != 1:
+            raise ValueError('gemm operands need a contiguous last dimension')
     S = max(A.shape[0] if A.dim() == 3 else 1, B.shape[0] if B.dim() == 3 else 1)
     M, K = A.shape[-2], A.shape[-1]
     if B.shape[-2] != K:
@@ -323,13 +324,13 @@ def gemm(A, B, out=None, Cin=None, alpha=1.0, beta=1.0, status=None):
     cdt = (torch.complex64 if single else torch.complex128) if (ca or cb) else A.dtype
     if out is None:
         out = torch.empty((S, M, N), dtype=cdt, device=A.device)
-    if out.dtype != cdt or out.shape[-2:] != (M, N) or out.stride(-1) != 1:
+    if out.dtype != cdt or out.shape[-2:] != (M, N) or (N > 1 and out.stride(-1) != 1):
         raise ValueError('gemm: bad output tensor')
     sa = A.stride(0) if A.dim() == 3 else 0
     sb = B.stride(0) if B.dim() == 3 else 0
     so = out.stride(0) if out.dim() == 3 else 0
     if Cin is not None:
-        if Cin.dtype != cdt or Cin.shape[-2:] != (M, N) or Cin.stride(-1) != 1:
+        if Cin.dtype != cdt or Cin.shape[-2:] != (M, N) or (N > 1 and Cin.stride(-1) != 1):
             raise ValueError('gemm: bad Cin tensor')
         sc, ldc_in = (Cin.stride(0) if Cin.dim() == 3 else 0), Cin.stride(-2)
     else:

@@ -201,24 +201,19 @@ __device__ __forceinline__ void heom_rhs_elem(const HeomP& p, const typename cpl
   oi = fma(-sh, self.y, oi);
   const C* xb = x + b * (int64_t)p.nnodes * p.E;
   const int base = local * p.nterms;
-  const int* ts = s.tstart + local * (p.n_sites + 1);
-  // a term of site j weighs occ_j(a) alpha + occ_j(b) beta, so only the
-  // sites occupied in state a or state b contribute (each visited once)
-  const int js[4] = {s.sx[2 * a], s.sx[2 * a + 1], s.sy[2 * bb], s.sy[2 * bb + 1]};
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int j = js[q];
-    if (j < 0) continue;
-    if (q >= 2 && (j == js[0] || j == js[1])) continue;
+  // every term of the node, the same sequence in every lane of a warp (the
+  // lanes serve one node), so each neighbour load is one coalesced access;
+  // a term of site j weighs occ_j(a) alpha + occ_j(b) beta
+  for (int t = 0; t < p.nterms; ++t) {
+    const int nb = s.nbr[base + t];
+    if (nb < 0) break;
+    const int j = s.site[base + t];
+    const C al = s.al[base + t], be = s.be[base + t];
     const T oa = s.ox[j * p.nx + a], ob = s.oy[j * p.ny + bb];
-    for (int t = base + ts[j]; t < base + ts[j + 1]; ++t) {
-      const int nb = s.nbr[t];
-      const C al = s.al[t], be = s.be[t];
-      const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
-      const C v = xb[(int64_t)nb * p.E + e];
-      orr = fma(fr, v.x, fma(-fi, v.y, orr));
-      oi = fma(fr, v.y, fma(fi, v.x, oi));
-    }
+    const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
+    const C v = xb[(int64_t)nb * p.E + e];
+    orr = fma(fr, v.x, fma(-fi, v.y, orr));
+    oi = fma(fr, v.y, fma(fi, v.x, oi));
   }
   T uc;
   if constexpr (sizeof(T) == 4)
@@ -457,25 +452,22 @@ __global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
         const T sh = ssh[l] + sW[e];
         orr = fma(-sh, self.x, orr);
         oi = fma(-sh, self.y, oi);
-        // couplings of the sites occupied in state a or state bb
-        const int* ts = sts + l * (N + 1);
-        const int js[4] = {ssx[2 * a], ssx[2 * a + 1], ssy[2 * bb], ssy[2 * bb + 1]};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int j = js[q];
-          if (j < 0) continue;
-          if (q >= 2 && (j == js[0] || j == js[1])) continue;
+        // couplings: every term of the node in the same order in all lanes
+        // (a warp serves one node when E is a multiple of 32), so each
+        // neighbour block is read with one coalesced access, local or
+        // through distributed shared memory
+        for (int t = l * nt; t < (l + 1) * nt; ++t) {
+          const int m = snb[t];
+          if (m < 0) break;
+          const int j = sst[t];
+          const int r = m / p.npcta, ml = m - r * p.npcta;
+          const Cx* src = r == rank ? xin : cluster.map_shared_rank(xin, r);
+          const Cx v = src[ml * E + e];
+          const Cx al = sal[t], be = sbe[t];
           const T oa = sox[j * nx + a], ob = soy[j * ny + bb];
-          for (int t = l * nt + ts[j]; t < l * nt + ts[j + 1]; ++t) {
-            const int m = snb[t];
-            const int r = m / p.npcta, ml = m - r * p.npcta;
-            const Cx* src = r == rank ? xin : cluster.map_shared_rank(xin, r);
-            const Cx v = src[ml * E + e];
-            const Cx al = sal[t], be = sbe[t];
-            const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
-            orr = fma(fr, v.x, fma(-fi, v.y, orr));
-            oi = fma(fr, v.y, fma(fi, v.x, oi));
-          }
+          const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
+          orr = fma(fr, v.x, fma(-fi, v.y, orr));
+          oi = fma(fr, v.y, fma(fi, v.x, oi));
         }
         const Cx d = cmk(uc * orr, uc * oi);
         acc[u] = stage == 0 ? d : cmk(acc[u].x + wg * d.x, acc[u].y + wg * d.y);

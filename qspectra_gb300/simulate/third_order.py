@@ -242,10 +242,10 @@ class ThirdOrderEngine:
                                   model.discard_imag_corr,
                                   ham.bath.matsubara_cutoff)
         S = Y.shape[0]
-        # M_q = U Y_q U^T for the 2N operators q: U (real) times all Y_q side
-        # by side, then every T_q times U^T (qsx_gemm_batched)
-        rdt = torch.float32 if Y.dtype == torch.complex64 else torch.float64
-        U = Uf.to(rdt).contiguous()
+        # M_q = U Y_q U^T for the 2N real planes q (real and imaginary parts):
+        # U times all Y_q side by side, then every T_q times U^T, real
+        # products in the working precision (qsx_gemm_batched)
+        U = Uf.to(Y.dtype).contiguous()
         T = _native.gemm(U, Y.view(S, P, 2 * N * P))
         del Y
         Mf = _native.gemm(T.view(S, P * 2 * N, P), U.transpose(1, 2).contiguous())
