@@ -67,10 +67,6 @@ struct HeomSmem {
   C* be;      // npc * nterms
   int* nbr;   // npc * nterms
   int* site;  // npc * nterms
-  int* tstart;  // npc * (n_sites + 1): each node's terms of site j are
-                // tstart[j] .. tstart[j + 1] - 1 (the host groups them by site)
-  int* sx;    // 2 * nx: the (at most two) sites occupied in x state a, -1 = none
-  int* sy;    // 2 * ny
   C* x;       // npc * E, this CTA's node blocks of the input
 };
 
@@ -81,7 +77,6 @@ __host__ __device__ inline size_t heom_smem_bytes(int nx, int ny, int n_sites, i
   size_t b = (size_t)npc * E * sizeof(C) + 2 * (size_t)npc * nterms * sizeof(C);
   b += ((size_t)nx * nx + ny * ny + (size_t)n_sites * (nx + ny) + E + npc) * sizeof(T);
   b += 2 * (size_t)npc * nterms * sizeof(int);
-  b += ((size_t)npc * (n_sites + 1) + 2 * (size_t)(nx + ny)) * sizeof(int);
   return b + 64;
 }
 
@@ -100,9 +95,6 @@ __device__ __forceinline__ HeomSmem<T> heom_carve(unsigned char* raw, const Heom
   s.shift = s.W + p.E;
   s.nbr = (int*)(s.shift + npc);
   s.site = s.nbr + npc * p.nterms;
-  s.tstart = s.site + npc * p.nterms;
-  s.sx = s.tstart + npc * (p.n_sites + 1);
-  s.sy = s.sx + 2 * p.nx;
   return s;
 }
 
@@ -142,32 +134,6 @@ __device__ __forceinline__ void heom_stage_smem(const HeomP& p, const typename c
   }
   const C* xb = x + (b * p.nnodes + n0) * (int64_t)p.E;
   for (int i = tid; i < nn * p.E; i += nt) s.x[i] = xb[i];
-  __syncthreads();
-  // per node, where each site's terms start (terms are grouped by site; a
-  // term whose site is out of range, or padding, belongs to no site)
-  for (int l = tid; l < npc; l += nt) {
-    int* ts = s.tstart + l * (p.n_sites + 1);
-    const int* st = s.site + l * p.nterms;
-    const int* nb = s.nbr + l * p.nterms;
-    int t = 0;
-    for (int j = 0; j <= p.n_sites; ++j) {
-      while (t < p.nterms && nb[t] >= 0 && st[t] < j) ++t;
-      ts[j] = t;
-    }
-  }
-  // the sites occupied in each state (number operators: at most two)
-  for (int i = tid; i < p.nx + p.ny; i += nt) {
-    const bool isx = i < p.nx;
-    const int st = isx ? i : i - p.nx;
-    const T* o = isx ? s.ox : s.oy;
-    const int n = isx ? p.nx : p.ny;
-    int found[2] = {-1, -1}, k = 0;
-    for (int j = 0; j < p.n_sites && k < 2; ++j)
-      if (o[j * n + st] != (T)0) found[k++] = j;
-    int* dst = isx ? s.sx + 2 * st : s.sy + 2 * st;
-    dst[0] = found[0];
-    dst[1] = found[1];
-  }
   __syncthreads();
 }
 
@@ -315,7 +281,6 @@ __host__ __device__ inline size_t heom_cluster_smem_bytes(int nx, int ny, int n_
   b += 2 * (size_t)npcta * nterms * sizeof(C);                         // alpha, beta
   b += ((size_t)nx * nx + ny * ny + (size_t)n_sites * (nx + ny) + E + npcta) * sizeof(T);
   b += 2 * (size_t)npcta * nterms * sizeof(int);                       // nbr, site
-  b += ((size_t)npcta * (n_sites + 1) + 2 * (size_t)(nx + ny)) * sizeof(int);
   return b + 64;
 }
 
@@ -343,9 +308,6 @@ __global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
   T* ssh = sW + E;
   int* snb = (int*)(ssh + p.npcta);
   int* sst = snb + p.npcta * nt;
-  int* sts = sst + p.npcta * nt;                        // [npcta][N + 1]
-  int* ssx = sts + p.npcta * (N + 1);                   // [nx][2]
-  int* ssy = ssx + 2 * nx;                              // [ny][2]
 
   const double* hx = p.Hx + smp * p.Hx_stride;
   const double* hy = p.Hy + smp * p.Hy_stride;
@@ -366,26 +328,6 @@ __global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
     sbe[i] = cmk((T)b.x, (T)b.y);
   }
   __syncthreads();
-  for (int l = tid; l < p.npcta; l += bd) {
-    int t = 0;
-    for (int j = 0; j <= N; ++j) {
-      while (t < nt && snb[l * nt + t] >= 0 && sst[l * nt + t] < j) ++t;
-      sts[l * (N + 1) + j] = t;
-    }
-  }
-  for (int i = tid; i < nx + ny; i += bd) {
-    const bool isx = i < nx;
-    const int st = isx ? i : i - nx;
-    const T* o = isx ? sox : soy;
-    const int n = isx ? nx : ny;
-    int found[2] = {-1, -1}, k = 0;
-    for (int j = 0; j < N && k < 2; ++j)
-      if (o[j * n + st] != (T)0) found[k++] = j;
-    int* dst = isx ? ssx + 2 * st : ssy + 2 * st;
-    dst[0] = found[0];
-    dst[1] = found[1];
-  }
-
   // this thread's elements: state (split-word in FP32) and RK4 accumulator
   Cx yh[EPT], yl[EPT], acc[EPT];
   const double2* y0 = p.y0 + smp * p.y0_stride;
@@ -426,9 +368,12 @@ __global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
       Cx* xout = sx + (size_t)(buf ^ 1) * p.npcta * E;
       const T cnext = stage == 2 ? h : (T)0.5 * h;
       const T wg = (stage == 0 || stage == 3) ? (T)1 : (T)2;
+      // commutator and diagonal terms of every element of this thread
+      T orr[EPT], oi[EPT];
 #pragma unroll
       for (int u = 0; u < EPT; ++u) {
         const int el = tid + u * bd;
+        orr[u] = oi[u] = (T)0;
         if (el >= Mloc) continue;
         const int l = el / E, e = el % E;
         const int a = e % nx, bb = e / nx;
@@ -448,28 +393,50 @@ __global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
           ci = fma(-hv, v.y, ci);
         }
         const Cx self = xs[e];
-        T orr = ci, oi = -cr;
         const T sh = ssh[l] + sW[e];
-        orr = fma(-sh, self.x, orr);
-        oi = fma(-sh, self.y, oi);
-        // couplings: every term of the node in the same order in all lanes
-        // (a warp serves one node when E is a multiple of 32), so each
-        // neighbour block is read with one coalesced access, local or
-        // through distributed shared memory
-        for (int t = l * nt; t < (l + 1) * nt; ++t) {
-          const int m = snb[t];
-          if (m < 0) break;
-          const int j = sst[t];
+        orr[u] = fma(-sh, self.x, ci);
+        oi[u] = fma(-sh, self.y, -cr);
+      }
+      // couplings, term by term across all of the thread's elements, so the
+      // neighbour loads of different elements (local or through distributed
+      // shared memory) are in flight together; the lanes serving one node
+      // read its terms in the same order (one coalesced access per warp when
+      // E is a multiple of 32)
+      for (int t = 0; t < nt; ++t) {
+        Cx v[EPT];
+        int tt[EPT];
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+          const int el = tid + u * bd;
+          tt[u] = -1;
+          v[u] = cmk((T)0, (T)0);
+          if (el >= Mloc) continue;
+          const int l = el / E;
+          const int m = snb[l * nt + t];
+          if (m < 0) continue;
+          tt[u] = l * nt + t;
           const int r = m / p.npcta, ml = m - r * p.npcta;
           const Cx* src = r == rank ? xin : cluster.map_shared_rank(xin, r);
-          const Cx v = src[ml * E + e];
-          const Cx al = sal[t], be = sbe[t];
+          v[u] = src[ml * E + el % E];
+        }
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+          if (tt[u] < 0) continue;
+          const int e = (tid + u * bd) % E;
+          const int a = e % nx, bb = e / nx;
+          const int j = sst[tt[u]];
+          const Cx al = sal[tt[u]], be = sbe[tt[u]];
           const T oa = sox[j * nx + a], ob = soy[j * ny + bb];
           const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
-          orr = fma(fr, v.x, fma(-fi, v.y, orr));
-          oi = fma(fr, v.y, fma(fi, v.x, oi));
+          orr[u] = fma(fr, v[u].x, fma(-fi, v[u].y, orr[u]));
+          oi[u] = fma(fr, v[u].y, fma(fi, v[u].x, oi[u]));
         }
-        const Cx d = cmk(uc * orr, uc * oi);
+      }
+#pragma unroll
+      for (int u = 0; u < EPT; ++u) {
+        const int el = tid + u * bd;
+        if (el >= Mloc) continue;
+        const Cx d = cmk(uc * orr[u], uc * oi[u]);
         acc[u] = stage == 0 ? d : cmk(acc[u].x + wg * d.x, acc[u].y + wg * d.y);
         if (stage < 3) {
           xout[el] = cmk(yh[u].x + cnext * d.x, yh[u].y + cnext * d.y);

@@ -208,6 +208,45 @@ class HEOMEquationOfMotion(EquationOfMotion):
         return out if is_tensor else out.cpu().numpy()
 
 
+class HEOMMultiBlockEquationOfMotion(EquationOfMotion):
+    """The HEOM generator on a Liouville subspace of several blocks (e.g.
+    'gg,ge,eg,ee'; heom.py:298-443 builds it on the union of the blocks).
+    H and the couplings are block-diagonal over the manifolds, so every block
+    XY of every node evolves on its own: each block runs its structured
+    generator on its share of the node vectors, gathered from and scattered
+    back to the positions that block holds in the union's ascending
+    column-stacked order."""
+
+    def __init__(self, model, liouville_subspace, heisenberg_picture):
+        super().__init__(None, liouville_subspace, heisenberg_picture, model)
+        full = model.lspace_model.liouville_subspace_index(liouville_subspace)
+        self.M = len(full)
+        self.nnodes = model.ado_count
+        self.parts = []
+        for blk in liouville_subspace.split(','):
+            eom = model.equation_of_motion(blk, heisenberg_picture)
+            pos = np.searchsorted(full, model.lspace_model.liouville_subspace_index(blk))
+            flat = (np.arange(self.nnodes)[:, None] * self.M + pos[None, :]).reshape(-1)
+            self.parts.append((eom, flat))
+
+    @property
+    def dim(self):
+        return self.nnodes * self.M
+
+    def gather(self, x, flat):
+        return x[..., _native.const_tensor(flat, torch.int64, x.device)]
+
+    def scatter(self, out, flat, values):
+        out[..., _native.const_tensor(flat, torch.int64, out.device)] = values
+
+    def __call__(self, t, rho):
+        x, is_tensor = _as_device(rho)
+        out = torch.zeros_like(x)
+        for eom, flat in self.parts:
+            self.scatter(out, flat, eom(t, self.gather(x, flat)))
+        return out if is_tensor else out.cpu().numpy()
+
+
 def map_over_ados(func, state, ado_count, from_size):
     s = np.asarray(state)
     blocks = s.reshape(s.shape[:-1] + (ado_count, from_size))
@@ -290,8 +329,13 @@ class HEOMModel(DynamicalModel):
         return Hx, Hy
 
     def equation_of_motion(self, liouville_subspace, heisenberg_picture=False):
-        """heom.py:228-244 as a GPU-resident callable."""
+        """heom.py:228-244 as a GPU-resident callable; a subspace of several
+        Liouville blocks composes the blocks' generators."""
         key = ('eom', liouville_subspace, bool(heisenberg_picture))
+        if key not in self._cache and ',' in liouville_subspace:
+            _native.require_gpu()
+            self._cache[key] = HEOMMultiBlockEquationOfMotion(self, liouville_subspace,
+                                                             heisenberg_picture)
         if key not in self._cache:
             _native.require_gpu()
             tb = self.tables(liouville_subspace, heisenberg_picture)
@@ -301,10 +345,28 @@ class HEOMModel(DynamicalModel):
         return self._cache[key]
 
     def HEOM_tensor(self, liouville_subspace, heisenberg_picture=False):
-        """The generator as a sparse matrix, without unit_convert (heom.py:298-443)."""
-        tb = self.tables(liouville_subspace, heisenberg_picture)
+        """The generator as a sparse matrix, without unit_convert (heom.py:298-443);
+        several Liouville blocks give the block-diagonal generator on their
+        union, in the union's ascending column-stacked order per node."""
         H = self.hamiltonian.H(self.hilbert_subspace)
-        return tb.sparse(H[tb.sx, tb.sx], H[tb.sy, tb.sy], 1.0)
+        if ',' not in liouville_subspace:
+            tb = self.tables(liouville_subspace, heisenberg_picture)
+            return tb.sparse(H[tb.sx, tb.sx], H[tb.sy, tb.sy], 1.0)
+        full = self.lspace_model.liouville_subspace_index(liouville_subspace)
+        M = len(full)
+        rows, cols, vals = [], [], []
+        for blk in liouville_subspace.split(','):
+            tb = self.tables(blk, heisenberg_picture)
+            L = tb.sparse(H[tb.sx, tb.sx], H[tb.sy, tb.sy], 1.0).tocoo()
+            pos = np.searchsorted(full, self.lspace_model.liouville_subspace_index(blk))
+            Mb = len(pos)
+            rows.append((L.row // Mb) * M + pos[L.row % Mb])
+            cols.append((L.col // Mb) * M + pos[L.col % Mb])
+            vals.append(L.data)
+        n = self.ado_count * M
+        return sps.coo_matrix((np.concatenate(vals), (np.concatenate(rows),
+                                                      np.concatenate(cols))),
+                              shape=(n, n)).tocsr()
 
     def thermal_state(self, liouville_subspace):
         rho0 = self.lspace_model.thermal_state(liouville_subspace)

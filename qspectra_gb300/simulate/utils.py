@@ -100,7 +100,10 @@ def integrate(f, y0, t, t0=None, method_name='rk4', f_params=None,
     None or a linear map from an operator (e.g. ``V.commutator``,
     ``V.expectation_value``).  A 2-D ``y0`` integrates every row.
     """
-    from ..dynamics.heom import HEOMEquationOfMotion
+    from ..dynamics.heom import HEOMEquationOfMotion, HEOMMultiBlockEquationOfMotion
+    if isinstance(f, HEOMMultiBlockEquationOfMotion):
+        return _integrate_heom_blocks(f, y0, t, t0, save_func, precision, step,
+                                      kwargs.pop('heom_nodes', None))
     from ..dynamics.zofe import ZOFEEquationOfMotion
     if isinstance(f, HEOMEquationOfMotion):
         return _integrate_heom(f, y0, t, t0, save_func, precision, step,
@@ -180,6 +183,32 @@ def _integrate_heom(f, y0, t, t0, save_func, precision, step, heom_nodes):
     if squeeze:
         state = state[0]
     return state.cpu().numpy() if as_numpy else state
+
+
+def _integrate_heom_blocks(f, y0, t, t0, save_func, precision, step, heom_nodes):
+    """integrate() for a HEOM generator on several Liouville blocks: the
+    blocks evolve independently, so each runs its own loop on its share of
+    the node vectors and the outputs are scattered back to the union."""
+    as_numpy = not isinstance(y0, torch.Tensor)
+    y = torch.as_tensor(np.asarray(y0, dtype=complex) if as_numpy else y0,
+                        dtype=torch.complex128, device='cuda')
+    nodes = f.nnodes if heom_nodes is None else int(heom_nodes)
+    out = None
+    for eom, flat in f.parts:
+        part = _integrate_heom(eom, f.gather(y, flat), t, t0, None, precision, step, nodes)
+        if out is None:
+            out = torch.zeros(part.shape[:-1] + (nodes * f.M,), dtype=part.dtype,
+                              device=part.device)
+        f.scatter(out, flat[:part.shape[-1]], part)
+    if save_func is not None:
+        if isinstance(save_func, LinearMap):
+            out = out @ save_func.matrix.T
+            if save_func.scalar:
+                out = out[..., 0]
+        else:
+            res = np.asarray(save_func(out.cpu().numpy()))
+            return res if as_numpy else torch.as_tensor(res, device='cuda')
+    return out.cpu().numpy() if as_numpy else out
 
 
 def uniform_save_plan(t, t0, step):
