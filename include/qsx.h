@@ -445,6 +445,10 @@ typedef struct {
   void* workspace;
   size_t workspace_bytes;
   int32_t* status;     /* device int: QSX_ERR_NONFINITE on NaN/Inf */
+  const double* gamma; /* complex128 [nnodes][nterms]: aki_temp_corr coefficient of
+                          each term (heom.py:438-442), or NULL */
+  const double* Wraw;  /* [nx * ny] unscaled double-commutator weights the gamma
+                          terms multiply (with occ_j(a) - occ_j(b)), or NULL */
 } qsx_heom_args;
 
 int qsx_heom_workspace_bytes(const qsx_heom_args* args, size_t* bytes);

@@ -67,7 +67,7 @@ class HeomArgs(ctypes.Structure):
         ('y0', _c_vp), ('y0_stride', ctypes.c_int64),
         ('out_state', _c_vp), ('out_mean', _c_vp),
         ('workspace', _c_vp), ('workspace_bytes', ctypes.c_size_t),
-        ('status', _c_vp),
+        ('status', _c_vp), ('gamma', _c_vp), ('Wraw', _c_vp),
     ]
 
 
@@ -830,6 +830,8 @@ def _heom_args(tables, Hx, Hy, unit_convert, batch, precision=QSX_FP64):
     a.W = d['W'].data_ptr() if d['W'] is not None else None
     a.shift, a.nbr, a.site = d['shift'].data_ptr(), d['nbr'].data_ptr(), d['site'].data_ptr()
     a.alpha, a.beta = d['alpha'].data_ptr(), d['beta'].data_ptr()
+    a.gamma = d['gamma'].data_ptr() if d['gamma'] is not None else None
+    a.Wraw = d['Wraw'].data_ptr() if d['Wraw'] is not None else None
     a.unit_convert = unit_convert
     return a
 

@@ -10,7 +10,10 @@
 // where j = site of term t, W[a][b] = sum_j (o_j(a) + o_j(b) - 2 o_j(a) o_j(b))
 // is the low-temperature double commutator sum_j [K_j, [K_j, .]] for number
 // operators, and the term table holds the up couplings (alpha, beta) =
-// (-i m, +i m) and the down couplings (-i m c_k, +i m conj(c_k)).  The
+// (-i m, +i m) and the down couplings (-i m c_k, +i m conj(c_k)).  With
+// aki_temp_corr (heom.py:385-442) a down term also carries
+// gamma_t Wd[a][b] (occ_j(a) - occ_j(b)) rho_nbr with the raw (unscaled)
+// double-commutator weights Wd.  The
 // transposed generator (Heisenberg picture) has the same form with the term
 // table transposed, which the host builds.
 #include <cooperative_groups.h>
@@ -37,6 +40,8 @@ struct HeomP {
   const int* site;      // [nnodes][nterms]
   const double2* alpha;  // [nnodes][nterms]
   const double2* beta;   // [nnodes][nterms]
+  const double2* gamma;  // [nnodes][nterms] or null (aki_temp_corr terms)
+  const double* Wraw;    // [E] or null
   double uc, h;
   // FP32 copies of the tables, made once per qsx_heom_rk4 call so the FP32
   // stage kernel stages them without FP64 conversions (null for FP64)
@@ -48,6 +53,8 @@ struct HeomP {
   const float* shift32;
   const float2* alpha32;
   const float2* beta32;
+  const float2* gamma32;
+  const float* Wraw32;
   float uc32, h32;
 };
 
@@ -65,6 +72,8 @@ struct HeomSmem {
   T* shift;   // npc
   C* al;      // npc * nterms
   C* be;      // npc * nterms
+  C* ga;      // npc * nterms (zero without aki_temp_corr)
+  T* Wr;      // E
   int* nbr;   // npc * nterms
   int* site;  // npc * nterms
   C* x;       // npc * E, this CTA's node blocks of the input
@@ -74,8 +83,8 @@ template <typename T>
 __host__ __device__ inline size_t heom_smem_bytes(int nx, int ny, int n_sites, int E, int npc,
                                                   int nterms) {
   using C = typename cplx<T>::type;
-  size_t b = (size_t)npc * E * sizeof(C) + 2 * (size_t)npc * nterms * sizeof(C);
-  b += ((size_t)nx * nx + ny * ny + (size_t)n_sites * (nx + ny) + E + npc) * sizeof(T);
+  size_t b = (size_t)npc * E * sizeof(C) + 3 * (size_t)npc * nterms * sizeof(C);
+  b += ((size_t)nx * nx + ny * ny + (size_t)n_sites * (nx + ny) + 2 * E + npc) * sizeof(T);
   b += 2 * (size_t)npc * nterms * sizeof(int);
   return b + 64;
 }
@@ -87,12 +96,14 @@ __device__ __forceinline__ HeomSmem<T> heom_carve(unsigned char* raw, const Heom
   s.x = (C*)raw;
   s.al = s.x + npc * p.E;
   s.be = s.al + npc * p.nterms;
-  s.Hx = (T*)(s.be + npc * p.nterms);
+  s.ga = s.be + npc * p.nterms;
+  s.Hx = (T*)(s.ga + npc * p.nterms);
   s.Hy = s.Hx + p.nx * p.nx;
   s.ox = s.Hy + p.ny * p.ny;
   s.oy = s.ox + p.n_sites * p.nx;
   s.W = s.oy + p.n_sites * p.ny;
-  s.shift = s.W + p.E;
+  s.Wr = s.W + p.E;
+  s.shift = s.Wr + p.E;
   s.nbr = (int*)(s.shift + npc);
   s.site = s.nbr + npc * p.nterms;
   return s;
@@ -110,6 +121,7 @@ __device__ __forceinline__ void heom_stage_smem(const HeomP& p, const typename c
     for (int i = tid; i < p.n_sites * p.nx; i += nt) s.ox[i] = p.occx32[i];
     for (int i = tid; i < p.n_sites * p.ny; i += nt) s.oy[i] = p.occy32[i];
     for (int i = tid; i < p.E; i += nt) s.W[i] = p.W32 ? p.W32[i] : 0.f;
+    for (int i = tid; i < p.E; i += nt) s.Wr[i] = p.Wraw32 ? p.Wraw32[i] : 0.f;
     for (int i = tid; i < npc; i += nt) s.shift[i] = i < nn ? p.shift32[n0 + i] : 0.f;
   } else {
     for (int i = tid; i < p.nx * p.nx; i += nt) s.Hx[i] = p.Hx[b * p.Hx_stride + i];
@@ -117,6 +129,7 @@ __device__ __forceinline__ void heom_stage_smem(const HeomP& p, const typename c
     for (int i = tid; i < p.n_sites * p.nx; i += nt) s.ox[i] = p.occx[i];
     for (int i = tid; i < p.n_sites * p.ny; i += nt) s.oy[i] = p.occy[i];
     for (int i = tid; i < p.E; i += nt) s.W[i] = p.W ? p.W[i] : 0.0;
+    for (int i = tid; i < p.E; i += nt) s.Wr[i] = p.Wraw ? p.Wraw[i] : 0.0;
     for (int i = tid; i < npc; i += nt) s.shift[i] = i < nn ? p.shift[n0 + i] : 0.0;
   }
   for (int i = tid; i < npc * p.nterms; i += nt) {
@@ -127,9 +140,11 @@ __device__ __forceinline__ void heom_stage_smem(const HeomP& p, const typename c
     if constexpr (sizeof(T) == 4) {
       s.al[i] = ok ? p.alpha32[g] : make_float2(0.f, 0.f);
       s.be[i] = ok ? p.beta32[g] : make_float2(0.f, 0.f);
+      s.ga[i] = (ok && p.gamma32) ? p.gamma32[g] : make_float2(0.f, 0.f);
     } else {
       s.al[i] = ok ? p.alpha[g] : make_double2(0.0, 0.0);
       s.be[i] = ok ? p.beta[g] : make_double2(0.0, 0.0);
+      s.ga[i] = (ok && p.gamma) ? p.gamma[g] : make_double2(0.0, 0.0);
     }
   }
   const C* xb = x + (b * p.nnodes + n0) * (int64_t)p.E;
@@ -174,9 +189,10 @@ __device__ __forceinline__ void heom_rhs_elem(const HeomP& p, const typename cpl
     const int nb = s.nbr[base + t];
     if (nb < 0) break;
     const int j = s.site[base + t];
-    const C al = s.al[base + t], be = s.be[base + t];
+    const C al = s.al[base + t], be = s.be[base + t], ga = s.ga[base + t];
     const T oa = s.ox[j * p.nx + a], ob = s.oy[j * p.ny + bb];
-    const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
+    const T gw = s.Wr[e] * (oa - ob);
+    const T fr = al.x * oa + be.x * ob + ga.x * gw, fi = al.y * oa + be.y * ob + ga.y * gw;
     const C v = xb[(int64_t)nb * p.E + e];
     orr = fma(fr, v.x, fma(-fi, v.y, orr));
     oi = fma(fr, v.y, fma(fi, v.x, oi));
@@ -267,6 +283,8 @@ struct HeomCP {
   const int* site;
   const double2* alpha;
   const double2* beta;
+  const double2* gamma;
+  const double* Wraw;
   double uc, h;
   const double2* y0;
   double2* saves;   // [batch][nsave][keep * E]
@@ -278,8 +296,8 @@ __host__ __device__ inline size_t heom_cluster_smem_bytes(int nx, int ny, int n_
                                                           int npcta, int nterms) {
   using C = typename cplx<T>::type;
   size_t b = 2 * (size_t)npcta * E * sizeof(C);                        // stage inputs
-  b += 2 * (size_t)npcta * nterms * sizeof(C);                         // alpha, beta
-  b += ((size_t)nx * nx + ny * ny + (size_t)n_sites * (nx + ny) + E + npcta) * sizeof(T);
+  b += 3 * (size_t)npcta * nterms * sizeof(C);                         // alpha, beta, gamma
+  b += ((size_t)nx * nx + ny * ny + (size_t)n_sites * (nx + ny) + 2 * E + npcta) * sizeof(T);
   b += 2 * (size_t)npcta * nterms * sizeof(int);                       // nbr, site
   return b + 64;
 }
@@ -300,12 +318,14 @@ __global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
   Cx* sx = (Cx*)smraw;                                  // [2][npcta E]
   Cx* sal = sx + 2 * (size_t)p.npcta * E;               // [npcta nterms]
   Cx* sbe = sal + (size_t)p.npcta * nt;
-  T* sHx = (T*)(sbe + (size_t)p.npcta * nt);
+  Cx* sga = sbe + (size_t)p.npcta * nt;
+  T* sHx = (T*)(sga + (size_t)p.npcta * nt);
   T* sHy = sHx + nx * nx;
   T* sox = sHy + ny * ny;
   T* soy = sox + N * nx;
   T* sW = soy + N * ny;
-  T* ssh = sW + E;
+  T* sWr = sW + E;
+  T* ssh = sWr + E;
   int* snb = (int*)(ssh + p.npcta);
   int* sst = snb + p.npcta * nt;
 
@@ -316,6 +336,7 @@ __global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
   for (int i = tid; i < N * nx; i += bd) sox[i] = (T)p.occx[i];
   for (int i = tid; i < N * ny; i += bd) soy[i] = (T)p.occy[i];
   for (int i = tid; i < E; i += bd) sW[i] = p.W ? (T)p.W[i] : (T)0;
+  for (int i = tid; i < E; i += bd) sWr[i] = p.Wraw ? (T)p.Wraw[i] : (T)0;
   for (int i = tid; i < p.npcta; i += bd) ssh[i] = i < nloc ? (T)p.shift[node0 + i] : (T)0;
   for (int i = tid; i < p.npcta * nt; i += bd) {
     const bool ok = i < nloc * nt;
@@ -324,8 +345,10 @@ __global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
     sst[i] = ok ? p.site[g] : 0;
     const double2 a = ok ? p.alpha[g] : make_double2(0.0, 0.0);
     const double2 b = ok ? p.beta[g] : make_double2(0.0, 0.0);
+    const double2 c = (ok && p.gamma) ? p.gamma[g] : make_double2(0.0, 0.0);
     sal[i] = cmk((T)a.x, (T)a.y);
     sbe[i] = cmk((T)b.x, (T)b.y);
+    sga[i] = cmk((T)c.x, (T)c.y);
   }
   __syncthreads();
   // this thread's elements: state (split-word in FP32) and RK4 accumulator
@@ -425,9 +448,10 @@ __global__ void __launch_bounds__(512, 1) heom_cluster_kernel(HeomCP p) {
           const int e = (tid + u * bd) % E;
           const int a = e % nx, bb = e / nx;
           const int j = sst[tt[u]];
-          const Cx al = sal[tt[u]], be = sbe[tt[u]];
+          const Cx al = sal[tt[u]], be = sbe[tt[u]], ga = sga[tt[u]];
           const T oa = sox[j * nx + a], ob = soy[j * ny + bb];
-          const T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
+          const T gw = sWr[e] * (oa - ob);
+          const T fr = al.x * oa + be.x * ob + ga.x * gw, fi = al.y * oa + be.y * ob + ga.y * gw;
           orr[u] = fma(fr, v[u].x, fma(-fi, v[u].y, orr[u]));
           oi[u] = fma(fr, v[u].y, fma(fi, v[u].x, oi[u]));
         }
@@ -561,12 +585,15 @@ static HeomP heom_params(const qsx_heom_args* a) {
   p.site = a->site;
   p.alpha = (const double2*)a->alpha;
   p.beta = (const double2*)a->beta;
+  p.gamma = (const double2*)a->gamma;
+  p.Wraw = a->Wraw;
   p.uc = a->unit_convert;
   p.h = a->h;
   p.uc32 = (float)a->unit_convert;
   p.h32 = (float)a->h;
   p.Hx32 = p.Hy32 = p.occx32 = p.occy32 = p.W32 = p.shift32 = nullptr;
-  p.alpha32 = p.beta32 = nullptr;
+  p.alpha32 = p.beta32 = p.gamma32 = nullptr;
+  p.Wraw32 = nullptr;
   return p;
 }
 
@@ -633,6 +660,8 @@ static int heom_rk4_cluster(const qsx_heom_args* a, double2* saves, cudaStream_t
   p.site = a->site;
   p.alpha = (const double2*)a->alpha;
   p.beta = (const double2*)a->beta;
+  p.gamma = (const double2*)a->gamma;
+  p.Wraw = a->Wraw;
   p.uc = a->unit_convert;
   p.h = a->h;
   p.y0 = (const double2*)a->y0;
@@ -670,7 +699,7 @@ __global__ void f64_to_f32_kernel(const double* __restrict__ src, float* __restr
 
 // element counts of the FP32 table copies: Hx, Hy, occx, occy, W, shift,
 // alpha and beta (the last two as floats, two per complex entry)
-static void heom_table_counts(const qsx_heom_args* a, int64_t c[8]) {
+static void heom_table_counts(const qsx_heom_args* a, int64_t c[10]) {
   const int64_t hb = a->H_stride ? a->batch : 1;
   c[0] = hb * a->nx * a->nx;
   c[1] = hb * a->ny * a->ny;
@@ -680,13 +709,15 @@ static void heom_table_counts(const qsx_heom_args* a, int64_t c[8]) {
   c[5] = a->nnodes;
   c[6] = 2 * (int64_t)a->nnodes * a->nterms;
   c[7] = c[6];
+  c[8] = a->gamma ? c[6] : 0;
+  c[9] = a->Wraw ? (int64_t)a->nx * a->ny : 0;
 }
 
 static size_t heom_table_bytes(const qsx_heom_args* a) {
-  int64_t c[8];
+  int64_t c[10];
   heom_table_counts(a, c);
   size_t b = 0;
-  for (int i = 0; i < 8; ++i) b += ((size_t)c[i] * sizeof(float) + 255) & ~(size_t)255;
+  for (int i = 0; i < 10; ++i) b += ((size_t)c[i] * sizeof(float) + 255) & ~(size_t)255;
   return b;
 }
 
@@ -788,12 +819,12 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
           a->out_mean ? (size_t)p.batch * nsave_ * keep * p.E * sizeof(double2) : 0;
       unsigned char* tp =
           (unsigned char*)((((size_t)saves + save_bytes) + 255) & ~(size_t)255);
-      int64_t c[8];
+      int64_t c[10];
       heom_table_counts(a, c);
-      const double* src[8] = {a->Hx, a->Hy, a->occx, a->occy, a->W, a->shift, a->alpha,
-                              a->beta};
-      float* dst[8];
-      for (int i = 0; i < 8; ++i) {
+      const double* src[10] = {a->Hx, a->Hy, a->occx, a->occy, a->W, a->shift, a->alpha,
+                               a->beta, a->gamma, a->Wraw};
+      float* dst[10];
+      for (int i = 0; i < 10; ++i) {
         dst[i] = (float*)tp;
         tp += ((size_t)c[i] * sizeof(float) + 255) & ~(size_t)255;
         if (c[i] > 0 && src[i])
@@ -808,6 +839,8 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
       p.shift32 = dst[5];
       p.alpha32 = (const float2*)dst[6];
       p.beta32 = (const float2*)dst[7];
+      p.gamma32 = a->gamma ? (const float2*)dst[8] : nullptr;
+      p.Wraw32 = a->Wraw ? dst[9] : nullptr;
     }
     const size_t smem = heom_smem_bytes<T>(p.nx, p.ny, p.n_sites, p.E, npc, p.nterms);
     QSX_CHECK_ARG(smem <= 227 * 1024, "qsx_heom_rk4: node tables too large for shared memory");

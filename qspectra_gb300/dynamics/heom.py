@@ -65,8 +65,14 @@ def corr_func_coeffs(K, gamma, T, reorg_en, nu, aki_temp_corr=False):
 class HEOMTables:
     """Node tables of the HEOM generator on one Liouville block XY.
 
-    terms[n] lists (neighbour m, site j, alpha, beta): node n receives
-    (alpha occ_j(a) + beta occ_j(b)) rho_m[a, b] (heom.py:410-442);
+    terms[n] lists (neighbour m, site j, alpha, beta, gamma): node n receives
+    (alpha occ_j(a) + beta occ_j(b) + gamma Wd[a, b] (occ_j(a) - occ_j(b)))
+    rho_m[a, b] (heom.py:410-442), with Wd[a, b] = sum_i (occ_i(a) + occ_i(b)
+    - 2 occ_i(a) occ_i(b)) the double commutator sum_i [K_i, [K_i, .]] for
+    number operators.  gamma is nonzero only for the down couplings under
+    aki_temp_corr (heom.py:438-442: -i 4 lam gamma^2 / (nu_1^2 - gamma^2)
+    times that double commutator, which for number operators is diagonal, so
+    the reference's product with the coupling's commutator is elementwise).
     ``transpose`` swaps sender and receiver (the Heisenberg picture).
     """
 
@@ -92,6 +98,9 @@ class HEOMTables:
         K = model.K
         nu = matsubara_frequencies(K, g, T)
         c = corr_func_coeffs(K, g, T, lam, nu, model.aki_temp_corr)
+        nu_inf = matsubara_frequencies(K + 5000, g, T)
+        c_inf = corr_func_coeffs(K + 5000, g, T, lam, nu_inf, model.aki_temp_corr)
+        kappa = 4 * lam * g ** 2 / (nu_inf[1] ** 2 - g ** 2)
         ados = model.ado_indices
         pos = {tuple(a.reshape(-1)): i for i, a in enumerate(ados)}
         self.nnodes = len(ados)
@@ -104,21 +113,20 @@ class HEOMTables:
                 p = pos.get(tuple(up.reshape(-1)))
                 if p is not None:
                     m = np.sqrt((njk + 1) * np.abs(c[k])) if model.modified_HEOM else 1.0
-                    terms[n].append((p, j, -1j * m, 1j * m))
+                    terms[n].append((p, j, -1j * m, 1j * m, 0.0))
                 if njk > 0:
                     dn = ado.copy()
                     dn[j, k] -= 1
                     q = pos[tuple(dn.reshape(-1))]
                     m = np.sqrt(njk / np.abs(c[k])) if model.modified_HEOM else njk
                     a_, b_ = -1j * m * c[k], 1j * m * np.conj(c[k])
-                    if model.aki_temp_corr:
-                        raise NotImplementedError('aki_temp_corr is not on the GPU path')
-                    terms[n].append((q, j, a_, b_))
+                    g_ = -1j * kappa if model.aki_temp_corr else 0.0
+                    terms[n].append((q, j, a_, b_, g_))
         if transpose:
             tt = [[] for _ in range(self.nnodes)]
             for n, lst in enumerate(terms):
-                for (m, j, a_, b_) in lst:
-                    tt[m].append((n, j, a_, b_))
+                for (m, j, a_, b_, g_) in lst:
+                    tt[m].append((n, j, a_, b_, g_))
             terms = tt
         # grouped by site (stable): the kernel visits only the sites a
         # state occupies, through per-site ranges of this list
@@ -130,19 +138,26 @@ class HEOMTables:
         self.site = np.zeros((self.nnodes, nt), np.int32)
         self.alpha = np.zeros((self.nnodes, nt), complex)
         self.beta = np.zeros((self.nnodes, nt), complex)
+        self.gamma = np.zeros((self.nnodes, nt), complex)
         for n, lst in enumerate(terms):
-            for t, (m, j, a_, b_) in enumerate(lst):
+            for t, (m, j, a_, b_, g_) in enumerate(lst):
                 self.nbr[n, t], self.site[n, t] = m, j
-                self.alpha[n, t], self.beta[n, t] = a_, b_
-        # low-temperature correction sum_j [K_j, [K_j, .]] (heom.py:386-408)
+                self.alpha[n, t], self.beta[n, t], self.gamma[n, t] = a_, b_, g_
+        ox, oy = self.occx[:, :, None], self.occy[:, None, :]
+        Wab = np.sum(ox + oy - 2 * ox * oy, axis=0).reshape(-1, order='F')  # [nx ny]
+        # raw double-commutator weights of the aki_temp_corr down terms
+        self.Wraw = Wab.astype(float) if model.aki_temp_corr else None
+        if not model.aki_temp_corr:
+            self.gamma = None
+        # low-temperature correction sum_j [K_j, [K_j, .]] (heom.py:386-408),
+        # also applied under aki_temp_corr with the coefficient c_1 / nu_1
         self.W = None
-        if model.low_temp_corr:
-            nu_inf = matsubara_frequencies(K + 5000, g, T)
-            c_inf = corr_func_coeffs(K + 5000, g, T, lam, nu_inf, model.aki_temp_corr)
-            tc = np.sum((np.array(c_inf) / nu_inf)[K + 1:]).real
-            ox, oy = self.occx[:, :, None], self.occy[:, None, :]
-            Wab = np.sum(ox + oy - 2 * ox * oy, axis=0)  # [nx, ny]
-            self.W = tc * Wab.reshape(-1, order='F')
+        if model.low_temp_corr or model.aki_temp_corr:
+            if model.aki_temp_corr:
+                tc = (c_inf[1] / nu_inf[1]).real
+            else:
+                tc = np.sum((np.array(c_inf) / nu_inf)[K + 1:]).real
+            self.W = tc * Wab
         self.n_sites = N
         self._dev = None
 
@@ -155,7 +170,9 @@ class HEOMTables:
                 W=None if self.W is None else t(self.W, torch.float64),
                 shift=t(self.shift, torch.float64), nbr=t(self.nbr, torch.int32),
                 site=t(self.site, torch.int32), alpha=t(self.alpha, torch.complex128),
-                beta=t(self.beta, torch.complex128))
+                beta=t(self.beta, torch.complex128),
+                gamma=None if self.gamma is None else t(self.gamma, torch.complex128),
+                Wraw=None if self.Wraw is None else t(self.Wraw, torch.float64))
         return self._dev
 
     def sparse(self, Hx, Hy, unit_convert):
@@ -176,8 +193,11 @@ class HEOMTables:
                 if m < 0:
                     continue
                 j = self.site[n, t]
-                d = (self.alpha[n, t] * np.kron(np.ones(self.ny), self.occx[j])
-                     + self.beta[n, t] * np.kron(self.occy[j], np.ones(self.nx)))
+                ox = np.kron(np.ones(self.ny), self.occx[j])
+                oy = np.kron(self.occy[j], np.ones(self.nx))
+                d = self.alpha[n, t] * ox + self.beta[n, t] * oy
+                if self.gamma is not None:
+                    d = d + self.gamma[n, t] * self.Wraw * (ox - oy)
                 nz = np.nonzero(d)[0]
                 rows.append(nz + n * E)
                 cols.append(nz + m * E)

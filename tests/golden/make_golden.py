@@ -474,6 +474,27 @@ def drivers_main(ref_root):
     out['ring8_sample_H'] = hs.H_1exc
     out['ring8_traj_node0'] = traj[:, :64]
     out['ring8_final_state'] = traj[-1]
+
+    # ---- HEOM options: a multi-block Liouville subspace, aki_temp_corr ------
+    H2 = np.array([[12400., -100], [-100, 12480]])
+    bathh = qs.DebyeBath(qs.CM_K * 300, 35, 106)
+    hamh = qs.ElectronicHamiltonian(H2, bath=bathh, dipoles=[[1, 0, 0]] * 2)
+    out['heomopt_H'] = H2
+    hm = qs.HEOMModel(hamh, hilbert_subspace='ge', unit_convert=qs.CM_FS, K=1, level_cutoff=3)
+    for tag, sub in (('multi', 'gg,ge,eg,ee'), ('multi2', 'ge,ee')):
+        L = hm.HEOM_tensor(sub).tocoo()
+        out['heomopt_{}_row'.format(tag)] = L.row
+        out['heomopt_{}_col'.format(tag)] = L.col
+        out['heomopt_{}_val'.format(tag)] = L.data
+        out['heomopt_{}_n'.format(tag)] = np.array(L.shape)
+    for tag, kw in (('aki', dict(low_temp_corr=True)), ('aki_nolt', dict(low_temp_corr=False))):
+        hm = qs.HEOMModel(hamh, hilbert_subspace='e', unit_convert=qs.CM_FS, K=1,
+                          level_cutoff=3, aki_temp_corr=True, **kw)
+        L = hm.HEOM_tensor('ee').tocoo()
+        out['heomopt_{}_row'.format(tag)] = L.row
+        out['heomopt_{}_col'.format(tag)] = L.col
+        out['heomopt_{}_val'.format(tag)] = L.data
+        out['heomopt_{}_n'.format(tag)] = np.array(L.shape)
     np.savez_compressed(os.path.join(HERE, 'reference_golden_drivers.npz'), **out)
     print('wrote', len(out), 'arrays')
 

@@ -96,3 +96,66 @@ def test_heom_cluster_form_matches_per_stage_form(golden, tag, kw, heis, precisi
                                     save_nodes=m.ado_count, precision=precision,
                                     variant=variant)['state'].cpu().numpy())
     assert rel_err(out[0], out[1]) < tol
+
+
+def _drivers():
+    import os
+    from conftest import ROOT
+    with np.load(os.path.join(ROOT, 'tests', 'golden', 'reference_golden_drivers.npz')) as z:
+        return {k: z[k] for k in z.files}
+
+
+def _ref_sparse(g, tag):
+    import scipy.sparse as sps
+    return sps.coo_matrix((g['heomopt_{}_val'.format(tag)],
+                           (g['heomopt_{}_row'.format(tag)], g['heomopt_{}_col'.format(tag)])),
+                          shape=tuple(g['heomopt_{}_n'.format(tag)])).tocsr()
+
+
+@pytest.mark.parametrize('tag,sub', [('multi', 'gg,ge,eg,ee'), ('multi2', 'ge,ee')])
+@pytest.mark.parametrize('heis', [False, True])
+def test_heom_multiblock_subspace_matches_reference(tag, sub, heis):
+    """A Liouville subspace of several blocks (the reference builds the
+    generator on their union): the composed GPU generator, applied and
+    integrated, against the reference's HEOM_tensor."""
+    g = _drivers()
+    ham = qg.ElectronicHamiltonian(g['heomopt_H'], bath=qg.DebyeBath(qg.CM_K * 300, 35, 106),
+                                   dipoles=[[1, 0, 0]] * 2)
+    m = qg.HEOMModel(ham, hilbert_subspace='ge', unit_convert=qg.CM_FS, K=1, level_cutoff=3)
+    ref = qg.CM_FS * _ref_sparse(g, tag)
+    if heis:
+        ref = ref.T.tocsr()
+    eom = m.equation_of_motion(sub, heisenberg_picture=heis)
+    rng = np.random.RandomState(5)
+    x = rng.randn(2, ref.shape[0]) + 1j * rng.randn(2, ref.shape[0])
+    assert rel_err(eom(0.0, x), (ref @ x.T).T) < 1e-13
+    t = np.arange(0, 20.0, 0.5)
+    traj = qg.integrate(eom, x[0], t, step=0.5)
+    oref = orc.rk4_integrate_sparse(ref, x[0], len(t) - 1, 0.5)
+    assert rel_err(traj, oref) < 1e-10
+
+
+@pytest.mark.parametrize('tag,low', [('aki', True), ('aki_nolt', False)])
+@pytest.mark.parametrize('precision,tol', [(_native.QSX_FP64, 1e-10), (_native.QSX_FP32, 1e-4)])
+def test_heom_aki_temp_corr_matches_reference(tag, low, precision, tol):
+    """aki_temp_corr (heom.py:385-442): the generator against the reference's,
+    and both RK4 forms (persistent cluster and per-stage kernels) against the
+    oracle's RK4 over the reference matrix."""
+    g = _drivers()
+    ham = qg.ElectronicHamiltonian(g['heomopt_H'], bath=qg.DebyeBath(qg.CM_K * 300, 35, 106),
+                                   dipoles=[[1, 0, 0]] * 2)
+    m = qg.HEOMModel(ham, hilbert_subspace='e', unit_convert=qg.CM_FS, K=1, level_cutoff=3,
+                     aki_temp_corr=True, low_temp_corr=low)
+    ref = qg.CM_FS * _ref_sparse(g, tag)
+    rng = np.random.RandomState(6)
+    x = rng.randn(ref.shape[0]) + 1j * rng.randn(ref.shape[0])
+    if precision == _native.QSX_FP64:
+        assert rel_err(m.equation_of_motion('ee')(0.0, x), ref @ x) < 1e-13
+    oref = orc.rk4_integrate_sparse(ref, x, 60, 0.5)
+    tb = m.tables('ee')
+    Hx, Hy = m.block_hamiltonians('ee')
+    for variant in (0, 1):
+        out = _native.heom_rk4(tb, Hx, Hy, torch.as_tensor(x).cuda(), 60, 0.5, qg.CM_FS,
+                               batch=1, save_nodes=m.ado_count, precision=precision,
+                               variant=variant)['state'][0].cpu().numpy()
+        assert rel_err(out, oref) < tol
