@@ -421,8 +421,10 @@ typedef struct {
   int32_t save_every;  /* output every save_every steps */
   int32_t save_nodes;  /* leading nodes saved per output (1 = physical rho) */
   int32_t variant;     /* 0: the library's choice (the persistent cluster form,
-                          one launch for the whole loop, when it fits); 1: one
-                          launch per RK4 stage */
+                          one launch for the whole loop, when its shared memory
+                          fits and every sample's cluster is resident at once;
+                          else one launch per RK4 stage); 1: one launch per RK4
+                          stage; 2: the cluster form whenever it fits */
   int64_t batch;       /* disorder samples */
   int64_t H_stride;    /* 0: Hx, Hy shared; else per sample [batch][n][n] */
   const double* Hx;    /* real [nx][nx], rotating frame */
@@ -497,7 +499,15 @@ int qsx_rk4_field_batched(const void* L, int64_t L_stride, const void* C,
  * One thread-block cluster per sample splits the pseudomodes over its CTAs
  * (cluster 0 = chosen by the library); n <= 32 and at most 4096 state
  * elements per CTA.
+ * hermit (ZOFEModel's rho_hermit / ham_hermit, zofe.py:179-192): with
+ * QSX_ZOFE_RHO_HERMIT the last rho term is sum_s S_s rho^H L_s^H (the
+ * conjugate transpose of the second), and with both flags the third is
+ * rho^H (i H - a^H) as well (the right operator is then b^H, which equals
+ * i H - a^H for the symmetric H this entry takes).  Field terms act on rho
+ * itself in every form.
  */
+#define QSX_ZOFE_RHO_HERMIT 1
+#define QSX_ZOFE_HAM_HERMIT 2
 typedef struct {
   int32_t precision;     /* QSX_FP64 or QSX_FP32 */
   int32_t n;             /* Hilbert-space states */
@@ -528,7 +538,7 @@ typedef struct {
                             mode 1: [batch][M], the right-hand side */
   double* out_proj;      /* complex128 [batch][nsteps/save_every + 1][nproj] or NULL */
   int32_t* status;       /* device int: QSX_ERR_NONFINITE on NaN/Inf */
-  int32_t reserved;      /* must be 0 */
+  int32_t hermit;        /* 0 or QSX_ZOFE_RHO_HERMIT [| QSX_ZOFE_HAM_HERMIT] */
   int32_t save_rho_only; /* 1: out_state keeps rho only (mode 0) */
 } qsx_zofe_args;
 

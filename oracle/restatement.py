@@ -1014,8 +1014,11 @@ class ZOFESpec:
     ``Omega``, ``gamma``, ``huang`` are (npm, n_sites).
     """
 
-    def __init__(self, ham, Omega, gamma, huang, hilbert_subspace='ge', unit_convert=1.0):
+    def __init__(self, ham, Omega, gamma, huang, hilbert_subspace='ge', unit_convert=1.0,
+                 rho_hermit=False, ham_hermit=False):
         self.ham = ham
+        self.rho_hermit = rho_hermit
+        self.ham_hermit = ham_hermit
         self.Omega = np.asarray(Omega, complex)
         self.gamma = np.asarray(gamma, complex)
         self.huang = np.asarray(huang, complex)
@@ -1027,7 +1030,8 @@ class ZOFESpec:
 
     def sample(self, n, random_orientations=False):
         return ZOFESpec(self.ham.sample(n, random_orientations), self.Omega, self.gamma,
-                        self.huang, self.hilbert_subspace, self.unit_convert)
+                        self.huang, self.hilbert_subspace, self.unit_convert,
+                        self.rho_hermit, self.ham_hermit)
 
     @property
     def time_step(self):
@@ -1042,8 +1046,8 @@ class ZOFESpec:
         return np.concatenate([rho.reshape(-1, order='F'), oop.reshape(-1, order='F')])
 
     def rhs(self, y):
-        """zofe.py:121-202 (rho_hermit = ham_hermit = False), times
-        unit_convert; L_n = -(number operators) (zofe.py:219-222)."""
+        """zofe.py:121-202, times unit_convert; L_n = -(number operators)
+        (zofe.py:219-222).  The rho^H forms follow zofe.py:179-192."""
         rho, oop = self.split(y)
         H = self.ham.H(self.hilbert_subspace)
         L = -np.array([np.diag(o) for o in occupations(self.ham.n_sites,
@@ -1055,8 +1059,17 @@ class ZOFESpec:
         a = np.einsum('sij,sjk->ik', Lh, S)
         b = -1j * H - a
         c = np.einsum('sij,jk,smk->im', L, rho, np.conj(S))
-        big = np.einsum('sij,jk,skm->im', S, rho, Lh)
-        rhodot = b @ rho + c + rho @ (1j * H - a.conj().T) + big
+        if not self.rho_hermit:
+            big = np.einsum('sij,jk,skm->im', S, rho, Lh)
+            if self.ham_hermit:
+                f = rho @ b.conj().T + big
+            else:
+                f = rho @ (1j * H - a.conj().T) + big
+        elif self.ham_hermit:
+            f = (b @ rho + c).conj().T
+        else:
+            f = rho @ (1j * H - a.conj().T) + c.conj().T
+        rhodot = b @ rho + c + f
         oopdot = (Gamma[:, :, None, None] * L[None]
                   - w[:, :, None, None] * oop
                   + np.einsum('kj,psjl->pskl', b, oop)

@@ -17,6 +17,8 @@ QSX_FP64 = 0
 QSX_FP32 = 1
 # status-word bits set by the kernels (the QSX_ERR_* codes of include/qsx.h)
 QSX_ERR_INVALID_ARG = 1
+QSX_ZOFE_RHO_HERMIT = 1
+QSX_ZOFE_HAM_HERMIT = 2
 QSX_ERR_CUDA = 2
 QSX_ERR_NONFINITE = 4
 
@@ -81,7 +83,7 @@ class ZofeArgs(ctypes.Structure):
         ('w', _c_vp), ('V', _c_vp), ('V_stride', ctypes.c_int64), ('coef', _c_vp),
         ('proj', _c_vp), ('unit_convert', ctypes.c_double), ('h', ctypes.c_double),
         ('y0', _c_vp), ('y0_stride', ctypes.c_int64), ('out_state', _c_vp),
-        ('out_proj', _c_vp), ('status', _c_vp), ('reserved', ctypes.c_int32),
+        ('out_proj', _c_vp), ('status', _c_vp), ('hermit', ctypes.c_int32),
         ('save_rho_only', ctypes.c_int32),
     ]
 
@@ -854,7 +856,8 @@ def heom_rk4(tables, Hx, Hy, y0, nsteps, h, unit_convert, batch=None, save_every
              check_finite=True, variant=0):
     """RK4 loop over the HEOM generator for all samples (qsx_heom_rk4).
     variant 0: the library's choice (one persistent cluster launch per call
-    when it fits); 1: one launch per RK4 stage."""
+    when it fits in one wave, else per-stage launches); 1: one launch per RK4
+    stage; 2: the cluster launch whenever its shared memory fits."""
     require_gpu()
     y0 = _need(y0.to(torch.complex128).contiguous(), torch.complex128, 'y0')
     if batch is None:
@@ -1072,7 +1075,7 @@ def rk4_field(L, C, coef, y0, nsteps, h, save_every=1, precision=QSX_FP64,
 
 def zofe_rk4(H, Ld, Gamma, w, y0, nsteps, h, unit_convert, save_every=1,
              precision=QSX_FP64, V=None, coef=None, proj=None, state=True, mode=0,
-             cluster=0, check_finite=True):
+             cluster=0, check_finite=True, hermit=0):
     """ZOFE time loop (qsx_zofe_rk4).
 
     H (n, n) or (B, n, n) float64; Ld (n_sites, n) float64; Gamma, w
@@ -1081,7 +1084,9 @@ def zofe_rk4(H, Ld, Gamma, w, y0, nsteps, h, unit_convert, save_every=1,
     complex128 for pulses; proj (P, n*n) complex128 rows over rho.  Returns a
     dict with 'state' (B, nsave, M) and/or 'proj' (B, nsave, P); with
     state='rho' the states hold rho only, (B, nsave, n*n) column-major; mode
-    1 returns the right-hand side at y0 as 'rhs' (B, M).
+    1 returns the right-hand side at y0 as 'rhs' (B, M).  ``hermit`` selects
+    the rho_hermit forms: 0, QSX_ZOFE_RHO_HERMIT or QSX_ZOFE_RHO_HERMIT |
+    QSX_ZOFE_HAM_HERMIT.
     """
     require_gpu()
     dev = y0.device
@@ -1110,6 +1115,7 @@ def zofe_rk4(H, Ld, Gamma, w, y0, nsteps, h, unit_convert, save_every=1,
     a = ZofeArgs()
     a.precision, a.n, a.n_sites, a.npm = precision, n, N, npm
     a.nsteps, a.save_every, a.mode, a.cluster = int(nsteps), int(save_every), int(mode), int(cluster)
+    a.hermit = int(hermit)
     a.batch = B
     a.H, a.H_stride = H.data_ptr(), (n * n if H.dim() == 3 else 0)
     a.Ld, a.Gamma, a.w = Ld.data_ptr(), Gamma.data_ptr(), w.data_ptr()

@@ -16,10 +16,11 @@
 //
 // FP32: 5th-generation tensor cores, 3xTF32 (hi/lo TF32 split of both
 // operands, A B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi, FP32 accumulation in
-// tensor memory).  Each CTA owns a 128 x 128 tile of C; the K loop moves in
-// chunks of 32, double-buffered: while the tensor core multiplies chunk k,
-// all threads load chunk k + 1 from global memory, split it and store it in
-// the K-major core-matrix layout of the other buffer.  One thread issues the
+// tensor memory).  Each CTA owns a 128 x 128 tile of C, two CTAs per SM; the
+// K loop moves in chunks of 16 through three buffers: while the tensor core
+// multiplies the previous chunks, all threads load the next one from global
+// memory (16-byte loads of A rows, 8-byte loads of complex B), split it and
+// store it in the K-major core-matrix layout of a free buffer.  One thread issues the
 // MMAs and commits them to the buffer's mbarrier; every wait is bounded and a
 // timeout sets QSX_ERR_CUDA in the status word.
 // FP64: CUDA cores, 64 x 64 tiles of C, 4 x 4 per thread, the same views.
@@ -47,6 +48,7 @@ struct GemmP {
   void* C;
   int64_t ldc, sC;
   double alpha, beta;
+  int avec;             // A rows 16-byte aligned (vector loads allowed)
   int* status;
 };
 
@@ -68,18 +70,45 @@ __device__ __forceinline__ T a_elem(const GemmP& p, const T* A, int m, int k) {
 }
 
 // ------------------------------------------------------------ FP32, tcgen05
-constexpr int GT_BM = 128, GT_BN = 128, GT_BK = 32, GT_THREADS = 256;
-constexpr uint32_t GT_PLANE = GT_BM * GT_BK * 4;             // 16 KB
-constexpr uint32_t GT_SBO = GT_BK * 32;                       // 1024 B
+constexpr int GT_BM = 128, GT_BN = 128, GT_BK = 16, GT_THREADS = 256, GT_STAGES = 3;
+constexpr uint32_t GT_PLANE = GT_BM * GT_BK * 4;             // 8 KB
+constexpr uint32_t GT_SBO = GT_BK * 32;                       // 512 B
 constexpr uint32_t GT_BUF = 4 * GT_PLANE;                     // A hi/lo, B hi/lo
-constexpr size_t GT_SMEM = 2 * (size_t)GT_BUF + 64;
+constexpr size_t GT_SMEM = GT_STAGES * (size_t)GT_BUF + 64;
 constexpr uint32_t GT_TMEM_COLS = 128;
 
-__global__ void __launch_bounds__(GT_THREADS, 1) gemm_tc_kernel(GemmP p) {
+// Four consecutive k of row m of A (real view): one 16-byte load when the
+// rows are 16-byte aligned and the quad lies inside the matrix.
+__device__ __forceinline__ float4 a_quad(const GemmP& p, const float* A, int m, int k) {
+  if (m < p.M && k + 3 < p.K && p.avec)
+    return __ldg(reinterpret_cast<const float4*>(A + (int64_t)m * p.lda + k));
+  return make_float4(a_elem(p, A, m, k), a_elem(p, A, m, k + 1), a_elem(p, A, m, k + 2),
+                     a_elem(p, A, m, k + 3));
+}
+
+// Four consecutive k (k a multiple of 4) of column n of the expanded right
+// operand B': for a complex source two 8-byte loads give the whole quad.
+__device__ __forceinline__ float4 b_quad(const GemmP& p, const float* B, int k, int n) {
+  if (p.bmode == GB_REAL || n >= p.N || k + 3 >= p.K)
+    return make_float4(b_elem(p, B, k, n), b_elem(p, B, k + 1, n), b_elem(p, B, k + 2, n),
+                       b_elem(p, B, k + 3, n));
+  const int kk = k >> 1, nn = n >> 1, u = n & 1;
+  if (p.bmode == GB_REAL_AS_CPLX) {
+    const float z0 = __ldg(B + (int64_t)kk * p.ldb + nn);
+    const float z1 = __ldg(B + (int64_t)(kk + 1) * p.ldb + nn);
+    return u == 0 ? make_float4(z0, 0.f, z1, 0.f) : make_float4(0.f, z0, 0.f, z1);
+  }
+  const float2 z0 = __ldg(reinterpret_cast<const float2*>(B) + (int64_t)kk * p.ldb + nn);
+  const float2 z1 = __ldg(reinterpret_cast<const float2*>(B) + (int64_t)(kk + 1) * p.ldb + nn);
+  // rows 2kk, 2kk + 1 of the 2 x 2 blocks [[br, bi], [-bi, br]]
+  return u == 0 ? make_float4(z0.x, -z0.y, z1.x, -z1.y) : make_float4(z0.y, z0.x, z1.y, z1.x);
+}
+
+__global__ void __launch_bounds__(GT_THREADS, 2) gemm_tc_kernel(GemmP p) {
   using namespace tc;
   extern __shared__ __align__(128) unsigned char smraw[];
-  uint64_t* mbar_p = reinterpret_cast<uint64_t*>(smraw + 2 * GT_BUF);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar_p + 2);
+  uint64_t* mbar_p = reinterpret_cast<uint64_t*>(smraw + GT_STAGES * GT_BUF);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar_p + GT_STAGES);
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * GT_BM, n0 = blockIdx.x * GT_BN;
@@ -88,7 +117,7 @@ __global__ void __launch_bounds__(GT_THREADS, 1) gemm_tc_kernel(GemmP p) {
   const float* B = (const float*)p.B + bz * p.sB * (p.bmode == GB_CPLX ? 2 : 1);
   if (tid == 0) {
     s_abort = 0;
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < GT_STAGES; ++i)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
                        (uint32_t)__cvta_generic_to_shared(mbar_p + i))
                    : "memory");
@@ -108,16 +137,16 @@ __global__ void __launch_bounds__(GT_THREADS, 1) gemm_tc_kernel(GemmP p) {
   const int nk = (p.K + GT_BK - 1) / GT_BK;
   int issued = 0;   // chunks whose MMAs were issued (uniform across threads)
   for (int kc = 0; kc < nk; ++kc) {
-    const int buf = kc & 1;
+    const int buf = kc % GT_STAGES;
     unsigned char* base = smraw + buf * GT_BUF;
     unsigned char* a_hi = base;
     unsigned char* a_lo = base + GT_PLANE;
     unsigned char* b_hi = base + 2 * GT_PLANE;
     unsigned char* b_lo = base + 3 * GT_PLANE;
-    if (kc >= 2) {   // the MMAs of chunk kc - 2 read this buffer
+    if (kc >= GT_STAGES) {   // the MMAs of chunk kc - GT_STAGES read this buffer
       if (tid == 0) {
         const uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar_p + buf);
-        if (!wait_parity(mb, (uint32_t)(((kc - 2) >> 1) & 1))) {
+        if (!wait_parity(mb, (uint32_t)(((kc - GT_STAGES) / GT_STAGES) & 1))) {
           if (p.status) atomicOr(p.status, QSX_ERR_CUDA);
           s_abort = 1;
         }
@@ -126,23 +155,21 @@ __global__ void __launch_bounds__(GT_THREADS, 1) gemm_tc_kernel(GemmP p) {
       if (s_abort) break;
     }
     const int k0 = kc * GT_BK;
-    // A chunk: row r = idx % 128 (rows fastest: conflict-free 16-byte stores)
+    // A chunk: a warp covers 8 rows x 16 k (64 contiguous bytes per row);
+    // its 16-byte stores fill 32 distinct bank groups
 #pragma unroll
-    for (int i = 0; i < (GT_BM * GT_BK / 4) / GT_THREADS; ++i) {
-      const int idx = tid + i * GT_THREADS;
-      const int r = idx & (GT_BM - 1), j = idx >> 7;
-      const int m = m0 + r, k = k0 + 4 * j;
-      st_split4(a_hi, a_lo, op_offset(r, 4 * j, GT_SBO), a_elem(p, A, m, k),
-                a_elem(p, A, m, k + 1), a_elem(p, A, m, k + 2), a_elem(p, A, m, k + 3));
+    for (int i = 0; i < (GT_BM / 8) / (GT_THREADS / 32); ++i) {
+      const int r = 8 * (warp + (GT_THREADS / 32) * i) + (lane & 7), j = lane >> 3;
+      const float4 v = a_quad(p, A, m0 + r, k0 + 4 * j);
+      st_split4(a_hi, a_lo, op_offset(r, 4 * j, GT_SBO), v.x, v.y, v.z, v.w);
     }
-    // B'^T chunk: row n (fastest: coalesced loads along the columns of B)
+    // B'^T chunk: rows n fastest (coalesced along the columns of B)
 #pragma unroll
     for (int i = 0; i < (GT_BN * GT_BK / 4) / GT_THREADS; ++i) {
       const int idx = tid + i * GT_THREADS;
       const int n = idx & (GT_BN - 1), j = idx >> 7;
-      const int nn = n0 + n, k = k0 + 4 * j;
-      st_split4(b_hi, b_lo, op_offset(n, 4 * j, GT_SBO), b_elem(p, B, k, nn),
-                b_elem(p, B, k + 1, nn), b_elem(p, B, k + 2, nn), b_elem(p, B, k + 3, nn));
+      const float4 v = b_quad(p, B, k0 + 4 * j, n0 + n);
+      st_split4(b_hi, b_lo, op_offset(n, 4 * j, GT_SBO), v.x, v.y, v.z, v.w);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -159,8 +186,8 @@ __global__ void __launch_bounds__(GT_THREADS, 1) gemm_tc_kernel(GemmP p) {
   // the last commit covers every MMA issued before it
   if (tid == 0 && !s_abort && issued > 0) {
     const int last = issued - 1;
-    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar_p + (last & 1));
-    if (!wait_parity(mb, (uint32_t)((last >> 1) & 1))) {
+    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(mbar_p + (last % GT_STAGES));
+    if (!wait_parity(mb, (uint32_t)((last / GT_STAGES) & 1))) {
       if (p.status) atomicOr(p.status, QSX_ERR_CUDA);
       s_abort = 1;
     }
@@ -191,8 +218,8 @@ __global__ void __launch_bounds__(GT_THREADS, 1) gemm_tc_kernel(GemmP p) {
   } else if (tid == 0 && issued > 0) {
     // let an unfinished chain drain (bounded) before the memory is freed
     const int last = issued - 1;
-    wait_parity((uint32_t)__cvta_generic_to_shared(mbar_p + (last & 1)),
-                (uint32_t)((last >> 1) & 1));
+    wait_parity((uint32_t)__cvta_generic_to_shared(mbar_p + (last % GT_STAGES)),
+                (uint32_t)((last / GT_STAGES) & 1));
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -299,6 +326,8 @@ extern "C" int qsx_gemm_batched(int precision, int mode, int64_t batch, int M, i
   p.alpha = alpha;
   p.beta = beta;
   p.status = status;
+  p.avec = precision == QSX_FP32 && (reinterpret_cast<uintptr_t>(A) & 15) == 0 &&
+           p.lda % 4 == 0 && p.sA % 4 == 0;
   (void)cb;
   cudaStream_t s = (cudaStream_t)stream;
   if (precision == QSX_FP32) {

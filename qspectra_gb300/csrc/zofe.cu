@@ -13,7 +13,9 @@
 // site s (already carrying the ZOFE sign).  A pulse p adds a_p(t) [V_p, .] to
 // both rho and every O (not scaled by unit_convert), which folds into the
 // small operators: the left operator becomes b + sum_p a_p V_p / unit_convert
-// and the right one (i H - a^H) - sum_p a_p V_p / unit_convert.
+// and the right one (i H - a^H) - sum_p a_p V_p / unit_convert.  The
+// rho_hermit forms (zofe.py:179-192) take rho^H in the last rho term and, with
+// ham_hermit, in the third one too (the field part still multiplies rho).
 //
 // GB300 layout: one thread-block cluster per sample.  The pseudomodes are
 // split over the cluster's CTAs; each CTA keeps its share of O (plus a
@@ -34,6 +36,7 @@ namespace qsx {
 struct ZofeP {
   int n, N, npm, pmc, csize;  // states, sites, pseudomodes, pseudomodes per CTA, cluster
   int nsteps, save_every, nsave, np, nproj, mode, rho_only;
+  int herm_big, herm_right;   // rho^H in sum_s S_s rho L_s^H / in rho (i H - a^H)
   int64_t batch, H_stride, V_stride, y0_stride;
   int64_t M;                  // n^2 + npm N n^2
   const double* H;            // real [n][n], rotating frame
@@ -115,7 +118,8 @@ __global__ void __launch_bounds__(EPT >= 4 ? 512 : 1024, 1)
   Cx* sPart = sS + Q;                         // [2][Q] partial sums (read by peers)
   Cx* sB = sPart + 2 * (size_t)Q;             // [n2] left operator, row-major
   Cx* sR = sB + n2;                           // [n2] right operator (rho), row-major
-  Cx* sG = sR + n2;                           // [pmc][N]
+  Cx* sF = sR + n2;                           // [n2] field part of the right operator
+  Cx* sG = sF + n2;                           // [pmc][N]
   Cx* sW = sG + (size_t)p.pmc * N;            // [pmc][N]
   Cx* sV = sW + (size_t)p.pmc * N;            // [np][n2]
   Cx* sa = sV + (size_t)np * n2;              // [np]
@@ -217,6 +221,7 @@ __global__ void __launch_bounds__(EPT >= 4 ? 512 : 1024, 1)
         const T Hik = sH[e];
         sB[e] = cmk(-aik.x + fv.x, -Hik - aik.y + fv.y);
         sR[e] = cmk(-aki.x - fv.x, Hik + aki.y - fv.y);
+        sF[e] = fv;
       }
       __syncthreads();
       // derivatives of this thread's elements
@@ -227,9 +232,16 @@ __global__ void __launch_bounds__(EPT >= 4 ? 512 : 1024, 1)
         Cx d = cmk((T)0, (T)0);
         if (e < n2) {
           const int i = e % n, m = e / n;  // rho[i][m], column-major
-          for (int j = 0; j < n; ++j) {
-            cfma(d, sB[i * n + j], sx[j + n * m]);
-            cfma(d, sx[i + n * j], sR[j * n + m]);
+          for (int j = 0; j < n; ++j) cfma(d, sB[i * n + j], sx[j + n * m]);
+          if (!p.herm_right) {
+            for (int j = 0; j < n; ++j) cfma(d, sx[i + n * j], sR[j * n + m]);
+          } else {
+            // rho^H (R + F) - rho F: the field still acts on rho itself
+            for (int j = 0; j < n; ++j) {
+              const Cx rh = sx[j + n * i], r = sx[i + n * j], f = sF[j * n + m];
+              cfma(d, cmk(rh.x, -rh.y), sR[j * n + m]);
+              cfma(d, cmk(rh.x - r.x, -rh.y - r.y), f);
+            }
           }
           // the couplings are site number operators: most L_s[i] vanish
           for (int s = 0; s < N; ++s) {
@@ -244,7 +256,14 @@ __global__ void __launch_bounds__(EPT >= 4 ? 512 : 1024, 1)
             }
             if (lm != (T)0) {
               Cx bs = cmk((T)0, (T)0);
-              for (int k = 0; k < n; ++k) cfma(bs, sS[s + N * (i + n * k)], sx[k + n * m]);
+              if (!p.herm_big) {
+                for (int k = 0; k < n; ++k) cfma(bs, sS[s + N * (i + n * k)], sx[k + n * m]);
+              } else {
+                for (int k = 0; k < n; ++k) {
+                  const Cx r = sx[m + n * k];
+                  cfma(bs, sS[s + N * (i + n * k)], cmk(r.x, -r.y));
+                }
+              }
               d = cmk(d.x + lm * bs.x, d.y + lm * bs.y);
             }
           }
@@ -342,7 +361,9 @@ extern "C" int qsx_zofe_rk4(const qsx_zofe_args* a, void* stream) {
                     a->npulses >= 0 && a->nproj >= 0 && a->batch >= 0 && a->nsteps >= 0 &&
                     a->save_every >= 1 && a->nsteps % a->save_every == 0 &&
                     (a->mode == 0 || a->mode == 1) && a->cluster >= 0 && a->cluster <= 8 &&
-                    a->reserved == 0 && (a->save_rho_only == 0 || a->save_rho_only == 1),
+                    (a->hermit == 0 || a->hermit == QSX_ZOFE_RHO_HERMIT ||
+                     a->hermit == (QSX_ZOFE_RHO_HERMIT | QSX_ZOFE_HAM_HERMIT)) &&
+                    (a->save_rho_only == 0 || a->save_rho_only == 1),
                 "qsx_zofe_rk4: bad sizes (n=%d, sites=%d, pseudomodes=%d, steps=%d)", a->n,
                 a->n_sites, a->npm, a->nsteps);
   if (a->batch == 0) return QSX_OK;
@@ -382,7 +403,7 @@ extern "C" int qsx_zofe_rk4(const qsx_zofe_args* a, void* stream) {
   const size_t cs = a->precision == QSX_FP32 ? sizeof(float2) : sizeof(double2);
   const size_t rs = a->precision == QSX_FP32 ? sizeof(float) : sizeof(double);
   const int np = a->npulses;
-  const size_t smem = ((size_t)n2 + (size_t)pmc * Q + 3 * (size_t)Q + 2 * (size_t)n2 +
+  const size_t smem = ((size_t)n2 + (size_t)pmc * Q + 3 * (size_t)Q + 3 * (size_t)n2 +
                        2 * (size_t)pmc * N + (size_t)np * n2 + np + (np & 1)) * cs +
                       ((size_t)n2 + (size_t)N * n) * rs;
   QSX_CHECK_ARG(smem <= 227 * 1024, "qsx_zofe_rk4: %zu bytes of shared memory needed", smem);
@@ -399,6 +420,8 @@ extern "C" int qsx_zofe_rk4(const qsx_zofe_args* a, void* stream) {
   p.nproj = a->nproj;
   p.mode = a->mode;
   p.rho_only = a->save_rho_only;
+  p.herm_big = (a->hermit & QSX_ZOFE_RHO_HERMIT) != 0;
+  p.herm_right = a->hermit == (QSX_ZOFE_RHO_HERMIT | QSX_ZOFE_HAM_HERMIT);
   p.batch = a->batch;
   p.H_stride = a->H_stride;
   p.V_stride = np ? a->V_stride : 0;

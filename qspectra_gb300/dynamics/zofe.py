@@ -100,6 +100,7 @@ class ZOFEEquationOfMotion:
         x = x.to(device='cuda', dtype=torch.complex128)
         Ld, G, w = self.model.zofe_tables()
         out = _native.zofe_rk4(self.H, Ld, G, w, x, 0, 1.0, self.model.unit_convert,
+                               hermit=self.model.zofe_hermit,
                                mode=1)['rhs']
         out = out[0] if x.dim() == 1 else out
         return out if isinstance(state, torch.Tensor) else out.cpu().numpy()
@@ -108,10 +109,11 @@ class ZOFEEquationOfMotion:
 class ZOFEModel(DynamicalModel):
     """ZOFE master equation with one pseudomode bath per site (zofe.py:44-229).
 
-    ``ham_hermit`` only selects an algebraically equal form of the same
-    right-hand side for Hermitian Hamiltonians (always the case here), so it
-    does not change results; ``rho_hermit`` replaces one term by the
-    conjugate of another, which the GPU path does not implement.
+    ``rho_hermit`` takes rho^H in place of rho in the last term of rho's
+    right-hand side (the conjugate transpose of the second term), and with
+    ``ham_hermit`` in the third as well (zofe.py:179-192); both are exact for
+    a Hermitian rho.  ``ham_hermit`` alone selects an algebraically equal form
+    for Hermitian Hamiltonians (always the case here).
     """
     system_operator = ZOFESpaceOperator
 
@@ -121,8 +123,6 @@ class ZOFEModel(DynamicalModel):
         if not isinstance(self.hamiltonian.bath, PseudomodeBath):
             raise NotImplementedError('ZOFE only implemented for baths of type '
                                       'PseudomodeBath')
-        if rho_hermit:
-            raise NotImplementedError('rho_hermit is not on the GPU path')
         numb_pm = self.hamiltonian.bath.numb_pm
         n_sit = self.hamiltonian.n_sites
         n_stat = self.hamiltonian.n_states(self.hilbert_subspace)
@@ -134,6 +134,14 @@ class ZOFEModel(DynamicalModel):
     @property
     def n_states(self):
         return self.oop_shape[2]
+
+    @property
+    def zofe_hermit(self):
+        """The kernel's form flags for rho_hermit / ham_hermit."""
+        if not self.rho_hermit:
+            return 0
+        return _native.QSX_ZOFE_RHO_HERMIT | (_native.QSX_ZOFE_HAM_HERMIT if self.ham_hermit
+                                              else 0)
 
     @property
     def state_size(self):

@@ -81,7 +81,7 @@ def _zofe_dynamics(model, initial_state, duration, times, ensemble_size, precisi
     n = model.n_states
     Ld, G, w = model.zofe_tables()
     out = _native.zofe_rk4(H, Ld, G, w, y0, nsteps, step, model.unit_convert, every,
-                           PRECISIONS[precision], state='rho')['state']
+                           PRECISIONS[precision], state='rho', hermit=model.zofe_hermit)['state']
     vec = out[:, first:].mean(0).cpu().numpy()          # (T, n*n), column-major rho
     return t, vec.reshape(len(vec), n, n).transpose(0, 2, 1)
 
@@ -207,7 +207,7 @@ def _zofe_fields(model, polarization, geometry, coef, nsteps, h, save_every,
                                      dtype=complex), device=dev)
     Ld, G, w = model.zofe_tables()
     return _native.zofe_rk4(H, Ld, G, w, y0, nsteps, h, model.unit_convert, save_every,
-                            prec, V=V, coef=coef)['state']
+                            prec, V=V, coef=coef, hermit=model.zofe_hermit)['state']
 
 
 def simulate_pump(dynamical_model, pump, polarization='x', time_extra=0, times=None,

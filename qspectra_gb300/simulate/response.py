@@ -96,7 +96,8 @@ def _zofe_linear(model, time_max, ensemble_size, polarization, precision, rotati
                                dtype=torch.complex128, device=dev)
     Ld, G, w = model.zofe_tables()
     out = _native.zofe_rk4(H, Ld, G, w, y0.contiguous(), nsteps, step, model.unit_convert,
-                           every, PRECISIONS[precision], proj=proj, state=False)['proj']
+                           every, PRECISIONS[precision], proj=proj, state=False,
+                           hermit=model.zofe_hermit)['proj']
     out = out[:, first:]
     if rotations is not None:
         out = (out * q[:, None, 1, :].to(out.dtype)).sum(-1, keepdim=True)

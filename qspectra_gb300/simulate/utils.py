@@ -249,7 +249,8 @@ def _integrate_zofe(f, y0, t, t0, save_func, precision, step):
                                device=Y.device)
     res = _native.zofe_rk4(f.H, Ld, G, w, Y if Y.shape[0] > 1 else Y[0], nsteps, step,
                            f.model.unit_convert, save_every=every,
-                           precision=_precision(precision), proj=proj, state=not expect)
+                           precision=_precision(precision), proj=proj, state=not expect,
+                           hermit=f.model.zofe_hermit)
     if expect:
         out = res['proj'][:, first:, 0]
     else:

@@ -21,6 +21,13 @@ def golden():
         return {k: z[k] for k in z.files}
 
 
+@pytest.fixture(scope='session')
+def golden_zofe_hermit():
+    path = os.path.join(ROOT, 'tests', 'golden', 'reference_golden_zofe_hermit.npz')
+    with np.load(path) as z:
+        return {k: z[k] for k in z.files}
+
+
 def rel_err(a, b):
     """max|a - b| / max|b| (the inf-norm relative error used by every test)."""
     a = np.asarray(a)

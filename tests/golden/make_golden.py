@@ -3,12 +3,14 @@
 Run from the repository root in a container where the reference checkout is
 available (read-only is fine), giving the checkout's path:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <reference-checkout> [base|drivers|all]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <reference-checkout> [base|drivers|zofe_hermit|all]
 
 ``base`` writes reference_golden.npz (generators, trajectories, spectra and
 small third-order cases); ``drivers`` writes reference_golden_drivers.npz
 (impulsive probe, 2D spectra, third order on the 128 x 3 x 128 grids at 6
-and 8 sites, and the 8-site 495-node HEOM trajectory).
+and 8 sites, and the 8-site 495-node HEOM trajectory); ``zofe_hermit``
+writes reference_golden_zofe_hermit.npz (ZOFE's rho_hermit / ham_hermit
+forms).
 
 Every fixture comes from the reference's own code path.  Its adaptive
 ``zvode`` integrator is swapped for a fixed-step RK4 harness that drives the
@@ -499,11 +501,71 @@ def drivers_main(ref_root):
     print('wrote', len(out), 'arrays')
 
 
+def zofe_hermit_main(ref_root):
+    """Fixtures for ZOFEModel's rho_hermit / ham_hermit forms (zofe.py:179-192)
+    on the 3-site chain of the base ZOFE fixtures: the right-hand side at
+    random (non-Hermitian) states for every flag pair, and linear response and
+    free dynamics with both flags set."""
+    qs = import_reference(ref_root)
+    import qspectra.simulate.response as qresp
+    import qspectra.simulate.eom as qeom
+    from qspectra_gb300 import workloads as wl
+    out = {}
+    Hz = wl.chain_hamiltonian(n_sites=3, seed=13)
+    extraz = wl.energy_spread_for_dt(Hz, 2.0, qs.CM_FS)
+    zpm = dict(Omega=[-200.0, 30.0, 250.0], gamma=[100.0, 50.0, 150.0],
+               huang=[-5e-3, 0.8, 1e-2])
+    on = np.ones(3, complex)
+    pmb = qs.PseudomodeBath(3, np.array([x * on for x in zpm['Omega']]),
+                            np.array([x * on for x in zpm['gamma']]),
+                            np.array([x * on for x in zpm['huang']]))
+    dipz = [[1.0, 0, 0], [0.4, 0.8, 0.0], [-0.3, 0.5, 0.6]]
+    hamz = qs.ElectronicHamiltonian(Hz, bath=pmb, dipoles=dipz,
+                                    disorder=wl.fwhm_for_sd(30.0), random_seed=9,
+                                    energy_spread_extra=extraz)
+    rng = np.random.RandomState(77)
+    Y = None
+    for rh, hh in ((False, False), (False, True), (True, False), (True, True)):
+        m = qs.ZOFEModel(hamz, hilbert_subspace='ge', unit_convert=qs.CM_FS,
+                         rho_hermit=rh, ham_hermit=hh)
+        eom = m.equation_of_motion('gg,ge,eg,ee')
+        if Y is None:
+            M = 16 + int(np.prod(m.oop_shape))
+            Y = rng.randn(3, M) + 1j * rng.randn(3, M)
+            out['zofeh_Y'] = Y
+        out['zofeh_rhs_{}{}'.format(int(rh), int(hh))] = np.array([eom(0.0, y) for y in Y])
+    m = qs.ZOFEModel(hamz, hilbert_subspace='ge', unit_convert=qs.CM_FS, rho_hermit=True,
+                     ham_hermit=True)
+    assert m.time_step == 2.0, m.time_step
+    qeom.integrate = rk4_harness(2.0)
+    qresp.integrate = rk4_harness(2.0)
+    _, x = qs.linear_response(m, 'gg->eg->gg', 256.0)
+    out['zofeh_lin'] = x
+    _, rho = qs.simulate_dynamics(m, [0, 1, 0, 0], 200.0)
+    out['zofeh_dyn_rho'] = rho
+    m = qs.ZOFEModel(hamz, hilbert_subspace='ge', unit_convert=qs.CM_FS, rho_hermit=True)
+    _, x = qs.linear_response(m, 'gg->eg->gg', 256.0)
+    out['zofeh_lin_rho_only'] = x
+    # a non-Hermitian start inside the one-exciton block, where the forms differ
+    rho0 = np.zeros((4, 4), complex)
+    rho0[1, 1], rho0[2, 2], rho0[1, 2], rho0[2, 3] = 0.6, 0.4, 0.3 + 0.1j, -0.2j
+    out['zofeh_rho0'] = rho0
+    for rh, hh in ((False, False), (True, False), (True, True)):
+        m = qs.ZOFEModel(hamz, hilbert_subspace='ge', unit_convert=qs.CM_FS,
+                         rho_hermit=rh, ham_hermit=hh)
+        _, rho = qs.simulate_dynamics(m, rho0, 200.0)
+        out['zofeh_dyn_nh_{}{}'.format(int(rh), int(hh))] = rho
+    np.savez_compressed(os.path.join(HERE, 'reference_golden_zofe_hermit.npz'), **out)
+    print('wrote', len(out), 'arrays')
+
+
 if __name__ == '__main__':
     if len(sys.argv) < 2:
-        sys.exit('usage: make_golden.py <reference-checkout> [base|drivers|all]')
+        sys.exit('usage: make_golden.py <reference-checkout> [base|drivers|zofe_hermit|all]')
     what = sys.argv[2] if len(sys.argv) > 2 else 'all'
     if what in ('base', 'all'):
         main(sys.argv[1])
     if what in ('drivers', 'all'):
         drivers_main(sys.argv[1])
+    if what in ('zofe_hermit', 'all'):
+        zofe_hermit_main(sys.argv[1])

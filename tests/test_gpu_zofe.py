@@ -133,3 +133,70 @@ def test_oversized_state_is_rejected():
     with pytest.raises(_native.QsxError):
         _native.zofe_rk4(H, Ld, G, w, torch.zeros(M, dtype=torch.complex128).cuda(), 2, 1.0,
                          orc.CM_FS)
+
+
+def zofe3_hermit(golden, rh, hh):
+    m = zofe3(golden)
+    m.rho_hermit, m.ham_hermit = bool(rh), bool(hh)
+    return m
+
+
+@pytest.mark.parametrize('rh,hh', [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_hermit_forms_rhs_match_reference(golden, golden_zofe_hermit, rh, hh):
+    """rho_hermit / ham_hermit (zofe.py:179-192) at random non-Hermitian
+    states, through the kernel's right-hand-side mode."""
+    g = golden_zofe_hermit
+    eom = zofe3_hermit(golden, rh, hh).equation_of_motion('gg,ge,eg,ee')
+    got = eom(0.0, torch.as_tensor(g['zofeh_Y']).cuda()).cpu().numpy()
+    assert rel_err(got, g['zofeh_rhs_{}{}'.format(rh, hh)]) < 1e-13
+
+
+@pytest.mark.parametrize('precision,tol', TOLS)
+def test_hermit_forms_drivers_match_reference(golden, golden_zofe_hermit, precision, tol):
+    g = golden_zofe_hermit
+    _, x = qg.linear_response(zofe3_hermit(golden, 1, 0), 'gg->eg->gg', 256.0,
+                              precision=precision)
+    assert rel_err(x, g['zofeh_lin_rho_only']) < tol
+    m = zofe3_hermit(golden, 1, 1)
+    _, x = qg.linear_response(m, 'gg->eg->gg', 256.0, precision=precision)
+    assert rel_err(x, g['zofeh_lin']) < tol
+    _, rho = qg.simulate_dynamics(m, [0, 1, 0, 0], 200.0, precision=precision)
+    assert rel_err(rho, g['zofeh_dyn_rho']) < tol
+    for rh, hh in ((0, 0), (1, 0), (1, 1)):
+        _, rho = qg.simulate_dynamics(zofe3_hermit(golden, rh, hh), g['zofeh_rho0'], 200.0,
+                                      precision=precision)
+        assert rel_err(rho, g['zofeh_dyn_nh_{}{}'.format(rh, hh)]) < tol
+
+
+@pytest.mark.parametrize('hermit', [1, 3])
+def test_hermit_forms_under_fields_match_oracle(hermit):
+    """Field terms a_p(t) [V_p, .] with the rho^H forms, from a non-Hermitian
+    state: the field still acts on rho itself (eom.py:77-105 adds it beside
+    the model's right-hand side)."""
+    om = oracle_zofe(3, 4, 'ge', seed=5)
+    om.rho_hermit, om.ham_hermit = True, hermit == 3
+    rng = np.random.RandomState(3)
+    n, M = om.n, om.n * om.n + int(np.prod(om.oop_shape))
+    y0 = 0.1 * (rng.randn(M) + 1j * rng.randn(M))
+    V = rng.randn(2, n, n) + 1j * rng.randn(2, n, n)
+    nsteps, h = 12, 1.0
+    coef = 1e-3 * (rng.randn(nsteps, 3, 2) + 1j * rng.randn(nsteps, 3, 2))
+
+    def f(step, ci, y):
+        d = om.rhs(y)
+        for p in range(2):
+            d = d + coef[step, ci, p] * om.commutator(V[p], y)
+        return d
+    y, ref = y0.copy(), [y0.copy()]
+    for k in range(nsteps):
+        k1 = f(k, 0, y)
+        k2 = f(k, 1, y + h / 2 * k1)
+        k3 = f(k, 1, y + h / 2 * k2)
+        k4 = f(k, 2, y + h * k3)
+        y = y + h / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        ref.append(y.copy())
+    Ld, G, w, H = device_tables(om)
+    st = _native.zofe_rk4(H, Ld, G, w, torch.as_tensor(y0).cuda(), nsteps, h, orc.CM_FS,
+                          V=torch.as_tensor(V).cuda(), coef=torch.as_tensor(coef).cuda(),
+                          hermit=hermit)['state'][0].cpu().numpy()
+    assert rel_err(st, np.array(ref)) < 1e-11

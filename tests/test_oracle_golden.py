@@ -281,3 +281,35 @@ def test_zofe_oracle_matches_reference(golden):
     t, st = orc.zofe_with_fields(m, [pump, pump], '-+', 'xx', 60.0)
     assert np.allclose(t, golden['zofe3_pump_t'])
     assert rel_err(st, golden['zofe3_pump']) < 1e-12
+
+
+@pytest.mark.parametrize('rh,hh', [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_zofe_hermit_forms_oracle_matches_reference(golden, golden_zofe_hermit, rh, hh):
+    """ZOFEModel's rho_hermit / ham_hermit forms (zofe.py:179-192): the
+    right-hand side at random non-Hermitian states."""
+    m = zofe3_model(golden)
+    m.rho_hermit, m.ham_hermit = bool(rh), bool(hh)
+    got = np.array([m.rhs(y) for y in golden_zofe_hermit['zofeh_Y']])
+    assert rel_err(got, golden_zofe_hermit['zofeh_rhs_{}{}'.format(rh, hh)]) < 1e-13
+
+
+def test_zofe_hermit_drivers_oracle_matches_reference(golden, golden_zofe_hermit):
+    g = golden_zofe_hermit
+    m = zofe3_model(golden)
+    m.rho_hermit = True
+    _, x = orc.zofe_linear_response(m, 256.0)
+    assert rel_err(x, g['zofeh_lin_rho_only']) < 1e-12
+    m.ham_hermit = True
+    _, x = orc.zofe_linear_response(m, 256.0)
+    assert rel_err(x, g['zofeh_lin']) < 1e-12
+    _, rho = orc.zofe_dynamics(m, [0, 1, 0, 0], 200.0)
+    assert rel_err(rho, g['zofeh_dyn_rho']) < 1e-12
+    # linear response and a Hermitian start cannot tell the forms apart (the
+    # auxiliary operators stay inside the one-exciton block); a non-Hermitian
+    # start inside that block does
+    for rh, hh in ((0, 0), (1, 0), (1, 1)):
+        m.rho_hermit, m.ham_hermit = bool(rh), bool(hh)
+        _, rho = orc.zofe_dynamics(m, g['zofeh_rho0'], 200.0)
+        assert rel_err(rho, g['zofeh_dyn_nh_{}{}'.format(rh, hh)]) < 1e-12
+    assert rel_err(g['zofeh_dyn_nh_10'], g['zofeh_dyn_nh_00']) > 1e-3
+    assert rel_err(g['zofeh_dyn_nh_11'], g['zofeh_dyn_nh_10']) > 1e-3
