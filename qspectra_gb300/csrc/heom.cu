@@ -43,19 +43,6 @@ struct HeomP {
   const double2* gamma;  // [nnodes][nterms] or null (aki_temp_corr terms)
   const double* Wraw;    // [E] or null
   double uc, h;
-  // FP32 copies of the tables, made once per qsx_heom_rk4 call so the FP32
-  // stage kernel stages them without FP64 conversions (null for FP64)
-  const float* Hx32;
-  const float* Hy32;
-  const float* occx32;
-  const float* occy32;
-  const float* W32;
-  const float* shift32;
-  const float2* alpha32;
-  const float2* beta32;
-  const float2* gamma32;
-  const float* Wraw32;
-  float uc32, h32;
 };
 
 // Per-CTA tables in the working precision T (staged once so the element
@@ -115,15 +102,6 @@ __device__ __forceinline__ void heom_stage_smem(const HeomP& p, const typename c
   using C = typename cplx<T>::type;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int nn = (npc < p.nnodes - n0 ? npc : p.nnodes - n0);
-  if constexpr (sizeof(T) == 4) {
-    for (int i = tid; i < p.nx * p.nx; i += nt) s.Hx[i] = p.Hx32[b * p.Hx_stride + i];
-    for (int i = tid; i < p.ny * p.ny; i += nt) s.Hy[i] = p.Hy32[b * p.Hy_stride + i];
-    for (int i = tid; i < p.n_sites * p.nx; i += nt) s.ox[i] = p.occx32[i];
-    for (int i = tid; i < p.n_sites * p.ny; i += nt) s.oy[i] = p.occy32[i];
-    for (int i = tid; i < p.E; i += nt) s.W[i] = p.W32 ? p.W32[i] : 0.f;
-    for (int i = tid; i < p.E; i += nt) s.Wr[i] = p.Wraw32 ? p.Wraw32[i] : 0.f;
-    for (int i = tid; i < npc; i += nt) s.shift[i] = i < nn ? p.shift32[n0 + i] : 0.f;
-  } else {
     for (int i = tid; i < p.nx * p.nx; i += nt) s.Hx[i] = p.Hx[b * p.Hx_stride + i];
     for (int i = tid; i < p.ny * p.ny; i += nt) s.Hy[i] = p.Hy[b * p.Hy_stride + i];
     for (int i = tid; i < p.n_sites * p.nx; i += nt) s.ox[i] = p.occx[i];
@@ -131,21 +109,14 @@ __device__ __forceinline__ void heom_stage_smem(const HeomP& p, const typename c
     for (int i = tid; i < p.E; i += nt) s.W[i] = p.W ? p.W[i] : 0.0;
     for (int i = tid; i < p.E; i += nt) s.Wr[i] = p.Wraw ? p.Wraw[i] : 0.0;
     for (int i = tid; i < npc; i += nt) s.shift[i] = i < nn ? p.shift[n0 + i] : 0.0;
-  }
   for (int i = tid; i < npc * p.nterms; i += nt) {
     const bool ok = i < nn * p.nterms;
     const int g = n0 * p.nterms + i;
     s.nbr[i] = ok ? p.nbr[g] : -1;
     s.site[i] = ok ? p.site[g] : 0;
-    if constexpr (sizeof(T) == 4) {
-      s.al[i] = ok ? p.alpha32[g] : make_float2(0.f, 0.f);
-      s.be[i] = ok ? p.beta32[g] : make_float2(0.f, 0.f);
-      s.ga[i] = (ok && p.gamma32) ? p.gamma32[g] : make_float2(0.f, 0.f);
-    } else {
-      s.al[i] = ok ? p.alpha[g] : make_double2(0.0, 0.0);
-      s.be[i] = ok ? p.beta[g] : make_double2(0.0, 0.0);
-      s.ga[i] = (ok && p.gamma) ? p.gamma[g] : make_double2(0.0, 0.0);
-    }
+    s.al[i] = ok ? p.alpha[g] : make_double2(0.0, 0.0);
+    s.be[i] = ok ? p.beta[g] : make_double2(0.0, 0.0);
+    s.ga[i] = (ok && p.gamma) ? p.gamma[g] : make_double2(0.0, 0.0);
   }
   const C* xb = x + (b * p.nnodes + n0) * (int64_t)p.E;
   for (int i = tid; i < nn * p.E; i += nt) s.x[i] = xb[i];
@@ -197,65 +168,428 @@ __device__ __forceinline__ void heom_rhs_elem(const HeomP& p, const typename cpl
     orr = fma(fr, v.x, fma(-fi, v.y, orr));
     oi = fma(fr, v.y, fma(fi, v.x, oi));
   }
-  T uc;
-  if constexpr (sizeof(T) == 4)
-    uc = p.uc32;
-  else
-    uc = p.uc;
+  const T uc = (T)p.uc;
   out.x = uc * orr;
   out.y = uc * oi;
 }
 
-// One RK4 stage (see qsx_heom_rk4): k = RHS(in); stage 0..2 write the next
-// stage input, stage 3 adds h/6 (acc + k) to the state (split-word in FP32).
+// ------------------------------------------- per-stage form, warp per node
+// One warp per node block and stage, no block-wide staging: the lanes own
+// the elements e = lane + 32 i of the block, the Hamiltonians, occupations
+// and weights are read through the L1 (a few hundred bytes shared by every
+// warp), the node's own block goes through a warp-private slice of shared
+// memory for the commutator, and the term table is read one packed record at
+// a time (the same address in every lane: one broadcast).  Each warp walks a
+// contiguous range of (sample, node) blocks, so the warps of a CTA touch
+// neighbouring nodes and their neighbour reads share the L1.
 template <typename T>
-__global__ void __launch_bounds__(256)
-    heom_stage_kernel(HeomP p, int stage, const typename cplx<T>::type* in,
-                      typename cplx<T>::type* yh, typename cplx<T>::type* __restrict__ yl,
-                      typename cplx<T>::type* __restrict__ acc,
-                      typename cplx<T>::type* __restrict__ next, int npc) {
-  using C = typename cplx<T>::type;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  HeomSmem<T> sm = heom_carve<T>(smraw, p, npc);
-  const int64_t b = blockIdx.y;
-  const int n0 = blockIdx.x * npc;
-  heom_stage_smem<T>(p, in, b, n0, npc, sm);
-  const int local = threadIdx.x / p.E, e = threadIdx.x % p.E;
-  const int node = n0 + local;
-  if (local >= npc || node >= p.nnodes) return;
-  C k;
-  heom_rhs_elem<T>(p, in, b, local, e, sm, k);
-  const int64_t idx = (b * p.nnodes + node) * (int64_t)p.E + e;
-  T h;
-  if constexpr (sizeof(T) == 4)
-    h = p.h32;
-  else
-    h = p.h;
+struct __align__(16) HTerm;
+template <>
+struct __align__(16) HTerm<float> {
+  int nbr, site;
+  float2 al, be, ga;
+};
+template <>
+struct __align__(16) HTerm<double> {
+  int nbr, site, pad0, pad1;
+  double2 al, be, ga;
+};
+
+template <typename T>
+__global__ void heom_pack_terms_kernel(const int* __restrict__ nbr, const int* __restrict__ site,
+                                       const double2* __restrict__ alpha,
+                                       const double2* __restrict__ beta,
+                                       const double2* __restrict__ gamma, int64_t n,
+                                       HTerm<T>* out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  HTerm<T> r;
+  r.nbr = nbr[i];
+  r.site = site[i];
+  const double2 a = alpha[i], b = beta[i];
+  const double2 g = gamma ? gamma[i] : make_double2(0.0, 0.0);
+  r.al = cmk((T)a.x, (T)a.y);
+  r.be = cmk((T)b.x, (T)b.y);
+  r.ga = cmk((T)g.x, (T)g.y);
+  if constexpr (sizeof(T) == 8) r.pad0 = r.pad1 = 0;
+  out[i] = r;
+}
+
+struct HeomWP {
+  int nx, ny, E, nnodes, nterms, n_sites, per_warp;
+  int64_t items;              // batch * nnodes
+  int64_t Hx_stride, Hy_stride;
+  const void* Hx;             // T tables (FP32 copies in the FP32 form)
+  const void* Hy;
+  const void* occx;
+  const void* occy;
+  const void* W;              // or null
+  const void* Wraw;           // or null
+  const void* shift;
+  const void* terms;          // HTerm<T> [nnodes][nterms]
+  int has_gamma;
+  double uc, h;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_term(const HTerm<T>* r, int& nbr, int& site,
+                                          typename cplx<T>::type& al,
+                                          typename cplx<T>::type& be,
+                                          typename cplx<T>::type& ga) {
+  if constexpr (sizeof(T) == 4) {
+    const int4 a = __ldg(reinterpret_cast<const int4*>(r));
+    const float4 b = __ldg(reinterpret_cast<const float4*>(r) + 1);
+    nbr = a.x;
+    site = a.y;
+    al = make_float2(__int_as_float(a.z), __int_as_float(a.w));
+    be = make_float2(b.x, b.y);
+    ga = make_float2(b.z, b.w);
+  } else {
+    const int4 a = __ldg(reinterpret_cast<const int4*>(r));
+    nbr = a.x;
+    site = a.y;
+    al = __ldg(reinterpret_cast<const double2*>(r) + 1);
+    be = __ldg(reinterpret_cast<const double2*>(r) + 2);
+    ga = __ldg(reinterpret_cast<const double2*>(r) + 3);
+  }
+}
+
+// RK4 bookkeeping of one element after its stage derivative k: stages 0..2
+// accumulate k and write the next stage input, stage 3 adds h/6 (acc + k) to
+// the state (split-word in FP32).
+template <typename T>
+__device__ __forceinline__ void heom_rk4_update(int stage, int64_t idx,
+                                                typename cplx<T>::type k, T h,
+                                                typename cplx<T>::type* yh,
+                                                typename cplx<T>::type* yl,
+                                                typename cplx<T>::type* acc,
+                                                typename cplx<T>::type* next) {
+  using Cx = typename cplx<T>::type;
   if (stage == 0) {
     acc[idx] = k;
-    const C y = yh[idx];
+    const Cx y = yh[idx];
     next[idx] = cmk(y.x + (T)0.5 * h * k.x, y.y + (T)0.5 * h * k.y);
   } else if (stage < 3) {
-    C a = acc[idx];
+    const Cx a = acc[idx];
     acc[idx] = cmk(a.x + (T)2 * k.x, a.y + (T)2 * k.y);
-    const C y = yh[idx];
+    const Cx y = yh[idx];
     const T c = stage == 1 ? (T)0.5 * h : h;
     next[idx] = cmk(y.x + c * k.x, y.y + c * k.y);
   } else {
-    const C a = acc[idx];
-    const T sx6 = h / (T)6;
-    const T ix = sx6 * (a.x + k.x), iy = sx6 * (a.y + k.y);
-    C y = yh[idx];
-    if (sizeof(T) == 4) {
-      C l = yl[idx];
-      float hx = (float)y.x, lx = (float)l.x, hy = (float)y.y, ly = (float)l.y;
-      dd_add(hx, lx, (float)ix);
-      dd_add(hy, ly, (float)iy);
-      yh[idx] = cmk((T)hx, (T)hy);
-      yl[idx] = cmk((T)lx, (T)ly);
+    const Cx a = acc[idx];
+    const T s6 = h / (T)6;
+    const T ix = s6 * (a.x + k.x), iy = s6 * (a.y + k.y);
+    const Cx y = yh[idx];
+    if constexpr (sizeof(T) == 4) {
+      const Cx l = yl[idx];
+      float hx = y.x, lx = l.x, hy = y.y, ly = l.y;
+      dd_add(hx, lx, ix);
+      dd_add(hy, ly, iy);
+      yh[idx] = cmk(hx, hy);
+      yl[idx] = cmk(lx, ly);
     } else {
       yh[idx] = cmk(y.x + ix, y.y + iy);
     }
+  }
+}
+
+// Any block shape (nx * ny <= 256): EPL elements per lane.
+template <typename T, int EPL>
+__global__ void __launch_bounds__(256)
+    heom_warp_stage_kernel(HeomWP p, int stage, const typename cplx<T>::type* __restrict__ in,
+                           typename cplx<T>::type* yh, typename cplx<T>::type* __restrict__ yl,
+                           typename cplx<T>::type* __restrict__ acc,
+                           typename cplx<T>::type* __restrict__ next) {
+  using Cx = typename cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  Cx* xs = reinterpret_cast<Cx*>(smraw) + (size_t)wib * 32 * EPL;
+  const int64_t warp = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+  const int64_t i0 = warp * p.per_warp;
+  const int64_t i1 = min(p.items, i0 + p.per_warp);
+  const int E = p.E, nx = p.nx, ny = p.ny, nt = p.nterms;
+  const T* Hx0 = (const T*)p.Hx;
+  const T* Hy0 = (const T*)p.Hy;
+  const T* ox = (const T*)p.occx;
+  const T* oy = (const T*)p.occy;
+  const T* shift = (const T*)p.shift;
+  const HTerm<T>* terms = (const HTerm<T>*)p.terms;
+  const T uc = (T)p.uc, h = (T)p.h;
+  // the lane's elements: indices and the per-element weights
+  int ea[EPL], eb[EPL];
+  T w[EPL], wr[EPL];
+#pragma unroll
+  for (int u = 0; u < EPL; ++u) {
+    const int e = lane + 32 * u;
+    const int ec = e < E ? e : 0;
+    ea[u] = ec % nx;
+    eb[u] = ec / nx;
+    w[u] = p.W ? __ldg((const T*)p.W + ec) : (T)0;
+    wr[u] = p.Wraw ? __ldg((const T*)p.Wraw + ec) : (T)0;
+  }
+  for (int64_t it = i0; it < i1; ++it) {
+    const int64_t b = it / p.nnodes;
+    const int n = (int)(it - b * p.nnodes);
+    const Cx* xb = in + b * (int64_t)p.nnodes * E;
+    const T* Hx = Hx0 + b * p.Hx_stride;
+    const T* Hy = Hy0 + b * p.Hy_stride;
+    Cx self[EPL];
+#pragma unroll
+    for (int u = 0; u < EPL; ++u) {
+      const int e = lane + 32 * u;
+      self[u] = cmk((T)0, (T)0);
+      if (e < E) {
+        self[u] = xb[(int64_t)n * E + e];
+        xs[e] = self[u];
+      }
+    }
+    __syncwarp();
+    const T sh = __ldg(shift + n);
+    T orr[EPL], oi[EPL];
+#pragma unroll
+    for (int u = 0; u < EPL; ++u) {
+      const int a = ea[u], bb = eb[u];
+      // -i (Hx x - x Hy)[a][bb]
+      T cr = 0, ci = 0;
+      for (int c = 0; c < nx; ++c) {
+        const T hv = __ldg(Hx + a * nx + c);
+        const Cx v = xs[c + nx * bb];
+        cr = fma(hv, v.x, cr);
+        ci = fma(hv, v.y, ci);
+      }
+      for (int c = 0; c < ny; ++c) {
+        const T hv = __ldg(Hy + c * ny + bb);
+        const Cx v = xs[a + nx * c];
+        cr = fma(-hv, v.x, cr);
+        ci = fma(-hv, v.y, ci);
+      }
+      const T d = sh + w[u];
+      orr[u] = fma(-d, self[u].x, ci);
+      oi[u] = fma(-d, self[u].y, -cr);
+    }
+    // couplings: every term of the node in the same order in all lanes
+    const HTerm<T>* tr = terms + (int64_t)n * nt;
+    for (int t = 0; t < nt; ++t) {
+      int m, j;
+      Cx al, be, ga;
+      load_term<T>(tr + t, m, j, al, be, ga);
+      if (m < 0) continue;
+      const Cx* xm = xb + (int64_t)m * E;
+#pragma unroll
+      for (int u = 0; u < EPL; ++u) {
+        const int e = lane + 32 * u;
+        if (e >= E) continue;
+        const Cx v = xm[e];
+        const T oa = __ldg(ox + j * nx + ea[u]), ob = __ldg(oy + j * ny + eb[u]);
+        T fr = al.x * oa + be.x * ob, fi = al.y * oa + be.y * ob;
+        if (p.has_gamma) {
+          const T gw = wr[u] * (oa - ob);
+          fr = fma(ga.x, gw, fr);
+          fi = fma(ga.y, gw, fi);
+        }
+        orr[u] = fma(fr, v.x, fma(-fi, v.y, orr[u]));
+        oi[u] = fma(fr, v.y, fma(fi, v.x, oi[u]));
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < EPL; ++u) {
+      const int e = lane + 32 * u;
+      if (e >= E) continue;
+      heom_rk4_update<T>(stage, (b * p.nnodes + n) * (int64_t)E + e,
+                         cmk(uc * orr[u], uc * oi[u]), h, yh, yl, acc, next);
+    }
+    __syncwarp();   // the block slice is rewritten by the next node
+  }
+}
+
+// Blocks of at most 8 x 8 (every one-exciton hierarchy up to 8 sites): two
+// elements per lane, the lane's rows of Hx and columns of Hy in registers
+// (reloaded when the sample changes), the term loop four terms at a time so
+// eight neighbour loads per lane are in flight, and independent accumulator
+// chains in the commutator.  NB = 8 fixes the block at 8 x 8 at compile time;
+// NB = 0 takes nx, ny <= 8 at run time.
+template <typename T, int NB, int G, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    heom_warp_small_kernel(HeomWP p, int stage, const typename cplx<T>::type* __restrict__ in,
+                           typename cplx<T>::type* yh, typename cplx<T>::type* __restrict__ yl,
+                           typename cplx<T>::type* __restrict__ acc,
+                           typename cplx<T>::type* __restrict__ next) {
+  using Cx = typename cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int nx = NB ? NB : p.nx, ny = NB ? NB : p.ny, E = NB ? NB * NB : p.E;
+  const int nt = p.nterms, N = p.n_sites, nnodes = p.nnodes;
+  Cx* xs = reinterpret_cast<Cx*>(smraw) + (size_t)wib * 64;
+  T* sox = reinterpret_cast<T*>(reinterpret_cast<Cx*>(smraw) + (size_t)(blockDim.x >> 5) * 64);
+  T* soy = sox + N * nx;
+  for (int i = threadIdx.x; i < N * nx; i += blockDim.x) sox[i] = ((const T*)p.occx)[i];
+  for (int i = threadIdx.x; i < N * ny; i += blockDim.x) soy[i] = ((const T*)p.occy)[i];
+  __syncthreads();
+  const int64_t warp = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+  const int64_t i0 = warp * p.per_warp;
+  const int64_t i1 = min(p.items, i0 + p.per_warp);
+  if (i0 >= i1) return;
+  const T* shift = (const T*)p.shift;
+  const HTerm<T>* terms = (const HTerm<T>*)p.terms;
+  const T uc = (T)p.uc, h = (T)p.h;
+  int ea[2], eb[2];
+  bool ev[2];
+  T w[2], wr[2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int e = lane + 32 * u;
+    ev[u] = e < E;
+    const int ec = ev[u] ? e : 0;
+    ea[u] = ec % nx;
+    eb[u] = ec / nx;
+    w[u] = p.W ? __ldg((const T*)p.W + ec) : (T)0;
+    wr[u] = p.Wraw ? __ldg((const T*)p.Wraw + ec) : (T)0;
+  }
+  // (sample, node) of the first item; later items step through them
+  int64_t b = i0 / nnodes;
+  int n = (int)(i0 - b * nnodes);
+  T hx[2][8], hy[2][8];
+  const Cx* xb = nullptr;
+  bool fresh = true;
+  for (int64_t it = i0; it < i1; ++it) {
+    if (fresh) {
+      fresh = false;
+      xb = in + b * (int64_t)nnodes * E;
+      const T* Hx = (const T*)p.Hx + b * p.Hx_stride;
+      const T* Hy = (const T*)p.Hy + b * p.Hy_stride;
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          // at 8 x 8 both elements of a lane share the row a (e and e + 32)
+          hx[u][c] = c < nx ? __ldg(Hx + ea[NB == 8 ? 0 : u] * nx + c) : (T)0;
+          hy[u][c] = c < ny ? __ldg(Hy + c * ny + eb[u]) : (T)0;
+        }
+    }
+    const int64_t base = it * E;
+    const Cx* xn = xb + n * E + lane;
+    Cx self[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      self[u] = cmk((T)0, (T)0);
+      if (ev[u]) {
+        self[u] = xn[32 * u];
+        xs[lane + 32 * u] = self[u];
+      }
+    }
+    const HTerm<T>* tr = terms + n * nt;
+    int gm[G], gj[G];
+    Cx gal[G], gbe[G], gga[G], gv[G][2];
+    auto load_group = [&](int t0) {
+#pragma unroll
+      for (int q = 0; q < G; ++q) {
+        gm[q] = -1;
+        gj[q] = 0;
+        if (t0 + q < nt) load_term<T>(tr + t0 + q, gm[q], gj[q], gal[q], gbe[q], gga[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < G; ++q) {
+        const Cx* xm = xb + (gm[q] < 0 ? 0 : gm[q]) * E + lane;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          gv[q][u] = cmk((T)0, (T)0);
+          if (gm[q] >= 0 && ev[u]) gv[q][u] = xm[32 * u];
+        }
+      }
+    };
+    T orr[2], oi[2];
+    auto use_group = [&]() {
+#pragma unroll
+      for (int q = 0; q < G; ++q) {
+        if (gm[q] < 0) continue;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const T oa = sox[gj[q] * nx + ea[u]], ob = soy[gj[q] * ny + eb[u]];
+          T fr = gal[q].x * oa + gbe[q].x * ob, fi = gal[q].y * oa + gbe[q].y * ob;
+          if (p.has_gamma) {
+            const T gw = wr[u] * (oa - ob);
+            fr = fma(gga[q].x, gw, fr);
+            fi = fma(gga[q].y, gw, fi);
+          }
+          orr[u] = fma(fr, gv[q][u].x, fma(-fi, gv[q][u].y, orr[u]));
+          oi[u] = fma(fr, gv[q][u].y, fma(fi, gv[q][u].x, oi[u]));
+        }
+      }
+    };
+    load_group(0);
+    // RK4 operands, then the commutator while the neighbour loads fly
+    Cx yv[2], av[2], lv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      yv[u] = av[u] = lv[u] = cmk((T)0, (T)0);
+      if (ev[u]) {
+        yv[u] = yh[base + lane + 32 * u];
+        if (stage > 0) av[u] = acc[base + lane + 32 * u];
+        if constexpr (sizeof(T) == 4) {
+          if (stage == 3) lv[u] = yl[base + lane + 32 * u];
+        }
+      }
+    }
+    __syncwarp();
+    const T sh = __ldg(shift + n);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      // -i (Hx x - x Hy)[a][bb] in four independent chains
+      T c0 = 0, s0 = 0, c1 = 0, s1 = 0;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        if (c < nx) {
+          const Cx xv = xs[c + nx * eb[u]];
+          c0 = fma(hx[u][c], xv.x, c0);
+          s0 = fma(hx[u][c], xv.y, s0);
+        }
+        if (c < ny) {
+          const Cx xv = xs[ea[u] + nx * c];
+          c1 = fma(hy[u][c], xv.x, c1);
+          s1 = fma(hy[u][c], xv.y, s1);
+        }
+      }
+      const T d = sh + w[u];
+      orr[u] = fma(-d, self[u].x, s0 - s1);
+      oi[u] = fma(-d, self[u].y, c1 - c0);
+    }
+    use_group();
+    for (int t0 = G; t0 < nt; t0 += G) {
+      load_group(t0);
+      use_group();
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (!ev[u]) continue;
+      const Cx k = cmk(uc * orr[u], uc * oi[u]);
+      const int64_t idx = base + lane + 32 * u;
+      if (stage == 0) {
+        acc[idx] = k;
+        next[idx] = cmk(yv[u].x + (T)0.5 * h * k.x, yv[u].y + (T)0.5 * h * k.y);
+      } else if (stage < 3) {
+        acc[idx] = cmk(av[u].x + (T)2 * k.x, av[u].y + (T)2 * k.y);
+        const T c = stage == 1 ? (T)0.5 * h : h;
+        next[idx] = cmk(yv[u].x + c * k.x, yv[u].y + c * k.y);
+      } else {
+        const T s6 = h / (T)6;
+        const T ix = s6 * (av[u].x + k.x), iy = s6 * (av[u].y + k.y);
+        if constexpr (sizeof(T) == 4) {
+          float hx_ = yv[u].x, lx = lv[u].x, hy_ = yv[u].y, ly = lv[u].y;
+          dd_add(hx_, lx, ix);
+          dd_add(hy_, ly, iy);
+          yh[idx] = cmk(hx_, hy_);
+          yl[idx] = cmk(lx, ly);
+        } else {
+          yh[idx] = cmk(yv[u].x + ix, yv[u].y + iy);
+        }
+      }
+    }
+    if (++n == nnodes) {
+      n = 0;
+      ++b;
+      fresh = true;
+    }
+    __syncwarp();   // the block slice is rewritten by the next node
   }
 }
 
@@ -550,6 +884,7 @@ static int heom_validate(const qsx_heom_args* a) {
   QSX_CHECK_ARG(a->nx >= 1 && a->ny >= 1 && a->nx <= 32 && a->ny <= 32 && a->nx * a->ny <= 256,
                 "qsx_heom: need nx, ny <= 32 and nx * ny <= 256");
   QSX_CHECK_ARG(a->nnodes >= 1 && a->nterms >= 0 && a->n_sites >= 1, "qsx_heom: bad sizes");
+  QSX_CHECK_ARG(a->variant >= 0 && a->variant <= 2, "qsx_heom: variant must be 0, 1 or 2");
   QSX_CHECK_ARG(a->batch >= 0 && a->batch <= 65535, "qsx_heom: batch must be in [0, 65535]");
   QSX_CHECK_ARG(a->nsteps >= 0 && a->save_every >= 1 && a->nsteps % a->save_every == 0,
                 "qsx_heom: nsteps must be a non-negative multiple of save_every");
@@ -589,17 +924,12 @@ static HeomP heom_params(const qsx_heom_args* a) {
   p.Wraw = a->Wraw;
   p.uc = a->unit_convert;
   p.h = a->h;
-  p.uc32 = (float)a->unit_convert;
-  p.h32 = (float)a->h;
-  p.Hx32 = p.Hy32 = p.occx32 = p.occy32 = p.W32 = p.shift32 = nullptr;
-  p.alpha32 = p.beta32 = p.gamma32 = nullptr;
-  p.Wraw32 = nullptr;
   return p;
 }
 
 template <typename T, int EPT>
 static cudaError_t launch_heom_cluster(const HeomCP& p, size_t smem, cudaStream_t s,
-                                       int* clusters) {
+                                       int* clusters, bool one_wave) {
   auto kern = heom_cluster_kernel<T, EPT>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
@@ -619,11 +949,18 @@ static cudaError_t launch_heom_cluster(const HeomCP& p, size_t smem, cudaStream_
   *clusters = 0;
   e = cudaOccupancyMaxActiveClusters(clusters, kern, &cfg);
   if (e != cudaSuccess || *clusters < 1) return e;
+  // the library's choice takes this form only when every sample's cluster is
+  // resident at once: a second wave would rerun the whole time loop
+  if (one_wave && p.batch > *clusters) {
+    *clusters = 0;
+    return cudaSuccess;
+  }
   return cudaLaunchKernelEx(&cfg, kern, p);
 }
 
-// The persistent cluster form when the shapes allow it: returns 1 if it ran
-// (or failed with *st set), 0 to fall back to the per-stage kernels.
+// The persistent cluster form when the shapes allow it (and, for variant 0,
+// when all samples fit in one wave): returns 1 if it ran (or failed with *st
+// set), 0 to fall back to the per-stage kernels.
 template <typename T>
 static int heom_rk4_cluster(const qsx_heom_args* a, double2* saves, cudaStream_t s, int* st) {
   const int E = a->nx * a->ny;
@@ -632,7 +969,11 @@ static int heom_rk4_cluster(const qsx_heom_args* a, double2* saves, cudaStream_t
   const int ept = (npcta * E + 511) / 512;
   const size_t smem =
       heom_cluster_smem_bytes<T>(a->nx, a->ny, a->n_sites, E, npcta, std::max(a->nterms, 1));
-  if (ept > 16 || smem > 200 * 1024) return 0;
+  // register budget: at most 8 elements a thread in FP32 and 4 in FP64 (the
+  // builds beyond spill; the spilled FP64 build at 8 elements a thread gave
+  // results off by 1e-3 on the 495-node hierarchy, so those shapes take the
+  // per-stage kernels)
+  if (ept > (sizeof(T) == 4 ? 8 : 4) || smem > 200 * 1024) return 0;
   HeomCP p;
   p.nx = a->nx;
   p.ny = a->ny;
@@ -670,15 +1011,15 @@ static int heom_rk4_cluster(const qsx_heom_args* a, double2* saves, cudaStream_t
   int clusters = 0;
   cudaError_t e;
   if (ept <= 1)
-    e = launch_heom_cluster<T, 1>(p, smem, s, &clusters);
+    e = launch_heom_cluster<T, 1>(p, smem, s, &clusters, a->variant == 0);
   else if (ept <= 2)
-    e = launch_heom_cluster<T, 2>(p, smem, s, &clusters);
+    e = launch_heom_cluster<T, 2>(p, smem, s, &clusters, a->variant == 0);
   else if (ept <= 4)
-    e = launch_heom_cluster<T, 4>(p, smem, s, &clusters);
-  else if (ept <= 8)
-    e = launch_heom_cluster<T, 8>(p, smem, s, &clusters);
+    e = launch_heom_cluster<T, 4>(p, smem, s, &clusters, a->variant == 0);
+  else if constexpr (sizeof(T) == 4)
+    e = launch_heom_cluster<T, 8>(p, smem, s, &clusters, a->variant == 0);
   else
-    e = launch_heom_cluster<T, 16>(p, smem, s, &clusters);
+    return 0;
   if (e != cudaSuccess) {
     *st = cuda_status(e, "qsx_heom_rk4 (cluster form)");
     return 1;
@@ -697,8 +1038,8 @@ __global__ void f64_to_f32_kernel(const double* __restrict__ src, float* __restr
   if (i < n) dst[i] = (float)src[i];
 }
 
-// element counts of the FP32 table copies: Hx, Hy, occx, occy, W, shift,
-// alpha and beta (the last two as floats, two per complex entry)
+// element counts of the FP32 table copies: Hx, Hy, occx, occy, W, shift and
+// Wraw (slots 6..8 are empty: the term tables are packed separately)
 static void heom_table_counts(const qsx_heom_args* a, int64_t c[10]) {
   const int64_t hb = a->H_stride ? a->batch : 1;
   c[0] = hb * a->nx * a->nx;
@@ -707,9 +1048,7 @@ static void heom_table_counts(const qsx_heom_args* a, int64_t c[10]) {
   c[3] = (int64_t)a->n_sites * a->ny;
   c[4] = a->W ? (int64_t)a->nx * a->ny : 0;
   c[5] = a->nnodes;
-  c[6] = 2 * (int64_t)a->nnodes * a->nterms;
-  c[7] = c[6];
-  c[8] = a->gamma ? c[6] : 0;
+  c[6] = c[7] = c[8] = 0;   // the term tables go into the packed records
   c[9] = a->Wraw ? (int64_t)a->nx * a->ny : 0;
 }
 
@@ -741,7 +1080,9 @@ int qsx_heom_workspace_bytes(const qsx_heom_args* a, size_t* bytes) {
   const size_t saves =
       a->out_mean ? (size_t)a->batch * nsave * a->save_nodes * a->nx * a->ny * sizeof(double2) : 0;
   const size_t tables = a->precision == QSX_FP32 ? heom_table_bytes(a) + 256 : 0;
-  *bytes = states + saves + 256 + tables;
+  const size_t terms = (size_t)a->nnodes * a->nterms *
+                       (a->precision == QSX_FP32 ? sizeof(HTerm<float>) : sizeof(HTerm<double>));
+  *bytes = states + saves + 256 + tables + terms + 256;
   return QSX_OK;
 }
 
@@ -779,9 +1120,6 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
   HeomP p = heom_params(a);
   cudaStream_t s = (cudaStream_t)stream;
   const size_t n = heom_state_elems(a);
-  const int npc = std::max(1, 256 / p.E);
-  const int threads = ((npc * p.E + 31) / 32) * 32;
-  dim3 grid((unsigned)((p.nnodes + npc - 1) / npc), (unsigned)p.batch);
   const int64_t per = (int64_t)p.nnodes * p.E;
   double2* node0 = a->out_state ? (double2*)a->out_state : nullptr;
   const int keep = a->save_nodes;
@@ -812,13 +1150,25 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
     C* s1 = s0 + n;
     double2* saves = (double2*)(((size_t)(s1 + n) + 255) & ~(size_t)255);
     if (!node0) node0 = saves;
+    const int nsave_ = p.nsave;
+    const size_t save_bytes =
+        a->out_mean ? (size_t)p.batch * nsave_ * keep * p.E * sizeof(double2) : 0;
+    unsigned char* tp = (unsigned char*)((((size_t)saves + save_bytes) + 255) & ~(size_t)255);
+    HeomWP w;
+    w.nx = p.nx;
+    w.ny = p.ny;
+    w.E = p.E;
+    w.nnodes = p.nnodes;
+    w.nterms = p.nterms;
+    w.n_sites = p.n_sites;
+    w.items = p.batch * p.nnodes;
+    w.Hx_stride = p.Hx_stride;
+    w.Hy_stride = p.Hy_stride;
+    w.has_gamma = a->gamma != nullptr;
+    w.uc = p.uc;
+    w.h = p.h;
     if constexpr (sizeof(T) == 4) {
       // FP32 copies of the tables after the saves
-      const int nsave_ = p.nsave;
-      const size_t save_bytes =
-          a->out_mean ? (size_t)p.batch * nsave_ * keep * p.E * sizeof(double2) : 0;
-      unsigned char* tp =
-          (unsigned char*)((((size_t)saves + save_bytes) + 255) & ~(size_t)255);
       int64_t c[10];
       heom_table_counts(a, c);
       const double* src[10] = {a->Hx, a->Hy, a->occx, a->occy, a->W, a->shift, a->alpha,
@@ -831,22 +1181,62 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
           f64_to_f32_kernel<<<(unsigned)((c[i] + 255) / 256), 256, 0, s>>>(src[i], dst[i], c[i]);
       }
       QSX_LAUNCH_CHECK("qsx_heom_rk4 tables");
-      p.Hx32 = dst[0];
-      p.Hy32 = dst[1];
-      p.occx32 = dst[2];
-      p.occy32 = dst[3];
-      p.W32 = a->W ? dst[4] : nullptr;
-      p.shift32 = dst[5];
-      p.alpha32 = (const float2*)dst[6];
-      p.beta32 = (const float2*)dst[7];
-      p.gamma32 = a->gamma ? (const float2*)dst[8] : nullptr;
-      p.Wraw32 = a->Wraw ? dst[9] : nullptr;
+      w.Hx = dst[0];
+      w.Hy = dst[1];
+      w.occx = dst[2];
+      w.occy = dst[3];
+      w.W = a->W ? dst[4] : nullptr;
+      w.shift = dst[5];
+      w.Wraw = a->Wraw ? dst[9] : nullptr;
+    } else {
+      w.Hx = a->Hx;
+      w.Hy = a->Hy;
+      w.occx = a->occx;
+      w.occy = a->occy;
+      w.W = a->W;
+      w.shift = a->shift;
+      w.Wraw = a->Wraw;
     }
-    const size_t smem = heom_smem_bytes<T>(p.nx, p.ny, p.n_sites, p.E, npc, p.nterms);
-    QSX_CHECK_ARG(smem <= 227 * 1024, "qsx_heom_rk4: node tables too large for shared memory");
-    cudaError_t ce = cudaFuncSetAttribute(heom_stage_kernel<T>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // packed term records
+    HTerm<T>* terms = (HTerm<T>*)tp;
+    const int64_t nrec = (int64_t)p.nnodes * p.nterms;
+    if (nrec > 0) {
+      heom_pack_terms_kernel<T><<<(unsigned)((nrec + 255) / 256), 256, 0, s>>>(
+          a->nbr, a->site, (const double2*)a->alpha, (const double2*)a->beta,
+          (const double2*)a->gamma, nrec, terms);
+      QSX_LAUNCH_CHECK("qsx_heom_rk4 terms");
+    }
+    w.terms = terms;
+    // blocks up to 8 x 8: the specialised kernel; wider ones: EPL elements a lane
+    const int epl = p.E <= 32 ? 1 : (p.E <= 64 ? 2 : (p.E <= 128 ? 4 : 8));
+    const bool small = p.nx <= 8 && p.ny <= 8;
+    auto kern = small      ? (p.nx == 8 && p.ny == 8 ? heom_warp_small_kernel<T, 8, 4, (sizeof(T) == 4 ? 2 : 1)>
+                                                     : heom_warp_small_kernel<T, 0, 4, (sizeof(T) == 4 ? 2 : 1)>)
+                : epl == 1 ? heom_warp_stage_kernel<T, 1>
+                : epl == 2 ? heom_warp_stage_kernel<T, 2>
+                : epl == 4 ? heom_warp_stage_kernel<T, 4>
+                           : heom_warp_stage_kernel<T, 8>;
+    const int wthreads = 256;
+    const size_t wsmem =
+        small ? (size_t)(wthreads / 32) * 64 * sizeof(C) + (size_t)p.n_sites * (p.nx + p.ny) * sizeof(T)
+              : (size_t)(wthreads / 32) * 32 * epl * sizeof(C);
+    if (wsmem > 48 * 1024) {
+      cudaError_t fe = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)wsmem);
+      if (fe != cudaSuccess) return cuda_status(fe, "qsx_heom_rk4");
+    }
+    // contiguous ranges of node blocks per warp, sized so one wave of
+    // resident warps covers them
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (ce == cudaSuccess)
+      ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, wthreads, wsmem);
     if (ce != cudaSuccess) return cuda_status(ce, "qsx_heom_rk4");
+    const int64_t resident = std::max<int64_t>(1, (int64_t)sms * std::max(per_sm, 1) * (wthreads / 32));
+    w.per_warp = (int)((w.items + resident - 1) / resident);
+    const int64_t warps = (w.items + w.per_warp - 1) / w.per_warp;
+    const unsigned wgrid = (unsigned)((warps + wthreads / 32 - 1) / (wthreads / 32));
     heom_init_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
         (const double2*)a->y0, a->y0_stride ? per : 0, per, p.batch, yh, yl);
     QSX_LAUNCH_CHECK("qsx_heom_rk4 init");
@@ -854,10 +1244,10 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
     heom_save_kernel<T><<<sg, 256, 0, s>>>(yh, yl, p.nnodes, p.E, keep, p.batch, 0, p.nsave,
                                           node0, a->status);
     for (int step = 1; step <= p.nsteps; ++step) {
-      heom_stage_kernel<T><<<grid, threads, smem, s>>>(p, 0, yh, yh, yl, acc, s0, npc);
-      heom_stage_kernel<T><<<grid, threads, smem, s>>>(p, 1, s0, yh, yl, acc, s1, npc);
-      heom_stage_kernel<T><<<grid, threads, smem, s>>>(p, 2, s1, yh, yl, acc, s0, npc);
-      heom_stage_kernel<T><<<grid, threads, smem, s>>>(p, 3, s0, yh, yl, acc, nullptr, npc);
+      kern<<<wgrid, wthreads, wsmem, s>>>(w, 0, yh, yh, yl, acc, s0);
+      kern<<<wgrid, wthreads, wsmem, s>>>(w, 1, s0, yh, yl, acc, s1);
+      kern<<<wgrid, wthreads, wsmem, s>>>(w, 2, s1, yh, yl, acc, s0);
+      kern<<<wgrid, wthreads, wsmem, s>>>(w, 3, s0, yh, yl, acc, nullptr);
       if (step % p.save_every == 0)
         heom_save_kernel<T><<<sg, 256, 0, s>>>(yh, yl, p.nnodes, p.E, keep, p.batch,
                                               step / p.save_every, p.nsave, node0, a->status);

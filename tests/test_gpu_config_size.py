@@ -124,8 +124,11 @@ def test_benchmarked_workload_host_entry_matches_oracle_slice(fmo7, fmo7_slice_o
 
 
 # --------------------------------------------------------------- HEOM ring 8
+@pytest.mark.parametrize('variant', [0, 1, 2])
 @pytest.mark.parametrize('precision,tol', TOLS)
-def test_heom_ring8_config_size_matches_reference(drivers, precision, tol):
+def test_heom_ring8_config_size_matches_reference(drivers, precision, tol, variant):
+    """variant 0: the library's choice (the persistent cluster kernel for
+    one sample); 1: the per-stage kernels; 2: the cluster kernel forced."""
     H = drivers['ring8_H']
     ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 300, 35, 106),
                                    disorder=wl.fwhm_for_sd(50.0), random_seed=7)
@@ -143,7 +146,7 @@ def test_heom_ring8_config_size_matches_reference(drivers, precision, tol):
     y0[0] = 1.0
     prec = _native.QSX_FP32 if precision == 'fp32' else _native.QSX_FP64
     out = _native.heom_rk4(tb, Hb, Hb, y0, 200, 0.5, qg.CM_FS, batch=1, save_every=1,
-                           save_nodes=495, precision=prec)
+                           save_nodes=495, precision=prec, variant=variant)
     st = out['state'][0].cpu().numpy()            # (201, 495 * 64)
     assert rel_err(st[:, :64], drivers['ring8_traj_node0']) < tol
     assert rel_err(st[-1], drivers['ring8_final_state']) < tol
