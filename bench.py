@@ -616,7 +616,7 @@ def our_arm(args):
         dist.init_process_group('nccl')
     import qspectra_gb300 as qg
     from qspectra_gb300 import _native
-    from qspectra_gb300.simulate.ensemble import RedfieldEnsembleWorkload
+    from qspectra_gb300.simulate.ensemble import RedfieldEnsembleWorkload, block_k_real_timings
 
     H, extra, fwhm = fmo7_inputs()
     S = args.samples
@@ -650,6 +650,25 @@ def our_arm(args):
     e1.record()
     barrier()
     eager_ms = e0.elapsed_time(e1) / args.steps
+    # the batching form, measured: the two legs of a step (the absorption leg
+    # on a side stream, the population leg on the caller's stream) and the
+    # whole step with both legs on one stream
+    legs = {'build_ms': statistics.mean(a.elapsed_time(b) for a, b in events['build']),
+            'absorption_leg_ms': statistics.mean(a.elapsed_time(b) for a, b in events['abs_leg']),
+            'population_leg_ms': statistics.mean(a.elapsed_time(b)
+                                                 for a, b in events['pop_leg'])}
+    work.overlap = False
+    for _ in range(2):
+        work.run(off, 'fp32', build_precision=args.build)
+    barrier()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record()
+    for _ in range(args.steps):
+        work.run(off, 'fp32', build_precision=args.build)
+    s1.record()
+    barrier()
+    work.overlap = True
+    one_stream_ms = s0.elapsed_time(s1) / args.steps
     # the same step as one CUDA graph launch (the library's capture/replay of
     # a step, checked bit for bit against the eager steps): when capture
     # succeeds it is the timed form for `value`, and the end-to-end calls
@@ -780,6 +799,13 @@ def our_arm(args):
                          'eager_ms_per_step': eager_ms,
                          'graph_vs_eager_rel_diff': graph_vs_eager}
                         if graph_ok else {'value': 'eager launches', 'e2e': 'eager launches'}),
+        'batching_form': dict(
+            legs, form=('one launch sequence per step over all 16384 samples: build, then the '
+                        'absorption leg on a side stream beside the population leg, '
+                        'captured as one CUDA graph'),
+            two_stream_eager_ms=eager_ms, one_stream_eager_ms=one_stream_ms,
+            graph_ms=graph_ms,
+            block_k_real=[{'K': v[0], 'ms': v[1]} for v in block_k_real_timings().values()]),
         'fp64_ms_per_step': fp64_ms, 'speedup_fp32_vs_fp64': fp64_ms / ms,
         'e2e': {'value': world * 1000.0 / e2e_ms, 'unit': UNIT,
                 'h2d_bytes_per_step': int(off_host.numel() * 8),

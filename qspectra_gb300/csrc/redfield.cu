@@ -925,15 +925,19 @@ __global__ void __launch_bounds__(256)
 // (16 bits each) in .x, .y and four signed 8-bit coefficients in .z, built
 // once by the host.  So the assembly is nb^3 operator sums in the working
 // precision plus one 16-byte load and four multiply-adds per entry.
-template <typename T>
+//
+// NB > 0 fixes the block size at compile time (the index divisions and the
+// product loops then fold to constants); NB = 0 takes nb at run time.
+template <typename T, int NB>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
     hermitian_propagator_kernel(const double* __restrict__ H, int64_t H_stride,
                                 const double2* __restrict__ G, const double2* __restrict__ Mo,
                                 const double* __restrict__ occ, int n, int n_sites,
-                                const int* __restrict__ states, int nb,
+                                const int* __restrict__ states, int nb_rt,
                                 const int4* __restrict__ recipe, double uc, double h,
                                 T* __restrict__ D) {
   extern __shared__ __align__(16) unsigned char smraw[];
+  const int nb = NB ? NB : nb_rt;
   const int m = nb * nb, ld = (m + 3) & ~3, nb3 = nb * m;
   T* rA = (T*)smraw;
   T* rB = rA + ld * ld;
@@ -945,7 +949,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
   const int64_t b = blockIdx.x;
   const double2* g = G + b * (int64_t)n * n;
   const double2* mo = Mo + b * (int64_t)n_sites * n * n;
-  for (int e = threadIdx.x; e < 3 * ld * ld; e += blockDim.x) rA[e] = (T)0;
+  // rA keeps zero padding (rB and rC are written whole by the steps below)
+  for (int e = threadIdx.x; e < ld * ld * (int)sizeof(T) / 16; e += blockDim.x)
+    reinterpret_cast<uint4*>(rA)[e] = make_uint4(0u, 0u, 0u, 0u);
   for (int e = threadIdx.x; e < nb; e += blockDim.x) st[e] = states[e];
   __syncthreads();
   // every FP64 operator entry of the block is converted once
@@ -1416,21 +1422,28 @@ int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
                       nb * sizeof(int);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e;
+  auto launch = [&](auto kern, auto* Dt) -> cudaError_t {
+    cudaError_t fe = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem);
+    if (fe != cudaSuccess) return fe;
+    kern<<<(unsigned)batch, 256, smem, s>>>(H, H_stride, (const double2*)G, (const double2*)M,
+                                            occ, n, n_sites, states, nb, (const int4*)recipe,
+                                            unit_convert, h, Dt);
+    return cudaSuccess;
+  };
+  // the one-exciton blocks of 7 and 8 sites get compile-time sizes
   if (precision == QSX_FP32) {
-    e = cudaFuncSetAttribute(hermitian_propagator_kernel<float>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_hermitian_batched");
-    hermitian_propagator_kernel<float><<<(unsigned)batch, 256, smem, s>>>(
-        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, states, nb,
-        (const int4*)recipe, unit_convert, h, (float*)D);
+    float* Df = (float*)D;
+    e = nb == 7 ? launch(hermitian_propagator_kernel<float, 7>, Df)
+        : nb == 8 ? launch(hermitian_propagator_kernel<float, 8>, Df)
+                  : launch(hermitian_propagator_kernel<float, 0>, Df);
   } else {
-    e = cudaFuncSetAttribute(hermitian_propagator_kernel<double>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_hermitian_batched");
-    hermitian_propagator_kernel<double><<<(unsigned)batch, 256, smem, s>>>(
-        H, H_stride, (const double2*)G, (const double2*)M, occ, n, n_sites, states, nb,
-        (const int4*)recipe, unit_convert, h, (double*)D);
+    double* Dd = (double*)D;
+    e = nb == 7 ? launch(hermitian_propagator_kernel<double, 7>, Dd)
+        : nb == 8 ? launch(hermitian_propagator_kernel<double, 8>, Dd)
+                  : launch(hermitian_propagator_kernel<double, 0>, Dd);
   }
+  if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_propagator_hermitian_batched");
   QSX_LAUNCH_CHECK("qsx_redfield_propagator_hermitian_batched");
   return QSX_OK;
 }

@@ -196,6 +196,81 @@ def pick_block_k_real(nsteps, m, nselect, max_k=64, tensor_core=None):
     return best
 
 
+# Measured choice of K for the real blocked loop: the candidates the cost
+# model ranks best are timed once (block build plus loop, on the first call's
+# own inputs) per (m, selected coordinates, steps, batch octave), and the
+# fastest is kept for the process.  set_block_k_real(K) pins a value.
+_TUNED_K_REAL = {}
+_PINNED_K_REAL = None
+K_REAL_CANDIDATES = 3
+
+
+def set_block_k_real(K=None):
+    """Pin the real blocked loop's K (None: tune by measurement)."""
+    global _PINNED_K_REAL
+    _PINNED_K_REAL = K
+
+
+def block_k_real_candidates(nsteps, m, nselect, tensor_core=None, count=K_REAL_CANDIDATES):
+    """The ``count`` K values the cost model of pick_block_k_real ranks best."""
+    ranked = []
+    for K in range(2, 65):
+        if nsteps % K or m + nselect * (K - 1) > 512:
+            continue
+        products = bin(K).count('1') - 1 + K.bit_length() - 1
+        build = nselect * m * m * max(K - 2, 0) + products * m ** 3
+        if tensor_core is not None and tensor_core(K):
+            build *= 0.6
+        ranked.append((2.0 * (nsteps // K) * (m + nselect * (K - 1)) * m + build, K))
+    return [K for _, K in sorted(ranked)[:count]]
+
+
+def _real_block_pass(Dr, K, coords, x0, nsteps, use_tc):
+    tc = _native.rk4_block_matrix_real_tc(Dr, K, coords) if use_tc else None
+    if tc is not None:
+        mat, tc_status = tc
+    else:
+        mat, tc_status = _native.rk4_block_matrix_real(Dr, K, coords), None
+    xm, status = _native.rk4_real_block_mean(mat, x0, nsteps, coords, K, check_finite=False)
+    return mat, tc_status, xm, status
+
+
+def tuned_block_k_real(Dr, coords, x0, nsteps, use_tc):
+    """K for the real blocked loop: pinned, measured once per shape, or (while
+    a CUDA graph is being captured, where nothing can be timed) the model's."""
+    m = int(Dr.shape[-1])
+    tcf = ((lambda k: _native.rk4_block_matrix_real_tc_supported(m, k, len(coords)))
+           if use_tc else None)
+    if _PINNED_K_REAL is not None:
+        return _PINNED_K_REAL
+    key = (m, len(coords), int(nsteps), int(np.log2(max(int(Dr.shape[0]), 1))), bool(use_tc))
+    if key in _TUNED_K_REAL:
+        return _TUNED_K_REAL[key][0]
+    cands = block_k_real_candidates(nsteps, m, len(coords), tcf)
+    if not cands:
+        return 1
+    if len(cands) == 1 or torch.cuda.is_current_stream_capturing():
+        return cands[0]
+    times = {}
+    for K in cands:
+        use = use_tc and bool(tcf(K))
+        _real_block_pass(Dr, K, coords, x0, nsteps, use)     # warm
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _real_block_pass(Dr, K, coords, x0, nsteps, use)
+        e1.record()
+        e1.synchronize()
+        times[K] = e0.elapsed_time(e1)
+    best = min(times, key=times.get)
+    _TUNED_K_REAL[key] = (best, times)
+    return best
+
+
+def block_k_real_timings():
+    """{shape key: (chosen K, {K: ms})} of the measured choices so far."""
+    return dict(_TUNED_K_REAL)
+
+
 def hermitian_block_size(idx, n_total):
     """nb when the column-stacked indices ``idx`` form one diagonal block of
     nb x nb states (e.g. 'ee'), else None."""
@@ -230,10 +305,10 @@ def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None,
     coords = np.unique(np.concatenate([sel, partner]))
     Dr = build.hermitian_propagator(idx, nb, h)
     use_tc = _TENSOR_CORE_BLOCKS and Dr.dtype == torch.float32
-    K = pick_block_k_real(
-        nsteps, m, len(coords),
-        tensor_core=(lambda k: _native.rk4_block_matrix_real_tc_supported(m, k, len(coords)))
-        if use_tc else None)
+    if x0 is None:
+        x0 = hermitian_coordinates(y0, nb)
+    K = tuned_block_k_real(Dr, coords, x0, nsteps, use_tc)
+    use_tc = use_tc and bool(_native.rk4_block_matrix_real_tc_supported(m, K, len(coords)))
     if events is not None:
         b0 = torch.cuda.Event(enable_timing=True)
         b0.record()
@@ -255,8 +330,6 @@ def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None,
         events['blockbuild_flops'] = 2.0 * Dr.shape[0] * (
             products * m ** 3 + max(K - 2, 0) * len(coords) * m * m)
     del Dr
-    if x0 is None:
-        x0 = hermitian_coordinates(y0, nb)
     if events is not None:
         e0 = torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -518,17 +591,29 @@ class RedfieldEnsembleWorkload:
             events.setdefault('build', []).append((a0, a1))
         # the absorption leg (eg propagator, time loop, DFT) runs on a side
         # stream, overlapping the population leg on the caller's stream
+        # (self.overlap = False runs it first on the caller's stream)
         main = torch.cuda.current_stream()
         if getattr(self, '_side', None) is None:
             self._side = torch.cuda.Stream()
+        side = self._side if getattr(self, 'overlap', True) else main
         ready = torch.cuda.Event()
         ready.record(main)
-        with torch.cuda.stream(self._side):
-            self._side.wait_event(ready)
+        with torch.cuda.stream(side):
+            side.wait_event(ready)
+            if events is not None:
+                l0 = torch.cuda.Event(enable_timing=True)
+                l0.record()
             D_eg = build.propagator(self.idx_eg, self.dt, prec, transpose=True)
             sig = projected_mean(D_eg, self.y_abs, self.proj_neg, len(self.t_abs) - 1)
             X = _native.dft(sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
                             self.model.rw_freq, self.model.unit_convert, 1)
+            if events is not None:
+                l1 = torch.cuda.Event(enable_timing=True)
+                l1.record()
+                events.setdefault('abs_leg', []).append((l0, l1))
+        if events is not None:
+            p0 = torch.cuda.Event(enable_timing=True)
+            p0.record()
         nb = can_use_hermitian(prec, self.idx_ee, self.n_sites + 1, self.y_dyn_np,
                                len(self.t_dyn) - 1)
         if nb is not None:
@@ -541,11 +626,16 @@ class RedfieldEnsembleWorkload:
             D_ee = build.propagator(self.idx_ee, self.dt, prec)
             pop = propagate_selected_mean(D_ee, self.y_dyn, len(self.t_dyn) - 1, self.select,
                                           prec, events)
-        main.wait_stream(self._side)
-        for t in (X, sig['status']):
-            t.record_stream(main)
-        for t in (build.G, build.M, build.E, build.U, build.occ, H):
-            t.record_stream(self._side)
+        if events is not None:
+            p1 = torch.cuda.Event(enable_timing=True)
+            p1.record()
+            events.setdefault('pop_leg', []).append((p0, p1))
+        if side is not main:
+            main.wait_stream(side)
+            for t in (X, sig['status']):
+                t.record_stream(main)
+            for t in (build.G, build.M, build.E, build.U, build.occ, H):
+                t.record_stream(side)
         status = sig['status'] | pop['status']
         pops = pop['mean_real'] if 'mean_real' in pop else pop['mean'].real
         return X.real, pops, status

@@ -63,3 +63,18 @@ def test_hermitian_coordinates_round_trip():
         assert x[a + nb * a] == rho[a, a].real
     back = ens.from_hermitian_coordinates(x, nb)
     assert np.allclose(back, y, atol=1e-14)
+
+
+def test_measured_block_k_candidates():
+    """The candidates the real-path tuner times: divisors of the step count,
+    ranked by the cost model, the model's own choice first."""
+    tc = lambda k: k in (3, 5, 9, 17, 33)   # 2^J + 1 shapes on the tensor cores
+    c = ens.block_k_real_candidates(999, 49, 7, tc)
+    assert c[0] == ens.pick_block_k_real(999, 49, 7, tensor_core=tc)
+    assert len(c) == 3 and all(999 % K == 0 for K in c)
+    assert ens.block_k_real_candidates(7, 49, 7) == [7]
+    ens.set_block_k_real(3)
+    try:
+        assert ens._PINNED_K_REAL == 3
+    finally:
+        ens.set_block_k_real(None)

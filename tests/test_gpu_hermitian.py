@@ -145,14 +145,23 @@ def test_workload_uses_real_form_and_matches_fp64():
     psi[0] = 1.0
     work = RedfieldEnsembleWorkload(m, 512.0, 1000.0, psi)
     offs = torch.as_tensor(m.hamiltonian.disorder_offsets(256)).cuda()
-    ev = {}
-    X32, P32, st = work.run(offs, 'fp32', ev)
     X64, P64, _ = work.run(offs, 'fp64')
-    assert ev['dyn_variant'] == 'real'
-    assert ev['blockbuild_variant'] == 'tcgen05'
-    assert int(st.item()) == 0
-    assert rel_err(P32.cpu().numpy(), P64.cpu().numpy()) < 1e-5
-    assert rel_err(X32.cpu().numpy(), X64.cpu().numpy()) < 1e-5
+    # K = 9 pinned: the tcgen05 build; then the measured choice of K
+    for pin, variant in ((9, 'tcgen05'), (None, None)):
+        ens.set_block_k_real(pin)
+        try:
+            ev = {}
+            X32, P32, st = work.run(offs, 'fp32', ev)
+        finally:
+            ens.set_block_k_real(None)
+        assert ev['dyn_variant'] == 'real'
+        if pin is not None:
+            assert ev['dyn_block_k'] == pin and ev['blockbuild_variant'] == variant
+        else:
+            assert 999 % ev['dyn_block_k'] == 0
+        assert int(st.item()) == 0
+        assert rel_err(P32.cpu().numpy(), P64.cpu().numpy()) < 1e-5
+        assert rel_err(X32.cpu().numpy(), X64.cpu().numpy()) < 1e-5
 
 
 def test_workload_graph_replay_matches_eager():
