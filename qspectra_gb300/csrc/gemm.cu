@@ -18,9 +18,10 @@
 // operands, A B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi, FP32 accumulation in
 // tensor memory).  Each CTA owns a 128 x 128 tile of C, two CTAs per SM; the
 // K loop moves in chunks of 16 through three buffers: while the tensor core
-// multiplies the previous chunks, all threads load the next one from global
-// memory (16-byte loads of A rows, 8-byte loads of complex B), split it and
-// store it in the K-major core-matrix layout of a free buffer.  One thread issues the
+// multiplies the previous chunks, all threads split and store the chunk
+// their registers hold (loaded from global memory two chunks ahead: 16-byte
+// loads of A rows, 8-byte loads of complex B) in the K-major core-matrix
+// layout of a free buffer.  One thread issues the
 // MMAs and commits them to the buffer's mbarrier; every wait is bounded and a
 // timeout sets QSX_ERR_CUDA in the status word.
 // FP64: CUDA cores, 64 x 64 tiles of C, 4 x 4 per thread, the same views.
@@ -136,7 +137,31 @@ __global__ void __launch_bounds__(GT_THREADS, 2) gemm_tc_kernel(GemmP p) {
   const uint32_t idesc = make_idesc(GT_BN);
   const int nk = (p.K + GT_BK - 1) / GT_BK;
   int issued = 0;   // chunks whose MMAs were issued (uniform across threads)
+  // Each thread's quads of a chunk: two of A (a warp covers 8 rows x 16 k,
+  // 64 contiguous bytes per row; its 16-byte stores fill 32 distinct bank
+  // groups) and two of B'^T (rows n fastest, coalesced along the columns of
+  // B).  The global loads run two chunks ahead of the split and store, in
+  // registers, so their latency hides behind two iterations of work.
+  constexpr int QA = (GT_BM / 8) / (GT_THREADS / 32), QB = (GT_BN * GT_BK / 4) / GT_THREADS;
+  auto load_chunk = [&](int kc, float4 (&va)[QA], float4 (&vb)[QB]) {
+    const int k0 = kc * GT_BK;
+#pragma unroll
+    for (int i = 0; i < QA; ++i) {
+      const int r = 8 * (warp + (GT_THREADS / 32) * i) + (lane & 7), j = lane >> 3;
+      va[i] = a_quad(p, A, m0 + r, k0 + 4 * j);
+    }
+#pragma unroll
+    for (int i = 0; i < QB; ++i) {
+      const int idx = tid + i * GT_THREADS;
+      const int n = idx & (GT_BN - 1), j = idx >> 7;
+      vb[i] = b_quad(p, B, k0 + 4 * j, n0 + n);
+    }
+  };
+  float4 ca[QA], cb[QB], na[QA], nb[QB], fa[QA], fb[QB];
+  if (nk > 0) load_chunk(0, ca, cb);
+  if (nk > 1) load_chunk(1, na, nb);
   for (int kc = 0; kc < nk; ++kc) {
+    if (kc + 2 < nk) load_chunk(kc + 2, fa, fb);
     const int buf = kc % GT_STAGES;
     unsigned char* base = smraw + buf * GT_BUF;
     unsigned char* a_hi = base;
@@ -154,22 +179,16 @@ __global__ void __launch_bounds__(GT_THREADS, 2) gemm_tc_kernel(GemmP p) {
       __syncthreads();
       if (s_abort) break;
     }
-    const int k0 = kc * GT_BK;
-    // A chunk: a warp covers 8 rows x 16 k (64 contiguous bytes per row);
-    // its 16-byte stores fill 32 distinct bank groups
 #pragma unroll
-    for (int i = 0; i < (GT_BM / 8) / (GT_THREADS / 32); ++i) {
+    for (int i = 0; i < QA; ++i) {
       const int r = 8 * (warp + (GT_THREADS / 32) * i) + (lane & 7), j = lane >> 3;
-      const float4 v = a_quad(p, A, m0 + r, k0 + 4 * j);
-      st_split4(a_hi, a_lo, op_offset(r, 4 * j, GT_SBO), v.x, v.y, v.z, v.w);
+      st_split4(a_hi, a_lo, op_offset(r, 4 * j, GT_SBO), ca[i].x, ca[i].y, ca[i].z, ca[i].w);
     }
-    // B'^T chunk: rows n fastest (coalesced along the columns of B)
 #pragma unroll
-    for (int i = 0; i < (GT_BN * GT_BK / 4) / GT_THREADS; ++i) {
+    for (int i = 0; i < QB; ++i) {
       const int idx = tid + i * GT_THREADS;
       const int n = idx & (GT_BN - 1), j = idx >> 7;
-      const float4 v = b_quad(p, B, k0 + 4 * j, n0 + n);
-      st_split4(b_hi, b_lo, op_offset(n, 4 * j, GT_SBO), v.x, v.y, v.z, v.w);
+      st_split4(b_hi, b_lo, op_offset(n, 4 * j, GT_SBO), cb[i].x, cb[i].y, cb[i].z, cb[i].w);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -182,6 +201,10 @@ __global__ void __launch_bounds__(GT_THREADS, 2) gemm_tc_kernel(GemmP p) {
                     (uint32_t)__cvta_generic_to_shared(mbar_p + buf), kc > 0 ? 1u : 0u);
     }
     issued = kc + 1;
+#pragma unroll
+    for (int i = 0; i < QA; ++i) ca[i] = na[i], na[i] = fa[i];
+#pragma unroll
+    for (int i = 0; i < QB; ++i) cb[i] = nb[i], nb[i] = fb[i];
   }
   // the last commit covers every MMA issued before it
   if (tid == 0 && !s_abort && issued > 0) {
