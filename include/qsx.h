@@ -656,6 +656,16 @@ int qsx_dft_batched(const double* x, int nt, int64_t batch, double t0,
                     double dt, const double* freqs, int nf, double rw_freq,
                     double unit_convert, int sign, double* X, void* stream);
 
+/*
+ * The same transform for signals from FP32 propagation (the FP32 contract,
+ * 1e-4): phases anchored in FP64 every 128 samples, rotated and summed in
+ * FP32 between anchors, slices added in FP64 (relative error of order 1e-6).
+ * Same arguments; nt <= 24576.
+ */
+int qsx_dft_batched_f32(const double* x, int nt, int64_t batch, double t0,
+                        double dt, const double* freqs, int nf, double rw_freq,
+                        double unit_convert, int sign, double* X, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -156,6 +156,8 @@ _PROTOS = {
                                   _c_dbl, _c_vp, _c_i64, _c_i64, _c_dbl, _c_vp, _c_vp]),
     'qsx_dft_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
                                  _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
+    'qsx_dft_batched_f32': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
+                                     _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_fblock_tensor': (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_vp, _c_i64, _c_dbl,
                                    _c_dbl, _c_dbl, _c_int, _c_int, _c_dbl, _c_int,
                                    _c_vp, _c_vp]),
@@ -798,8 +800,10 @@ def rk4(matrix, y0, nsteps, save_every=1, form=0, h=0.0, precision=None,
     return out
 
 
-def dft(x, t0, dt, freqs, rw_freq=0.0, unit_convert=1.0, sign=1):
-    """X[b, k] = dt Σ_n x[b, n] exp(i sign (f_k - rw) uc (t0 + n dt))."""
+def dft(x, t0, dt, freqs, rw_freq=0.0, unit_convert=1.0, sign=1, precision=QSX_FP64):
+    """X[b, k] = dt Σ_n x[b, n] exp(i sign (f_k - rw) uc (t0 + n dt));
+    precision QSX_FP32 rotates and sums in FP32 between FP64 phase anchors
+    (qsx_dft_batched_f32), for signals from FP32 propagation."""
     require_gpu()
     x = _need(x.to(torch.complex128).contiguous(), torch.complex128, 'x')
     squeeze = x.dim() == 1
@@ -809,9 +813,10 @@ def dft(x, t0, dt, freqs, rw_freq=0.0, unit_convert=1.0, sign=1):
                   torch.float64, 'freqs', 1)
     B, nt = x.shape
     X = torch.empty((B, freqs.numel()), dtype=torch.complex128, device=x.device)
-    _check(load().qsx_dft_batched(_p(x), nt, B, t0, dt, _p(freqs), freqs.numel(),
-                                  rw_freq, unit_convert, sign, _p(X), _stream()),
-           'qsx_dft_batched')
+    fn = load().qsx_dft_batched_f32 if (precision == QSX_FP32 and nt <= 24576) \
+        else load().qsx_dft_batched
+    _check(fn(_p(x), nt, B, t0, dt, _p(freqs), freqs.numel(), rw_freq, unit_convert, sign,
+              _p(X), _stream()), 'qsx_dft_batched')
     return X[0] if squeeze else X
 
 

@@ -53,7 +53,85 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The same sum for signals that come from FP32 propagation: the phase is
+// anchored in FP64 at the start of each time slice (one sincos a thread),
+// then rotated and accumulated in FP32 over the slice (at most 128 samples,
+// a relative drift of order 1e-5 at worst), with the slices added in FP64.
+// The signal is read once per CTA and converted to FP32 in shared memory, so
+// the inner loop issues no FP64 work.
+__global__ void __launch_bounds__(256)
+    dft_f32_kernel(const double2* __restrict__ x, int nt, double t0, double dt,
+                   const double* __restrict__ freqs, int nf, double rw, double uc, int sign,
+                   double2* __restrict__ X) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2* sx = reinterpret_cast<float2*>(smraw);   // [nt]
+  __shared__ double2 part[32][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int kl = lane & 7, slice = w * 4 + (lane >> 3);
+  const int64_t b = blockIdx.y;
+  const int k = blockIdx.x * 8 + kl;
+  const double2* xb = x + b * nt;
+  for (int n = threadIdx.x; n < nt; n += blockDim.x) {
+    const double2 v = xb[n];
+    sx[n] = make_float2((float)v.x, (float)v.y);
+  }
+  __syncthreads();
+  const double wk = k < nf ? (double)sign * (freqs[k] - rw) * uc : 0.0;
+  double sd, cd;
+  sincos(wk * dt, &sd, &cd);
+  const float sdf = (float)sd, cdf = (float)cd;
+  const int chunk = (nt + 31) / 32;
+  const int n0 = slice * chunk, n1 = min(nt, n0 + chunk);
+  double2 acc = make_double2(0.0, 0.0);
+  float2 ph = make_float2(1.f, 0.f), a32 = make_float2(0.f, 0.f);
+  for (int n = n0; n < n1; ++n) {
+    if (((n - n0) & 127) == 0) {   // FP64 anchor (at most every 128 samples)
+      acc.x += (double)a32.x;
+      acc.y += (double)a32.y;
+      a32 = make_float2(0.f, 0.f);
+      double s, c;
+      sincos(wk * (t0 + (double)n * dt), &s, &c);
+      ph = make_float2((float)c, (float)s);
+    }
+    const float2 v = sx[n];
+    a32.x = fmaf(v.x, ph.x, fmaf(-v.y, ph.y, a32.x));
+    a32.y = fmaf(v.x, ph.y, fmaf(v.y, ph.x, a32.y));
+    ph = make_float2(ph.x * cdf - ph.y * sdf, ph.x * sdf + ph.y * cdf);
+  }
+  acc.x += (double)a32.x;
+  acc.y += (double)a32.y;
+  part[slice][kl] = acc;
+  __syncthreads();
+  if (threadIdx.x < 8 && k < nf) {
+    double2 t = part[0][kl];
+#pragma unroll
+    for (int i = 1; i < 32; ++i) t = cadd(t, part[i][kl]);
+    X[b * nf + k] = cscale(t, dt);
+  }
+}
+
 }  // namespace qsx
+
+extern "C" int qsx_dft_batched_f32(const double* x, int nt, int64_t batch, double t0, double dt,
+                                   const double* freqs, int nf, double rw_freq,
+                                   double unit_convert, int sign, double* X, void* stream) {
+  QSX_CHECK_ARG(nt >= 1 && nt <= 24576 && nf >= 1 && batch >= 0 && batch <= 65535,
+                "qsx_dft_batched_f32: bad sizes nt=%d nf=%d (nt <= 24576)", nt, nf);
+  QSX_CHECK_ARG(sign == 1 || sign == -1, "qsx_dft_batched_f32: sign must be +1 or -1");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(x && freqs && X, "qsx_dft_batched_f32: null pointer");
+  const size_t smem = (size_t)nt * sizeof(float2);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(qsx::dft_f32_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return qsx::cuda_status(e, "qsx_dft_batched_f32");
+  }
+  dim3 grid((unsigned)((nf + 7) / 8), (unsigned)batch);
+  qsx::dft_f32_kernel<<<grid, 256, smem, (cudaStream_t)stream>>>(
+      (const double2*)x, nt, t0, dt, freqs, nf, rw_freq, unit_convert, sign, (double2*)X);
+  QSX_LAUNCH_CHECK("qsx_dft_batched_f32");
+  return QSX_OK;
+}
 
 extern "C" int qsx_dft_batched(const double* x, int nt, int64_t batch, double t0, double dt,
                                const double* freqs, int nf, double rw_freq,

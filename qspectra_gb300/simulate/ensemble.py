@@ -606,7 +606,7 @@ class RedfieldEnsembleWorkload:
             D_eg = build.propagator(self.idx_eg, self.dt, prec, transpose=True)
             sig = projected_mean(D_eg, self.y_abs, self.proj_neg, len(self.t_abs) - 1)
             X = _native.dft(sig['mean'][:, 0], self.dft_t0, self.dt, self.freqs,
-                            self.model.rw_freq, self.model.unit_convert, 1)
+                            self.model.rw_freq, self.model.unit_convert, 1, prec)
             if events is not None:
                 l1 = torch.cuda.Event(enable_timing=True)
                 l1.record()

@@ -153,6 +153,20 @@ def test_fourier_transform_matches_oracle_fft():
             assert rel_err(X, oX) < 1e-12
 
 
+@pytest.mark.parametrize('nt', [1, 37, 2048, 4095])
+def test_fp32_dft_matches_fp64_dft(nt):
+    """qsx_dft_batched_f32 (FP32 rotation and sums between FP64 phase
+    anchors) against the FP64 transform at the FP32 contract, on the
+    workload's grid shape (1 fs steps, rotating-frame frequencies)."""
+    rng = np.random.RandomState(nt)
+    x = torch.as_tensor(rng.randn(2, nt) + 1j * rng.randn(2, nt)).cuda()
+    f = torch.linspace(11800.0, 13000.0, 1024, dtype=torch.float64, device='cuda')
+    args = (x, -0.5 * (nt - 1), 1.0, f, 12400.0, qg.CM_FS, 1)
+    X64 = _native.dft(*args).cpu().numpy()
+    X32 = _native.dft(*args, precision=_native.QSX_FP32).cpu().numpy()
+    assert rel_err(X32, X64) < 2e-5
+
+
 def test_fourier_transform_analytic():
     """Reference tests/test_simulate_utils.py:8-55 (analytic transforms)."""
     a = (1.0 + 0.3j) / 100
