@@ -266,6 +266,15 @@ int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
                                               const int* states, int nb,
                                               const int* recipe, double h,
                                               int precision, void* D, void* stream);
+
+/*
+ * Rows of complex column-stacked n x n matrices to and from the coordinates
+ * of their Hermitian and anti-Hermitian parts (V = V_h + i V_a): merge 0
+ * splits in complex [batch][rows][m] into out real [batch][2 rows][m] (the
+ * V_h rows, then the V_a rows); merge 1 is the inverse.
+ */
+int qsx_hermitian_rows(const void* in, int n, int64_t rows, int64_t batch, int precision,
+                       int merge, void* out, void* stream);
 int qsx_rk4_block_matrix_real_batched(const void* D, int m, int64_t batch,
                                       int precision, int K, const int* select,
                                       int nselect, void* out, void* stream);

@@ -111,6 +111,8 @@ _PROTOS = {
     'qsx_rk4_block_matrix_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_int,
                                               _c_vp, _c_int, _c_vp, _c_vp]),
     'qsx_hermitian_real_form': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_vp, _c_vp]),
+    'qsx_hermitian_rows': (_c_int, [_c_vp, _c_int, _c_i64, _c_i64, _c_int, _c_int, _c_vp,
+                                    _c_vp]),
     'qsx_rk4_proj_block_build': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_vp, _c_int, _c_vp,
                                           _c_vp]),
     'qsx_rk4_proj_block_workspace_bytes': (ctypes.c_size_t, [_c_int, _c_i64, _c_int, _c_int,
@@ -445,6 +447,32 @@ def redfield_propagator(H, G, M, occ, idx, unit_convert, h, precision=QSX_FP64,
         return None
     _check(st, 'qsx_redfield_propagator_batched')
     return D
+
+
+def hermitian_rows(x, n, merge=False):
+    """Rows of column-stacked n x n matrices to / from the Hermitian
+    coordinates of their Hermitian and anti-Hermitian parts
+    (qsx_hermitian_rows): complex (B, R, n^2) -> real (B, 2R, n^2), or back
+    with ``merge``."""
+    require_gpu()
+    x = x.contiguous()
+    B, rows, m = x.shape
+    if m != n * n:
+        raise ValueError('row length must be n^2')
+    if merge:
+        prec = QSX_FP32 if x.dtype == torch.float32 else QSX_FP64
+        if rows % 2:
+            raise ValueError('merge needs the split layout (2R rows)')
+        rows //= 2
+        out = torch.empty((B, rows, m), dtype=torch.complex64 if prec == QSX_FP32
+                          else torch.complex128, device=x.device)
+    else:
+        prec = QSX_FP32 if x.dtype == torch.complex64 else QSX_FP64
+        out = torch.empty((B, 2 * rows, m), dtype=torch.float32 if prec == QSX_FP32
+                          else torch.float64, device=x.device)
+    _check(load().qsx_hermitian_rows(_p(x), n, rows, B, prec, 1 if merge else 0, _p(out),
+                                     _stream()), 'qsx_hermitian_rows')
+    return out
 
 
 def hermitian_real_form(A, n):

@@ -604,6 +604,52 @@ __device__ __forceinline__ auto hermitian_entry(const C* __restrict__ A, int lda
   return a <= b ? v.x : v.y;
 }
 
+// Rows of complex column-stacked n x n matrices V to and from Hermitian
+// coordinates of their Hermitian and anti-Hermitian parts: V = V_h + i V_a
+// with V_h = (V + V^H) / 2 and V_a = (V - V^H) / 2i, coordinates as above.
+// Split: in complex [batch][rows][m] -> out real [batch][2 rows][m] (the
+// V_h rows, then the V_a rows); merge: the inverse.
+template <typename T>
+__global__ void hermitian_rows_kernel(const void* __restrict__ in, int n, int64_t rows,
+                                      int merge, void* __restrict__ out) {
+  using C = typename cplx<T>::type;
+  const int m = n * n;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * m) return;
+  const int64_t b = blockIdx.y, r = e / m;
+  const int k = (int)(e % m), a = k % n, c = k / n;
+  const int q = c + n * a;   // the transposed entry
+  if (!merge) {
+    const C* v = (const C*)in + (b * rows + r) * m;
+    const C vp = v[k], vq = v[q];
+    T xh, xa;
+    if (a <= c) {
+      xh = (T)0.5 * (vp.x + vq.x);
+      xa = (T)0.5 * (vp.y + vq.y);
+    } else {
+      xh = (T)0.5 * (vq.y - vp.y);
+      xa = (T)0.5 * (vp.x - vq.x);
+    }
+    T* o = (T*)out + (b * 2 * rows + r) * m;
+    o[k] = xh;
+    o[rows * m + k] = xa;
+  } else {
+    const T* xh = (const T*)in + (b * 2 * rows + r) * m;
+    const T* xa = xh + rows * m;
+    // V_h[a][c] and V_a[a][c] from their coordinates
+    T hr, hi, ar, ai;
+    if (a == c) {
+      hr = xh[k]; hi = (T)0; ar = xa[k]; ai = (T)0;
+    } else if (a < c) {
+      hr = xh[k]; hi = xh[q]; ar = xa[k]; ai = xa[q];
+    } else {
+      hr = xh[q]; hi = -xh[k]; ar = xa[q]; ai = -xa[k];
+    }
+    C* o = (C*)out + (b * rows + r) * m;
+    o[k] = cmk(hr - ai, hi + ar);
+  }
+}
+
 // D = P - I for one RK4 step, P = sum_{k<=4} A^k / k!, A = h L, evaluated
 // Paterson-Stockmeyer style with two products:
 //   A2 = A A,   D = A + A2 / 2 + A2 (A / 6 + A2 / 24).
@@ -1580,6 +1626,25 @@ int qsx_rk4_propagator_batched(const double* L, int m, int64_t batch, double h,
                                                                  (double2*)D);
   }
   QSX_LAUNCH_CHECK("qsx_rk4_propagator_batched");
+  return QSX_OK;
+}
+
+int qsx_hermitian_rows(const void* in, int n, int64_t rows, int64_t batch, int precision,
+                       int merge, void* out, void* stream) {
+  QSX_CHECK_ARG(n >= 1 && n <= 64 && rows >= 0 && batch >= 0 && batch <= 65535 &&
+                    (merge == 0 || merge == 1) &&
+                    (precision == QSX_FP32 || precision == QSX_FP64),
+                "qsx_hermitian_rows: bad arguments (n=%d)", n);
+  if (batch == 0 || rows == 0) return QSX_OK;
+  QSX_CHECK_ARG(in && out && in != out, "qsx_hermitian_rows: null or aliased pointer");
+  const int64_t total = rows * n * n;
+  const dim3 grid((unsigned)((total + 255) / 256), (unsigned)batch);
+  if (precision == QSX_FP32)
+    hermitian_rows_kernel<float><<<grid, 256, 0, (cudaStream_t)stream>>>(in, n, rows, merge, out);
+  else
+    hermitian_rows_kernel<double><<<grid, 256, 0, (cudaStream_t)stream>>>(in, n, rows, merge,
+                                                                         out);
+  QSX_LAUNCH_CHECK("qsx_hermitian_rows");
   return QSX_OK;
 }
 

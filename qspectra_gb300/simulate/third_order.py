@@ -333,8 +333,12 @@ class ThirdOrderEngine:
         base = int(np.gcd.reduce([k for k in gaps if k] or [1]))
         Xg = None
         if Wt is not None and any(gaps):
+            # the ee block maps Hermitian matrices to Hermitian matrices (real
+            # symmetric site-basis Hamiltonian), so its powers run in the real
+            # form (Hermitian coordinates): real products, a quarter of the
+            # complex multiply-adds
             Lee = build.block(self._idx('ee'))
-            A = (dt * Lee).to(cdt)
+            A = _native.hermitian_real_form((dt * Lee).to(cdt), N)
             del Lee
             A2 = _native.gemm(A, A)
             # D = A + A^2 / 2 + A^2 (A / 6 + A^2 / 24), one step of RK4
@@ -361,10 +365,14 @@ class ThirdOrderEngine:
                                  for a, b in left], 1).to(cdt)             # (S, L, T1, N^2)
                 r = r.view(S, nL * T1, N * N)
                 Wv = Wt.view(S * nL, N * N, T3)
+                # the t1 states as coordinates of their Hermitian and
+                # anti-Hermitian parts, propagated by the real powers
+                x = _native.hermitian_rows(r, N)                      # (S, 2 L T1, N^2)
                 for j, k in enumerate(gaps):
                     for _ in range(k // base):
-                        r = _native.gemm(r, Xg, Cin=r)          # r (I + X_g)
-                    part = _native.gemm(r.view(S * nL, T1, N * N), Wv)
+                        x = _native.gemm(x, Xg, Cin=x)          # x (I + X_g)
+                    rk = _native.hermitian_rows(x, N, merge=True)
+                    part = _native.gemm(rk.view(S * nL, T1, N * N), Wv)
                     total[:, j, :] += part.to(torch.complex128).sum(0)
             if gc:
                 for (a, b), g in zip(left, gc):

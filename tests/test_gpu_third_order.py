@@ -153,3 +153,30 @@ def test_eigh_large_two_exciton_block():
     assert np.max(np.abs(E[0].cpu().numpy() - ref)) < 1e-11
     U = U[0].cpu().numpy()
     assert np.max(np.abs(U @ np.diag(E[0].cpu().numpy()) @ U.T - Hf)) < 1e-10
+
+
+@pytest.mark.parametrize('dtype,tol', [(torch.complex128, 1e-13), (torch.complex64, 1e-5)])
+def test_hermitian_rows_round_trip_and_real_form_action(dtype, tol):
+    """qsx_hermitian_rows splits rows into the coordinates of their Hermitian
+    and anti-Hermitian parts and merges them back; on those coordinates the
+    real form of a Hermiticity-preserving map acts as the map itself."""
+    from qspectra_gb300 import _native
+    rng = np.random.RandomState(5)
+    n, S, R = 5, 3, 7
+    v = rng.randn(S, R, n * n) + 1j * rng.randn(S, R, n * n)
+    x = torch.as_tensor(v).to(dtype).cuda()
+    back = _native.hermitian_rows(_native.hermitian_rows(x, n), n, merge=True)
+    assert rel_err(back.cpu().numpy(), x.cpu().numpy()) < tol
+    # a Hermiticity-preserving map: X -> K X K^H + X B with K complex,
+    # B Hermitian, as a matrix on column-stacked vectors
+    K = rng.randn(n, n) + 1j * rng.randn(n, n)
+    Bh = rng.randn(n, n) + 1j * rng.randn(n, n)
+    Bh = Bh + Bh.conj().T
+    I = np.eye(n)
+    A = np.kron(K.conj(), K) + np.kron(Bh.T, I) + np.kron(I, Bh)
+    At = torch.as_tensor(np.broadcast_to(A, (S,) + A.shape).copy()).to(dtype).cuda()
+    Ar = _native.hermitian_real_form(At, n)
+    ref = np.einsum('kl,srl->srk', A, v)
+    y = torch.einsum('skl,srl->srk', Ar, _native.hermitian_rows(x, n))
+    got = _native.hermitian_rows(y.contiguous(), n, merge=True).cpu().numpy()
+    assert rel_err(got, ref) < 10 * tol
