@@ -291,10 +291,12 @@ def heom_ring8(torch, qg, native, samples=64, nsteps=1999):
         res[name] = r['mean']
         out[name + '_ms'] = ms * (nsteps / steps)
         out[name + '_steps_timed'] = steps
-    # both forms forced, FP32 over 200 steps, scaled: the per-stage kernels
-    # (one launch per RK4 stage, a warp per node block) and the persistent
-    # cluster kernel (one cluster of CTAs per sample for the whole loop)
-    for key, variant in (('fp32_per_stage_kernels_ms', 1), ('fp32_cluster_kernel_ms', 2)):
+    # the forms forced, FP32 over 200 steps, scaled: the per-stage kernels
+    # (one launch per RK4 stage, a warp per node block), the persistent
+    # cluster kernel (one cluster of CTAs per sample for the whole loop) and
+    # the per-stage kernels with the node commutators on the tensor cores
+    for key, variant in (('fp32_per_stage_kernels_ms', 1), ('fp32_cluster_kernel_ms', 2),
+                         ('fp32_tensor_core_commutators_ms', 3)):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         native.heom_rk4(tb, Hb, Hb, y0, 200, 0.5, qg.CM_FS, batch=samples, save_every=1,
@@ -305,7 +307,8 @@ def heom_ring8(torch, qg, native, samples=64, nsteps=1999):
         out[key] = e0.elapsed_time(e1) * (nsteps / 200)
     out['form'] = ('library choice (fp32_ms, fp64_ms): the persistent cluster kernel when every '
                    "sample's cluster is resident at once, else per-stage kernels with a warp "
-                   'per node block; both forced beside')
+                   'per node block; both forced beside, and the per-stage kernels with '
+                   'the node commutators on the tensor cores (variant 3)')
     k = res['fp64'].shape[0]
     a, b = res['fp32'][:k], res['fp64']
     out['fp32_vs_fp64_rel_err_first_{}_steps'.format(k - 1)] = float(

@@ -433,7 +433,12 @@ typedef struct {
                           one launch for the whole loop, when its shared memory
                           fits and every sample's cluster is resident at once;
                           else one launch per RK4 stage); 1: one launch per RK4
-                          stage; 2: the cluster form whenever it fits */
+                          stage; 2: the cluster form whenever it fits; 3: one
+                          launch per RK4 stage with the node commutators
+                          -i (Hx rho_n - rho_n Hy) of a tile of 64 node blocks
+                          as one 3xTF32 tcgen05 product against
+                          L = I (x) Hx - Hy^T (x) I (FP32 blocks up to 8 x 8;
+                          other cases as 1) */
   int64_t batch;       /* disorder samples */
   int64_t H_stride;    /* 0: Hx, Hy shared; else per sample [batch][n][n] */
   const double* Hx;    /* real [nx][nx], rotating frame */

@@ -890,7 +890,10 @@ def heom_rk4(tables, Hx, Hy, y0, nsteps, h, unit_convert, batch=None, save_every
     """RK4 loop over the HEOM generator for all samples (qsx_heom_rk4).
     variant 0: the library's choice (one persistent cluster launch per call
     when it fits in one wave, else per-stage launches); 1: one launch per RK4
-    stage; 2: the cluster launch whenever its shared memory fits."""
+    stage; 2: the cluster launch whenever its shared memory fits; 3: one
+    launch per RK4 stage with the node commutators on the tensor cores (a
+    tcgen05 3xTF32 product per tile of 64 node blocks; FP32 blocks up to
+    8 x 8, other cases as 1)."""
     require_gpu()
     y0 = _need(y0.to(torch.complex128).contiguous(), torch.complex128, 'y0')
     if batch is None:

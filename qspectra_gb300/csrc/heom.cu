@@ -21,6 +21,7 @@
 #include <algorithm>
 
 #include "qsx_common.cuh"
+#include "qsx_tc.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -593,6 +594,263 @@ __global__ void __launch_bounds__(256, MINB)
   }
 }
 
+// ------------------------- per-stage form, node commutators on the tensor cores
+// FP32, blocks up to 8 x 8.  For a tile of up to 64 node blocks of one sample,
+// the commutators vec(Hx rho - rho Hy) = L vec(rho),
+//   L[(a,b),(c,d)] = Hx[a][c] d_bd - d_ac Hy[d][b]   (vec index a + nx b),
+// are one tcgen05 product: A = the tile's blocks, one row per node and part
+// (row 2k the real part of node k, row 2k + 1 its imaginary part; K = E
+// padded to 8), B^T = L (N = E padded to 16), 3xTF32 (hi/lo TF32 split of
+// both operands; lo is stored raw, the tensor core reads its leading TF32
+// bits), FP32 accumulation in tensor memory.  L depends on the sample only
+// and is rebuilt when a CTA's tile moves to another sample.  The accumulator
+// rows go to shared memory as complex node blocks, and then, one warp per node
+// block as in heom_warp_small_kernel, the lanes add -i uc (commutator),
+// -(shift + W) rho and the coupling terms, and do the RK4 bookkeeping.
+// Persistent CTAs, two per SM, stride over the tiles (measured against 32-node
+// tiles with one tile per CTA: 643 against 720 ms for 64 samples x 1999
+// steps); the completion wait is bounded (a timeout sets QSX_ERR_CUDA in
+// *status and the CTA stops).
+constexpr int HTC_NODES = 64;   // node blocks per tile: A rows 0 .. 2 HTC_NODES - 1
+
+__device__ __forceinline__ void htc_split4(unsigned char* hi, unsigned char* lo, uint32_t off,
+                                           float a, float b, float c, float d) {
+  const float4 h = make_float4(tc::tf32_round(a), tc::tf32_round(b), tc::tf32_round(c),
+                               tc::tf32_round(d));
+  *reinterpret_cast<float4*>(hi + off) = h;
+  *reinterpret_cast<float4*>(lo + off) = make_float4(a - h.x, b - h.y, c - h.z, d - h.w);
+}
+
+// shared-memory bytes: A hi/lo (128 x KP), B^T hi/lo (NP x KP), occupations,
+// then the mbarrier and the tensor-memory address
+__host__ __device__ inline size_t heom_tc_smem_bytes(int E, int n_sites, int nx, int ny) {
+  const size_t kp = (E + 7) & ~7, np = (E + 15) & ~15;
+  const size_t planes = 2 * (size_t)tc::ROWS * kp * 4 + 2 * np * kp * 4;
+  return ((planes + (size_t)n_sites * (nx + ny) * 4 + 15) & ~(size_t)15) + 16;
+}
+
+__global__ void __launch_bounds__(256, 2)
+    heom_tc_stage_kernel(HeomWP p, int stage, const float2* __restrict__ in, float2* yh,
+                         float2* __restrict__ yl, float2* __restrict__ acc,
+                         float2* __restrict__ next, int* status) {
+  using namespace tc;
+  using Cx = float2;
+  constexpr int G = 4;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  const int nx = p.nx, ny = p.ny, E = p.E, N = p.n_sites, nnodes = p.nnodes, nt = p.nterms;
+  const int kp = (E + 7) & ~7, np = (E + 15) & ~15, kq = kp / 4;
+  const uint32_t sbo = (uint32_t)kp * 32u;
+  const uint32_t PA = ROWS * kp * 4, PB = np * kp * 4;
+  unsigned char* a_hi = smraw;
+  unsigned char* a_lo = a_hi + PA;
+  unsigned char* b_hi = a_lo + PA;
+  unsigned char* b_lo = b_hi + PB;
+  Cx* S = reinterpret_cast<Cx*>(a_hi);   // [HTC_NODES][E] commutators, once the MMA is done
+  float* sox = reinterpret_cast<float*>(b_lo + PB);
+  float* soy = sox + N * nx;
+  const size_t off_mbar = ((size_t)(2 * PA + 2 * PB) + (size_t)N * (nx + ny) * 4 + 15) & ~(size_t)15;
+  uint64_t* mbar_p = reinterpret_cast<uint64_t*>(smraw + off_mbar);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar_p + 1);
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t mbar = (uint32_t)__cvta_generic_to_shared(mbar_p);
+
+  for (int i = tid; i < N * nx; i += blockDim.x) sox[i] = ((const float*)p.occx)[i];
+  for (int i = tid; i < N * ny; i += blockDim.x) soy[i] = ((const float*)p.occy)[i];
+  for (uint32_t i = tid; i < 2 * PA / 16; i += blockDim.x)
+    reinterpret_cast<uint4*>(a_hi)[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) {
+    s_abort = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint64_t da_hi = smem_desc((uint32_t)__cvta_generic_to_shared(a_hi), sbo);
+  const uint64_t da_lo = smem_desc((uint32_t)__cvta_generic_to_shared(a_lo), sbo);
+  const uint64_t db_hi = smem_desc((uint32_t)__cvta_generic_to_shared(b_hi), sbo);
+  const uint64_t db_lo = smem_desc((uint32_t)__cvta_generic_to_shared(b_lo), sbo);
+  const uint32_t idesc = make_idesc(np);
+  const int lg = warp & 3, c0 = 32 * (warp >> 2);
+  const uint32_t taddr = tmem + ((uint32_t)(32 * lg) << 16) + (uint32_t)c0;
+
+  // this lane's two elements of a node block
+  int ea[2], eb[2];
+  bool ev[2];
+  float w[2], wr[2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int e = lane + 32 * u;
+    ev[u] = e < E;
+    const int ec = ev[u] ? e : 0;
+    ea[u] = ec % nx;
+    eb[u] = ec / nx;
+    w[u] = p.W ? __ldg((const float*)p.W + ec) : 0.f;
+    wr[u] = p.Wraw ? __ldg((const float*)p.Wraw + ec) : 0.f;
+  }
+  const float* shift = (const float*)p.shift;
+  const HTerm<float>* terms = (const HTerm<float>*)p.terms;
+  const float uc = (float)p.uc, h = (float)p.h;
+
+  const int tiles_per = (nnodes + HTC_NODES - 1) / HTC_NODES;
+  const int64_t ntiles = (p.items / nnodes) * tiles_per;
+  int64_t cur_b = -1;
+  uint32_t parity = 0;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t b = t / tiles_per;
+    const int n0 = (int)(t - b * tiles_per) * HTC_NODES;
+    const int nn = min(HTC_NODES, nnodes - n0);
+    const Cx* xb = in + b * (int64_t)nnodes * E;   // the sample's stage input
+    __syncthreads();   // the previous tile's warps are done with the staging
+    // A: node k's real part in row 2k, imaginary part in row 2k + 1
+    for (int g = tid; g < HTC_NODES * kq; g += blockDim.x) {
+      const int k = g / kq, e0 = 4 * (g - k * kq);
+      float re[4], im[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int e = e0 + q;
+        const Cx v = (k < nn && e < E) ? xb[(int64_t)(n0 + k) * E + e] : make_float2(0.f, 0.f);
+        re[q] = v.x;
+        im[q] = v.y;
+      }
+      htc_split4(a_hi, a_lo, op_offset(2 * k, e0, sbo), re[0], re[1], re[2], re[3]);
+      htc_split4(a_hi, a_lo, op_offset(2 * k + 1, e0, sbo), im[0], im[1], im[2], im[3]);
+    }
+    if (b != cur_b) {
+      // B^T = L of sample b: row n = output element, column k = input element
+      cur_b = b;
+      const float* Hx = (const float*)p.Hx + b * p.Hx_stride;
+      const float* Hy = (const float*)p.Hy + b * p.Hy_stride;
+      for (int g = tid; g < np * kq; g += blockDim.x) {
+        const int n = g / kq, k0 = 4 * (g - n * kq);
+        float v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int k = k0 + q;
+          float x = 0.f;
+          if (n < E && k < E) {
+            const int a = n % nx, bb = n / nx, c = k % nx, d = k / nx;
+            if (bb == d) x = __ldg(Hx + a * nx + c);
+            if (a == c) x -= __ldg(Hy + d * ny + bb);
+          }
+          v[q] = x;
+        }
+        htc_split4(b_hi, b_lo, op_offset(n, k0, sbo), v[0], v[1], v[2], v[3]);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      issue_product(tmem, da_hi, da_lo, db_hi, db_lo, kp / 8, idesc, mbar);
+      if (!wait_parity(mbar, parity)) {
+        if (status) atomicOr(status, QSX_ERR_CUDA);
+        s_abort = 1;
+      }
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (s_abort) break;
+    parity ^= 1;
+    {
+      // accumulator lane 2k + part, columns c0 .. c0 + 31 -> S[k][e].part
+      float v[32];
+      tmem_load(taddr, v);
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      const int L = 32 * lg + lane, k = L >> 1, part = L & 1;
+      if (k < nn) {
+        float* sk = reinterpret_cast<float*>(S + k * E) + part;
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+          if (c0 + c < E) sk[2 * (c0 + c)] = v[c];
+      }
+    }
+    __syncthreads();
+    // one warp per node block: the rest of the generator and the RK4 step
+    for (int k = warp; k < nn; k += blockDim.x >> 5) {
+      const int n = n0 + k;
+      const int64_t base = (b * (int64_t)nnodes + n) * E;
+      const HTerm<float>* tr = terms + (int64_t)n * nt;
+      int gm[G], gj[G];
+      Cx gal[G], gbe[G], gga[G], gv[G][2];
+      auto load_group = [&](int t0) {
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+          gm[q] = -1;
+          gj[q] = 0;
+          if (t0 + q < nt) load_term<float>(tr + t0 + q, gm[q], gj[q], gal[q], gbe[q], gga[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+          const Cx* xm = xb + (int64_t)(gm[q] < 0 ? 0 : gm[q]) * E + lane;
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            gv[q][u] = make_float2(0.f, 0.f);
+            if (gm[q] >= 0 && ev[u]) gv[q][u] = xm[32 * u];
+          }
+        }
+      };
+      float orr[2], oi[2];
+      auto use_group = [&]() {
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+          if (gm[q] < 0) continue;
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const float oa = sox[gj[q] * nx + ea[u]], ob = soy[gj[q] * ny + eb[u]];
+            float fr = gal[q].x * oa + gbe[q].x * ob, fi = gal[q].y * oa + gbe[q].y * ob;
+            if (p.has_gamma) {
+              const float gw = wr[u] * (oa - ob);
+              fr = fmaf(gga[q].x, gw, fr);
+              fi = fmaf(gga[q].y, gw, fi);
+            }
+            orr[u] = fmaf(fr, gv[q][u].x, fmaf(-fi, gv[q][u].y, orr[u]));
+            oi[u] = fmaf(fr, gv[q][u].y, fmaf(fi, gv[q][u].x, oi[u]));
+          }
+        }
+      };
+      load_group(0);
+      const float sh = __ldg(shift + n);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        orr[u] = oi[u] = 0.f;
+        if (ev[u]) {
+          const int e = lane + 32 * u;
+          const Cx self = xb[(int64_t)n * E + e];
+          const Cx cm = S[k * E + e];   // (Hx rho - rho Hy)[e]
+          const float d = sh + w[u];
+          orr[u] = fmaf(-d, self.x, cm.y);
+          oi[u] = fmaf(-d, self.y, -cm.x);
+        }
+      }
+      use_group();
+      for (int t0 = G; t0 < nt; t0 += G) {
+        load_group(t0);
+        use_group();
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+        if (ev[u])
+          heom_rk4_update<float>(stage, base + lane + 32 * u, make_float2(uc * orr[u], uc * oi[u]),
+                                 h, yh, yl, acc, next);
+    }
+  }
+  if (s_abort && tid == 0) wait_parity(mbar, parity);   // let an unfinished product drain
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+}
+
 // ------------------------------------------------ persistent cluster form
 // The whole RK4 loop in one launch: one thread-block cluster per disorder
 // sample, the hierarchy nodes split into contiguous ranges over its C CTAs.
@@ -884,7 +1142,7 @@ static int heom_validate(const qsx_heom_args* a) {
   QSX_CHECK_ARG(a->nx >= 1 && a->ny >= 1 && a->nx <= 32 && a->ny <= 32 && a->nx * a->ny <= 256,
                 "qsx_heom: need nx, ny <= 32 and nx * ny <= 256");
   QSX_CHECK_ARG(a->nnodes >= 1 && a->nterms >= 0 && a->n_sites >= 1, "qsx_heom: bad sizes");
-  QSX_CHECK_ARG(a->variant >= 0 && a->variant <= 2, "qsx_heom: variant must be 0, 1 or 2");
+  QSX_CHECK_ARG(a->variant >= 0 && a->variant <= 3, "qsx_heom: variant must be 0, 1, 2 or 3");
   QSX_CHECK_ARG(a->batch >= 0 && a->batch <= 65535, "qsx_heom: batch must be in [0, 65535]");
   QSX_CHECK_ARG(a->nsteps >= 0 && a->save_every >= 1 && a->nsteps % a->save_every == 0,
                 "qsx_heom: nsteps must be a non-negative multiple of save_every");
@@ -1127,7 +1385,7 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
   auto run = [&](auto tag) -> int {
     using T = decltype(tag);
     using C = typename cplx<T>::type;
-    if (a->variant != 1) {
+    if (a->variant == 0 || a->variant == 2) {
       // the whole loop in one launch, one cluster per sample
       double2* saves = (double2*)(((size_t)ws + 255) & ~(size_t)255);
       double2* dst = node0 ? node0 : saves;
@@ -1237,6 +1495,23 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
     w.per_warp = (int)((w.items + resident - 1) / resident);
     const int64_t warps = (w.items + w.per_warp - 1) / w.per_warp;
     const unsigned wgrid = (unsigned)((warps + wthreads / 32 - 1) / (wthreads / 32));
+    // variant 3: FP32 blocks up to 8 x 8 with the node commutators on the
+    // tensor cores (heom_tc_stage_kernel); other shapes take the kernels above
+    bool tc_stage = false;
+    size_t tsmem = 0;
+    unsigned tgrid = 0;
+    if constexpr (sizeof(T) == 4) {
+      if (a->variant == 3 && small) {
+        tc_stage = true;
+        tsmem = heom_tc_smem_bytes(p.E, p.n_sites, p.nx, p.ny);
+        cudaError_t te = cudaFuncSetAttribute(heom_tc_stage_kernel,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)tsmem);
+        if (te != cudaSuccess) return cuda_status(te, "qsx_heom_rk4");
+        const int64_t tiles = p.batch * ((p.nnodes + HTC_NODES - 1) / HTC_NODES);
+        tgrid = (unsigned)std::min<int64_t>(tiles, 2 * (int64_t)sms);
+      }
+    }
     heom_init_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
         (const double2*)a->y0, a->y0_stride ? per : 0, per, p.batch, yh, yl);
     QSX_LAUNCH_CHECK("qsx_heom_rk4 init");
@@ -1244,6 +1519,20 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
     heom_save_kernel<T><<<sg, 256, 0, s>>>(yh, yl, p.nnodes, p.E, keep, p.batch, 0, p.nsave,
                                           node0, a->status);
     for (int step = 1; step <= p.nsteps; ++step) {
+      if constexpr (sizeof(T) == 4) {
+        if (tc_stage) {
+          heom_tc_stage_kernel<<<tgrid, 256, tsmem, s>>>(w, 0, yh, yh, yl, acc, s0, a->status);
+          heom_tc_stage_kernel<<<tgrid, 256, tsmem, s>>>(w, 1, s0, yh, yl, acc, s1, a->status);
+          heom_tc_stage_kernel<<<tgrid, 256, tsmem, s>>>(w, 2, s1, yh, yl, acc, s0, a->status);
+          heom_tc_stage_kernel<<<tgrid, 256, tsmem, s>>>(w, 3, s0, yh, yl, acc, nullptr,
+                                                         a->status);
+          if (step % p.save_every == 0)
+            heom_save_kernel<T><<<sg, 256, 0, s>>>(yh, yl, p.nnodes, p.E, keep, p.batch,
+                                                  step / p.save_every, p.nsave, node0,
+                                                  a->status);
+          continue;
+        }
+      }
       kern<<<wgrid, wthreads, wsmem, s>>>(w, 0, yh, yh, yl, acc, s0);
       kern<<<wgrid, wthreads, wsmem, s>>>(w, 1, s0, yh, yl, acc, s1);
       kern<<<wgrid, wthreads, wsmem, s>>>(w, 2, s1, yh, yl, acc, s0);

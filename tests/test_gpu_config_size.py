@@ -124,11 +124,13 @@ def test_benchmarked_workload_host_entry_matches_oracle_slice(fmo7, fmo7_slice_o
 
 
 # --------------------------------------------------------------- HEOM ring 8
-@pytest.mark.parametrize('variant', [0, 1, 2])
+@pytest.mark.parametrize('variant', [0, 1, 2, 3])
 @pytest.mark.parametrize('precision,tol', TOLS)
 def test_heom_ring8_config_size_matches_reference(drivers, precision, tol, variant):
     """variant 0: the library's choice (the persistent cluster kernel for
-    one sample); 1: the per-stage kernels; 2: the cluster kernel forced."""
+    one sample); 1: the per-stage kernels; 2: the cluster kernel forced; 3:
+    the per-stage kernels with the node commutators on the tensor cores
+    (FP32; FP64 takes variant 1)."""
     H = drivers['ring8_H']
     ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 300, 35, 106),
                                    disorder=wl.fwhm_for_sd(50.0), random_seed=7)

@@ -80,7 +80,8 @@ def test_heom_fp32_split_word_and_batch():
 def test_heom_cluster_form_matches_per_stage_form(golden, tag, kw, heis, precision, tol):
     """The persistent cluster kernel (whole loop in one launch, node ranges
     over the cluster's CTAs, neighbours through distributed shared memory)
-    against the per-stage kernels, on every generator case, both pictures,
+    and the per-stage kernels with the node commutators on the tensor cores
+    (variant 3, FP32) against the per-stage kernels, on every generator case, both pictures,
     with per-sample Hamiltonians and all nodes saved."""
     m = model2(golden, **kw)
     tb = m.tables('ee', transpose=heis)
@@ -91,12 +92,13 @@ def test_heom_cluster_form_matches_per_stage_form(golden, tag, kw, heis, precisi
     E = tb.nx * tb.ny
     y0 = torch.as_tensor(rng.randn(S, m.ado_count * E) + 1j * rng.randn(S, m.ado_count * E)).cuda()
     out = []
-    for variant in (0, 1, 2):
+    for variant in (0, 1, 2, 3):
         out.append(_native.heom_rk4(tb, Hb, Hb, y0, 60, 0.5, qg.CM_FS, batch=S, save_every=6,
                                     save_nodes=m.ado_count, precision=precision,
                                     variant=variant)['state'].cpu().numpy())
     assert rel_err(out[0], out[1]) < tol
     assert rel_err(out[2], out[1]) < tol
+    assert rel_err(out[3], out[1]) < tol   # node commutators on the tensor cores (FP32)
 
 
 def _drivers():
@@ -155,7 +157,7 @@ def test_heom_aki_temp_corr_matches_reference(tag, low, precision, tol):
     oref = orc.rk4_integrate_sparse(ref, x, 60, 0.5)
     tb = m.tables('ee')
     Hx, Hy = m.block_hamiltonians('ee')
-    for variant in (0, 1, 2):
+    for variant in (0, 1, 2, 3):
         out = _native.heom_rk4(tb, Hx, Hy, torch.as_tensor(x).cuda(), 60, 0.5, qg.CM_FS,
                                batch=1, save_nodes=m.ado_count, precision=precision,
                                variant=variant)['state'][0].cpu().numpy()
