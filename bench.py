@@ -296,7 +296,8 @@ def heom_ring8(torch, qg, native, samples=64, nsteps=1999):
     # cluster kernel (one cluster of CTAs per sample for the whole loop) and
     # the per-stage kernels with the node commutators on the tensor cores
     for key, variant in (('fp32_per_stage_kernels_ms', 1), ('fp32_cluster_kernel_ms', 2),
-                         ('fp32_tensor_core_commutators_ms', 3)):
+                         ('fp32_tensor_core_commutators_ms', 3),
+                         ('fp32_per_stage_all_terms_ms', 4)):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         native.heom_rk4(tb, Hb, Hb, y0, 200, 0.5, qg.CM_FS, batch=samples, save_every=1,

@@ -438,7 +438,10 @@ typedef struct {
                           -i (Hx rho_n - rho_n Hy) of a tile of 64 node blocks
                           as one 3xTF32 tcgen05 product against
                           L = I (x) Hx - Hy^T (x) I (FP32 blocks up to 8 x 8;
-                          other cases as 1) */
+                          other cases as 1); 4: as 1, but with every coupling
+                          term of a node visited by every element (blocks up
+                          to 8 x 8 otherwise visit only the terms of the
+                          sites their row and column couple to) */
   int64_t batch;       /* disorder samples */
   int64_t H_stride;    /* 0: Hx, Hy shared; else per sample [batch][n][n] */
   const double* Hx;    /* real [nx][nx], rotating frame */

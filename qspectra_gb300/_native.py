@@ -893,7 +893,9 @@ def heom_rk4(tables, Hx, Hy, y0, nsteps, h, unit_convert, batch=None, save_every
     stage; 2: the cluster launch whenever its shared memory fits; 3: one
     launch per RK4 stage with the node commutators on the tensor cores (a
     tcgen05 3xTF32 product per tile of 64 node blocks; FP32 blocks up to
-    8 x 8, other cases as 1)."""
+    8 x 8, other cases as 1); 4: as 1 with every coupling term of a node
+    visited by every element (blocks up to 8 x 8 otherwise visit only the
+    terms of their own sites)."""
     require_gpu()
     y0 = _need(y0.to(torch.complex128).contiguous(), torch.complex128, 'y0')
     if batch is None:

@@ -228,6 +228,8 @@ struct HeomWP {
   const void* Wraw;           // or null
   const void* shift;
   const void* terms;          // HTerm<T> [nnodes][nterms]
+  const void* site_terms;     // HTerm<T> [nnodes][n_sites][site_slots], grouped by site, or null
+  int site_slots;             // max(nterms, 2)
   int has_gamma;
   double uc, h;
 };
@@ -594,6 +596,296 @@ __global__ void __launch_bounds__(256, MINB)
   }
 }
 
+// ------------------------------ per-stage form, coupling terms by site
+// The coupling of element (a, b) of node n is
+//   sum_t (alpha_t occx[j_t][a] + beta_t occy[j_t][b]
+//          + gamma_t Wraw[a][b] (occx[j_t][a] - occy[j_t][b])) rho_{nbr_t}[a][b],
+// so only the terms whose site j_t couples to row a or to column b
+// contribute.  With the site number operators of one-exciton states that is
+// one site each: the terms of a node are packed once per call, grouped by
+// site ([node][site][slot] records, at least two slots, padded with nbr = -1;
+// each record's `site` field holds the number of records of its (node,
+// site), since the kernel knows the site), and each
+// lane visits only its own sites' terms instead of every term of the node,
+// with the neighbour loads of both its elements in flight together.  A lane
+// whose row or column couples to more than one site takes the full term
+// loop.
+template <typename T>
+__global__ void heom_pack_site_terms_kernel(const HTerm<T>* __restrict__ terms, int nnodes,
+                                            int nterms, int n_sites, int slots,
+                                            HTerm<T>* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;   // (node, site)
+  if (i >= (int64_t)nnodes * n_sites) return;
+  const int n = (int)(i / n_sites), j = (int)(i - (int64_t)n * n_sites);
+  const HTerm<T>* tr = terms + (int64_t)n * nterms;
+  HTerm<T>* o = out + i * slots;
+  int c = 0;
+  for (int t = 0; t < nterms; ++t)
+    if (tr[t].nbr >= 0 && tr[t].site == j) ++c;
+  int k = 0;
+  for (int t = 0; t < nterms; ++t) {
+    HTerm<T> r = tr[t];
+    if (r.nbr >= 0 && r.site == j) {
+      r.site = c;
+      o[k++] = r;
+    }
+  }
+  for (; k < slots; ++k) {
+    HTerm<T> r = {};
+    r.nbr = -1;
+    r.site = c;
+    o[k] = r;
+  }
+}
+
+template <typename T, int NB, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    heom_warp_site_kernel(HeomWP p, int stage, const typename cplx<T>::type* __restrict__ in,
+                          typename cplx<T>::type* yh, typename cplx<T>::type* __restrict__ yl,
+                          typename cplx<T>::type* __restrict__ acc,
+                          typename cplx<T>::type* __restrict__ next) {
+  using Cx = typename cplx<T>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int nx = NB ? NB : p.nx, ny = NB ? NB : p.ny, E = NB ? NB * NB : p.E;
+  const int nt = p.nterms, N = p.n_sites, nnodes = p.nnodes;
+  Cx* xs = reinterpret_cast<Cx*>(smraw) + (size_t)wib * 64;
+  T* sox = reinterpret_cast<T*>(reinterpret_cast<Cx*>(smraw) + (size_t)(blockDim.x >> 5) * 64);
+  T* soy = sox + N * nx;
+  for (int i = threadIdx.x; i < N * nx; i += blockDim.x) sox[i] = ((const T*)p.occx)[i];
+  for (int i = threadIdx.x; i < N * ny; i += blockDim.x) soy[i] = ((const T*)p.occy)[i];
+  __syncthreads();
+  const int64_t warp = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+  const int64_t i0 = warp * p.per_warp;
+  const int64_t i1 = min(p.items, i0 + p.per_warp);
+  if (i0 >= i1) return;
+  const T* shift = (const T*)p.shift;
+  const HTerm<T>* terms = (const HTerm<T>*)p.terms;
+  const HTerm<T>* sterms = (const HTerm<T>*)p.site_terms;
+  const int slots = p.site_slots;
+  const T uc = (T)p.uc, h = (T)p.h;
+  int ea[2], eb[2];
+  bool ev[2];
+  T w[2], wr[2];
+  // the site of row a and, when it differs, the site of column b for each of
+  // this lane's elements; `full` when a row or column couples to more than
+  // one site (those lanes take every term)
+  int js[2][2];
+  bool full[2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int e = lane + 32 * u;
+    ev[u] = e < E;
+    const int ec = ev[u] ? e : 0;
+    ea[u] = ec % nx;
+    eb[u] = ec / nx;
+    w[u] = p.W ? __ldg((const T*)p.W + ec) : (T)0;
+    wr[u] = p.Wraw ? __ldg((const T*)p.Wraw + ec) : (T)0;
+    int na = 0, nb = 0, ja = -1, jb = -1;
+    for (int j = 0; j < N; ++j) {
+      if (sox[j * nx + ea[u]] != (T)0) {
+        ja = j;
+        ++na;
+      }
+      if (soy[j * ny + eb[u]] != (T)0) {
+        jb = j;
+        ++nb;
+      }
+    }
+    full[u] = na > 1 || nb > 1;
+    js[u][0] = ja;
+    js[u][1] = jb != ja ? jb : -1;
+  }
+  const bool any_full = __any_sync(0xffffffffu, full[0] || full[1]);
+  int64_t b = i0 / nnodes;
+  int n = (int)(i0 - b * nnodes);
+  T hx[2][8], hy[2][8];
+  const Cx* xb = nullptr;
+  bool fresh = true;
+  for (int64_t it = i0; it < i1; ++it) {
+    if (fresh) {
+      fresh = false;
+      xb = in + b * (int64_t)nnodes * E;
+      const T* Hx = (const T*)p.Hx + b * p.Hx_stride;
+      const T* Hy = (const T*)p.Hy + b * p.Hy_stride;
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          hx[u][c] = c < nx ? __ldg(Hx + ea[NB == 8 ? 0 : u] * nx + c) : (T)0;
+          hy[u][c] = c < ny ? __ldg(Hy + c * ny + eb[u]) : (T)0;
+        }
+    }
+    const int64_t base = it * E;
+    const Cx* xn = xb + n * E + lane;
+    Cx self[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      self[u] = cmk((T)0, (T)0);
+      if (ev[u]) {
+        self[u] = xn[32 * u];
+        xs[lane + 32 * u] = self[u];
+      }
+    }
+    Cx yv[2], av[2], lv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      yv[u] = av[u] = lv[u] = cmk((T)0, (T)0);
+      if (ev[u]) {
+        yv[u] = yh[base + lane + 32 * u];
+        if (stage > 0) av[u] = acc[base + lane + 32 * u];
+        if constexpr (sizeof(T) == 4) {
+          if (stage == 3) lv[u] = yl[base + lane + 32 * u];
+        }
+      }
+    }
+    // the coupling terms of this lane's sites: the first two terms of each
+    // site (coefficient and neighbour node) for both elements, then every
+    // neighbour load in flight together
+    T orr[2] = {(T)0, (T)0}, oi[2] = {(T)0, (T)0};
+    auto coef = [&](int u, int j, const HTerm<T>& r, T& fr, T& fi) {
+      const T oa = sox[j * nx + ea[u]], ob = soy[j * ny + eb[u]];
+      fr = r.al.x * oa + r.be.x * ob;
+      fi = r.al.y * oa + r.be.y * ob;
+      if (p.has_gamma) {
+        const T gw = wr[u] * (oa - ob);
+        fr = fma(r.ga.x, gw, fr);
+        fi = fma(r.ga.y, gw, fi);
+      }
+    };
+    int cnt[2][2], nbi[2][2][2];
+    T cfr[2][2][2], cfi[2][2][2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const bool on = ev[u] && !full[u] && js[u][q] >= 0;
+        cnt[u][q] = 0;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          nbi[u][q][r] = -1;
+          cfr[u][q][r] = cfi[u][q][r] = (T)0;
+          if (on) {
+            // the first two slots always exist (padding: nbr = -1)
+            HTerm<T> rec;
+            load_term<T>(sterms + ((int64_t)n * N + js[u][q]) * slots + r, rec.nbr, rec.site,
+                         rec.al, rec.be, rec.ga);
+            cnt[u][q] = rec.site;
+            nbi[u][q][r] = rec.nbr;
+            if (rec.nbr >= 0) coef(u, js[u][q], rec, cfr[u][q][r], cfi[u][q][r]);
+          }
+        }
+      }
+    Cx nv[2][2][2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+          nv[u][q][r] = nbi[u][q][r] >= 0 ? xb[(int64_t)nbi[u][q][r] * E + lane + 32 * u]
+                                          : cmk((T)0, (T)0);
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const Cx v = nv[u][q][r];
+          orr[u] = fma(cfr[u][q][r], v.x, fma(-cfi[u][q][r], v.y, orr[u]));
+          oi[u] = fma(cfr[u][q][r], v.y, fma(cfi[u][q][r], v.x, oi[u]));
+        }
+    // sites with more than two terms (several exponents per bath)
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        for (int r = 2; r < cnt[u][q]; ++r) {
+          HTerm<T> rq;
+          load_term<T>(sterms + ((int64_t)n * N + js[u][q]) * slots + r, rq.nbr, rq.site, rq.al,
+                       rq.be, rq.ga);
+          T fr, fi;
+          coef(u, js[u][q], rq, fr, fi);
+          const Cx v = xb[(int64_t)rq.nbr * E + lane + 32 * u];
+          orr[u] = fma(fr, v.x, fma(-fi, v.y, orr[u]));
+          oi[u] = fma(fr, v.y, fma(fi, v.x, oi[u]));
+        }
+    if (any_full) {
+      // lanes whose row or column couples to more than one site: every term
+      const HTerm<T>* tr = terms + (int64_t)n * nt;
+      for (int t = 0; t < nt; ++t) {
+        HTerm<T> rq;
+        load_term<T>(tr + t, rq.nbr, rq.site, rq.al, rq.be, rq.ga);
+        if (rq.nbr < 0) continue;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (!(ev[u] && full[u])) continue;
+          T fr, fi;
+          coef(u, rq.site, rq, fr, fi);
+          const Cx v = xb[(int64_t)rq.nbr * E + lane + 32 * u];
+          orr[u] = fma(fr, v.x, fma(-fi, v.y, orr[u]));
+          oi[u] = fma(fr, v.y, fma(fi, v.x, oi[u]));
+        }
+      }
+    }
+    __syncwarp();
+    const T sh = __ldg(shift + n);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      // -i (Hx x - x Hy)[a][bb] in four independent chains
+      T c0 = 0, s0 = 0, c1 = 0, s1 = 0;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        if (c < nx) {
+          const Cx xv = xs[c + nx * eb[u]];
+          c0 = fma(hx[u][c], xv.x, c0);
+          s0 = fma(hx[u][c], xv.y, s0);
+        }
+        if (c < ny) {
+          const Cx xv = xs[ea[u] + nx * c];
+          c1 = fma(hy[u][c], xv.x, c1);
+          s1 = fma(hy[u][c], xv.y, s1);
+        }
+      }
+      const T d = sh + w[u];
+      orr[u] += fma(-d, self[u].x, s0 - s1);
+      oi[u] += fma(-d, self[u].y, c1 - c0);
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (!ev[u]) continue;
+      const Cx k = cmk(uc * orr[u], uc * oi[u]);
+      const int64_t idx = base + lane + 32 * u;
+      if (stage == 0) {
+        acc[idx] = k;
+        next[idx] = cmk(yv[u].x + (T)0.5 * h * k.x, yv[u].y + (T)0.5 * h * k.y);
+      } else if (stage < 3) {
+        acc[idx] = cmk(av[u].x + (T)2 * k.x, av[u].y + (T)2 * k.y);
+        const T c = stage == 1 ? (T)0.5 * h : h;
+        next[idx] = cmk(yv[u].x + c * k.x, yv[u].y + c * k.y);
+      } else {
+        const T s6 = h / (T)6;
+        const T ix = s6 * (av[u].x + k.x), iy = s6 * (av[u].y + k.y);
+        if constexpr (sizeof(T) == 4) {
+          float hx_ = yv[u].x, lx = lv[u].x, hy_ = yv[u].y, ly = lv[u].y;
+          dd_add(hx_, lx, ix);
+          dd_add(hy_, ly, iy);
+          yh[idx] = cmk(hx_, hy_);
+          yl[idx] = cmk(lx, ly);
+        } else {
+          yh[idx] = cmk(yv[u].x + ix, yv[u].y + iy);
+        }
+      }
+    }
+    if (++n == nnodes) {
+      n = 0;
+      ++b;
+      fresh = true;
+    }
+    __syncwarp();   // the block slice is rewritten by the next node
+  }
+}
+
 // ------------------------- per-stage form, node commutators on the tensor cores
 // FP32, blocks up to 8 x 8.  For a tile of up to 64 node blocks of one sample,
 // the commutators vec(Hx rho - rho Hy) = L vec(rho),
@@ -636,7 +928,7 @@ __global__ void __launch_bounds__(256, 2)
   using namespace tc;
   using Cx = float2;
   constexpr int G = 4;
-  extern __shared__ __align__(128) unsigned char smraw[];
+  extern __shared__ __align__(16) unsigned char smraw[];   // tcgen05 planes: 16-byte aligned
   const int nx = p.nx, ny = p.ny, E = p.E, N = p.n_sites, nnodes = p.nnodes, nt = p.nterms;
   const int kp = (E + 7) & ~7, np = (E + 15) & ~15, kq = kp / 4;
   const uint32_t sbo = (uint32_t)kp * 32u;
@@ -1142,7 +1434,7 @@ static int heom_validate(const qsx_heom_args* a) {
   QSX_CHECK_ARG(a->nx >= 1 && a->ny >= 1 && a->nx <= 32 && a->ny <= 32 && a->nx * a->ny <= 256,
                 "qsx_heom: need nx, ny <= 32 and nx * ny <= 256");
   QSX_CHECK_ARG(a->nnodes >= 1 && a->nterms >= 0 && a->n_sites >= 1, "qsx_heom: bad sizes");
-  QSX_CHECK_ARG(a->variant >= 0 && a->variant <= 3, "qsx_heom: variant must be 0, 1, 2 or 3");
+  QSX_CHECK_ARG(a->variant >= 0 && a->variant <= 4, "qsx_heom: variant must be in 0..4");
   QSX_CHECK_ARG(a->batch >= 0 && a->batch <= 65535, "qsx_heom: batch must be in [0, 65535]");
   QSX_CHECK_ARG(a->nsteps >= 0 && a->save_every >= 1 && a->nsteps % a->save_every == 0,
                 "qsx_heom: nsteps must be a non-negative multiple of save_every");
@@ -1340,7 +1632,11 @@ int qsx_heom_workspace_bytes(const qsx_heom_args* a, size_t* bytes) {
   const size_t tables = a->precision == QSX_FP32 ? heom_table_bytes(a) + 256 : 0;
   const size_t terms = (size_t)a->nnodes * a->nterms *
                        (a->precision == QSX_FP32 ? sizeof(HTerm<float>) : sizeof(HTerm<double>));
-  *bytes = states + saves + 256 + tables + terms + 256;
+  // the terms again, grouped by site, and their counts (per-stage kernels
+  // for blocks up to 8 x 8)
+  const size_t site_terms = (size_t)a->nnodes * a->n_sites * std::max(a->nterms, 2) *
+                            (a->precision == QSX_FP32 ? sizeof(HTerm<float>) : sizeof(HTerm<double>));
+  *bytes = states + saves + 256 + tables + terms + 256 + site_terms + 256;
   return QSX_OK;
 }
 
@@ -1465,10 +1761,25 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
       QSX_LAUNCH_CHECK("qsx_heom_rk4 terms");
     }
     w.terms = terms;
+    w.site_terms = nullptr;
+    w.site_slots = std::max(p.nterms, 2);
     // blocks up to 8 x 8: the specialised kernel; wider ones: EPL elements a lane
     const int epl = p.E <= 32 ? 1 : (p.E <= 64 ? 2 : (p.E <= 128 ? 4 : 8));
     const bool small = p.nx <= 8 && p.ny <= 8;
-    auto kern = small      ? (p.nx == 8 && p.ny == 8 ? heom_warp_small_kernel<T, 8, 4, (sizeof(T) == 4 ? 2 : 1)>
+    // blocks up to 8 x 8: the coupling terms grouped by site (variant 4: the
+    // term loop over every term of the node instead)
+    const bool by_site = small && a->variant != 4 && nrec > 0;
+    if (by_site) {
+      HTerm<T>* sterms = (HTerm<T>*)((((size_t)(terms + nrec)) + 255) & ~(size_t)255);
+      const int64_t ns = (int64_t)p.nnodes * p.n_sites;
+      heom_pack_site_terms_kernel<T><<<(unsigned)((ns + 255) / 256), 256, 0, s>>>(
+          terms, p.nnodes, p.nterms, p.n_sites, w.site_slots, sterms);
+      QSX_LAUNCH_CHECK("qsx_heom_rk4 site terms");
+      w.site_terms = sterms;
+    }
+    auto kern = by_site    ? (p.nx == 8 && p.ny == 8 ? heom_warp_site_kernel<T, 8, (sizeof(T) == 4 ? 2 : 1)>
+                                                     : heom_warp_site_kernel<T, 0, (sizeof(T) == 4 ? 2 : 1)>)
+                : small    ? (p.nx == 8 && p.ny == 8 ? heom_warp_small_kernel<T, 8, 4, (sizeof(T) == 4 ? 2 : 1)>
                                                      : heom_warp_small_kernel<T, 0, 4, (sizeof(T) == 4 ? 2 : 1)>)
                 : epl == 1 ? heom_warp_stage_kernel<T, 1>
                 : epl == 2 ? heom_warp_stage_kernel<T, 2>

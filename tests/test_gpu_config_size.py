@@ -124,13 +124,14 @@ def test_benchmarked_workload_host_entry_matches_oracle_slice(fmo7, fmo7_slice_o
 
 
 # --------------------------------------------------------------- HEOM ring 8
-@pytest.mark.parametrize('variant', [0, 1, 2, 3])
+@pytest.mark.parametrize('variant', [0, 1, 2, 3, 4])
 @pytest.mark.parametrize('precision,tol', TOLS)
 def test_heom_ring8_config_size_matches_reference(drivers, precision, tol, variant):
     """variant 0: the library's choice (the persistent cluster kernel for
     one sample); 1: the per-stage kernels; 2: the cluster kernel forced; 3:
     the per-stage kernels with the node commutators on the tensor cores
-    (FP32; FP64 takes variant 1)."""
+    (FP32; FP64 takes variant 1); 4: the per-stage kernels with every term of
+    a node visited by every element."""
     H = drivers['ring8_H']
     ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 300, 35, 106),
                                    disorder=wl.fwhm_for_sd(50.0), random_seed=7)

@@ -92,13 +92,14 @@ def test_heom_cluster_form_matches_per_stage_form(golden, tag, kw, heis, precisi
     E = tb.nx * tb.ny
     y0 = torch.as_tensor(rng.randn(S, m.ado_count * E) + 1j * rng.randn(S, m.ado_count * E)).cuda()
     out = []
-    for variant in (0, 1, 2, 3):
+    for variant in (0, 1, 2, 3, 4):
         out.append(_native.heom_rk4(tb, Hb, Hb, y0, 60, 0.5, qg.CM_FS, batch=S, save_every=6,
                                     save_nodes=m.ado_count, precision=precision,
                                     variant=variant)['state'].cpu().numpy())
     assert rel_err(out[0], out[1]) < tol
     assert rel_err(out[2], out[1]) < tol
     assert rel_err(out[3], out[1]) < tol   # node commutators on the tensor cores (FP32)
+    assert rel_err(out[4], out[1]) < tol   # per-stage, every term of the node per element
 
 
 def _drivers():
@@ -157,7 +158,7 @@ def test_heom_aki_temp_corr_matches_reference(tag, low, precision, tol):
     oref = orc.rk4_integrate_sparse(ref, x, 60, 0.5)
     tb = m.tables('ee')
     Hx, Hy = m.block_hamiltonians('ee')
-    for variant in (0, 1, 2, 3):
+    for variant in (0, 1, 2, 3, 4):
         out = _native.heom_rk4(tb, Hx, Hy, torch.as_tensor(x).cuda(), 60, 0.5, qg.CM_FS,
                                batch=1, save_nodes=m.ado_count, precision=precision,
                                variant=variant)['state'][0].cpu().numpy()
