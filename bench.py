@@ -66,6 +66,10 @@ def parse_args():
     p.add_argument('--no-third', action='store_true')
     p.add_argument('--no-adjoint', action='store_true')
     p.add_argument('--no-zofe', action='store_true')
+    p.add_argument('--block-k-real', type=int, default=0,
+                   help='pin the real population loop\'s block size K (0: measured per '
+                        'shape, as a user call does; a profiler distorts that measurement, '
+                        'so profiling commands pin the K the plain run reports)')
     p.add_argument('--no-graph', action='store_true',
                    help='time the eager launches only (no CUDA graph capture)')
     p.add_argument('--zofe-samples', type=int, default=152)
@@ -620,7 +624,10 @@ def our_arm(args):
         dist.init_process_group('nccl')
     import qspectra_gb300 as qg
     from qspectra_gb300 import _native
-    from qspectra_gb300.simulate.ensemble import RedfieldEnsembleWorkload, block_k_real_timings
+    from qspectra_gb300.simulate.ensemble import (RedfieldEnsembleWorkload, block_k_real_timings,
+                                                  set_block_k_real)
+    if args.block_k_real:
+        set_block_k_real(args.block_k_real)
 
     H, extra, fwhm = fmo7_inputs()
     S = args.samples
