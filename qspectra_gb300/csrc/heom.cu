@@ -603,9 +603,11 @@ __global__ void __launch_bounds__(256, MINB)
 // so only the terms whose site j_t couples to row a or to column b
 // contribute.  With the site number operators of one-exciton states that is
 // one site each: the terms of a node are packed once per call, grouped by
-// site ([node][site][slot] records, at least two slots, padded with nbr = -1;
+// site ([node][slot][site] records, at least two slots, padded with nbr = -1;
 // each record's `site` field holds the number of records of its (node,
-// site), since the kernel knows the site), and each
+// site), since the kernel knows the site).  A warp copies a node's first two
+// slots of every site (contiguous) into its shared-memory slice with
+// coalesced 16-byte loads, and each
 // lane visits only its own sites' terms instead of every term of the node,
 // with the neighbour loads of both its elements in flight together.  A lane
 // whose row or column couples to more than one site takes the full term
@@ -618,7 +620,7 @@ __global__ void heom_pack_site_terms_kernel(const HTerm<T>* __restrict__ terms, 
   if (i >= (int64_t)nnodes * n_sites) return;
   const int n = (int)(i / n_sites), j = (int)(i - (int64_t)n * n_sites);
   const HTerm<T>* tr = terms + (int64_t)n * nterms;
-  HTerm<T>* o = out + i * slots;
+  HTerm<T>* o = out + (int64_t)n * slots * n_sites + j;   // slot k at o[k * n_sites]
   int c = 0;
   for (int t = 0; t < nterms; ++t)
     if (tr[t].nbr >= 0 && tr[t].site == j) ++c;
@@ -627,14 +629,14 @@ __global__ void heom_pack_site_terms_kernel(const HTerm<T>* __restrict__ terms, 
     HTerm<T> r = tr[t];
     if (r.nbr >= 0 && r.site == j) {
       r.site = c;
-      o[k++] = r;
+      o[(int64_t)(k++) * n_sites] = r;
     }
   }
   for (; k < slots; ++k) {
     HTerm<T> r = {};
     r.nbr = -1;
     r.site = c;
-    o[k] = r;
+    o[(int64_t)k * n_sites] = r;
   }
 }
 
@@ -649,8 +651,14 @@ __global__ void __launch_bounds__(256, MINB)
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int nx = NB ? NB : p.nx, ny = NB ? NB : p.ny, E = NB ? NB * NB : p.E;
   const int nt = p.nterms, N = p.n_sites, nnodes = p.nnodes;
-  Cx* xs = reinterpret_cast<Cx*>(smraw) + (size_t)wib * 64;
-  T* sox = reinterpret_cast<T*>(reinterpret_cast<Cx*>(smraw) + (size_t)(blockDim.x >> 5) * 64);
+  // per warp: its node block (64 complex), then the node's first two
+  // coupling slots of every site (2 N records); then the occupations
+  HTerm<T>* hrec = reinterpret_cast<HTerm<T>*>(smraw) + (size_t)wib * 2 * N;
+  Cx* xs = reinterpret_cast<Cx*>(reinterpret_cast<HTerm<T>*>(smraw) +
+                                 (size_t)(blockDim.x >> 5) * 2 * N) + (size_t)wib * 64;
+  T* sox = reinterpret_cast<T*>(reinterpret_cast<Cx*>(reinterpret_cast<HTerm<T>*>(smraw) +
+                                                      (size_t)(blockDim.x >> 5) * 2 * N) +
+                                (size_t)(blockDim.x >> 5) * 64);
   T* soy = sox + N * nx;
   for (int i = threadIdx.x; i < N * nx; i += blockDim.x) sox[i] = ((const T*)p.occx)[i];
   for (int i = threadIdx.x; i < N * ny; i += blockDim.x) soy[i] = ((const T*)p.occy)[i];
@@ -663,6 +671,7 @@ __global__ void __launch_bounds__(256, MINB)
   const HTerm<T>* terms = (const HTerm<T>*)p.terms;
   const HTerm<T>* sterms = (const HTerm<T>*)p.site_terms;
   const int slots = p.site_slots;
+  const int hchunks = 2 * N * (int)sizeof(HTerm<T>) / 16;   // 16-byte pieces of the head
   const T uc = (T)p.uc, h = (T)p.h;
   int ea[2], eb[2];
   bool ev[2];
@@ -727,6 +736,11 @@ __global__ void __launch_bounds__(256, MINB)
         xs[lane + 32 * u] = self[u];
       }
     }
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(sterms + (int64_t)n * slots * N);
+      uint4* dst = reinterpret_cast<uint4*>(hrec);
+      for (int c = lane; c < hchunks; c += 32) dst[c] = __ldg(src + c);
+    }
     Cx yv[2], av[2], lv[2];
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
@@ -739,6 +753,7 @@ __global__ void __launch_bounds__(256, MINB)
         }
       }
     }
+    __syncwarp();   // the head records are in the slice
     // the coupling terms of this lane's sites: the first two terms of each
     // site (coefficient and neighbour node) for both elements, then every
     // neighbour load in flight together
@@ -767,9 +782,7 @@ __global__ void __launch_bounds__(256, MINB)
           cfr[u][q][r] = cfi[u][q][r] = (T)0;
           if (on) {
             // the first two slots always exist (padding: nbr = -1)
-            HTerm<T> rec;
-            load_term<T>(sterms + ((int64_t)n * N + js[u][q]) * slots + r, rec.nbr, rec.site,
-                         rec.al, rec.be, rec.ga);
+            const HTerm<T> rec = hrec[r * N + js[u][q]];
             cnt[u][q] = rec.site;
             nbi[u][q][r] = rec.nbr;
             if (rec.nbr >= 0) coef(u, js[u][q], rec, cfr[u][q][r], cfi[u][q][r]);
@@ -802,7 +815,7 @@ __global__ void __launch_bounds__(256, MINB)
       for (int q = 0; q < 2; ++q)
         for (int r = 2; r < cnt[u][q]; ++r) {
           HTerm<T> rq;
-          load_term<T>(sterms + ((int64_t)n * N + js[u][q]) * slots + r, rq.nbr, rq.site, rq.al,
+          load_term<T>(sterms + ((int64_t)n * slots + r) * N + js[u][q], rq.nbr, rq.site, rq.al,
                        rq.be, rq.ga);
           T fr, fi;
           coef(u, js[u][q], rq, fr, fi);
@@ -1787,7 +1800,8 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
                            : heom_warp_stage_kernel<T, 8>;
     const int wthreads = 256;
     const size_t wsmem =
-        small ? (size_t)(wthreads / 32) * 64 * sizeof(C) + (size_t)p.n_sites * (p.nx + p.ny) * sizeof(T)
+        small ? (size_t)(wthreads / 32) * 64 * sizeof(C) + (size_t)p.n_sites * (p.nx + p.ny) * sizeof(T) +
+                    (by_site ? (size_t)(wthreads / 32) * 2 * p.n_sites * sizeof(HTerm<T>) : 0)
               : (size_t)(wthreads / 32) * 32 * epl * sizeof(C);
     if (wsmem > 48 * 1024) {
       cudaError_t fe = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
