@@ -175,22 +175,36 @@ def from_hermitian_coordinates(x, n):
     return x[..., re_idx] + 1j * sign * x[..., im_idx]
 
 
+def padded_block_steps(nsteps, K):
+    """Steps the real blocked loop runs for block size K: the smallest
+    multiple of K that covers ``nsteps`` (the outputs past ``nsteps`` are
+    dropped; the ones up to it are the same as for any other K)."""
+    return -(-int(nsteps) // K) * K
+
+
+def _block_k_real_cost(nsteps, m, nselect, K, tensor_core):
+    products = bin(K).count('1') - 1 + K.bit_length() - 1
+    build = nselect * m * m * max(K - 2, 0) + products * m ** 3
+    if tensor_core is not None and tensor_core(K):
+        build *= 0.6
+    nblk = padded_block_steps(nsteps, K) // K
+    return 2.0 * nblk * (m + nselect * (K - 1)) * m + build
+
+
 def pick_block_k_real(nsteps, m, nselect, max_k=64, tensor_core=None):
     """K minimising the executed work of the real blocked loop: per block-step
     (m + nsel (K-1)) m multiply-adds (weighted twice: the loop is the
-    latency-bound part), plus the block build, nsel m^2 (K-2) for the
-    selected rows and m^3 per product of the binary powering.  Where
-    ``tensor_core(K)`` says the tcgen05 build takes K, the build terms weigh
-    0.6 (its measured time against the CUDA-core build at K = 9)."""
+    latency-bound part) over ceil(nsteps / K) block-steps, plus the block
+    build, nsel m^2 (K-2) for the selected rows and m^3 per product of the
+    binary powering.  Where ``tensor_core(K)`` says the tcgen05 build takes
+    K, the build terms weigh 0.6 (its measured time against the CUDA-core
+    build at K = 9).  K need not divide nsteps: the loop runs
+    padded_block_steps(nsteps, K) steps, at most K - 1 more."""
     best, best_cost = 1, None
-    for K in range(2, max_k + 1):
-        if nsteps % K or m + nselect * (K - 1) > 512:
+    for K in range(2, min(max_k, max(int(nsteps), 1)) + 1):
+        if m + nselect * (K - 1) > 512:
             continue
-        products = bin(K).count('1') - 1 + K.bit_length() - 1
-        build = nselect * m * m * max(K - 2, 0) + products * m ** 3
-        if tensor_core is not None and tensor_core(K):
-            build *= 0.6
-        cost = 2.0 * (nsteps // K) * (m + nselect * (K - 1)) * m + build
+        cost = _block_k_real_cost(nsteps, m, nselect, K, tensor_core)
         if best_cost is None or cost < best_cost:
             best, best_cost = K, cost
     return best
@@ -202,7 +216,7 @@ def pick_block_k_real(nsteps, m, nselect, max_k=64, tensor_core=None):
 # fastest is kept for the process.  set_block_k_real(K) pins a value.
 _TUNED_K_REAL = {}
 _PINNED_K_REAL = None
-K_REAL_CANDIDATES = 3
+K_REAL_CANDIDATES = 5
 
 
 def set_block_k_real(K=None):
@@ -214,14 +228,10 @@ def set_block_k_real(K=None):
 def block_k_real_candidates(nsteps, m, nselect, tensor_core=None, count=K_REAL_CANDIDATES):
     """The ``count`` K values the cost model of pick_block_k_real ranks best."""
     ranked = []
-    for K in range(2, 65):
-        if nsteps % K or m + nselect * (K - 1) > 512:
+    for K in range(2, min(64, max(int(nsteps), 1)) + 1):
+        if m + nselect * (K - 1) > 512:
             continue
-        products = bin(K).count('1') - 1 + K.bit_length() - 1
-        build = nselect * m * m * max(K - 2, 0) + products * m ** 3
-        if tensor_core is not None and tensor_core(K):
-            build *= 0.6
-        ranked.append((2.0 * (nsteps // K) * (m + nselect * (K - 1)) * m + build, K))
+        ranked.append((_block_k_real_cost(nsteps, m, nselect, K, tensor_core), K))
     return [K for _, K in sorted(ranked)[:count]]
 
 
@@ -231,8 +241,9 @@ def _real_block_pass(Dr, K, coords, x0, nsteps, use_tc):
         mat, tc_status = tc
     else:
         mat, tc_status = _native.rk4_block_matrix_real(Dr, K, coords), None
-    xm, status = _native.rk4_real_block_mean(mat, x0, nsteps, coords, K, check_finite=False)
-    return mat, tc_status, xm, status
+    xm, status = _native.rk4_real_block_mean(mat, x0, padded_block_steps(nsteps, K), coords, K,
+                                             check_finite=False)
+    return mat, tc_status, xm[:nsteps + 1], status
 
 
 def tuned_block_k_real(Dr, coords, x0, nsteps, use_tc):
@@ -334,7 +345,10 @@ def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None,
         e0 = torch.cuda.Event(enable_timing=True)
         e0.record()
     if K > 1:
-        xm, status = _native.rk4_real_block_mean(mat, x0, nsteps, coords, K, check_finite=False)
+        # the loop runs whole blocks; the outputs past nsteps are dropped
+        xm, status = _native.rk4_real_block_mean(mat, x0, padded_block_steps(nsteps, K), coords,
+                                                 K, check_finite=False)
+        xm = xm[:nsteps + 1]
     else:
         raise NotImplementedError('the real blocked loop needs a block size K > 1')
     if tc_status is not None:
@@ -343,7 +357,8 @@ def propagate_hermitian_mean(build, idx, nb, h, y0, nsteps, select, events=None,
         e1 = torch.cuda.Event(enable_timing=True)
         e1.record()
         events.setdefault('dyn', []).append((e0, e1))
-        events['dyn_flops'] = 2.0 * mat.shape[0] * (nsteps // K) * mat.shape[1] * m
+        events['dyn_flops'] = (2.0 * mat.shape[0] * (padded_block_steps(nsteps, K) // K)
+                               * mat.shape[1] * m)
         events['dyn_block_k'] = K
         events['dyn_variant'] = 'real'
     if np.all(a == b) and np.array_equal(coords, sel):

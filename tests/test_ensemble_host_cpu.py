@@ -18,17 +18,16 @@ def tc_supported(m, K, nsel):
     return b * nsel <= 64
 
 
-def test_block_size_divides_the_steps_and_prefers_cheap_builds():
-    for nsteps in (999, 512, 300, 2047, 1023, 24):
+def test_block_size_covers_the_steps_and_prefers_cheap_builds():
+    for nsteps in (999, 512, 300, 2047, 1023, 24, 997):
         K = ens.pick_block_k_real(nsteps, 49, 7)
         Kt = ens.pick_block_k_real(nsteps, 49, 7,
                                    tensor_core=lambda k: tc_supported(49, k, 7))
         for k in (K, Kt):
-            assert k == 1 or nsteps % k == 0
+            assert 1 < k <= 64
             assert 49 + 7 * (k - 1) <= 512
-    # the fmo7 population run: 999 steps, K = 9 either way (a tensor-core shape)
-    assert ens.pick_block_k_real(999, 49, 7) == 9
-    assert tc_supported(49, 9, 7)
+            run = ens.padded_block_steps(nsteps, k)
+            assert run % k == 0 and nsteps <= run < nsteps + k
     # a cheaper build only makes tensor-core shapes more attractive: when the
     # plain choice is one, so is the weighted choice (possibly a larger K)
     for nsteps in (512, 360, 720, 1000):
@@ -38,8 +37,11 @@ def test_block_size_divides_the_steps_and_prefers_cheap_builds():
             assert tc_supported(49, Kt, 7) and Kt >= K
 
 
-def test_no_block_size_when_no_divisor_fits():
-    assert ens.pick_block_k_real(997, 49, 7) == 1        # prime, above the largest K
+def test_padded_block_steps():
+    assert ens.padded_block_steps(999, 9) == 999
+    assert ens.padded_block_steps(999, 8) == 1000
+    assert ens.padded_block_steps(997, 8) == 1000
+    assert ens.padded_block_steps(8, 8) == 8
 
 
 def test_hermitian_block_detection():
@@ -66,13 +68,16 @@ def test_hermitian_coordinates_round_trip():
 
 
 def test_measured_block_k_candidates():
-    """The candidates the real-path tuner times: divisors of the step count,
-    ranked by the cost model, the model's own choice first."""
-    tc = lambda k: k in (3, 5, 9, 17, 33)   # 2^J + 1 shapes on the tensor cores
+    """The candidates the real-path tuner times, ranked by the cost model, the
+    model's own choice first; block sizes that do not divide the step count
+    run whole blocks past it."""
+    tc = lambda k: k in (3, 5, 8, 9, 17, 33)   # tensor-core shapes
     c = ens.block_k_real_candidates(999, 49, 7, tc)
     assert c[0] == ens.pick_block_k_real(999, 49, 7, tensor_core=tc)
-    assert len(c) == 3 and all(999 % K == 0 for K in c)
-    assert ens.block_k_real_candidates(7, 49, 7) == [7]
+    assert len(c) == ens.K_REAL_CANDIDATES and len(set(c)) == len(c)
+    assert 8 in c and 9 in c     # 1000 = 125 x 8 steps against 999 = 111 x 9
+    small = ens.block_k_real_candidates(7, 49, 7)
+    assert len(small) == ens.K_REAL_CANDIDATES and all(2 <= K <= 7 for K in small)
     ens.set_block_k_real(3)
     try:
         assert ens._PINNED_K_REAL == 3
