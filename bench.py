@@ -612,6 +612,31 @@ def ncu_traffic(path=os.path.join(ROOT, 'profiles', 'rk4_block_f32_fmo7.md')):
     return float(m.group(1)) if m else None
 
 
+def replica_sample_start(rank, samples_per_rank):
+    """First disorder-sample index of a rank's replica: the ranks take
+    disjoint consecutive ranges of the same seeded draws (weak scaling, no
+    data-path collective)."""
+    return rank * samples_per_rank
+
+
+def max_over_ranks(values, world, device):
+    """Element-wise MAX of a list of floats over the ranks (every rank gets
+    it); the values themselves when there is one rank."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def whole_job_rate(world, ms_per_step):
+    """Ensembles per second of the whole job: every rank finishes one
+    ensemble per step, and the step takes the slowest rank's time."""
+    return world * 1000.0 / ms_per_step
+
+
 def our_arm(args):
     import torch
     import torch.distributed as dist
@@ -639,7 +664,8 @@ def our_arm(args):
     psi = np.zeros(7)
     psi[0] = 1.0
     work = RedfieldEnsembleWorkload(model, ABS_TIME, DYN_TIME, psi)
-    off_host = torch.as_tensor(model.hamiltonian.disorder_offsets(S, start=rank * S)).pin_memory()
+    off_host = torch.as_tensor(model.hamiltonian.disorder_offsets(
+        S, start=replica_sample_start(rank, S))).pin_memory()
     off = off_host.cuda()
 
     def barrier():
@@ -703,16 +729,14 @@ def our_arm(args):
                              float((Pg - P32).abs().max() / P32.abs().max()))
     clocks = clocks_stop(clk) if rank == 0 else None
     if world > 1:
-        t = torch.tensor([ms, graph_ms or 0.0], device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t[0].item())
-        graph_ms = float(t[1].item()) if graph_ok else None
+        ms, gmax = max_over_ranks([ms, graph_ms or 0.0], world, 'cuda')
+        graph_ms = gmax if graph_ok else None
     eager_ms = ms
     if graph_ok and graph_vs_eager <= 1e-12:   # the replay must reproduce the step
         ms = graph_ms
     if int(status.item()) & _native.QSX_ERR_NONFINITE:
         raise _native.IntegratorError('non-finite state in the timed run')
-    value = world * 1000.0 / ms
+    value = whole_job_rate(world, ms)
     dyn_ms = statistics.mean(a.elapsed_time(b) for a, b in events['dyn'])
     bb_ms = (statistics.mean(a.elapsed_time(b) for a, b in events['blockbuild'])
              if events.get('blockbuild') else None)
@@ -726,10 +750,7 @@ def our_arm(args):
         Xh, Ph = work.run_host(off_host, 'fp32', build_precision=args.build)
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks([e2e_ms], world, 'cuda')[0]
 
     # plain FP64 form, side by side, and the FP32 error against it
     work.run(off, 'fp64')
@@ -818,7 +839,7 @@ def our_arm(args):
             graph_ms=graph_ms,
             block_k_real=[{'K': v[0], 'ms': v[1]} for v in block_k_real_timings().values()]),
         'fp64_ms_per_step': fp64_ms, 'speedup_fp32_vs_fp64': fp64_ms / ms,
-        'e2e': {'value': world * 1000.0 / e2e_ms, 'unit': UNIT,
+        'e2e': {'value': whole_job_rate(world, e2e_ms), 'unit': UNIT,
                 'h2d_bytes_per_step': int(off_host.numel() * 8),
                 'd2h_bytes_per_step': int((nf + Ph.size + 1) * 8)},
         'roofline': block_roofline(events, bb_flops, bb_ms, peak),
