@@ -163,3 +163,35 @@ def test_heom_aki_temp_corr_matches_reference(tag, low, precision, tol):
                                batch=1, save_nodes=m.ado_count, precision=precision,
                                variant=variant)['state'][0].cpu().numpy()
         assert rel_err(out, oref) < tol
+
+
+@pytest.mark.parametrize('block', ['ff', 'ef', 'ee'])
+@pytest.mark.parametrize('precision,tol', [(_native.QSX_FP64, 1e-10), (_native.QSX_FP32, 1e-4)])
+def test_heom_two_exciton_blocks_every_kernel_form(block, precision, tol):
+    """A 'gef' hierarchy: two-exciton states couple to two sites each, so the
+    site-grouped stage kernel takes its full term loop for those rows and
+    columns.  Every kernel form against the oracle's generator (heom.py:
+    298-443) driven by the fixed-step RK4."""
+    H = wl.chain_hamiltonian(n_sites=3, seed=4)
+    ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 300, 35, 106))
+    m = qg.HEOMModel(ham, hilbert_subspace='gef', unit_convert=qg.CM_FS, K=0, level_cutoff=3,
+                     low_temp_corr=True)
+    om = orc.HEOMSpec(orc.ElectronicHamiltonianSpec(H, rw_freq=m.rw_freq),
+                      orc.DebyeBathSpec(orc.CM_K * 300, 35, 106), 'gef', orc.CM_FS,
+                      level_cutoff=3, K=0, low_temp_corr=True)
+    lsub = block
+    L = om.eom_matrix(lsub)
+    tb = m.tables(lsub)
+    E = tb.nx * tb.ny
+    assert L.shape[0] == m.ado_count * E
+    rng = np.random.RandomState(8)
+    y0 = rng.randn(L.shape[0]) + 1j * rng.randn(L.shape[0])
+    ref = orc.rk4_integrate_sparse(L, y0, 80, 0.5, save_every=8)
+    Hx, Hy = m.block_hamiltonians(lsub)
+    out = []
+    for variant in (1, 3, 4):
+        r = _native.heom_rk4(tb, Hx, Hy, torch.as_tensor(y0).cuda(), 80, 0.5, qg.CM_FS,
+                             batch=1, save_every=8, save_nodes=m.ado_count,
+                             precision=precision, variant=variant)
+        out.append(r['state'][0].cpu().numpy())
+        assert rel_err(out[-1], ref) < tol, variant
