@@ -683,6 +683,25 @@ int qsx_dft_batched_f32(const double* x, int nt, int64_t batch, double t0,
                         double dt, const double* freqs, int nf, double rw_freq,
                         double unit_convert, int sign, double* X, void* stream);
 
+/*
+ * Two-dimensional transform of a third-order signal for the 2D spectrum
+ * (two_dimensional_spectra, qspectra/simulate/response.py:430-455: the t1
+ * transform with sign -1, then the t3 transform, each as
+ * fourier_transform, qspectra/simulate/utils.py:154-219), both axes in one
+ * launch, FP64:
+ *   X[k1][b][k3] = dt1 dt3 sum_{n1, n3} x[n1 s1 + b sb + n3 s3]
+ *                  exp(i sign1 (f1[k1] - rw) uc (t01 + n1 dt1))
+ *                  exp(i sign3 (f3[k3] - rw) uc (t03 + n3 dt3)),
+ * x complex128 with element strides s1, sb, s3 (the engine's (t1, t2, t3)
+ * array: s1 = batch n3, sb = n3, s3 = 1); X complex128 [nf1][batch][nf3].
+ * n1 <= 1600.
+ */
+int qsx_dft2_batched(const double* x, int n1, int64_t batch, int n3, int64_t s1,
+                     int64_t sb, int64_t s3, double t01, double dt1, const double* f1,
+                     int nf1, int sign1, double t03, double dt3, const double* f3,
+                     int nf3, int sign3, double rw_freq, double unit_convert, double* X,
+                     void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -160,6 +160,9 @@ _PROTOS = {
                                  _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
     'qsx_dft_batched_f32': (_c_int, [_c_vp, _c_int, _c_i64, _c_dbl, _c_dbl, _c_vp,
                                      _c_int, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
+    'qsx_dft2_batched': (_c_int, [_c_vp, _c_int, _c_i64, _c_int, _c_i64, _c_i64, _c_i64,
+                                  _c_dbl, _c_dbl, _c_vp, _c_int, _c_int, _c_dbl, _c_dbl, _c_vp,
+                                  _c_int, _c_int, _c_dbl, _c_dbl, _c_vp, _c_vp]),
     'qsx_fblock_tensor': (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_vp, _c_i64, _c_dbl,
                                    _c_dbl, _c_dbl, _c_int, _c_int, _c_dbl, _c_int,
                                    _c_vp, _c_vp]),
@@ -846,6 +849,27 @@ def dft(x, t0, dt, freqs, rw_freq=0.0, unit_convert=1.0, sign=1, precision=QSX_F
     _check(fn(_p(x), nt, B, t0, dt, _p(freqs), freqs.numel(), rw_freq, unit_convert, sign,
               _p(X), _stream()), 'qsx_dft_batched')
     return X[0] if squeeze else X
+
+
+def dft2(x, t01, dt1, f1, sign1, t03, dt3, f3, sign3, rw_freq=0.0, unit_convert=1.0):
+    """Both time axes of a (n1, B, n3) complex signal transformed in one
+    launch (qsx_dft2_batched): X[k1, b, k3] = dt1 dt3 sum x[n1, b, n3]
+    exp(i sign1 (f1 - rw) uc t1) exp(i sign3 (f3 - rw) uc t3)."""
+    require_gpu()
+    x = _need(x.to(torch.complex128), torch.complex128, 'x', 3)
+    n1, B, n3 = x.shape
+    s1, sb, s3 = x.stride()
+    dev = x.device
+    f1 = _need(torch.as_tensor(f1, dtype=torch.float64, device=dev).contiguous(),
+               torch.float64, 'f1', 1)
+    f3 = _need(torch.as_tensor(f3, dtype=torch.float64, device=dev).contiguous(),
+               torch.float64, 'f3', 1)
+    X = torch.empty((f1.numel(), B, f3.numel()), dtype=torch.complex128, device=dev)
+    _check(load().qsx_dft2_batched(_p(x), n1, B, n3, s1, sb, s3, t01, dt1, _p(f1), f1.numel(),
+                                   int(sign1), t03, dt3, _p(f3), f3.numel(), int(sign3),
+                                   rw_freq, unit_convert, _p(X), _stream()),
+           'qsx_dft2_batched')
+    return X
 
 
 def _heom_args(tables, Hx, Hy, unit_convert, batch, precision=QSX_FP64):

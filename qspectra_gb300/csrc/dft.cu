@@ -110,6 +110,72 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Two-dimensional transform of a third-order signal x[n1][b][n3] (t1, t2,
+// t3; any strides) over t1 and t3 in one launch (FP64):
+//   X[k1][b][k3] = dt1 dt3 sum_{n1, n3} x[n1][b][n3]
+//                  exp(i s1 (f1_k1 - rw) uc t1_n1) exp(i s3 (f3_k3 - rw) uc t3_n3),
+// t_n = t0 + n dt on each axis.  CTA (chunk of 8 t3 frequencies, b): first the
+// t3 transform of every t1 row for those frequencies, into shared memory
+// (Y[n1][8]); then the t1 transform of Y for every t1 frequency.  Each sum
+// advances its twiddle by complex rotation, re-seeded from sincos every 32
+// samples, as dft_kernel does.
+constexpr int DFT2_F3 = 8;
+
+__global__ void __launch_bounds__(256)
+    dft2_kernel(const double2* __restrict__ x, int n1, int n3, int64_t s1, int64_t sb,
+                int64_t s3, double t01, double dt1, const double* __restrict__ f1, int nf1,
+                int sign1, double t03, double dt3, const double* __restrict__ f3, int nf3,
+                int sign3, double rw, double uc, double2* __restrict__ X) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  double2* Y = reinterpret_cast<double2*>(smraw);   // [n1][DFT2_F3]
+  const int k3base = blockIdx.x * DFT2_F3;
+  const int64_t b = blockIdx.y;
+  const int64_t nb = gridDim.y;
+  const double2* xb = x + b * sb;
+  // t3 transform: one (n1, k3) sum a thread
+  for (int o = threadIdx.x; o < n1 * DFT2_F3; o += blockDim.x) {
+    const int r = o / DFT2_F3, kl = o % DFT2_F3, k = k3base + kl;
+    double2 acc = make_double2(0.0, 0.0);
+    if (k < nf3) {
+      const double wk = (double)sign3 * (f3[k] - rw) * uc;
+      double sd, cd;
+      sincos(wk * dt3, &sd, &cd);
+      const double2* xr = xb + (int64_t)r * s1;
+      double2 ph = make_double2(1.0, 0.0);
+      for (int n = 0; n < n3; ++n) {
+        if ((n & 31) == 0) {
+          double sn, cn;
+          sincos(wk * (t03 + (double)n * dt3), &sn, &cn);
+          ph = make_double2(cn, sn);
+        }
+        cfma(acc, xr[(int64_t)n * s3], ph);
+        ph = make_double2(ph.x * cd - ph.y * sd, ph.x * sd + ph.y * cd);
+      }
+    }
+    Y[r * DFT2_F3 + kl] = cscale(acc, dt3);
+  }
+  __syncthreads();
+  // t1 transform: one (k1, k3) sum a thread
+  for (int o = threadIdx.x; o < nf1 * DFT2_F3; o += blockDim.x) {
+    const int k1 = o / DFT2_F3, kl = o % DFT2_F3, k = k3base + kl;
+    if (k >= nf3) continue;
+    const double wk = (double)sign1 * (f1[k1] - rw) * uc;
+    double sd, cd;
+    sincos(wk * dt1, &sd, &cd);
+    double2 acc = make_double2(0.0, 0.0), ph = make_double2(1.0, 0.0);
+    for (int n = 0; n < n1; ++n) {
+      if ((n & 31) == 0) {
+        double sn, cn;
+        sincos(wk * (t01 + (double)n * dt1), &sn, &cn);
+        ph = make_double2(cn, sn);
+      }
+      cfma(acc, Y[n * DFT2_F3 + kl], ph);
+      ph = make_double2(ph.x * cd - ph.y * sd, ph.x * sd + ph.y * cd);
+    }
+    X[((int64_t)k1 * nb + b) * nf3 + k] = cscale(acc, dt1);
+  }
+}
+
 }  // namespace qsx
 
 extern "C" int qsx_dft_batched_f32(const double* x, int nt, int64_t batch, double t0, double dt,
@@ -145,5 +211,32 @@ extern "C" int qsx_dft_batched(const double* x, int nt, int64_t batch, double t0
   qsx::dft_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(
       (const double2*)x, nt, t0, dt, freqs, nf, rw_freq, unit_convert, sign, (double2*)X);
   QSX_LAUNCH_CHECK("qsx_dft_batched");
+  return QSX_OK;
+}
+
+extern "C" int qsx_dft2_batched(const double* x, int n1, int64_t batch, int n3, int64_t s1,
+                                int64_t sb, int64_t s3, double t01, double dt1,
+                                const double* f1, int nf1, int sign1, double t03, double dt3,
+                                const double* f3, int nf3, int sign3, double rw_freq,
+                                double unit_convert, double* X, void* stream) {
+  QSX_CHECK_ARG(n1 >= 1 && n3 >= 1 && nf1 >= 1 && nf3 >= 1 && batch >= 0 && batch <= 65535,
+                "qsx_dft2_batched: bad sizes n1=%d n3=%d nf1=%d nf3=%d", n1, n3, nf1, nf3);
+  QSX_CHECK_ARG((sign1 == 1 || sign1 == -1) && (sign3 == 1 || sign3 == -1),
+                "qsx_dft2_batched: signs must be +1 or -1");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(x && f1 && f3 && X, "qsx_dft2_batched: null pointer");
+  const size_t smem = (size_t)n1 * qsx::DFT2_F3 * sizeof(double2);
+  QSX_CHECK_ARG(smem <= 200 * 1024, "qsx_dft2_batched: n1 = %d too long (at most %d)", n1,
+                (int)(200 * 1024 / (qsx::DFT2_F3 * sizeof(double2))));
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(qsx::dft2_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return qsx::cuda_status(e, "qsx_dft2_batched");
+  }
+  dim3 grid((unsigned)((nf3 + qsx::DFT2_F3 - 1) / qsx::DFT2_F3), (unsigned)batch);
+  qsx::dft2_kernel<<<grid, 256, smem, (cudaStream_t)stream>>>(
+      (const double2*)x, n1, n3, s1, sb, s3, t01, dt1, f1, nf1, sign1, t03, dt3, f3, nf3, sign3,
+      rw_freq, unit_convert, (double2*)X);
+  QSX_LAUNCH_CHECK("qsx_dft2_batched");
   return QSX_OK;
 }

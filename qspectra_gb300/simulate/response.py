@@ -11,7 +11,7 @@ from ..polarization import (FOURTH_ORDER_INVARIANTS, check_polarizations,
                              invariant_polarizations, invariant_weights_4th_order)
 from .. import _native
 from .ensemble import ensemble_linear_signal
-from .utils import fourier_transform, integrate
+from .utils import fft_frequencies, fourier_transform, integrate, symmetric_grid
 
 PUMP_PROBE_PATHWAYS = {'GSB': 'gg->eg->gg',
                        'ESE': 'ee->eg->gg',
@@ -311,13 +311,24 @@ def two_dimensional_spectra(dynamical_model, coherence_time_max,
                             ensemble_size=None, ensemble_random_orientations=False,
                             exact_isotropic_average=False, precision='fp64',
                             **integrate_kwargs):
-    """2D spectrum: FT over t1 (sign -1) and t3 (response.py:430-455)."""
+    """2D spectrum: FT over t1 (sign -1) and t3 (response.py:430-455), both
+    axes of the third-order signal in one GPU launch (qsx_dft2_batched) on
+    the reference's FFT frequency grids."""
     (t1, t2, t3), X = third_order_response(
         dynamical_model, coherence_time_max, population_time_max, population_times,
         geometry, polarization, include_signal, ensemble_size,
         ensemble_random_orientations, exact_isotropic_average, precision,
         **integrate_kwargs)
     rw, uc = dynamical_model.rw_freq, dynamical_model.unit_convert
-    f1, X1 = fourier_transform(t1, X, 0, rw_freq=rw, sign=-1, unit_convert=uc)
-    f3, X3 = fourier_transform(t3, X1, 2, rw_freq=rw, unit_convert=uc)
-    return (f1, t2, f3), X3
+    t1, t3 = np.asarray(t1, float), np.asarray(t3, float)
+    f1 = fft_frequencies(t1, rw, uc, sign=-1)
+    f3 = fft_frequencies(t3, rw, uc, sign=1)
+    # the sample that ifftshift moves to index 0 is the time origin
+    s1, _ = symmetric_grid(t1)
+    s3, _ = symmetric_grid(t3)
+    as_numpy = not isinstance(X, torch.Tensor)
+    xt = torch.as_tensor(np.asarray(X, dtype=complex) if as_numpy else X,
+                         dtype=torch.complex128).cuda().contiguous()
+    X3 = _native.dft2(xt, t1[0] - s1[s1.size // 2], t1[1] - t1[0], f1, -1,
+                      t3[0] - s3[s3.size // 2], t3[1] - t3[0], f3, 1, rw, uc)
+    return (f1, t2, f3), (X3.cpu().numpy() if as_numpy else X3)

@@ -16,6 +16,7 @@ import os
 
 import numpy as np
 import pytest
+import torch
 
 import qspectra_gb300 as qg
 from conftest import ROOT, rel_err
@@ -120,3 +121,33 @@ def test_third_order_full_grids(drivers, N, precision, tol):
                                                   precision=precision)
         assert R.shape == (128, 3, 128)
         assert rel_err(R, drivers['chain{}_3rd_ens2_{}'.format(N, geo)]) < tol
+
+
+@pytest.mark.parametrize('n1,nb,n3,sign1,sign3', [(128, 3, 128, -1, 1), (37, 2, 50, 1, -1),
+                                                  (5, 1, 300, -1, -1)])
+def test_dft2_matches_two_one_dimensional_passes(n1, nb, n3, sign1, sign3):
+    """qsx_dft2_batched (both time axes in one launch) against the 1D
+    transform applied along t3, then along t1, and against a NumPy double
+    sum."""
+    from qspectra_gb300 import _native
+    rng = np.random.RandomState(n1 + n3)
+    x = rng.randn(n1, nb, n3) + 1j * rng.randn(n1, nb, n3)
+    xt = torch.as_tensor(x).cuda()
+    t01, dt1, t03, dt3 = -3.0, 2.0, 0.5, 1.5
+    rw, uc = 12300.0, qg.CM_FS
+    f1 = rw + np.linspace(-400.0, 350.0, 41)
+    f3 = rw + np.linspace(-300.0, 420.0, 23)
+    got = _native.dft2(xt, t01, dt1, f1, sign1, t03, dt3, f3, sign3, rw, uc).cpu().numpy()
+    a = _native.dft(xt.reshape(n1 * nb, n3).contiguous(), t03, dt3, torch.as_tensor(f3), rw,
+                    uc, sign3).reshape(n1, nb, -1)
+    a = torch.movedim(a, 0, -1).contiguous()                           # (nb, nf3, n1)
+    two = _native.dft(a.reshape(-1, n1).contiguous(), t01, dt1, torch.as_tensor(f1), rw, uc,
+                      sign1).reshape(nb, len(f3), len(f1))
+    two = torch.movedim(two, -1, 0).cpu().numpy()                      # (nf1, nb, nf3)
+    assert rel_err(got, two) < 1e-12
+    t1 = t01 + dt1 * np.arange(n1)
+    t3 = t03 + dt3 * np.arange(n3)
+    e1 = np.exp(1j * sign1 * np.outer(f1 - rw, t1) * uc)             # (nf1, n1)
+    e3 = np.exp(1j * sign3 * np.outer(f3 - rw, t3) * uc)             # (nf3, n3)
+    ref = dt1 * dt3 * np.einsum('kn,nbm,jm->kbj', e1, x, e3)
+    assert rel_err(got, ref) < 1e-11
