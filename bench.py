@@ -73,7 +73,7 @@ def parse_args():
     p.add_argument('--no-graph', action='store_true',
                    help='time the eager launches only (no CUDA graph capture)')
     p.add_argument('--zofe-samples', type=int, default=152)
-    p.add_argument('--only', choices=['heom', 'third', 'adjoint', 'zofe'],
+    p.add_argument('--only', choices=['heom', 'third', 'adjoint', 'zofe', 'plain'],
                    help='run one auxiliary workload alone and print its JSON')
     p.add_argument('--third-samples', type=int, default=256)
     p.add_argument('--third-reps', type=int, default=2)
@@ -323,6 +323,57 @@ def heom_ring8(torch, qg, native, samples=64, nsteps=1999):
     out['fp32_tflops_executed_form'] = flops / (out['fp32_ms'] * 1e-3) / 1e12
     out['fp64_ms_note'] = 'FP64 timed over {} steps and scaled to {}'.format(min(200, nsteps),
                                                                              nsteps)
+    return out
+
+
+def plain_fmo7(torch, qg, reps=5, cpu=True):
+    """The single-model workload (no disorder) through the public API, as a
+    user calls it: simulate_dynamics of the 'ee' populations from site 1 over
+    1 ps and absorption_spectra over 2048 steps, dt 1 fs, in FP64 (the plain
+    form) and in FP32; the reference's own two calls (zvode, one process, one
+    BLAS thread) beside it."""
+    H, extra, _ = fmo7_inputs()
+    ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 77, 35, 106),
+                                   dipoles=[[1, 0, 0]] * 7, energy_spread_extra=extra)
+    model = qg.RedfieldModel(ham, hilbert_subspace='ge', unit_convert=qg.CM_FS, secular=False)
+    psi = np.zeros(7)
+    psi[0] = 1.0
+    out = {'workload': 'fmo7 single model: simulate_dynamics (ee, 1000 x 1 fs) + '
+                       'absorption_spectra (2048 x 1 fs), no disorder, public API calls'}
+    res = {}
+    for prec in ('fp64', 'fp32'):
+        def call():
+            _, rho = qg.simulate_dynamics(model, psi, 1000.0, precision=prec)
+            _, X = qg.absorption_spectra(model, 2048.0, precision=prec)
+            return np.asarray(rho), np.asarray(X)
+        call()
+        times = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res[prec] = call()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        out[prec + '_ms'] = 1000.0 * statistics.median(times)
+    r64, x64 = res['fp64']
+    r32, x32 = res['fp32']
+    out['fp32_vs_fp64_rel_err'] = {
+        'populations': float(np.abs(r32 - r64).max() / np.abs(r64).max()),
+        'spectrum': float(np.abs(x32 - x64).max() / np.abs(x64).max())}
+    if cpu:
+        import multiprocessing as mp
+        from oracle import reference_shipped as rs
+        if rs.available():
+            for var in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+                os.environ[var] = '1'
+            with mp.get_context('spawn').Pool(1) as pool:
+                pool.apply(rs.time_as_shipped, (H, extra, 0.0, 1))   # warm (imports)
+                walls = [pool.apply(rs.time_as_shipped, (H, extra, 0.0, 1)) for _ in range(3)]
+            out['cpu_baseline'] = {
+                'value': 1000.0 * statistics.median(walls), 'unit': 'ms', 'cores': 1,
+                'kind': 'reference',
+                'sample': "the reference's absorption_spectra(model, 2048) + simulate_dynamics("
+                          "model, psi, 1000) on one model (baseline/_ref, zvode), one process"}
     return out
 
 
@@ -801,6 +852,7 @@ def our_arm(args):
            if rank == 0 and not args.no_adjoint else None)
     zofe = (zofe_fmo7(torch, qg, _native, samples=args.zofe_samples)
             if rank == 0 and not args.no_zofe else None)
+    plain = plain_fmo7(torch, qg, cpu=not args.no_cpu_baseline) if rank == 0 else None
     if rank != 0:
         return 0
     peak = fma_peak_tflops(torch, _native)
@@ -866,6 +918,8 @@ def our_arm(args):
         line['heom_ring8'] = heom
     if zofe is not None:
         line['zofe_fmo7'] = zofe
+    if plain is not None:
+        line['plain_fmo7'] = plain
     if base is not None:
         line['cpu_baseline'] = base
     print(json.dumps(line), flush=True)
@@ -889,6 +943,8 @@ def main():
                              nsteps=args.heom_steps)
         elif args.only == 'zofe':
             out = zofe_fmo7(torch, qg, _native, samples=args.zofe_samples)
+        elif args.only == 'plain':
+            out = plain_fmo7(torch, qg)
         elif args.only == 'third':
             out = third_order_chain24(torch, qg, samples=args.third_samples,
                                       fp64_samples=args.third_fp64_samples,
