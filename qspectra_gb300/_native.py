@@ -652,7 +652,9 @@ def rk4_real_block_mean(mat, y0, nsteps, select, K, check_finite=True, group=0):
     if mat.dtype != torch.float32 or mat.dim() != 3 or not mat.is_cuda:
         raise TypeError('mat must be a (B, rows, m) float32 CUDA tensor')
     B, rows, m = mat.shape
-    if mat.stride(2) != 1 or mat.stride(1) != m or mat.stride(0) != (rows * m + 3) // 4 * 4:
+    # (a batch of one may report any stride for its size-1 sample dimension)
+    if mat.stride(2) != 1 or mat.stride(1) != m or (
+            B > 1 and mat.stride(0) != (rows * m + 3) // 4 * 4):
         raise ValueError('mat must use the padded sample layout of rk4_block_matrix_real')
     y0 = y0.to(device=mat.device, dtype=torch.float64).contiguous()
     sel = const_tensor(np.asarray(select, dtype=np.int32), torch.int32, mat.device)
