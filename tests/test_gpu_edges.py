@@ -73,3 +73,30 @@ def test_single_sample_ensemble_workload_matches_oracle(precision, tol):
     _, rho = orc.simulate_dynamics(om, psi, 300.0)
     assert rel_err(X.cpu().numpy(), oX) < tol
     assert rel_err(pops.cpu().numpy(), np.einsum('tii->ti', rho).real) < tol
+
+
+@pytest.mark.parametrize('n_sites', [3, 7])
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-10), ('fp32', 1e-4)])
+def test_drivers_with_one_sample_ensembles_match_oracle(n_sites, precision, tol):
+    """absorption_spectra and simulate_dynamics with ensemble_size=1 (the
+    batched pipelines on a batch of one) against the oracle's one-sample
+    ensemble average (decorators.py:40-64)."""
+    H = wl.fmo7_hamiltonian(n_sites)
+    extra = wl.energy_spread_for_dt(H, 1.0, qg.CM_FS)
+    fwhm = wl.fwhm_for_sd(80.0)
+    ham = qg.ElectronicHamiltonian(H, bath=qg.DebyeBath(qg.CM_K * 77, 35, 106),
+                                   dipoles=[[1, 0, 0]] * n_sites, disorder=fwhm, random_seed=3,
+                                   energy_spread_extra=extra)
+    m = qg.RedfieldModel(ham, hilbert_subspace='ge', unit_convert=qg.CM_FS, secular=False)
+    obath = orc.DebyeBathSpec(orc.CM_K * 77, 35, 106)
+    oham = orc.ElectronicHamiltonianSpec(H, dipoles=[[1, 0, 0]] * n_sites, disorder=fwhm,
+                                         random_seed=3, energy_spread_extra=extra, bath=obath)
+    om = orc.RedfieldSpec(oham, obath, 'ge', orc.CM_FS, secular=False)
+    f, X = qg.absorption_spectra(m, 300.0, ensemble_size=1, precision=precision)
+    _, oX = orc.ensemble_average(om, 1, orc.absorption_spectra, 300.0)
+    assert rel_err(X, oX) < tol
+    psi = np.zeros(n_sites)
+    psi[-1] = 1.0
+    _, rho = qg.simulate_dynamics(m, psi, 200.0, ensemble_size=1, precision=precision)
+    _, orho = orc.ensemble_average(om, 1, orc.simulate_dynamics, psi, 200.0)
+    assert rel_err(rho, orho) < tol
