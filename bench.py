@@ -87,6 +87,9 @@ def parse_args():
     return p.parse_args()
 
 
+LIB_KERNELS_PER_STEP = 15
+
+
 def fmo7_inputs():
     from qspectra_gb300 import workloads as wl
     from qspectra_gb300.constants import CM_FS
@@ -906,7 +909,12 @@ def our_arm(args):
             'bound': 'fp32_fma', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
             'frac': achieved / peak, 'flops_per_launch': flops_dyn, 'launch_ms': dyn_ms,
             'traffic': traffic, 'hbm': hbm_view(traffic, dyn_ms)},
-        'gpu_launches': 12 * args.steps,
+        # the library's kernels per step of the timed FP32-build form: disordered
+        # Hamiltonians, zero fill, two eigensolve kernels, operators, the eg
+        # propagator, projection build, loop and reduction, DFT, Hermitian
+        # propagator, tensor-core block build, chain, contraction, reduction
+        # (the launch list of one step; torch adds five status-word kernels)
+        'gpu_launches': LIB_KERNELS_PER_STEP * args.steps,
         'clocks': clocks,
     }
     if adj is not None:
