@@ -87,3 +87,26 @@ def test_tensor_core_block_shapes(lib):
             for nsel in (1, 4, 7, 8, 16, 49):
                 assert lib.qsx_rk4_block_matrix_real_tc_supported(m, K, nsel) == \
                     expected(m, K, nsel), (m, K, nsel)
+
+
+def test_missing_library_raises_instead_of_falling_back(tmp_path, monkeypatch):
+    """Without the built library the package raises; there is no CPU path."""
+    monkeypatch.setattr(_native, '_LIB', None)
+    with pytest.raises(_native.QsxError, match='not found'):
+        _native.load(str(tmp_path / 'libqsx_missing.so'))
+
+
+def test_drivers_need_a_gpu(monkeypatch):
+    """With no visible GPU every numeric entry point raises QsxError."""
+    import numpy as np
+    import torch
+    import qspectra_gb300 as qg
+    monkeypatch.setattr(torch.cuda, 'is_available', lambda: False)
+    with pytest.raises(_native.QsxError, match='needs a CUDA GPU'):
+        _native.require_gpu()
+    ham = qg.ElectronicHamiltonian(np.diag([12000.0, 12100.0]),
+                                   bath=qg.DebyeBath(qg.CM_K * 77, 35, 106),
+                                   dipoles=[[1, 0, 0]] * 2)
+    m = qg.RedfieldModel(ham, hilbert_subspace='ge', unit_convert=qg.CM_FS)
+    with pytest.raises(_native.QsxError):
+        qg.absorption_spectra(m, 100.0)
