@@ -400,9 +400,21 @@ def projected_mean(D, y0, proj, nsteps):
                                                and proj.dim() == 2 and P <= 4) else 1
     if K > 1:
         mean, status = _native.rk4_proj_block_mean(D, y0, proj, nsteps, K, check_finite=False)
-        return {'mean': mean, 'status': status}
-    return _native.rk4(D, y0, nsteps, 1, proj=proj, per_sample=False, mean=True,
-                       check_finite=False)
+        out = {'mean': mean, 'status': status}
+    else:
+        out = _native.rk4(D, y0, nsteps, 1, proj=proj, per_sample=False, mean=True,
+                          check_finite=False)
+    return fold_nonfinite(out)
+
+
+def fold_nonfinite(out):
+    """OR QSX_ERR_NONFINITE into ``out['status']`` when ``out['mean']`` holds
+    a NaN or an infinity.  The loops above run without their per-step check:
+    a non-finite state of any sample reaches the projected mean (a zero
+    weight times an infinity is NaN), so one test of the mean replaces it."""
+    bad = torch.isfinite(out['mean']).logical_not().any()
+    out['status'] = out['status'] | (bad.to(out['status'].dtype) * _native.QSX_ERR_NONFINITE)
+    return out
 
 
 def redfield_batch_build(model, batch, precision=_native.QSX_FP64, build_precision=None):

@@ -100,3 +100,27 @@ def test_drivers_with_one_sample_ensembles_match_oracle(n_sites, precision, tol)
     _, rho = qg.simulate_dynamics(m, psi, 200.0, ensemble_size=1, precision=precision)
     _, orho = orc.ensemble_average(om, 1, orc.simulate_dynamics, psi, 200.0)
     assert rel_err(rho, orho) < tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('dtype', [torch.complex64, torch.complex128])
+def test_projected_mean_reports_a_non_finite_sample(dtype):
+    """The absorption leg's loops run without their per-step finite check;
+    one sample whose step matrix holds a NaN still sets QSX_ERR_NONFINITE
+    (through the projected mean) and raise_for_status raises
+    IntegratorError, as integrate() does in the reference
+    (simulate/utils.py:12-13).  A clean ensemble reports status 0."""
+    from qspectra_gb300.simulate.ensemble import projected_mean, raise_for_status
+    B, m, nsteps = 64, 7, 400
+    g = torch.Generator().manual_seed(11)
+    D = (torch.randn(B, m, m, dtype=torch.complex128, generator=g) * 1e-3).to(dtype).cuda()
+    y0 = torch.randn(m, dtype=torch.complex128, generator=g).cuda()
+    proj = torch.randn(1, m, dtype=torch.complex128, generator=g).cuda()
+    clean = projected_mean(D, y0, proj, nsteps)
+    assert int(clean['status'].item()) == 0
+    raise_for_status(int(clean['status'].item()))
+    D[5, 2, 3] = float('nan')
+    bad = projected_mean(D, y0, proj, nsteps)
+    assert int(bad['status'].item()) & _native.QSX_ERR_NONFINITE
+    with pytest.raises(_native.IntegratorError):
+        raise_for_status(int(bad['status'].item()))
