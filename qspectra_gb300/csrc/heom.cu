@@ -651,14 +651,17 @@ __global__ void __launch_bounds__(256, MINB)
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int nx = NB ? NB : p.nx, ny = NB ? NB : p.ny, E = NB ? NB * NB : p.E;
   const int nt = p.nterms, N = p.n_sites, nnodes = p.nnodes;
-  // per warp: its node block (64 complex), then the node's first two
-  // coupling slots of every site (2 N records); then the occupations
-  HTerm<T>* hrec = reinterpret_cast<HTerm<T>*>(smraw) + (size_t)wib * 2 * N;
-  Cx* xs = reinterpret_cast<Cx*>(reinterpret_cast<HTerm<T>*>(smraw) +
-                                 (size_t)(blockDim.x >> 5) * 2 * N) + (size_t)wib * 64;
+  // per warp, twice (the node in work and the next one, copied in by
+  // cp.async while this one computes): the node's first two coupling slots
+  // of every site (2 N records) and its node block (64 complex); then the
+  // occupations
+  const int nw = blockDim.x >> 5;
+  HTerm<T>* hrec2 = reinterpret_cast<HTerm<T>*>(smraw) + (size_t)wib * 4 * N;
+  Cx* xs2 = reinterpret_cast<Cx*>(reinterpret_cast<HTerm<T>*>(smraw) + (size_t)nw * 4 * N) +
+            (size_t)wib * 128;
   T* sox = reinterpret_cast<T*>(reinterpret_cast<Cx*>(reinterpret_cast<HTerm<T>*>(smraw) +
-                                                      (size_t)(blockDim.x >> 5) * 2 * N) +
-                                (size_t)(blockDim.x >> 5) * 64);
+                                                      (size_t)nw * 4 * N) +
+                                (size_t)nw * 128);
   T* soy = sox + N * nx;
   for (int i = threadIdx.x; i < N * nx; i += blockDim.x) sox[i] = ((const T*)p.occx)[i];
   for (int i = threadIdx.x; i < N * ny; i += blockDim.x) soy[i] = ((const T*)p.occy)[i];
@@ -708,10 +711,46 @@ __global__ void __launch_bounds__(256, MINB)
   const bool any_full = __any_sync(0xffffffffu, full[0] || full[1]);
   int64_t b = i0 / nnodes;
   int n = (int)(i0 - b * nnodes);
+  // node (bb, nn): its head records and block into buffer `buf`
+  auto prefetch = [&](int64_t bb, int nn, int buf) {
+    const char* src = reinterpret_cast<const char*>(sterms + (int64_t)nn * slots * N);
+    const uint32_t dh = (uint32_t)__cvta_generic_to_shared(hrec2 + buf * 2 * N);
+    for (int c = lane; c < hchunks; c += 32)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dh + 16u * c),
+                   "l"(src + 16 * c)
+                   : "memory");
+    const Cx* xsrc = in + (bb * nnodes + nn) * (int64_t)E + lane;
+    const uint32_t dx = (uint32_t)__cvta_generic_to_shared(xs2 + buf * 64 + lane);
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      if (ev[u]) {
+        if constexpr (sizeof(Cx) == 8)
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dx + 8u * 32 * u),
+                       "l"(xsrc + 32 * u)
+                       : "memory");
+        else
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dx + 16u * 32 * u),
+                       "l"(xsrc + 32 * u)
+                       : "memory");
+      }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  prefetch(b, n, 0);
+  int buf = 0;
   T hx[2][8], hy[2][8];
   const Cx* xb = nullptr;
   bool fresh = true;
-  for (int64_t it = i0; it < i1; ++it) {
+  for (int64_t it = i0; it < i1; ++it, buf ^= 1) {
+    // this node's copies have landed (every lane's), then the next node's
+    // are issued into the other buffer
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncwarp();
+    if (it + 1 < i1) {
+      const bool wrap = n + 1 == nnodes;
+      prefetch(wrap ? b + 1 : b, wrap ? 0 : n + 1, buf ^ 1);
+    }
+    const HTerm<T>* hrec = hrec2 + buf * 2 * N;
+    const Cx* xs = xs2 + buf * 64;
     if (fresh) {
       fresh = false;
       xb = in + b * (int64_t)nnodes * E;
@@ -726,21 +765,9 @@ __global__ void __launch_bounds__(256, MINB)
         }
     }
     const int64_t base = it * E;
-    const Cx* xn = xb + n * E + lane;
     Cx self[2];
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      self[u] = cmk((T)0, (T)0);
-      if (ev[u]) {
-        self[u] = xn[32 * u];
-        xs[lane + 32 * u] = self[u];
-      }
-    }
-    {
-      const uint4* src = reinterpret_cast<const uint4*>(sterms + (int64_t)n * slots * N);
-      uint4* dst = reinterpret_cast<uint4*>(hrec);
-      for (int c = lane; c < hchunks; c += 32) dst[c] = __ldg(src + c);
-    }
+    for (int u = 0; u < 2; ++u) self[u] = ev[u] ? xs[lane + 32 * u] : cmk((T)0, (T)0);
     Cx yv[2], av[2], lv[2];
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
@@ -753,7 +780,6 @@ __global__ void __launch_bounds__(256, MINB)
         }
       }
     }
-    __syncwarp();   // the head records are in the slice
     // the coupling terms of this lane's sites: the first two terms of each
     // site (coefficient and neighbour node) for both elements, then every
     // neighbour load in flight together
@@ -895,7 +921,7 @@ __global__ void __launch_bounds__(256, MINB)
       ++b;
       fresh = true;
     }
-    __syncwarp();   // the block slice is rewritten by the next node
+    __syncwarp();   // this buffer is rewritten by the node after next
   }
 }
 
@@ -1800,8 +1826,9 @@ int qsx_heom_rk4(const qsx_heom_args* a, void* stream) {
                            : heom_warp_stage_kernel<T, 8>;
     const int wthreads = 256;
     const size_t wsmem =
-        small ? (size_t)(wthreads / 32) * 64 * sizeof(C) + (size_t)p.n_sites * (p.nx + p.ny) * sizeof(T) +
-                    (by_site ? (size_t)(wthreads / 32) * 2 * p.n_sites * sizeof(HTerm<T>) : 0)
+        small ? (size_t)(wthreads / 32) * 64 * sizeof(C) * (by_site ? 2 : 1) +
+                    (size_t)p.n_sites * (p.nx + p.ny) * sizeof(T) +
+                    (by_site ? (size_t)(wthreads / 32) * 4 * p.n_sites * sizeof(HTerm<T>) : 0)
               : (size_t)(wthreads / 32) * 32 * epl * sizeof(C);
     if (wsmem > 48 * 1024) {
       cudaError_t fe = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
