@@ -640,6 +640,16 @@ __global__ void heom_pack_site_terms_kernel(const HTerm<T>* __restrict__ terms, 
   }
 }
 
+// two-wide multiply-add a * b + c per component: one packed FFMA2 in FP32
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ double2 pfma(double2 a, double2 b, double2 c) {
+  return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
+}
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ double2 pmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x, a.y * b.y);
+}
+
 template <typename T, int NB, int MINB>
 __global__ void __launch_bounds__(256, MINB)
     heom_warp_site_kernel(HeomWP p, int stage, const typename cplx<T>::type* __restrict__ in,
@@ -761,7 +771,8 @@ __global__ void __launch_bounds__(256, MINB)
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           hx[u][c] = c < nx ? __ldg(Hx + ea[NB == 8 ? 0 : u] * nx + c) : (T)0;
-          hy[u][c] = c < ny ? __ldg(Hy + c * ny + eb[u]) : (T)0;
+          // negated: the commutator sums Hx x - x Hy in one accumulator
+          hy[u][c] = c < ny ? -__ldg(Hy + c * ny + eb[u]) : (T)0;
         }
     }
     const int64_t base = it * E;
@@ -782,20 +793,24 @@ __global__ void __launch_bounds__(256, MINB)
     }
     // the coupling terms of this lane's sites: the first two terms of each
     // site (coefficient and neighbour node) for both elements, then every
-    // neighbour load in flight together
-    T orr[2] = {(T)0, (T)0}, oi[2] = {(T)0, (T)0};
-    auto coef = [&](int u, int j, const HTerm<T>& r, T& fr, T& fi) {
+    // neighbour load in flight together.  Complex sums in packed two-wide
+    // multiply-adds: o += f v as o += f.x (v.x, v.y) + (-f.y, f.y) (v.y, v.x)
+    Cx o[2] = {cmk((T)0, (T)0), cmk((T)0, (T)0)};
+    auto coef = [&](int u, int j, const HTerm<T>& r) -> Cx {
       const T oa = sox[j * nx + ea[u]], ob = soy[j * ny + eb[u]];
-      fr = r.al.x * oa + r.be.x * ob;
-      fi = r.al.y * oa + r.be.y * ob;
+      Cx f = pfma(r.be, cmk(ob, ob), pmul(r.al, cmk(oa, oa)));
       if (p.has_gamma) {
         const T gw = wr[u] * (oa - ob);
-        fr = fma(r.ga.x, gw, fr);
-        fi = fma(r.ga.y, gw, fi);
+        f = pfma(r.ga, cmk(gw, gw), f);
       }
+      return f;
+    };
+    auto cmac = [](Cx& acc_, Cx f, Cx v) {
+      acc_ = pfma(cmk(f.x, f.x), v, acc_);
+      acc_ = pfma(cmk(-f.y, f.y), cmk(v.y, v.x), acc_);
     };
     int cnt[2][2], nbi[2][2][2];
-    T cfr[2][2][2], cfi[2][2][2];
+    Cx cf[2][2][2];
 #pragma unroll
     for (int u = 0; u < 2; ++u)
 #pragma unroll
@@ -805,13 +820,13 @@ __global__ void __launch_bounds__(256, MINB)
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
           nbi[u][q][r] = -1;
-          cfr[u][q][r] = cfi[u][q][r] = (T)0;
+          cf[u][q][r] = cmk((T)0, (T)0);
           if (on) {
             // the first two slots always exist (padding: nbr = -1)
             const HTerm<T> rec = hrec[r * N + js[u][q]];
             cnt[u][q] = rec.site;
             nbi[u][q][r] = rec.nbr;
-            if (rec.nbr >= 0) coef(u, js[u][q], rec, cfr[u][q][r], cfi[u][q][r]);
+            if (rec.nbr >= 0) cf[u][q][r] = coef(u, js[u][q], rec);
           }
         }
       }
@@ -829,11 +844,7 @@ __global__ void __launch_bounds__(256, MINB)
 #pragma unroll
       for (int q = 0; q < 2; ++q)
 #pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          const Cx v = nv[u][q][r];
-          orr[u] = fma(cfr[u][q][r], v.x, fma(-cfi[u][q][r], v.y, orr[u]));
-          oi[u] = fma(cfr[u][q][r], v.y, fma(cfi[u][q][r], v.x, oi[u]));
-        }
+        for (int r = 0; r < 2; ++r) cmac(o[u], cf[u][q][r], nv[u][q][r]);
     // sites with more than two terms (several exponents per bath)
 #pragma unroll
     for (int u = 0; u < 2; ++u)
@@ -843,11 +854,7 @@ __global__ void __launch_bounds__(256, MINB)
           HTerm<T> rq;
           load_term<T>(sterms + ((int64_t)n * slots + r) * N + js[u][q], rq.nbr, rq.site, rq.al,
                        rq.be, rq.ga);
-          T fr, fi;
-          coef(u, js[u][q], rq, fr, fi);
-          const Cx v = xb[(int64_t)rq.nbr * E + lane + 32 * u];
-          orr[u] = fma(fr, v.x, fma(-fi, v.y, orr[u]));
-          oi[u] = fma(fr, v.y, fma(fi, v.x, oi[u]));
+          cmac(o[u], coef(u, js[u][q], rq), xb[(int64_t)rq.nbr * E + lane + 32 * u]);
         }
     if (any_full) {
       // lanes whose row or column couples to more than one site: every term
@@ -859,11 +866,7 @@ __global__ void __launch_bounds__(256, MINB)
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           if (!(ev[u] && full[u])) continue;
-          T fr, fi;
-          coef(u, rq.site, rq, fr, fi);
-          const Cx v = xb[(int64_t)rq.nbr * E + lane + 32 * u];
-          orr[u] = fma(fr, v.x, fma(-fi, v.y, orr[u]));
-          oi[u] = fma(fr, v.y, fma(fi, v.x, oi[u]));
+          cmac(o[u], coef(u, rq.site, rq), xb[(int64_t)rq.nbr * E + lane + 32 * u]);
         }
       }
     }
@@ -871,29 +874,22 @@ __global__ void __launch_bounds__(256, MINB)
     const T sh = __ldg(shift + n);
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-      // -i (Hx x - x Hy)[a][bb] in four independent chains
-      T c0 = 0, s0 = 0, c1 = 0, s1 = 0;
+      // g = (Hx x - x Hy)[a][bb] in two packed chains (hy holds -Hy); the
+      // step adds -i g - d x
+      Cx g0 = cmk((T)0, (T)0), g1 = cmk((T)0, (T)0);
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        if (c < nx) {
-          const Cx xv = xs[c + nx * eb[u]];
-          c0 = fma(hx[u][c], xv.x, c0);
-          s0 = fma(hx[u][c], xv.y, s0);
-        }
-        if (c < ny) {
-          const Cx xv = xs[ea[u] + nx * c];
-          c1 = fma(hy[u][c], xv.x, c1);
-          s1 = fma(hy[u][c], xv.y, s1);
-        }
+        if (c < nx) g0 = pfma(cmk(hx[u][c], hx[u][c]), xs[c + nx * eb[u]], g0);
+        if (c < ny) g1 = pfma(cmk(hy[u][c], hy[u][c]), xs[ea[u] + nx * c], g1);
       }
       const T d = sh + w[u];
-      orr[u] += fma(-d, self[u].x, s0 - s1);
-      oi[u] += fma(-d, self[u].y, c1 - c0);
+      o[u].x += fma(-d, self[u].x, g0.y + g1.y);
+      o[u].y += fma(-d, self[u].y, -(g0.x + g1.x));
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
       if (!ev[u]) continue;
-      const Cx k = cmk(uc * orr[u], uc * oi[u]);
+      const Cx k = cmk(uc * o[u].x, uc * o[u].y);
       const int64_t idx = base + lane + 32 * u;
       if (stage == 0) {
         acc[idx] = k;
