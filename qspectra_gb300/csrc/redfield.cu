@@ -1468,11 +1468,17 @@ int qsx_redfield_propagator_hermitian_batched(const double* H, int64_t H_stride,
                       nb * sizeof(int);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e;
+  // one thread per 4 x 4 tile of the two products, whole warps, at most 256:
+  // the 169 tiles of 7 sites take 192 threads in one round (256 threads left
+  // 87 idle in every product), and five such CTAs fit an SM where four of
+  // 256 did (64 registers a thread)
+  const int tiles = (ld / 4) * (ld / 4);
+  const int threads = std::min(256, (tiles + 31) / 32 * 32);
   auto launch = [&](auto kern, auto* Dt) -> cudaError_t {
     cudaError_t fe = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem);
     if (fe != cudaSuccess) return fe;
-    kern<<<(unsigned)batch, 256, smem, s>>>(H, H_stride, (const double2*)G, (const double2*)M,
+    kern<<<(unsigned)batch, threads, smem, s>>>(H, H_stride, (const double2*)G, (const double2*)M,
                                             occ, n, n_sites, states, nb, (const int4*)recipe,
                                             unit_convert, h, Dt);
     return cudaSuccess;
