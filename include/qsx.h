@@ -126,6 +126,25 @@ int qsx_redfield_build_w64(const double* H, int n, int off, int n_sites,
                            int corr_pieces, double corr_width, double unit_convert,
                            double* E, double* U, double* G, double* M,
                            void* stream);
+/*
+ * FP32 site-basis Redfield operators for one-exciton Hilbert spaces ('e',
+ * 'ge'; 2 <= n_sites <= 8), one warp per sample, from an FP32
+ * eigendecomposition (E, U as qsx_eigh_batched_prec with QSX_FP32 stores
+ * them).  Same outputs as qsx_redfield_operators_batched with site_basis != 0
+ * and QSX_FP32 (redfield_tensor, qspectra/dynamics/redfield.py:9-74, in
+ * operator form): with the number-operator couplings of one-exciton states,
+ * M_i = Y_i (C Y_i^T), Y_i[a][c] = U[a][c] U[i][c], C[c][d] = C(E_d - E_c),
+ * and row i of G is row i of M_i.  The coupled block is rows/columns
+ * [off, off + n_sites) of each n x n matrix (n <= 32).  Outputs G complex128
+ * [batch][n][n], M complex128 [batch][n_sites][n][n], scaled by
+ * unit_convert, zero outside the block.
+ */
+int qsx_redfield_operators_w32(const double* E, const double* U, int n, int off,
+                               int n_sites, int64_t batch, double temperature,
+                               double reorg_energy, double cutoff_freq,
+                               int matsubara_cutoff, int discard_imag_corr,
+                               double unit_convert, double* G, double* M,
+                               void* stream);
 /* The Matsubara sum S(x) = sum_{k=1}^{K-1} nu_k / ((nu_k^2 - gamma^2)
  * (nu_k - i x)), nu_k = 2 pi k T, of the Debye correlation function
  * (qspectra/bath.py:95-102) as a piecewise Chebyshev table: piece j covers

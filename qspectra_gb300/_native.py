@@ -149,6 +149,9 @@ _PROTOS = {
     'qsx_redfield_build_w64': (_c_int, [_c_vp, _c_int, _c_int, _c_int, _c_i64, _c_vp, _c_dbl,
                                         _c_dbl, _c_dbl, _c_int, _c_int, _c_vp, _c_int, _c_dbl,
                                         _c_dbl, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    'qsx_redfield_operators_w32': (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_int, _c_i64,
+                                            _c_dbl, _c_dbl, _c_dbl, _c_int, _c_int, _c_dbl,
+                                            _c_vp, _c_vp, _c_vp]),
     'qsx_debye_matsubara_table': (_c_int, [_c_dbl, _c_dbl, _c_int, _c_int, _c_dbl, _c_vp]),
     'qsx_debye_matsubara_table_degree': (_c_int, []),
     'qsx_disordered_hamiltonians': (_c_int, [_c_vp, _c_int, _c_vp, _c_i64, _c_int, _c_int,
@@ -289,6 +292,26 @@ def redfield_operators(E, U, occ, bath, unit_convert, discard_imag_corr=False,
         int(site_basis), int(precision), _p(G), _p(M), _p(K), _stream()),
         'qsx_redfield_operators_batched')
     return G, M, K
+
+
+def redfield_operators_w32(E, U, n_sites, off, bath, unit_convert, discard_imag_corr=False,
+                           matsubara_cutoff=1000):
+    """FP32 site-basis operators G, M of a one-exciton Hilbert space, one
+    warp per sample (qsx_redfield_operators_w32); E (B, n), U (B, n, n)
+    float64 from the FP32 eigensolve; the coupled block is [off, off +
+    n_sites)."""
+    require_gpu()
+    _need(E, torch.float64, 'E', 2)
+    _need(U, torch.float64, 'U', 3)
+    B, n = E.shape
+    dev = E.device
+    G = torch.empty((B, n, n), dtype=torch.complex128, device=dev)
+    M = torch.empty((B, n_sites, n, n), dtype=torch.complex128, device=dev)
+    _check(load().qsx_redfield_operators_w32(
+        _p(E), _p(U), n, off, n_sites, B, bath.temperature, bath.reorg_energy,
+        bath.cutoff_freq, matsubara_cutoff, int(discard_imag_corr), unit_convert, _p(G),
+        _p(M), _stream()), 'qsx_redfield_operators_w32')
+    return G, M
 
 
 def disordered_hamiltonians(base, offsets, off):

@@ -351,6 +351,115 @@ static cudaError_t launch_bw(const double* H, int n, int off, int64_t batch, con
   return cudaGetLastError();
 }
 
+// FP32 operator build for the same one-exciton, site-basis case, one warp
+// per sample, from the FP32 eigendecomposition (E, U as stored by
+// qsx_eigh_batched_prec): the closed-form FP32 correlation function on the
+// eigenvalue differences (as redfield_operators_kernel<float>), then
+// M_i = Y_i (C Y_i^T) and G row i = M_i row i, all N sites' products over
+// the warp's lanes, with no block barrier.  Outputs as qsx_redfield_
+// operators_batched (site basis), computed in FP32 and stored as complex128.
+template <int NB>
+struct Ow32Smem {
+  float2 C[NB * NB];
+  float2 T[NB * NB * NB];    // [i][c][b]
+  float X[NB * NB];
+  float lam[NB];
+  float Y[NB * NB * NB];     // [i][a][c]
+};
+
+template <int NB>
+__global__ void __launch_bounds__(32 * BW_WARPS)
+    redfield_operators_w32_kernel(const double* __restrict__ E, const double* __restrict__ U,
+                                  int n, int off, int64_t batch, DebyeParams bath, double uc,
+                                  double2* __restrict__ G, double2* __restrict__ M) {
+  constexpr int NN = NB * NB;
+  constexpr int NNN = NB * NB * NB;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Ow32Smem<NB>& sm = reinterpret_cast<Ow32Smem<NB>*>(smraw)[w];
+  const int64_t b = (int64_t)blockIdx.x * BW_WARPS + w;
+  if (b >= batch) return;   // whole warps leave; no CTA barrier below
+  const int nn = n * n;
+  const double* u = U + b * nn;
+  for (int e = lane; e < NN; e += 32) {
+    const int r = e / NB, c = e % NB;
+    sm.X[e] = (float)u[(off + r) * n + off + c];
+  }
+  if (lane < NB) sm.lam[lane] = (float)E[b * n + off + lane];
+  __syncwarp();
+  // correlation function on the eigenvalue differences; (c, d) and (d, c)
+  // share one evaluation
+  for (int e = lane; e < NN; e += 32) {
+    const int c = e / NB, d = e % NB;
+    if (c > d) continue;
+    float2 cp, cn;
+    debye_corr_pair_f(bath, sm.lam[d] - sm.lam[c], cp, cn);
+    sm.C[c * NB + d] = cp;
+    sm.C[d * NB + c] = cn;
+  }
+  // Y_i[a][c] = X[a][c] X[i][c]
+  for (int e = lane; e < NNN; e += 32) {
+    const int i = e / NN, a = (e / NB) % NB, c = e % NB;
+    sm.Y[e] = sm.X[a * NB + c] * sm.X[i * NB + c];
+  }
+  __syncwarp();
+  // T_i[c][b] = sum_d C[c][d] Y_i[b][d]
+  for (int e = lane; e < NNN; e += 32) {
+    const int i = e / NN, c = (e / NB) % NB, bb = e % NB;
+    float2 acc = make_float2(0.f, 0.f);
+    const float* yi = sm.Y + i * NN + bb * NB;
+#pragma unroll
+    for (int d = 0; d < NB; ++d) {
+      const float2 cv = sm.C[c * NB + d];
+      const float y = yi[d];
+      acc.x = fmaf(cv.x, y, acc.x);
+      acc.y = fmaf(cv.y, y, acc.y);
+    }
+    sm.T[e] = acc;
+  }
+  __syncwarp();
+  // M_i[a][b] = uc sum_c Y_i[a][c] T_i[c][b]; G row i = M_i row i
+  const float ucf = (float)uc;
+  double2* Mb = M + b * (int64_t)NB * nn;
+  double2* Gb = G + b * nn;
+  for (int e = lane; e < NNN; e += 32) {
+    const int i = e / NN, a = (e / NB) % NB, bb = e % NB;
+    float2 acc = make_float2(0.f, 0.f);
+    const float* yi = sm.Y + i * NN + a * NB;
+    const float2* ti = sm.T + i * NN + bb;
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      const float y = yi[c];
+      const float2 t = ti[c * NB];
+      acc.x = fmaf(y, t.x, acc.x);
+      acc.y = fmaf(y, t.y, acc.y);
+    }
+    const double2 v = make_double2((double)(acc.x * ucf), (double)(acc.y * ucf));
+    Mb[(int64_t)i * nn + (off + a) * n + off + bb] = v;
+    if (a == i) Gb[(off + a) * n + off + bb] = v;
+  }
+  // zeros outside the coupled block
+  if (off > 0 || n > off + NB) {
+    for (int e = lane; e < nn; e += 32) {
+      const int r = e / n, c = e % n;
+      if (r >= off && r < off + NB && c >= off && c < off + NB) continue;
+      Gb[e] = make_double2(0.0, 0.0);
+      for (int i = 0; i < NB; ++i) Mb[(int64_t)i * nn + e] = make_double2(0.0, 0.0);
+    }
+  }
+}
+
+template <int NB>
+static cudaError_t launch_ow32(const double* E, const double* U, int n, int off, int64_t batch,
+                               const DebyeParams& bath, double uc, double* G, double* M,
+                               cudaStream_t s) {
+  const size_t smem = sizeof(Ow32Smem<NB>) * BW_WARPS;
+  const int64_t grid = (batch + BW_WARPS - 1) / BW_WARPS;
+  redfield_operators_w32_kernel<NB><<<(unsigned)grid, 32 * BW_WARPS, smem, s>>>(
+      E, U, n, off, batch, bath, uc, (double2*)G, (double2*)M);
+  return cudaGetLastError();
+}
+
 }  // namespace qsx
 
 // Host: Chebyshev coefficients of the Matsubara sum
@@ -439,5 +548,39 @@ extern "C" int qsx_redfield_build_w64(const double* H, int n, int off, int n_sit
     default: e = launch_bw<8>(H, n, off, batch, U_approx, bath, ctab, unit_convert, E, U, G, M, s); break;
   }
   if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_build_w64");
+  return QSX_OK;
+}
+
+extern "C" int qsx_redfield_operators_w32(const double* E, const double* U, int n, int off,
+                                          int n_sites, int64_t batch, double temperature,
+                                          double reorg_energy, double cutoff_freq,
+                                          int matsubara_cutoff, int discard_imag_corr,
+                                          double unit_convert, double* G, double* M,
+                                          void* stream) {
+  using namespace qsx;
+  QSX_CHECK_ARG(n_sites >= 2 && n_sites <= 8,
+                "qsx_redfield_operators_w32: n_sites must be 2..8 (got %d)", n_sites);
+  QSX_CHECK_ARG(off >= 0 && off + n_sites <= n && n <= 32,
+                "qsx_redfield_operators_w32: the coupled block [%d, %d) must lie in n = %d <= 32",
+                off, off + n_sites, n);
+  QSX_CHECK_ARG(batch >= 0, "qsx_redfield_operators_w32: negative batch");
+  if (batch == 0) return QSX_OK;
+  QSX_CHECK_ARG(E && U && G && M, "qsx_redfield_operators_w32: null pointer");
+  QSX_CHECK_ARG(temperature > 0 && cutoff_freq > 0 && matsubara_cutoff >= 1,
+                "qsx_redfield_operators_w32: bad bath parameters");
+  const DebyeParams bath = make_debye(temperature, reorg_energy, cutoff_freq, matsubara_cutoff,
+                                      discard_imag_corr);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaSuccess;
+  switch (n_sites) {
+    case 2: e = launch_ow32<2>(E, U, n, off, batch, bath, unit_convert, G, M, s); break;
+    case 3: e = launch_ow32<3>(E, U, n, off, batch, bath, unit_convert, G, M, s); break;
+    case 4: e = launch_ow32<4>(E, U, n, off, batch, bath, unit_convert, G, M, s); break;
+    case 5: e = launch_ow32<5>(E, U, n, off, batch, bath, unit_convert, G, M, s); break;
+    case 6: e = launch_ow32<6>(E, U, n, off, batch, bath, unit_convert, G, M, s); break;
+    case 7: e = launch_ow32<7>(E, U, n, off, batch, bath, unit_convert, G, M, s); break;
+    default: e = launch_ow32<8>(E, U, n, off, batch, bath, unit_convert, G, M, s); break;
+  }
+  if (e != cudaSuccess) return cuda_status(e, "qsx_redfield_operators_w32");
   return QSX_OK;
 }

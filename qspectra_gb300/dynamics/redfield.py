@@ -74,6 +74,15 @@ class RedfieldBuild:
             self.K = None
             return
         self.E, self.U = _native.eigh(H, bounds, build_precision)
+        if (build_precision == _native.QSX_FP32 and self.site_ops and one_exciton
+                and 2 <= n_sites <= 8 and self.n == off + n_sites):
+            # FP32 build of a one-exciton space: the warp-per-sample operator
+            # form (qsx_redfield_operators_w32)
+            self.G, self.M = _native.redfield_operators_w32(
+                self.E, self.U, n_sites, off, bath, unit_convert, discard_imag_corr,
+                matsubara_cutoff=bath.matsubara_cutoff)
+            self.K = None
+            return
         self.G, self.M, self.K = _native.redfield_operators(
             self.E, self.U, self.occ, bath, unit_convert, discard_imag_corr,
             site_basis=self.site_ops, matsubara_cutoff=bath.matsubara_cutoff,

@@ -98,3 +98,36 @@ def test_workload_fp32_propagation_with_either_build(golden, build_precision):
     assert int(status.item()) == 0
     assert rel_err(X.cpu().numpy(), golden['fmo7_ens8_abs_X']) < 1e-4
     assert rel_err(P.cpu().numpy(), golden['fmo7_ens8_pops']) < 1e-4
+
+
+@pytest.mark.parametrize('N,space,discard', [(7, 'ge', False), (3, 'e', False), (8, 'ge', True),
+                                             (2, 'ge', False)])
+def test_fp32_warp_operator_build_matches_cta_operator_build(N, space, discard):
+    """The FP32 build of one-exciton spaces takes the warp-per-sample operator
+    form (qsx_redfield_operators_w32): the same G and M as the general FP32
+    operator kernel (qsx_redfield_operators_batched, QSX_FP32) on the same
+    FP32 eigendecomposition, to FP32 rounding, and close to the FP64 build."""
+    B = 300
+    Hn = ge_hamiltonians(N, B, seed=30 + N, degenerate=False)
+    if space == 'e':
+        Hn = np.ascontiguousarray(Hn[:, 1:, 1:])
+    H = torch.as_tensor(Hn).cuda()
+    bath = qg.DebyeBath(qg.CM_K * 77, 35, 106)
+    occ = occupation_table(N, space)
+    got = RedfieldBuild(H, N, space, occ, bath, qg.CM_FS, discard_imag_corr=discard,
+                        precision=_native.QSX_FP32, build_precision=_native.QSX_FP32)
+    assert got.K is None and not got.refined
+    occ_t = torch.as_tensor(np.asarray(occ, dtype=np.float64)).cuda()
+    G32, M32, _ = _native.redfield_operators(got.E, got.U, occ_t, bath, qg.CM_FS, discard,
+                                             site_basis=True, precision=_native.QSX_FP32)
+    ref = RedfieldBuild(H, N, space, occ, bath, qg.CM_FS, discard_imag_corr=discard,
+                        precision=_native.QSX_FP64)
+    for a, b in ((got.G, G32), (got.M, M32)):
+        assert rel_err(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
+    for a, b in ((got.G, ref.G), (got.M, ref.M)):
+        assert rel_err(a.cpu().numpy(), b.cpu().numpy()) < 1e-4
+    # zero outside the coupled block ('ge': the ground-state row and column)
+    if space == 'ge':
+        assert torch.count_nonzero(got.M[:, :, 0, :]) == 0
+        assert torch.count_nonzero(got.M[:, :, :, 0]) == 0
+        assert torch.count_nonzero(got.G[:, 0, :]) == 0
