@@ -393,28 +393,20 @@ def can_use_hermitian(precision, idx, n_total, y0, nsteps):
 def projected_mean(D, y0, proj, nsteps):
     """Ensemble mean of proj . y_n (n = 0..nsteps) for y_{n+1} = (I + D) y_n:
     the K-step blocked projection loop for FP32 blocks of up to 8 states and
-    a shared projection, else the step-by-step batched loop."""
+    a shared projection, else the step-by-step batched loop.  Both kernels
+    OR QSX_ERR_NONFINITE into the returned status word when a sample's final
+    state is not finite (a NaN or an infinity never returns to a finite
+    value), so ``raise_for_status`` reports a blow-up without a host sync
+    inside the loop (``check_finite=False`` only skips raising here)."""
     m = D.shape[-1]
     P = proj.shape[-2]
     K = _native.proj_block_k(nsteps, m, P) if (D.dtype == torch.complex64 and m <= 8
                                                and proj.dim() == 2 and P <= 4) else 1
     if K > 1:
         mean, status = _native.rk4_proj_block_mean(D, y0, proj, nsteps, K, check_finite=False)
-        out = {'mean': mean, 'status': status}
-    else:
-        out = _native.rk4(D, y0, nsteps, 1, proj=proj, per_sample=False, mean=True,
-                          check_finite=False)
-    return fold_nonfinite(out)
-
-
-def fold_nonfinite(out):
-    """OR QSX_ERR_NONFINITE into ``out['status']`` when ``out['mean']`` holds
-    a NaN or an infinity.  The loops above run without their per-step check:
-    a non-finite state of any sample reaches the projected mean (a zero
-    weight times an infinity is NaN), so one test of the mean replaces it."""
-    bad = torch.isfinite(out['mean']).logical_not().any()
-    out['status'] = out['status'] | (bad.to(out['status'].dtype) * _native.QSX_ERR_NONFINITE)
-    return out
+        return {'mean': mean, 'status': status}
+    return _native.rk4(D, y0, nsteps, 1, proj=proj, per_sample=False, mean=True,
+                       check_finite=False)
 
 
 def redfield_batch_build(model, batch, precision=_native.QSX_FP64, build_precision=None):

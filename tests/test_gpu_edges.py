@@ -105,11 +105,11 @@ def test_drivers_with_one_sample_ensembles_match_oracle(n_sites, precision, tol)
 @pytest.mark.gpu
 @pytest.mark.parametrize('dtype', [torch.complex64, torch.complex128])
 def test_projected_mean_reports_a_non_finite_sample(dtype):
-    """The absorption leg's loops run without their per-step finite check;
-    one sample whose step matrix holds a NaN still sets QSX_ERR_NONFINITE
-    (through the projected mean) and raise_for_status raises
-    IntegratorError, as integrate() does in the reference
-    (simulate/utils.py:12-13).  A clean ensemble reports status 0."""
+    """The absorption leg's loops check each sample's final state on the
+    device: one sample whose step matrix holds a NaN sets QSX_ERR_NONFINITE
+    in the status word, and raise_for_status raises IntegratorError, as
+    integrate() does in the reference (simulate/utils.py:12-13).  A clean
+    ensemble reports status 0."""
     from qspectra_gb300.simulate.ensemble import projected_mean, raise_for_status
     B, m, nsteps = 64, 7, 400
     g = torch.Generator().manual_seed(11)
