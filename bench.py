@@ -859,6 +859,16 @@ def our_arm(args):
     if rank != 0:
         return 0
     peak = fma_peak_tflops(torch, _native)
+    # the plain FP64 form against the measured FP64 FMA rate.  Its algorithmic
+    # work per step: the step-by-step complex loops in propagator form (one
+    # complex GEMV per RK4 step: ee 49 x 49, eg 7 x 7; 8 flops per complex
+    # multiply-add) and the two one-step propagators (two complex m^3
+    # products each, Paterson-Stockmeyer)
+    peak64 = fma_peak_tflops(torch, _native, _native.QSX_FP64)
+    m_ee, m_eg = len(work.idx_ee), len(work.idx_eg)
+    n_dyn, n_abs = len(work.t_dyn) - 1, len(work.t_abs) - 1
+    fp64_flops = 8.0 * S * (n_dyn * m_ee ** 2 + n_abs * m_eg ** 2 + 2 * (m_ee ** 3 + m_eg ** 3))
+    fp64_achieved = fp64_flops / (fp64_ms * 1e-3) / 1e12
     flops_dyn = events['dyn_flops']  # executed form (K-step blocked rows)
     dense_equiv = float(S) * (DYN_TIME - 1) * 49 * 49 * 8  # one 49x49 GEMV per step
     achieved = flops_dyn / (dyn_ms * 1e-3) / 1e12
@@ -894,6 +904,13 @@ def our_arm(args):
             graph_ms=graph_ms,
             block_k_real=[{'K': v[0], 'ms': v[1]} for v in block_k_real_timings().values()]),
         'fp64_ms_per_step': fp64_ms, 'speedup_fp32_vs_fp64': fp64_ms / ms,
+        'roofline_fp64_form': {
+            'kernel': 'plain FP64 step (complex propagator-form RK4 loops, ee {0} x {0} for {1} '
+                      'steps and eg {2} x {2} for {3} steps, and their one-step propagators; '
+                      'the whole step timed)'.format(m_ee, n_dyn, m_eg, n_abs),
+            'bound': 'fp64_fma', 'achieved': fp64_achieved, 'peak': peak64, 'unit': 'TFLOP/s',
+            'frac': fp64_achieved / peak64 if peak64 else None, 'flops_per_step': fp64_flops,
+            'peak_source': 'measured live by the FMA probe (libqsx_probe.so, FP64 FMA)'},
         'e2e': {'value': whole_job_rate(world, e2e_ms), 'unit': UNIT,
                 'h2d_bytes_per_step': int(off_host.numel() * 8),
                 'd2h_bytes_per_step': int((nf + Ph.size + 1) * 8)},
