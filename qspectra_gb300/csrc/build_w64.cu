@@ -35,6 +35,8 @@
 //     M_i = U (Kt_i o C) U^T = Y_i (C Y_i^T),  G = sum_i diag(occ_i) M_i
 //   (row i of G is row i of M_i).  All N sites' products are spread over the
 //   warp's lanes together (N n^2 outputs), so few lanes idle.
+// The file also holds the FP32 counterpart of the operator stage
+// (redfield_operators_w32_kernel, below), for FP32 builds of the same spaces.
 // Outputs have the layout of qsx_redfield_operators_batched (site basis):
 // G [batch][n][n], M [batch][N][n][n] complex128 scaled by unit_convert,
 // zero outside the coupled block, and E [batch][n], U [batch][n][n] with the
