@@ -369,10 +369,44 @@ struct Ow32Smem {
   float Y[NB * NB * NB];     // [i][a][c]
 };
 
+// float -> double from the IEEE 754 fields, exact: a normal number keeps
+// its sign and fraction (widened by 29 bits) and re-biases its exponent
+// (127 -> 1023); zeros, subnormals, infinities and NaNs take the hardware
+// conversion.  Integer operations only, so the FP32 kernels that store
+// complex128 results leave GB300's narrow FP64 pipe alone.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) |
+                               ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
+// The flat loops below visit e = lane, lane + 32, ... of an [NB][NB][NB]
+// array as (i, a, b); 32 = DI NB^2 + DA NB + DB, so each step adds those
+// with two carries instead of dividing.
+template <int NB>
+struct Flat3 {
+  static constexpr int DB = 32 % NB, DA = (32 / NB) % NB, DI = 32 / (NB * NB);
+  int i, a, b;
+  __device__ __forceinline__ explicit Flat3(int e) : i(e / (NB * NB)), a((e / NB) % NB), b(e % NB) {}
+  __device__ __forceinline__ void next() {
+    b += DB;
+    const int ca = b >= NB ? 1 : 0;
+    b -= ca * NB;
+    a += DA + ca;
+    const int ci = a >= NB ? 1 : 0;
+    a -= ci * NB;
+    i += DI + ci;
+  }
+};
+
 template <int NB>
 __global__ void __launch_bounds__(32 * BW_WARPS)
     redfield_operators_w32_kernel(const double* __restrict__ E, const double* __restrict__ U,
-                                  int n, int off, int64_t batch, DebyeParams bath, double uc,
+                                  int n, int off, int64_t batch, DebyeF bath, float uc,
                                   double2* __restrict__ G, double2* __restrict__ M) {
   constexpr int NN = NB * NB;
   constexpr int NNN = NB * NB * NB;
@@ -400,45 +434,50 @@ __global__ void __launch_bounds__(32 * BW_WARPS)
     sm.C[d * NB + c] = cn;
   }
   // Y_i[a][c] = X[a][c] X[i][c]
-  for (int e = lane; e < NNN; e += 32) {
-    const int i = e / NN, a = (e / NB) % NB, c = e % NB;
-    sm.Y[e] = sm.X[a * NB + c] * sm.X[i * NB + c];
+  {
+    Flat3<NB> ix(lane);
+    for (int e = lane; e < NNN; e += 32, ix.next())
+      sm.Y[e] = sm.X[ix.a * NB + ix.b] * sm.X[ix.i * NB + ix.b];
   }
   __syncwarp();
   // T_i[c][b] = sum_d C[c][d] Y_i[b][d]
-  for (int e = lane; e < NNN; e += 32) {
-    const int i = e / NN, c = (e / NB) % NB, bb = e % NB;
-    float2 acc = make_float2(0.f, 0.f);
-    const float* yi = sm.Y + i * NN + bb * NB;
+  {
+    Flat3<NB> ix(lane);
+    for (int e = lane; e < NNN; e += 32, ix.next()) {
+      float2 acc = make_float2(0.f, 0.f);
+      const float* yi = sm.Y + ix.i * NN + ix.b * NB;
+      const float2* cr = sm.C + ix.a * NB;
 #pragma unroll
-    for (int d = 0; d < NB; ++d) {
-      const float2 cv = sm.C[c * NB + d];
-      const float y = yi[d];
-      acc.x = fmaf(cv.x, y, acc.x);
-      acc.y = fmaf(cv.y, y, acc.y);
+      for (int d = 0; d < NB; ++d) {
+        const float2 cv = cr[d];
+        const float y = yi[d];
+        acc.x = fmaf(cv.x, y, acc.x);
+        acc.y = fmaf(cv.y, y, acc.y);
+      }
+      sm.T[e] = acc;
     }
-    sm.T[e] = acc;
   }
   __syncwarp();
   // M_i[a][b] = uc sum_c Y_i[a][c] T_i[c][b]; G row i = M_i row i
-  const float ucf = (float)uc;
   double2* Mb = M + b * (int64_t)NB * nn;
   double2* Gb = G + b * nn;
-  for (int e = lane; e < NNN; e += 32) {
-    const int i = e / NN, a = (e / NB) % NB, bb = e % NB;
-    float2 acc = make_float2(0.f, 0.f);
-    const float* yi = sm.Y + i * NN + a * NB;
-    const float2* ti = sm.T + i * NN + bb;
+  {
+    Flat3<NB> ix(lane);
+    for (int e = lane; e < NNN; e += 32, ix.next()) {
+      float2 acc = make_float2(0.f, 0.f);
+      const float* yi = sm.Y + ix.i * NN + ix.a * NB;
+      const float2* ti = sm.T + ix.i * NN + ix.b;
 #pragma unroll
-    for (int c = 0; c < NB; ++c) {
-      const float y = yi[c];
-      const float2 t = ti[c * NB];
-      acc.x = fmaf(y, t.x, acc.x);
-      acc.y = fmaf(y, t.y, acc.y);
+      for (int c = 0; c < NB; ++c) {
+        const float y = yi[c];
+        const float2 t = ti[c * NB];
+        acc.x = fmaf(y, t.x, acc.x);
+        acc.y = fmaf(y, t.y, acc.y);
+      }
+      const double2 v = make_double2(f2d_exact(acc.x * uc), f2d_exact(acc.y * uc));
+      Mb[(int64_t)ix.i * nn + (off + ix.a) * n + off + ix.b] = v;
+      if (ix.a == ix.i) Gb[(off + ix.a) * n + off + ix.b] = v;
     }
-    const double2 v = make_double2((double)(acc.x * ucf), (double)(acc.y * ucf));
-    Mb[(int64_t)i * nn + (off + a) * n + off + bb] = v;
-    if (a == i) Gb[(off + a) * n + off + bb] = v;
   }
   // zeros outside the coupled block
   if (off > 0 || n > off + NB) {
@@ -458,7 +497,7 @@ static cudaError_t launch_ow32(const double* E, const double* U, int n, int off,
   const size_t smem = sizeof(Ow32Smem<NB>) * BW_WARPS;
   const int64_t grid = (batch + BW_WARPS - 1) / BW_WARPS;
   redfield_operators_w32_kernel<NB><<<(unsigned)grid, 32 * BW_WARPS, smem, s>>>(
-      E, U, n, off, batch, bath, uc, (double2*)G, (double2*)M);
+      E, U, n, off, batch, debye_f(bath), (float)uc, (double2*)G, (double2*)M);
   return cudaGetLastError();
 }
 

@@ -140,9 +140,41 @@ __device__ __forceinline__ float2 digamma_asymptotic_f(float2 z) {
   return csub(csub(lz, cscale(zi, 0.5f)), s);
 }
 
-__device__ __forceinline__ float2 debye_matsubara_f(const DebyeParams& p, float x) {
-  const float c = (float)(2.0 * M_PI * p.T);
-  const float a = (float)p.gamma / c;
+// The FP32 forms' bath constants, each rounded once from the FP64
+// parameters (on the host for kernels that take them as an argument, so the
+// FP32 evaluation issues no FP64 instruction).
+struct DebyeF {
+  float c;          // 2 pi T
+  float gamma, fa, fb, cot_term;
+  float four_t;     // 4 T
+  float lam_gamma;  // lam gamma
+  float zero_re;    // lam 2T / gamma: Re C(0)
+  float neg_lam;    // -lam: Im C(0)
+  float lam, T;
+  int matsubara, real_only;
+};
+
+__host__ __device__ __forceinline__ DebyeF debye_f(const DebyeParams& p) {
+  DebyeF q;
+  q.c = (float)(2.0 * M_PI * p.T);
+  q.gamma = (float)p.gamma;
+  q.fa = (float)p.fa;
+  q.fb = (float)p.fb;
+  q.cot_term = (float)p.cot_term;
+  q.four_t = (float)(4.0 * p.T);
+  q.lam_gamma = (float)(p.lam * p.gamma);
+  q.zero_re = (float)(p.lam * (2.0 * p.T / p.gamma));
+  q.neg_lam = (float)-p.lam;
+  q.lam = (float)p.lam;
+  q.T = (float)p.T;
+  q.matsubara = p.matsubara;
+  q.real_only = p.real_only;
+  return q;
+}
+
+__device__ __forceinline__ float2 debye_matsubara_f(const DebyeF& p, float x) {
+  const float c = p.c;
+  const float a = p.gamma / c;
   const float y = x / c;
   const float2 amb = cmk(a, -y), apb = cmk(a, y);
   const float2 A = cscale(crecip(amb), 0.5f);
@@ -158,23 +190,23 @@ __device__ __forceinline__ float2 debye_matsubara_f(const DebyeParams& p, float 
   }
   if (K >= 9)
     g = cadd(g, csub(digamma_asymptotic_f(cmk((float)K, -y)), digamma_asymptotic_f(cmk(8.0f, -y))));
-  const float2 S = cadd(cadd(cscale(A, (float)p.fa), cscale(B, (float)p.fb)), cmul(D, g));
+  const float2 S = cadd(cadd(cscale(A, p.fa), cscale(B, p.fb)), cmul(D, g));
   return cscale(S, 1.0f / (c * c));
 }
 
-__device__ __forceinline__ float2 debye_from_matsubara_f(const DebyeParams& p, float x, float2 S) {
-  const float2 first = cdiv(cmk((float)p.cot_term, -1.0f), cmk((float)p.gamma, -x));
-  return cscale(cadd(first, cscale(S, (float)(4.0 * p.T))), (float)(p.lam * p.gamma));
+__device__ __forceinline__ float2 debye_from_matsubara_f(const DebyeF& p, float x, float2 S) {
+  const float2 first = cdiv(cmk(p.cot_term, -1.0f), cmk(p.gamma, -x));
+  return cscale(cadd(first, cscale(S, p.four_t)), p.lam_gamma);
 }
 
-__device__ __forceinline__ float2 debye_real_f(const DebyeParams& p, float x) {
-  const float lam = (float)p.lam, gam = (float)p.gamma, T = (float)p.T;
+__device__ __forceinline__ float2 debye_real_f(const DebyeF& p, float x) {
+  const float lam = p.lam, gam = p.gamma, T = p.T;
   if (x == 0.0f) return cmk(T * 2.0f * lam / gam, 0.0f);
   const float J = 2.0f * lam * gam * x / (gam * gam + x * x);
   return cmk((1.0f / expm1f(x / T) + 1.0f) * J, 0.0f);
 }
 
-__device__ __forceinline__ void debye_corr_pair_f(const DebyeParams& p, float x, float2& cpos,
+__device__ __forceinline__ void debye_corr_pair_f(const DebyeF& p, float x, float2& cpos,
                                                   float2& cneg) {
   if (p.real_only) {
     cpos = debye_real_f(p, x);
@@ -182,12 +214,17 @@ __device__ __forceinline__ void debye_corr_pair_f(const DebyeParams& p, float x,
     return;
   }
   if (x == 0.0f) {
-    cpos = cneg = cmk((float)(p.lam * (2.0 * p.T / p.gamma)), (float)-p.lam);
+    cpos = cneg = cmk(p.zero_re, p.neg_lam);
     return;
   }
   const float2 S = debye_matsubara_f(p, x);
   cpos = debye_from_matsubara_f(p, x, S);
   cneg = debye_from_matsubara_f(p, -x, cconj(S));
+}
+
+__device__ __forceinline__ void debye_corr_pair_f(const DebyeParams& p, float x, float2& cpos,
+                                                  float2& cneg) {
+  debye_corr_pair_f(debye_f(p), x, cpos, cneg);
 }
 
 // precision dispatch used by templated builds
